@@ -1,0 +1,615 @@
+"""Symbolic compilation of factorized products into flat device programs.
+
+The reference evaluates each product ``c * F_1 ... F_m |0>`` with transformed
+factors ``F + [F, T] = creator ^ . + (iota_a T) ^ . + iota_a`` on lazy term
+lists of padded blocks (``src/c3l/cc/component_tensor.py:764-786`` and
+``:1166-1233``).  The structure of those term lists does not depend on the
+site count n, so this module expands it once, symbolically, and emits tables
+that a handful of generic GPU kernels execute.
+
+Atoms
+    An atom is a homogeneous exterior form obtained from a *base* by a chain
+    of interior products with factor annihilators (applied in order):
+
+    * ``B1(f, src)`` = creator(f) + iota_f src_2   (degree 1; the creator only
+      for the amplitudes ``T``, not for a tangent ``V``),
+    * ``B3(f, src)`` = iota_f src_4                (degree 3),
+    * ``X(d)``       = degree-d part of an EOM response vector.
+
+    Merging the creator with the degree-one shift is exact: both are wedged
+    and contracted identically (the reference keeps them as separate terms).
+
+Monomials
+    A term is ``coef * atom_1 ^ atom_2 ^ ...``; degree-zero atoms are scalars.
+    Terms are canonicalized (graded sort with signs) and merged.  For each
+    term the highest-degree atom (variable sources first) is the *anchor* and
+    the rest of the wedge is summed per anchor into a *rest form*:
+
+        out = sum_anchor anchor ^ rest_anchor,
+        rest_anchor = sum_terms coef * scalars * (wedge of the other atoms).
+
+    Both sums are evaluated by one generic kernel that sums shuffle-signed
+    products of padded block entries ("instances") per output element.
+
+Tables
+    ``ContractTask`` rows build atoms; ``Instance`` rows drive the wedge
+    evaluator; ``Tile`` rows split outputs into thread blocks.  All are
+    NumPy structured arrays with the exact layout of the C structs in
+    ``include/c3l_gb300.h``.
+"""
+
+from __future__ import annotations
+
+from collections import defaultdict
+from dataclasses import dataclass, field
+from itertools import combinations, product
+
+import numpy as np
+
+from .layout import Coordinates
+
+MAX_FACTORS = 6
+MAX_SOURCES = 4
+TILE = 256
+
+CONTRACT_DTYPE = np.dtype([
+    ("dst_off", np.int64), ("deg", np.int32), ("nsrc", np.int32),
+    ("const_off", np.int64),
+    ("src_off", np.int64, (MAX_SOURCES,)), ("vec_off", np.int64, (MAX_SOURCES,)),
+    ("axis", np.int32, (MAX_SOURCES,)), ("sign", np.float64, (MAX_SOURCES,)),
+], align=True)
+
+INSTANCE_DTYPE = np.dtype([
+    ("coef", np.float64, (2,)), ("nfac", np.int32), ("pad", np.int32),
+    ("fac_off", np.int64, (MAX_FACTORS,)), ("fac_deg", np.int32, (MAX_FACTORS,)),
+    ("axes", np.int8, (MAX_FACTORS, 4)),
+], align=True)
+
+BLOCK_DTYPE = np.dtype([
+    ("inst_begin", np.int64), ("inst_end", np.int64), ("out_off", np.int64),
+    ("deg", np.int32), ("pad", np.int32),
+], align=True)
+
+TILE_DTYPE = np.dtype([("block", np.int32), ("count", np.int32), ("start", np.int64)], align=True)
+
+
+def _e(g: int) -> tuple:
+    return tuple(1 if h == g else 0 for h in range(4))
+
+
+def _sub(a, b):
+    return tuple(x - y for x, y in zip(a, b))
+
+
+def _add(a, b):
+    return tuple(x + y for x, y in zip(a, b))
+
+
+@dataclass(frozen=True, order=True)
+class Atom:
+    src: str          # "T", "V" (static tangent) or "X" (EOM response)
+    f: int            # factor index; -1 for X
+    part: int         # degree of the base
+    chain: tuple = () # factors contracted in order
+
+    @property
+    def degree(self) -> int:
+        return self.part - len(self.chain)
+
+    def contract(self, g: int) -> "Atom":
+        return Atom(self.src, self.f, self.part, self.chain + (g,))
+
+
+SRC_RANK = {"V": 0, "X": 0, "T": 1}
+
+
+def _atom_sort_key(a: Atom):
+    return (-a.degree, SRC_RANK[a.src], a.f, a.part, a.chain)
+
+
+def _odd_inversions(seq) -> bool:
+    odd = False
+    for i in range(len(seq)):
+        for j in range(i + 1, len(seq)):
+            if seq[i] > seq[j]:
+                odd = not odd
+    return odd
+
+
+def multi_shuffles(out_key: tuple, keys: list):
+    """All axis assignments of a multi-factor block wedge and their signs.
+
+    Output axes are group-major; factor j receives ``keys[j][g]`` axes of
+    group g, in increasing order.  The sign is the parity of the
+    concatenated factor axis lists -- the iterated form of
+    ``src/c3l/cc/component_tensor.py:63-79``.
+    """
+    starts = np.cumsum((0,) + tuple(out_key))
+    per_group = []
+    for g in range(4):
+        axes = list(range(int(starts[g]), int(starts[g + 1])))
+        sizes = [k[g] for k in keys]
+        assignments = []
+
+        def rec(remaining, j, acc):
+            if j == len(sizes):
+                if not remaining:
+                    assignments.append(list(acc))
+                return
+            for pick in combinations(remaining, sizes[j]):
+                rest = [a for a in remaining if a not in pick]
+                rec(rest, j + 1, acc + [list(pick)])
+
+        rec(axes, 0, [])
+        per_group.append(assignments)
+    for choice in product(*per_group):
+        lists = [[ax for g in range(4) for ax in choice[g][j]] for j in range(len(keys))]
+        flat = [ax for lst in lists for ax in lst]
+        yield (-1.0 if _odd_inversions(flat) else 1.0), lists
+
+
+class Symbolic:
+    """Block-structure bookkeeping and term expansion for one problem."""
+
+    def __init__(self, spec, static_coords: Coordinates, eom_keys=()):
+        self.n = n = spec.n
+        cre = np.asarray(spec.creators)
+        ann = np.asarray(spec.annihilators)
+        self.F = cre.shape[0]
+        self.cre_groups = [tuple(g for g in range(4) if np.any(cre[f, g * n:(g + 1) * n])) for f in range(self.F)]
+        self.ann_groups = [tuple(g for g in range(4) if np.any(ann[f, g * n:(g + 1) * n])) for f in range(self.F)]
+        skeys = list(static_coords.keys)
+        self.source_keys = {
+            "T": {2: frozenset(k for k in skeys if sum(k) == 2), 4: frozenset(k for k in skeys if sum(k) == 4)},
+            "V": {2: frozenset(k for k in skeys if sum(k) == 2), 4: frozenset(k for k in skeys if sum(k) == 4)},
+            "X": {d: frozenset(k for k in eom_keys if sum(k) == d) for d in (1, 3)},
+        }
+        self._blocks: dict = {}
+
+    # -------------------------------------------------------------- blocks
+    def _contract_keys(self, keys, g: int):
+        out = set()
+        for k in keys:
+            for h in self.ann_groups[g]:
+                if k[h] > 0:
+                    out.add(_sub(k, _e(h)))
+        return frozenset(out)
+
+    def blocks(self, a: Atom) -> frozenset:
+        got = self._blocks.get(a)
+        if got is not None:
+            return got
+        if a.chain:
+            res = self._contract_keys(self.blocks(Atom(a.src, a.f, a.part, a.chain[:-1])), a.chain[-1])
+        elif a.src == "X":
+            res = self.source_keys["X"][a.part]
+        else:
+            base = self._contract_keys(self.source_keys[a.src][a.part + 1], a.f)
+            if a.part == 1 and a.src == "T":
+                base = base | frozenset(_e(g) for g in self.cre_groups[a.f])
+            res = base
+        self._blocks[a] = res
+        return res
+
+    def nonzero(self, a: Atom) -> bool:
+        return a.degree >= 0 and bool(self.blocks(a))
+
+    # ----------------------------------------------------------- expansion
+    @staticmethod
+    def canonical(coef: complex, atoms: tuple):
+        """Graded sort of the non-scalar atoms; scalars sorted freely."""
+        scal = sorted(a for a in atoms if a.degree == 0)
+        non = [a for a in atoms if a.degree > 0]
+        sign = 1.0
+        # bubble sort with graded transposition signs
+        changed = True
+        while changed:
+            changed = False
+            for i in range(len(non) - 1):
+                if _atom_sort_key(non[i + 1]) < _atom_sort_key(non[i]):
+                    if (non[i].degree * non[i + 1].degree) % 2:
+                        sign = -sign
+                    non[i], non[i + 1] = non[i + 1], non[i]
+                    changed = True
+        return coef * sign, tuple(non) + tuple(scal)
+
+    def apply_factor(self, states, f: int):
+        """Transformed factor on lazy terms (component_tensor.py:764-786)."""
+        out = []
+        wedges = [a for a in (Atom("T", f, 1), Atom("T", f, 3)) if self.nonzero(a)]
+        has_ann = bool(self.ann_groups[f])
+        for coef, atoms in states:
+            for w in wedges:
+                out.append((coef, (w,) + atoms))
+            if has_ann:
+                prefix = 0
+                for pos, a in enumerate(atoms):
+                    if a.degree > 0:
+                        b = a.contract(f)
+                        if self.nonzero(b):
+                            out.append((coef * (-1) ** prefix, atoms[:pos] + (b,) + atoms[pos + 1:]))
+                    prefix += a.degree
+        return out
+
+    def expand(self, products, init: tuple, max_out: int, keep: set):
+        """All monomials of ``sum_p c_p F_1..F_m init |0>`` with degree in ``keep``."""
+        acc: dict = defaultdict(complex)
+        for coef, facs in products:
+            states = [(coef, init)]
+            m = len(facs)
+            for step, f in enumerate(reversed(facs)):
+                remaining = m - step - 1
+                states = [(c, a) for c, a in self.apply_factor(states, f)
+                          if sum(x.degree for x in a) - remaining <= max_out]
+            for c, atoms in states:
+                if sum(x.degree for x in atoms) in keep:
+                    cc, ca = self.canonical(c, atoms)
+                    acc[ca] += cc
+        return {k: v for k, v in acc.items() if v != 0}
+
+    def differentiate(self, terms: dict, var: str = "V"):
+        """Product rule: replace one amplitude atom at a time by its tangent."""
+        acc: dict = defaultdict(complex)
+        for atoms, coef in terms.items():
+            for j, a in enumerate(atoms):
+                if a.src != "T":
+                    continue
+                d = Atom(var, a.f, a.part, a.chain)
+                if not self.nonzero(d):
+                    continue
+                cc, ca = self.canonical(coef, atoms[:j] + (d,) + atoms[j + 1:])
+                acc[ca] += cc
+        return {k: v for k, v in acc.items() if v != 0}
+
+
+# ====================================================================== plan
+@dataclass
+class Stage:
+    """One wedge-evaluation launch: output blocks, their instances and tiles."""
+
+    name: str
+    kind: str                 # "padded" or "canonical"
+    blocks: np.ndarray        # BLOCK_DTYPE
+    instances: np.ndarray     # INSTANCE_DTYPE
+    tiles: np.ndarray         # TILE_DTYPE
+    elements: np.ndarray | None = None   # canonical: int64 vector positions
+    digits: np.ndarray | None = None     # canonical: int32 packed index digits
+    element_block: np.ndarray | None = None
+
+
+@dataclass
+class ContractLevel:
+    tasks: np.ndarray         # CONTRACT_DTYPE
+    tiles: np.ndarray         # TILE_DTYPE
+
+
+@dataclass
+class Program:
+    n: int
+    ws_size: int
+    vectors: np.ndarray                       # complex [*]: factor creator/annihilator group vectors
+    source_offsets: dict                      # src -> {key: ws offset}
+    levels: dict = field(default_factory=dict)   # class -> [ContractLevel]
+    stages: dict = field(default_factory=dict)   # name -> Stage
+    atom_offsets: dict = field(default_factory=dict)
+    rest_offsets: dict = field(default_factory=dict)
+
+
+class Builder:
+    """Lays out the workspace and emits the device tables."""
+
+    def __init__(self, sym: Symbolic, spec):
+        self.sym = sym
+        self.n = sym.n
+        self.ws = 0
+        self.source_offsets: dict = {}
+        self.atom_offsets: dict = {}
+        self.rest_offsets: dict = {}
+        n = self.n
+        cre = np.asarray(spec.creators)
+        ann = np.asarray(spec.annihilators)
+        F = cre.shape[0]
+        # vectors table: [F][kind(0=creator,1=annihilator)][group][n]
+        self.vectors = np.zeros((F, 2, 4, n), np.complex128)
+        for f in range(F):
+            for g in range(4):
+                self.vectors[f, 0, g] = cre[f, g * n:(g + 1) * n]
+                self.vectors[f, 1, g] = ann[f, g * n:(g + 1) * n]
+        self.levels: dict = defaultdict(lambda: defaultdict(list))
+        self.stage_data: dict = {}
+
+    def vec_off(self, f: int, kind: int, g: int) -> int:
+        return ((f * 2 + kind) * 4 + g) * self.n
+
+    def alloc(self, key: tuple) -> int:
+        off = self.ws
+        self.ws += self.n ** sum(key)
+        return off
+
+    def add_source(self, src: str, keys) -> None:
+        self.source_offsets[src] = {k: self.alloc(k) for k in sorted(keys)}
+
+    # ------------------------------------------------------------- atoms
+    def atom_class(self, a: Atom) -> str:
+        return a.src
+
+    def ensure_atom(self, a: Atom) -> dict:
+        """Allocate (and emit contraction tasks for) an atom and its parents."""
+        got = self.atom_offsets.get(a)
+        if got is not None:
+            return got
+        sym = self.sym
+        if a.src == "X" and not a.chain:
+            offs = {k: self.source_offsets["X"][k] for k in sym.blocks(a)}
+            self.atom_offsets[a] = offs
+            return offs
+        if a.chain:
+            parent = Atom(a.src, a.f, a.part, a.chain[:-1])
+            pof = self.ensure_atom(parent)
+            g = a.chain[-1]
+            level = len(a.chain)
+        else:
+            parent = None
+            pof = self.source_offsets[a.src]
+            g = a.f
+            level = 0
+        offs = {}
+        for k in sorted(sym.blocks(a)):
+            offs[k] = self.alloc(k)
+        for k, dst in offs.items():
+            srcs = []
+            for h in sym.ann_groups[g]:
+                sk = _add(k, _e(h))
+                if parent is None:
+                    valid = sk in sym.source_keys[a.src][a.part + 1]
+                else:
+                    valid = sk in sym.blocks(parent)
+                if not valid:
+                    continue
+                axis = sum(sk[:h])
+                srcs.append((pof[sk], self.vec_off(g, 1, h), axis, (-1.0) ** axis))
+            const = -1
+            if parent is None and a.part == 1 and a.src == "T" and sum(k) == 1:
+                gc = k.index(1)
+                if gc in sym.cre_groups[a.f]:
+                    const = self.vec_off(a.f, 0, gc)
+            assert len(srcs) <= MAX_SOURCES
+            self.levels[a.src][level].append((dst, sum(k), const, srcs))
+        self.atom_offsets[a] = offs
+        return offs
+
+    # ------------------------------------------------------ wedge stages
+    def rest_blocks(self, anchor: Atom, out_keys, terms) -> set:
+        sym = self.sym
+        need = set()
+        for ko in out_keys:
+            for ka in sym.blocks(anchor):
+                kr = _sub(ko, ka)
+                if min(kr) >= 0:
+                    need.add(kr)
+        possible = set()
+        for (scal, rest), _ in terms.items():
+            for choice in product(*[sorted(sym.blocks(a)) for a in rest]):
+                s = (0, 0, 0, 0)
+                for k in choice:
+                    s = _add(s, k)
+                possible.add(s)
+        return need & possible
+
+    def wedge_instances(self, out_key, coef, scal, atoms, atom_offs_fn):
+        """Instances for ``coef * scalars * wedge(atoms)`` at one output block."""
+        sym = self.sym
+        rows = []
+        soffs = [atom_offs_fn(s)[(0, 0, 0, 0)] for s in scal]
+        for choice in product(*[sorted(sym.blocks(a)) for a in atoms]):
+            s = (0, 0, 0, 0)
+            for k in choice:
+                s = _add(s, k)
+            if s != tuple(out_key):
+                continue
+            for sign, lists in multi_shuffles(out_key, list(choice)):
+                facs = [(atom_offs_fn(a)[k], sum(k), lst) for a, k, lst in zip(atoms, choice, lists)]
+                facs += [(o, 0, []) for o in soffs]
+                rows.append((coef * sign, facs))
+        return rows
+
+    def emit_stage(self, name: str, kind: str, block_rows, elements=None, digits=None, element_block=None):
+        """block_rows: list of (out_off, deg, [instances]) in output order."""
+        nb = len(block_rows)
+        blocks = np.zeros(nb, BLOCK_DTYPE)
+        inst_list = []
+        for b, (out_off, deg, rows) in enumerate(block_rows):
+            blocks[b]["inst_begin"] = len(inst_list)
+            inst_list.extend(rows)
+            blocks[b]["inst_end"] = len(inst_list)
+            blocks[b]["out_off"] = out_off
+            blocks[b]["deg"] = deg
+        inst = np.zeros(len(inst_list), INSTANCE_DTYPE)
+        for i, (coef, facs) in enumerate(inst_list):
+            assert len(facs) <= MAX_FACTORS, len(facs)
+            inst[i]["coef"] = (coef.real, coef.imag)
+            inst[i]["nfac"] = len(facs)
+            inst[i]["axes"] = -1
+            for j, (off, deg, lst) in enumerate(facs):
+                inst[i]["fac_off"][j] = off
+                inst[i]["fac_deg"][j] = deg
+                for q, ax in enumerate(lst):
+                    inst[i]["axes"][j][q] = ax
+        tiles = []
+        if kind == "padded":
+            for b, (out_off, deg, rows) in enumerate(block_rows):
+                size = self.n ** deg
+                for s in range(0, size, TILE):
+                    tiles.append((b, min(TILE, size - s), s))
+        else:
+            eb = np.asarray(element_block)
+            order_ok = np.all(np.diff(eb) >= 0)
+            assert order_ok, "canonical elements must be grouped by block"
+            for b in range(nb):
+                idx = np.flatnonzero(eb == b)
+                if idx.size == 0:
+                    continue
+                lo, hi = int(idx[0]), int(idx[-1]) + 1
+                for s in range(lo, hi, TILE):
+                    tiles.append((b, min(TILE, hi - s), s))
+        tarr = np.zeros(len(tiles), TILE_DTYPE)
+        for i, (b, c, s) in enumerate(tiles):
+            tarr[i] = (b, c, s)
+        self.stage_data[name] = Stage(name, kind, blocks, inst, tarr, elements, digits, element_block)
+
+    def finish(self) -> Program:
+        levels = {}
+        for cls, by_level in self.levels.items():
+            lv = []
+            for level in sorted(by_level):
+                rows = by_level[level]
+                tasks = np.zeros(len(rows), CONTRACT_DTYPE)
+                tiles = []
+                for i, (dst, deg, const, srcs) in enumerate(rows):
+                    tasks[i]["dst_off"] = dst
+                    tasks[i]["deg"] = deg
+                    tasks[i]["nsrc"] = len(srcs)
+                    tasks[i]["const_off"] = const
+                    for j, (so, vo, ax, sg) in enumerate(srcs):
+                        tasks[i]["src_off"][j] = so
+                        tasks[i]["vec_off"][j] = vo
+                        tasks[i]["axis"][j] = ax
+                        tasks[i]["sign"][j] = sg
+                    size = self.n ** deg
+                    for s in range(0, size, TILE):
+                        tiles.append((i, min(TILE, size - s), s))
+                tarr = np.zeros(len(tiles), TILE_DTYPE)
+                for i, t in enumerate(tiles):
+                    tarr[i] = t
+                lv.append(ContractLevel(tasks, tarr))
+            levels[cls] = lv
+        return Program(self.n, self.ws, self.vectors.reshape(-1), self.source_offsets, levels,
+                       self.stage_data, self.atom_offsets, self.rest_offsets)
+
+
+def _group_by_anchor(terms: dict):
+    """(anchor, out_degree) -> {(scalars, rest atoms): coef}; plus pure scalars."""
+    groups: dict = defaultdict(lambda: defaultdict(complex))
+    scalars: dict = defaultdict(complex)
+    for atoms, coef in terms.items():
+        non = [a for a in atoms if a.degree > 0]
+        scal = tuple(a for a in atoms if a.degree == 0)
+        D = sum(a.degree for a in non)
+        if not non:
+            scalars[scal] += coef
+            continue
+        anchor = non[0]
+        groups[(anchor, D)][(scal, tuple(non[1:]))] += coef
+    return groups, scalars
+
+
+def _digits(coords: Coordinates, positions: np.ndarray) -> np.ndarray:
+    tup = coords.tuples[positions]
+    out = np.zeros(len(positions), np.int64)
+    for c in range(tup.shape[1]):
+        col = np.where(tup[:, c] >= 0, tup[:, c], 0)
+        out |= (col & 0xFF) << (8 * c)
+    return out.astype(np.int64)
+
+
+def compile_output(builder: Builder, name: str, terms: dict, coords: Coordinates,
+                   positions: np.ndarray, rest_stage: str, scalar_stage: str | None):
+    """Emit rest stage(s) and the canonical output stage for a term set.
+
+    ``positions``: vector positions (in ``coords``) to evaluate, any order; the
+    stage stores them grouped by block.  Returns the offset of the scalar
+    (degree-zero) output in the workspace or -1.
+    """
+    sym = builder.sym
+    groups, scalars = _group_by_anchor(terms)
+    out_keys_by_deg = defaultdict(set)
+    for k in coords.keys:
+        out_keys_by_deg[sum(k)].add(k)
+    # rest forms
+    rest_rows_by_class = defaultdict(list)
+    rest_info = {}
+    for (anchor, D), rterms in sorted(groups.items(), key=lambda kv: (_atom_sort_key(kv[0][0]), kv[0][1])):
+        out_keys = out_keys_by_deg.get(D, set())
+        if not out_keys:
+            continue
+        blocks = builder.rest_blocks(anchor, out_keys, rterms)
+        if not blocks:
+            continue
+        builder.ensure_atom(anchor)
+        cls = "T"
+        for (scal, rest) in rterms:
+            for a in scal + rest:
+                builder.ensure_atom(a)
+                if a.src != "T":
+                    cls = a.src
+        offs = {k: builder.alloc(k) for k in sorted(blocks)}
+        builder.rest_offsets[(name, anchor, D)] = offs
+        rest_info[(anchor, D)] = offs
+        for k in sorted(blocks):
+            rows = []
+            for (scal, rest), coef in rterms.items():
+                rows.extend(builder.wedge_instances(k, coef, scal, rest, lambda a: builder.atom_offsets[a]))
+            rest_rows_by_class[cls].append((offs[k], sum(k), rows))
+    for cls, rows in rest_rows_by_class.items():
+        builder.emit_stage(f"{rest_stage}_{cls}", "padded", rows)
+    # scalar output
+    scalar_off = -1
+    if scalar_stage is not None and scalars:
+        rows = []
+        cls = "T"
+        for scal, coef in scalars.items():
+            for a in scal:
+                builder.ensure_atom(a)
+                if a.src != "T":
+                    cls = a.src
+            rows.extend(builder.wedge_instances((0, 0, 0, 0), coef, scal, (), lambda a: builder.atom_offsets[a]))
+        scalar_off = builder.alloc((0, 0, 0, 0))
+        builder.emit_stage(scalar_stage, "padded", [(scalar_off, 0, rows)])
+    # canonical output
+    pos = np.asarray(positions, np.int64)
+    blk = coords.block_of[pos]
+    order = np.argsort(blk, kind="stable")
+    pos = pos[order]
+    blk = blk[order]
+    block_rows = []
+    for b, key in enumerate(coords.keys):
+        rows = []
+        for (anchor, D), offs in rest_info.items():
+            if D != sum(key):
+                continue
+            aoffs = builder.atom_offsets[anchor]
+            for ka in sorted(sym.blocks(anchor)):
+                kr = _sub(key, ka)
+                if min(kr) < 0 or kr not in offs:
+                    continue
+                for sign, lists in multi_shuffles(key, [ka, kr]):
+                    rows.append((complex(sign), [(aoffs[ka], sum(ka), lists[0]), (offs[kr], sum(kr), lists[1])]))
+        block_rows.append((-1, sum(key), rows))
+    builder.emit_stage(name, "canonical", block_rows, elements=pos, digits=_digits(coords, pos), element_block=blk)
+    return scalar_off
+
+
+# ================================================================ front ends
+def static_terms(sym: Symbolic, spec):
+    """Residual monomials (degrees 0, 2, 4) and their tangents."""
+    res = sym.expand(list(spec.products()), (), 4, {0, 2, 4})
+    return res, sym.differentiate(res, "V")
+
+
+def eom_terms(sym: Symbolic, spec, eom_keys, vacuum: dict):
+    """Sigma monomials: products acting on X, minus vacuum ^ X (component_tensor.py:2116-2223)."""
+    acc: dict = defaultdict(complex)
+    degs = sorted({sum(k) for k in eom_keys})
+    for d in degs:
+        x = Atom("X", -1, d)
+        if not sym.nonzero(x):
+            continue
+        part = sym.expand(list(spec.products()), (x,), 3, {1, 3})
+        for k, v in part.items():
+            acc[k] += v
+        for atoms, coef in vacuum.items():
+            if sum(a.degree for a in atoms) + d not in (1, 3):
+                continue
+            cc, ca = sym.canonical(-coef, atoms + (x,))
+            acc[ca] += cc
+    return {k: v for k, v in acc.items() if v != 0}

@@ -1,0 +1,164 @@
+"""Self-contained description of one factorized CCSD problem.
+
+A ``ProblemSpec`` carries exactly what the coupled-cluster hot path consumes
+from the reference's setup layer (``src/c3l/cc/factorized.py:248-423``):
+
+* ``n`` -- sites per particle-hole group; the 4n modes are ordered
+  (up+, up-, down+, down-) as in ``src/c3l/ci/sectors.py:23-36``;
+* the distinct linear mode operators of the products, each split into a
+  creator vector and an annihilator vector over the 4n modes
+  (``src/c3l/cc/component_tensor.py:571-583``);
+* the factorized products: coefficient and written (left-to-right) factor
+  order (``src/c3l/ci/matrix_free.py:77-92``); they are applied right to left;
+* the reference rapidities (one per mode);
+* the mode-level tilde partners and phases (``src/c3l/ci/tilde.py:211-251``)
+  from which the amplitude tilde map is induced (``src/c3l/cc/symmetry.py:150-187``);
+* for every site and spin, the factor indices of the physical operators
+  c, c^dagger, tilde c and tilde c^dagger used as EOM sources and sinks.
+
+Specs are plain ``.npz`` files.  ``from_reference`` builds one from the
+reference's ``ComponentStaticProblem`` when that package is importable.
+"""
+
+from __future__ import annotations
+
+from dataclasses import dataclass
+from pathlib import Path
+
+import numpy as np
+
+
+@dataclass(frozen=True)
+class ProblemSpec:
+    n: int
+    creators: np.ndarray          # complex [F, 4n]
+    annihilators: np.ndarray      # complex [F, 4n]
+    product_coefficients: np.ndarray  # complex [P]
+    product_factors: np.ndarray   # int [P, maxlen], -1 padded, written order
+    product_lengths: np.ndarray   # int [P]
+    rapidities: np.ndarray        # complex [4n]
+    mode_partner: np.ndarray      # int [4n]
+    mode_phase: np.ndarray        # complex [4n]
+    source_factor: np.ndarray     # int [n, 2, 4]: c, c_dagger, tilde_c, tilde_c_dagger
+    impurity_site: int = 0
+    recipe: str = ""
+
+    def __post_init__(self) -> None:
+        n = int(self.n)
+        M = 4 * n
+        if n < 1:
+            raise ValueError("n must be positive")
+        for name in ("creators", "annihilators"):
+            arr = np.asarray(getattr(self, name))
+            if arr.ndim != 2 or arr.shape[1] != M or not np.all(np.isfinite(arr)):
+                raise ValueError(f"{name} must be a finite [F, 4n] array")
+        if np.asarray(self.creators).shape != np.asarray(self.annihilators).shape:
+            raise ValueError("creator and annihilator tables disagree")
+        if np.asarray(self.rapidities).shape != (M,):
+            raise ValueError("rapidities must have one entry per mode")
+        partner = np.asarray(self.mode_partner)
+        if partner.shape != (M,) or not np.array_equal(partner[partner], np.arange(M)):
+            raise ValueError("mode tilde partners must be an involution over the modes")
+        F = np.asarray(self.creators).shape[0]
+        pf = np.asarray(self.product_factors)
+        pl = np.asarray(self.product_lengths)
+        if pf.ndim != 2 or pl.shape != (pf.shape[0],) or np.asarray(self.product_coefficients).shape != (pf.shape[0],):
+            raise ValueError("product tables are inconsistent")
+        for row, ln in zip(pf, pl):
+            if ln < 1 or np.any(row[:ln] < 0) or np.any(row[:ln] >= F):
+                raise ValueError("a product references a missing factor")
+
+    @property
+    def num_factors(self) -> int:
+        return int(np.asarray(self.creators).shape[0])
+
+    def products(self):
+        for coef, row, ln in zip(self.product_coefficients, self.product_factors, self.product_lengths):
+            yield complex(coef), tuple(int(f) for f in row[:ln])
+
+    # ------------------------------------------------------------------ io
+    @classmethod
+    def load(cls, path: str | Path) -> "ProblemSpec":
+        data = np.load(path)
+        return cls(
+            n=int(data["n"]),
+            creators=np.asarray(data["creators"], np.complex128),
+            annihilators=np.asarray(data["annihilators"], np.complex128),
+            product_coefficients=np.asarray(data["product_coefficients"], np.complex128),
+            product_factors=np.asarray(data["product_factors"], np.int64),
+            product_lengths=np.asarray(data["product_lengths"], np.int64),
+            rapidities=np.asarray(data["rapidities"], np.complex128),
+            mode_partner=np.asarray(data["mode_partner"], np.int64),
+            mode_phase=np.asarray(data["mode_phase"], np.complex128),
+            source_factor=np.asarray(data["source_factor"], np.int64),
+            impurity_site=int(data["impurity_site"]) if "impurity_site" in data else 0,
+            recipe=str(data["recipe"]) if "recipe" in data else "",
+        )
+
+    def as_dict(self) -> dict:
+        return {
+            "n": np.int64(self.n), "creators": self.creators, "annihilators": self.annihilators,
+            "product_coefficients": self.product_coefficients, "product_factors": self.product_factors,
+            "product_lengths": self.product_lengths, "rapidities": self.rapidities,
+            "mode_partner": self.mode_partner, "mode_phase": self.mode_phase,
+            "source_factor": self.source_factor, "impurity_site": np.int64(self.impurity_site),
+            "recipe": np.array(self.recipe),
+        }
+
+    def save(self, path: str | Path) -> None:
+        np.savez_compressed(path, **self.as_dict())
+
+    # ------------------------------------------------------- reference adapter
+    @classmethod
+    def from_reference(cls, static_problem) -> "ProblemSpec":
+        """Lower a reference ``ComponentStaticProblem`` (needs the reference package).
+
+        Reads ``static_problem.oracle`` (a ``FactorizedCCProblem``): its
+        products, rapidities and normal-mode reference.
+        """
+        from c3l.ci.matrix_free import physical_mode_operator
+        from c3l.ci.tilde import tilde_map_from_references
+
+        cc = static_problem.oracle
+        if cc.model.symmetry != "spin":
+            raise ValueError("only the spinful (up/down conserving) layout is supported")
+        n = cc.model.n_sites
+        M = 4 * n
+        keys: dict = {}
+        cre: list = []
+        ann: list = []
+
+        def index(op) -> int:
+            key = op.components
+            if key not in keys:
+                c = np.zeros(M, complex)
+                a = np.zeros(M, complex)
+                for kind, mode, coefficient in key:
+                    (c if kind == "create" else a)[mode] += coefficient
+                keys[key] = len(cre)
+                cre.append(c)
+                ann.append(a)
+            return keys[key]
+
+        maxlen = max(len(p.factors) for p in cc.products)
+        pf = -np.ones((len(cc.products), maxlen), np.int64)
+        pl = np.zeros(len(cc.products), np.int64)
+        pc = np.zeros(len(cc.products), complex)
+        for i, p in enumerate(cc.products):
+            pc[i] = p.coefficient
+            pl[i] = len(p.factors)
+            for j, f in enumerate(p.factors):
+                pf[i, j] = index(f)
+        src = -np.ones((n, 2, 4), np.int64)
+        for site in range(n):
+            for spin in range(2):
+                for k, ch in enumerate(("c", "c_dagger", "tilde_c", "tilde_c_dagger")):
+                    src[site, spin, k] = index(physical_mode_operator(cc.reference, site, spin, ch))
+        det = tilde_map_from_references(cc.reference.up, cc.reference.down)
+        return cls(
+            n=n, creators=np.asarray(cre), annihilators=np.asarray(ann),
+            product_coefficients=pc, product_factors=pf, product_lengths=pl,
+            rapidities=np.asarray(cc.rapidities, complex),
+            mode_partner=np.asarray(det.partners, np.int64), mode_phase=np.asarray(det.factors, complex),
+            source_factor=src, impurity_site=int(cc.model.impurity_site), recipe="reference",
+        )

@@ -1,0 +1,356 @@
+"""Generate problem specs and golden vectors by running the reference itself.
+
+This script is test infrastructure.  It imports the reference package
+(``c3l``) from a source tree given on the command line (default: the
+read-only checkout next to this repository), builds each seeded model with the
+reference's own setup code, runs the reference's CPU hot path and writes:
+
+* ``<name>.spec.npz`` -- the self-contained problem description consumed by
+  ``c3lindblad_gb300.spec.ProblemSpec`` (site count, distinct linear factors as
+  creator/annihilator vectors over the 4n particle-hole modes, the factorized
+  products, rapidities, mode-level tilde partners/phases, source operators);
+* ``<name>.golden.npz`` -- reference outputs on that problem: residual and JVP
+  at deterministic amplitudes (the fixture recipe of the reference's
+  ``tests/cc/test_component_jax.py:41-44``), cluster/EOM masks and tilde maps
+  (small n only), the converged Newton--Krylov solution, the EOM diagonal,
+  a sigma action, the sources, and G^R on a frequency grid.
+
+The GPU machine never runs this script; only the ``.npz`` files travel.
+
+Usage: ``python tests/golden/make_fixtures.py [--reference SRC] [names...]``
+"""
+
+from __future__ import annotations
+
+import argparse
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+
+
+def _import_reference(src: str):
+    sys.path.insert(0, src)
+    import c3l  # noqa: F401
+
+
+# ---------------------------------------------------------------- models
+def model_readme():
+    """README quick-start model (reference README.md)."""
+    from c3l import FermionicLindbladModel
+
+    return FermionicLindbladModel(
+        E=np.array([[-0.6, 0.28, 0.28], [0.28, -1.2, 0.0], [0.28, 0.0, 1.2]]),
+        gamma_loss=np.diag([0.0, 0.06, 0.48]),
+        gamma_gain=np.diag([0.0, 0.48, 0.06]),
+        U=1.2,
+    )
+
+
+def model_s135():
+    """Compact interacting model of the reference tests (tests/s135_fixture.py:8-30)."""
+    from c3l import FermionicLindbladModel
+
+    U = 1.2
+    bath = np.linspace(-1.2, 1.2, 2)
+    E = np.diag(np.concatenate(([-U / 2.0], bath))).astype(np.complex128)
+    coupling = 0.28 + 0.04 * (1.0 - np.abs(bath) / np.max(np.abs(bath)))
+    E[0, 1:] = coupling
+    E[1:, 0] = coupling
+    scaled = (bath - bath[0]) / (bath[-1] - bath[0])
+    loss = np.zeros(3)
+    gain = np.zeros(3)
+    loss[1:] = 0.06 + 0.42 * scaled
+    gain[1:] = 0.48 - 0.42 * scaled
+    return FermionicLindbladModel(E, np.diag(loss), np.diag(gain), U=U)
+
+
+def model_twosrc():
+    """Two-site complex-hopping model (tests/cc/test_component_jax.py:47-58)."""
+    from c3l import FermionicLindbladModel
+
+    U = 0.4
+    E = np.asarray(((-0.5 * U, 0.18j), (-0.18j, 0.25)))
+    return FermionicLindbladModel(E, np.diag((0.0, 0.32)), np.diag((0.0, 0.11)), U=U)
+
+
+def model_siam(num_modes: int, seed: int):
+    """Single-impurity Anderson model with Lindblad pseudomodes (seeded)."""
+    from c3l import FermionicLindbladModel
+
+    rng = np.random.default_rng(seed)
+    U = 4.0
+    eb = rng.uniform(-3, 3, num_modes)
+    V = rng.normal(0, 0.3, num_modes)
+    r = rng.uniform(0.05, 0.5, num_modes)
+    f = 1.0 / (np.exp(eb / 0.1) + 1.0)
+    E = np.diag(np.r_[-U / 2, eb]).astype(complex)
+    E[0, 1:] = V
+    E[1:, 0] = V
+    return FermionicLindbladModel(E, np.diag(np.r_[0, r * (1 - f)]), np.diag(np.r_[0, r * f]), U=U)
+
+
+def model_kanamori(norb: int, modes_per_orbital: int, seed: int):
+    """Multi-orbital Kanamori impurity with seeded pseudomode baths."""
+    from c3l import FermionicLindbladModel
+    from c3l.cc._static_schema import interaction_from_spatial_tensor
+    from c3l.interactions import SparseTwoBodyInteraction
+
+    rng = np.random.default_rng(seed)
+    U, J = 2.0, 0.3
+    Up = U - 2 * J
+    K = np.zeros((norb,) * 4)
+    for a in range(norb):
+        for b in range(norb):
+            if a == b:
+                K[a, a, a, a] = U / 2
+            else:
+                K[a, b, a, b] = Up / 2
+                K[a, b, b, a] = J / 2
+                K[a, a, b, b] = J / 2
+    terms = interaction_from_spatial_tensor(K)
+    nm = modes_per_orbital
+    n = norb * (1 + nm)
+    E = np.zeros((n, n), complex)
+    loss = np.zeros(n)
+    gain = np.zeros(n)
+    E[:norb, :norb] = np.diag(rng.uniform(-0.2, 0.2, norb)) - U / 2
+    for o in range(norb):
+        eb = rng.uniform(-3, 3, nm)
+        V = rng.normal(0, 0.3, nm)
+        r = rng.uniform(0.05, 0.5, nm)
+        f = 1 / (np.exp(eb / 0.1) + 1)
+        s = slice(norb + o * nm, norb + (o + 1) * nm)
+        E[s, s] = np.diag(eb)
+        E[o, s] = V
+        E[s, o] = V
+        loss[s] = r * (1 - f)
+        gain[s] = r * f
+    inter = SparseTwoBodyInteraction(2 * n, terms.terms)
+    return FermionicLindbladModel(
+        E, np.diag(loss), np.diag(gain), U=0.0,
+        interaction_sites=tuple(range(norb)), two_body_interaction=inter,
+    )
+
+
+def _restricted_reference(model):
+    from c3l.ci.reference import full_hartree_fock_reference
+    from c3l.gaussian_mean_field import solve_ghf
+
+    hf = solve_ghf(
+        model.physical_E, model.interaction, model.physical_gamma_loss, model.physical_gamma_gain,
+        restricted=True, tolerance=1e-10, max_iterations=600, damping=0.5,
+        terminal_least_squares=True,
+    )
+    if not hf.converged:
+        raise RuntimeError("restricted GHF reference did not converge")
+    return full_hartree_fock_reference(model, hf.fock, hf.gamma)
+
+
+# name -> (builder, reference recipe, amplitude scale, omega grid, eta, solve?)
+FIXTURES = {
+    "readme": dict(model=model_readme, recipe="full_hf", scale=7e-4,
+                   omega=np.linspace(-4.0, 4.0, 81), eta=0.0, solve=True),
+    "s135fix": dict(model=model_s135, recipe="legacy_half_filled:0.3", scale=7e-4,
+                    omega=np.linspace(-3.0, 3.0, 25), eta=0.05, solve=True),
+    "twosrc": dict(model=model_twosrc, recipe="legacy_half_filled:0.3", scale=5e-4,
+                   omega=np.linspace(-2.0, 2.0, 17), eta=0.1, solve=True),
+    "siam10": dict(model=lambda: model_siam(10, 0), recipe="legacy_half_filled:0.5", scale=1e-3,
+                   omega=np.linspace(-8.0, 8.0, 1001)[::50], eta=0.0, solve=True),
+    "kanamori3x2": dict(model=lambda: model_kanamori(3, 2, 2), recipe="restricted_ghf", scale=1e-3,
+                        omega=np.linspace(-10.0, 10.0, 2001)[::200], eta=0.02, solve=True),
+    "kanamori3x8": dict(model=lambda: model_kanamori(3, 8, 2), recipe="restricted_ghf", scale=1e-3,
+                        omega=None, eta=0.02, solve=False),
+}
+
+
+def build_problem(spec):
+    from c3l.cc.factorized import factorized_cc_problem
+
+    model = spec["model"]()
+    recipe = spec["recipe"]
+    if recipe == "full_hf":
+        cc = factorized_cc_problem(model, "CCSD")
+    elif recipe.startswith("legacy_half_filled"):
+        m_up = float(recipe.split(":")[1])
+        cc = factorized_cc_problem(model, "CCSD", m_up=m_up, reference_mode="legacy_half_filled")
+    elif recipe == "restricted_ghf":
+        cc = factorized_cc_problem(model, "CCSD", reference=_restricted_reference(model))
+    else:
+        raise ValueError(recipe)
+    return cc
+
+
+def export_spec(cc, path: Path, recipe: str) -> dict:
+    """Write the self-contained problem description."""
+    from c3l.ci.matrix_free import physical_mode_operator
+    from c3l.ci.tilde import tilde_map_from_references
+
+    n = cc.model.n_sites
+    M = 4 * n
+    keys: dict = {}
+    creators: list = []
+    annihilators: list = []
+
+    def factor_index(op) -> int:
+        key = op.components
+        if key not in keys:
+            c = np.zeros(M, complex)
+            a = np.zeros(M, complex)
+            for kind, mode, coefficient in key:
+                (c if kind == "create" else a)[mode] += coefficient
+            keys[key] = len(creators)
+            creators.append(c)
+            annihilators.append(a)
+        return keys[key]
+
+    maxlen = max(len(p.factors) for p in cc.products)
+    prod_factors = -np.ones((len(cc.products), maxlen), np.int64)
+    prod_len = np.zeros(len(cc.products), np.int64)
+    prod_coef = np.zeros(len(cc.products), complex)
+    for i, p in enumerate(cc.products):
+        prod_coef[i] = p.coefficient
+        prod_len[i] = len(p.factors)
+        for j, f in enumerate(p.factors):
+            prod_factors[i, j] = factor_index(f)
+    nprod_factors = len(creators)
+    # physical operators used by the EOM sources/sink (reference
+    # component_tensor.py:2816-2858), for every site and spin
+    channels = ("c", "c_dagger", "tilde_c", "tilde_c_dagger")
+    src_index = -np.ones((n, 2, 4), np.int64)
+    for site in range(n):
+        for spin in range(2):
+            for k, ch in enumerate(channels):
+                src_index[site, spin, k] = factor_index(physical_mode_operator(cc.reference, site, spin, ch))
+    det = tilde_map_from_references(cc.reference.up, cc.reference.down)
+    out = dict(
+        n=np.int64(n),
+        creators=np.asarray(creators),
+        annihilators=np.asarray(annihilators),
+        product_coefficients=prod_coef,
+        product_factors=prod_factors,
+        product_lengths=prod_len,
+        product_factor_count=np.int64(nprod_factors),
+        rapidities=np.asarray(cc.rapidities, complex),
+        mode_partner=np.asarray(det.partners, np.int64),
+        mode_phase=np.asarray(det.factors, complex),
+        source_factor=src_index,
+        impurity_site=np.int64(cc.model.impurity_site),
+        recipe=np.array(recipe),
+    )
+    np.savez_compressed(path, **out)
+    return out
+
+
+def export_golden(name, fx, cc, path: Path) -> None:
+    from c3l.cc.component_tensor import (
+        ComponentEOMProblem, ComponentStaticProblem, component_eom_context,
+        component_eom_sigma, component_eom_sources, component_static_jvp,
+        component_static_residual,
+    )
+    from c3l.cc.component_response import ComponentSigmaOperator, component_retarded_green
+    from c3l.cc.component_solver import solve_component_ccsd
+    from c3l.cc.eom import eom_ccsd_problem
+
+    g: dict = {}
+    t0 = time.perf_counter()
+    static = ComponentStaticProblem.compile(cc, fuse_products=True)
+    g["setup_seconds"] = time.perf_counter() - t0
+    n = cc.model.n_sites
+    idx = np.arange(cc.num_variables, dtype=np.float64)
+    T = cc.tilde.unpack(fx["scale"] * np.cos(idx + 0.13))
+    D = cc.tilde.unpack(0.2 * np.sin(idx + 0.31))
+    g["fixed_variables"] = fx["scale"] * np.cos(idx + 0.13)
+    g["fixed_direction_variables"] = 0.2 * np.sin(idx + 0.31)
+    g["fixed_amplitudes"] = T
+    g["fixed_direction"] = D
+    t0 = time.perf_counter()
+    res = component_static_residual(static, T)
+    g["residual_seconds"] = time.perf_counter() - t0
+    g["residual"] = res.retained
+    g["residual_reference"] = np.complex128(res.reference)
+    t0 = time.perf_counter()
+    jvp = component_static_jvp(static, T, D)
+    g["jvp_seconds"] = time.perf_counter() - t0
+    g["jvp"] = jvp.retained
+    g["jvp_reference"] = np.complex128(jvp.reference)
+    if 4 * n <= 62:
+        g["cluster_masks"] = np.asarray(cc.cluster_basis.masks, np.int64)
+    g["tilde_partner"] = np.asarray(cc.tilde.partner, np.int64)
+    g["tilde_phase"] = np.asarray(cc.tilde.phase, complex)
+    g["tilde_independent"] = np.asarray(cc.tilde.independent, np.int64)
+    print(f"  [{name}] residual {g['residual_seconds']:.2f}s jvp {g['jvp_seconds']:.2f}s", flush=True)
+    if not fx["solve"]:
+        np.savez_compressed(path, **g)
+        return
+    t0 = time.perf_counter()
+    sol = solve_component_ccsd(static)
+    g["solve_seconds"] = time.perf_counter() - t0
+    g["solution_amplitudes"] = sol.amplitudes
+    g["solution_variables"] = sol.variables
+    g["solution_packed_residual_norm"] = sol.packed_residual_norm
+    g["solution_iterations"] = sol.iterations
+    g["solution_residual_evaluations"] = sol.residual_evaluations
+    g["solution_jvp_evaluations"] = sol.jvp_evaluations
+    g["solution_converged"] = sol.converged
+    print(f"  [{name}] solve {g['solve_seconds']:.2f}s iters {sol.iterations} |r| {sol.packed_residual_norm:.2e}", flush=True)
+    eom = eom_ccsd_problem(cc, response_spin=0)
+    if 4 * n <= 62:
+        g["eom_masks"] = np.asarray(eom.basis.masks, np.int64)
+        g["eom_charges"] = np.asarray(eom.basis.charge_labels, np.int64)
+    for charge in (1, -1):
+        tag = "p" if charge == 1 else "m"
+        problem = ComponentEOMProblem.compile(eom, static, charge=charge)
+        t0 = time.perf_counter()
+        context = component_eom_context(problem, sol.amplitudes)
+        g[f"eom{tag}_context_seconds"] = time.perf_counter() - t0
+        op = ComponentSigmaOperator(context)
+        g[f"eom{tag}_positions"] = np.asarray(problem.positions, np.int64)
+        g[f"eom{tag}_diagonal"] = op.diagonal
+        dim = op.dimension
+        k = np.arange(dim, dtype=np.float64)
+        x = np.cos(0.7 * k + 0.2) + 1j * np.sin(0.3 * k - 0.1)
+        g[f"eom{tag}_probe"] = x
+        t0 = time.perf_counter()
+        g[f"eom{tag}_sigma"] = component_eom_sigma(context, x).retained
+        g[f"eom{tag}_sigma_seconds"] = time.perf_counter() - t0
+        src = component_eom_sources(context)
+        g[f"eom{tag}_addition"] = src.addition
+        g[f"eom{tag}_removal"] = src.removal
+        g[f"eom{tag}_sink"] = src.sink
+        if fx["omega"] is not None and charge == 1:
+            t0 = time.perf_counter()
+            green = component_retarded_green(op, src, fx["omega"], fx["eta"])
+            g["green_seconds"] = time.perf_counter() - t0
+            g["green_omega"] = green.omega
+            g["green_eta"] = np.float64(fx["eta"])
+            g["green_addition"] = green.addition
+            g["green_removal"] = green.removal
+            g["green_retarded"] = green.retarded
+            g["green_sigma_calls"] = op.action_calls
+            print(f"  [{name}] green {g['green_seconds']:.2f}s ({op.action_calls} sigma calls)", flush=True)
+    np.savez_compressed(path, **g)
+
+
+def main() -> None:
+    parser = argparse.ArgumentParser()
+    parser.add_argument("--reference", default=str(HERE.parents[2] / "reference" / "src"))
+    parser.add_argument("names", nargs="*")
+    args = parser.parse_args()
+    _import_reference(args.reference)
+    names = args.names or list(FIXTURES)
+    for name in names:
+        fx = FIXTURES[name]
+        t0 = time.perf_counter()
+        cc = build_problem(fx)
+        print(f"[{name}] n={cc.model.n_sites} amps={cc.num_amplitudes} products={len(cc.products)} "
+              f"setup {time.perf_counter() - t0:.1f}s", flush=True)
+        export_spec(cc, HERE / f"{name}.spec.npz", fx["recipe"])
+        export_golden(name, fx, cc, HERE / f"{name}.golden.npz")
+
+
+if __name__ == "__main__":
+    main()
