@@ -1,0 +1,364 @@
+"""Time-to-solution benchmark of the coupled-cluster hot path on one GB300.
+
+A *step* is the full hot path on one synthetic model: the CCSD steady state
+by Newton--Krylov from zero amplitudes, then the charge +1 EOM block of the
+impurity (context, sources) and G^R on the whole frequency grid.
+
+Workload (default): the single-impurity Anderson model with 10 Lindblad
+pseudomodes (n = 11 sites, 20,933 amplitudes, EOM dimension 1,947), seeded
+as described in ``tests/golden/make_fixtures.py`` (``siam10``), with 1001
+frequencies in [-8, 8] and eta = 0.  Inputs are synthetic (seeded), not a
+dataset.
+
+``value``  -- seconds per step with the problem tables already resident in HBM
+              (CUDA events on the launching stream, L2 flushed between steps).
+``e2e``    -- the same step through the public API from host buffers: the
+              problem tables are uploaded (H2D) and the amplitudes and G^R are
+              read back (D2H) inside the timed region.
+``--impl reference`` times the CPU restatement of the reference algorithm
+(``oracle/``) on the host cores and prints the same metric.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "s to CCSD+G^R(omega) at ≤1e-8 vs FP64: mixed+batched+warm vs plain FP64, 1 GB300"
+WORKLOADS = {
+    "siam10": dict(spec="siam10", omega=(-8.0, 8.0, 1001), eta=0.0,
+                   label="SIAM U=4, 10 pseudomodes (n=11, 20933 amplitudes, S13 dim 1947), "
+                         "charge+1 G^R on 1001 omega in [-8,8], eta=0"),
+}
+
+
+def _peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), float(d["bf16_tflops"]), "measured"
+    return 6800.0, 1900.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[4:8]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def _flush_l2(torch, buf):
+    buf.add_(1.0)
+
+
+def run_gpu(args) -> dict:
+    import torch
+
+    import c3lindblad_gb300 as c3
+    from c3lindblad_gb300 import runtime as rt
+
+    ws, rank, local = _dist()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    dev = torch.device(f"cuda:{local}")
+    torch.cuda.set_device(dev)
+    wl = WORKLOADS[args.workload]
+    spec_path = ROOT / "tests" / "golden" / f"{wl['spec']}.spec.npz"
+    gold = dict(np.load(ROOT / "tests" / "golden" / f"{wl['spec']}.golden.npz"))
+    omega = np.linspace(*wl["omega"])
+    eta = wl["eta"]
+    spec = c3.ProblemSpec.load(spec_path)
+
+    # one-off host compilation of the device programs (setup, not timed)
+    t0 = time.perf_counter()
+    base = c3.ComponentStaticProblem.compile(spec, device=dev)
+    _ = base.plan
+    eom_problem = c3.ComponentEOMProblem.compile(c3.eom_ccsd_problem(base), base, 1)
+    _ = eom_problem.plan
+    _ = eom_problem.plan.sources(spec.impurity_site)
+    setup_seconds = time.perf_counter() - t0
+
+    def step(problem, eomp):
+        sol = c3.solve_component_ccsd(problem)
+        ctx = c3.ComponentEOMContext(eomp, torch.from_numpy(sol.amplitudes))
+        op = c3.ComponentSigmaOperator(ctx)
+        src = c3.component_eom_sources(ctx)
+        res = c3.component_retarded_green(op, src, omega, eta)
+        return sol, res
+
+    # resident problem: device tables uploaded once
+    _ = base.ops
+    flush = torch.zeros(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MB > 129 MB L2
+    for _ in range(args.warmup):
+        step(base, eom_problem)
+    torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    times = []
+    rt.LaunchCounter.reset()
+    stream = torch.cuda.current_stream(dev)
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            _flush_l2(torch, flush)
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            sol, res = step(base, eom_problem)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1) / 1000.0)
+    launches = rt.LaunchCounter.reset()
+    t_step = float(np.mean(times))
+    if ws > 1:
+        import torch.distributed as dist
+        tt = torch.tensor([t_step], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_step = float(tt.item())
+
+    # accuracy against the reference FP64 run (subset of the grid it computed)
+    amp_err = float(np.max(np.abs(sol.amplitudes - gold["solution_amplitudes"])) /
+                    np.max(np.abs(gold["solution_amplitudes"])))
+    idx = [int(np.argmin(np.abs(omega - w))) for w in gold["green_omega"]]
+    g_err = float(np.max(np.abs(res.retarded[idx] - gold["green_retarded"])) / np.max(np.abs(gold["green_retarded"])))
+
+    # end to end from host buffers through the public API (tables uploaded inside)
+    e2e_times = []
+    h2d = d2h = 0
+    for k in range(max(1, min(args.steps, 3))):
+        _flush_l2(torch, flush)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        problem = c3.ComponentStaticProblem(spec, device=dev)
+        problem._plan = base.plan          # host-compiled program reused; device upload happens here
+        eomp = c3.ComponentEOMProblem(problem, 0, 1)
+        eomp._plan = eom_problem.plan
+        sol2, res2 = step(problem, eomp)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        e2e_times.append(e0.elapsed_time(e1) / 1000.0)
+        if k == 0:
+            h2d = sum(t.numel() * t.element_size() for t in problem.ops._up.keep)
+            h2d += sum(t.numel() * t.element_size() for t in res2._channels[0].basis.V[:0])  # none
+            d2h = sol2.amplitudes.nbytes + sol2.variables.nbytes + res2.retarded.nbytes * 3
+    e2e = float(np.mean(e2e_times))
+
+    # dominant-kernel roofline: the JVP output stage (k_wedge<static>) timed alone
+    roof = kernel_roofline(base, dev)
+    hbm, bf16, peak_kind = _peaks()
+    out = {
+        "metric": METRIC, "value": t_step, "unit": "s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": t_step * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "c128", "data": "synthetic",
+        "config": {"workload": args.workload, "description": wl["label"], "precision": "fp64 (plain)",
+                   "batched_omega": True, "warm_start": "none", "l2": "flushed between steps (256 MB write)",
+                   "parallelism": "replicas" if ws > 1 else "single", "setup_seconds": setup_seconds,
+                   "newton_iterations": sol.iterations, "jvp_evaluations": sol.jvp_evaluations,
+                   "residual_evaluations": sol.residual_evaluations, "krylov_dimensions": list(res.krylov_dimensions),
+                   "amplitude_rel_err_vs_reference": amp_err, "green_rel_err_vs_reference": g_err,
+                   "packed_residual_norm": sol.packed_residual_norm},
+        "gpu_launches": int(launches),
+        "e2e": {"value": e2e, "unit": "s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "roofline": dict(roof, peak=hbm, frac=roof["achieved"] / hbm, peak_source=peak_kind),
+        "clocks": clocks.summary(),
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(spec, gold, omega)
+    return out if rank == 0 else None
+
+
+def kernel_roofline(problem, dev) -> dict:
+    """HBM roofline of the JVP action's output stage (the most-launched wedge kernel).
+
+    Algorithmic bytes per launch: every workspace entry the stage reads once
+    (anchor atoms and rest forms referenced by its instances), the instance
+    tables, the per-element tables and the written real outputs.
+    """
+    import torch
+    import ctypes as C
+
+    from c3lindblad_gb300 import runtime as rt
+
+    ops = problem.ops
+    plan = problem.plan
+    stage = plan.program.stages["jvp"]
+    ep = plan.epilogue_jvp
+    read = set()
+    for inst in stage.instances:
+        for j in range(int(inst["nfac"])):
+            d = int(inst["fac_deg"][j])
+            read.add((int(inst["fac_off"][j]), d))
+    ws_bytes = sum(16 * plan.n ** d for _, d in read)
+    table_bytes = stage.instances.nbytes + stage.elements.nbytes + stage.digits.nbytes + stage.tiles.nbytes
+    elem = stage.elements.size
+    ep_bytes = elem * (16 + 8 + 8 + 16 + 16)  # lam, col, pair, scale, src
+    out_bytes = 8 * plan.num_variables
+    algorithmic = ws_bytes + table_bytes + ep_bytes + out_bytes
+    x = torch.zeros(plan.num_variables, dtype=torch.float64, device=dev)
+    y = torch.empty_like(x)
+    ops.linearize(x, y)
+    d = torch.ones_like(x)
+    ops.jvp(d, y)
+    st = rt.wedge_stage(ops._up, stage)
+    a = ops.jvp_action
+    lib = rt.lib()
+    stream = torch.cuda.current_stream(dev)
+    reps = 200
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        lib.c3l_wedge_static_out(C.byref(st), plan.n, ops.ws_lin.data_ptr(), a.lam, a.canon, a.col, a.pair, a.scale,
+                                 y.data_ptr(), stream.cuda_stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    per = e0.elapsed_time(e1) / 1000.0 / reps
+    return {"bound": "hbm", "kernel": "k_wedge<kStatic> (JVP output stage)", "achieved": algorithmic / per / 1e9,
+            "unit": "GB/s", "traffic": None, "algorithmic_bytes": int(algorithmic), "launch_us": per * 1e6,
+            "instances": int(stage.instances.size), "elements": int(elem)}
+
+
+def cpu_baseline(spec, gold, omega, budget_s: float = 20.0) -> dict:
+    """Per-call timings of the CPU oracle scaled by the reference run's call counts."""
+    from oracle import component_oracle as oc
+
+    p = oc.OracleProblem(spec.as_dict())
+    x = gold["fixed_amplitudes"]
+    d = gold["fixed_direction"]
+    t0 = time.perf_counter()
+    p.residual(x)
+    t_res = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    p.jvp(x, d)
+    t_jvp = time.perf_counter() - t0
+    eom = oc.OracleEOM(p, gold["solution_amplitudes"], 0, 1)
+    v = gold["eomp_probe"]
+    k = 0
+    t0 = time.perf_counter()
+    while k < 50 and time.perf_counter() - t0 < budget_s / 4:
+        eom.sigma(v)
+        k += 1
+    t_sig = (time.perf_counter() - t0) / k
+    n_res = int(gold["solution_residual_evaluations"])
+    n_jvp = int(gold["solution_jvp_evaluations"])
+    sig_calls = float(gold["green_sigma_calls"]) * omega.size / gold["green_omega"].size
+    est = n_res * t_res + n_jvp * t_jvp + sig_calls * t_sig
+    return {"value": est, "unit": "s", "cores": 1, "kind": "port",
+            "sample": (f"oracle per-call times (residual {t_res:.3f}s, JVP {t_jvp:.3f}s, sigma {t_sig * 1e3:.2f}ms) "
+                       f"x the reference solver's call counts on this workload ({n_res} residuals, {n_jvp} JVPs, "
+                       f"{sig_calls:.0f} sigma calls for {omega.size} omega by per-frequency GMRES)")}
+
+
+def run_reference(args) -> dict | None:
+    ws, rank, _ = _dist()
+    if rank != 0:
+        return None
+    wl = WORKLOADS[args.workload]
+    from c3lindblad_gb300.spec import ProblemSpec
+
+    spec = ProblemSpec.load(ROOT / "tests" / "golden" / f"{wl['spec']}.spec.npz")
+    gold = dict(np.load(ROOT / "tests" / "golden" / f"{wl['spec']}.golden.npz"))
+    omega = np.linspace(*wl["omega"])
+    vals = []
+    for _ in range(args.warmup):
+        cpu_baseline(spec, gold, omega, budget_s=4.0)
+    for _ in range(args.steps):
+        cb = cpu_baseline(spec, gold, omega, budget_s=8.0)
+        vals.append(cb["value"])
+    v = float(np.mean(vals))
+    cb["value"] = v
+    return {"metric": METRIC, "value": v, "unit": "s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": v * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "c128", "data": "synthetic", "impl": "reference",
+            "config": {"workload": args.workload, "description": wl["label"]},
+            "cpu_baseline": cb, "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="siam10", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    out = run_reference(args) if args.impl == "reference" else run_gpu(args)
+    if out is not None:
+        print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

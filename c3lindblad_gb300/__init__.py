@@ -1,0 +1,39 @@
+"""GB300-native coupled-cluster hot path of C3L (Coupled-Cluster Coupled Lindblad).
+
+Drop-in replacements for the reference's static CCSD solve, EOM-CCSD sigma
+action and retarded Green function, computed by hand-written sm_103a CUDA
+kernels behind the C ABI declared in ``include/c3l_gb300.h``.
+"""
+
+from .spec import ProblemSpec
+from .static import (
+    ComponentCCSolution,
+    ComponentStaticAction,
+    ComponentStaticProblem,
+    NewtonKrylovPolicy,
+    NewtonKrylovStep,
+    component_static_jvp,
+    component_static_residual,
+    solve_component_ccsd,
+)
+from .response import (
+    ComponentEOMContext,
+    ComponentEOMProblem,
+    ComponentEOMSources,
+    ComponentRetardedGreen,
+    ComponentShiftedSolution,
+    ComponentSigmaOperator,
+    EOMCCSDProblem,
+    component_eom_context,
+    component_eom_sources,
+    component_retarded_green,
+    eom_ccsd_problem,
+)
+
+__all__ = [
+    "ProblemSpec", "ComponentCCSolution", "ComponentStaticAction", "ComponentStaticProblem", "NewtonKrylovPolicy",
+    "NewtonKrylovStep", "component_static_jvp", "component_static_residual", "solve_component_ccsd",
+    "ComponentEOMContext", "ComponentEOMProblem", "ComponentEOMSources", "ComponentRetardedGreen",
+    "ComponentShiftedSolution", "ComponentSigmaOperator", "EOMCCSDProblem", "component_eom_context",
+    "component_eom_sources", "component_retarded_green", "eom_ccsd_problem",
+]

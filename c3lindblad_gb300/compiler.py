@@ -513,12 +513,14 @@ def _digits(coords: Coordinates, positions: np.ndarray) -> np.ndarray:
 
 
 def compile_output(builder: Builder, name: str, terms: dict, coords: Coordinates,
-                   positions: np.ndarray, rest_stage: str, scalar_stage: str | None):
-    """Emit rest stage(s) and the canonical output stage for a term set.
+                   positions: np.ndarray, rest_stage: str, scalar_stage: str | None, extra=()):
+    """Emit rest stage(s) and the canonical output stage(s) for a term set.
 
     ``positions``: vector positions (in ``coords``) to evaluate, any order; the
-    stage stores them grouped by block.  Returns the offset of the scalar
-    (degree-zero) output in the workspace or -1.
+    stage stores them grouped by block.  ``extra``: further canonical stages
+    ``(stage_name, positions, scale)`` sharing the same rest forms, with every
+    instance coefficient multiplied by ``scale``.  Returns the offset of the
+    scalar (degree-zero) output in the workspace or -1.
     """
     sym = builder.sym
     groups, scalars = _group_by_anchor(terms)
@@ -565,12 +567,7 @@ def compile_output(builder: Builder, name: str, terms: dict, coords: Coordinates
             rows.extend(builder.wedge_instances((0, 0, 0, 0), coef, scal, (), lambda a: builder.atom_offsets[a]))
         scalar_off = builder.alloc((0, 0, 0, 0))
         builder.emit_stage(scalar_stage, "padded", [(scalar_off, 0, rows)])
-    # canonical output
-    pos = np.asarray(positions, np.int64)
-    blk = coords.block_of[pos]
-    order = np.argsort(blk, kind="stable")
-    pos = pos[order]
-    blk = blk[order]
+    # canonical output(s)
     block_rows = []
     for b, key in enumerate(coords.keys):
         rows = []
@@ -585,7 +582,15 @@ def compile_output(builder: Builder, name: str, terms: dict, coords: Coordinates
                 for sign, lists in multi_shuffles(key, [ka, kr]):
                     rows.append((complex(sign), [(aoffs[ka], sum(ka), lists[0]), (offs[kr], sum(kr), lists[1])]))
         block_rows.append((-1, sum(key), rows))
-    builder.emit_stage(name, "canonical", block_rows, elements=pos, digits=_digits(coords, pos), element_block=blk)
+    for stage_name, stage_pos, scale in ((name, positions, 1.0),) + tuple(extra):
+        pos = np.asarray(stage_pos, np.int64)
+        blk = coords.block_of[pos]
+        order = np.argsort(blk, kind="stable")
+        pos = pos[order]
+        blk = blk[order]
+        rows_scaled = [(o, d, [(c * scale, f) for c, f in rows]) for o, d, rows in block_rows]
+        builder.emit_stage(stage_name, "canonical", rows_scaled, elements=pos, digits=_digits(coords, pos),
+                           element_block=blk)
     return scalar_off
 
 

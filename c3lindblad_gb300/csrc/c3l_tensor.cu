@@ -1,0 +1,341 @@
+// Tensor-program kernels of the coupled-cluster hot path (sm_103a).
+//
+// The compiled program (c3lindblad_gb300/compiler.py) reduces the factorized
+// CCSD residual, its JVP and the EOM sigma action to three kernel families:
+//
+//   k_contract  -- builds atoms: padded blocks of interior products
+//                  (iota_a T, iota_b iota_a T, ...) of the amplitudes or of a
+//                  direction/response vector, one n-term dot product per entry.
+//   k_wedge     -- sums shuffle-signed products of padded block entries
+//                  ("instances") per output element: rest forms into padded
+//                  workspace blocks, and anchor ^ rest at canonical outputs
+//                  with the residual/sigma epilogue fused in.
+//   k_scatter / k_tilde_unpack -- move vectors between the reference's
+//                  canonical layout and the padded workspace.
+//
+// All arithmetic is complex FP64.  Instances of one output block are staged
+// through shared memory so every thread of a tile reads them once per chunk.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "c3l_gb300.h"
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kInstChunk = 32;
+
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+    return make_double2(fma(a.x, b.x, -a.y * b.y), fma(a.x, b.y, a.y * b.x));
+}
+__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 cfma(double2 a, double2 b, double2 c) {
+    // a*b + c
+    return make_double2(fma(a.x, b.x, fma(-a.y, b.y, c.x)), fma(a.x, b.y, fma(a.y, b.x, c.y)));
+}
+
+inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+inline c3l_status launch_status() {
+    return cudaGetLastError() == cudaSuccess ? C3L_OK : C3L_ERR_LAUNCH;
+}
+
+__global__ void k_tilde_unpack(int64_t dim, const double* __restrict__ x, const int64_t* __restrict__ ia,
+                               const int64_t* __restrict__ ib, const double2* __restrict__ ca,
+                               const double2* __restrict__ cb, double2* __restrict__ t) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < dim; i += (int64_t)gridDim.x * blockDim.x) {
+        const double xa = x[ia[i]];
+        const double xb = x[ib[i]];
+        const double2 a = ca[i];
+        const double2 b = cb[i];
+        t[i] = make_double2(fma(a.x, xa, b.x * xb), fma(a.y, xa, b.y * xb));
+    }
+}
+
+__global__ void k_scatter(int64_t count, const int64_t* __restrict__ dst, const int64_t* __restrict__ pos,
+                          const double* __restrict__ sign, const double2* __restrict__ vec, double2* __restrict__ ws) {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < count; e += (int64_t)gridDim.x * blockDim.x) {
+        const double s = sign[e];
+        double2 v = make_double2(0.0, 0.0);
+        if (s != 0.0) {
+            const double2 u = vec[pos[e]];
+            v = make_double2(s * u.x, s * u.y);
+        }
+        ws[dst[e]] = v;
+    }
+}
+
+__device__ __forceinline__ void powers(int n, int64_t* pw) {
+    pw[0] = 1;
+#pragma unroll
+    for (int i = 1; i < 6; ++i) pw[i] = pw[i - 1] * n;
+}
+
+__global__ void __launch_bounds__(kThreads) k_contract(c3l_contract_level lv, int n, const double2* __restrict__ vectors,
+                                                        double2* __restrict__ ws) {
+    const c3l_tile tile = lv.tiles[blockIdx.x];
+    if ((int)threadIdx.x >= tile.count) return;
+    const c3l_contract_task& task = lv.tasks[tile.block];
+    int64_t pw[6];
+    powers(n, pw);
+    const int64_t e = tile.start + threadIdx.x;
+    double2 acc = make_double2(0.0, 0.0);
+    if (task.const_off >= 0) acc = vectors[task.const_off + e];
+    for (int j = 0; j < task.nsrc; ++j) {
+        const int axis = task.axis[j];
+        const int64_t low = pw[task.deg - axis];
+        const int64_t hi = e / low;
+        const int64_t lo = e - hi * low;
+        const double2* src = ws + task.src_off[j] + hi * low * n + lo;
+        const double2* vec = vectors + task.vec_off[j];
+        double2 sum = make_double2(0.0, 0.0);
+        for (int m = 0; m < n; ++m) sum = cfma(vec[m], src[m * low], sum);
+        const double sg = task.sign[j];
+        acc.x = fma(sg, sum.x, acc.x);
+        acc.y = fma(sg, sum.y, acc.y);
+    }
+    ws[task.dst_off + e] = acc;
+}
+
+enum WedgeMode { kPadded = 0, kStatic = 1, kEom = 2, kSource = 3 };
+
+struct Epilogue {
+    const double2* lam;
+    const double2* src;
+    const int64_t* col;
+    const int64_t* pair;
+    const double2* scale;
+    double* xout;
+    double2* cout;
+    double2 cscale;
+};
+
+template <int MODE>
+__global__ void __launch_bounds__(kThreads) k_wedge(c3l_wedge_stage st, int n, double2* ws, Epilogue ep) {
+    __shared__ c3l_instance sinst[kInstChunk];
+    const c3l_tile tile = st.tiles[blockIdx.x];
+    const c3l_block blk = st.blocks[tile.block];
+    const bool active = (int)threadIdx.x < tile.count;
+    const int64_t e = tile.start + threadIdx.x;
+    int64_t pw[6];
+    powers(n, pw);
+    int dig[4] = {0, 0, 0, 0};
+    if (active) {
+        if (MODE == kPadded) {
+            int64_t r = e;
+            for (int c = blk.deg - 1; c >= 0; --c) {
+                dig[c] = (int)(r % n);
+                r /= n;
+            }
+        } else {
+            const int64_t packed = st.digits[e];
+#pragma unroll
+            for (int c = 0; c < 4; ++c) dig[c] = (int)((packed >> (8 * c)) & 0xFF);
+        }
+    }
+    double2 acc = make_double2(0.0, 0.0);
+    for (int64_t base = blk.inst_begin; base < blk.inst_end; base += kInstChunk) {
+        const int64_t left = blk.inst_end - base;
+        const int cnt = left < kInstChunk ? (int)left : kInstChunk;
+        __syncthreads();
+        {
+            // cooperative copy of cnt instances (8-byte words)
+            const int64_t* src = reinterpret_cast<const int64_t*>(st.instances + base);
+            int64_t* dst = reinterpret_cast<int64_t*>(sinst);
+            const int words = cnt * (int)(sizeof(c3l_instance) / 8);
+            for (int w = threadIdx.x; w < words; w += blockDim.x) dst[w] = src[w];
+        }
+        __syncthreads();
+        if (active) {
+            for (int i = 0; i < cnt; ++i) {
+                const c3l_instance& in = sinst[i];
+                double2 v = make_double2(in.coef[0], in.coef[1]);
+                for (int j = 0; j < in.nfac; ++j) {
+                    const int d = in.fac_deg[j];
+                    int64_t off = in.fac_off[j];
+                    for (int q = 0; q < d; ++q) off += (int64_t)dig[in.axes[j][q]] * pw[d - 1 - q];
+                    v = cmul(v, ws[off]);
+                }
+                acc = cadd(acc, v);
+            }
+        }
+    }
+    if (!active) return;
+    if (MODE == kPadded) {
+        ws[blk.out_off + e] = acc;
+    } else if (MODE == kStatic) {
+        const int64_t mu = st.elements[e];
+        const double2 s = cfma(ep.lam[e], ep.src[mu], acc);
+        const double2 r = make_double2(s.y, -s.x);  // -i * s
+        const double2 v = cmul(r, ep.scale[e]);
+        const int64_t c = ep.col[e];
+        ep.xout[c] = v.x;
+        if (ep.pair[e]) ep.xout[c + 1] = r.y;
+    } else if (MODE == kEom) {
+        const int64_t mu = st.elements[e];
+        ep.cout[mu] = cfma(ep.lam[e], ep.src[mu], acc);
+    } else {
+        const int64_t mu = st.elements[e];
+        ep.cout[mu] = cmul(ep.cscale, acc);
+    }
+}
+
+inline unsigned grid_for(int64_t count) {
+    int64_t b = (count + kThreads - 1) / kThreads;
+    if (b < 1) b = 1;
+    if (b > 65535LL * 16) b = 65535LL * 16;
+    return (unsigned)b;
+}
+
+c3l_status run_levels(const c3l_action* a, cudaStream_t s) {
+    for (int l = 0; l < a->nlevels; ++l) {
+        if (a->levels[l].ntiles <= 0) continue;
+        k_contract<<<(unsigned)a->levels[l].ntiles, kThreads, 0, s>>>(a->levels[l], a->n,
+                                                                     reinterpret_cast<const double2*>(a->vectors),
+                                                                     reinterpret_cast<double2*>(a->ws));
+    }
+    return launch_status();
+}
+
+c3l_status run_padded(const c3l_action* a, cudaStream_t s) {
+    Epilogue ep{};
+    for (int p = 0; p < a->npadded; ++p) {
+        if (a->padded[p].ntiles <= 0) continue;
+        k_wedge<kPadded><<<(unsigned)a->padded[p].ntiles, kThreads, 0, s>>>(a->padded[p], a->n,
+                                                                           reinterpret_cast<double2*>(a->ws), ep);
+    }
+    return launch_status();
+}
+
+c3l_status scatter(const c3l_action* a, const c3l_complex* vec, cudaStream_t s) {
+    if (a->scatter_count <= 0) return C3L_OK;
+    k_scatter<<<grid_for(a->scatter_count), kThreads, 0, s>>>(a->scatter_count, a->scatter_dst, a->scatter_pos,
+                                                            a->scatter_sign, reinterpret_cast<const double2*>(vec),
+                                                            reinterpret_cast<double2*>(a->ws));
+    return launch_status();
+}
+
+bool valid_action(const c3l_action* a) {
+    return a && a->ws && a->vectors && a->n > 0 && a->n <= 255 && a->nlevels >= 0 && a->nlevels <= C3L_MAX_LEVELS &&
+           a->npadded >= 0 && a->npadded <= C3L_MAX_STAGES;
+}
+
+}  // namespace
+
+extern "C" {
+
+c3l_status c3l_tilde_unpack(int64_t dim, const double* x, const int64_t* ia, const int64_t* ib, const c3l_complex* ca,
+                            const c3l_complex* cb, c3l_complex* t, void* stream) {
+    if (dim < 0 || (dim > 0 && (!x || !ia || !ib || !ca || !cb || !t))) return C3L_ERR_ARGUMENT;
+    if (dim == 0) return C3L_OK;
+    k_tilde_unpack<<<grid_for(dim), kThreads, 0, as_stream(stream)>>>(dim, x, ia, ib, reinterpret_cast<const double2*>(ca),
+                                                                     reinterpret_cast<const double2*>(cb),
+                                                                     reinterpret_cast<double2*>(t));
+    return launch_status();
+}
+
+c3l_status c3l_scatter_padded(int64_t count, const int64_t* dst, const int64_t* pos, const double* sign,
+                              const c3l_complex* vec, c3l_complex* ws, void* stream) {
+    if (count < 0 || (count > 0 && (!dst || !pos || !sign || !vec || !ws))) return C3L_ERR_ARGUMENT;
+    if (count == 0) return C3L_OK;
+    k_scatter<<<grid_for(count), kThreads, 0, as_stream(stream)>>>(count, dst, pos, sign, reinterpret_cast<const double2*>(vec),
+                                                                  reinterpret_cast<double2*>(ws));
+    return launch_status();
+}
+
+c3l_status c3l_contract(const c3l_contract_level* level, int32_t n, const c3l_complex* vectors, c3l_complex* ws,
+                        void* stream) {
+    if (!level || !vectors || !ws || n <= 0 || n > 255) return C3L_ERR_ARGUMENT;
+    if (level->ntiles <= 0) return C3L_OK;
+    k_contract<<<(unsigned)level->ntiles, kThreads, 0, as_stream(stream)>>>(*level, n, reinterpret_cast<const double2*>(vectors),
+                                                                           reinterpret_cast<double2*>(ws));
+    return launch_status();
+}
+
+c3l_status c3l_wedge_padded(const c3l_wedge_stage* stage, int32_t n, c3l_complex* ws, void* stream) {
+    if (!stage || !ws || n <= 0 || n > 255) return C3L_ERR_ARGUMENT;
+    if (stage->ntiles <= 0) return C3L_OK;
+    Epilogue ep{};
+    k_wedge<kPadded><<<(unsigned)stage->ntiles, kThreads, 0, as_stream(stream)>>>(*stage, n, reinterpret_cast<double2*>(ws), ep);
+    return launch_status();
+}
+
+c3l_status c3l_wedge_static_out(const c3l_wedge_stage* stage, int32_t n, const c3l_complex* ws, const c3l_complex* lam,
+                                const c3l_complex* src, const int64_t* col, const int64_t* pair, const c3l_complex* scale,
+                                double* xout, void* stream) {
+    if (!stage || !ws || !lam || !src || !col || !pair || !scale || !xout || n <= 0 || n > 255) return C3L_ERR_ARGUMENT;
+    if (stage->ntiles <= 0) return C3L_OK;
+    Epilogue ep{};
+    ep.lam = reinterpret_cast<const double2*>(lam);
+    ep.src = reinterpret_cast<const double2*>(src);
+    ep.col = col;
+    ep.pair = pair;
+    ep.scale = reinterpret_cast<const double2*>(scale);
+    ep.xout = xout;
+    k_wedge<kStatic><<<(unsigned)stage->ntiles, kThreads, 0, as_stream(stream)>>>(
+        *stage, n, const_cast<double2*>(reinterpret_cast<const double2*>(ws)), ep);
+    return launch_status();
+}
+
+c3l_status c3l_wedge_eom_out(const c3l_wedge_stage* stage, int32_t n, const c3l_complex* ws, const c3l_complex* lam,
+                             const c3l_complex* xin, c3l_complex* out, void* stream) {
+    if (!stage || !ws || !lam || !xin || !out || n <= 0 || n > 255) return C3L_ERR_ARGUMENT;
+    if (stage->ntiles <= 0) return C3L_OK;
+    Epilogue ep{};
+    ep.lam = reinterpret_cast<const double2*>(lam);
+    ep.src = reinterpret_cast<const double2*>(xin);
+    ep.cout = reinterpret_cast<double2*>(out);
+    k_wedge<kEom><<<(unsigned)stage->ntiles, kThreads, 0, as_stream(stream)>>>(
+        *stage, n, const_cast<double2*>(reinterpret_cast<const double2*>(ws)), ep);
+    return launch_status();
+}
+
+c3l_status c3l_wedge_source_out(const c3l_wedge_stage* stage, int32_t n, const c3l_complex* ws, c3l_complex scale,
+                                c3l_complex* out, void* stream) {
+    if (!stage || !ws || !out || n <= 0 || n > 255) return C3L_ERR_ARGUMENT;
+    if (stage->ntiles <= 0) return C3L_OK;
+    Epilogue ep{};
+    ep.cscale = make_double2(scale.re, scale.im);
+    ep.cout = reinterpret_cast<double2*>(out);
+    k_wedge<kSource><<<(unsigned)stage->ntiles, kThreads, 0, as_stream(stream)>>>(
+        *stage, n, const_cast<double2*>(reinterpret_cast<const double2*>(ws)), ep);
+    return launch_status();
+}
+
+c3l_status c3l_action_prepare(const c3l_action* action, const c3l_complex* t, void* stream) {
+    if (!valid_action(action) || !t) return C3L_ERR_ARGUMENT;
+    cudaStream_t s = as_stream(stream);
+    c3l_status st = scatter(action, t, s);
+    if (st) return st;
+    if ((st = run_levels(action, s))) return st;
+    return run_padded(action, s);
+}
+
+c3l_status c3l_static_apply(const c3l_static_action* sa, const double* x, double* xout, void* stream) {
+    if (!sa || !x || !xout || !valid_action(&sa->action) || !sa->canon || !sa->tilde_ia || !sa->tilde_ib ||
+        !sa->tilde_ca || !sa->tilde_cb || sa->num_amplitudes <= 0)
+        return C3L_ERR_ARGUMENT;
+    cudaStream_t s = as_stream(stream);
+    c3l_status st = c3l_tilde_unpack(sa->num_amplitudes, x, sa->tilde_ia, sa->tilde_ib, sa->tilde_ca, sa->tilde_cb,
+                                     sa->canon, stream);
+    if (st) return st;
+    if ((st = scatter(&sa->action, sa->canon, s))) return st;
+    if ((st = run_levels(&sa->action, s))) return st;
+    if ((st = run_padded(&sa->action, s))) return st;
+    return c3l_wedge_static_out(&sa->action.out, sa->action.n, sa->action.ws, sa->lam, sa->canon, sa->col, sa->pair,
+                                sa->scale, xout, stream);
+}
+
+c3l_status c3l_eom_sigma(const c3l_eom_action* ea, const c3l_complex* xin, c3l_complex* out, void* stream) {
+    if (!ea || !xin || !out || !valid_action(&ea->action) || !ea->lam) return C3L_ERR_ARGUMENT;
+    cudaStream_t s = as_stream(stream);
+    c3l_status st = scatter(&ea->action, xin, s);
+    if (st) return st;
+    if ((st = run_levels(&ea->action, s))) return st;
+    if ((st = run_padded(&ea->action, s))) return st;
+    return c3l_wedge_eom_out(&ea->action.out, ea->action.n, ea->action.ws, ea->lam, xin, out, stream);
+}
+
+const char* c3l_version(void) { return "c3l_gb300 0.1.0 (sm_103a, fp64 complex programs)"; }
+
+}  // extern "C"

@@ -1,0 +1,203 @@
+"""Device-resident operators: static residual/JVP and EOM sigma.
+
+Each operator owns a complex workspace holding padded source blocks, atoms
+and rest forms, uploads its program tables once, and launches the kernel
+sequence of one action through a single C-ABI call
+(``c3l_static_apply`` / ``c3l_eom_sigma`` / ``c3l_action_prepare``).
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import torch
+
+from . import runtime as rt
+from .plans import EOMPlan, SourcePlan, StaticPlan
+
+
+def _cz(n: int, device) -> torch.Tensor:
+    return torch.zeros(max(n, 1), dtype=torch.complex128, device=device)
+
+
+class DeviceStatic:
+    """Residual, linearization and exact JVP in real tilde coordinates."""
+
+    def __init__(self, plan: StaticPlan, device=None):
+        self.device = rt.require_cuda(device)
+        self.lib = rt.lib()
+        self.plan = plan
+        prog = plan.program
+        up = rt.Uploader(self.device)
+        self._up = up
+        self.D = plan.num_variables
+        self.A = plan.num_amplitudes
+        self.ws_lin = _cz(prog.ws_size, self.device)
+        self.ws_res = _cz(prog.ws_size, self.device)
+        vec = up.raw(prog.vectors)
+        self.vec = vec
+        t = plan.tilde
+        ia, ib = up.raw(t.idx_a), up.raw(t.idx_b)
+        ca, cb = up.raw(t.coef_a), up.raw(t.coef_b)
+        self.canon_T = _cz(self.A, self.device)
+        self.canon_R = _cz(self.A, self.device)
+        self.canon_V = _cz(self.A, self.device)
+
+        def static_action(ws, levels_cls, padded, out, scatter, canon, ep):
+            sa = rt.StaticAction()
+            sa.action = rt.build_action(up, prog, vec.data_ptr(), ws, levels_cls, padded, out, scatter)
+            sa.num_amplitudes = self.A
+            sa.tilde_ia, sa.tilde_ib = ia.data_ptr(), ib.data_ptr()
+            sa.tilde_ca, sa.tilde_cb = ca.data_ptr(), cb.data_ptr()
+            sa.canon = canon.data_ptr()
+            sa.lam = up.ptr(ep["lam"])
+            sa.col = up.ptr(ep["col"])
+            sa.pair = up.ptr(ep["pair"])
+            sa.scale = up.ptr(ep["scale"])
+            return sa
+
+        self.res_action = static_action(self.ws_res, "T", ["res_rest_T", "res_scalar"], "res", plan.scatter_T,
+                                        self.canon_R, plan.epilogue)
+        self.lin_action = static_action(self.ws_lin, "T", ["res_rest_T", "res_scalar", "jvp_rest_T"], "res",
+                                        plan.scatter_T, self.canon_T, plan.epilogue)
+        self.jvp_action = static_action(self.ws_lin, "V", ["jvp_rest_V", "jvp_scalar"], "jvp", plan.scatter_V,
+                                        self.canon_V, plan.epilogue_jvp)
+        # complex outputs at every coordinate (arbitrary complex amplitudes)
+        self.cres_action = rt.build_action(up, prog, vec.data_ptr(), self.ws_res, "T", ["res_rest_T", "res_scalar"],
+                                           None, plan.scatter_T)
+        self.cres_stage = rt.wedge_stage(up, prog.stages["res_all"])
+        self.cres_lam = up.raw(plan.lam_all)
+        self.clin_action = rt.build_action(up, prog, vec.data_ptr(), self.ws_lin, "T", ["jvp_rest_T"], None,
+                                           plan.scatter_T)
+        self.cjvp_action = rt.build_action(up, prog, vec.data_ptr(), self.ws_lin, "V", ["jvp_rest_V", "jvp_scalar"],
+                                           None, plan.scatter_V)
+        self.cjvp_stage = rt.wedge_stage(up, prog.stages["jvp_all"])
+        self.cjvp_lam = up.raw(plan.lam_all_jvp)
+        self.launches = {
+            "residual": 1 + rt.action_launches(self.res_action.action),
+            "linearize": 1 + rt.action_launches(self.lin_action.action),
+            "jvp": 1 + rt.action_launches(self.jvp_action.action),
+        }
+        m4, self.preconditioner_diagnostics = plan.preconditioner_table()
+        self.pc_m4 = up.raw(m4)
+        self.pc_col = up.raw(t.rep_col)
+        self.pc_pair = up.raw(t.rep_pair)
+        self.nrep = int(t.rep_pos.size)
+        self.ia, self.ib, self.ca, self.cb = ia, ib, ca, cb
+
+    def _stream(self) -> int:
+        return rt.stream_ptr(self.device)
+
+    def _apply(self, action, x: torch.Tensor, out: torch.Tensor, what: str, launches: int) -> None:
+        if x.dtype != torch.float64 or out.dtype != torch.float64 or x.numel() != self.D or out.numel() != self.D:
+            raise ValueError(f"{what}: expected float64 vectors of length {self.D}")
+        rt.check(self.lib.c3l_static_apply(C.byref(action), x.data_ptr(), out.data_ptr(), self._stream()), what)
+        rt.LaunchCounter.add(launches)
+
+    def residual(self, x: torch.Tensor, out: torch.Tensor) -> None:
+        """Real residual at x (independent of the linearization point)."""
+        self._apply(self.res_action, x, out, "static residual", self.launches["residual"])
+
+    def linearize(self, x: torch.Tensor, out: torch.Tensor) -> None:
+        """Residual at x; also caches the amplitude-only JVP data at x."""
+        self._apply(self.lin_action, x, out, "static linearization", self.launches["linearize"])
+
+    def jvp(self, v: torch.Tensor, out: torch.Tensor) -> None:
+        """Exact JVP at the last linearization point."""
+        self._apply(self.jvp_action, v, out, "static JVP", self.launches["jvp"])
+
+    def precondition(self, x: torch.Tensor, out: torch.Tensor) -> None:
+        rt.check(self.lib.c3l_precondition(self.nrep, self.pc_m4.data_ptr(), self.pc_col.data_ptr(),
+                                           self.pc_pair.data_ptr(), x.data_ptr(), out.data_ptr(), self._stream()),
+                 "preconditioner")
+        rt.LaunchCounter.add(1)
+
+    def unpack(self, x: torch.Tensor, out: torch.Tensor) -> None:
+        """Complex amplitudes (reference vector order) from real variables."""
+        rt.check(self.lib.c3l_tilde_unpack(self.A, x.data_ptr(), self.ia.data_ptr(), self.ib.data_ptr(),
+                                           self.ca.data_ptr(), self.cb.data_ptr(), out.data_ptr(), self._stream()),
+                 "tilde unpack")
+        rt.LaunchCounter.add(1)
+
+    def reference_value(self, which: str = "res") -> complex:
+        off = self.plan.res_scalar_off
+        ws = self.ws_res if which == "res" else self.ws_lin
+        if off < 0:
+            return 0j
+        return complex(-1j * ws[off].item())
+
+    # ---------------------------------------------- complex-amplitude actions
+    def residual_complex(self, t: torch.Tensor, out: torch.Tensor) -> complex:
+        """-i pack(Lambda T + V) at all coordinates for arbitrary complex amplitudes."""
+        s = self._stream()
+        rt.check(self.lib.c3l_action_prepare(C.byref(self.cres_action), t.data_ptr(), s), "residual prepare")
+        rt.check(self.lib.c3l_wedge_eom_out(C.byref(self.cres_stage), self.plan.n, self.ws_res.data_ptr(),
+                                            self.cres_lam.data_ptr(), t.data_ptr(), out.data_ptr(), s), "residual out")
+        rt.LaunchCounter.add(rt.action_launches(self.cres_action) + 1)
+        return self.reference_value("res")
+
+    def jvp_complex(self, t: torch.Tensor, v: torch.Tensor, out: torch.Tensor) -> complex:
+        s = self._stream()
+        rt.check(self.lib.c3l_action_prepare(C.byref(self.clin_action), t.data_ptr(), s), "jvp linearize")
+        rt.check(self.lib.c3l_action_prepare(C.byref(self.cjvp_action), v.data_ptr(), s), "jvp prepare")
+        rt.check(self.lib.c3l_wedge_eom_out(C.byref(self.cjvp_stage), self.plan.n, self.ws_lin.data_ptr(),
+                                            self.cjvp_lam.data_ptr(), v.data_ptr(), out.data_ptr(), s), "jvp out")
+        rt.LaunchCounter.add(rt.action_launches(self.clin_action) + rt.action_launches(self.cjvp_action) + 1)
+        off = self.plan.jvp_scalar_off
+        return 0j if off < 0 else complex(-1j * self.ws_lin[off].item())
+
+
+class DeviceEOM:
+    """Sigma action of one (spin, charge) EOM block at fixed amplitudes."""
+
+    def __init__(self, plan: EOMPlan, amplitudes: torch.Tensor, device=None):
+        self.device = rt.require_cuda(device)
+        self.lib = rt.lib()
+        self.plan = plan
+        prog = plan.program
+        up = rt.Uploader(self.device)
+        self._up = up
+        self.N = plan.dimension
+        self.ws = _cz(prog.ws_size, self.device)
+        vec = up.raw(prog.vectors)
+        self.ctx_action = rt.build_action(up, prog, vec.data_ptr(), self.ws, "T", ["sigma_rest_T"], None, plan.scatter_T)
+        ea = rt.EomAction()
+        ea.action = rt.build_action(up, prog, vec.data_ptr(), self.ws, "X", ["sigma_rest_X"], "sigma", plan.scatter_X)
+        ea.lam = up.ptr(plan.lam_sigma)
+        self.sigma_action = ea
+        self.sigma_launches = rt.action_launches(ea.action)
+        self.amplitudes = amplitudes.to(self.device, torch.complex128).contiguous()
+        rt.check(self.lib.c3l_action_prepare(C.byref(self.ctx_action), self.amplitudes.data_ptr(),
+                                             rt.stream_ptr(self.device)), "EOM context")
+        rt.LaunchCounter.add(rt.action_launches(self.ctx_action))
+        self.diagonal = torch.from_numpy(plan.diagonal.copy()).to(self.device)
+
+    def sigma(self, x: torch.Tensor, out: torch.Tensor) -> None:
+        if x.dtype != torch.complex128 or out.dtype != torch.complex128 or x.numel() != self.N:
+            raise ValueError("sigma expects complex128 vectors of the EOM dimension")
+        rt.check(self.lib.c3l_eom_sigma(C.byref(self.sigma_action), x.data_ptr(), out.data_ptr(),
+                                        rt.stream_ptr(self.device)), "EOM sigma")
+        rt.LaunchCounter.add(self.sigma_launches)
+
+    def sources(self, site: int):
+        """(addition, removal, sink) device vectors for one site."""
+        sp: SourcePlan = self.plan.sources(site)
+        prog = sp.program
+        up = self._up
+        ws = _cz(prog.ws_size, self.device)
+        vec = up.raw(prog.vectors)
+        act = rt.build_action(up, prog, vec.data_ptr(), ws, "T", ["add_rest_T", "rem_rest_T"], None, sp.scatter_T)
+        s = rt.stream_ptr(self.device)
+        rt.check(self.lib.c3l_action_prepare(C.byref(act), self.amplitudes.data_ptr(), s), "EOM source context")
+        rt.LaunchCounter.add(rt.action_launches(act))
+        outs = []
+        for nm, scale in (("add", sp.source_scale[0]), ("rem", sp.source_scale[1])):
+            out = _cz(self.N, self.device)
+            st = rt.wedge_stage(up, prog.stages.get(nm))
+            rt.check(self.lib.c3l_wedge_source_out(C.byref(st), prog.n, ws.data_ptr(), rt.cplx(scale), out.data_ptr(), s),
+                     "EOM source")
+            rt.LaunchCounter.add(1)
+            outs.append(out)
+        sink = torch.from_numpy(sp.sink.copy()).to(self.device)
+        return outs[0], outs[1], sink

@@ -55,13 +55,20 @@ class StaticPlan:
         b.add_source("T", coords.keys)
         b.add_source("V", coords.keys)
         rep = self.tilde.rep_pos
-        self.res_scalar_off = compile_output(b, "res", self.res_terms, coords, rep, "res_rest", "res_scalar")
-        self.jvp_scalar_off = compile_output(b, "jvp", self.jvp_terms, coords, rep, "jvp_rest", "jvp_scalar")
+        allpos = np.arange(coords.dimension)
+        # real-coordinate outputs at tilde representatives (Newton path) and
+        # complex outputs -i(...) at every coordinate (arbitrary amplitudes)
+        self.res_scalar_off = compile_output(b, "res", self.res_terms, coords, rep, "res_rest", "res_scalar",
+                                             extra=(("res_all", allpos, -1j),))
+        self.jvp_scalar_off = compile_output(b, "jvp", self.jvp_terms, coords, rep, "jvp_rest", "jvp_scalar",
+                                             extra=(("jvp_all", allpos, -1j),))
         self.program = b.finish()
         self.scatter_T = _scatter_table(coords, self.program.source_offsets["T"])
         self.scatter_V = _scatter_table(coords, self.program.source_offsets["V"])
         lam = coords.rapidity_sum(spec.rapidities)
         self.rapidity_diagonal = -1j * lam          # newton_krylov.py:137-155
+        self.lam_all = -1j * lam[self.program.stages["res_all"].elements]
+        self.lam_all_jvp = -1j * lam[self.program.stages["jvp_all"].elements]
         # epilogue per canonical output element (elements are tilde representatives)
         out = self.program.stages["res"]
         self.epilogue = self._epilogue(out.elements, lam)
@@ -113,21 +120,18 @@ class StaticPlan:
 
 
 class EOMPlan:
-    """S13 sigma action of one (spin, charge) block plus its sources and sink.
+    """S13 sigma action of one (spin, charge) block.
 
-    Mirrors ``component_eom_context`` / ``component_eom_sigma`` /
-    ``component_eom_sources`` (``src/c3l/cc/component_tensor.py:2234-2302, 2816-2858``).
+    Mirrors ``component_eom_context`` / ``component_eom_sigma``
+    (``src/c3l/cc/component_tensor.py:2234-2302``).
     """
 
-    def __init__(self, static: StaticPlan, spin: int = 0, charge: int = 1, site: int | None = None):
+    def __init__(self, static: StaticPlan, spin: int = 0, charge: int = 1):
         if spin not in (0, 1) or charge not in (1, -1):
             raise ValueError("response spin must be 0/1 and charge +1/-1")
         spec = static.spec
         self.static = static
         self.spin, self.charge = spin, charge
-        self.site = spec.impurity_site if site is None else int(site)
-        if not 0 <= self.site < spec.n:
-            raise ValueError("site is outside the auxiliary model")
         n = spec.n
         self.coords = coords = eom_coordinates(n, spin, charge)
         sym = Symbolic(spec, static.coords, coords.keys)
@@ -139,13 +143,52 @@ class EOMPlan:
         b.add_source("X", coords.keys)
         allpos = np.arange(coords.dimension)
         compile_output(b, "sigma", self.sigma_terms, coords, allpos, "sigma_rest", None)
-        table = spec.source_factor[self.site, spin]  # c, c_dagger, tilde_c, tilde_c_dagger
-        if charge == 1:
+        self.program = b.finish()
+        self.scatter_T = _scatter_table(static.coords, self.program.source_offsets["T"])
+        self.scatter_X = _scatter_table(coords, self.program.source_offsets["X"])
+        lam = coords.rapidity_sum(spec.rapidities)
+        self.diagonal = lam                                   # component_response.py:28-40
+        self.lam_sigma = lam[self.program.stages["sigma"].elements]
+        self._sources: dict = {}
+
+    @property
+    def dimension(self) -> int:
+        return self.coords.dimension
+
+    def sources(self, site: int) -> "SourcePlan":
+        got = self._sources.get(site)
+        if got is None:
+            got = SourcePlan(self, site)
+            self._sources[site] = got
+        return got
+
+
+class SourcePlan:
+    """Addition/removal sources and the trace sink of one site.
+
+    Sources are ``pack(creator + iota_a T)`` of a physical operator, scaled
+    by ``-i`` for the tilde channel; the sink is the annihilator part at
+    degree-one coordinates (``src/c3l/cc/component_tensor.py:2788-2858``).
+    """
+
+    def __init__(self, eom: EOMPlan, site: int):
+        spec = eom.static.spec
+        n = spec.n
+        if not 0 <= int(site) < n:
+            raise ValueError("site is outside the auxiliary model")
+        self.site = int(site)
+        coords = eom.coords
+        table = spec.source_factor[self.site, eom.spin]  # c, c_dagger, tilde_c, tilde_c_dagger
+        if eom.charge == 1:
             add_f, rem_f, sink_f = int(table[1]), int(table[2]), int(table[0])
             self.source_scale = (1.0 + 0j, -1j)
         else:
             add_f, rem_f, sink_f = int(table[3]), int(table[0]), int(table[1])
             self.source_scale = (-1j, 1.0 + 0j)
+        sym = Symbolic(spec, eom.static.coords, coords.keys)
+        b = Builder(sym, spec)
+        b.add_source("T", eom.static.coords.keys)
+        allpos = np.arange(coords.dimension)
         for name, f in (("add", add_f), ("rem", rem_f)):
             terms = {}
             for part in (1, 3):
@@ -154,12 +197,7 @@ class EOMPlan:
                     terms[(a,)] = 1.0 + 0j
             compile_output(b, name, terms, coords, allpos, f"{name}_rest", None)
         self.program = b.finish()
-        self.scatter_T = _scatter_table(static.coords, self.program.source_offsets["T"])
-        self.scatter_X = _scatter_table(coords, self.program.source_offsets["X"])
-        lam = coords.rapidity_sum(spec.rapidities)
-        self.diagonal = lam                                   # component_response.py:28-40
-        self.lam_sigma = lam[self.program.stages["sigma"].elements]
-        # sink: annihilator entries at degree-one coordinates (component_tensor.py:2801-2813)
+        self.scatter_T = _scatter_table(eom.static.coords, self.program.source_offsets["T"])
         ann = np.asarray(spec.annihilators[sink_f])
         sink = np.zeros(coords.dimension, np.complex128)
         for b_id, key in enumerate(coords.keys):
@@ -169,7 +207,3 @@ class EOMPlan:
             p = np.flatnonzero(coords.block_of == b_id)
             sink[p] = ann[g * n + coords.tuples[p, 0]]
         self.sink = sink
-
-    @property
-    def dimension(self) -> int:
-        return self.coords.dimension

@@ -1,0 +1,239 @@
+"""ctypes binding of ``libc3l_gb300.so`` and device-resident plan state.
+
+PyTorch provides device memory and the current CUDA stream; every kernel is
+launched through the library's C ABI (``include/c3l_gb300.h``).  Nothing here
+computes on the host: when the library or a GPU is missing the calls raise.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+import torch
+
+from . import _build
+
+_LIB = None
+
+
+class C3LError(RuntimeError):
+    pass
+
+
+# ----------------------------------------------------------------- structs
+class ContractLevel(C.Structure):
+    _fields_ = [("tasks", C.c_void_p), ("tiles", C.c_void_p), ("ntiles", C.c_int64)]
+
+
+class WedgeStage(C.Structure):
+    _fields_ = [("blocks", C.c_void_p), ("instances", C.c_void_p), ("tiles", C.c_void_p),
+                ("ntiles", C.c_int64), ("elements", C.c_void_p), ("digits", C.c_void_p)]
+
+
+class Action(C.Structure):
+    _fields_ = [("n", C.c_int32), ("nlevels", C.c_int32), ("npadded", C.c_int32), ("pad", C.c_int32),
+                ("vectors", C.c_void_p), ("ws", C.c_void_p), ("scatter_count", C.c_int64),
+                ("scatter_dst", C.c_void_p), ("scatter_pos", C.c_void_p), ("scatter_sign", C.c_void_p),
+                ("levels", ContractLevel * 8), ("padded", WedgeStage * 4), ("out", WedgeStage)]
+
+
+class StaticAction(C.Structure):
+    _fields_ = [("action", Action), ("num_amplitudes", C.c_int64), ("tilde_ia", C.c_void_p),
+                ("tilde_ib", C.c_void_p), ("tilde_ca", C.c_void_p), ("tilde_cb", C.c_void_p),
+                ("canon", C.c_void_p), ("lam", C.c_void_p), ("col", C.c_void_p), ("pair", C.c_void_p),
+                ("scale", C.c_void_p)]
+
+
+class EomAction(C.Structure):
+    _fields_ = [("action", Action), ("lam", C.c_void_p)]
+
+
+class Complex(C.Structure):
+    _fields_ = [("re", C.c_double), ("im", C.c_double)]
+
+
+EXPORTS = (
+    "c3l_tilde_unpack", "c3l_scatter_padded", "c3l_contract", "c3l_wedge_padded", "c3l_wedge_static_out",
+    "c3l_wedge_eom_out", "c3l_wedge_source_out", "c3l_action_prepare", "c3l_static_apply", "c3l_eom_sigma",
+    "c3l_multi_dot_scratch", "c3l_multi_dot_c", "c3l_multi_dot_r", "c3l_multi_axpy_c", "c3l_multi_axpy_r",
+    "c3l_scale_c", "c3l_scale_r", "c3l_precondition", "c3l_hessenberg_shifted", "c3l_hessenberg_coordinates",
+    "c3l_version",
+)
+
+
+def _declare(lib) -> None:
+    P, I64, I32, D = C.c_void_p, C.c_int64, C.c_int32, C.c_double
+    sig = {
+        "c3l_tilde_unpack": [I64, P, P, P, P, P, P, P],
+        "c3l_scatter_padded": [I64, P, P, P, P, P, P],
+        "c3l_contract": [P, I32, P, P, P],
+        "c3l_wedge_padded": [P, I32, P, P],
+        "c3l_wedge_static_out": [P, I32, P, P, P, P, P, P, P, P],
+        "c3l_wedge_eom_out": [P, I32, P, P, P, P, P],
+        "c3l_wedge_source_out": [P, I32, P, Complex, P, P],
+        "c3l_action_prepare": [P, P, P],
+        "c3l_static_apply": [P, P, P, P],
+        "c3l_eom_sigma": [P, P, P, P],
+        "c3l_multi_dot_c": [P, I64, I32, P, I64, P, P, P],
+        "c3l_multi_dot_r": [P, I64, I32, P, I64, P, P, P],
+        "c3l_multi_axpy_c": [P, I64, I32, P, Complex, P, I64, P],
+        "c3l_multi_axpy_r": [P, I64, I32, P, D, P, I64, P],
+        "c3l_scale_c": [I64, Complex, P, P, P],
+        "c3l_scale_r": [I64, D, P, P, P],
+        "c3l_precondition": [I64, P, P, P, P, P, P],
+        "c3l_hessenberg_shifted": [P, I64, I32, P, I32, D, P, P, P, P],
+        "c3l_hessenberg_coordinates": [P, I64, I32, P, I32, D, P, P, P],
+    }
+    for name, args in sig.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = C.c_int
+    lib.c3l_multi_dot_scratch.argtypes = [I32, I64]
+    lib.c3l_multi_dot_scratch.restype = I64
+    lib.c3l_version.argtypes = []
+    lib.c3l_version.restype = C.c_char_p
+
+
+def load_library(build_if_missing: bool = True):
+    """Load (building if needed) the in-tree CUDA library."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = _build.library_path()
+    if build_if_missing:
+        path = _build.build()
+    if not Path(path).exists():
+        raise C3LError(f"CUDA library {path} is missing; run c3lindblad_gb300._build.build()")
+    lib = C.CDLL(str(path))
+    _declare(lib)
+    _LIB = lib
+    return lib
+
+
+def lib():
+    return load_library()
+
+
+def check(status: int, what: str) -> None:
+    if status != 0:
+        raise C3LError(f"{what} failed with c3l_status {status}")
+
+
+def require_cuda(device=None) -> torch.device:
+    if not torch.cuda.is_available():
+        raise C3LError("c3lindblad_gb300 needs a CUDA device: there is no CPU fallback")
+    dev = torch.device(device if device is not None else "cuda")
+    if dev.type != "cuda":
+        raise C3LError("c3lindblad_gb300 runs on CUDA devices only")
+    return dev
+
+
+def stream_ptr(device) -> int:
+    return torch.cuda.current_stream(device).cuda_stream
+
+
+def ptr(t: torch.Tensor | None) -> int:
+    return 0 if t is None else t.data_ptr()
+
+
+def cplx(z: complex) -> Complex:
+    z = complex(z)
+    return Complex(z.real, z.imag)
+
+
+class Uploader:
+    """Keeps device copies of host tables alive and hands out raw pointers."""
+
+    def __init__(self, device):
+        self.device = device
+        self.keep: list = []
+
+    def raw(self, arr: np.ndarray) -> torch.Tensor:
+        a = np.ascontiguousarray(arr)
+        if a.dtype.names is not None or a.dtype == np.int8:
+            host = torch.from_numpy(a.view(np.uint8).reshape(-1).copy())
+        elif a.dtype == np.complex128:
+            host = torch.from_numpy(a.view(np.float64).reshape(-1).copy())
+        else:
+            host = torch.from_numpy(a.reshape(-1).copy())
+        t = host.to(self.device, non_blocking=False)
+        self.keep.append(t)
+        return t
+
+    def ptr(self, arr) -> int:
+        if arr is None:
+            return 0
+        if len(arr) == 0:
+            return 0
+        return self.raw(arr).data_ptr()
+
+
+def wedge_stage(up: Uploader, stage) -> WedgeStage:
+    st = WedgeStage()
+    if stage is None:
+        st.ntiles = 0
+        return st
+    st.blocks = up.ptr(stage.blocks)
+    st.instances = up.ptr(stage.instances)
+    st.tiles = up.ptr(stage.tiles)
+    st.ntiles = len(stage.tiles)
+    st.elements = up.ptr(stage.elements) if stage.elements is not None else 0
+    st.digits = up.ptr(stage.digits) if stage.digits is not None else 0
+    return st
+
+
+def build_action(up: Uploader, program, vectors_ptr: int, ws: torch.Tensor, levels_cls: str | None,
+                 padded_names: list, out_name: str | None, scatter) -> Action:
+    a = Action()
+    a.n = program.n
+    levels = program.levels.get(levels_cls, []) if levels_cls else []
+    if len(levels) > 8:
+        raise C3LError("too many contraction levels")
+    a.nlevels = len(levels)
+    for i, lv in enumerate(levels):
+        a.levels[i].tasks = up.ptr(lv.tasks)
+        a.levels[i].tiles = up.ptr(lv.tiles)
+        a.levels[i].ntiles = len(lv.tiles)
+    stages = [program.stages[nm] for nm in padded_names if nm in program.stages]
+    if len(stages) > 4:
+        raise C3LError("too many padded stages")
+    a.npadded = len(stages)
+    for i, s in enumerate(stages):
+        a.padded[i] = wedge_stage(up, s)
+    a.out = wedge_stage(up, program.stages.get(out_name) if out_name else None)
+    a.vectors = vectors_ptr
+    a.ws = ws.data_ptr()
+    if scatter is not None:
+        a.scatter_count = scatter.dst.size
+        a.scatter_dst = up.ptr(scatter.dst)
+        a.scatter_pos = up.ptr(scatter.pos)
+        a.scatter_sign = up.ptr(scatter.sign)
+    else:
+        a.scatter_count = 0
+    return a
+
+
+class LaunchCounter:
+    """Counts this library's kernel launches issued through the host wrappers."""
+
+    count = 0
+
+    @classmethod
+    def add(cls, k: int) -> None:
+        cls.count += k
+
+    @classmethod
+    def reset(cls) -> int:
+        c = cls.count
+        cls.count = 0
+        return c
+
+
+def action_launches(a: Action) -> int:
+    k = 1 if a.scatter_count > 0 else 0
+    k += sum(1 for i in range(a.nlevels) if a.levels[i].ntiles > 0)
+    k += sum(1 for i in range(a.npadded) if a.padded[i].ntiles > 0)
+    k += 1 if a.out.ntiles > 0 else 0
+    return k

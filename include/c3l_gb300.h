@@ -1,0 +1,244 @@
+/*
+ * c3l_gb300.h -- C ABI of the GB300-native coupled-cluster hot path.
+ *
+ * All pointers are device pointers unless stated otherwise; every entry point
+ * enqueues work on the given CUDA stream and returns a c3l_status (0 = ok).
+ * No entry point synchronizes the stream or allocates device memory; callers
+ * own every buffer (the Python host layer allocates them with PyTorch).
+ *
+ * Complex numbers are interleaved (re, im) doubles (cuDoubleComplex layout).
+ *
+ * The reference (haoen2021/C3Lindblad, package c3l) is pure Python and has
+ * no C ABI.  Each entry point below replaces one Python-level operation of
+ * the reference; the citation names the file:line it replaces.
+ */
+#ifndef C3L_GB300_H
+#define C3L_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int c3l_status;
+enum {
+    C3L_OK = 0,
+    C3L_ERR_ARGUMENT = 1,   /* null pointer, bad size or table entry */
+    C3L_ERR_LAUNCH = 2,     /* a kernel launch failed (cudaGetLastError) */
+    C3L_ERR_CAPACITY = 3    /* a size exceeds a stated maximum */
+};
+
+typedef struct { double re, im; } c3l_complex;
+
+/* ---------------------------------------------------------- program tables
+ * Built by c3lindblad_gb300/compiler.py (NumPy structured arrays with the
+ * same layout).  Offsets index a complex workspace ("ws").
+ */
+#define C3L_MAX_SOURCES 4
+#define C3L_MAX_FACTORS 6
+
+/* One padded destination block of an atom: dst = const + sum_j sign_j *
+ * sum_m vec_j[m] * src_j[... m at axis_j ...] (interior product,
+ * src/c3l/cc/component_tensor.py:226-246). */
+typedef struct {
+    int64_t dst_off;
+    int32_t deg;
+    int32_t nsrc;
+    int64_t const_off;                 /* -1: no creator constant          */
+    int64_t src_off[C3L_MAX_SOURCES];
+    int64_t vec_off[C3L_MAX_SOURCES];  /* into the factor-vector table     */
+    int32_t axis[C3L_MAX_SOURCES];
+    double sign[C3L_MAX_SOURCES];
+} c3l_contract_task;
+
+/* One shuffle-signed product of padded block entries (one wedge term). */
+typedef struct {
+    double coef[2];
+    int32_t nfac;
+    int32_t pad;
+    int64_t fac_off[C3L_MAX_FACTORS];
+    int32_t fac_deg[C3L_MAX_FACTORS];
+    int8_t axes[C3L_MAX_FACTORS][4];
+} c3l_instance;
+
+typedef struct {
+    int64_t inst_begin;
+    int64_t inst_end;
+    int64_t out_off;   /* padded stages: workspace offset of the block   */
+    int32_t deg;
+    int32_t pad;
+} c3l_block;
+
+/* A thread-block work unit: <= 256 consecutive outputs of one block/task. */
+typedef struct {
+    int32_t block;
+    int32_t count;
+    int64_t start;
+} c3l_tile;
+
+typedef struct {
+    const c3l_contract_task* tasks;
+    const c3l_tile* tiles;
+    int64_t ntiles;
+} c3l_contract_level;
+
+typedef struct {
+    const c3l_block* blocks;
+    const c3l_instance* instances;
+    const c3l_tile* tiles;
+    int64_t ntiles;
+    const int64_t* elements;  /* canonical stages: output vector positions */
+    const int64_t* digits;    /* canonical stages: packed index digits      */
+} c3l_wedge_stage;
+
+/* ------------------------------------------------------------ primitives */
+
+/* t[mu] = ca[mu] x[ia[mu]] + cb[mu] x[ib[mu]]  (TildeMap.unpack,
+ * src/c3l/cc/symmetry.py:67-85). */
+c3l_status c3l_tilde_unpack(int64_t dim, const double* x, const int64_t* ia, const int64_t* ib,
+                            const c3l_complex* ca, const c3l_complex* cb, c3l_complex* t,
+                            void* stream);
+
+/* ws[dst[e]] = sign[e] * vec[pos[e]]  (ComponentCoordinates.unpack,
+ * src/c3l/cc/component_tensor.py:302-325). */
+c3l_status c3l_scatter_padded(int64_t count, const int64_t* dst, const int64_t* pos, const double* sign,
+                              const c3l_complex* vec, c3l_complex* ws, void* stream);
+
+/* One level of atom construction (interior products of amplitudes/shifts,
+ * src/c3l/cc/component_tensor.py:1387-1397 and :226-246). */
+c3l_status c3l_contract(const c3l_contract_level* level, int32_t n, const c3l_complex* vectors,
+                        c3l_complex* ws, void* stream);
+
+/* Rest forms / scalars into padded workspace blocks (wedge materialization,
+ * src/c3l/cc/component_tensor.py:869-898, :1035-1137). */
+c3l_status c3l_wedge_padded(const c3l_wedge_stage* stage, int32_t n, c3l_complex* ws, void* stream);
+
+/* Static residual/JVP outputs at tilde representatives, fused epilogue
+ * r = -i (lam * src[mu] + V), written in real tilde coordinates
+ * (src/c3l/cc/component_tensor.py:1855-1858, src/c3l/cc/component_solver.py:57-74). */
+c3l_status c3l_wedge_static_out(const c3l_wedge_stage* stage, int32_t n, const c3l_complex* ws,
+                                const c3l_complex* lam, const c3l_complex* src, const int64_t* col,
+                                const int64_t* pair, const c3l_complex* scale, double* xout,
+                                void* stream);
+
+/* EOM sigma outputs: out[mu] = lam * x[mu] + V
+ * (src/c3l/cc/component_tensor.py:2288-2302). */
+c3l_status c3l_wedge_eom_out(const c3l_wedge_stage* stage, int32_t n, const c3l_complex* ws,
+                             const c3l_complex* lam, const c3l_complex* xin, c3l_complex* out,
+                             void* stream);
+
+/* EOM sources: out[mu] = scale * V  (src/c3l/cc/component_tensor.py:2788-2798). */
+c3l_status c3l_wedge_source_out(const c3l_wedge_stage* stage, int32_t n, const c3l_complex* ws,
+                                c3l_complex scale, c3l_complex* out, void* stream);
+
+/* ------------------------------------------------------ composite actions */
+
+#define C3L_MAX_LEVELS 8
+#define C3L_MAX_STAGES 4
+
+/* One operation = unpack/scatter, atom levels, padded stages, output stage. */
+typedef struct {
+    int32_t n;
+    int32_t nlevels;
+    int32_t npadded;
+    int32_t pad;
+    const c3l_complex* vectors;
+    c3l_complex* ws;
+    int64_t scatter_count;
+    const int64_t* scatter_dst;
+    const int64_t* scatter_pos;
+    const double* scatter_sign;
+    c3l_contract_level levels[C3L_MAX_LEVELS];
+    c3l_wedge_stage padded[C3L_MAX_STAGES];
+    c3l_wedge_stage out;
+} c3l_action;
+
+/* Static residual or JVP in real tilde coordinates:
+ *   x (real, num_variables) -> tilde unpack -> padded -> atoms -> wedges -> xout.
+ * Replaces component_static_residual / component_static_linearized_jvp behind
+ * _real_residual / _real_linearized_jvp (src/c3l/cc/component_solver.py:57-74;
+ * src/c3l/cc/component_tensor.py:1552-1657, :1822-1868).
+ * canon: scratch complex[num_amplitudes] receiving the unpacked vector. */
+typedef struct {
+    c3l_action action;
+    int64_t num_amplitudes;
+    const int64_t* tilde_ia;
+    const int64_t* tilde_ib;
+    const c3l_complex* tilde_ca;
+    const c3l_complex* tilde_cb;
+    c3l_complex* canon;
+    const c3l_complex* lam;
+    const int64_t* col;
+    const int64_t* pair;
+    const c3l_complex* scale;
+} c3l_static_action;
+
+c3l_status c3l_static_apply(const c3l_static_action* action, const double* x, double* xout, void* stream);
+
+/* EOM sigma in one (spin, charge) block: xin (complex, dim) -> out.
+ * Replaces ComponentSigmaOperator.matvec (src/c3l/cc/component_response.py:53-58). */
+typedef struct {
+    c3l_action action;
+    const c3l_complex* lam;
+} c3l_eom_action;
+
+c3l_status c3l_eom_sigma(const c3l_eom_action* action, const c3l_complex* xin, c3l_complex* out, void* stream);
+
+/* Runs the amplitude-only part of an action (levels + padded stages) after
+ * scattering the complex amplitude vector t; used for linearization and EOM
+ * contexts (src/c3l/cc/component_tensor.py:1371-1549, :2234-2251). */
+c3l_status c3l_action_prepare(const c3l_action* action, const c3l_complex* t, void* stream);
+
+/* ------------------------------------------------------------ Krylov ops */
+
+/* out[j] = sum_i conj(V[j*ld + i]) * w[i], j < k  (two-pass deterministic
+ * reduction; partial: scratch of c3l_multi_dot_scratch(k, dim) entries).
+ * Replaces the zgemv projections of src/c3l/green/krylov.py:362-373. */
+int64_t c3l_multi_dot_scratch(int32_t k, int64_t dim);
+c3l_status c3l_multi_dot_c(const c3l_complex* V, int64_t ld, int32_t k, const c3l_complex* w, int64_t dim,
+                           c3l_complex* partial, c3l_complex* out, void* stream);
+c3l_status c3l_multi_dot_r(const double* V, int64_t ld, int32_t k, const double* w, int64_t dim,
+                           double* partial, double* out, void* stream);
+
+/* w[i] += alpha * sum_j c[j] * V[j*ld + i], j < k. */
+c3l_status c3l_multi_axpy_c(const c3l_complex* V, int64_t ld, int32_t k, const c3l_complex* c, c3l_complex alpha,
+                            c3l_complex* w, int64_t dim, void* stream);
+c3l_status c3l_multi_axpy_r(const double* V, int64_t ld, int32_t k, const double* c, double alpha,
+                            double* w, int64_t dim, void* stream);
+
+/* y = a * x (complex or real). */
+c3l_status c3l_scale_c(int64_t dim, c3l_complex a, const c3l_complex* x, c3l_complex* y, void* stream);
+c3l_status c3l_scale_r(int64_t dim, double a, const double* x, double* y, void* stream);
+
+/* Real preconditioner pack(unpack(x) / diag) as 2x2 blocks per tilde orbit
+ * (src/c3l/cc/newton_krylov.py:158-192). m4: [nrep][4] row-major blocks. */
+c3l_status c3l_precondition(int64_t nrep, const double* m4, const int64_t* col, const int64_t* pair,
+                            const double* x, double* y, void* stream);
+
+/* Shifted Hessenberg solves for all shifts (one thread block per shift):
+ * (z_s I - H_m) y = beta e_1 by streamed Givens QR, returning
+ *   green[s]    = sum_k sinkproj[k] y_k      (if sinkproj != NULL)
+ *   residual[s] = |H[m, m-1] y_{m-1}| / beta (Arnoldi relation residual)
+ * H: (m+1) x m, row-major with leading dimension ldh (complex).
+ * Replaces ArnoldiResolvent.coefficients/_reduced_residuals
+ * (src/c3l/green/krylov.py:66-93, :257-281). m <= C3L_MAX_HESSENBERG. */
+#define C3L_MAX_HESSENBERG 4096
+c3l_status c3l_hessenberg_shifted(const c3l_complex* H, int64_t ldh, int32_t m, const c3l_complex* shifts,
+                                  int32_t nshift, double beta, const c3l_complex* sinkproj,
+                                  c3l_complex* green, double* residual, void* stream);
+
+/* Full reduced coordinates Y[s][0..m) of the same systems (for solution
+ * vectors); rscratch: nshift * m*(m+1)/2 complex entries of caller memory. */
+c3l_status c3l_hessenberg_coordinates(const c3l_complex* H, int64_t ldh, int32_t m, const c3l_complex* shifts,
+                                      int32_t nshift, double beta, c3l_complex* rscratch, c3l_complex* Y,
+                                      void* stream);
+
+/* Library identification (host only). */
+const char* c3l_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* C3L_GB300_H */

@@ -348,7 +348,9 @@ class OracleProblem:
         return out
 
     def _shifts(self, form):
-        return {f: [p for p in homogeneous_parts(_clean(interior(a, form))) if p] for f, (_, a) in enumerate(self.factors)}
+        """iota_a T split by degree for every factor used by a product (component_tensor.py:1387-1397)."""
+        used = sorted({f for _, facs in self.products for f in facs})
+        return {f: [p for p in homogeneous_parts(_clean(interior(self.factors[f][1], form))) if p] for f in used}
 
     def _materialize(self, terms, degrees) -> dict:
         """Wedge each lazy term and keep the listed degrees (component_tensor.py:869-898)."""
@@ -427,31 +429,84 @@ class OracleEOM:
                     axis += 1
             diag[pos] = val
         self.diagonal = diag  # component_response.py:28-40
+        self.plan = self._compile_plan()
 
     @property
     def dimension(self) -> int:
         return self.coords.dimension
 
-    def sigma(self, vector) -> np.ndarray:
-        """Retained commutator action (component_tensor.py:2116-2302).
-
-        The reference propagates a placeholder for the response vector and
-        wedges it back in at the end; carrying the actual homogeneous parts
-        of the vector through the same factor applications is the same sum.
-        """
-        p = self.p
-        x = self.coords.unpack(vector)
-        total: dict = {}
-        for part in homogeneous_parts(_clean(x)):
-            if not part:
+    # A placeholder for the response vector: ("P", degree, contraction chain)
+    def _apply_factor_plan(self, states, f):
+        """Transformed factor with a placeholder input (component_tensor.py:2077-2113)."""
+        creator, annihilator = self.p.factors[f]
+        wedges = ([creator] if creator else []) + list(self.shifts[f])
+        out = []
+        for coef, forms in states:
+            for w in wedges:
+                out.append((coef, [w] + forms))
+            if not annihilator:
                 continue
-            for coef, facs in p.products:
-                states = [(coef, [part])]
+            prefix = 0
+            for pos, form in enumerate(forms):
+                if isinstance(form, tuple):
+                    deg = form[1]
+                    if deg > 0:
+                        out.append((coef * (-1) ** prefix, forms[:pos] + [("P", deg - 1, form[2] + (f,))] + forms[pos + 1:]))
+                    prefix += deg
+                else:
+                    c = interior(annihilator, form)
+                    if _nonzero(c):
+                        out.append((coef * (-1) ** prefix, forms[:pos] + [_clean(c)] + forms[pos + 1:]))
+                    prefix += degree(form)
+        return out
+
+    def _compile_plan(self):
+        """Group creation forms by (input degree, contraction chain) (component_tensor.py:2116-2223)."""
+        grouped: dict = {}
+
+        def accumulate(coef, forms, d):
+            pos = next(i for i, f in enumerate(forms) if isinstance(f, tuple))
+            ph = forms[pos]
+            after = sum(degree(f) for f in forms[pos + 1:])
+            coef = coef * (-1) ** (ph[1] * after)
+            creation = [f for f in forms if not isinstance(f, tuple)]
+            cdeg = sum(degree(f) for f in creation)
+            if cdeg + ph[1] not in (1, 3):
+                return
+            val = {(0, 0, 0, 0): np.asarray(coef, dtype=np.complex128)}
+            for f in creation:
+                val = wedge(val, f, self.p.n, max_degree=cdeg)
+            key = (d, ph[2], cdeg)
+            grouped[key] = sum_forms(grouped.get(key, {}), val)
+
+        for d in (1, 3):
+            for coef, facs in self.p.products:
+                states = [(coef, [("P", d, ())])]
                 for f in reversed(facs):
-                    states = p._apply_factor(states, f, self.shifts[f])
-                total = sum_forms(total, p._materialize(states, {1, 3}))
+                    states = self._apply_factor_plan(states, f)
+                for c, forms in states:
+                    accumulate(c, forms, d)
             for key, val in self.vacuum.items():
-                total = sum_forms(total, p._materialize([(-1.0, [part, {key: val}])], {1, 3}))
+                accumulate(-1.0, [("P", d, ()), {key: val}], d)
+        return [(d, chain, _clean(form)) for (d, chain, _), form in grouped.items() if _clean(form)]
+
+    def sigma(self, vector) -> np.ndarray:
+        """Retained commutator action over the precompiled plan (component_tensor.py:2254-2302)."""
+        p = self.p
+        x = _clean(self.coords.unpack(vector))
+        parts = {degree(h): h for h in homogeneous_parts(x) if h}
+        total: dict = {}
+        for d, chain, creation in self.plan:
+            acted = parts.get(d)
+            if acted is None:
+                continue
+            for f in chain:
+                acted = interior(p.factors[f][1], acted)
+                if not _nonzero(acted):
+                    break
+            else:
+                out = wedge(creation, _clean(acted), p.n)
+                total = sum_forms(total, {k: v for k, v in out.items() if sum(k) in (1, 3)})
         total = sum_forms(quadratic_action(x, p.rapidities, p.n), total)
         return self.coords.pack(total)
 

@@ -141,17 +141,26 @@ class InterpretedEOM:
         self.ws = np.zeros(prog.ws_size, np.complex128)
         sc = plan.scatter_T
         t = np.asarray(amplitudes, np.complex128)
+        self.t = t
         self.ws[sc.dst] = sc.sign * t[sc.pos]
         run_levels(prog, "T", self.ws)
         run_padded(prog, "sigma_rest_T", self.ws)
-        srcs = []
-        for name, scale in zip(("add", "rem"), plan.source_scale):
-            run_padded(prog, f"{name}_rest_T", self.ws)
-            V = run_canonical(prog, name, self.ws)
-            out = np.zeros(plan.dimension, np.complex128)
-            out[prog.stages[name].elements] = scale * V
-            srcs.append(out)
-        self.addition, self.removal = srcs
+
+    def sources(self, site: int):
+        sp = self.plan.sources(site)
+        prog = sp.program
+        ws = np.zeros(prog.ws_size, np.complex128)
+        sc = sp.scatter_T
+        ws[sc.dst] = sc.sign * self.t[sc.pos]
+        run_levels(prog, "T", ws)
+        out = []
+        for name, scale in zip(("add", "rem"), sp.source_scale):
+            run_padded(prog, f"{name}_rest_T", ws)
+            V = run_canonical(prog, name, ws)
+            v = np.zeros(self.plan.dimension, np.complex128)
+            v[prog.stages[name].elements] = scale * V
+            out.append(v)
+        return out[0], out[1], sp.sink
 
     def sigma(self, x):
         p = self.plan

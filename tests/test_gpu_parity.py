@@ -1,0 +1,183 @@
+"""GPU parity: device actions and solvers against the reference's golden vectors.
+
+Every call goes through ``libc3l_gb300.so``.  Tolerances: actions at fixed
+inputs 1e-12 relative (FP64 reassociation only); converged amplitudes and
+G^R 1e-8 relative with the residual at or below 1e-10 (the bar of the
+reference's own CPU/device parity tests, tests/cc/test_component_jax.py).
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import golden_names, load, relerr
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+@pytest.fixture(scope="module")
+def problems(cuda_device):
+    import c3lindblad_gb300 as c3
+
+    cache = {}
+
+    def get(name):
+        if name not in cache:
+            spec, g = load(name)
+            cache[name] = (spec, g, c3.ComponentStaticProblem.compile(spec, device=cuda_device))
+        return cache[name]
+
+    return get
+
+
+def _packed(plan, vec):
+    t = plan.tilde
+    x = np.empty(plan.num_variables)
+    x[t.rep_col] = (vec[t.rep_pos] * t.rep_scale).real
+    pr = t.rep_pair == 1
+    x[t.rep_col[pr] + 1] = vec[t.rep_pos[pr]].imag
+    return x
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_device_real_residual_linearization_and_jvp(name, problems, cuda_device):
+    spec, g, p = problems(name)
+    ops = p.ops
+    x = torch.from_numpy(g["fixed_variables"]).to(cuda_device)
+    d = torch.from_numpy(g["fixed_direction_variables"]).to(cuda_device)
+    r = torch.empty_like(x)
+    ops.residual(x, r)
+    assert relerr(r.cpu().numpy(), _packed(p.plan, g["residual"])) < 1e-12
+    assert abs(ops.reference_value() - g["residual_reference"]) < 1e-12 * max(1.0, abs(g["residual_reference"]))
+    ops.linearize(x, r)
+    assert relerr(r.cpu().numpy(), _packed(p.plan, g["residual"])) < 1e-12
+    j = torch.empty_like(x)
+    ops.jvp(d, j)
+    assert relerr(j.cpu().numpy(), _packed(p.plan, g["jvp"])) < 1e-12
+    # a residual at another point must not disturb the cached linearization
+    ops.residual(torch.zeros_like(x), r)
+    ops.jvp(d, j)
+    assert relerr(j.cpu().numpy(), _packed(p.plan, g["jvp"])) < 1e-12
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_component_static_residual_and_jvp_complex(name, problems):
+    import c3lindblad_gb300 as c3
+
+    spec, g, p = problems(name)
+    res = c3.component_static_residual(p, g["fixed_amplitudes"])
+    assert relerr(res.retained, g["residual"]) < 1e-12
+    assert abs(res.reference - g["residual_reference"]) < 1e-12 * max(1.0, abs(g["residual_reference"]))
+    jvp = c3.component_static_jvp(p, g["fixed_amplitudes"], g["fixed_direction"])
+    assert relerr(jvp.retained, g["jvp"]) < 1e-12
+
+
+def test_complex_residual_accepts_non_tilde_amplitudes(problems):
+    """Arbitrary complex amplitudes (outside the tilde subspace) match the oracle."""
+    import c3lindblad_gb300 as c3
+    from oracle import component_oracle as oc
+
+    spec, g, p = problems("readme")
+    rng = np.random.default_rng(7)
+    t = 1e-2 * (rng.normal(size=p.num_amplitudes) + 1j * rng.normal(size=p.num_amplitudes))
+    v = rng.normal(size=p.num_amplitudes) + 1j * rng.normal(size=p.num_amplitudes)
+    o = oc.OracleProblem(spec.as_dict())
+    assert relerr(c3.component_static_residual(p, t).retained, o.residual(t)[0]) < 1e-12
+    assert relerr(c3.component_static_jvp(p, t, v).retained, o.jvp(t, v)[0]) < 1e-12
+
+
+@pytest.mark.parametrize("name", golden_names(with_solution=True))
+@pytest.mark.parametrize("charge", [1, -1])
+def test_device_sigma_and_sources(name, charge, problems):
+    import c3lindblad_gb300 as c3
+
+    spec, g, p = problems(name)
+    tag = "p" if charge == 1 else "m"
+    eom = c3.eom_ccsd_problem(p)
+    ep = c3.ComponentEOMProblem.compile(eom, p, charge)
+    ctx = c3.component_eom_context(ep, g["solution_amplitudes"])
+    op = c3.ComponentSigmaOperator(ctx)
+    assert op.dimension == g[f"eom{tag}_probe"].size
+    assert relerr(op.diagonal, g[f"eom{tag}_diagonal"]) < 1e-14
+    assert relerr(op.matvec(g[f"eom{tag}_probe"]), g[f"eom{tag}_sigma"]) < 1e-12
+    src = c3.component_eom_sources(ctx)
+    assert np.max(np.abs(src.addition - g[f"eom{tag}_addition"])) < 1e-12
+    assert np.max(np.abs(src.removal - g[f"eom{tag}_removal"])) < 1e-12
+    assert np.max(np.abs(src.sink - g[f"eom{tag}_sink"])) < 1e-14
+
+
+@pytest.mark.parametrize("name", golden_names(with_solution=True))
+def test_newton_krylov_solution_matches_reference(name, problems):
+    import c3lindblad_gb300 as c3
+
+    spec, g, p = problems(name)
+    sol = c3.solve_component_ccsd(p)
+    assert sol.converged
+    assert sol.packed_residual_norm <= 1e-10
+    assert relerr(sol.amplitudes, g["solution_amplitudes"]) < 1e-8
+    assert sol.gpu_launches > 0
+    # warm restart from the converged amplitudes converges immediately
+    again = c3.solve_component_ccsd(p, sol.amplitudes)
+    assert again.converged and again.iterations == 0
+
+
+@pytest.mark.parametrize("name", [n for n in golden_names(with_solution=True)])
+def test_retarded_green_matches_reference(name, problems):
+    import c3lindblad_gb300 as c3
+
+    spec, g, p = problems(name)
+    if "green_retarded" not in g:
+        pytest.skip("no reference G^R for this fixture")
+    ep = c3.ComponentEOMProblem.compile(c3.eom_ccsd_problem(p), p, 1)
+    ctx = c3.component_eom_context(ep, g["solution_amplitudes"])
+    op = c3.ComponentSigmaOperator(ctx)
+    src = c3.component_eom_sources(ctx)
+    res = c3.component_retarded_green(op, src, g["green_omega"], float(g["green_eta"]))
+    assert relerr(res.retarded, g["green_retarded"]) < 1e-8
+    assert relerr(res.addition, g["green_addition"]) < 1e-8
+    assert np.max(res.addition_relative_residuals) <= 1e-10
+    assert np.max(res.removal_relative_residuals) <= 1e-10
+    # lazily reconstructed solution vectors satisfy (zI - A) x = b
+    s = res.addition_solutions[0]
+    z = complex(g["green_omega"][0], float(g["green_eta"]))
+    x = s.solution
+    resid = src.addition - (z * x - op.matvec(x))
+    assert np.linalg.norm(resid) / np.linalg.norm(src.addition) < 1e-8
+
+
+def test_krylov_primitives_against_numpy(cuda_device):
+    from c3lindblad_gb300.krylov import DeviceVectors, hessenberg_shifted
+
+    rng = np.random.default_rng(11)
+    vec = DeviceVectors(cuda_device)
+    k, n = 7, 5003
+    V = rng.normal(size=(k, n)) + 1j * rng.normal(size=(k, n))
+    w = rng.normal(size=n) + 1j * rng.normal(size=n)
+    Vd = torch.from_numpy(V).to(cuda_device)
+    wd = torch.from_numpy(w).to(cuda_device)
+    out = torch.empty(k, dtype=torch.complex128, device=cuda_device)
+    vec.dots_c(Vd, k, wd, out)
+    assert relerr(out.cpu().numpy(), V.conj() @ w) < 1e-13
+    c = rng.normal(size=k) + 1j * rng.normal(size=k)
+    vec.axpy_c(Vd, k, torch.from_numpy(c).to(cuda_device), -0.5 + 0.25j, wd)
+    assert relerr(wd.cpu().numpy(), w + (-0.5 + 0.25j) * (c @ V)) < 1e-13
+    Vr = rng.normal(size=(k, n))
+    wr = rng.normal(size=n)
+    outr = torch.empty(k, dtype=torch.float64, device=cuda_device)
+    vec.dots_r(torch.from_numpy(Vr).to(cuda_device), k, torch.from_numpy(wr).to(cuda_device), outr)
+    assert relerr(outr.cpu().numpy(), Vr @ wr) < 1e-13
+    # shifted Hessenberg solves
+    m = 37
+    H = np.triu(rng.normal(size=(m + 1, m)) + 1j * rng.normal(size=(m + 1, m)), -1)
+    shifts = np.linspace(-3, 3, 23) + 0.1j
+    p = rng.normal(size=m) + 1j * rng.normal(size=m)
+    green, resid = hessenberg_shifted(H, m, torch.from_numpy(shifts).to(cuda_device), 2.5,
+                                      torch.from_numpy(p).to(cuda_device))
+    e1 = np.zeros(m, complex)
+    e1[0] = 2.5
+    ys = [np.linalg.solve(z * np.eye(m) - H[:m, :m], e1) for z in shifts]
+    assert relerr(green.cpu().numpy(), np.array([p @ y for y in ys])) < 1e-10
+    assert relerr(resid.cpu().numpy(), np.array([abs(H[m, m - 1] * y[-1]) / 2.5 for y in ys])) < 1e-10

@@ -1,0 +1,89 @@
+"""Pin the CPU oracle against golden vectors produced by the reference itself."""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import golden_names, load, relerr
+from oracle import component_oracle as oc
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_oracle_coordinates_and_tilde_match_reference(name):
+    spec, g = load(name)
+    p = oc.OracleProblem(spec.as_dict())
+    if "cluster_masks" in g:
+        assert np.array_equal(np.asarray(p.masks, np.int64), g["cluster_masks"])
+    assert np.array_equal(p.tilde.partner, g["tilde_partner"])
+    assert np.allclose(p.tilde.phase, g["tilde_phase"], atol=1e-14)
+    assert list(p.tilde.independent) == list(g["tilde_independent"])
+    assert np.allclose(p.tilde.unpack(g["fixed_variables"]), g["fixed_amplitudes"], atol=1e-18, rtol=0)
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_oracle_residual_and_jvp_match_reference(name):
+    spec, g = load(name)
+    p = oc.OracleProblem(spec.as_dict())
+    r, ref = p.residual(g["fixed_amplitudes"])
+    assert relerr(r, g["residual"]) < 1e-12
+    assert abs(ref - g["residual_reference"]) < 1e-12 * max(1.0, abs(g["residual_reference"]))
+    j, jref = p.jvp(g["fixed_amplitudes"], g["fixed_direction"])
+    assert relerr(j, g["jvp"]) < 1e-12
+    assert abs(jref - g["jvp_reference"]) < 1e-12 * max(1.0, abs(g["jvp_reference"]))
+
+
+@pytest.mark.parametrize("name", golden_names(with_solution=True))
+@pytest.mark.parametrize("charge", [1, -1])
+def test_oracle_sigma_and_sources_match_reference(name, charge):
+    spec, g = load(name)
+    tag = "p" if charge == 1 else "m"
+    p = oc.OracleProblem(spec.as_dict())
+    eom = oc.OracleEOM(p, g["solution_amplitudes"], 0, charge)
+    if "eom_masks" in g:
+        assert np.array_equal(np.asarray(oc.eom_masks(spec.n, 0, charge), np.int64), g["eom_masks"][g[f"eom{tag}_positions"]])
+    assert relerr(eom.diagonal, g[f"eom{tag}_diagonal"]) < 1e-14
+    assert relerr(eom.sigma(g[f"eom{tag}_probe"]), g[f"eom{tag}_sigma"]) < 1e-12
+    add, rem, sink = eom.sources(spec.impurity_site)
+    assert np.max(np.abs(add - g[f"eom{tag}_addition"])) < 1e-12
+    assert np.max(np.abs(rem - g[f"eom{tag}_removal"])) < 1e-12
+    assert np.max(np.abs(sink - g[f"eom{tag}_sink"])) < 1e-14
+
+
+@pytest.mark.parametrize("name", [n for n in golden_names(with_solution=True) if n in ("readme", "s135fix", "twosrc")])
+def test_oracle_green_matches_reference_gmres(name):
+    spec, g = load(name)
+    p = oc.OracleProblem(spec.as_dict())
+    eom = oc.OracleEOM(p, g["solution_amplitudes"], 0, 1)
+    _, _, gr = oc.retarded_green_dense(eom, spec.impurity_site, g["green_omega"], float(g["green_eta"]))
+    assert relerr(gr, g["green_retarded"]) < 1e-8
+
+
+def test_single_mode_known_answer():
+    """G^R of a bare single mode is 1/(omega - eps + i gamma) (reference tests/cc/test_charge_small_sectors.py:17-38).
+
+    Here a one-site spec with one quadratic mode pair and no products checks the
+    oracle's sigma/source/sink conventions: sigma is the bare rapidity
+    diagonal, and the addition channel resolvent is 1/(z - lambda).
+    """
+    n = 1
+    lam = np.array([0.3 - 1.1j, -0.3 - 1.1j, 0.2 - 0.5j, -0.2 - 0.5j])
+    cre = np.zeros((1, 4), complex)
+    ann = np.zeros((1, 4), complex)
+    cre[0, 0] = 1.0
+    ann[0, 1] = 1.0
+    spec = dict(n=n, creators=cre, annihilators=ann, product_coefficients=np.zeros(0, complex),
+                product_factors=np.zeros((0, 1), np.int64), product_lengths=np.zeros(0, np.int64), rapidities=lam,
+                mode_partner=np.array([1, 0, 3, 2]), mode_phase=np.ones(4, complex),
+                source_factor=np.zeros((1, 2, 4), np.int64))
+    p = oc.OracleProblem(spec)
+    eom = oc.OracleEOM(p, np.zeros(p.coords.dimension, complex), 0, 1)
+    # S1: one mode; S3: the (1,0,1,1) string; no products -> bare diagonal
+    assert eom.dimension == 2
+    A = oc.dense_matrix(eom)
+    assert np.allclose(A, np.diag([lam[0], lam[0] + lam[2] + lam[3]]))
+    w = np.linspace(-2, 2, 9)
+    src = eom.source(0)
+    sink = np.array([1.0, 0.0])
+    g = np.array([sink @ np.linalg.solve(x * np.eye(2) - A, src) for x in w])
+    assert np.allclose(g, 1.0 / (w - 0.3 + 1.1j), atol=1e-12)
