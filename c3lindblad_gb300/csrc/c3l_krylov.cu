@@ -13,6 +13,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <mutex>
+
 #include "c3l_gb300.h"
 
 namespace {
@@ -353,6 +355,34 @@ __global__ void k_hessenberg_coordinates(const double2* __restrict__ H, int64_t 
     for (int c = threadIdx.x; c < m; c += blockDim.x) Y[(int64_t)blockIdx.x * m + c] = rr[c];
 }
 
+// Fixed scratch for c3l_hessenberg_coordinates_noalloc: the packed R factors
+// of the shifted solves live here instead of in caller-provided memory.  The
+// array is part of the library's device image, so every GPU that loads the
+// library holds these C3L_NOALLOC_SCRATCH_ENTRIES complex entries until the
+// process exits.
+static __device__ __align__(256) double2 g_noalloc_scratch[C3L_NOALLOC_SCRATCH_ENTRIES];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+void* g_noalloc_ptr[kMaxDevices] = {};
+
+// Device address of g_noalloc_scratch on the current device.  In host code the
+// array's name is only a host-side stand-in, so the address is looked up once
+// per device (with that device current) and cached.
+c3l_status noalloc_scratch(double2** out) {
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess) return C3L_ERR_LAUNCH;
+    if (dev < 0 || dev >= kMaxDevices) return C3L_ERR_CAPACITY;
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_ptr[dev]) {
+        void* p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return C3L_ERR_LAUNCH;
+        g_noalloc_ptr[dev] = p;
+    }
+    *out = static_cast<double2*>(g_noalloc_ptr[dev]);
+    return C3L_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -464,6 +494,33 @@ c3l_status c3l_hessenberg_coordinates(const c3l_complex* H, int64_t ldh, int32_t
         reinterpret_cast<const double2*>(H), ldh, m, reinterpret_cast<const double2*>(shifts), beta,
         reinterpret_cast<double2*>(rscratch), reinterpret_cast<double2*>(Y));
     return launch_status();
+}
+
+c3l_status c3l_hessenberg_coordinates_noalloc(const c3l_complex* H, int64_t ldh, int32_t m, const c3l_complex* shifts,
+                                              int32_t nshift, double beta, c3l_complex* Y, void* stream) {
+    if (m <= 0 || nshift < 0 || !H || !shifts || !Y || ldh < m || !(beta > 0.0)) return C3L_ERR_ARGUMENT;
+    if (m > C3L_MAX_HESSENBERG) return C3L_ERR_CAPACITY;
+    const int64_t per = (int64_t)m * (m + 1) / 2;
+    if (per > (int64_t)C3L_NOALLOC_SCRATCH_ENTRIES) return C3L_ERR_CAPACITY;
+    if (nshift == 0) return C3L_OK;
+    double2* scratch = nullptr;
+    c3l_status st = noalloc_scratch(&scratch);
+    if (st) return st;
+    const size_t smem = 2 * (size_t)m * sizeof(double2);
+    if (set_smem((const void*)k_hessenberg_coordinates, smem)) return C3L_ERR_LAUNCH;
+    // shifts are processed in chunks that fit the fixed scratch; chunks run
+    // back to back on the caller's stream, so they reuse it in order
+    const int32_t chunk = (int32_t)((int64_t)C3L_NOALLOC_SCRATCH_ENTRIES / per < nshift
+                                        ? (int64_t)C3L_NOALLOC_SCRATCH_ENTRIES / per
+                                        : nshift);
+    for (int32_t s0 = 0; s0 < nshift; s0 += chunk) {
+        const int32_t cnt = nshift - s0 < chunk ? nshift - s0 : chunk;
+        k_hessenberg_coordinates<<<(unsigned)cnt, kThreads, smem, as_stream(stream)>>>(
+            reinterpret_cast<const double2*>(H), ldh, m, reinterpret_cast<const double2*>(shifts) + s0, beta, scratch,
+            reinterpret_cast<double2*>(Y) + (int64_t)s0 * m);
+        if (cudaGetLastError() != cudaSuccess) return C3L_ERR_LAUNCH;
+    }
+    return C3L_OK;
 }
 
 }  // extern "C"

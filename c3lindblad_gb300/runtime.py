@@ -59,7 +59,7 @@ EXPORTS = (
     "c3l_wedge_eom_out", "c3l_wedge_source_out", "c3l_action_prepare", "c3l_static_apply", "c3l_eom_sigma",
     "c3l_multi_dot_scratch", "c3l_multi_dot_c", "c3l_multi_dot_r", "c3l_multi_axpy_c", "c3l_multi_axpy_r",
     "c3l_scale_c", "c3l_scale_r", "c3l_precondition", "c3l_hessenberg_shifted", "c3l_hessenberg_coordinates",
-    "c3l_version",
+    "c3l_hessenberg_coordinates_noalloc", "c3l_version",
 )
 
 
@@ -85,6 +85,7 @@ def _declare(lib) -> None:
         "c3l_precondition": [I64, P, P, P, P, P, P],
         "c3l_hessenberg_shifted": [P, I64, I32, P, I32, D, P, P, P, P],
         "c3l_hessenberg_coordinates": [P, I64, I32, P, I32, D, P, P, P],
+        "c3l_hessenberg_coordinates_noalloc": [P, I64, I32, P, I32, D, P, P],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)

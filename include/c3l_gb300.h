@@ -234,6 +234,28 @@ c3l_status c3l_hessenberg_coordinates(const c3l_complex* H, int64_t ldh, int32_t
                                       int32_t nshift, double beta, c3l_complex* rscratch, c3l_complex* Y,
                                       void* stream);
 
+/* Allocation-free variant of c3l_hessenberg_coordinates, for callers that
+ * cannot allocate device memory: a host application that owns the device
+ * memory budget (and hands this library only its input and output buffers),
+ * or a caller that must not allocate between setup and shutdown.  It has no
+ * counterpart in the reference, whose reduced solves run on the host.
+ *
+ * The R-factor scratch is a fixed array inside the library's device image of
+ * C3L_NOALLOC_SCRATCH_ENTRIES complex entries (32 MiB), held on every GPU that
+ * loads the library until the process exits.  One shift needs m*(m+1)/2
+ * entries; m*(m+1)/2 > C3L_NOALLOC_SCRATCH_ENTRIES (m >= 2048) is rejected with
+ * C3L_ERR_CAPACITY.  Larger shift counts are processed in chunks on `stream`.
+ *
+ * The first call on each device looks up the array's device address (with
+ * that device current) and caches it; make that first call before any stream
+ * capture.  Every call shares the one array and leaves its contents behind;
+ * each call writes every scratch entry it reads, so nothing has to start at
+ * zero.  Calls that overlap on the GPU (other streams, other host threads)
+ * race on the array: serialize them.  No cudaMalloc or cudaFree is called. */
+#define C3L_NOALLOC_SCRATCH_ENTRIES (1 << 21)
+c3l_status c3l_hessenberg_coordinates_noalloc(const c3l_complex* H, int64_t ldh, int32_t m, const c3l_complex* shifts,
+                                              int32_t nshift, double beta, c3l_complex* Y, void* stream);
+
 /* Library identification (host only). */
 const char* c3l_version(void);
 
