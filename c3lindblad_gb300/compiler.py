@@ -50,7 +50,8 @@ from .layout import Coordinates
 
 MAX_FACTORS = 6
 MAX_SOURCES = 4
-TILE = 256
+TILE = 256        # outputs per contraction tile (one thread each)
+WEDGE_TILE = 64   # outputs per wedge tile (instances split over 4 thread groups)
 
 CONTRACT_DTYPE = np.dtype([
     ("dst_off", np.int64), ("deg", np.int32), ("nsrc", np.int32),
@@ -439,8 +440,8 @@ class Builder:
         if kind == "padded":
             for b, (out_off, deg, rows) in enumerate(block_rows):
                 size = self.n ** deg
-                for s in range(0, size, TILE):
-                    tiles.append((b, min(TILE, size - s), s))
+                for s in range(0, size, WEDGE_TILE):
+                    tiles.append((b, min(WEDGE_TILE, size - s), s))
         else:
             eb = np.asarray(element_block)
             order_ok = np.all(np.diff(eb) >= 0)
@@ -450,8 +451,8 @@ class Builder:
                 if idx.size == 0:
                     continue
                 lo, hi = int(idx[0]), int(idx[-1]) + 1
-                for s in range(lo, hi, TILE):
-                    tiles.append((b, min(TILE, hi - s), s))
+                for s in range(lo, hi, WEDGE_TILE):
+                    tiles.append((b, min(WEDGE_TILE, hi - s), s))
         tarr = np.zeros(len(tiles), TILE_DTYPE)
         for i, (b, c, s) in enumerate(tiles):
             tarr[i] = (b, c, s)

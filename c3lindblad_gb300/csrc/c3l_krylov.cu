@@ -21,6 +21,7 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr int kMaxPartial = 256;
+constexpr int kHessThreads = 128;
 
 inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 inline c3l_status launch_status() { return cudaGetLastError() == cudaSuccess ? C3L_OK : C3L_ERR_LAUNCH; }
@@ -125,26 +126,59 @@ __global__ void k_dot_final_r(const double* __restrict__ partial, int nb, double
     if (threadIdx.x == 0) out[j] = s;
 }
 
-__global__ void k_axpy_c(const double2* __restrict__ V, int64_t ld, int k, const double2* __restrict__ c, double2 alpha,
-                         double2* __restrict__ w, int64_t dim) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < dim; i += (int64_t)gridDim.x * blockDim.x) {
+// w[i] += alpha * sum_j c[j] V[j, i]: a 32 x 8 block covers 32 consecutive
+// entries (coalesced in i) and splits the k rows over 8 thread rows, so a
+// short vector with a long basis (Arnoldi) still fills the GPU.
+constexpr int kAxX = 32, kAxY = 8;
+
+__global__ void __launch_bounds__(kAxX * kAxY) k_axpy_c(const double2* __restrict__ V, int64_t ld, int k,
+                                                         const double2* __restrict__ c, double2 alpha,
+                                                         double2* __restrict__ w, int64_t dim) {
+    __shared__ double2 part[kAxY][kAxX];
+    for (int64_t base = (int64_t)blockIdx.x * kAxX; base < dim; base += (int64_t)gridDim.x * kAxX) {
+        const int64_t i = base + threadIdx.x;
         double2 s = make_double2(0.0, 0.0);
-        for (int j = 0; j < k; ++j) {
-            const double2 p = cmul(c[j], V[(int64_t)j * ld + i]);
-            s.x += p.x;
-            s.y += p.y;
+        if (i < dim) {
+            for (int j = threadIdx.y; j < k; j += kAxY) {
+                const double2 p = cmul(c[j], V[(int64_t)j * ld + i]);
+                s.x += p.x;
+                s.y += p.y;
+            }
         }
-        const double2 a = cmul(alpha, s);
-        w[i] = make_double2(w[i].x + a.x, w[i].y + a.y);
+        part[threadIdx.y][threadIdx.x] = s;
+        __syncthreads();
+        if (threadIdx.y == 0 && i < dim) {
+            double2 t = part[0][threadIdx.x];
+#pragma unroll
+            for (int y = 1; y < kAxY; ++y) {
+                t.x += part[y][threadIdx.x].x;
+                t.y += part[y][threadIdx.x].y;
+            }
+            const double2 a = cmul(alpha, t);
+            w[i] = make_double2(w[i].x + a.x, w[i].y + a.y);
+        }
+        __syncthreads();
     }
 }
 
-__global__ void k_axpy_r(const double* __restrict__ V, int64_t ld, int k, const double* __restrict__ c, double alpha,
-                         double* __restrict__ w, int64_t dim) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < dim; i += (int64_t)gridDim.x * blockDim.x) {
+__global__ void __launch_bounds__(kAxX * kAxY) k_axpy_r(const double* __restrict__ V, int64_t ld, int k,
+                                                         const double* __restrict__ c, double alpha,
+                                                         double* __restrict__ w, int64_t dim) {
+    __shared__ double part[kAxY][kAxX];
+    for (int64_t base = (int64_t)blockIdx.x * kAxX; base < dim; base += (int64_t)gridDim.x * kAxX) {
+        const int64_t i = base + threadIdx.x;
         double s = 0.0;
-        for (int j = 0; j < k; ++j) s = fma(c[j], V[(int64_t)j * ld + i], s);
-        w[i] = fma(alpha, s, w[i]);
+        if (i < dim)
+            for (int j = threadIdx.y; j < k; j += kAxY) s = fma(c[j], V[(int64_t)j * ld + i], s);
+        part[threadIdx.y][threadIdx.x] = s;
+        __syncthreads();
+        if (threadIdx.y == 0 && i < dim) {
+            double t = part[0][threadIdx.x];
+#pragma unroll
+            for (int y = 1; y < kAxY; ++y) t += part[y][threadIdx.x];
+            w[i] = fma(alpha, t, w[i]);
+        }
+        __syncthreads();
     }
 }
 
@@ -171,6 +205,12 @@ __global__ void k_precondition(int64_t nrep, const double* __restrict__ m4, cons
             y[c] = m[0] * x[c];
         }
     }
+}
+
+unsigned axpy_grid(int64_t dim) {
+    int64_t b = (dim + kAxX - 1) / kAxX;
+    if (b > 8192) b = 8192;
+    return (unsigned)(b < 1 ? 1 : b);
 }
 
 unsigned grid_for(int64_t count) {
@@ -212,10 +252,15 @@ __device__ __forceinline__ void givens(double2 a, double2 b, double& c, double2&
 
 // Streamed Givens QR of (z I - H_m) with the transposed forward solve
 // u = R^{-T} p, so that green = p^T y = sum_k u_k (Q^H beta e1)_k without
-// storing R.  Shared memory: w[m] (current working row), acc[m].
-__global__ void k_hessenberg_shifted(const double2* __restrict__ H, int64_t ldh, int m, const double2* __restrict__ shifts,
-                                     double beta, const double2* __restrict__ sinkproj, double2* __restrict__ green,
-                                     double* __restrict__ residual) {
+// storing R.  Shared memory: w[m] (current working row), acc[m].  Thread 0
+// alone forms each rotation (FP64 is a narrow pipe on this part: the
+// rotation is computed once per step, not once per thread); all threads then
+// update the remaining columns.
+__global__ void __launch_bounds__(kHessThreads) k_hessenberg_shifted(const double2* __restrict__ H, int64_t ldh, int m,
+                                                                     const double2* __restrict__ shifts, double beta,
+                                                                     const double2* __restrict__ sinkproj,
+                                                                     double2* __restrict__ green,
+                                                                     double* __restrict__ residual) {
     extern __shared__ double2 dyn[];
     double2* w = dyn;
     double2* acc = dyn + m;
@@ -226,43 +271,41 @@ __global__ void k_hessenberg_shifted(const double2* __restrict__ H, int64_t ldh,
         w[c] = a_entry(H, ldh, 0, c, z);
         acc[c] = make_double2(0.0, 0.0);
     }
-    double2 rhs_w = make_double2(beta, 0.0);  // tracked by every thread identically
+    // thread-0 state
+    double2 rhs_w = make_double2(beta, 0.0);
     double2 G = make_double2(0.0, 0.0);
     double2 ylast = make_double2(0.0, 0.0);
     __syncthreads();
     for (int k = 0; k < m; ++k) {
-        double c;
-        double2 s, rkk;
-        if (k < m - 1) {
-            givens(w[k], a_entry(H, ldh, k + 1, k, z), c, s, rkk);
-        } else {
-            c = 1.0;
-            s = make_double2(0.0, 0.0);
-            rkk = w[k];
-        }
-        const double2 rrhs = make_double2(c * rhs_w.x, c * rhs_w.y);
-        // new rhs of the working row: -conj(s) * rhs_w  (the next row's rhs is 0)
-        rhs_w = cmul(make_double2(-s.x, s.y), rhs_w);
         if (threadIdx.x == 0) {
-            rot_c = c;
-            rot_s = s;
+            double c;
+            double2 s, rkk;
+            if (k < m - 1) {
+                givens(w[k], a_entry(H, ldh, k + 1, k, z), c, s, rkk);
+            } else {
+                c = 1.0;
+                s = make_double2(0.0, 0.0);
+                rkk = w[k];
+            }
+            const double2 rrhs = make_double2(c * rhs_w.x, c * rhs_w.y);
+            rhs_w = cmul(make_double2(-s.x, s.y), rhs_w);  // -conj(s) * rhs_w (the next row's rhs is 0)
             double2 u = make_double2(0.0, 0.0);
             if (sinkproj) {
                 const double2 p = sinkproj[k];
                 u = cdiv(make_double2(p.x - acc[k].x, p.y - acc[k].y), rkk);
+                const double2 gu = cmul(u, rrhs);
+                G.x += gu.x;
+                G.y += gu.y;
             }
+            if (k == m - 1) ylast = cdiv(rrhs, rkk);
+            rot_c = c;
+            rot_s = s;
             u_k = u;
         }
         __syncthreads();
-        const double2 u = u_k;
-        if (sinkproj) {
-            const double2 gu = cmul(u, rrhs);
-            G.x += gu.x;
-            G.y += gu.y;
-        }
-        if (k == m - 1) ylast = cdiv(rrhs, rkk);
         const double cc = rot_c;
         const double2 ss = rot_s;
+        const double2 u = u_k;
         const double2 mcs = make_double2(-ss.x, ss.y);  // -conj(s)
         for (int col = k + 1 + threadIdx.x; col < m; col += blockDim.x) {
             const double2 rv = (k < m - 1) ? a_entry(H, ldh, k + 1, col, z) : make_double2(0.0, 0.0);
@@ -288,10 +331,93 @@ __global__ void k_hessenberg_shifted(const double2* __restrict__ H, int64_t ldh,
     }
 }
 
+// FP32 residual-only variant used for Arnoldi convergence checks: the same
+// streamed Givens elimination on (z I - H_m) rounded to single precision,
+// returning |h_{m,m-1} y_{m-1}| / beta.  Its relative error is ~cond * 1e-7,
+// ample for a stopping decision; a positive decision is confirmed in FP64.
+__global__ void __launch_bounds__(kHessThreads) k_hessenberg_residual_f32(const double2* __restrict__ H, int64_t ldh,
+                                                                          int m, const double2* __restrict__ shifts,
+                                                                          double beta, double* __restrict__ residual) {
+    extern __shared__ float2 dynf[];
+    float2* w = dynf;
+    __shared__ float rot_c;
+    __shared__ float2 rot_s;
+    const double2 zd = shifts[blockIdx.x];
+    const float2 z = make_float2((float)zd.x, (float)zd.y);
+    auto entry = [&](int row, int c) -> float2 {
+        const double2 h = H[(int64_t)row * ldh + c];
+        return (row == c) ? make_float2(z.x - (float)h.x, z.y - (float)h.y) : make_float2((float)-h.x, (float)-h.y);
+    };
+    for (int c = threadIdx.x; c < m; c += blockDim.x) w[c] = entry(0, c);
+    float2 rhs = make_float2((float)beta, 0.0f);
+    float2 ylast = make_float2(0.0f, 0.0f);
+    // the running rhs is a product of sines and may fall below FP32 range:
+    // keep it rescaled by powers of 1e20 and track the decimal exponent
+    int rhs_exp = 0;
+    int y_exp = 0;
+    __syncthreads();
+    for (int k = 0; k < m; ++k) {
+        if (threadIdx.x == 0) {
+            const float2 a = w[k];
+            float c;
+            float2 sn, rkk;
+            if (k < m - 1) {
+                const float2 b = entry(k + 1, k);
+                const float na = hypotf(a.x, a.y), nb = hypotf(b.x, b.y);
+                if (nb == 0.0f) {
+                    c = 1.0f; sn = make_float2(0.0f, 0.0f); rkk = a;
+                } else if (na == 0.0f) {
+                    c = 0.0f; sn = make_float2(1.0f, 0.0f); rkk = b;
+                } else {
+                    const float rho = hypotf(na, nb);
+                    c = na / rho;
+                    const float2 ph = make_float2(a.x / na, a.y / na);
+                    const float2 bb = make_float2(b.x / rho, -b.y / rho);
+                    sn = make_float2(ph.x * bb.x - ph.y * bb.y, ph.x * bb.y + ph.y * bb.x);
+                    rkk = make_float2(ph.x * rho, ph.y * rho);
+                }
+            } else {
+                c = 1.0f; sn = make_float2(0.0f, 0.0f); rkk = a;
+            }
+            const float2 rrhs = make_float2(c * rhs.x, c * rhs.y);
+            if (k == m - 1) {
+                const float d = rkk.x * rkk.x + rkk.y * rkk.y;
+                ylast = make_float2((rrhs.x * rkk.x + rrhs.y * rkk.y) / d, (rrhs.y * rkk.x - rrhs.x * rkk.y) / d);
+                y_exp = rhs_exp;
+            }
+            rhs = make_float2(-sn.x * rhs.x - sn.y * rhs.y, -sn.x * rhs.y + sn.y * rhs.x);  // -conj(s) rhs
+            const float mag = fmaxf(fabsf(rhs.x), fabsf(rhs.y));
+            if (mag != 0.0f && mag < 1e-20f) {
+                rhs.x *= 1e20f;
+                rhs.y *= 1e20f;
+                rhs_exp -= 20;
+            }
+            rot_c = c;
+            rot_s = sn;
+        }
+        __syncthreads();
+        const float cc = rot_c;
+        const float2 ss = rot_s;
+        for (int col = k + 1 + threadIdx.x; col < m; col += blockDim.x) {
+            const float2 rv = (k < m - 1) ? entry(k + 1, col) : make_float2(0.0f, 0.0f);
+            const float2 wv = w[col];
+            // w' = -conj(s) w + c r
+            w[col] = make_float2(-ss.x * wv.x - ss.y * wv.y + cc * rv.x, -ss.x * wv.y + ss.y * wv.x + cc * rv.y);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const double2 hs = H[(int64_t)m * ldh + (m - 1)];
+        residual[blockIdx.x] = hypot(hs.x, hs.y) * hypot((double)ylast.x, (double)ylast.y) * pow(10.0, (double)y_exp) / beta;
+    }
+}
+
 // Same elimination storing R (packed rows) in caller scratch, then back
 // substitution for the full reduced coordinates y.
-__global__ void k_hessenberg_coordinates(const double2* __restrict__ H, int64_t ldh, int m, const double2* __restrict__ shifts,
-                                         double beta, double2* __restrict__ rscratch, double2* __restrict__ Y) {
+__global__ void __launch_bounds__(kHessThreads) k_hessenberg_coordinates(const double2* __restrict__ H, int64_t ldh, int m,
+                                                                         const double2* __restrict__ shifts, double beta,
+                                                                         double2* __restrict__ rscratch,
+                                                                         double2* __restrict__ Y) {
     extern __shared__ double2 dyn[];
     double2* w = dyn;        // working row
     double2* rr = dyn + m;   // R rhs, then y
@@ -304,23 +430,23 @@ __global__ void k_hessenberg_coordinates(const double2* __restrict__ H, int64_t 
     double2 rhs_w = make_double2(beta, 0.0);
     __syncthreads();
     for (int k = 0; k < m; ++k) {
-        double c;
-        double2 s, rkk;
-        if (k < m - 1) {
-            givens(w[k], a_entry(H, ldh, k + 1, k, z), c, s, rkk);
-        } else {
-            c = 1.0;
-            s = make_double2(0.0, 0.0);
-            rkk = w[k];
-        }
         const int64_t row = (int64_t)k * m - (int64_t)k * (k - 1) / 2;  // packed row start (length m-k)
         if (threadIdx.x == 0) {
+            double c;
+            double2 s, rkk;
+            if (k < m - 1) {
+                givens(w[k], a_entry(H, ldh, k + 1, k, z), c, s, rkk);
+            } else {
+                c = 1.0;
+                s = make_double2(0.0, 0.0);
+                rkk = w[k];
+            }
             rot_c = c;
             rot_s = s;
             R[row] = rkk;
             rr[k] = make_double2(c * rhs_w.x, c * rhs_w.y);
+            rhs_w = cmul(make_double2(-s.x, s.y), rhs_w);
         }
-        rhs_w = cmul(make_double2(-s.x, s.y), rhs_w);
         __syncthreads();
         const double cc = rot_c;
         const double2 ss = rot_s;
@@ -353,6 +479,35 @@ __global__ void k_hessenberg_coordinates(const double2* __restrict__ H, int64_t 
         __syncthreads();
     }
     for (int c = threadIdx.x; c < m; c += blockDim.x) Y[(int64_t)blockIdx.x * m + c] = rr[c];
+}
+
+// One Arnoldi column on the device: H[:k, j] = c1 + c2, h = |w'' | from
+// |w'|^2 - |c2|^2, H[k, j] = h (column-major Hc, ld = ldc), then w /= h
+// unless h <= tol (breakdown: w is left as is and detected by the host).
+// coeff: [c1 (k) | c2 (k) | |w'|^2].
+__global__ void k_arnoldi_column(const double2* __restrict__ coeff, int k, double2* __restrict__ w, int64_t n,
+                                 double2* __restrict__ Hc, int64_t ldc, int j, double tol) {
+    __shared__ double red[32];
+    double s = 0.0;
+    for (int i = threadIdx.x; i < k; i += blockDim.x) {
+        const double2 c2 = coeff[k + i];
+        s += c2.x * c2.x + c2.y * c2.y;
+    }
+    s = block_sum(s, red);
+    __shared__ double h_sh;
+    if (threadIdx.x == 0) h_sh = sqrt(fmax(coeff[2 * k].x - s, 0.0));
+    __syncthreads();
+    const double h = h_sh;
+    if (blockIdx.x == 0) {
+        double2* col = Hc + (int64_t)j * ldc;
+        for (int i = threadIdx.x; i < k; i += blockDim.x)
+            col[i] = make_double2(coeff[i].x + coeff[k + i].x, coeff[i].y + coeff[k + i].y);
+        if (threadIdx.x == 0) col[k] = make_double2(h, 0.0);
+    }
+    if (!(h > tol)) return;
+    const double inv = 1.0 / h;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        w[i] = make_double2(w[i].x * inv, w[i].y * inv);
 }
 
 // Fixed scratch for c3l_hessenberg_coordinates_noalloc: the packed R factors
@@ -421,7 +576,7 @@ c3l_status c3l_multi_axpy_c(const c3l_complex* V, int64_t ld, int32_t k, const c
     if (k < 0 || dim < 0) return C3L_ERR_ARGUMENT;
     if (k == 0 || dim == 0) return C3L_OK;
     if (!V || !c || !w || ld < dim) return C3L_ERR_ARGUMENT;
-    k_axpy_c<<<grid_for(dim), kThreads, 0, as_stream(stream)>>>(reinterpret_cast<const double2*>(V), ld, k,
+    k_axpy_c<<<axpy_grid(dim), dim3(kAxX, kAxY), 0, as_stream(stream)>>>(reinterpret_cast<const double2*>(V), ld, k,
                                                                 reinterpret_cast<const double2*>(c),
                                                                 make_double2(alpha.re, alpha.im),
                                                                 reinterpret_cast<double2*>(w), dim);
@@ -433,7 +588,7 @@ c3l_status c3l_multi_axpy_r(const double* V, int64_t ld, int32_t k, const double
     if (k < 0 || dim < 0) return C3L_ERR_ARGUMENT;
     if (k == 0 || dim == 0) return C3L_OK;
     if (!V || !c || !w || ld < dim) return C3L_ERR_ARGUMENT;
-    k_axpy_r<<<grid_for(dim), kThreads, 0, as_stream(stream)>>>(V, ld, k, c, alpha, w, dim);
+    k_axpy_r<<<axpy_grid(dim), dim3(kAxX, kAxY), 0, as_stream(stream)>>>(V, ld, k, c, alpha, w, dim);
     return launch_status();
 }
 
@@ -477,7 +632,7 @@ c3l_status c3l_hessenberg_shifted(const c3l_complex* H, int64_t ldh, int32_t m, 
     if (nshift == 0) return C3L_OK;
     const size_t smem = 2 * (size_t)m * sizeof(double2);
     if (set_smem((const void*)k_hessenberg_shifted, smem)) return C3L_ERR_LAUNCH;
-    k_hessenberg_shifted<<<(unsigned)nshift, kThreads, smem, as_stream(stream)>>>(
+    k_hessenberg_shifted<<<(unsigned)nshift, kHessThreads, smem, as_stream(stream)>>>(
         reinterpret_cast<const double2*>(H), ldh, m, reinterpret_cast<const double2*>(shifts), beta,
         reinterpret_cast<const double2*>(sinkproj), reinterpret_cast<double2*>(green), residual);
     return launch_status();
@@ -490,7 +645,7 @@ c3l_status c3l_hessenberg_coordinates(const c3l_complex* H, int64_t ldh, int32_t
     if (nshift == 0) return C3L_OK;
     const size_t smem = 2 * (size_t)m * sizeof(double2);
     if (set_smem((const void*)k_hessenberg_coordinates, smem)) return C3L_ERR_LAUNCH;
-    k_hessenberg_coordinates<<<(unsigned)nshift, kThreads, smem, as_stream(stream)>>>(
+    k_hessenberg_coordinates<<<(unsigned)nshift, kHessThreads, smem, as_stream(stream)>>>(
         reinterpret_cast<const double2*>(H), ldh, m, reinterpret_cast<const double2*>(shifts), beta,
         reinterpret_cast<double2*>(rscratch), reinterpret_cast<double2*>(Y));
     return launch_status();
@@ -515,12 +670,35 @@ c3l_status c3l_hessenberg_coordinates_noalloc(const c3l_complex* H, int64_t ldh,
                                         : nshift);
     for (int32_t s0 = 0; s0 < nshift; s0 += chunk) {
         const int32_t cnt = nshift - s0 < chunk ? nshift - s0 : chunk;
-        k_hessenberg_coordinates<<<(unsigned)cnt, kThreads, smem, as_stream(stream)>>>(
+        k_hessenberg_coordinates<<<(unsigned)cnt, kHessThreads, smem, as_stream(stream)>>>(
             reinterpret_cast<const double2*>(H), ldh, m, reinterpret_cast<const double2*>(shifts) + s0, beta, scratch,
             reinterpret_cast<double2*>(Y) + (int64_t)s0 * m);
         if (cudaGetLastError() != cudaSuccess) return C3L_ERR_LAUNCH;
     }
     return C3L_OK;
+}
+
+c3l_status c3l_hessenberg_residual_f32(const c3l_complex* H, int64_t ldh, int32_t m, const c3l_complex* shifts,
+                                       int32_t nshift, double beta, double* residual, void* stream) {
+    if (m <= 0 || nshift < 0 || !H || !shifts || !residual || ldh < m || !(beta > 0.0)) return C3L_ERR_ARGUMENT;
+    if (m > C3L_MAX_HESSENBERG) return C3L_ERR_CAPACITY;
+    if (nshift == 0) return C3L_OK;
+    const size_t smem = (size_t)m * sizeof(float2);
+    if (set_smem((const void*)k_hessenberg_residual_f32, smem)) return C3L_ERR_LAUNCH;
+    k_hessenberg_residual_f32<<<(unsigned)nshift, kHessThreads, smem, as_stream(stream)>>>(
+        reinterpret_cast<const double2*>(H), ldh, m, reinterpret_cast<const double2*>(shifts), beta, residual);
+    return launch_status();
+}
+
+c3l_status c3l_arnoldi_column(const c3l_complex* coeff, int32_t k, c3l_complex* w, int64_t n, c3l_complex* Hc, int64_t ldc,
+                              int32_t j, double tol, void* stream) {
+    if (!coeff || !w || !Hc || k <= 0 || n <= 0 || ldc < k + 1 || j < 0) return C3L_ERR_ARGUMENT;
+    int64_t blocks = (n + kThreads - 1) / kThreads;
+    if (blocks > 1024) blocks = 1024;
+    k_arnoldi_column<<<(unsigned)blocks, kThreads, 0, as_stream(stream)>>>(
+        reinterpret_cast<const double2*>(coeff), k, reinterpret_cast<double2*>(w), n, reinterpret_cast<double2*>(Hc), ldc,
+        j, tol);
+    return launch_status();
 }
 
 }  // extern "C"

@@ -110,13 +110,22 @@ struct Epilogue {
     double2 cscale;
 };
 
+// One block = one tile of up to kWE outputs of one output block; the block's
+// instances are split over kWG thread groups (instance i goes to group
+// i % kWG) and the groups' partial sums are added in shared memory.
+constexpr int kWE = 64;
+constexpr int kWG = kThreads / kWE;
+
 template <int MODE>
 __global__ void __launch_bounds__(kThreads) k_wedge(c3l_wedge_stage st, int n, double2* ws, Epilogue ep) {
     __shared__ c3l_instance sinst[kInstChunk];
+    __shared__ double2 red[kWG][kWE];
     const c3l_tile tile = st.tiles[blockIdx.x];
     const c3l_block blk = st.blocks[tile.block];
-    const bool active = (int)threadIdx.x < tile.count;
-    const int64_t e = tile.start + threadIdx.x;
+    const int ex = threadIdx.x % kWE;
+    const int gy = threadIdx.x / kWE;
+    const bool active = ex < tile.count;
+    const int64_t e = tile.start + ex;
     int64_t pw[6];
     powers(n, pw);
     int dig[4] = {0, 0, 0, 0};
@@ -147,7 +156,7 @@ __global__ void __launch_bounds__(kThreads) k_wedge(c3l_wedge_stage st, int n, d
         }
         __syncthreads();
         if (active) {
-            for (int i = 0; i < cnt; ++i) {
+            for (int i = gy; i < cnt; i += kWG) {
                 const c3l_instance& in = sinst[i];
                 double2 v = make_double2(in.coef[0], in.coef[1]);
                 for (int j = 0; j < in.nfac; ++j) {
@@ -160,7 +169,11 @@ __global__ void __launch_bounds__(kThreads) k_wedge(c3l_wedge_stage st, int n, d
             }
         }
     }
-    if (!active) return;
+    red[gy][ex] = acc;
+    __syncthreads();
+    if (!active || gy != 0) return;
+#pragma unroll
+    for (int g = 1; g < kWG; ++g) acc = cadd(acc, red[g][ex]);
     if (MODE == kPadded) {
         ws[blk.out_off + e] = acc;
     } else if (MODE == kStatic) {

@@ -159,19 +159,33 @@ class DeviceEOM:
         up = rt.Uploader(self.device)
         self._up = up
         self.N = plan.dimension
-        self.ws = _cz(prog.ws_size, self.device)
-        vec = up.raw(prog.vectors)
-        self.ctx_action = rt.build_action(up, prog, vec.data_ptr(), self.ws, "T", ["sigma_rest_T"], None, plan.scatter_T)
-        ea = rt.EomAction()
-        ea.action = rt.build_action(up, prog, vec.data_ptr(), self.ws, "X", ["sigma_rest_X"], "sigma", plan.scatter_X)
-        ea.lam = up.ptr(plan.lam_sigma)
-        self.sigma_action = ea
-        self.sigma_launches = rt.action_launches(ea.action)
+        self.vec = up.raw(prog.vectors)
+        self.lam = up.raw(plan.lam_sigma)
         self.amplitudes = amplitudes.to(self.device, torch.complex128).contiguous()
-        rt.check(self.lib.c3l_action_prepare(C.byref(self.ctx_action), self.amplitudes.data_ptr(),
-                                             rt.stream_ptr(self.device)), "EOM context")
-        rt.LaunchCounter.add(rt.action_launches(self.ctx_action))
+        self.workspaces: list = []
+        self.sigma_actions: list = []
+        self.ensure_channels(1)
+        self.ws = self.workspaces[0]
+        self.sigma_action = self.sigma_actions[0]
+        self.sigma_launches = rt.action_launches(self.sigma_action.action)
         self.diagonal = torch.from_numpy(plan.diagonal.copy()).to(self.device)
+
+    def ensure_channels(self, count: int) -> None:
+        """One workspace (amplitude part prepared) per concurrently used channel."""
+        prog = self.plan.program
+        up = self._up
+        while len(self.workspaces) < count:
+            ws = _cz(prog.ws_size, self.device)
+            ctx = rt.build_action(up, prog, self.vec.data_ptr(), ws, "T", ["sigma_rest_T"], None, self.plan.scatter_T)
+            rt.check(self.lib.c3l_action_prepare(C.byref(ctx), self.amplitudes.data_ptr(), rt.stream_ptr(self.device)),
+                     "EOM context")
+            rt.LaunchCounter.add(rt.action_launches(ctx))
+            ea = rt.EomAction()
+            ea.action = rt.build_action(up, prog, self.vec.data_ptr(), ws, "X", ["sigma_rest_X"], "sigma",
+                                        self.plan.scatter_X)
+            ea.lam = self.lam.data_ptr()
+            self.workspaces.append(ws)
+            self.sigma_actions.append(ea)
 
     def sigma(self, x: torch.Tensor, out: torch.Tensor) -> None:
         if x.dtype != torch.complex128 or out.dtype != torch.complex128 or x.numel() != self.N:

@@ -1,7 +1,8 @@
 """Device Krylov solvers: restarted GMRES (Newton corrections) and CGS2 Arnoldi.
 
-Vectors live on the GPU; every vector operation is a kernel of the C ABI.
-Only O(restart) / O(m) scalars (projection coefficients, norms) cross to the
+The iteration loops run in C++ inside the library (``c3l_gmres``,
+``c3l_arnoldi``); this module owns their device/pinned buffers and wraps the
+vector kernels used elsewhere.  Only O(restart) / O(m) scalars cross to the
 host per iteration, where the Givens updates and stopping tests run.
 """
 
@@ -86,134 +87,6 @@ class DeviceVectors:
         rt.LaunchCounter.add(1)
 
 
-# =================================================================== GMRES
-def _lartg(f: float, g: float):
-    """Real plane rotation with c*f + s*g = r, -s*f + c*g = 0."""
-    if g == 0.0:
-        return 1.0, 0.0, f
-    if f == 0.0:
-        return 0.0, math.copysign(1.0, g), abs(g)
-    r = math.hypot(f, g)
-    c = abs(f) / r
-    s = math.copysign(1.0, f) * g / r
-    return c, s, math.copysign(r, f)
-
-
-@dataclass
-class GMRESResult:
-    x: torch.Tensor
-    info: int
-    history: list
-
-
-def gmres(vec: DeviceVectors, matvec, psolve, b: torch.Tensor, *, rtol: float, atol: float, restart: int,
-          maxiter: int) -> GMRESResult:
-    """Left-preconditioned restarted GMRES with SciPy's control flow.
-
-    Follows ``scipy.sparse.linalg.gmres`` (the solver the reference calls at
-    ``src/c3l/cc/component_solver.py:181``): the preconditioned residual drives
-    the inner loop, the true residual ``b - A x`` is checked after each
-    cycle, and the inner tolerance is adapted between cycles.  Orthogonal-
-    ization is classical Gram--Schmidt twice on the device.
-    """
-    dev = b.device
-    n = b.numel()
-    history: list = []
-    bnrm2 = vec.norm_r(b)
-    atol = max(float(atol), float(rtol) * bnrm2)
-    x = torch.zeros(n, dtype=torch.float64, device=dev)
-    if bnrm2 == 0.0:
-        return GMRESResult(b.clone(), 0, history)
-    eps = float(np.finfo(np.float64).eps)
-    restart = min(restart, n)
-    tmp = torch.empty(n, dtype=torch.float64, device=dev)
-    psolve(b, tmp)
-    Mb_nrm2 = vec.norm_r(tmp)
-    ptol_max_factor = 1.0
-    ptol = Mb_nrm2 * min(ptol_max_factor, atol / bnrm2)
-    V = torch.empty((restart + 1, n), dtype=torch.float64, device=dev)
-    coeff = torch.empty(2 * (restart + 1) + 2, dtype=torch.float64, device=dev)
-    r = b.clone()
-    rnorm = bnrm2
-    presid = 0.0
-    for iteration in range(maxiter):
-        if iteration == 0 and bnrm2 < atol:
-            return GMRESResult(x, 0, history)
-        psolve(r, V[0])
-        beta = vec.norm_r(V[0])
-        vec.scale_r(1.0 / beta, V[0], V[0])
-        S = np.zeros(restart + 1)
-        S[0] = beta
-        h = np.zeros((restart, restart + 1))
-        givens = np.zeros((restart, 2))
-        breakdown = False
-        col = 0
-        for col in range(restart):
-            matvec(V[col], tmp)
-            w = V[col + 1]
-            psolve(tmp, w)
-            k = col + 1
-            c1 = coeff[:k]
-            c2 = coeff[k:2 * k]
-            nrm = coeff[2 * k:2 * k + 2]
-            vec.dots_r(w, 1, w, nrm[0:1])               # h0^2
-            vec.dots_r(V, k, w, c1)
-            vec.axpy_r(V, k, c1, -1.0, w)
-            vec.dots_r(V, k, w, c2)
-            vec.axpy_r(V, k, c2, -1.0, w)
-            vec.dots_r(w, 1, w, nrm[1:2])               # h1^2
-            host = coeff[:2 * k + 2].cpu().numpy()
-            h0 = math.sqrt(max(host[2 * k], 0.0))
-            hcol = host[:k] + host[k:2 * k]
-            h1 = math.sqrt(max(host[2 * k + 1], 0.0))
-            h[col, :k] = hcol
-            h[col, col + 1] = h1
-            if h1 <= eps * h0:
-                h[col, col + 1] = 0.0
-                breakdown = True
-            else:
-                vec.scale_r(1.0 / h1, w, w)
-            for j in range(col):
-                c, s = givens[j]
-                n0, n1 = h[col, j], h[col, j + 1]
-                h[col, j], h[col, j + 1] = c * n0 + s * n1, -s * n0 + c * n1
-            c, s, mag = _lartg(h[col, col], h[col, col + 1])
-            givens[col] = (c, s)
-            h[col, col], h[col, col + 1] = mag, 0.0
-            t = -s * S[col]
-            S[col], S[col + 1] = c * S[col], t
-            presid = abs(t)
-            history.append(presid / bnrm2)
-            if presid <= ptol or breakdown:
-                break
-        if h[col, col] == 0:
-            S[col] = 0
-        y = np.array(S[:col + 1], dtype=np.float64)
-        for j in range(col, 0, -1):
-            if y[j] != 0:
-                y[j] /= h[j, j]
-                y[:j] -= y[j] * h[j, :j]
-        if y[0] != 0:
-            y[0] /= h[0, 0]
-        ydev = torch.from_numpy(y).to(dev)
-        vec.axpy_r(V, col + 1, ydev, 1.0, x)
-        matvec(x, tmp)
-        r.copy_(b)
-        vec.axpy_r(tmp, 1, vec.one_r, -1.0, r)
-        rnorm = vec.norm_r(r)
-        if rnorm <= atol:
-            break
-        elif breakdown:
-            break
-        elif presid <= ptol:
-            ptol_max_factor = max(eps, 0.25 * ptol_max_factor)
-        else:
-            ptol_max_factor = min(1.0, 1.5 * ptol_max_factor)
-        ptol = presid * min(ptol_max_factor, atol / rnorm)
-    info = 0 if rnorm <= atol else maxiter
-    return GMRESResult(x, info, history)
-
-
 # ================================================================= Arnoldi
 @dataclass
 class ArnoldiBasis:
@@ -246,73 +119,6 @@ def hessenberg_shifted(H: np.ndarray, m: int, shifts: torch.Tensor, beta: float,
     return green, resid
 
 
-def arnoldi(vec: DeviceVectors, matvec, b: torch.Tensor, shifts: torch.Tensor, *, maximum_dimension: int,
-            residual_tolerance: float, minimum_dimension: int = 16, check_interval: int = 8,
-            breakdown_tolerance: float = 1.0e-14) -> ArnoldiBasis:
-    """Two-pass classical Gram--Schmidt Arnoldi for (z I - K)^{-1} b.
-
-    Same recurrence, breakdown test and stopping rule as the reference's
-    ``arnoldi_resolvent`` (``src/c3l/green/krylov.py:284-417``); the reduced
-    shifted solves for the stopping test run on the device for all shifts.
-    """
-    started = time.perf_counter()
-    dev = b.device
-    N = b.numel()
-    m_max = int(maximum_dimension)
-    if m_max < 1 or m_max > N:
-        raise ValueError("maximum_dimension must lie in [1, operator.dimension]")
-    beta = vec.norm_r(torch.view_as_real(b).reshape(-1))
-    if beta == 0.0:
-        raise ValueError("rhs must be nonzero")
-    V = torch.empty((m_max + 1, N), dtype=torch.complex128, device=dev)
-    H = np.zeros((m_max + 1, m_max), dtype=np.complex128)
-    vec.scale_c(1.0 / beta, b, V[0])
-    coeff = torch.empty(2 * (m_max + 1) + 1, dtype=torch.complex128, device=dev)
-    check_dims: list = []
-    check_res: list = []
-    actual = m_max
-    breakdown = False
-    action = 0.0
-    for j in range(m_max):
-        t0 = time.perf_counter()
-        w = V[j + 1]
-        matvec(V[j], w)
-        action += time.perf_counter() - t0
-        k = j + 1
-        c1 = coeff[:k]
-        c2 = coeff[k:2 * k]
-        nrm = coeff[2 * k:2 * k + 1]
-        vec.dots_c(V, k, w, c1)
-        vec.axpy_c(V, k, c1, -1.0, w)
-        vec.dots_c(V, k, w, c2)
-        vec.axpy_c(V, k, c2, -1.0, w)
-        vec.dots_c(w, 1, w, nrm)
-        host = coeff[:2 * k + 1].cpu().numpy()
-        if not np.all(np.isfinite(host)):
-            raise FloatingPointError("Nonfinite Arnoldi step")
-        H[:k, j] = host[:k] + host[k:2 * k]
-        hn = math.sqrt(max(host[2 * k].real, 0.0))
-        H[j + 1, j] = hn
-        actual = j + 1
-        if abs(hn) <= breakdown_tolerance:
-            breakdown = True
-            break
-        vec.scale_c(1.0 / hn, w, w)
-        if actual >= minimum_dimension and (actual % check_interval == 0 or actual == m_max):
-            _, res = hessenberg_shifted(H, actual, shifts, beta, None)
-            worst = float(res.max().item())
-            check_dims.append(actual)
-            check_res.append(worst)
-            if worst <= residual_tolerance:
-                break
-    if not check_dims or check_dims[-1] != actual:
-        _, res = hessenberg_shifted(H, actual, shifts, beta, None)
-        check_dims.append(actual)
-        check_res.append(float(res.max().item()))
-    return ArnoldiBasis(V, H[:actual + 1, :actual], beta, actual, breakdown, check_dims, check_res,
-                        bool(check_res[-1] <= residual_tolerance), action, time.perf_counter() - started)
-
-
 def project_sink(vec: DeviceVectors, basis: ArnoldiBasis, sink: torch.Tensor) -> torch.Tensor:
     """p_k = sink . v_k (bilinear, no conjugation) for k < m."""
     out = torch.empty(basis.m, dtype=torch.complex128, device=sink.device)
@@ -338,3 +144,97 @@ def reduced_coordinates(basis: ArnoldiBasis, shifts: torch.Tensor, chunk_bytes: 
                                                 rt.stream_ptr(dev)), "hessenberg_coordinates")
         rt.LaunchCounter.add(1)
     return Y
+
+
+# ============================================================ C++ drivers
+class DeviceGMRES:
+    """Buffers and call wrapper for ``c3l_gmres`` (one per static problem)."""
+
+    def __init__(self, ops, restart: int):
+        self.ops = ops
+        dev = ops.device
+        n = ops.D
+        self.restart = int(min(restart, n))
+        r = self.restart
+        lib = rt.lib()
+        self.V = torch.empty((r + 1, n), dtype=torch.float64, device=dev)
+        self.tmp = torch.empty(n, dtype=torch.float64, device=dev)
+        self.r = torch.empty(n, dtype=torch.float64, device=dev)
+        self.coeff = torch.zeros(2 * (r + 2) + 4, dtype=torch.float64, device=dev)
+        self.partial = torch.empty(max(int(lib.c3l_multi_dot_scratch(r + 1, n)), 1), dtype=torch.float64, device=dev)
+        self.host = torch.zeros(3 * (r + 2) + 4, dtype=torch.float64).pin_memory()
+        self.history = np.zeros(4096, dtype=np.float64)
+
+    def solve(self, b: torch.Tensor, x: torch.Tensor, *, rtol: float, atol: float, maxiter: int):
+        ops = self.ops
+        a = rt.GmresArgs()
+        a.jvp = C.addressof(ops.jvp_action)
+        a.nrep = ops.nrep
+        a.pc_m4, a.pc_col, a.pc_pair = ops.pc_m4.data_ptr(), ops.pc_col.data_ptr(), ops.pc_pair.data_ptr()
+        a.dim = ops.D
+        a.b, a.x = b.data_ptr(), x.data_ptr()
+        a.rtol, a.atol = float(rtol), float(atol)
+        a.restart, a.maxiter = self.restart, int(maxiter)
+        a.V, a.tmp, a.r = self.V.data_ptr(), self.tmp.data_ptr(), self.r.data_ptr()
+        a.coeff, a.partial, a.host = self.coeff.data_ptr(), self.partial.data_ptr(), self.host.data_ptr()
+        a.history = self.history.ctypes.data
+        a.history_capacity = self.history.size
+        rt.check(rt.lib().c3l_gmres(C.byref(a), rt.stream_ptr(ops.device)), "gmres")
+        hist = list(self.history[:min(a.history_len, self.history.size)])
+        rt.LaunchCounter.add(a.matvecs * ops.launches["jvp"] + a.history_len * 7 + 8)
+        return int(a.info), hist, int(a.matvecs)
+
+
+def arnoldi_channels(ops, sources, shifts: torch.Tensor, *, maximum_dimension: int, residual_tolerance: float,
+                     minimum_dimension: int = 16, check_interval: int = 8, breakdown_tolerance: float = 1.0e-14):
+    """Run ``c3l_arnoldi`` on several sources at once (one stream and workspace each)."""
+    started = time.perf_counter()
+    dev = shifts.device
+    lib = rt.lib()
+    N = ops.N
+    m_max = int(maximum_dimension)
+    nch = len(sources)
+    ops.ensure_channels(nch)
+    keep = []
+    chans = (rt.ArnoldiChannel * nch)()
+    streams = [torch.cuda.Stream(device=dev) for _ in range(nch)]
+    cur = torch.cuda.current_stream(dev)
+    Hs = []
+    for c, b in enumerate(sources):
+        V = torch.empty((m_max + 1, N), dtype=torch.complex128, device=dev)
+        Hcol = torch.zeros((m_max, m_max + 1), dtype=torch.complex128, device=dev)
+        coeff = torch.zeros(2 * (m_max + 1) + 2, dtype=torch.complex128, device=dev)
+        partial = torch.empty(max(int(lib.c3l_multi_dot_scratch(m_max + 1, N)), 1), dtype=torch.complex128, device=dev)
+        host = torch.zeros(2 * (m_max + 1) + 2, dtype=torch.complex128).pin_memory()
+        H = np.zeros((m_max + 1, m_max), dtype=np.complex128)
+        Hdev = torch.empty((m_max + 1) * m_max, dtype=torch.complex128, device=dev)
+        rdev = torch.empty(shifts.numel(), dtype=torch.float64, device=dev)
+        rhost = torch.zeros(shifts.numel(), dtype=torch.float64).pin_memory()
+        cdims = np.zeros(m_max // max(check_interval, 1) + 4, dtype=np.int32)
+        cres = np.zeros(cdims.size, dtype=np.float64)
+        keep += [V, coeff, partial, host, Hdev, rdev, rhost, cdims, cres, b, Hcol]
+        Hs.append(H)
+        q = chans[c]
+        q.sigma = C.addressof(ops.sigma_actions[c])
+        q.b, q.V, q.coeff, q.partial, q.host = b.data_ptr(), V.data_ptr(), coeff.data_ptr(), partial.data_ptr(), host.data_ptr()
+        q.Hcol = Hcol.data_ptr()
+        q.H, q.Hdev, q.resid_dev, q.resid_host = H.ctypes.data, Hdev.data_ptr(), rdev.data_ptr(), rhost.data_ptr()
+        q.check_dims, q.check_res, q.check_capacity = cdims.ctypes.data, cres.ctypes.data, cdims.size
+    for st in streams:
+        st.wait_stream(cur)
+    sp = (C.c_void_p * nch)(*[st.cuda_stream for st in streams])
+    rt.check(lib.c3l_arnoldi(chans, nch, N, shifts.data_ptr(), shifts.numel(), m_max, float(residual_tolerance),
+                             int(minimum_dimension), int(check_interval), float(breakdown_tolerance), sp), "arnoldi")
+    for st in streams:
+        cur.wait_stream(st)
+    out = []
+    for c in range(nch):
+        q = chans[c]
+        m = int(q.m)
+        V = keep[c * 11]
+        nchk = min(int(q.nchecks), keep[c * 11 + 7].size)
+        rt.LaunchCounter.add(m * (ops.sigma_launches + 7) + 2 * nchk + 3)
+        out.append(ArnoldiBasis(V, Hs[c][:m + 1, :m].copy(), float(q.beta), m, bool(q.breakdown),
+                                list(keep[c * 11 + 7][:nchk]), list(keep[c * 11 + 8][:nchk]), bool(q.converged),
+                                float(q.action_seconds), time.perf_counter() - started))
+    return out

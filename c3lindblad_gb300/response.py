@@ -23,7 +23,7 @@ import numpy as np
 import torch
 
 from . import runtime as rt
-from .krylov import DeviceVectors, arnoldi, hessenberg_shifted, reduced_coordinates
+from .krylov import DeviceVectors, arnoldi_channels, hessenberg_shifted, reduced_coordinates
 from .static import ComponentStaticProblem, _is_reference_object
 
 
@@ -251,9 +251,11 @@ def component_retarded_green(operator, sources, omega, eta: float, *, rtol: floa
     out = []
     channels = []
     sink_conj = torch.conj(sink).resolve_conj().contiguous()
-    for src in (add, rem):
-        basis = arnoldi(vec, op.matvec_device, src, shifts, maximum_dimension=max_dim, residual_tolerance=rtol,
-                        minimum_dimension=min(16, max_dim), check_interval=8)
+    bases = arnoldi_channels(op.context.ops, [add.contiguous(), rem.contiguous()], shifts,
+                             maximum_dimension=max_dim, residual_tolerance=rtol,
+                             minimum_dimension=min(16, max_dim), check_interval=8)
+    op.action_calls += sum(b.m for b in bases)
+    for basis in bases:
         if not basis.converged:
             raise RuntimeError("a component EOM shifted solve failed to converge")
         proj = torch.empty(basis.m, dtype=torch.complex128, device=dev)

@@ -54,12 +54,32 @@ class Complex(C.Structure):
     _fields_ = [("re", C.c_double), ("im", C.c_double)]
 
 
+class GmresArgs(C.Structure):
+    _fields_ = [("jvp", C.c_void_p), ("nrep", C.c_int64), ("pc_m4", C.c_void_p), ("pc_col", C.c_void_p),
+                ("pc_pair", C.c_void_p), ("dim", C.c_int64), ("b", C.c_void_p), ("x", C.c_void_p),
+                ("rtol", C.c_double), ("atol", C.c_double), ("restart", C.c_int32), ("maxiter", C.c_int32),
+                ("V", C.c_void_p), ("tmp", C.c_void_p), ("r", C.c_void_p), ("coeff", C.c_void_p),
+                ("partial", C.c_void_p), ("host", C.c_void_p), ("history", C.c_void_p),
+                ("history_capacity", C.c_int32), ("history_len", C.c_int32), ("info", C.c_int32),
+                ("matvecs", C.c_int32)]
+
+
+class ArnoldiChannel(C.Structure):
+    _fields_ = [("sigma", C.c_void_p), ("b", C.c_void_p), ("V", C.c_void_p), ("Hcol", C.c_void_p), ("coeff", C.c_void_p),
+                ("partial", C.c_void_p), ("host", C.c_void_p), ("H", C.c_void_p), ("Hdev", C.c_void_p),
+                ("resid_dev", C.c_void_p), ("resid_host", C.c_void_p), ("check_dims", C.c_void_p),
+                ("check_res", C.c_void_p), ("check_capacity", C.c_int32), ("m", C.c_int32),
+                ("breakdown", C.c_int32), ("converged", C.c_int32), ("nchecks", C.c_int32), ("pad", C.c_int32),
+                ("beta", C.c_double), ("action_seconds", C.c_double)]
+
+
 EXPORTS = (
     "c3l_tilde_unpack", "c3l_scatter_padded", "c3l_contract", "c3l_wedge_padded", "c3l_wedge_static_out",
     "c3l_wedge_eom_out", "c3l_wedge_source_out", "c3l_action_prepare", "c3l_static_apply", "c3l_eom_sigma",
     "c3l_multi_dot_scratch", "c3l_multi_dot_c", "c3l_multi_dot_r", "c3l_multi_axpy_c", "c3l_multi_axpy_r",
     "c3l_scale_c", "c3l_scale_r", "c3l_precondition", "c3l_hessenberg_shifted", "c3l_hessenberg_coordinates",
-    "c3l_hessenberg_coordinates_noalloc", "c3l_version",
+    "c3l_hessenberg_coordinates_noalloc", "c3l_gmres", "c3l_arnoldi", "c3l_hessenberg_residual_f32",
+    "c3l_arnoldi_column", "c3l_version",
 )
 
 
@@ -86,6 +106,10 @@ def _declare(lib) -> None:
         "c3l_hessenberg_shifted": [P, I64, I32, P, I32, D, P, P, P, P],
         "c3l_hessenberg_coordinates": [P, I64, I32, P, I32, D, P, P, P],
         "c3l_hessenberg_coordinates_noalloc": [P, I64, I32, P, I32, D, P, P],
+        "c3l_gmres": [P, P],
+        "c3l_hessenberg_residual_f32": [P, I64, I32, P, I32, D, P, P],
+        "c3l_arnoldi_column": [P, I32, P, I64, P, I64, I32, D, P],
+        "c3l_arnoldi": [P, I32, I64, P, I32, I32, D, I32, I32, D, P],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)

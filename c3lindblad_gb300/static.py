@@ -19,7 +19,7 @@ import numpy as np
 import torch
 
 from . import runtime as rt
-from .krylov import DeviceVectors, gmres
+from .krylov import DeviceGMRES, DeviceVectors
 from .spec import ProblemSpec
 
 
@@ -201,6 +201,13 @@ class ComponentStaticProblem:
     def device(self) -> torch.device:
         return self.ops.device
 
+    def gmres_solver(self, restart: int):
+        """Device GMRES buffers sized for ``restart`` (cached per restart length)."""
+        cache = self.__dict__.setdefault("_gmres", {})
+        if restart not in cache:
+            cache[restart] = DeviceGMRES(self.ops, restart)
+        return cache[restart]
+
     @property
     def n(self) -> int:
         return self.spec.n
@@ -315,6 +322,9 @@ def solve_component_ccsd(problem, initial_amplitudes=None, *, policy: NewtonKryl
     prev_norm = None
     prev_tol = None
     jvp_count = [0]
+    solver = p.gmres_solver(controls.gmres_restart)
+    step = torch.empty(D, dtype=torch.float64, device=dev)
+    negr = torch.empty(D, dtype=torch.float64, device=dev)
 
     def matvec(v, out):
         jvp_count[0] += 1
@@ -331,11 +341,10 @@ def solve_component_ccsd(problem, initial_amplitudes=None, *, policy: NewtonKryl
             break
         lin_tol = forcing_tolerance(norm, controls, previous_norm=prev_norm, previous_tolerance=prev_tol)
         lin_atol = 0.0 if controls.forcing_strategy == "legacy" else controls.gmres_absolute_tolerance_factor * controls.tolerance
-        negr = torch.empty_like(r)
         vec.scale_r(-1.0, r, negr)
-        res = gmres(vec, matvec, ops.precondition, negr, rtol=lin_tol, atol=lin_atol,
-                    restart=controls.gmres_restart, maxiter=controls.gmres_maximum_restart_cycles)
-        step = res.x
+        info, gm_history, gm_matvecs = solver.solve(negr, step, rtol=lin_tol, atol=lin_atol,
+                                                    maxiter=controls.gmres_maximum_restart_cycles)
+        jvp_count[0] += gm_matvecs
         matvec(step, jstep)
         # linear defect J s + r, merit slope r . J s, step norm
         vec.dots_r(r, 1, jstep, scal[0:1])
@@ -347,8 +356,8 @@ def solve_component_ccsd(problem, initial_amplitudes=None, *, policy: NewtonKryl
         true_rel = float(defect_norm / max(norm, np.finfo(float).tiny))
         if controls.forcing_strategy == "eisenstat_walker" and not _acceptable_inexact_newton_step(
                 norm, merit_slope, defect_norm, relative_tolerance=lin_tol, absolute_tolerance=lin_atol):
-            history.append(NewtonKrylovStep(iteration, norm, lin_tol, int(res.info), len(res.history),
-                                            tuple(res.history), true_rel, step_norm, 0.0, norm))
+            history.append(NewtonKrylovStep(iteration, norm, lin_tol, info, len(gm_history),
+                                            tuple(gm_history), true_rel, step_norm, 0.0, norm))
             break
         damping = 1.0
         accepted_norm = np.inf
@@ -368,8 +377,8 @@ def solve_component_ccsd(problem, initial_amplitudes=None, *, policy: NewtonKryl
                     accepted_step_callback(iteration, amp.cpu().numpy(), accepted_norm)
                 break
             damping *= 0.5
-        history.append(NewtonKrylovStep(iteration, norm, lin_tol, int(res.info), len(res.history),
-                                        tuple(res.history), true_rel, step_norm, float(damping), accepted_norm))
+        history.append(NewtonKrylovStep(iteration, norm, lin_tol, info, len(gm_history),
+                                        tuple(gm_history), true_rel, step_norm, float(damping), accepted_norm))
         if not accepted:
             break
         prev_norm = norm

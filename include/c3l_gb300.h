@@ -70,7 +70,8 @@ typedef struct {
     int32_t pad;
 } c3l_block;
 
-/* A thread-block work unit: <= 256 consecutive outputs of one block/task. */
+/* A thread-block work unit: consecutive outputs of one block/task (<= 256 for
+ * contraction tasks, <= 64 for wedge stages). */
 typedef struct {
     int32_t block;
     int32_t count;
@@ -228,11 +229,99 @@ c3l_status c3l_hessenberg_shifted(const c3l_complex* H, int64_t ldh, int32_t m, 
                                   int32_t nshift, double beta, const c3l_complex* sinkproj,
                                   c3l_complex* green, double* residual, void* stream);
 
+/* Single-precision residual-only variant for convergence checks: returns
+ * residual[s] = |H[m, m-1] y_{m-1}| / beta with relative error ~cond * 1e-7. */
+c3l_status c3l_hessenberg_residual_f32(const c3l_complex* H, int64_t ldh, int32_t m, const c3l_complex* shifts,
+                                       int32_t nshift, double beta, double* residual, void* stream);
+
+/* Arnoldi column j on the device from the CGS2 coefficients
+ * coeff = [c1 (k) | c2 (k) | |w'|^2]: Hc[j*ldc + i] = c1_i + c2_i (i < k),
+ * Hc[j*ldc + k] = h = sqrt(|w'|^2 - |c2|^2), and w /= h unless h <= tol. */
+c3l_status c3l_arnoldi_column(const c3l_complex* coeff, int32_t k, c3l_complex* w, int64_t n, c3l_complex* Hc,
+                              int64_t ldc, int32_t j, double tol, void* stream);
+
 /* Full reduced coordinates Y[s][0..m) of the same systems (for solution
  * vectors); rscratch: nshift * m*(m+1)/2 complex entries of caller memory. */
 c3l_status c3l_hessenberg_coordinates(const c3l_complex* H, int64_t ldh, int32_t m, const c3l_complex* shifts,
                                       int32_t nshift, double beta, c3l_complex* rscratch, c3l_complex* Y,
                                       void* stream);
+
+/* ----------------------------------------------------------- Krylov drivers */
+
+/* Left-preconditioned restarted GMRES for a Newton correction, with SciPy's
+ * control flow (the solver of src/c3l/cc/component_solver.py:181-191): A is
+ * the device JVP action, M the rapidity preconditioner.  Orthogonalization is
+ * classical Gram-Schmidt twice on the device; the Givens updates run on the
+ * host from one pinned read-back per inner iteration.
+ * Device buffers: V[(restart+1)*dim], tmp[dim], r[dim], x[dim] (output),
+ * coeff[2*(restart+2)+3], partial[c3l_multi_dot_scratch(restart+1, dim)];
+ * host: host[3*(restart+2)+2] (pinned), history[history_capacity]. */
+typedef struct {
+    const c3l_static_action* jvp;
+    int64_t nrep;
+    const double* pc_m4;
+    const int64_t* pc_col;
+    const int64_t* pc_pair;
+    int64_t dim;
+    const double* b;
+    double* x;
+    double rtol;
+    double atol;
+    int32_t restart;
+    int32_t maxiter;
+    double* V;
+    double* tmp;
+    double* r;
+    double* coeff;
+    double* partial;
+    double* host;
+    double* history;
+    int32_t history_capacity;
+    /* outputs */
+    int32_t history_len;
+    int32_t info;
+    int32_t matvecs;
+} c3l_gmres_args;
+
+c3l_status c3l_gmres(c3l_gmres_args* args, void* stream);
+
+/* One Arnoldi channel (source vector and its own sigma workspace). */
+typedef struct {
+    const c3l_eom_action* sigma;
+    const c3l_complex* b;
+    c3l_complex* V;          /* device (m_max+1) x N, row-major        */
+    c3l_complex* Hcol;       /* device m_max x (m_max+1), column-major  */
+    c3l_complex* coeff;      /* device >= 2*(m_max+1)+1                */
+    c3l_complex* partial;    /* device c3l_multi_dot_scratch(m_max+1, N) */
+    c3l_complex* host;       /* pinned >= 2*(m_max+1)+1                */
+    c3l_complex* H;          /* host (m_max+1) x m_max, zeroed          */
+    c3l_complex* Hdev;       /* device (m_max+1) x m_max                */
+    double* resid_dev;       /* device [nshift]                         */
+    double* resid_host;      /* pinned [nshift]                         */
+    int32_t* check_dims;     /* host [check_capacity]                   */
+    double* check_res;       /* host [check_capacity]                   */
+    int32_t check_capacity;
+    /* outputs */
+    int32_t m;
+    int32_t breakdown;
+    int32_t converged;
+    int32_t nchecks;
+    int32_t pad;
+    double beta;
+    double action_seconds;
+} c3l_arnoldi_channel;
+
+/* CGS2 Arnoldi for (z I - K)^{-1} b on every channel, channel c on streams[c]
+ * (src/c3l/green/krylov.py:284-417): stops a channel when the Arnoldi-relation
+ * residual is <= tol for every shift (checked every check_interval steps from
+ * min_dim on) or on breakdown (|h_{j+1,j}| <= breakdown_tol).  Steps run
+ * without host synchronization between checks: each step's column of H is
+ * formed on the device, and the host reads the new columns at each check.
+ * Checks run in FP32 (c3l_hessenberg_residual_f32); a passing check is
+ * confirmed in FP64 (c3l_hessenberg_shifted) before a channel stops. */
+c3l_status c3l_arnoldi(c3l_arnoldi_channel* channels, int32_t nchannels, int64_t N, const c3l_complex* shifts,
+                       int32_t nshift, int32_t m_max, double tol, int32_t min_dim, int32_t check_interval,
+                       double breakdown_tol, void* const* streams);
 
 /* Allocation-free variant of c3l_hessenberg_coordinates, for callers that
  * cannot allocate device memory: a host application that owns the device

@@ -181,3 +181,13 @@ def test_krylov_primitives_against_numpy(cuda_device):
     ys = [np.linalg.solve(z * np.eye(m) - H[:m, :m], e1) for z in shifts]
     assert relerr(green.cpu().numpy(), np.array([p @ y for y in ys])) < 1e-10
     assert relerr(resid.cpu().numpy(), np.array([abs(H[m, m - 1] * y[-1]) / 2.5 for y in ys])) < 1e-10
+    # single-precision convergence-check variant: same residuals to ~1e-4 relative
+    from c3lindblad_gb300 import runtime as rt
+
+    Hd = torch.from_numpy(np.ascontiguousarray(H[:m + 1, :m])).to(cuda_device)
+    r32 = torch.empty(shifts.size, dtype=torch.float64, device=cuda_device)
+    st = rt.lib().c3l_hessenberg_residual_f32(Hd.data_ptr(), m, m, torch.from_numpy(shifts).to(cuda_device).data_ptr(),
+                                              shifts.size, 2.5, r32.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    assert st == 0
+    want = np.array([abs(H[m, m - 1] * y[-1]) / 2.5 for y in ys])
+    assert np.max(np.abs(r32.cpu().numpy() - want) / want) < 1e-3
