@@ -41,6 +41,9 @@ WORKLOADS = {
     "siam10": dict(spec="siam10", omega=(-8.0, 8.0, 1001), eta=0.0,
                    label="SIAM U=4, 10 pseudomodes (n=11, 20933 amplitudes, S13 dim 1947), "
                          "charge+1 G^R on 1001 omega in [-8,8], eta=0"),
+    "readme": dict(spec="readme", omega=(-4.0, 4.0, 81), eta=0.0,
+                   label="README quick-start model (n=3, 117 amplitudes, S13 dim 39), "
+                         "charge+1 G^R on 81 omega in [-4,4], eta=0"),
 }
 
 

@@ -69,7 +69,7 @@ c3l_status c3l_gmres(c3l_gmres_args* a, void* stream) {
     a->matvecs = 0;
     auto matvec = [&](const double* in, double* out) -> c3l_status {
         a->matvecs += 1;
-        return c3l_static_apply(a->jvp, in, out, stream);
+        return a->use_f32 ? c3l_static_apply_f32(a->jvp, in, out, stream) : c3l_static_apply(a->jvp, in, out, stream);
     };
     auto psolve = [&](const double* in, double* out) -> c3l_status {
         return c3l_precondition(a->nrep, a->pc_m4, a->pc_col, a->pc_pair, in, out, stream);

@@ -13,8 +13,13 @@
 //   k_scatter / k_tilde_unpack -- move vectors between the reference's
 //                  canonical layout and the padded workspace.
 //
-// All arithmetic is complex FP64.  Instances of one output block are staged
-// through shared memory so every thread of a tile reads them once per chunk.
+// Every kernel is templated on the workspace element: complex FP64 (double2)
+// for residuals, sources and the refinement path, complex FP32 (float2) for
+// the inner Krylov operator of the mixed-precision Newton solve.  FP64 runs
+// on a narrow pipe on this part, FP32 on the full-width one.  Epilogues
+// (the rapidity diagonal and the -i factor) are always evaluated in FP64.
+// Instances of one output block are staged through shared memory and split
+// over four thread groups.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -25,13 +30,40 @@ namespace {
 constexpr int kThreads = 256;
 constexpr int kInstChunk = 32;
 
-__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
-    return make_double2(fma(a.x, b.x, -a.y * b.y), fma(a.x, b.y, a.y * b.x));
+template <typename C> struct Cx;
+template <> struct Cx<double2> {
+    using R = double;
+    static __device__ __forceinline__ double2 make(double a, double b) { return make_double2(a, b); }
+};
+template <> struct Cx<float2> {
+    using R = float;
+    static __device__ __forceinline__ float2 make(double a, double b) { return make_float2((float)a, (float)b); }
+};
+
+template <typename C>
+__device__ __forceinline__ C cmul(C a, C b) {
+    C r;
+    r.x = fma(a.x, b.x, -a.y * b.y);
+    r.y = fma(a.x, b.y, a.y * b.x);
+    return r;
 }
-__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
-__device__ __forceinline__ double2 cfma(double2 a, double2 b, double2 c) {
-    // a*b + c
-    return make_double2(fma(a.x, b.x, fma(-a.y, b.y, c.x)), fma(a.x, b.y, fma(a.y, b.x, c.y)));
+template <typename C>
+__device__ __forceinline__ C cadd(C a, C b) {
+    C r;
+    r.x = a.x + b.x;
+    r.y = a.y + b.y;
+    return r;
+}
+template <typename C>
+__device__ __forceinline__ C cfma(C a, C b, C c) {  // a*b + c
+    C r;
+    r.x = fma(a.x, b.x, fma(-a.y, b.y, c.x));
+    r.y = fma(a.x, b.y, fma(a.y, b.x, c.y));
+    return r;
+}
+template <typename C>
+__device__ __forceinline__ double2 to_d2(C a) {
+    return make_double2((double)a.x, (double)a.y);
 }
 
 inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
@@ -52,8 +84,9 @@ __global__ void k_tilde_unpack(int64_t dim, const double* __restrict__ x, const 
     }
 }
 
+template <typename C>
 __global__ void k_scatter(int64_t count, const int64_t* __restrict__ dst, const int64_t* __restrict__ pos,
-                          const double* __restrict__ sign, const double2* __restrict__ vec, double2* __restrict__ ws) {
+                          const double* __restrict__ sign, const double2* __restrict__ vec, C* __restrict__ ws) {
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < count; e += (int64_t)gridDim.x * blockDim.x) {
         const double s = sign[e];
         double2 v = make_double2(0.0, 0.0);
@@ -61,7 +94,14 @@ __global__ void k_scatter(int64_t count, const int64_t* __restrict__ dst, const 
             const double2 u = vec[pos[e]];
             v = make_double2(s * u.x, s * u.y);
         }
-        ws[dst[e]] = v;
+        ws[dst[e]] = Cx<C>::make(v.x, v.y);
+    }
+}
+
+__global__ void k_downcast(int64_t count, const double2* __restrict__ src, float2* __restrict__ dst) {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < count; e += (int64_t)gridDim.x * blockDim.x) {
+        const double2 v = src[e];
+        dst[e] = make_float2((float)v.x, (float)v.y);
     }
 }
 
@@ -71,26 +111,27 @@ __device__ __forceinline__ void powers(int n, int64_t* pw) {
     for (int i = 1; i < 6; ++i) pw[i] = pw[i - 1] * n;
 }
 
-__global__ void __launch_bounds__(kThreads) k_contract(c3l_contract_level lv, int n, const double2* __restrict__ vectors,
-                                                        double2* __restrict__ ws) {
+template <typename C>
+__global__ void __launch_bounds__(kThreads) k_contract(c3l_contract_level lv, int n, const C* __restrict__ vectors,
+                                                        C* __restrict__ ws) {
     const c3l_tile tile = lv.tiles[blockIdx.x];
     if ((int)threadIdx.x >= tile.count) return;
     const c3l_contract_task& task = lv.tasks[tile.block];
     int64_t pw[6];
     powers(n, pw);
     const int64_t e = tile.start + threadIdx.x;
-    double2 acc = make_double2(0.0, 0.0);
+    C acc = Cx<C>::make(0.0, 0.0);
     if (task.const_off >= 0) acc = vectors[task.const_off + e];
     for (int j = 0; j < task.nsrc; ++j) {
         const int axis = task.axis[j];
         const int64_t low = pw[task.deg - axis];
         const int64_t hi = e / low;
         const int64_t lo = e - hi * low;
-        const double2* src = ws + task.src_off[j] + hi * low * n + lo;
-        const double2* vec = vectors + task.vec_off[j];
-        double2 sum = make_double2(0.0, 0.0);
+        const C* src = ws + task.src_off[j] + hi * low * n + lo;
+        const C* vec = vectors + task.vec_off[j];
+        C sum = Cx<C>::make(0.0, 0.0);
         for (int m = 0; m < n; ++m) sum = cfma(vec[m], src[m * low], sum);
-        const double sg = task.sign[j];
+        const typename Cx<C>::R sg = (typename Cx<C>::R)task.sign[j];
         acc.x = fma(sg, sum.x, acc.x);
         acc.y = fma(sg, sum.y, acc.y);
     }
@@ -110,16 +151,20 @@ struct Epilogue {
     double2 cscale;
 };
 
+__device__ __forceinline__ double2 dmul(double2 a, double2 b) {
+    return make_double2(fma(a.x, b.x, -a.y * b.y), fma(a.x, b.y, a.y * b.x));
+}
+
 // One block = one tile of up to kWE outputs of one output block; the block's
 // instances are split over kWG thread groups (instance i goes to group
 // i % kWG) and the groups' partial sums are added in shared memory.
 constexpr int kWE = 64;
 constexpr int kWG = kThreads / kWE;
 
-template <int MODE>
-__global__ void __launch_bounds__(kThreads) k_wedge(c3l_wedge_stage st, int n, double2* ws, Epilogue ep) {
+template <int MODE, typename C>
+__global__ void __launch_bounds__(kThreads) k_wedge(c3l_wedge_stage st, int n, C* ws, Epilogue ep) {
     __shared__ c3l_instance sinst[kInstChunk];
-    __shared__ double2 red[kWG][kWE];
+    __shared__ C red[kWG][kWE];
     const c3l_tile tile = st.tiles[blockIdx.x];
     const c3l_block blk = st.blocks[tile.block];
     const int ex = threadIdx.x % kWE;
@@ -142,7 +187,7 @@ __global__ void __launch_bounds__(kThreads) k_wedge(c3l_wedge_stage st, int n, d
             for (int c = 0; c < 4; ++c) dig[c] = (int)((packed >> (8 * c)) & 0xFF);
         }
     }
-    double2 acc = make_double2(0.0, 0.0);
+    C acc = Cx<C>::make(0.0, 0.0);
     for (int64_t base = blk.inst_begin; base < blk.inst_end; base += kInstChunk) {
         const int64_t left = blk.inst_end - base;
         const int cnt = left < kInstChunk ? (int)left : kInstChunk;
@@ -158,7 +203,7 @@ __global__ void __launch_bounds__(kThreads) k_wedge(c3l_wedge_stage st, int n, d
         if (active) {
             for (int i = gy; i < cnt; i += kWG) {
                 const c3l_instance& in = sinst[i];
-                double2 v = make_double2(in.coef[0], in.coef[1]);
+                C v = Cx<C>::make(in.coef[0], in.coef[1]);
                 for (int j = 0; j < in.nfac; ++j) {
                     const int d = in.fac_deg[j];
                     int64_t off = in.fac_off[j];
@@ -178,18 +223,22 @@ __global__ void __launch_bounds__(kThreads) k_wedge(c3l_wedge_stage st, int n, d
         ws[blk.out_off + e] = acc;
     } else if (MODE == kStatic) {
         const int64_t mu = st.elements[e];
-        const double2 s = cfma(ep.lam[e], ep.src[mu], acc);
+        const double2 a = to_d2(acc);
+        const double2 lam = ep.lam[e], src = ep.src[mu];
+        const double2 s = make_double2(fma(lam.x, src.x, fma(-lam.y, src.y, a.x)), fma(lam.x, src.y, fma(lam.y, src.x, a.y)));
         const double2 r = make_double2(s.y, -s.x);  // -i * s
-        const double2 v = cmul(r, ep.scale[e]);
+        const double2 v = dmul(r, ep.scale[e]);
         const int64_t c = ep.col[e];
         ep.xout[c] = v.x;
         if (ep.pair[e]) ep.xout[c + 1] = r.y;
     } else if (MODE == kEom) {
         const int64_t mu = st.elements[e];
-        ep.cout[mu] = cfma(ep.lam[e], ep.src[mu], acc);
+        const double2 a = to_d2(acc);
+        const double2 lam = ep.lam[e], src = ep.src[mu];
+        ep.cout[mu] = make_double2(fma(lam.x, src.x, fma(-lam.y, src.y, a.x)), fma(lam.x, src.y, fma(lam.y, src.x, a.y)));
     } else {
         const int64_t mu = st.elements[e];
-        ep.cout[mu] = cmul(ep.cscale, acc);
+        ep.cout[mu] = dmul(ep.cscale, to_d2(acc));
     }
 }
 
@@ -200,37 +249,87 @@ inline unsigned grid_for(int64_t count) {
     return (unsigned)b;
 }
 
+template <typename C>
 c3l_status run_levels(const c3l_action* a, cudaStream_t s) {
     for (int l = 0; l < a->nlevels; ++l) {
         if (a->levels[l].ntiles <= 0) continue;
-        k_contract<<<(unsigned)a->levels[l].ntiles, kThreads, 0, s>>>(a->levels[l], a->n,
-                                                                     reinterpret_cast<const double2*>(a->vectors),
-                                                                     reinterpret_cast<double2*>(a->ws));
+        k_contract<C><<<(unsigned)a->levels[l].ntiles, kThreads, 0, s>>>(a->levels[l], a->n,
+                                                                        reinterpret_cast<const C*>(a->vectors),
+                                                                        reinterpret_cast<C*>(a->ws));
     }
     return launch_status();
 }
 
+template <typename C>
 c3l_status run_padded(const c3l_action* a, cudaStream_t s) {
     Epilogue ep{};
     for (int p = 0; p < a->npadded; ++p) {
         if (a->padded[p].ntiles <= 0) continue;
-        k_wedge<kPadded><<<(unsigned)a->padded[p].ntiles, kThreads, 0, s>>>(a->padded[p], a->n,
-                                                                           reinterpret_cast<double2*>(a->ws), ep);
+        k_wedge<kPadded, C><<<(unsigned)a->padded[p].ntiles, kThreads, 0, s>>>(a->padded[p], a->n,
+                                                                              reinterpret_cast<C*>(a->ws), ep);
     }
     return launch_status();
 }
 
+template <typename C>
 c3l_status scatter(const c3l_action* a, const c3l_complex* vec, cudaStream_t s) {
     if (a->scatter_count <= 0) return C3L_OK;
-    k_scatter<<<grid_for(a->scatter_count), kThreads, 0, s>>>(a->scatter_count, a->scatter_dst, a->scatter_pos,
-                                                            a->scatter_sign, reinterpret_cast<const double2*>(vec),
-                                                            reinterpret_cast<double2*>(a->ws));
+    k_scatter<C><<<grid_for(a->scatter_count), kThreads, 0, s>>>(a->scatter_count, a->scatter_dst, a->scatter_pos,
+                                                               a->scatter_sign, reinterpret_cast<const double2*>(vec),
+                                                               reinterpret_cast<C*>(a->ws));
     return launch_status();
 }
 
 bool valid_action(const c3l_action* a) {
     return a && a->ws && a->vectors && a->n > 0 && a->n <= 255 && a->nlevels >= 0 && a->nlevels <= C3L_MAX_LEVELS &&
            a->npadded >= 0 && a->npadded <= C3L_MAX_STAGES;
+}
+
+template <typename C>
+c3l_status action_prepare(const c3l_action* action, const c3l_complex* t, cudaStream_t s) {
+    c3l_status st = scatter<C>(action, t, s);
+    if (st) return st;
+    if ((st = run_levels<C>(action, s))) return st;
+    return run_padded<C>(action, s);
+}
+
+template <typename C>
+c3l_status static_apply(const c3l_static_action* sa, const double* x, double* xout, void* stream) {
+    if (!sa || !x || !xout || !valid_action(&sa->action) || !sa->canon || !sa->tilde_ia || !sa->tilde_ib ||
+        !sa->tilde_ca || !sa->tilde_cb || !sa->lam || !sa->col || !sa->pair || !sa->scale || sa->num_amplitudes <= 0)
+        return C3L_ERR_ARGUMENT;
+    cudaStream_t s = as_stream(stream);
+    c3l_status st = c3l_tilde_unpack(sa->num_amplitudes, x, sa->tilde_ia, sa->tilde_ib, sa->tilde_ca, sa->tilde_cb,
+                                     sa->canon, stream);
+    if (st) return st;
+    if ((st = action_prepare<C>(&sa->action, sa->canon, s))) return st;
+    if (sa->action.out.ntiles <= 0) return C3L_OK;
+    Epilogue ep{};
+    ep.lam = reinterpret_cast<const double2*>(sa->lam);
+    ep.src = reinterpret_cast<const double2*>(sa->canon);
+    ep.col = sa->col;
+    ep.pair = sa->pair;
+    ep.scale = reinterpret_cast<const double2*>(sa->scale);
+    ep.xout = xout;
+    k_wedge<kStatic, C><<<(unsigned)sa->action.out.ntiles, kThreads, 0, s>>>(sa->action.out, sa->action.n,
+                                                                            reinterpret_cast<C*>(sa->action.ws), ep);
+    return launch_status();
+}
+
+template <typename C>
+c3l_status eom_sigma(const c3l_eom_action* ea, const c3l_complex* xin, c3l_complex* out, void* stream) {
+    if (!ea || !xin || !out || !valid_action(&ea->action) || !ea->lam) return C3L_ERR_ARGUMENT;
+    cudaStream_t s = as_stream(stream);
+    c3l_status st = action_prepare<C>(&ea->action, xin, s);
+    if (st) return st;
+    if (ea->action.out.ntiles <= 0) return C3L_OK;
+    Epilogue ep{};
+    ep.lam = reinterpret_cast<const double2*>(ea->lam);
+    ep.src = reinterpret_cast<const double2*>(xin);
+    ep.cout = reinterpret_cast<double2*>(out);
+    k_wedge<kEom, C><<<(unsigned)ea->action.out.ntiles, kThreads, 0, s>>>(ea->action.out, ea->action.n,
+                                                                         reinterpret_cast<C*>(ea->action.ws), ep);
+    return launch_status();
 }
 
 }  // namespace
@@ -251,8 +350,16 @@ c3l_status c3l_scatter_padded(int64_t count, const int64_t* dst, const int64_t* 
                               const c3l_complex* vec, c3l_complex* ws, void* stream) {
     if (count < 0 || (count > 0 && (!dst || !pos || !sign || !vec || !ws))) return C3L_ERR_ARGUMENT;
     if (count == 0) return C3L_OK;
-    k_scatter<<<grid_for(count), kThreads, 0, as_stream(stream)>>>(count, dst, pos, sign, reinterpret_cast<const double2*>(vec),
-                                                                  reinterpret_cast<double2*>(ws));
+    k_scatter<double2><<<grid_for(count), kThreads, 0, as_stream(stream)>>>(
+        count, dst, pos, sign, reinterpret_cast<const double2*>(vec), reinterpret_cast<double2*>(ws));
+    return launch_status();
+}
+
+c3l_status c3l_downcast(int64_t count, const c3l_complex* src, c3l_complex32* dst, void* stream) {
+    if (count < 0 || (count > 0 && (!src || !dst))) return C3L_ERR_ARGUMENT;
+    if (count == 0) return C3L_OK;
+    k_downcast<<<grid_for(count), kThreads, 0, as_stream(stream)>>>(count, reinterpret_cast<const double2*>(src),
+                                                                   reinterpret_cast<float2*>(dst));
     return launch_status();
 }
 
@@ -260,8 +367,8 @@ c3l_status c3l_contract(const c3l_contract_level* level, int32_t n, const c3l_co
                         void* stream) {
     if (!level || !vectors || !ws || n <= 0 || n > 255) return C3L_ERR_ARGUMENT;
     if (level->ntiles <= 0) return C3L_OK;
-    k_contract<<<(unsigned)level->ntiles, kThreads, 0, as_stream(stream)>>>(*level, n, reinterpret_cast<const double2*>(vectors),
-                                                                           reinterpret_cast<double2*>(ws));
+    k_contract<double2><<<(unsigned)level->ntiles, kThreads, 0, as_stream(stream)>>>(
+        *level, n, reinterpret_cast<const double2*>(vectors), reinterpret_cast<double2*>(ws));
     return launch_status();
 }
 
@@ -269,7 +376,8 @@ c3l_status c3l_wedge_padded(const c3l_wedge_stage* stage, int32_t n, c3l_complex
     if (!stage || !ws || n <= 0 || n > 255) return C3L_ERR_ARGUMENT;
     if (stage->ntiles <= 0) return C3L_OK;
     Epilogue ep{};
-    k_wedge<kPadded><<<(unsigned)stage->ntiles, kThreads, 0, as_stream(stream)>>>(*stage, n, reinterpret_cast<double2*>(ws), ep);
+    k_wedge<kPadded, double2><<<(unsigned)stage->ntiles, kThreads, 0, as_stream(stream)>>>(
+        *stage, n, reinterpret_cast<double2*>(ws), ep);
     return launch_status();
 }
 
@@ -285,7 +393,7 @@ c3l_status c3l_wedge_static_out(const c3l_wedge_stage* stage, int32_t n, const c
     ep.pair = pair;
     ep.scale = reinterpret_cast<const double2*>(scale);
     ep.xout = xout;
-    k_wedge<kStatic><<<(unsigned)stage->ntiles, kThreads, 0, as_stream(stream)>>>(
+    k_wedge<kStatic, double2><<<(unsigned)stage->ntiles, kThreads, 0, as_stream(stream)>>>(
         *stage, n, const_cast<double2*>(reinterpret_cast<const double2*>(ws)), ep);
     return launch_status();
 }
@@ -298,7 +406,7 @@ c3l_status c3l_wedge_eom_out(const c3l_wedge_stage* stage, int32_t n, const c3l_
     ep.lam = reinterpret_cast<const double2*>(lam);
     ep.src = reinterpret_cast<const double2*>(xin);
     ep.cout = reinterpret_cast<double2*>(out);
-    k_wedge<kEom><<<(unsigned)stage->ntiles, kThreads, 0, as_stream(stream)>>>(
+    k_wedge<kEom, double2><<<(unsigned)stage->ntiles, kThreads, 0, as_stream(stream)>>>(
         *stage, n, const_cast<double2*>(reinterpret_cast<const double2*>(ws)), ep);
     return launch_status();
 }
@@ -310,45 +418,37 @@ c3l_status c3l_wedge_source_out(const c3l_wedge_stage* stage, int32_t n, const c
     Epilogue ep{};
     ep.cscale = make_double2(scale.re, scale.im);
     ep.cout = reinterpret_cast<double2*>(out);
-    k_wedge<kSource><<<(unsigned)stage->ntiles, kThreads, 0, as_stream(stream)>>>(
+    k_wedge<kSource, double2><<<(unsigned)stage->ntiles, kThreads, 0, as_stream(stream)>>>(
         *stage, n, const_cast<double2*>(reinterpret_cast<const double2*>(ws)), ep);
     return launch_status();
 }
 
 c3l_status c3l_action_prepare(const c3l_action* action, const c3l_complex* t, void* stream) {
     if (!valid_action(action) || !t) return C3L_ERR_ARGUMENT;
-    cudaStream_t s = as_stream(stream);
-    c3l_status st = scatter(action, t, s);
-    if (st) return st;
-    if ((st = run_levels(action, s))) return st;
-    return run_padded(action, s);
+    return action_prepare<double2>(action, t, as_stream(stream));
+}
+
+c3l_status c3l_action_prepare_f32(const c3l_action* action, const c3l_complex* t, void* stream) {
+    if (!valid_action(action) || !t) return C3L_ERR_ARGUMENT;
+    return action_prepare<float2>(action, t, as_stream(stream));
 }
 
 c3l_status c3l_static_apply(const c3l_static_action* sa, const double* x, double* xout, void* stream) {
-    if (!sa || !x || !xout || !valid_action(&sa->action) || !sa->canon || !sa->tilde_ia || !sa->tilde_ib ||
-        !sa->tilde_ca || !sa->tilde_cb || sa->num_amplitudes <= 0)
-        return C3L_ERR_ARGUMENT;
-    cudaStream_t s = as_stream(stream);
-    c3l_status st = c3l_tilde_unpack(sa->num_amplitudes, x, sa->tilde_ia, sa->tilde_ib, sa->tilde_ca, sa->tilde_cb,
-                                     sa->canon, stream);
-    if (st) return st;
-    if ((st = scatter(&sa->action, sa->canon, s))) return st;
-    if ((st = run_levels(&sa->action, s))) return st;
-    if ((st = run_padded(&sa->action, s))) return st;
-    return c3l_wedge_static_out(&sa->action.out, sa->action.n, sa->action.ws, sa->lam, sa->canon, sa->col, sa->pair,
-                                sa->scale, xout, stream);
+    return static_apply<double2>(sa, x, xout, stream);
+}
+
+c3l_status c3l_static_apply_f32(const c3l_static_action* sa, const double* x, double* xout, void* stream) {
+    return static_apply<float2>(sa, x, xout, stream);
 }
 
 c3l_status c3l_eom_sigma(const c3l_eom_action* ea, const c3l_complex* xin, c3l_complex* out, void* stream) {
-    if (!ea || !xin || !out || !valid_action(&ea->action) || !ea->lam) return C3L_ERR_ARGUMENT;
-    cudaStream_t s = as_stream(stream);
-    c3l_status st = scatter(&ea->action, xin, s);
-    if (st) return st;
-    if ((st = run_levels(&ea->action, s))) return st;
-    if ((st = run_padded(&ea->action, s))) return st;
-    return c3l_wedge_eom_out(&ea->action.out, ea->action.n, ea->action.ws, ea->lam, xin, out, stream);
+    return eom_sigma<double2>(ea, xin, out, stream);
 }
 
-const char* c3l_version(void) { return "c3l_gb300 0.1.0 (sm_103a, fp64 complex programs)"; }
+c3l_status c3l_eom_sigma_f32(const c3l_eom_action* ea, const c3l_complex* xin, c3l_complex* out, void* stream) {
+    return eom_sigma<float2>(ea, xin, out, stream);
+}
+
+const char* c3l_version(void) { return "c3l_gb300 0.2.0 (sm_103a, fp64/fp32 complex programs)"; }
 
 }  // extern "C"

@@ -44,9 +44,9 @@ class DeviceStatic:
         self.canon_R = _cz(self.A, self.device)
         self.canon_V = _cz(self.A, self.device)
 
-        def static_action(ws, levels_cls, padded, out, scatter, canon, ep):
+        def static_action(ws, levels_cls, padded, out, scatter, canon, ep, vectors=vec):
             sa = rt.StaticAction()
-            sa.action = rt.build_action(up, prog, vec.data_ptr(), ws, levels_cls, padded, out, scatter)
+            sa.action = rt.build_action(up, prog, vectors.data_ptr(), ws, levels_cls, padded, out, scatter)
             sa.num_amplitudes = self.A
             sa.tilde_ia, sa.tilde_ib = ia.data_ptr(), ib.data_ptr()
             sa.tilde_ca, sa.tilde_cb = ca.data_ptr(), cb.data_ptr()
@@ -63,6 +63,11 @@ class DeviceStatic:
                                         plan.scatter_T, self.canon_T, plan.epilogue)
         self.jvp_action = static_action(self.ws_lin, "V", ["jvp_rest_V", "jvp_scalar"], "jvp", plan.scatter_V,
                                         self.canon_V, plan.epilogue_jvp)
+        # single-precision twin of the JVP (inner operator of the mixed-precision solve)
+        self.vec32 = up.raw(prog.vectors.astype(np.complex64))
+        self.ws32_lin = torch.zeros(max(prog.ws_size, 1), dtype=torch.complex64, device=self.device)
+        self.jvp32_action = static_action(self.ws32_lin, "V", ["jvp_rest_V", "jvp_scalar"], "jvp", plan.scatter_V,
+                                          self.canon_V, plan.epilogue_jvp, vectors=self.vec32)
         # complex outputs at every coordinate (arbitrary complex amplitudes)
         self.cres_action = rt.build_action(up, prog, vec.data_ptr(), self.ws_res, "T", ["res_rest_T", "res_scalar"],
                                            None, plan.scatter_T)
@@ -106,6 +111,20 @@ class DeviceStatic:
     def jvp(self, v: torch.Tensor, out: torch.Tensor) -> None:
         """Exact JVP at the last linearization point."""
         self._apply(self.jvp_action, v, out, "static JVP", self.launches["jvp"])
+
+    def to_single(self) -> None:
+        """Copy the linearization workspace into its FP32 twin (after ``linearize``)."""
+        rt.check(self.lib.c3l_downcast(self.ws_lin.numel(), self.ws_lin.data_ptr(), self.ws32_lin.data_ptr(),
+                                       self._stream()), "downcast")
+        rt.LaunchCounter.add(1)
+
+    def jvp32(self, v: torch.Tensor, out: torch.Tensor) -> None:
+        """JVP with FP32 contractions at the last linearization point (after ``to_single``)."""
+        if v.dtype != torch.float64 or out.dtype != torch.float64 or v.numel() != self.D or out.numel() != self.D:
+            raise ValueError(f"jvp32: expected float64 vectors of length {self.D}")
+        rt.check(self.lib.c3l_static_apply_f32(C.byref(self.jvp32_action), v.data_ptr(), out.data_ptr(),
+                                               self._stream()), "static JVP (fp32)")
+        rt.LaunchCounter.add(self.launches["jvp"])
 
     def precondition(self, x: torch.Tensor, out: torch.Tensor) -> None:
         rt.check(self.lib.c3l_precondition(self.nrep, self.pc_m4.data_ptr(), self.pc_col.data_ptr(),

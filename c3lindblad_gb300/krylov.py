@@ -165,10 +165,12 @@ class DeviceGMRES:
         self.host = torch.zeros(3 * (r + 2) + 4, dtype=torch.float64).pin_memory()
         self.history = np.zeros(4096, dtype=np.float64)
 
-    def solve(self, b: torch.Tensor, x: torch.Tensor, *, rtol: float, atol: float, maxiter: int):
+    def solve(self, b: torch.Tensor, x: torch.Tensor, *, rtol: float, atol: float, maxiter: int,
+              single: bool = False):
         ops = self.ops
         a = rt.GmresArgs()
-        a.jvp = C.addressof(ops.jvp_action)
+        a.jvp = C.addressof(ops.jvp32_action if single else ops.jvp_action)
+        a.use_f32 = 1 if single else 0
         a.nrep = ops.nrep
         a.pc_m4, a.pc_col, a.pc_pair = ops.pc_m4.data_ptr(), ops.pc_col.data_ptr(), ops.pc_pair.data_ptr()
         a.dim = ops.D

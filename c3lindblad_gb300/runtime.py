@@ -61,7 +61,7 @@ class GmresArgs(C.Structure):
                 ("V", C.c_void_p), ("tmp", C.c_void_p), ("r", C.c_void_p), ("coeff", C.c_void_p),
                 ("partial", C.c_void_p), ("host", C.c_void_p), ("history", C.c_void_p),
                 ("history_capacity", C.c_int32), ("history_len", C.c_int32), ("info", C.c_int32),
-                ("matvecs", C.c_int32)]
+                ("matvecs", C.c_int32), ("use_f32", C.c_int32)]
 
 
 class ArnoldiChannel(C.Structure):
@@ -79,7 +79,8 @@ EXPORTS = (
     "c3l_multi_dot_scratch", "c3l_multi_dot_c", "c3l_multi_dot_r", "c3l_multi_axpy_c", "c3l_multi_axpy_r",
     "c3l_scale_c", "c3l_scale_r", "c3l_precondition", "c3l_hessenberg_shifted", "c3l_hessenberg_coordinates",
     "c3l_hessenberg_coordinates_noalloc", "c3l_gmres", "c3l_arnoldi", "c3l_hessenberg_residual_f32",
-    "c3l_arnoldi_column", "c3l_version",
+    "c3l_arnoldi_column", "c3l_static_apply_f32", "c3l_eom_sigma_f32", "c3l_action_prepare_f32", "c3l_downcast",
+    "c3l_version",
 )
 
 
@@ -107,6 +108,10 @@ def _declare(lib) -> None:
         "c3l_hessenberg_coordinates": [P, I64, I32, P, I32, D, P, P, P],
         "c3l_hessenberg_coordinates_noalloc": [P, I64, I32, P, I32, D, P, P],
         "c3l_gmres": [P, P],
+        "c3l_static_apply_f32": [P, P, P, P],
+        "c3l_eom_sigma_f32": [P, P, P, P],
+        "c3l_action_prepare_f32": [P, P, P],
+        "c3l_downcast": [I64, P, P, P],
         "c3l_hessenberg_residual_f32": [P, I64, I32, P, I32, D, P, P],
         "c3l_arnoldi_column": [P, I32, P, I64, P, I64, I32, D, P],
         "c3l_arnoldi": [P, I32, I64, P, I32, I32, D, I32, I32, D, P],
@@ -181,6 +186,8 @@ class Uploader:
             host = torch.from_numpy(a.view(np.uint8).reshape(-1).copy())
         elif a.dtype == np.complex128:
             host = torch.from_numpy(a.view(np.float64).reshape(-1).copy())
+        elif a.dtype == np.complex64:
+            host = torch.from_numpy(a.view(np.float32).reshape(-1).copy())
         else:
             host = torch.from_numpy(a.reshape(-1).copy())
         t = host.to(self.device, non_blocking=False)

@@ -280,9 +280,13 @@ def _acceptable_inexact_newton_step(r_norm: float, merit_slope: float, defect_no
                 and merit_slope < 0.0)
 
 
+MIXED_GMRES_FLOOR = 1.0e-6
+
+
 def solve_component_ccsd(problem, initial_amplitudes=None, *, policy: NewtonKrylovPolicy | None = None,
                          rank6_tile_size: int = 4096, compute_rank6: bool = False,
-                         accepted_step_callback: Callable | None = None, warm_start=None) -> ComponentCCSolution:
+                         accepted_step_callback: Callable | None = None, warm_start=None,
+                         precision: str = "fp64") -> ComponentCCSolution:
     """Solve the tilde-real CCSD equations with device residuals and JVPs.
 
     Control flow, forcing terms, Armijo backtracking and the final
@@ -291,7 +295,16 @@ def solve_component_ccsd(problem, initial_amplitudes=None, *, policy: NewtonKryl
     ``c3lindblad_gb300.warmstart``); it is ignored when
     ``initial_amplitudes`` is given, and convergence of the plain residual
     decides the answer either way.
+
+    ``precision="mixed"`` applies the JVP inside GMRES with FP32 contractions
+    (the GMRES tolerance is floored at 1e-6, the accuracy of that operator)
+    while every residual, the line search and the true linear defect stay
+    FP64 -- iterative refinement, so the converged amplitudes meet the same
+    FP64 residual tolerance.
     """
+    if precision not in ("fp64", "mixed"):
+        raise ValueError("precision must be 'fp64' or 'mixed'")
+    mixed = precision == "mixed"
     if compute_rank6:
         raise NotImplementedError("the rank-six truncation diagnostic is not part of the GPU path")
     controls = NewtonKrylovPolicy() if policy is None else policy
@@ -333,6 +346,8 @@ def solve_component_ccsd(problem, initial_amplitudes=None, *, policy: NewtonKryl
     for iteration in range(controls.maximum_newton_iterations + 1):
         ops.linearize(x, r)
         residual_evaluations += 1
+        if mixed:
+            ops.to_single()
         norm = vec.norm_r(r)
         if norm <= controls.tolerance:
             converged = True
@@ -342,8 +357,9 @@ def solve_component_ccsd(problem, initial_amplitudes=None, *, policy: NewtonKryl
         lin_tol = forcing_tolerance(norm, controls, previous_norm=prev_norm, previous_tolerance=prev_tol)
         lin_atol = 0.0 if controls.forcing_strategy == "legacy" else controls.gmres_absolute_tolerance_factor * controls.tolerance
         vec.scale_r(-1.0, r, negr)
-        info, gm_history, gm_matvecs = solver.solve(negr, step, rtol=lin_tol, atol=lin_atol,
-                                                    maxiter=controls.gmres_maximum_restart_cycles)
+        info, gm_history, gm_matvecs = solver.solve(negr, step, rtol=max(lin_tol, MIXED_GMRES_FLOOR) if mixed else lin_tol,
+                                                    atol=lin_atol, maxiter=controls.gmres_maximum_restart_cycles,
+                                                    single=mixed)
         jvp_count[0] += gm_matvecs
         matvec(step, jstep)
         # linear defect J s + r, merit slope r . J s, step norm

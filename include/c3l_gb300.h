@@ -30,6 +30,7 @@ enum {
 };
 
 typedef struct { double re, im; } c3l_complex;
+typedef struct { float re, im; } c3l_complex32;
 
 /* ---------------------------------------------------------- program tables
  * Built by c3lindblad_gb300/compiler.py (NumPy structured arrays with the
@@ -186,6 +187,17 @@ typedef struct {
 
 c3l_status c3l_eom_sigma(const c3l_eom_action* action, const c3l_complex* xin, c3l_complex* out, void* stream);
 
+/* Single-precision variants: the action's `vectors` and `ws` point to
+ * complex FP32 copies (c3l_complex32) of the factor-vector table and of the
+ * workspace; inputs, outputs and epilogues stay FP64.  They serve as the inner
+ * operator of the mixed-precision solves (the Newton residual stays FP64).
+ * c3l_downcast copies an FP64 workspace (e.g. after an FP64 linearization)
+ * into its FP32 twin. */
+c3l_status c3l_static_apply_f32(const c3l_static_action* action, const double* x, double* xout, void* stream);
+c3l_status c3l_eom_sigma_f32(const c3l_eom_action* action, const c3l_complex* xin, c3l_complex* out, void* stream);
+c3l_status c3l_action_prepare_f32(const c3l_action* action, const c3l_complex* t, void* stream);
+c3l_status c3l_downcast(int64_t count, const c3l_complex* src, c3l_complex32* dst, void* stream);
+
 /* Runs the amplitude-only part of an action (levels + padded stages) after
  * scattering the complex amplitude vector t; used for linearization and EOM
  * contexts (src/c3l/cc/component_tensor.py:1371-1549, :2234-2251). */
@@ -281,6 +293,8 @@ typedef struct {
     int32_t history_len;
     int32_t info;
     int32_t matvecs;
+    /* input: nonzero applies the JVP with c3l_static_apply_f32 */
+    int32_t use_f32;
 } c3l_gmres_args;
 
 c3l_status c3l_gmres(c3l_gmres_args* args, void* stream);

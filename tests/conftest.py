@@ -19,14 +19,28 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA device (GB300) and the built CUDA library")
 
 
-def golden_names(with_solution: bool = False):
+def golden_names(with_solution: bool = False, with_eom: bool = False, with_green: bool = False,
+                 compact: bool = False):
+    """Fixtures with full golden vectors (default) or compact sampled ones."""
     names = []
     for f in sorted(GOLDEN.glob("*.golden.npz")):
         name = f.name[: -len(".golden.npz")]
-        if with_solution and "solution_amplitudes" not in np.load(f).files:
+        files = np.load(f).files
+        if ("compact" in files) != compact:
+            continue
+        if with_solution and "solution_amplitudes" not in files:
+            continue
+        if with_eom and "eomp_sigma" not in files and "eomp_sigma_sample" not in files:
+            continue
+        if with_green and "green_retarded" not in files:
             continue
         names.append(name)
     return names
+
+
+def eom_amplitudes(g):
+    """Amplitudes at which the reference evaluated its EOM goldens."""
+    return g["eom_amplitudes"] if "eom_amplitudes" in g else g["solution_amplitudes"]
 
 
 def load(name: str):

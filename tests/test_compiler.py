@@ -12,7 +12,7 @@ import ctypes
 import numpy as np
 import pytest
 
-from conftest import golden_names, load, relerr
+from conftest import eom_amplitudes, golden_names, load, relerr
 from c3lindblad_gb300 import compiler, layout
 from c3lindblad_gb300.plans import EOMPlan, StaticPlan
 from oracle import component_oracle as oc
@@ -80,13 +80,13 @@ def test_compiled_residual_and_jvp(name, plans):
     assert abs(jref - g["jvp_reference"]) < 1e-12 * max(1.0, abs(g["jvp_reference"]))
 
 
-@pytest.mark.parametrize("name", golden_names(with_solution=True))
+@pytest.mark.parametrize("name", golden_names(with_eom=True))
 @pytest.mark.parametrize("charge", [1, -1])
 def test_compiled_sigma_and_sources(name, charge, plans):
     spec, g, plan = plans(name)
     tag = "p" if charge == 1 else "m"
     ep = EOMPlan(plan, 0, charge)
-    it = InterpretedEOM(ep, g["solution_amplitudes"])
+    it = InterpretedEOM(ep, eom_amplitudes(g))
     assert relerr(ep.diagonal, g[f"eom{tag}_diagonal"]) < 1e-14
     assert relerr(it.sigma(g[f"eom{tag}_probe"]), g[f"eom{tag}_sigma"]) < 1e-12
     add, rem, sink = it.sources(spec.impurity_site)

@@ -11,7 +11,7 @@ from __future__ import annotations
 import numpy as np
 import pytest
 
-from conftest import golden_names, load, relerr
+from conftest import eom_amplitudes, golden_names, load, relerr
 
 pytestmark = pytest.mark.gpu
 
@@ -89,7 +89,7 @@ def test_complex_residual_accepts_non_tilde_amplitudes(problems):
     assert relerr(c3.component_static_jvp(p, t, v).retained, o.jvp(t, v)[0]) < 1e-12
 
 
-@pytest.mark.parametrize("name", golden_names(with_solution=True))
+@pytest.mark.parametrize("name", golden_names(with_eom=True))
 @pytest.mark.parametrize("charge", [1, -1])
 def test_device_sigma_and_sources(name, charge, problems):
     import c3lindblad_gb300 as c3
@@ -98,7 +98,7 @@ def test_device_sigma_and_sources(name, charge, problems):
     tag = "p" if charge == 1 else "m"
     eom = c3.eom_ccsd_problem(p)
     ep = c3.ComponentEOMProblem.compile(eom, p, charge)
-    ctx = c3.component_eom_context(ep, g["solution_amplitudes"])
+    ctx = c3.component_eom_context(ep, eom_amplitudes(g))
     op = c3.ComponentSigmaOperator(ctx)
     assert op.dimension == g[f"eom{tag}_probe"].size
     assert relerr(op.diagonal, g[f"eom{tag}_diagonal"]) < 1e-14
@@ -124,7 +124,7 @@ def test_newton_krylov_solution_matches_reference(name, problems):
     assert again.converged and again.iterations == 0
 
 
-@pytest.mark.parametrize("name", [n for n in golden_names(with_solution=True)])
+@pytest.mark.parametrize("name", golden_names(with_green=True))
 def test_retarded_green_matches_reference(name, problems):
     import c3lindblad_gb300 as c3
 
@@ -191,3 +191,79 @@ def test_krylov_primitives_against_numpy(cuda_device):
     assert st == 0
     want = np.array([abs(H[m, m - 1] * y[-1]) / 2.5 for y in ys])
     assert np.max(np.abs(r32.cpu().numpy() - want) / want) < 1e-3
+
+
+# ------------------------------------------------------------ large fixtures
+def _fixed_inputs(plan, scale):
+    t = plan.tilde
+    idx = np.arange(plan.num_variables, dtype=np.float64)
+    x = scale * np.cos(idx + 0.13)
+    d = 0.2 * np.sin(idx + 0.31)
+    unpack = lambda v: t.coef_a * v[t.idx_a] + t.coef_b * v[t.idx_b]
+    return unpack(x), unpack(d)
+
+
+def _close(got, want, norm, tol):
+    return np.linalg.norm(got - want) <= tol * max(np.linalg.norm(want), 1e-300) and \
+        np.max(np.abs(got - want)) <= tol * norm
+
+
+@pytest.mark.parametrize("name", golden_names(compact=True))
+def test_large_fixture_residual_jvp_sigma_at_sampled_coordinates(name, problems):
+    """n = 27 Kanamori (779,301 amplitudes): reference outputs at 4,096 sampled coordinates."""
+    import c3lindblad_gb300 as c3
+
+    spec, g, p = problems(name)
+    T, D = _fixed_inputs(p.plan, float(g["scale"]))
+    pos = g["sample_positions"]
+    res = c3.component_static_residual(p, T)
+    assert _close(res.retained[pos], g["residual_sample"], float(g["residual_norm"]), 1e-11)
+    assert abs(np.linalg.norm(res.retained) - g["residual_norm"]) <= 1e-11 * g["residual_norm"]
+    jvp = c3.component_static_jvp(p, T, D)
+    assert _close(jvp.retained[pos], g["jvp_sample"], float(g["jvp_norm"]), 1e-11)
+    assert abs(np.linalg.norm(jvp.retained) - g["jvp_norm"]) <= 1e-11 * g["jvp_norm"]
+    for charge, tag in ((1, "p"), (-1, "m")):
+        if f"eom{tag}_sigma_sample" not in g:
+            continue
+        ep = c3.ComponentEOMProblem.compile(c3.eom_ccsd_problem(p), p, charge)
+        ctx = c3.component_eom_context(ep, T)
+        op = c3.ComponentSigmaOperator(ctx)
+        assert op.dimension == int(g[f"eom{tag}_dimension"])
+        k = np.arange(op.dimension, dtype=np.float64)
+        probe = np.cos(0.7 * k + 0.2) + 1j * np.sin(0.3 * k - 0.1)
+        sig = op.matvec(probe)
+        ep_pos = g[f"eom{tag}_sample_positions"]
+        assert _close(sig[ep_pos], g[f"eom{tag}_sigma_sample"], float(g[f"eom{tag}_sigma_norm"]), 1e-11)
+        assert abs(np.linalg.norm(sig) - g[f"eom{tag}_sigma_norm"]) <= 1e-11 * g[f"eom{tag}_sigma_norm"]
+        src = c3.component_eom_sources(ctx)
+        for key, val in (("addition", src.addition), ("removal", src.removal), ("sink", src.sink),
+                         ("diagonal", op.diagonal)):
+            want = g[f"eom{tag}_{key}_sample"]
+            assert np.max(np.abs(val[ep_pos] - want)) <= 1e-12 * max(1.0, np.max(np.abs(want)))
+
+
+@pytest.mark.parametrize("name", [n for n in golden_names(with_solution=True)])
+def test_mixed_precision_solve_meets_fp64_tolerance(name, problems):
+    """FP32 inner JVPs with FP64 residuals converge to the FP64 reference root."""
+    import c3lindblad_gb300 as c3
+
+    spec, g, p = problems(name)
+    sol = c3.solve_component_ccsd(p, precision="mixed")
+    assert sol.converged and sol.packed_residual_norm <= 1e-10
+    assert relerr(sol.amplitudes, g["solution_amplitudes"]) < 1e-8
+
+
+def test_single_precision_jvp_tracks_fp64(problems, cuda_device):
+    spec, g, p = problems("siam10")
+    ops = p.ops
+    x = torch.from_numpy(g["fixed_variables"]).to(cuda_device)
+    d = torch.from_numpy(g["fixed_direction_variables"]).to(cuda_device)
+    r = torch.empty_like(x)
+    ops.linearize(x, r)
+    ops.to_single()
+    j64 = torch.empty_like(x)
+    j32 = torch.empty_like(x)
+    ops.jvp(d, j64)
+    ops.jvp32(d, j32)
+    err = relerr(j32.cpu().numpy(), j64.cpu().numpy())
+    assert 0 < err < 1e-5
