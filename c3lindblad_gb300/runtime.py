@@ -80,7 +80,7 @@ EXPORTS = (
     "c3l_scale_c", "c3l_scale_r", "c3l_precondition", "c3l_hessenberg_shifted", "c3l_hessenberg_coordinates",
     "c3l_hessenberg_coordinates_noalloc", "c3l_gmres", "c3l_arnoldi", "c3l_hessenberg_residual_f32",
     "c3l_arnoldi_column", "c3l_static_apply_f32", "c3l_eom_sigma_f32", "c3l_action_prepare_f32", "c3l_downcast",
-    "c3l_version",
+    "c3l_mlp_forward", "c3l_mlp_backward", "c3l_mlp_adam", "c3l_warm_features", "c3l_warm_apply", "c3l_version",
 )
 
 
@@ -112,6 +112,11 @@ def _declare(lib) -> None:
         "c3l_eom_sigma_f32": [P, P, P, P],
         "c3l_action_prepare_f32": [P, P, P],
         "c3l_downcast": [I64, P, P, P],
+        "c3l_mlp_forward": [I64, P, P, P, P],
+        "c3l_mlp_backward": [I64, P, P, P, C.c_float, P, P, P, P],
+        "c3l_mlp_adam": [P, P, P, P, C.c_float, C.c_float, C.c_float, C.c_float, I32, P, P],
+        "c3l_warm_features": [I64, P, P, P, P, P, P, D, D, P, P],
+        "c3l_warm_apply": [I64, P, P, P, P, D, P, P],
         "c3l_hessenberg_residual_f32": [P, I64, I32, P, I32, D, P, P],
         "c3l_arnoldi_column": [P, I32, P, I64, P, I64, I32, D, P],
         "c3l_arnoldi": [P, I32, I64, P, I32, I32, D, I32, I32, D, P],

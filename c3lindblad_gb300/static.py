@@ -319,8 +319,18 @@ def solve_component_ccsd(problem, initial_amplitudes=None, *, policy: NewtonKryl
     if initial_amplitudes is not None:
         x = torch.from_numpy(p.pack(initial_amplitudes)).to(dev)
     elif warm_start is not None:
+        # the learned guess is kept only if its FP64 residual beats the zero guess
         x = warm_start.initial_variables(p)
-        warm_label = getattr(warm_start, "label", "learned")
+        rw = torch.empty(D, dtype=torch.float64, device=dev)
+        ops.residual(x, rw)
+        zero = torch.zeros(D, dtype=torch.float64, device=dev)
+        r0 = torch.empty(D, dtype=torch.float64, device=dev)
+        ops.residual(zero, r0)
+        if vec.norm_r(rw) < vec.norm_r(r0):
+            warm_label = getattr(warm_start, "label", "learned")
+        else:
+            x = zero
+            warm_label = "rejected"
     else:
         x = torch.zeros(D, dtype=torch.float64, device=dev)
     pre = RapidityPreconditionerDiagnostics(**ops.preconditioner_diagnostics)

@@ -337,6 +337,40 @@ c3l_status c3l_arnoldi(c3l_arnoldi_channel* channels, int32_t nchannels, int64_t
                        int32_t nshift, int32_t m_max, double tol, int32_t min_dim, int32_t check_interval,
                        double breakdown_tol, void* const* streams);
 
+/* ------------------------------------------------------- learned warm start
+ * An element-wise MLP (C3L_MLP_INPUTS -> HIDDEN -> HIDDEN -> OUTPUTS, tanh)
+ * mapping per-amplitude features to a correction of the first-order guess.
+ * BF16 inputs/weights/activations, FP32 accumulation.  Parameters are laid
+ * out W1[H][F] b1[H] W2[H][H] b2[H] W3[O][H] b3[O].  No counterpart in the
+ * reference, whose solve starts from zero amplitudes
+ * (src/c3l/cc/component_solver.py:121-122); the converged answer is still
+ * judged by the FP64 residual, and the zero guess remains the fallback. */
+#define C3L_MLP_INPUTS 16
+#define C3L_MLP_HIDDEN 32
+#define C3L_MLP_OUTPUTS 2
+#define C3L_MLP_PARAMS (C3L_MLP_HIDDEN * C3L_MLP_INPUTS + C3L_MLP_HIDDEN + C3L_MLP_HIDDEN * C3L_MLP_HIDDEN + \
+                        C3L_MLP_HIDDEN + C3L_MLP_OUTPUTS * C3L_MLP_HIDDEN + C3L_MLP_OUTPUTS)
+
+/* Y[n][O] (FP32) from X[n][F] (BF16) and BF16 weights. */
+c3l_status c3l_mlp_forward(int64_t n, const void* X, const void* weights_bf16, float* Y, void* stream);
+/* Adds d/dparams of sum_s w_s |y_s - t_s|^2 * inv_wsum into grad[PARAMS] (FP32,
+ * caller zeroes it) and the unscaled weighted loss into loss[0]; W may be NULL
+ * (unit weights).  Accumulation order across blocks is not fixed. */
+c3l_status c3l_mlp_backward(int64_t n, const void* X, const float* T, const float* W, float inv_wsum,
+                            const void* weights_bf16, float* grad, float* loss, void* stream);
+/* One Adam step (bias-corrected, step >= 1) on FP32 params; refreshes the BF16 copy. */
+c3l_status c3l_mlp_adam(float* params, const float* grad, float* m, float* v, float lr, float beta1, float beta2,
+                        float eps, int32_t step, void* weights_bf16, void* stream);
+/* Features of each tilde-orbit representative: modes[nrep][4] (-1 padded),
+ * the first two Jacobi iterates t1, t2 (real tilde coordinates), scale sigma
+ * and interaction scale u. */
+c3l_status c3l_warm_features(int64_t nrep, const int64_t* modes, const int64_t* col, const int64_t* pair,
+                             const c3l_complex* rapidities, const double* t1, const double* t2, double sigma,
+                             double u, void* X, void* stream);
+/* x0 = t1 + sigma * Y at every representative's real columns. */
+c3l_status c3l_warm_apply(int64_t nrep, const int64_t* col, const int64_t* pair, const double* t1, const float* Y,
+                          double sigma, double* x0, void* stream);
+
 /* Allocation-free variant of c3l_hessenberg_coordinates, for callers that
  * cannot allocate device memory: a host application that owns the device
  * memory budget (and hands this library only its input and output buffers),

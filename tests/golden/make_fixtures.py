@@ -352,6 +352,39 @@ def _export_eom(g, cc, static, amplitudes, fx, name, _unused) -> None:
             print(f"  [{name}] green {g['green_seconds']:.2f}s ({op.action_calls} sigma calls)", flush=True)
 
 
+def export_warmstart_family(count: int, path: Path) -> None:
+    """Seeded SIAM models (10 pseudomodes, U uniform in [2, 6]) for the learned warm start.
+
+    Only the problem specs are exported: the training targets are the
+    amplitudes the GPU solver itself produces on these models.
+    """
+    from c3l import FermionicLindbladModel
+    from c3l.cc.factorized import factorized_cc_problem
+
+    out = {"count": np.int64(count)}
+    for i in range(count):
+        rng = np.random.default_rng(1000 + i)
+        U = float(rng.uniform(2.0, 6.0))
+        nm = 10
+        eb = rng.uniform(-3, 3, nm)
+        V = rng.normal(0, 0.3, nm)
+        r = rng.uniform(0.05, 0.5, nm)
+        f = 1.0 / (np.exp(eb / 0.1) + 1.0)
+        E = np.diag(np.r_[-U / 2, eb]).astype(complex)
+        E[0, 1:] = V
+        E[1:, 0] = V
+        model = FermionicLindbladModel(E, np.diag(np.r_[0, r * (1 - f)]), np.diag(np.r_[0, r * f]), U=U)
+        cc = factorized_cc_problem(model, "CCSD", m_up=0.5, reference_mode="legacy_half_filled")
+        tmp = HERE / "_tmp_ws.npz"
+        spec = export_spec(cc, tmp, "legacy_half_filled:0.5")
+        tmp.unlink()
+        for k, v in spec.items():
+            out[f"m{i}_{k}"] = v
+        out[f"m{i}_U"] = np.float64(U)
+        print(f"  warm-start model {i}: U={U:.3f}", flush=True)
+    np.savez_compressed(path, **out)
+
+
 COMPACT_SAMPLES = 4096
 
 
@@ -396,6 +429,9 @@ def main() -> None:
     parser.add_argument("names", nargs="*")
     args = parser.parse_args()
     _import_reference(args.reference)
+    if args.names == ["warmstart"]:
+        export_warmstart_family(64, HERE / "warmstart_siam.npz")
+        return
     names = args.names or list(FIXTURES)
     for name in names:
         fx = FIXTURES[name]
