@@ -398,6 +398,23 @@ c3l_status c3l_wedge_static_out(const c3l_wedge_stage* stage, int32_t n, const c
     return launch_status();
 }
 
+c3l_status c3l_wedge_static_out_f32(const c3l_wedge_stage* stage, int32_t n, const c3l_complex32* ws,
+                                    const c3l_complex* lam, const c3l_complex* src, const int64_t* col,
+                                    const int64_t* pair, const c3l_complex* scale, double* xout, void* stream) {
+    if (!stage || !ws || !lam || !src || !col || !pair || !scale || !xout || n <= 0 || n > 255) return C3L_ERR_ARGUMENT;
+    if (stage->ntiles <= 0) return C3L_OK;
+    Epilogue ep{};
+    ep.lam = reinterpret_cast<const double2*>(lam);
+    ep.src = reinterpret_cast<const double2*>(src);
+    ep.col = col;
+    ep.pair = pair;
+    ep.scale = reinterpret_cast<const double2*>(scale);
+    ep.xout = xout;
+    k_wedge<kStatic, float2><<<(unsigned)stage->ntiles, kThreads, 0, as_stream(stream)>>>(
+        *stage, n, const_cast<float2*>(reinterpret_cast<const float2*>(ws)), ep);
+    return launch_status();
+}
+
 c3l_status c3l_wedge_eom_out(const c3l_wedge_stage* stage, int32_t n, const c3l_complex* ws, const c3l_complex* lam,
                              const c3l_complex* xin, c3l_complex* out, void* stream) {
     if (!stage || !ws || !lam || !xin || !out || n <= 0 || n > 255) return C3L_ERR_ARGUMENT;

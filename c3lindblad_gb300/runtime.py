@@ -80,7 +80,7 @@ EXPORTS = (
     "c3l_scale_c", "c3l_scale_r", "c3l_precondition", "c3l_hessenberg_shifted", "c3l_hessenberg_coordinates",
     "c3l_hessenberg_coordinates_noalloc", "c3l_gmres", "c3l_arnoldi", "c3l_hessenberg_residual_f32",
     "c3l_arnoldi_column", "c3l_static_apply_f32", "c3l_eom_sigma_f32", "c3l_action_prepare_f32", "c3l_downcast",
-    "c3l_mlp_forward", "c3l_mlp_backward", "c3l_mlp_adam", "c3l_warm_features", "c3l_warm_apply", "c3l_version",
+    "c3l_wedge_static_out_f32", "c3l_mlp_forward", "c3l_mlp_backward", "c3l_mlp_adam", "c3l_warm_features", "c3l_warm_apply", "c3l_version",
 )
 
 
@@ -93,6 +93,7 @@ def _declare(lib) -> None:
         "c3l_wedge_padded": [P, I32, P, P],
         "c3l_wedge_static_out": [P, I32, P, P, P, P, P, P, P, P],
         "c3l_wedge_eom_out": [P, I32, P, P, P, P, P],
+        "c3l_wedge_static_out_f32": [P, I32, P, P, P, P, P, P, P, P],
         "c3l_wedge_source_out": [P, I32, P, Complex, P, P],
         "c3l_action_prepare": [P, P, P],
         "c3l_static_apply": [P, P, P, P],

@@ -192,7 +192,28 @@ class LearnedWarmStart:
                                          Y.data_ptr(), float(sigma), x0.data_ptr(), rt.stream_ptr(t1.device)),
                  "warm apply")
         rt.LaunchCounter.add(1)
-        return x0
+        return self.safeguard(problem, x0)
+
+    @staticmethod
+    def safeguard(problem, x0: torch.Tensor, scales=(1.0, 0.5, 0.25, 0.125)) -> torch.Tensor:
+        """Backtrack along the guess: keep the scaled guess with the lowest FP64
+        residual, or the zero guess if none beats it."""
+        from .krylov import DeviceVectors
+
+        ops = problem.ops
+        vec = DeviceVectors(x0.device)
+        r = torch.empty_like(x0)
+        ops.residual(torch.zeros_like(x0), r)
+        best, best_norm = torch.zeros_like(x0), vec.norm_r(r)
+        trial = torch.empty_like(x0)
+        for a in scales:
+            vec.scale_r(a, x0, trial)
+            ops.residual(trial, r)
+            nrm = vec.norm_r(r)
+            if nrm < best_norm:
+                best_norm = nrm
+                best = trial.clone()
+        return best
 
 
 @dataclass

@@ -124,6 +124,11 @@ c3l_status c3l_wedge_static_out(const c3l_wedge_stage* stage, int32_t n, const c
                                 const int64_t* pair, const c3l_complex* scale, double* xout,
                                 void* stream);
 
+/* The same output stage over a complex FP32 workspace (FP64 epilogue). */
+c3l_status c3l_wedge_static_out_f32(const c3l_wedge_stage* stage, int32_t n, const c3l_complex32* ws,
+                                    const c3l_complex* lam, const c3l_complex* src, const int64_t* col,
+                                    const int64_t* pair, const c3l_complex* scale, double* xout, void* stream);
+
 /* EOM sigma outputs: out[mu] = lam * x[mu] + V
  * (src/c3l/cc/component_tensor.py:2288-2302). */
 c3l_status c3l_wedge_eom_out(const c3l_wedge_stage* stage, int32_t n, const c3l_complex* ws,
