@@ -47,7 +47,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     sources = sorted(CSRC.glob("*.cu"))
     header = INCLUDE / "c3l_gb300.h"
     out = library_path()
-    if not force and not _stale(out, sources + [header, Path(__file__)]):
+    if not force and not _stale(out, sources + sorted(CSRC.glob("*.h")) + [header, Path(__file__)]):
         return out
     compiler = nvcc()
     flags = [ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", f"-I{INCLUDE}"]

@@ -51,7 +51,9 @@ from .layout import Coordinates
 MAX_FACTORS = 6
 MAX_SOURCES = 4
 TILE = 256        # outputs per contraction tile (one thread each)
-WEDGE_TILE = 64   # outputs per wedge tile (instances split over 4 thread groups)
+WEDGE_WIDTHS = (64, 32, 16, 8)  # outputs per wedge tile; a block of 256 threads splits
+                                # each output's instances over 256 / width thread groups
+WEDGE_MIN_TILES = 608           # narrowest width reaching this many tiles (4 per GB300 SM)
 
 CONTRACT_DTYPE = np.dtype([
     ("dst_off", np.int64), ("deg", np.int32), ("nsrc", np.int32),
@@ -276,6 +278,7 @@ class Stage:
     elements: np.ndarray | None = None   # canonical: int64 vector positions
     digits: np.ndarray | None = None     # canonical: int32 packed index digits
     element_block: np.ndarray | None = None
+    width: int = 64                      # outputs per tile
 
 
 @dataclass
@@ -436,27 +439,28 @@ class Builder:
                 inst[i]["fac_deg"][j] = deg
                 for q, ax in enumerate(lst):
                     inst[i]["axes"][j][q] = ax
-        tiles = []
         if kind == "padded":
-            for b, (out_off, deg, rows) in enumerate(block_rows):
-                size = self.n ** deg
-                for s in range(0, size, WEDGE_TILE):
-                    tiles.append((b, min(WEDGE_TILE, size - s), s))
+            ranges = [(b, 0, self.n ** deg) for b, (out_off, deg, rows) in enumerate(block_rows)]
         else:
             eb = np.asarray(element_block)
             order_ok = np.all(np.diff(eb) >= 0)
             assert order_ok, "canonical elements must be grouped by block"
+            ranges = []
             for b in range(nb):
                 idx = np.flatnonzero(eb == b)
-                if idx.size == 0:
-                    continue
-                lo, hi = int(idx[0]), int(idx[-1]) + 1
-                for s in range(lo, hi, WEDGE_TILE):
-                    tiles.append((b, min(WEDGE_TILE, hi - s), s))
+                if idx.size:
+                    ranges.append((b, int(idx[0]), int(idx[-1]) + 1))
+        # the widest tile that still gives every SM several blocks
+        width = WEDGE_WIDTHS[-1]
+        for w in WEDGE_WIDTHS:
+            if sum(-(-(hi - lo) // w) for _, lo, hi in ranges) >= WEDGE_MIN_TILES:
+                width = w
+                break
+        tiles = [(b, min(width, hi - s), s) for b, lo, hi in ranges for s in range(lo, hi, width)]
         tarr = np.zeros(len(tiles), TILE_DTYPE)
         for i, (b, c, s) in enumerate(tiles):
             tarr[i] = (b, c, s)
-        self.stage_data[name] = Stage(name, kind, blocks, inst, tarr, elements, digits, element_block)
+        self.stage_data[name] = Stage(name, kind, blocks, inst, tarr, elements, digits, element_block, width)
 
     def finish(self) -> Program:
         levels = {}

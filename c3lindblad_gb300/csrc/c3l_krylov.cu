@@ -14,8 +14,10 @@
 #include <stdint.h>
 
 #include <mutex>
+#include <type_traits>
 
 #include "c3l_gb300.h"
+#include "c3l_internal.h"
 
 namespace {
 
@@ -91,6 +93,43 @@ __global__ void __launch_bounds__(kThreads) k_dot_partial_c(const double2* __res
     if (threadIdx.x == 0) partial[(int64_t)j * gridDim.x + blockIdx.x] = make_double2(re, im);
 }
 
+// Single pass for short vectors: one block per row reduces the whole row
+// (deterministic order), so no partial buffer or second launch is needed.
+// The Arnoldi basis of an EOM block is a few thousand entries long.
+constexpr int64_t kRowDotMax = 8192;
+
+__global__ void __launch_bounds__(kThreads) k_dot_rows_c(const double2* __restrict__ V, int64_t ld,
+                                                         const double2* __restrict__ w, int64_t dim,
+                                                         double2* __restrict__ out) {
+    __shared__ double sm[32];
+    const int j = blockIdx.x;
+    const double2* v = V + (int64_t)j * ld;
+    double re = 0.0, im = 0.0;
+    const int64_t step = blockDim.x;
+    int64_t i = threadIdx.x;
+    for (; i + 3 * step < dim; i += 4 * step) {  // four independent loads in flight
+        double2 a[4], b[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            a[u] = v[i + u * step];
+            b[u] = w[i + u * step];
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            re = fma(a[u].x, b[u].x, fma(a[u].y, b[u].y, re));
+            im = fma(a[u].x, b[u].y, fma(-a[u].y, b[u].x, im));
+        }
+    }
+    for (; i < dim; i += step) {
+        const double2 a = v[i], b = w[i];
+        re = fma(a.x, b.x, fma(a.y, b.y, re));
+        im = fma(a.x, b.y, fma(-a.y, b.x, im));
+    }
+    re = block_sum(re, sm);
+    im = block_sum(im, sm);
+    if (threadIdx.x == 0) out[j] = make_double2(re, im);
+}
+
 __global__ void __launch_bounds__(kThreads) k_dot_partial_r(const double* __restrict__ V, int64_t ld,
                                                             const double* __restrict__ w, int64_t dim,
                                                             double* __restrict__ partial) {
@@ -126,35 +165,55 @@ __global__ void k_dot_final_r(const double* __restrict__ partial, int nb, double
     if (threadIdx.x == 0) out[j] = s;
 }
 
-// w[i] += alpha * sum_j c[j] V[j, i]: a 32 x 8 block covers 32 consecutive
-// entries (coalesced in i) and splits the k rows over 8 thread rows, so a
-// short vector with a long basis (Arnoldi) still fills the GPU.
+// w[i] += alpha * sum_j c[j] V[j, i]: an X x Y block covers X consecutive
+// entries (coalesced in i) and splits the k rows over Y thread rows.  A long
+// basis over a short vector (Arnoldi on an EOM block) uses 4 x 64 blocks so
+// that the grid spans every SM; short bases use 32 x 8.
 constexpr int kAxX = 32, kAxY = 8;
+constexpr int kAxXLong = 4, kAxYLong = 64;
 
-__global__ void __launch_bounds__(kAxX * kAxY) k_axpy_c(const double2* __restrict__ V, int64_t ld, int k,
-                                                         const double2* __restrict__ c, double2 alpha,
-                                                         double2* __restrict__ w, int64_t dim) {
-    __shared__ double2 part[kAxY][kAxX];
-    for (int64_t base = (int64_t)blockIdx.x * kAxX; base < dim; base += (int64_t)gridDim.x * kAxX) {
+template <int X, int Y>
+__global__ void __launch_bounds__(X * Y) k_axpy_c(const double2* __restrict__ V, int64_t ld, int k,
+                                                   const double2* __restrict__ c, double2 alpha,
+                                                   double2* __restrict__ w, int64_t dim) {
+    __shared__ double2 part[Y][X];
+    for (int64_t base = (int64_t)blockIdx.x * X; base < dim; base += (int64_t)gridDim.x * X) {
         const int64_t i = base + threadIdx.x;
         double2 s = make_double2(0.0, 0.0);
         if (i < dim) {
-            for (int j = threadIdx.y; j < k; j += kAxY) {
-                const double2 p = cmul(c[j], V[(int64_t)j * ld + i]);
-                s.x += p.x;
-                s.y += p.y;
+            int j = threadIdx.y;
+            for (; j + 3 * Y < k; j += 4 * Y) {  // four independent loads in flight
+                double2 cj[4], v[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    cj[u] = c[j + u * Y];
+                    v[u] = V[(int64_t)(j + u * Y) * ld + i];
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    s.x = fma(cj[u].x, v[u].x, fma(-cj[u].y, v[u].y, s.x));
+                    s.y = fma(cj[u].x, v[u].y, fma(cj[u].y, v[u].x, s.y));
+                }
+            }
+            for (; j < k; j += Y) {
+                const double2 cj = c[j], v = V[(int64_t)j * ld + i];
+                s.x = fma(cj.x, v.x, fma(-cj.y, v.y, s.x));
+                s.y = fma(cj.x, v.y, fma(cj.y, v.x, s.y));
             }
         }
         part[threadIdx.y][threadIdx.x] = s;
         __syncthreads();
-        if (threadIdx.y == 0 && i < dim) {
-            double2 t = part[0][threadIdx.x];
-#pragma unroll
-            for (int y = 1; y < kAxY; ++y) {
-                t.x += part[y][threadIdx.x].x;
-                t.y += part[y][threadIdx.x].y;
+        // tree over the Y partial rows
+        for (int h = Y / 2; h > 0; h >>= 1) {
+            if ((int)threadIdx.y < h) {
+                const double2 o = part[threadIdx.y + h][threadIdx.x];
+                part[threadIdx.y][threadIdx.x].x += o.x;
+                part[threadIdx.y][threadIdx.x].y += o.y;
             }
-            const double2 a = cmul(alpha, t);
+            __syncthreads();
+        }
+        if (threadIdx.y == 0 && i < dim) {
+            const double2 a = cmul(alpha, part[0][threadIdx.x]);
             w[i] = make_double2(w[i].x + a.x, w[i].y + a.y);
         }
         __syncthreads();
@@ -207,8 +266,8 @@ __global__ void k_precondition(int64_t nrep, const double* __restrict__ m4, cons
     }
 }
 
-unsigned axpy_grid(int64_t dim) {
-    int64_t b = (dim + kAxX - 1) / kAxX;
+unsigned axpy_grid(int64_t dim, int x = kAxX) {
+    int64_t b = (dim + x - 1) / x;
     if (b > 8192) b = 8192;
     return (unsigned)(b < 1 ? 1 : b);
 }
@@ -248,6 +307,33 @@ __device__ __forceinline__ void givens(double2 a, double2 b, double& c, double2&
     const double2 ph = make_double2(a.x / na, a.y / na);
     s = cmul(ph, make_double2(b.x / rho, -b.y / rho));  // (a/|a|) conj(b) / rho
     r = make_double2(ph.x * rho, ph.y * rho);
+}
+
+// The same rotation with v = num / r, from two reciprocal square roots instead
+// of hypot and divisions: c = |a|/rho, s = ph conj(b)/rho, r = ph rho with
+// ph = a/|a|, hence num / r = num conj(ph) / rho.  Falls back to the careful
+// form when |a|^2 is outside the safe range.
+__device__ __forceinline__ void givens_fast(double2 a, double2 b, double2 num, bool want_v, double& c, double2& s,
+                                            double2& v) {
+    const double na2 = fma(a.x, a.x, a.y * a.y);
+    const double nb2 = fma(b.x, b.x, b.y * b.y);
+    if (!(na2 > 1e-280 && na2 < 1e280 && nb2 < 1e280)) {
+        double2 r;
+        givens(a, b, c, s, r);
+        v = want_v ? cdiv(num, r) : make_double2(0.0, 0.0);
+        return;
+    }
+    const double inv_na = rsqrt(na2);
+    const double inv_rho = rsqrt(na2 + nb2);
+    c = na2 * inv_na * inv_rho;
+    const double2 ph = make_double2(a.x * inv_na, a.y * inv_na);
+    s = cmul(ph, make_double2(b.x * inv_rho, -b.y * inv_rho));
+    if (want_v) {
+        const double2 t = cconjmul(ph, num);  // conj(ph) num
+        v = make_double2(t.x * inv_rho, t.y * inv_rho);
+    } else {
+        v = make_double2(0.0, 0.0);
+    }
 }
 
 // Streamed Givens QR of (z I - H_m) with the transposed forward solve
@@ -331,84 +417,171 @@ __global__ void __launch_bounds__(kHessThreads) k_hessenberg_shifted(const doubl
     }
 }
 
-// FP32 residual-only variant used for Arnoldi convergence checks: the same
-// streamed Givens elimination on (z I - H_m) rounded to single precision,
-// returning |h_{m,m-1} y_{m-1}| / beta.  Its relative error is ~cond * 1e-7,
-// ample for a stopping decision; a positive decision is confirmed in FP64.
-__global__ void __launch_bounds__(kHessThreads) k_hessenberg_residual_f32(const double2* __restrict__ H, int64_t ldh,
-                                                                          int m, const double2* __restrict__ shifts,
-                                                                          double beta, double* __restrict__ residual) {
-    extern __shared__ float2 dynf[];
-    float2* w = dynf;
-    __shared__ float rot_c;
-    __shared__ float2 rot_s;
-    const double2 zd = shifts[blockIdx.x];
-    const float2 z = make_float2((float)zd.x, (float)zd.y);
-    auto entry = [&](int row, int c) -> float2 {
-        const double2 h = H[(int64_t)row * ldh + c];
-        return (row == c) ? make_float2(z.x - (float)h.x, z.y - (float)h.y) : make_float2((float)-h.x, (float)-h.y);
-    };
-    for (int c = threadIdx.x; c < m; c += blockDim.x) w[c] = entry(0, c);
-    float2 rhs = make_float2((float)beta, 0.0f);
-    float2 ylast = make_float2(0.0f, 0.0f);
-    // the running rhs is a product of sines and may fall below FP32 range:
-    // keep it rescaled by powers of 1e20 and track the decimal exponent
-    int rhs_exp = 0;
-    int y_exp = 0;
-    __syncthreads();
-    for (int k = 0; k < m; ++k) {
-        if (threadIdx.x == 0) {
-            const float2 a = w[k];
-            float c;
-            float2 sn, rkk;
-            if (k < m - 1) {
-                const float2 b = entry(k + 1, k);
-                const float na = hypotf(a.x, a.y), nb = hypotf(b.x, b.y);
-                if (nb == 0.0f) {
-                    c = 1.0f; sn = make_float2(0.0f, 0.0f); rkk = a;
-                } else if (na == 0.0f) {
-                    c = 0.0f; sn = make_float2(1.0f, 0.0f); rkk = b;
-                } else {
-                    const float rho = hypotf(na, nb);
-                    c = na / rho;
-                    const float2 ph = make_float2(a.x / na, a.y / na);
-                    const float2 bb = make_float2(b.x / rho, -b.y / rho);
-                    sn = make_float2(ph.x * bb.x - ph.y * bb.y, ph.x * bb.y + ph.y * bb.x);
-                    rkk = make_float2(ph.x * rho, ph.y * rho);
+// Incremental shifted solves for Arnoldi convergence checks and the final
+// Green function.  The Givens QR of the Hessenberg matrix (z I - H) is
+// column-incremental: the rotations G_0..G_{j-1} of the first j columns do not
+// change when columns are appended.  Each call processes the new columns
+// [j0, j1) of every shift once, storing per shift and column the rotation
+// (c_j real, s_j complex) and v_j of the transposed sink solve R^T v = p, so
+// that the square system of any dimension m gives
+//   y_{m-1} = g'_{m-1} / pivot,  residual = |h_{m,m-1}| |y_{m-1}| / beta,
+//   green   = sum_{j<m-1} v_j g_j + v'_{m-1} g'_{m-1}
+// from O(1) per-shift scalars (g' the rotated right-hand side entry carried
+// into the next row, acc = sum v_j g_j over finalized columns).  Over a whole
+// Arnoldi run each shift costs one O(m^2/2) elimination instead of one per
+// check.
+//
+// Layout: one group of kAdvLanes lanes per shift; lane t advances column
+// j = cs + t of a chunk.  Rotations of earlier chunks are applied by all
+// lanes at once (phase A); inside the chunk the rotation of column cs + q is
+// formed by lane q and broadcast by warp shuffles to lanes t > q (phase B).
+constexpr int kAdvLanes = 8;
+constexpr int kAdvThreads = 32;
+constexpr int kAdvShiftsPerBlock = kAdvThreads / kAdvLanes;
+constexpr int kAdvDepth = 4;
+
+// Entry (r, c) of z I - H for a column-major Hessenberg (column c at col).
+__device__ __forceinline__ double2 shifted_entry(const double2* __restrict__ col, int r, int c, double2 z) {
+    const double2 h = col[r];
+    return (r == c) ? make_double2(z.x - h.x, z.y - h.y) : make_double2(-h.x, -h.y);
+}
+
+__global__ void __launch_bounds__(kAdvThreads) k_hessenberg_advance(
+    const double2* __restrict__ Hc, int64_t ldc, int j0, int j1, const double2* __restrict__ shifts, int nshift,
+    double beta, double btol, const double2* __restrict__ sinkc, double* __restrict__ rot_c,
+    double2* __restrict__ rot_s, double2* __restrict__ vs, double2* __restrict__ carry, double2* __restrict__ accum,
+    double2* __restrict__ green, double* __restrict__ residual, c3l_hessenberg_status* __restrict__ status) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & (kAdvLanes - 1);
+    const int sraw = blockIdx.x * kAdvShiftsPerBlock + (int)(threadIdx.x / kAdvLanes);
+    const bool live = sraw < nshift;
+    const int sh = live ? sraw : nshift - 1;
+    const double2 z = shifts[sh];
+    double2 g = j0 == 0 ? make_double2(beta, 0.0) : carry[sh];
+    double2 acc = j0 == 0 ? make_double2(0.0, 0.0) : accum[sh];
+    bool stop = false;
+    for (int cs = j0; cs < j1 && !stop; cs += kAdvLanes) {
+        const int c = min(cs + lane, j1 - 1);  // lanes past j1 shadow the last column (never stored)
+        const double2* col = Hc + (int64_t)c * ldc;
+        double2 x = shifted_entry(col, 0, c, z);
+        double2 dot = make_double2(0.0, 0.0);
+        // phase A: rotations of finalized columns.  Off the diagonal the entry
+        // is a = -h; the loads of a step do not depend on the arithmetic chain,
+        // so they are issued kAdvDepth steps ahead (register double buffer).
+        auto rotate_h = [&](double ci, double2 si, double2 h, double2 v) {
+            const double2 sh = cmul(si, h);
+            const double2 r = make_double2(fma(ci, x.x, -sh.x), fma(ci, x.y, -sh.y));
+            const double2 sx = cconjmul(si, x);  // conj(s) x
+            x = make_double2(fma(-ci, h.x, -sx.x), fma(-ci, h.y, -sx.y));
+            dot = make_double2(fma(r.x, v.x, fma(-r.y, v.y, dot.x)), fma(r.x, v.y, fma(r.y, v.x, dot.y)));
+        };
+        const double2 zero2 = make_double2(0.0, 0.0);
+        const int offdiag = cs - 1;  // steps i < cs - 1 never touch a diagonal entry (c >= cs)
+        double bc[2][kAdvDepth];
+        double2 bs[2][kAdvDepth], bv[2][kAdvDepth], bh[2][kAdvDepth];
+        auto fetch = [&](int buf, int i0) {
+#pragma unroll
+            for (int u = 0; u < kAdvDepth; ++u) {
+                const int64_t at = (int64_t)(i0 + u) * nshift + sh;
+                bc[buf][u] = rot_c[at];
+                bs[buf][u] = rot_s[at];
+                bv[buf][u] = sinkc ? vs[at] : zero2;
+                bh[buf][u] = col[i0 + u + 1];
+            }
+        };
+        const int full_groups = offdiag > 0 ? offdiag / kAdvDepth : 0;
+        if (full_groups > 0) fetch(0, 0);
+        for (int gi = 0; gi < full_groups; gi += 2) {
+            if (gi + 1 < full_groups) fetch(1, (gi + 1) * kAdvDepth);
+#pragma unroll
+            for (int u = 0; u < kAdvDepth; ++u) rotate_h(bc[0][u], bs[0][u], bh[0][u], bv[0][u]);
+            if (gi + 1 >= full_groups) break;
+            if (gi + 2 < full_groups) fetch(0, (gi + 2) * kAdvDepth);
+#pragma unroll
+            for (int u = 0; u < kAdvDepth; ++u) rotate_h(bc[1][u], bs[1][u], bh[1][u], bv[1][u]);
+        }
+        for (int i = full_groups * kAdvDepth; i < offdiag; ++i) {
+            const int64_t at = (int64_t)i * nshift + sh;
+            rotate_h(rot_c[at], rot_s[at], col[i + 1], sinkc ? vs[at] : zero2);
+        }
+        if (cs > 0) {  // last finalized rotation: row cs may be this lane's diagonal
+            const int64_t at = (int64_t)(cs - 1) * nshift + sh;
+            const double2 a = shifted_entry(col, cs, c, z);
+            const double2 h = make_double2(-a.x, -a.y);
+            rotate_h(rot_c[at], rot_s[at], h, sinkc ? vs[at] : zero2);
+        }
+        // phase B: columns of this chunk, one rotation per step
+        for (int q = 0; q < kAdvLanes; ++q) {
+            const int cq = cs + q;
+            if (cq >= j1) break;
+            const double2 hsub = Hc[(int64_t)cq * ldc + cq + 1];
+            const bool brk = !(fabs(hsub.x) > btol);
+            double fc = 0.0;
+            double2 fs = make_double2(0.0, 0.0), fv = make_double2(0.0, 0.0);
+            if (lane == q) {
+                const double2 u = sinkc ? make_double2(sinkc[cq].x, -sinkc[cq].y) : make_double2(0.0, 0.0);
+                const double2 num = make_double2(u.x - dot.x, u.y - dot.y);
+                if (cq == j1 - 1 || brk) {
+                    const double2 y = cdiv(g, x);
+                    const double res = hypot(hsub.x, hsub.y) * hypot(y.x, y.y) / beta;
+                    double2 gr = acc;
+                    if (sinkc) {
+                        const double2 t = cmul(cdiv(num, x), g);
+                        gr = make_double2(acc.x + t.x, acc.y + t.y);
+                    }
+                    if (live) {
+                        residual[sh] = res;
+                        if (green) green[sh] = gr;
+                        if (isfinite(res) && isfinite(gr.x) && isfinite(gr.y)) {
+                            atomicMax(&status->worst, (unsigned long long)__double_as_longlong(res));
+                        } else {
+                            atomicExch(&status->bad, 1);
+                        }
+                        if (brk) status->first_break = cq + 1;
+                    }
                 }
-            } else {
-                c = 1.0f; sn = make_float2(0.0f, 0.0f); rkk = a;
+                if (!brk) {
+                    givens_fast(x, make_double2(-hsub.x, -hsub.y), num, sinkc != nullptr, fc, fs, fv);
+                    const double2 t = cmul(fv, make_double2(fc * g.x, fc * g.y));
+                    acc = make_double2(acc.x + t.x, acc.y + t.y);
+                    g = cconjmul(fs, g);
+                    g = make_double2(-g.x, -g.y);
+                    if (live) {
+                        const int64_t at = (int64_t)cq * nshift + sh;
+                        rot_c[at] = fc;
+                        rot_s[at] = fs;
+                        vs[at] = fv;
+                    }
+                }
             }
-            const float2 rrhs = make_float2(c * rhs.x, c * rhs.y);
-            if (k == m - 1) {
-                const float d = rkk.x * rkk.x + rkk.y * rkk.y;
-                ylast = make_float2((rrhs.x * rkk.x + rrhs.y * rkk.y) / d, (rrhs.y * rkk.x - rrhs.x * rkk.y) / d);
-                y_exp = rhs_exp;
+            if (brk) {
+                stop = true;
+                break;
             }
-            rhs = make_float2(-sn.x * rhs.x - sn.y * rhs.y, -sn.x * rhs.y + sn.y * rhs.x);  // -conj(s) rhs
-            const float mag = fmaxf(fabsf(rhs.x), fabsf(rhs.y));
-            if (mag != 0.0f && mag < 1e-20f) {
-                rhs.x *= 1e20f;
-                rhs.y *= 1e20f;
-                rhs_exp -= 20;
+            const int src = (int)(threadIdx.x & ~(kAdvLanes - 1)) + q;
+            fc = __shfl_sync(full, fc, src);
+            fs.x = __shfl_sync(full, fs.x, src);
+            fs.y = __shfl_sync(full, fs.y, src);
+            fv.x = __shfl_sync(full, fv.x, src);
+            fv.y = __shfl_sync(full, fv.y, src);
+            g.x = __shfl_sync(full, g.x, src);
+            g.y = __shfl_sync(full, g.y, src);
+            acc.x = __shfl_sync(full, acc.x, src);
+            acc.y = __shfl_sync(full, acc.y, src);
+            if (lane > q) {
+                const double2 a = shifted_entry(col, cq + 1, c, z);
+                const double2 sa = cmul(fs, a);
+                const double2 r = make_double2(fma(fc, x.x, sa.x), fma(fc, x.y, sa.y));
+                const double2 sx = cconjmul(fs, x);
+                x = make_double2(fma(fc, a.x, -sx.x), fma(fc, a.y, -sx.y));
+                if (sinkc) dot = make_double2(fma(r.x, fv.x, fma(-r.y, fv.y, dot.x)), fma(r.x, fv.y, fma(r.y, fv.x, dot.y)));
             }
-            rot_c = c;
-            rot_s = sn;
         }
-        __syncthreads();
-        const float cc = rot_c;
-        const float2 ss = rot_s;
-        for (int col = k + 1 + threadIdx.x; col < m; col += blockDim.x) {
-            const float2 rv = (k < m - 1) ? entry(k + 1, col) : make_float2(0.0f, 0.0f);
-            const float2 wv = w[col];
-            // w' = -conj(s) w + c r
-            w[col] = make_float2(-ss.x * wv.x - ss.y * wv.y + cc * rv.x, -ss.x * wv.y + ss.y * wv.x + cc * rv.y);
-        }
-        __syncthreads();
+        __syncwarp();
     }
-    if (threadIdx.x == 0) {
-        const double2 hs = H[(int64_t)m * ldh + (m - 1)];
-        residual[blockIdx.x] = hypot(hs.x, hs.y) * hypot((double)ylast.x, (double)ylast.y) * pow(10.0, (double)y_exp) / beta;
+    if (lane == 0 && live) {
+        carry[sh] = g;
+        accum[sh] = acc;
     }
 }
 
@@ -510,6 +683,373 @@ __global__ void k_arnoldi_column(const double2* __restrict__ coeff, int k, doubl
         w[i] = make_double2(w[i].x * inv, w[i].y * inv);
 }
 
+// ------------------------------------------------- device-indexed steps
+// Kernels of one Krylov step whose row count k = *jdev + 1 is read from device
+// memory (see c3l_internal.h).
+constexpr int64_t kSegLen = 4096;
+
+__device__ __forceinline__ void dot_acc(double& s, double a, double b) { s = fma(a, b, s); }
+__device__ __forceinline__ void dot_acc(double2& s, double2 a, double2 b) {  // += conj(a) b
+    s.x = fma(a.x, b.x, fma(a.y, b.y, s.x));
+    s.y = fma(a.x, b.y, fma(-a.y, b.x, s.y));
+}
+__device__ __forceinline__ void axpy_acc(double& s, double c, double v) { s = fma(c, v, s); }
+__device__ __forceinline__ void axpy_acc(double2& s, double2 c, double2 v) {  // += c v
+    s.x = fma(c.x, v.x, fma(-c.y, v.y, s.x));
+    s.y = fma(c.x, v.y, fma(c.y, v.x, s.y));
+}
+__device__ __forceinline__ void dot_acc_plain(double& s, double v) { s += v; }
+__device__ __forceinline__ void dot_acc_plain(double2& s, double2 v) {
+    s.x += v.x;
+    s.y += v.y;
+}
+__device__ __forceinline__ double norm2(double v) { return v * v; }
+__device__ __forceinline__ double norm2(double2 v) { return fma(v.x, v.x, v.y * v.y); }
+__device__ __forceinline__ double real_of(double v) { return v; }
+__device__ __forceinline__ double real_of(double2 v) { return v.x; }
+__device__ __forceinline__ double sum_of(double a, double b) { return a + b; }
+__device__ __forceinline__ double2 sum_of(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+template <typename T> __device__ __forceinline__ T from_real(double v);
+template <> __device__ __forceinline__ double from_real<double>(double v) { return v; }
+template <> __device__ __forceinline__ double2 from_real<double2>(double v) { return make_double2(v, 0.0); }
+__device__ __forceinline__ double scaled_diff(double w, double t, double inv) { return (w - t) * inv; }
+__device__ __forceinline__ double2 scaled_diff(double2 w, double2 t, double inv) {
+    return make_double2((w.x - t.x) * inv, (w.y - t.y) * inv);
+}
+__device__ __forceinline__ void zero(double& v) { v = 0.0; }
+__device__ __forceinline__ void zero(double2& v) { v = make_double2(0.0, 0.0); }
+__device__ __forceinline__ double block_sum_t(double v, double* sm) { return block_sum(v, sm); }
+__device__ __forceinline__ double2 block_sum_t(double2 v, double* sm) {
+    const double re = block_sum(v.x, sm);
+    const double im = block_sum(v.y, sm);
+    return make_double2(re, im);
+}
+__device__ __forceinline__ double add_scaled(double w, double a, double t) { return fma(a, t, w); }
+__device__ __forceinline__ double2 add_scaled(double2 w, double2 a, double2 t) {
+    const double2 u = cmul(a, t);
+    return make_double2(w.x + u.x, w.y + u.y);
+}
+
+// All blocks of a launch call this once; it returns true in the block that
+// finished last, after which that block sees every other block's writes.
+__device__ __forceinline__ bool last_block(unsigned* done) {
+    __shared__ bool last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(done, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (last) __threadfence();
+    return last;
+}
+
+// Arnoldi column from the reduced projections (run by one block): c2 holds
+// the pass-2 projections (k) followed by |w'|^2, so h = sqrt(|w'|^2 - |c2|^2);
+// H[:k+1, j] = c1 + c2 | h goes to column j of Hc, h to hval, and the step
+// counter of the other parity to k.
+__device__ void arnoldi_column_tail(const double2* __restrict__ c1, const double2* __restrict__ c2, int k,
+                                    double2* __restrict__ Hc, int64_t ldc, double* __restrict__ hval, int* next) {
+    __shared__ double red[32];
+    double sq = 0.0;
+    for (int i = threadIdx.x; i < k; i += blockDim.x) sq = fma(c2[i].x, c2[i].x, fma(c2[i].y, c2[i].y, sq));
+    sq = block_sum(sq, red);
+    double2* col = Hc + (int64_t)(k - 1) * ldc;
+    for (int i = threadIdx.x; i < k; i += blockDim.x) col[i] = make_double2(c1[i].x + c2[i].x, c1[i].y + c2[i].y);
+    if (threadIdx.x == 0) {
+        const double h = sqrt(fmax(c2[k].x - sq, 0.0));
+        col[k] = make_double2(h, 0.0);
+        *hval = h;
+        *next = k;
+    }
+}
+
+// Rows [0, k) of V (plus the vector itself when self) dotted with w, k =
+// *cur + 1, in segments of seglen; with one segment the block writes out[row]
+// directly, otherwise partial[row][seg].  COLUMN: the last block also forms
+// the Arnoldi column (single-segment case).
+template <typename T, bool COLUMN>
+__global__ void __launch_bounds__(kThreads) k_dot_rows_dev(const T* __restrict__ V, int64_t ld, const int* cur,
+                                                           int self, const T* __restrict__ w, int64_t dim, int nseg,
+                                                           int64_t seglen, T* __restrict__ partial,
+                                                           T* __restrict__ out, unsigned* done,
+                                                           const T* __restrict__ c1, T* __restrict__ Hc, int64_t ldc,
+                                                           double* __restrict__ hval, int* next) {
+    __shared__ double sm[32];
+    const int k = *cur + 1;
+    const int items = (k + self) * nseg;
+    for (int item = blockIdx.x; item < items; item += gridDim.x) {
+        const int row = item / nseg;
+        const int seg = item - row * nseg;
+        const T* v = row < k ? V + (int64_t)row * ld : w;
+        const int64_t lo = (int64_t)seg * seglen;
+        const int64_t hi = min(dim, lo + seglen);
+        const int64_t step = blockDim.x;
+        T acc;
+        zero(acc);
+        int64_t i = lo + threadIdx.x;
+        for (; i + 3 * step < hi; i += 4 * step) {
+            T a[4], b[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                a[u] = v[i + u * step];
+                b[u] = w[i + u * step];
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) dot_acc(acc, a[u], b[u]);
+        }
+        for (; i < hi; i += step) dot_acc(acc, v[i], w[i]);
+        acc = block_sum_t(acc, sm);
+        if (threadIdx.x == 0) {
+            if (nseg == 1) out[row] = acc;
+            else partial[(int64_t)row * nseg + seg] = acc;
+        }
+    }
+    if (COLUMN) {
+        if (last_block(done)) {
+            if constexpr (std::is_same<T, double2>::value) arnoldi_column_tail(c1, out, k, Hc, ldc, hval, next);
+            if (threadIdx.x == 0) *done = 0u;
+        }
+    }
+}
+
+template <typename T, bool COLUMN>
+__global__ void __launch_bounds__(kThreads) k_dot_final_dev(const T* __restrict__ partial, const int* cur, int self,
+                                                            int nseg, T* __restrict__ out, unsigned* done,
+                                                            const T* __restrict__ c1, T* __restrict__ Hc,
+                                                            int64_t ldc, double* __restrict__ hval, int* next) {
+    __shared__ double sm[32];
+    const int k = *cur + 1;
+    const int rows = k + self;
+    for (int row = blockIdx.x; row < rows; row += gridDim.x) {
+        T acc;
+        zero(acc);
+        for (int b = threadIdx.x; b < nseg; b += blockDim.x) dot_acc_plain(acc, partial[(int64_t)row * nseg + b]);
+        acc = block_sum_t(acc, sm);
+        if (threadIdx.x == 0) out[row] = acc;
+    }
+    if (COLUMN) {
+        if (last_block(done)) {
+            if constexpr (std::is_same<T, double2>::value) arnoldi_column_tail(c1, out, k, Hc, ldc, hval, next);
+            if (threadIdx.x == 0) *done = 0u;
+        }
+    }
+}
+
+template <typename T, int X, int Y>
+__global__ void __launch_bounds__(X * Y) k_axpy_dev(const T* __restrict__ V, int64_t ld, const int* cur,
+                                                     const T* __restrict__ c, T alpha, T* __restrict__ w,
+                                                     int64_t dim) {
+    __shared__ T part[Y][X];
+    const int k = *cur + 1;
+    for (int64_t base = (int64_t)blockIdx.x * X; base < dim; base += (int64_t)gridDim.x * X) {
+        const int64_t i = base + threadIdx.x;
+        T s;
+        zero(s);
+        if (i < dim) {
+            int j = threadIdx.y;
+            for (; j + 3 * Y < k; j += 4 * Y) {
+                T cj[4], v[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    cj[u] = c[j + u * Y];
+                    v[u] = V[(int64_t)(j + u * Y) * ld + i];
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u) axpy_acc(s, cj[u], v[u]);
+            }
+            for (; j < k; j += Y) axpy_acc(s, c[j], V[(int64_t)j * ld + i]);
+        }
+        part[threadIdx.y][threadIdx.x] = s;
+        __syncthreads();
+        for (int h = Y / 2; h > 0; h >>= 1) {
+            if ((int)threadIdx.y < h) {
+                T o = part[threadIdx.y + h][threadIdx.x];
+                T cur2 = part[threadIdx.y][threadIdx.x];
+                dot_acc_plain(cur2, o);
+                part[threadIdx.y][threadIdx.x] = cur2;
+            }
+            __syncthreads();
+        }
+        if (threadIdx.y == 0 && i < dim) w[i] = add_scaled(w[i], alpha, part[0][threadIdx.x]);
+        __syncthreads();
+    }
+}
+
+// Second Arnoldi update and normalization: V[k] = xnext = (w' - V c2) / h,
+// unscaled when h <= tol (breakdown, detected by the shifted solves).
+template <int X, int Y>
+__global__ void __launch_bounds__(X * Y) k_arnoldi_scale(double2* V, int64_t ld, const int* cur,
+                                                          const double2* __restrict__ c2,
+                                                          const double* __restrict__ hval, double tol,
+                                                          const double2* __restrict__ w, int64_t n,
+                                                          double2* __restrict__ xnext) {
+    __shared__ double2 part[Y][X];
+    const int k = *cur + 1;
+    const double h = *hval;
+    const double inv = h > tol ? 1.0 / h : 1.0;
+    double2* Vk = V + (int64_t)k * ld;
+    for (int64_t base = (int64_t)blockIdx.x * X; base < n; base += (int64_t)gridDim.x * X) {
+        const int64_t i = base + threadIdx.x;
+        double2 s = make_double2(0.0, 0.0);
+        if (i < n) {
+            int j = threadIdx.y;
+            for (; j + 3 * Y < k; j += 4 * Y) {
+                double2 cj[4], v[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    cj[u] = c2[j + u * Y];
+                    v[u] = V[(int64_t)(j + u * Y) * ld + i];
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u) axpy_acc(s, cj[u], v[u]);
+            }
+            for (; j < k; j += Y) axpy_acc(s, c2[j], V[(int64_t)j * ld + i]);
+        }
+        part[threadIdx.y][threadIdx.x] = s;
+        __syncthreads();
+        for (int hh = Y / 2; hh > 0; hh >>= 1) {
+            if ((int)threadIdx.y < hh) {
+                double2 c = part[threadIdx.y][threadIdx.x];
+                dot_acc_plain(c, part[threadIdx.y + hh][threadIdx.x]);
+                part[threadIdx.y][threadIdx.x] = c;
+            }
+            __syncthreads();
+        }
+        if (threadIdx.y == 0 && i < n) {
+            const double2 t = part[0][threadIdx.x];
+            const double2 x = make_double2((w[i].x - t.x) * inv, (w[i].y - t.y) * inv);
+            Vk[i] = x;
+            xnext[i] = x;
+        }
+        __syncthreads();
+    }
+}
+
+// ------------------------------------------------ GMRES (real) CGS2 step
+// Short basis (k <= restart + 1 rows) over a long vector: each block owns a
+// column segment for all rows, writes partial[block][row], and the block that
+// finishes last reduces the partials in a fixed order.  Warp r8 of a block
+// handles rows r8, r8 + 8, ...; its lanes stride the block's segment.
+constexpr int kGmWarps = kThreads / 32;
+
+__device__ __forceinline__ void gm_partials(const double* __restrict__ V, int64_t ld, int k,
+                                            const double* __restrict__ w, int64_t lo, int64_t hi,
+                                            double* __restrict__ partial, int R) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int r = warp; r <= k; r += kGmWarps) {
+        const double* v = r < k ? V + (int64_t)r * ld : w;
+        double s0 = 0.0, s1 = 0.0;
+        int64_t c = lo + lane;
+        for (; c + 32 < hi; c += 64) {
+            s0 = fma(v[c], w[c], s0);
+            s1 = fma(v[c + 32], w[c + 32], s1);
+        }
+        if (c < hi) s0 = fma(v[c], w[c], s0);
+        const double t = warp_sum(s0 + s1);
+        if (lane == 0) partial[(int64_t)blockIdx.x * R + r] = t;
+    }
+}
+
+// out[r] = sum over blocks of partial[block][r], r <= k (fixed order)
+__device__ __forceinline__ void gm_reduce(const double* __restrict__ partial, int R, int nb, int k,
+                                          double* __restrict__ out) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int r = warp; r <= k; r += kGmWarps) {
+        double s = 0.0;
+        for (int b = lane; b < nb; b += 32) s += partial[(int64_t)b * R + r];
+        s = warp_sum(s);
+        if (lane == 0) out[r] = s;
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) k_gm_dot(const double* __restrict__ V, int64_t ld, const int* cur,
+                                                     const double* __restrict__ w, int64_t n, int64_t seg,
+                                                     double* __restrict__ partial, int R, unsigned* done,
+                                                     double* __restrict__ out) {
+    const int k = *cur + 1;
+    const int64_t lo = (int64_t)blockIdx.x * seg;
+    gm_partials(V, ld, k, w, lo, min(n, lo + seg), partial, R);
+    if (last_block(done)) {
+        gm_reduce(partial, R, gridDim.x, k, out);
+        if (threadIdx.x == 0) *done = 0u;
+    }
+}
+
+// w' = w - V c1 on the block's segment, then the pass-2 partials; the last
+// block reduces c2, forms h0 = |w|, h = sqrt(|w'|^2 - |c2|^2), writes the
+// column [c1 + c2 | h | h0] to host-mapped slot j and advances the counter.
+__global__ void __launch_bounds__(kThreads) k_gm_axpy_dot(const double* __restrict__ V, int64_t ld, const int* cur,
+                                                          int* next, const double* __restrict__ c1,
+                                                          double* __restrict__ w, int64_t n, int64_t seg,
+                                                          double* __restrict__ partial, int R, unsigned* done,
+                                                          double* __restrict__ c2, double* __restrict__ hval,
+                                                          double* __restrict__ slots, int stride) {
+    __shared__ double cs[C3L_GMRES_MAX_ROWS];
+    __shared__ double red[32];
+    const int k = *cur + 1;
+    for (int r = threadIdx.x; r < k; r += blockDim.x) cs[r] = c1[r];
+    __syncthreads();
+    const int64_t lo = (int64_t)blockIdx.x * seg;
+    const int64_t hi = min(n, lo + seg);
+    for (int64_t c = lo + threadIdx.x; c < hi; c += blockDim.x) {
+        double s0 = 0.0, s1 = 0.0;
+        int r = 0;
+        for (; r + 1 < k; r += 2) {
+            s0 = fma(cs[r], V[(int64_t)r * ld + c], s0);
+            s1 = fma(cs[r + 1], V[(int64_t)(r + 1) * ld + c], s1);
+        }
+        if (r < k) s0 = fma(cs[r], V[(int64_t)r * ld + c], s0);
+        w[c] -= s0 + s1;
+    }
+    __syncthreads();
+    gm_partials(V, ld, k, w, lo, hi, partial, R);
+    if (last_block(done)) {
+        gm_reduce(partial, R, gridDim.x, k, c2);
+        __syncthreads();
+        double sq = 0.0;
+        for (int r = threadIdx.x; r < k; r += blockDim.x) sq = fma(c2[r], c2[r], sq);
+        sq = block_sum(sq, red);
+        const int j = k - 1;
+        double* slot = slots + (int64_t)j * stride;
+        for (int r = threadIdx.x; r < k; r += blockDim.x) slot[r] = c1[r] + c2[r];
+        if (threadIdx.x == 0) {
+            const double h0 = sqrt(fmax(c1[k], 0.0));
+            const double h = sqrt(fmax(c2[k] - sq, 0.0));
+            hval[0] = h0;
+            hval[1] = h;
+            slot[k] = h;
+            slot[k + 1] = h0;
+            *next = k;
+            *done = 0u;
+        }
+    }
+}
+
+// V[k] = xnext = (w' - V c2) / h unless h <= eps h0 (breakdown: unscaled)
+__global__ void __launch_bounds__(kThreads) k_gm_scale(double* V, int64_t ld, const int* cur,
+                                                       const double* __restrict__ c2, const double* __restrict__ hval,
+                                                       double eps, const double* __restrict__ w, int64_t n,
+                                                       double* __restrict__ xnext) {
+    __shared__ double cs[C3L_GMRES_MAX_ROWS];
+    const int k = *cur + 1;
+    for (int r = threadIdx.x; r < k; r += blockDim.x) cs[r] = c2[r];
+    __syncthreads();
+    const double h0 = hval[0], h = hval[1];
+    const double inv = h > eps * h0 ? 1.0 / h : 1.0;
+    double* Vk = V + (int64_t)k * ld;
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+        double s0 = 0.0, s1 = 0.0;
+        int r = 0;
+        for (; r + 1 < k; r += 2) {
+            s0 = fma(cs[r], V[(int64_t)r * ld + c], s0);
+            s1 = fma(cs[r + 1], V[(int64_t)(r + 1) * ld + c], s1);
+        }
+        if (r < k) s0 = fma(cs[r], V[(int64_t)r * ld + c], s0);
+        const double x = (w[c] - (s0 + s1)) * inv;
+        Vk[c] = x;
+        xnext[c] = x;
+    }
+}
+
 // Fixed scratch for c3l_hessenberg_coordinates_noalloc: the packed R factors
 // of the shifted solves live here instead of in caller-provided memory.  The
 // array is part of the library's device image, so every GPU that loads the
@@ -540,17 +1080,154 @@ c3l_status noalloc_scratch(double2** out) {
 
 }  // namespace
 
+namespace c3l {
+
+RowDot row_dot_plan(int max_rows, int64_t dim, int sms) {
+    RowDot p;
+    p.max_rows = max_rows < 1 ? 1 : max_rows;
+    p.nseg = dim > kRowDotMax ? (int)((dim + kSegLen - 1) / kSegLen) : 1;
+    p.seglen = p.nseg == 1 ? (dim > 0 ? dim : 1) : kSegLen;
+    int64_t g = (int64_t)p.max_rows * p.nseg;
+    const int64_t cap = 4 * (int64_t)(sms > 0 ? sms : 152);  // rows beyond the grid are strided
+    if (g > cap) g = cap;
+    p.grid = (unsigned)(g < 1 ? 1 : g);
+    return p;
+}
+
+int64_t row_dot_partial_size(const RowDot& p) { return p.nseg == 1 ? 0 : (int64_t)p.max_rows * p.nseg; }
+
+template <typename T, bool COLUMN>
+static c3l_status dot_rows_dev(const T* V, int64_t ld, const int* cur, int self, const T* w, int64_t dim,
+                               const RowDot& p, T* partial, T* out, unsigned* done, const T* c1, T* Hc, int64_t ldc,
+                               double* hval, int* next, cudaStream_t s) {
+    if (!V || !cur || !w || !out || dim <= 0 || ld < dim || (p.nseg > 1 && !partial)) return C3L_ERR_ARGUMENT;
+    if (COLUMN && (!done || !c1 || !Hc || !hval || !next)) return C3L_ERR_ARGUMENT;
+    if (p.nseg == 1) {
+        k_dot_rows_dev<T, COLUMN><<<p.grid, kThreads, 0, s>>>(V, ld, cur, self, w, dim, 1, p.seglen, partial, out,
+                                                             done, c1, Hc, ldc, hval, next);
+    } else {
+        k_dot_rows_dev<T, false><<<p.grid, kThreads, 0, s>>>(V, ld, cur, self, w, dim, p.nseg, p.seglen, partial,
+                                                            out, nullptr, nullptr, nullptr, 0, nullptr, nullptr);
+        const unsigned g = (unsigned)(p.max_rows > 1024 ? 1024 : p.max_rows);
+        k_dot_final_dev<T, COLUMN><<<g, kThreads, 0, s>>>(partial, cur, self, p.nseg, out, done, c1, Hc, ldc, hval,
+                                                          next);
+    }
+    return launch_status();
+}
+
+c3l_status dot_rows_dev_c(const c3l_complex* V, int64_t ld, const int* cur, int self, const c3l_complex* w,
+                          int64_t dim, const RowDot& p, c3l_complex* partial, c3l_complex* out, cudaStream_t s) {
+    return dot_rows_dev<double2, false>(reinterpret_cast<const double2*>(V), ld, cur, self,
+                                        reinterpret_cast<const double2*>(w), dim, p,
+                                        reinterpret_cast<double2*>(partial), reinterpret_cast<double2*>(out),
+                                        nullptr, nullptr, nullptr, 0, nullptr, nullptr, s);
+}
+
+c3l_status dot_rows_column_dev_c(const c3l_complex* V, int64_t ld, const int* cur, int* next, const c3l_complex* w,
+                                 int64_t dim, const RowDot& p, c3l_complex* partial, unsigned* done,
+                                 const c3l_complex* c1, c3l_complex* c2, c3l_complex* Hc, int64_t ldc, double* hval,
+                                 cudaStream_t s) {
+    return dot_rows_dev<double2, true>(reinterpret_cast<const double2*>(V), ld, cur, 1,
+                                       reinterpret_cast<const double2*>(w), dim, p,
+                                       reinterpret_cast<double2*>(partial), reinterpret_cast<double2*>(c2), done,
+                                       reinterpret_cast<const double2*>(c1), reinterpret_cast<double2*>(Hc), ldc,
+                                       hval, next, s);
+}
+
+c3l_status axpy_dev_c(const c3l_complex* V, int64_t ld, const int* cur, int max_k, const c3l_complex* c,
+                      c3l_complex alpha, c3l_complex* w, int64_t dim, cudaStream_t s) {
+    if (!V || !cur || !c || !w || dim <= 0 || ld < dim) return C3L_ERR_ARGUMENT;
+    const double2* Vd = reinterpret_cast<const double2*>(V);
+    const double2* cd = reinterpret_cast<const double2*>(c);
+    const double2 al = make_double2(alpha.re, alpha.im);
+    double2* wd = reinterpret_cast<double2*>(w);
+    if (max_k >= kAxYLong)
+        k_axpy_dev<double2, kAxXLong, kAxYLong><<<axpy_grid(dim, kAxXLong), dim3(kAxXLong, kAxYLong), 0, s>>>(
+            Vd, ld, cur, cd, al, wd, dim);
+    else
+        k_axpy_dev<double2, kAxX, kAxY><<<axpy_grid(dim), dim3(kAxX, kAxY), 0, s>>>(Vd, ld, cur, cd, al, wd, dim);
+    return launch_status();
+}
+
+c3l_status arnoldi_scale_dev(c3l_complex* V, int64_t ld, const int* cur, int max_k, const c3l_complex* c2,
+                             const double* hval, double tol, const c3l_complex* w, int64_t n, c3l_complex* xnext,
+                             cudaStream_t s) {
+    if (!V || !cur || !c2 || !hval || !w || !xnext || n <= 0 || ld < n) return C3L_ERR_ARGUMENT;
+    double2* Vd = reinterpret_cast<double2*>(V);
+    const double2* cd = reinterpret_cast<const double2*>(c2);
+    const double2* wd = reinterpret_cast<const double2*>(w);
+    double2* xd = reinterpret_cast<double2*>(xnext);
+    if (max_k >= kAxYLong)
+        k_arnoldi_scale<kAxXLong, kAxYLong><<<axpy_grid(n, kAxXLong), dim3(kAxXLong, kAxYLong), 0, s>>>(
+            Vd, ld, cur, cd, hval, tol, wd, n, xd);
+    else
+        k_arnoldi_scale<kAxX, kAxY><<<axpy_grid(n), dim3(kAxX, kAxY), 0, s>>>(Vd, ld, cur, cd, hval, tol, wd, n, xd);
+    return launch_status();
+}
+
+GmPlan gm_plan(int64_t n, int max_rows, int sms) {
+    GmPlan p;
+    p.R = max_rows;
+    int64_t blocks = (n + kThreads - 1) / kThreads;
+    const int64_t cap = 2 * (int64_t)(sms > 0 ? sms : 152);
+    if (blocks > cap) blocks = cap;
+    if (blocks < 1) blocks = 1;
+    p.seg = ((n + blocks - 1) / blocks + 31) / 32 * 32;
+    p.blocks = (unsigned)((n + p.seg - 1) / p.seg);
+    int64_t sg = (n + kThreads - 1) / kThreads;
+    if (sg > cap) sg = cap;
+    p.scale_grid = (unsigned)(sg < 1 ? 1 : sg);
+    return p;
+}
+
+c3l_status gm_dot(const double* V, int64_t ld, const int* cur, const double* w, int64_t n, const GmPlan& p,
+                  double* partial, unsigned* done, double* out, cudaStream_t s) {
+    if (!V || !cur || !w || !partial || !done || !out || n <= 0 || p.R > C3L_GMRES_MAX_ROWS) return C3L_ERR_ARGUMENT;
+    k_gm_dot<<<p.blocks, kThreads, 0, s>>>(V, ld, cur, w, n, p.seg, partial, p.R, done, out);
+    return launch_status();
+}
+
+c3l_status gm_axpy_dot(const double* V, int64_t ld, const int* cur, int* next, const double* c1, double* w, int64_t n,
+                       const GmPlan& p, double* partial, unsigned* done, double* c2, double* hval, double* slots,
+                       int stride, cudaStream_t s) {
+    if (!V || !cur || !next || !c1 || !w || !partial || !done || !c2 || !hval || !slots || n <= 0 ||
+        p.R > C3L_GMRES_MAX_ROWS)
+        return C3L_ERR_ARGUMENT;
+    k_gm_axpy_dot<<<p.blocks, kThreads, 0, s>>>(V, ld, cur, next, c1, w, n, p.seg, partial, p.R, done, c2, hval, slots,
+                                                stride);
+    return launch_status();
+}
+
+c3l_status gm_scale(double* V, int64_t ld, const int* cur, const double* c2, const double* hval, double eps,
+                    const double* w, int64_t n, const GmPlan& p, double* xnext, cudaStream_t s) {
+    if (!V || !cur || !c2 || !hval || !w || !xnext || n <= 0) return C3L_ERR_ARGUMENT;
+    k_gm_scale<<<p.scale_grid, kThreads, 0, s>>>(V, ld, cur, c2, hval, eps, w, n, xnext);
+    return launch_status();
+}
+
+}  // namespace c3l
+
 extern "C" {
 
-int64_t c3l_multi_dot_scratch(int32_t k, int64_t dim) { return (int64_t)k * partial_blocks(k, dim); }
+int64_t c3l_multi_dot_scratch(int32_t k, int64_t dim) {
+    const int64_t nseg = dim > kRowDotMax ? (dim + kSegLen - 1) / kSegLen : 1;
+    const int64_t nb = partial_blocks(k, dim);
+    return (int64_t)k * (nb > nseg ? nb : nseg);
+}
 
 c3l_status c3l_multi_dot_c(const c3l_complex* V, int64_t ld, int32_t k, const c3l_complex* w, int64_t dim,
                            c3l_complex* partial, c3l_complex* out, void* stream) {
     if (k < 0 || dim < 0 || k > 65535) return C3L_ERR_ARGUMENT;
     if (k == 0) return C3L_OK;
     if (!V || !w || !partial || !out || ld < dim) return C3L_ERR_ARGUMENT;
-    const int64_t nb = partial_blocks(k, dim);
     cudaStream_t s = as_stream(stream);
+    if (dim <= kRowDotMax) {
+        k_dot_rows_c<<<(unsigned)k, kThreads, 0, s>>>(reinterpret_cast<const double2*>(V), ld,
+                                                      reinterpret_cast<const double2*>(w), dim,
+                                                      reinterpret_cast<double2*>(out));
+        return launch_status();
+    }
+    const int64_t nb = partial_blocks(k, dim);
     k_dot_partial_c<<<dim3((unsigned)nb, (unsigned)k), kThreads, 0, s>>>(reinterpret_cast<const double2*>(V), ld,
                                                                         reinterpret_cast<const double2*>(w), dim,
                                                                         reinterpret_cast<double2*>(partial));
@@ -576,10 +1253,15 @@ c3l_status c3l_multi_axpy_c(const c3l_complex* V, int64_t ld, int32_t k, const c
     if (k < 0 || dim < 0) return C3L_ERR_ARGUMENT;
     if (k == 0 || dim == 0) return C3L_OK;
     if (!V || !c || !w || ld < dim) return C3L_ERR_ARGUMENT;
-    k_axpy_c<<<axpy_grid(dim), dim3(kAxX, kAxY), 0, as_stream(stream)>>>(reinterpret_cast<const double2*>(V), ld, k,
-                                                                reinterpret_cast<const double2*>(c),
-                                                                make_double2(alpha.re, alpha.im),
-                                                                reinterpret_cast<double2*>(w), dim);
+    const double2* Vd = reinterpret_cast<const double2*>(V);
+    const double2* cd = reinterpret_cast<const double2*>(c);
+    const double2 al = make_double2(alpha.re, alpha.im);
+    double2* wd = reinterpret_cast<double2*>(w);
+    if (k >= kAxYLong)
+        k_axpy_c<kAxXLong, kAxYLong><<<axpy_grid(dim, kAxXLong), dim3(kAxXLong, kAxYLong), 0, as_stream(stream)>>>(
+            Vd, ld, k, cd, al, wd, dim);
+    else
+        k_axpy_c<kAxX, kAxY><<<axpy_grid(dim), dim3(kAxX, kAxY), 0, as_stream(stream)>>>(Vd, ld, k, cd, al, wd, dim);
     return launch_status();
 }
 
@@ -678,16 +1360,25 @@ c3l_status c3l_hessenberg_coordinates_noalloc(const c3l_complex* H, int64_t ldh,
     return C3L_OK;
 }
 
-c3l_status c3l_hessenberg_residual_f32(const c3l_complex* H, int64_t ldh, int32_t m, const c3l_complex* shifts,
-                                       int32_t nshift, double beta, double* residual, void* stream) {
-    if (m <= 0 || nshift < 0 || !H || !shifts || !residual || ldh < m || !(beta > 0.0)) return C3L_ERR_ARGUMENT;
-    if (m > C3L_MAX_HESSENBERG) return C3L_ERR_CAPACITY;
-    if (nshift == 0) return C3L_OK;
-    const size_t smem = (size_t)m * sizeof(float2);
-    if (set_smem((const void*)k_hessenberg_residual_f32, smem)) return C3L_ERR_LAUNCH;
-    k_hessenberg_residual_f32<<<(unsigned)nshift, kHessThreads, smem, as_stream(stream)>>>(
-        reinterpret_cast<const double2*>(H), ldh, m, reinterpret_cast<const double2*>(shifts), beta, residual);
-    return launch_status();
+c3l_status c3l_hessenberg_advance(c3l_hessenberg_state* st, const c3l_complex* Hc, int64_t ldc, int32_t m,
+                                  void* stream) {
+    if (!st || !Hc || !st->shifts || !st->rot_c || !st->rot_s || !st->vsink || !st->carry || !st->accum ||
+        !st->residual || !st->status || st->nshift <= 0 || st->m_max <= 0 || !(st->beta > 0.0))
+        return C3L_ERR_ARGUMENT;
+    if (m < st->done || m > st->m_max || ldc < (int64_t)st->m_max + 1 || st->done < 0) return C3L_ERR_ARGUMENT;
+    cudaStream_t s = as_stream(stream);
+    if (cudaMemsetAsync(st->status, 0, sizeof(c3l_hessenberg_status), s) != cudaSuccess) return C3L_ERR_LAUNCH;
+    if (m == st->done) return C3L_OK;
+    const unsigned blocks = (unsigned)((st->nshift + kAdvShiftsPerBlock - 1) / kAdvShiftsPerBlock);
+    k_hessenberg_advance<<<blocks, kAdvThreads, 0, s>>>(
+        reinterpret_cast<const double2*>(Hc), ldc, st->done, m, reinterpret_cast<const double2*>(st->shifts),
+        st->nshift, st->beta, st->breakdown_tol, reinterpret_cast<const double2*>(st->sinkproj_conj), st->rot_c,
+        reinterpret_cast<double2*>(st->rot_s), reinterpret_cast<double2*>(st->vsink),
+        reinterpret_cast<double2*>(st->carry), reinterpret_cast<double2*>(st->accum),
+        reinterpret_cast<double2*>(st->green), st->residual, st->status);
+    if (cudaGetLastError() != cudaSuccess) return C3L_ERR_LAUNCH;
+    st->done = m;
+    return C3L_OK;
 }
 
 c3l_status c3l_arnoldi_column(const c3l_complex* coeff, int32_t k, c3l_complex* w, int64_t n, c3l_complex* Hc, int64_t ldc,

@@ -3,22 +3,24 @@
 // c3l_gmres   -- left-preconditioned restarted GMRES with SciPy's control flow
 //                (the solver the reference calls for Newton corrections,
 //                src/c3l/cc/component_solver.py:181), the operator being the
-//                device JVP action.  Each inner iteration enqueues the JVP, the
-//                preconditioner and a CGS2 pass (projections fused with the
-//                norm), then reads back O(k) scalars in one pinned copy.
+//                device JVP action.  One inner iteration (JVP, preconditioner,
+//                CGS2, column) is a replayed CUDA graph; the host runs the
+//                Givens updates one iteration behind the GPU.
 // c3l_arnoldi -- CGS2 Arnoldi of src/c3l/green/krylov.py:284-417 for several
 //                independent channels at once: each channel runs on its own
 //                stream and workspace, so the channels' kernels overlap on the
-//                GPU while the host handles one channel's scalars.
+//                GPU; the shifted solves advance incrementally at each check.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstring>
 #include <vector>
 
 #include "c3l_gb300.h"
+#include "c3l_internal.h"
 
 namespace {
 
@@ -48,13 +50,95 @@ void lartg(double f, double g, double& c, double& s, double& r) {
     }
 }
 
+int sm_count() {
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
+        return 152;
+    return sms;
+}
+
+// A CUDA graph captured from a callback that enqueues work on a stream.
+// Capture runs on a private stream, so the caller's stream (possibly the
+// legacy default stream) only ever sees graph launches.
+class StepGraph {
+  public:
+    StepGraph() = default;
+    StepGraph(const StepGraph&) = delete;
+    StepGraph& operator=(const StepGraph&) = delete;
+    ~StepGraph() {
+        if (exec_) cudaGraphExecDestroy(exec_);
+        if (graph_) cudaGraphDestroy(graph_);
+    }
+    template <typename F>
+    c3l_status capture(cudaStream_t cap, F&& enqueue) {
+        if (cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return C3L_ERR_LAUNCH;
+        const c3l_status st = enqueue(cap);
+        cudaGraph_t g = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(cap, &g);
+        if (st) {
+            if (g) cudaGraphDestroy(g);
+            return st;
+        }
+        if (e != cudaSuccess || !g) return C3L_ERR_LAUNCH;
+        graph_ = g;
+        if (cudaGraphInstantiate(&exec_, graph_, 0) != cudaSuccess) return C3L_ERR_LAUNCH;
+        size_t count = 0;
+        if (cudaGraphGetNodes(graph_, nullptr, &count) != cudaSuccess) return C3L_ERR_LAUNCH;
+        nodes_ = (int64_t)count;
+        return C3L_OK;
+    }
+    c3l_status launch(cudaStream_t s) const {
+        return exec_ && cudaGraphLaunch(exec_, s) == cudaSuccess ? C3L_OK : C3L_ERR_LAUNCH;
+    }
+    int64_t nodes() const { return nodes_; }
+
+  private:
+    cudaGraph_t graph_ = nullptr;
+    cudaGraphExec_t exec_ = nullptr;
+    int64_t nodes_ = 0;
+};
+
+struct OwnedStream {
+    cudaStream_t s = nullptr;
+    ~OwnedStream() {
+        if (s) cudaStreamDestroy(s);
+    }
+    c3l_status create() {
+        return cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) == cudaSuccess ? C3L_OK : C3L_ERR_LAUNCH;
+    }
+};
+
+struct OwnedEvents {
+    std::vector<cudaEvent_t> ev;
+    ~OwnedEvents() {
+        for (cudaEvent_t e : ev)
+            if (e) cudaEventDestroy(e);
+    }
+    c3l_status create(int count) {
+        ev.assign(count, nullptr);
+        for (auto& e : ev)
+            if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return C3L_ERR_LAUNCH;
+        return C3L_OK;
+    }
+};
+
 }  // namespace
 
 extern "C" {
 
+int64_t c3l_gmres_scratch(int32_t restart, int64_t dim) {
+    if (restart <= 0 || dim <= 0) return 0;
+    const int r = (int)std::min<int64_t>(restart, dim);
+    const c3l::GmPlan gp = c3l::gm_plan(dim, r + 2, sm_count());
+    return (int64_t)gp.blocks * (r + 2);
+}
+
 c3l_status c3l_gmres(c3l_gmres_args* a, void* stream) {
     if (!a || !a->jvp || !a->b || !a->x || !a->V || !a->tmp || !a->r || !a->coeff || !a->partial || !a->host ||
-        !a->pc_m4 || !a->pc_col || !a->pc_pair || a->dim <= 0 || a->restart <= 0 || a->maxiter <= 0)
+        !a->pc_m4 || !a->pc_col || !a->pc_pair || !a->work || !a->counters || !a->slots || a->dim <= 0 ||
+        a->partial_capacity <= 0 ||
+        a->restart <= 0 || a->maxiter <= 0)
         return C3L_ERR_ARGUMENT;
     cudaStream_t s = as_stream(stream);
     const int64_t n = a->dim;
@@ -67,16 +151,70 @@ c3l_status c3l_gmres(c3l_gmres_args* a, void* stream) {
     c3l_status st;
     a->history_len = 0;
     a->matvecs = 0;
+    a->launches = 0;
+    // one inner iteration as a graph: xcur -> M J -> wfix, CGS2 against
+    // V[0..j] in three kernels, column j into host-mapped slot j, V[j+1] =
+    // xcur = w'' / h.  The step index alternates between two counters, so
+    // there is one graph per parity.
+    double* xcur = a->work;
+    double* wfix = a->work + n;
+    const int R = restart + 2;
+    double* c1 = coeff;
+    double* c2 = coeff + R;
+    double* hval = coeff + 2 * R;
+    unsigned* done = reinterpret_cast<unsigned*>(a->counters + 2);
+    const int stride = restart + 3;
+    if (R > C3L_GMRES_MAX_ROWS) return C3L_ERR_CAPACITY;
+    const c3l::GmPlan gp = c3l::gm_plan(n, R, sm_count());
+    if ((int64_t)gp.blocks * R > a->partial_capacity) return C3L_ERR_CAPACITY;
+    c3l_static_action fused;
+    const c3l_static_action* op = a->jvp;
+    if (a->pc_m4_elem) {
+        fused = *a->jvp;
+        fused.pc_m4 = a->pc_m4_elem;
+        op = &fused;
+    }
+    OwnedStream cap;
+    if ((st = cap.create())) return st;
+    StepGraph inner[2];
+    for (int par = 0; par < 2; ++par) {
+        const int* cur = a->counters + par;
+        int* next = a->counters + (1 - par);
+        st = inner[par].capture(cap.s, [&](cudaStream_t cs) -> c3l_status {
+            void* csv = reinterpret_cast<void*>(cs);
+            c3l_status q;
+            if (a->pc_m4_elem) {
+                q = a->use_f32 ? c3l_static_apply_f32(op, xcur, wfix, csv) : c3l_static_apply(op, xcur, wfix, csv);
+                if (q) return q;
+            } else {
+                q = a->use_f32 ? c3l_static_apply_f32(op, xcur, a->tmp, csv) : c3l_static_apply(op, xcur, a->tmp, csv);
+                if (q) return q;
+                if ((q = c3l_precondition(a->nrep, a->pc_m4, a->pc_col, a->pc_pair, a->tmp, wfix, csv))) return q;
+            }
+            if ((q = c3l::gm_dot(V, n, cur, wfix, n, gp, a->partial, done, c1, cs))) return q;
+            if ((q = c3l::gm_axpy_dot(V, n, cur, next, c1, wfix, n, gp, a->partial, done, c2, hval, a->slots, stride,
+                                      cs)))
+                return q;
+            return c3l::gm_scale(V, n, cur, c2, hval, eps, wfix, n, gp, xcur, cs);
+        });
+        if (st) return st;
+    }
+    // kernels of one operator application: the graph less the three CGS2 kernels
+    const int64_t jvp_nodes = inner[0].nodes() - 3 - (a->pc_m4_elem ? 0 : 1);
+    OwnedEvents ev;
+    if ((st = ev.create(2))) return st;
     auto matvec = [&](const double* in, double* out) -> c3l_status {
         a->matvecs += 1;
         return a->use_f32 ? c3l_static_apply_f32(a->jvp, in, out, stream) : c3l_static_apply(a->jvp, in, out, stream);
     };
     auto psolve = [&](const double* in, double* out) -> c3l_status {
+        a->launches += 1;
         return c3l_precondition(a->nrep, a->pc_m4, a->pc_col, a->pc_pair, in, out, stream);
     };
     auto norm = [&](const double* v, double& out) -> c3l_status {
         c3l_status q = c3l_multi_dot_r(v, n, 1, v, n, a->partial, coeff, stream);
         if (q) return q;
+        a->launches += 2;
         if ((q = d2h(host, coeff, sizeof(double), s))) return q;
         out = std::sqrt(std::max(host[0], 0.0));
         return C3L_OK;
@@ -108,34 +246,36 @@ c3l_status c3l_gmres(c3l_gmres_args* a, void* stream) {
         double beta;
         if ((st = norm(V, beta))) return st;
         if ((st = c3l_scale_r(n, 1.0 / beta, V, V, stream))) return st;
+        if (cudaMemcpyAsync(xcur, V, n * sizeof(double), cudaMemcpyDeviceToDevice, s) != cudaSuccess ||
+            cudaMemsetAsync(a->counters, 0, 4 * sizeof(int32_t), s) != cudaSuccess)
+            return C3L_ERR_LAUNCH;
+        a->launches += 1;  // scale
         std::fill(S.begin(), S.end(), 0.0);
         std::fill(h.begin(), h.end(), 0.0);
         S[0] = beta;
         bool breakdown = false;
         int col = 0;
+        auto enqueue = [&](int j) -> c3l_status {
+            c3l_status q = inner[j & 1].launch(s);
+            if (q) return q;
+            a->launches += inner[j & 1].nodes();
+            return cudaEventRecord(ev.ev[j & 1], s) == cudaSuccess ? C3L_OK : C3L_ERR_LAUNCH;
+        };
+        if ((st = enqueue(0))) return st;
         for (col = 0; col < restart; ++col) {
-            double* w = V + (int64_t)(col + 1) * n;
-            if ((st = matvec(V + (int64_t)col * n, a->tmp))) return st;
-            if ((st = psolve(a->tmp, w))) return st;
+            // keep the GPU one iteration ahead; an iteration past the stop is discarded
+            if (col + 1 < restart && (st = enqueue(col + 1))) return st;
+            if (cudaEventSynchronize(ev.ev[col & 1]) != cudaSuccess) return C3L_ERR_LAUNCH;
+            a->matvecs += 1;
             const int k = col + 1;
-            // pass 1: [V_0..V_col, w]^T w -> c1 and |w|^2 (w is the row after V_col)
-            if ((st = c3l_multi_dot_r(V, n, k + 1, w, n, a->partial, coeff, stream))) return st;
-            if ((st = c3l_multi_axpy_r(V, n, k, coeff, -1.0, w, n, stream))) return st;
-            // pass 2: c2 and |w'|^2 ; |w''|^2 = |w'|^2 - |c2|^2 (w'' = w' - V c2, V orthonormal)
-            if ((st = c3l_multi_dot_r(V, n, k + 1, w, n, a->partial, coeff + k + 1, stream))) return st;
-            if ((st = c3l_multi_axpy_r(V, n, k, coeff + k + 1, -1.0, w, n, stream))) return st;
-            if ((st = d2h(host, coeff, 2 * (k + 1) * sizeof(double), s))) return st;
-            const double h0 = std::sqrt(std::max(host[k], 0.0));
-            double c2sq = 0.0;
-            for (int j = 0; j < k; ++j) c2sq += host[k + 1 + j] * host[k + 1 + j];
-            const double h1 = std::sqrt(std::max(host[2 * k + 1] - c2sq, 0.0));
-            for (int j = 0; j < k; ++j) H(col, j) = host[j] + host[k + 1 + j];
+            const volatile double* slot = a->slots + (int64_t)col * stride;
+            for (int j = 0; j < k; ++j) H(col, j) = slot[j];
+            const double h1 = slot[k];
+            const double h0 = slot[k + 1];
             H(col, col + 1) = h1;
             if (h1 <= eps * h0) {
                 H(col, col + 1) = 0.0;
                 breakdown = true;
-            } else if ((st = c3l_scale_r(n, 1.0 / h1, w, w, stream))) {
-                return st;
             }
             for (int j = 0; j < col; ++j) {
                 const double n0 = H(col, j), n1 = H(col, j + 1);
@@ -176,6 +316,7 @@ c3l_status c3l_gmres(c3l_gmres_args* a, void* stream) {
         if ((st = matvec(a->x, a->tmp))) return st;
         if (cudaMemcpyAsync(a->r, a->b, n * sizeof(double), cudaMemcpyDeviceToDevice, s) != cudaSuccess) return C3L_ERR_LAUNCH;
         if ((st = c3l_multi_axpy_r(a->tmp, n, 1, ones, -1.0, a->r, n, stream))) return st;
+        a->launches += 2 + jvp_nodes;  // two axpys and the JVP
         if ((st = norm(a->r, rnorm))) return st;
         if (rnorm <= atol) break;
         if (breakdown) break;
@@ -195,13 +336,57 @@ c3l_status c3l_arnoldi(c3l_arnoldi_channel* ch, int32_t nch, int64_t N, const c3
         return C3L_ERR_ARGUMENT;
     for (int c = 0; c < nch; ++c) {
         const c3l_arnoldi_channel& q = ch[c];
-        if (!q.sigma || !q.b || !q.V || !q.Hcol || !q.coeff || !q.partial || !q.host || !q.H || !q.Hdev ||
-            !q.resid_dev || !q.resid_host)
+        const c3l_hessenberg_state& h = q.hess;
+        if (!q.sigma || !q.b || !q.V || !q.Hcol || !q.coeff || !q.partial || !q.host || !q.status_host || !q.work ||
+            !q.counters || !h.rot_c || !h.rot_s || !h.vsink || !h.carry || !h.accum || !h.residual || !h.status ||
+            h.m_max < m_max || h.nshift != nshift || (q.sink_conj && !h.sinkproj_conj))
             return C3L_ERR_ARGUMENT;
     }
     const int64_t ldc = (int64_t)m_max + 1;
+    const c3l::RowDot rd = c3l::row_dot_plan(m_max + 1, N, sm_count());
+    if (c3l::row_dot_partial_size(rd) > c3l_multi_dot_scratch(m_max + 1, N)) return C3L_ERR_CAPACITY;
     c3l_status st;
-    std::vector<int> active(nch, 1), synced(nch, 0);
+    // one Arnoldi step per channel as a graph: xnext -> sigma -> wfix, CGS2
+    // against V[0..j] (the pass-2 projections also form column j of H and
+    // h), V[j+1] = xnext = w'' / h.  The step index alternates between two
+    // counters: graphs exist for both parities, and `interval` chains
+    // check_interval steps starting at either parity.
+    OwnedStream cap;
+    if ((st = cap.create())) return st;
+    std::vector<StepGraph> one(2 * nch), interval(2 * nch);
+    for (int c = 0; c < nch; ++c) {
+        c3l_arnoldi_channel& q = ch[c];
+        c3l_complex* xnext = q.work;
+        c3l_complex* wfix = q.work + N;
+        c3l_complex* c1 = q.coeff;
+        c3l_complex* c2 = q.coeff + (m_max + 1);
+        double* hval = reinterpret_cast<double*>(q.coeff + 2 * (m_max + 1));
+        unsigned* done = reinterpret_cast<unsigned*>(q.counters + 2);
+        auto step = [&](cudaStream_t cs, int par) -> c3l_status {
+            const int* cur = q.counters + par;
+            int* next = q.counters + (1 - par);
+            c3l_status r = c3l_eom_sigma(q.sigma, xnext, wfix, reinterpret_cast<void*>(cs));
+            if (r) return r;
+            if ((r = c3l::dot_rows_dev_c(q.V, N, cur, 0, wfix, N, rd, q.partial, c1, cs))) return r;
+            if ((r = c3l::axpy_dev_c(q.V, N, cur, m_max, c1, c3l_complex{-1.0, 0.0}, wfix, N, cs))) return r;
+            if ((r = c3l::dot_rows_column_dev_c(q.V, N, cur, next, wfix, N, rd, q.partial, done, c1, c2, q.Hcol, ldc,
+                                                hval, cs)))
+                return r;
+            return c3l::arnoldi_scale_dev(q.V, N, cur, m_max, c2, hval, breakdown_tol, wfix, N, xnext, cs);
+        };
+        for (int par = 0; par < 2; ++par) {
+            if ((st = one[2 * c + par].capture(cap.s, [&](cudaStream_t cs) { return step(cs, par); }))) return st;
+            if ((st = interval[2 * c + par].capture(cap.s, [&](cudaStream_t cs) -> c3l_status {
+                     for (int i = 0; i < check_interval; ++i) {
+                         const c3l_status r = step(cs, (par + i) & 1);
+                         if (r) return r;
+                     }
+                     return C3L_OK;
+                 })))
+                return st;
+        }
+    }
+    std::vector<int> active(nch, 1);
     for (int c = 0; c < nch; ++c) {
         c3l_arnoldi_channel& q = ch[c];
         cudaStream_t s = as_stream(streams[c]);
@@ -210,115 +395,110 @@ c3l_status c3l_arnoldi(c3l_arnoldi_channel* ch, int32_t nch, int64_t N, const c3
         q.converged = 0;
         q.nchecks = 0;
         q.action_seconds = 0.0;
+        q.launches = 0;
         if ((st = c3l_multi_dot_c(q.b, N, 1, q.b, N, q.partial, q.coeff, streams[c]))) return st;
         if ((st = d2h(q.host, q.coeff, sizeof(c3l_complex), s))) return st;
         q.beta = std::sqrt(std::max(q.host[0].re, 0.0));
         if (!(q.beta > 0.0) || !std::isfinite(q.beta)) return C3L_ERR_ARGUMENT;
         if ((st = c3l_scale_c(N, c3l_complex{1.0 / q.beta, 0.0}, q.b, q.V, streams[c]))) return st;
+        if ((st = c3l_scale_c(N, c3l_complex{1.0 / q.beta, 0.0}, q.b, q.work, streams[c]))) return st;
+        if (cudaMemsetAsync(q.counters, 0, 4 * sizeof(int32_t), s) != cudaSuccess) return C3L_ERR_LAUNCH;
+        q.launches += (N > 8192 ? 2 : 1) + 2;
+        q.hess.shifts = shifts;
+        q.hess.beta = q.beta;
+        q.hess.breakdown_tol = breakdown_tol;
+        q.hess.done = 0;
+        if (!q.sink_conj) q.hess.sinkproj_conj = nullptr;
     }
-    // copy device columns [synced, upto) of H into the host row-major matrix and
-    // scan them for breakdown / non-finite values; returns the first bad column
-    auto pull = [&](c3l_arnoldi_channel& q, int c, int upto, int& first_break, bool& bad) -> c3l_status {
-        cudaStream_t s = as_stream(streams[c]);
-        const int j0 = synced[c];
-        first_break = -1;
-        bad = false;
-        if (upto <= j0) return C3L_OK;
-        std::vector<c3l_complex> cols((size_t)(upto - j0) * ldc);
-        if (cudaMemcpyAsync(cols.data(), q.Hcol + (int64_t)j0 * ldc, cols.size() * sizeof(c3l_complex),
-                            cudaMemcpyDeviceToHost, s) != cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess)
-            return C3L_ERR_LAUNCH;
-        for (int j = j0; j < upto; ++j) {
-            const c3l_complex* col = cols.data() + (size_t)(j - j0) * ldc;
-            for (int i = 0; i <= j + 1; ++i) {
-                if (!std::isfinite(col[i].re) || !std::isfinite(col[i].im)) bad = true;
-                q.H[(int64_t)i * m_max + j] = col[i];
-            }
-            if (first_break < 0 && std::fabs(col[j + 1].re) <= breakdown_tol) first_break = j;
-        }
-        synced[c] = upto;
-        return C3L_OK;
-    };
-    auto check = [&](c3l_arnoldi_channel& q, int c, int m, bool fp64, double& worst) -> c3l_status {
+    // advance the channel's shifted solves to dimension `upto` and read the
+    // status word: worst residual, first breakdown column, non-finite flag
+    auto check = [&](c3l_arnoldi_channel& q, int c, int upto, double& worst, int& first_break) -> c3l_status {
         void* stream = streams[c];
         cudaStream_t s = as_stream(stream);
-        // H[:m+1, :m] from the host matrix (row pitch m_max) into a dense device copy (ld = m)
-        if (cudaMemcpy2DAsync(q.Hdev, m * sizeof(c3l_complex), q.H, m_max * sizeof(c3l_complex),
-                              m * sizeof(c3l_complex), m + 1, cudaMemcpyHostToDevice, s) != cudaSuccess)
-            return C3L_ERR_LAUNCH;
-        c3l_status r = fp64 ? c3l_hessenberg_shifted(q.Hdev, m, m, shifts, nshift, q.beta, nullptr, nullptr,
-                                                      q.resid_dev, stream)
-                            : c3l_hessenberg_residual_f32(q.Hdev, m, m, shifts, nshift, q.beta, q.resid_dev, stream);
-        if (r) return r;
-        if ((r = d2h(q.resid_host, q.resid_dev, nshift * sizeof(double), s))) return r;
-        worst = 0.0;
-        for (int i = 0; i < nshift; ++i) worst = std::max(worst, q.resid_host[i]);
+        const int done = q.hess.done;
+        c3l_status r;
+        if (q.sink_conj && upto > done) {
+            c3l_complex* out = const_cast<c3l_complex*>(q.hess.sinkproj_conj) + done;
+            if ((r = c3l_multi_dot_c(q.V + (int64_t)done * N, N, upto - done, q.sink_conj, N, q.partial, out, stream)))
+                return r;
+            q.launches += N > 8192 ? 2 : 1;
+        }
+        if ((r = c3l_hessenberg_advance(&q.hess, q.Hcol, ldc, upto, stream))) return r;
+        q.launches += 1;
+        if ((r = d2h(q.status_host, q.hess.status, sizeof(c3l_hessenberg_status), s))) return r;
+        const c3l_hessenberg_status hs = *q.status_host;
+        if (hs.bad) return C3L_ERR_ARGUMENT;  // non-finite Arnoldi step
+        unsigned long long bits = hs.worst;
+        std::memcpy(&worst, &bits, sizeof(double));
+        first_break = hs.first_break - 1;
         if (q.check_dims && q.nchecks < q.check_capacity) {
-            q.check_dims[q.nchecks] = m;
+            q.check_dims[q.nchecks] = first_break >= 0 ? first_break + 1 : upto;
             q.check_res[q.nchecks] = worst;
         }
         q.nchecks += 1;
         return C3L_OK;
     };
-    int remaining = nch;
-    for (int j = 0; j < m_max && remaining > 0; ++j) {
-        const int k = j + 1;
-        const bool due = k >= min_dim && (k % check_interval == 0 || k == m_max);
-        for (int c = 0; c < nch; ++c) {
-            if (!active[c]) continue;
-            c3l_arnoldi_channel& q = ch[c];
-            c3l_complex* w = q.V + (int64_t)k * N;
-            if ((st = c3l_eom_sigma(q.sigma, q.V + (int64_t)j * N, w, streams[c]))) return st;
-            if ((st = c3l_multi_dot_c(q.V, N, k, w, N, q.partial, q.coeff, streams[c]))) return st;
-            if ((st = c3l_multi_axpy_c(q.V, N, k, q.coeff, c3l_complex{-1.0, 0.0}, w, N, streams[c]))) return st;
-            // pass 2 with the squared norm of the pass-1 vector (last entry)
-            if ((st = c3l_multi_dot_c(q.V, N, k + 1, w, N, q.partial, q.coeff + k, streams[c]))) return st;
-            if ((st = c3l_multi_axpy_c(q.V, N, k, q.coeff + k, c3l_complex{-1.0, 0.0}, w, N, streams[c]))) return st;
-            if ((st = c3l_arnoldi_column(q.coeff, k, w, N, q.Hcol, ldc, j, breakdown_tol, streams[c]))) return st;
-            q.m = k;
-        }
-        if (!due) continue;
-        for (int c = 0; c < nch; ++c) {
-            if (!active[c]) continue;
-            c3l_arnoldi_channel& q = ch[c];
-            int first_break;
-            bool bad;
-            if ((st = pull(q, c, k, first_break, bad))) return st;
-            if (bad) return C3L_ERR_ARGUMENT;  // non-finite Arnoldi step
-            if (first_break >= 0) {
-                q.m = first_break + 1;
-                q.breakdown = 1;
-                active[c] = 0;
-                remaining -= 1;
-                continue;
-            }
-            double worst;
-            if ((st = check(q, c, k, false, worst))) return st;
-            if (worst <= tol) {
-                if ((st = check(q, c, k, true, worst))) return st;
-                if (worst <= tol) {
-                    q.converged = 1;
-                    active[c] = 0;
-                    remaining -= 1;
-                }
-            }
-        }
-    }
-    // channels that stopped on breakdown or at m_max: pull the rest and check in FP64
-    for (int c = 0; c < nch; ++c) {
-        c3l_arnoldi_channel& q = ch[c];
-        if (q.converged) continue;
-        int first_break;
-        bool bad;
-        if ((st = pull(q, c, q.m, first_break, bad))) return st;
-        if (bad) return C3L_ERR_ARGUMENT;
+    auto settle = [&](c3l_arnoldi_channel& q, int first_break, double worst) {
         if (first_break >= 0) {
             q.m = first_break + 1;
             q.breakdown = 1;
         }
-        double worst;
-        if ((st = check(q, c, q.m, true, worst))) return st;
         q.converged = worst <= tol ? 1 : 0;
+    };
+    auto due = [&](int k) { return k >= min_dim && (k % check_interval == 0 || k == m_max); };
+    int remaining = nch;
+    int j = 0;  // steps taken by every active channel
+    while (j < m_max && remaining > 0) {
+        int target = j + 1;
+        while (!due(target)) ++target;  // terminates: due(m_max) holds
+        const int steps = target - j;
+        for (int c = 0; c < nch; ++c) {
+            if (!active[c]) continue;
+            c3l_arnoldi_channel& q = ch[c];
+            cudaStream_t s = as_stream(streams[c]);
+            int left = steps;
+            int at = j;  // steps taken so far: the parity of the next step
+            while (left >= check_interval) {
+                const StepGraph& g = interval[2 * c + (at & 1)];
+                if ((st = g.launch(s))) return st;
+                q.launches += g.nodes();
+                left -= check_interval;
+                at += check_interval;
+            }
+            for (; left > 0; --left, ++at) {
+                const StepGraph& g = one[2 * c + (at & 1)];
+                if ((st = g.launch(s))) return st;
+                q.launches += g.nodes();
+            }
+            q.m = target;
+        }
+        j = target;
+        for (int c = 0; c < nch; ++c) {
+            if (!active[c]) continue;
+            c3l_arnoldi_channel& q = ch[c];
+            double worst;
+            int first_break;
+            if ((st = check(q, c, j, worst, first_break))) return st;
+            if (first_break >= 0 || worst <= tol || j == m_max) {
+                settle(q, first_break, worst);
+                active[c] = 0;
+                remaining -= 1;
+            }
+        }
+    }
+    // host copy of H[:m+1, :m] (row-major, leading dimension m_max)
+    for (int c = 0; c < nch; ++c) {
+        c3l_arnoldi_channel& q = ch[c];
+        if (!q.H || q.m <= 0) continue;
+        cudaStream_t s = as_stream(streams[c]);
+        const int m = q.m;
+        std::vector<c3l_complex> cols((size_t)m * (m + 1));
+        if (cudaMemcpy2DAsync(cols.data(), (m + 1) * sizeof(c3l_complex), q.Hcol, ldc * sizeof(c3l_complex),
+                              (m + 1) * sizeof(c3l_complex), m, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess)
+            return C3L_ERR_LAUNCH;
+        for (int jj = 0; jj < m; ++jj)
+            for (int i = 0; i <= jj + 1 && i <= m; ++i) q.H[(int64_t)i * m_max + jj] = cols[(size_t)jj * (m + 1) + i];
     }
     return C3L_OK;
 }

@@ -129,8 +129,17 @@ __global__ void __launch_bounds__(kThreads) k_contract(c3l_contract_level lv, in
         const int64_t lo = e - hi * low;
         const C* src = ws + task.src_off[j] + hi * low * n + lo;
         const C* vec = vectors + task.vec_off[j];
-        C sum = Cx<C>::make(0.0, 0.0);
-        for (int m = 0; m < n; ++m) sum = cfma(vec[m], src[m * low], sum);
+        // four independent partial sums keep four loads in flight
+        C s0 = Cx<C>::make(0.0, 0.0), s1 = s0, s2 = s0, s3 = s0;
+        int m = 0;
+        for (; m + 3 < n; m += 4) {
+            s0 = cfma(vec[m], src[m * low], s0);
+            s1 = cfma(vec[m + 1], src[(m + 1) * low], s1);
+            s2 = cfma(vec[m + 2], src[(m + 2) * low], s2);
+            s3 = cfma(vec[m + 3], src[(m + 3) * low], s3);
+        }
+        for (; m < n; ++m) s0 = cfma(vec[m], src[m * low], s0);
+        const C sum = cadd(cadd(s0, s1), cadd(s2, s3));
         const typename Cx<C>::R sg = (typename Cx<C>::R)task.sign[j];
         acc.x = fma(sg, sum.x, acc.x);
         acc.y = fma(sg, sum.y, acc.y);
@@ -149,6 +158,7 @@ struct Epilogue {
     double* xout;
     double2* cout;
     double2 cscale;
+    const double* m4;  // static outputs: optional 2x2 preconditioner block per element
 };
 
 __device__ __forceinline__ double2 dmul(double2 a, double2 b) {
@@ -157,12 +167,11 @@ __device__ __forceinline__ double2 dmul(double2 a, double2 b) {
 
 // One block = one tile of up to kWE outputs of one output block; the block's
 // instances are split over kWG thread groups (instance i goes to group
-// i % kWG) and the groups' partial sums are added in shared memory.
-constexpr int kWE = 64;
-constexpr int kWG = kThreads / kWE;
-
-template <int MODE, typename C>
+// i % kWG) and the groups' partial sums are added in shared memory.  Narrow
+// tiles (small kWE) put more blocks on the GPU when a stage has few outputs.
+template <int MODE, typename C, int kWE>
 __global__ void __launch_bounds__(kThreads) k_wedge(c3l_wedge_stage st, int n, C* ws, Epilogue ep) {
+    constexpr int kWG = kThreads / kWE;
     __shared__ c3l_instance sinst[kInstChunk];
     __shared__ C red[kWG][kWE];
     const c3l_tile tile = st.tiles[blockIdx.x];
@@ -229,8 +238,18 @@ __global__ void __launch_bounds__(kThreads) k_wedge(c3l_wedge_stage st, int n, C
         const double2 r = make_double2(s.y, -s.x);  // -i * s
         const double2 v = dmul(r, ep.scale[e]);
         const int64_t c = ep.col[e];
-        ep.xout[c] = v.x;
-        if (ep.pair[e]) ep.xout[c + 1] = r.y;
+        if (ep.m4) {  // fused preconditioner: y = M [x_c, x_c+1] (pack(unpack(.)/diag))
+            const double* m = ep.m4 + 4 * e;
+            if (ep.pair[e]) {
+                ep.xout[c] = fma(m[0], v.x, m[1] * r.y);
+                ep.xout[c + 1] = fma(m[2], v.x, m[3] * r.y);
+            } else {
+                ep.xout[c] = m[0] * v.x;
+            }
+        } else {
+            ep.xout[c] = v.x;
+            if (ep.pair[e]) ep.xout[c + 1] = r.y;
+        }
     } else if (MODE == kEom) {
         const int64_t mu = st.elements[e];
         const double2 a = to_d2(acc);
@@ -240,6 +259,20 @@ __global__ void __launch_bounds__(kThreads) k_wedge(c3l_wedge_stage st, int n, C
         const int64_t mu = st.elements[e];
         ep.cout[mu] = dmul(ep.cscale, to_d2(acc));
     }
+}
+
+template <int MODE, typename C>
+c3l_status launch_wedge(const c3l_wedge_stage& st, int n, C* ws, const Epilogue& ep, cudaStream_t s) {
+    const unsigned grid = (unsigned)st.ntiles;
+    switch (st.width) {
+        case 8: k_wedge<MODE, C, 8><<<grid, kThreads, 0, s>>>(st, n, ws, ep); break;
+        case 16: k_wedge<MODE, C, 16><<<grid, kThreads, 0, s>>>(st, n, ws, ep); break;
+        case 32: k_wedge<MODE, C, 32><<<grid, kThreads, 0, s>>>(st, n, ws, ep); break;
+        case 0:
+        case 64: k_wedge<MODE, C, 64><<<grid, kThreads, 0, s>>>(st, n, ws, ep); break;
+        default: return C3L_ERR_ARGUMENT;
+    }
+    return launch_status();
 }
 
 inline unsigned grid_for(int64_t count) {
@@ -265,10 +298,10 @@ c3l_status run_padded(const c3l_action* a, cudaStream_t s) {
     Epilogue ep{};
     for (int p = 0; p < a->npadded; ++p) {
         if (a->padded[p].ntiles <= 0) continue;
-        k_wedge<kPadded, C><<<(unsigned)a->padded[p].ntiles, kThreads, 0, s>>>(a->padded[p], a->n,
-                                                                              reinterpret_cast<C*>(a->ws), ep);
+        const c3l_status st = launch_wedge<kPadded, C>(a->padded[p], a->n, reinterpret_cast<C*>(a->ws), ep, s);
+        if (st) return st;
     }
-    return launch_status();
+    return C3L_OK;
 }
 
 template <typename C>
@@ -311,9 +344,8 @@ c3l_status static_apply(const c3l_static_action* sa, const double* x, double* xo
     ep.pair = sa->pair;
     ep.scale = reinterpret_cast<const double2*>(sa->scale);
     ep.xout = xout;
-    k_wedge<kStatic, C><<<(unsigned)sa->action.out.ntiles, kThreads, 0, s>>>(sa->action.out, sa->action.n,
-                                                                            reinterpret_cast<C*>(sa->action.ws), ep);
-    return launch_status();
+    ep.m4 = sa->pc_m4;
+    return launch_wedge<kStatic, C>(sa->action.out, sa->action.n, reinterpret_cast<C*>(sa->action.ws), ep, s);
 }
 
 template <typename C>
@@ -327,9 +359,7 @@ c3l_status eom_sigma(const c3l_eom_action* ea, const c3l_complex* xin, c3l_compl
     ep.lam = reinterpret_cast<const double2*>(ea->lam);
     ep.src = reinterpret_cast<const double2*>(xin);
     ep.cout = reinterpret_cast<double2*>(out);
-    k_wedge<kEom, C><<<(unsigned)ea->action.out.ntiles, kThreads, 0, s>>>(ea->action.out, ea->action.n,
-                                                                         reinterpret_cast<C*>(ea->action.ws), ep);
-    return launch_status();
+    return launch_wedge<kEom, C>(ea->action.out, ea->action.n, reinterpret_cast<C*>(ea->action.ws), ep, s);
 }
 
 }  // namespace
@@ -376,9 +406,7 @@ c3l_status c3l_wedge_padded(const c3l_wedge_stage* stage, int32_t n, c3l_complex
     if (!stage || !ws || n <= 0 || n > 255) return C3L_ERR_ARGUMENT;
     if (stage->ntiles <= 0) return C3L_OK;
     Epilogue ep{};
-    k_wedge<kPadded, double2><<<(unsigned)stage->ntiles, kThreads, 0, as_stream(stream)>>>(
-        *stage, n, reinterpret_cast<double2*>(ws), ep);
-    return launch_status();
+    return launch_wedge<kPadded, double2>(*stage, n, reinterpret_cast<double2*>(ws), ep, as_stream(stream));
 }
 
 c3l_status c3l_wedge_static_out(const c3l_wedge_stage* stage, int32_t n, const c3l_complex* ws, const c3l_complex* lam,
@@ -393,9 +421,8 @@ c3l_status c3l_wedge_static_out(const c3l_wedge_stage* stage, int32_t n, const c
     ep.pair = pair;
     ep.scale = reinterpret_cast<const double2*>(scale);
     ep.xout = xout;
-    k_wedge<kStatic, double2><<<(unsigned)stage->ntiles, kThreads, 0, as_stream(stream)>>>(
-        *stage, n, const_cast<double2*>(reinterpret_cast<const double2*>(ws)), ep);
-    return launch_status();
+    return launch_wedge<kStatic, double2>(*stage, n, const_cast<double2*>(reinterpret_cast<const double2*>(ws)), ep,
+                                          as_stream(stream));
 }
 
 c3l_status c3l_wedge_static_out_f32(const c3l_wedge_stage* stage, int32_t n, const c3l_complex32* ws,
@@ -410,9 +437,8 @@ c3l_status c3l_wedge_static_out_f32(const c3l_wedge_stage* stage, int32_t n, con
     ep.pair = pair;
     ep.scale = reinterpret_cast<const double2*>(scale);
     ep.xout = xout;
-    k_wedge<kStatic, float2><<<(unsigned)stage->ntiles, kThreads, 0, as_stream(stream)>>>(
-        *stage, n, const_cast<float2*>(reinterpret_cast<const float2*>(ws)), ep);
-    return launch_status();
+    return launch_wedge<kStatic, float2>(*stage, n, const_cast<float2*>(reinterpret_cast<const float2*>(ws)), ep,
+                                         as_stream(stream));
 }
 
 c3l_status c3l_wedge_eom_out(const c3l_wedge_stage* stage, int32_t n, const c3l_complex* ws, const c3l_complex* lam,
@@ -423,9 +449,8 @@ c3l_status c3l_wedge_eom_out(const c3l_wedge_stage* stage, int32_t n, const c3l_
     ep.lam = reinterpret_cast<const double2*>(lam);
     ep.src = reinterpret_cast<const double2*>(xin);
     ep.cout = reinterpret_cast<double2*>(out);
-    k_wedge<kEom, double2><<<(unsigned)stage->ntiles, kThreads, 0, as_stream(stream)>>>(
-        *stage, n, const_cast<double2*>(reinterpret_cast<const double2*>(ws)), ep);
-    return launch_status();
+    return launch_wedge<kEom, double2>(*stage, n, const_cast<double2*>(reinterpret_cast<const double2*>(ws)), ep,
+                                       as_stream(stream));
 }
 
 c3l_status c3l_wedge_source_out(const c3l_wedge_stage* stage, int32_t n, const c3l_complex* ws, c3l_complex scale,
@@ -435,9 +460,8 @@ c3l_status c3l_wedge_source_out(const c3l_wedge_stage* stage, int32_t n, const c
     Epilogue ep{};
     ep.cscale = make_double2(scale.re, scale.im);
     ep.cout = reinterpret_cast<double2*>(out);
-    k_wedge<kSource, double2><<<(unsigned)stage->ntiles, kThreads, 0, as_stream(stream)>>>(
-        *stage, n, const_cast<double2*>(reinterpret_cast<const double2*>(ws)), ep);
-    return launch_status();
+    return launch_wedge<kSource, double2>(*stage, n, const_cast<double2*>(reinterpret_cast<const double2*>(ws)), ep,
+                                          as_stream(stream));
 }
 
 c3l_status c3l_action_prepare(const c3l_action* action, const c3l_complex* t, void* stream) {

@@ -88,6 +88,13 @@ class DeviceStatic:
         self.pc_m4 = up.raw(m4)
         self.pc_col = up.raw(t.rep_col)
         self.pc_pair = up.raw(t.rep_pair)
+        # the same blocks in the JVP output stage's element order (fused M J)
+        rep_of = np.full(plan.num_amplitudes, -1, np.int64)
+        rep_of[t.rep_pos] = np.arange(t.rep_pos.size)
+        elem_rep = rep_of[prog.stages["jvp"].elements]
+        if np.any(elem_rep < 0):
+            raise rt.C3LError("JVP output elements must be tilde representatives")
+        self.pc_m4_elem = up.raw(np.ascontiguousarray(m4[elem_rep]))
         self.nrep = int(t.rep_pos.size)
         self.ia, self.ib, self.ca, self.cb = ia, ib, ca, cb
 

@@ -102,6 +102,8 @@ class ArnoldiBasis:
     converged: bool
     action_seconds: float
     wall_seconds: float
+    green: torch.Tensor | None = None     # [nshift] sink . y at dimension m (device)
+    residual: torch.Tensor | None = None  # [nshift] Arnoldi-relation residuals at m (device)
 
 
 def hessenberg_shifted(H: np.ndarray, m: int, shifts: torch.Tensor, beta: float, sinkproj: torch.Tensor | None):
@@ -161,8 +163,12 @@ class DeviceGMRES:
         self.tmp = torch.empty(n, dtype=torch.float64, device=dev)
         self.r = torch.empty(n, dtype=torch.float64, device=dev)
         self.coeff = torch.zeros(2 * (r + 2) + 4, dtype=torch.float64, device=dev)
-        self.partial = torch.empty(max(int(lib.c3l_multi_dot_scratch(r + 1, n)), 1), dtype=torch.float64, device=dev)
+        self.partial = torch.empty(max(int(lib.c3l_multi_dot_scratch(r + 1, n)), int(lib.c3l_gmres_scratch(r, n)), 1),
+                                   dtype=torch.float64, device=dev)
         self.host = torch.zeros(3 * (r + 2) + 4, dtype=torch.float64).pin_memory()
+        self.work = torch.empty(2 * n, dtype=torch.float64, device=dev)
+        self.counters = torch.zeros(4, dtype=torch.int32, device=dev)
+        self.slots = torch.zeros(r * (r + 3) + 1, dtype=torch.float64).pin_memory()  # written by the GPU
         self.history = np.zeros(4096, dtype=np.float64)
 
     def solve(self, b: torch.Tensor, x: torch.Tensor, *, rtol: float, atol: float, maxiter: int,
@@ -181,15 +187,50 @@ class DeviceGMRES:
         a.coeff, a.partial, a.host = self.coeff.data_ptr(), self.partial.data_ptr(), self.host.data_ptr()
         a.history = self.history.ctypes.data
         a.history_capacity = self.history.size
+        a.work, a.counters, a.slots = self.work.data_ptr(), self.counters.data_ptr(), self.slots.data_ptr()
+        a.pc_m4_elem = ops.pc_m4_elem.data_ptr()
+        a.partial_capacity = self.partial.numel()
         rt.check(rt.lib().c3l_gmres(C.byref(a), rt.stream_ptr(ops.device)), "gmres")
         hist = list(self.history[:min(a.history_len, self.history.size)])
-        rt.LaunchCounter.add(a.matvecs * ops.launches["jvp"] + a.history_len * 7 + 8)
+        rt.LaunchCounter.add(int(a.launches))
         return int(a.info), hist, int(a.matvecs)
 
 
+class HessenbergTracker:
+    """Device buffers of the incremental shifted solves of one Arnoldi basis."""
+
+    def __init__(self, m_max: int, shifts: torch.Tensor, with_sink: bool):
+        dev = shifts.device
+        ns = shifts.numel()
+        self.shifts = shifts
+        self.rot_c = torch.empty((m_max, ns), dtype=torch.float64, device=dev)
+        self.rot_s = torch.empty((m_max, ns), dtype=torch.complex128, device=dev)
+        self.vsink = torch.empty((m_max, ns), dtype=torch.complex128, device=dev)
+        self.carry = torch.empty(ns, dtype=torch.complex128, device=dev)
+        self.accum = torch.empty(ns, dtype=torch.complex128, device=dev)
+        self.green = torch.empty(ns, dtype=torch.complex128, device=dev) if with_sink else None
+        self.residual = torch.empty(ns, dtype=torch.float64, device=dev)
+        self.sinkproj_conj = torch.zeros(m_max, dtype=torch.complex128, device=dev) if with_sink else None
+        self.status = torch.zeros(2, dtype=torch.int64, device=dev)  # c3l_hessenberg_status (16 bytes)
+        self.status_host = torch.zeros(2, dtype=torch.int64).pin_memory()
+        self.m_max = m_max
+
+    def fill(self, st: rt.HessenbergState) -> None:
+        st.m_max, st.nshift, st.done = self.m_max, self.shifts.numel(), 0
+        st.shifts = self.shifts.data_ptr()
+        st.sinkproj_conj = rt.ptr(self.sinkproj_conj)
+        st.rot_c, st.rot_s, st.vsink = self.rot_c.data_ptr(), self.rot_s.data_ptr(), self.vsink.data_ptr()
+        st.carry, st.accum = self.carry.data_ptr(), self.accum.data_ptr()
+        st.green, st.residual, st.status = rt.ptr(self.green), self.residual.data_ptr(), self.status.data_ptr()
+
+
 def arnoldi_channels(ops, sources, shifts: torch.Tensor, *, maximum_dimension: int, residual_tolerance: float,
-                     minimum_dimension: int = 16, check_interval: int = 8, breakdown_tolerance: float = 1.0e-14):
-    """Run ``c3l_arnoldi`` on several sources at once (one stream and workspace each)."""
+                     minimum_dimension: int = 16, check_interval: int = 8, breakdown_tolerance: float = 1.0e-14,
+                     sink: torch.Tensor | None = None):
+    """Run ``c3l_arnoldi`` on several sources at once (one stream and workspace each).
+
+    With ``sink`` the bases also carry the Green function sink . (z - K)^{-1} b
+    for every shift at their final dimension (``ArnoldiBasis.green``)."""
     started = time.perf_counter()
     dev = shifts.device
     lib = rt.lib()
@@ -197,31 +238,37 @@ def arnoldi_channels(ops, sources, shifts: torch.Tensor, *, maximum_dimension: i
     m_max = int(maximum_dimension)
     nch = len(sources)
     ops.ensure_channels(nch)
-    keep = []
     chans = (rt.ArnoldiChannel * nch)()
     streams = [torch.cuda.Stream(device=dev) for _ in range(nch)]
     cur = torch.cuda.current_stream(dev)
-    Hs = []
+    sink_conj = torch.conj(sink).resolve_conj().contiguous() if sink is not None else None
+    per = []
     for c, b in enumerate(sources):
-        V = torch.empty((m_max + 1, N), dtype=torch.complex128, device=dev)
-        Hcol = torch.zeros((m_max, m_max + 1), dtype=torch.complex128, device=dev)
-        coeff = torch.zeros(2 * (m_max + 1) + 2, dtype=torch.complex128, device=dev)
-        partial = torch.empty(max(int(lib.c3l_multi_dot_scratch(m_max + 1, N)), 1), dtype=torch.complex128, device=dev)
-        host = torch.zeros(2 * (m_max + 1) + 2, dtype=torch.complex128).pin_memory()
-        H = np.zeros((m_max + 1, m_max), dtype=np.complex128)
-        Hdev = torch.empty((m_max + 1) * m_max, dtype=torch.complex128, device=dev)
-        rdev = torch.empty(shifts.numel(), dtype=torch.float64, device=dev)
-        rhost = torch.zeros(shifts.numel(), dtype=torch.float64).pin_memory()
-        cdims = np.zeros(m_max // max(check_interval, 1) + 4, dtype=np.int32)
-        cres = np.zeros(cdims.size, dtype=np.float64)
-        keep += [V, coeff, partial, host, Hdev, rdev, rhost, cdims, cres, b, Hcol]
-        Hs.append(H)
+        d = {
+            "V": torch.empty((m_max + 1, N), dtype=torch.complex128, device=dev),
+            "Hcol": torch.zeros((m_max, m_max + 1), dtype=torch.complex128, device=dev),
+            "coeff": torch.zeros(2 * (m_max + 1) + 2, dtype=torch.complex128, device=dev),
+            "partial": torch.empty(max(int(lib.c3l_multi_dot_scratch(m_max + 1, N)), 1), dtype=torch.complex128,
+                                   device=dev),
+            "host": torch.zeros(2 * (m_max + 1) + 2, dtype=torch.complex128).pin_memory(),
+            "H": np.zeros((m_max + 1, m_max), dtype=np.complex128),
+            "cdims": np.zeros(m_max // max(check_interval, 1) + 4, dtype=np.int32),
+            "hess": HessenbergTracker(m_max, shifts, sink is not None),
+            "work": torch.empty(2 * N, dtype=torch.complex128, device=dev),
+            "counters": torch.zeros(4, dtype=torch.int32, device=dev),
+            "b": b,
+        }
+        d["cres"] = np.zeros(d["cdims"].size, dtype=np.float64)
+        per.append(d)
         q = chans[c]
         q.sigma = C.addressof(ops.sigma_actions[c])
-        q.b, q.V, q.coeff, q.partial, q.host = b.data_ptr(), V.data_ptr(), coeff.data_ptr(), partial.data_ptr(), host.data_ptr()
-        q.Hcol = Hcol.data_ptr()
-        q.H, q.Hdev, q.resid_dev, q.resid_host = H.ctypes.data, Hdev.data_ptr(), rdev.data_ptr(), rhost.data_ptr()
-        q.check_dims, q.check_res, q.check_capacity = cdims.ctypes.data, cres.ctypes.data, cdims.size
+        q.b, q.sink_conj = b.data_ptr(), rt.ptr(sink_conj)
+        q.V, q.Hcol, q.coeff = d["V"].data_ptr(), d["Hcol"].data_ptr(), d["coeff"].data_ptr()
+        q.partial, q.host, q.H = d["partial"].data_ptr(), d["host"].data_ptr(), d["H"].ctypes.data
+        d["hess"].fill(q.hess)
+        q.status_host = d["hess"].status_host.data_ptr()
+        q.work, q.counters = d["work"].data_ptr(), d["counters"].data_ptr()
+        q.check_dims, q.check_res, q.check_capacity = d["cdims"].ctypes.data, d["cres"].ctypes.data, d["cdims"].size
     for st in streams:
         st.wait_stream(cur)
     sp = (C.c_void_p * nch)(*[st.cuda_stream for st in streams])
@@ -232,11 +279,12 @@ def arnoldi_channels(ops, sources, shifts: torch.Tensor, *, maximum_dimension: i
     out = []
     for c in range(nch):
         q = chans[c]
+        d = per[c]
         m = int(q.m)
-        V = keep[c * 11]
-        nchk = min(int(q.nchecks), keep[c * 11 + 7].size)
-        rt.LaunchCounter.add(m * (ops.sigma_launches + 7) + 2 * nchk + 3)
-        out.append(ArnoldiBasis(V, Hs[c][:m + 1, :m].copy(), float(q.beta), m, bool(q.breakdown),
-                                list(keep[c * 11 + 7][:nchk]), list(keep[c * 11 + 8][:nchk]), bool(q.converged),
-                                float(q.action_seconds), time.perf_counter() - started))
+        nchk = min(int(q.nchecks), d["cdims"].size)
+        rt.LaunchCounter.add(int(q.launches))
+        out.append(ArnoldiBasis(d["V"], d["H"][:m + 1, :m].copy(), float(q.beta), m, bool(q.breakdown),
+                                list(d["cdims"][:nchk]), list(d["cres"][:nchk]), bool(q.converged),
+                                float(q.action_seconds), time.perf_counter() - started,
+                                d["hess"].green, d["hess"].residual))
     return out

@@ -23,7 +23,7 @@ import numpy as np
 import torch
 
 from . import runtime as rt
-from .krylov import DeviceVectors, arnoldi_channels, hessenberg_shifted, reduced_coordinates
+from .krylov import DeviceVectors, arnoldi_channels, reduced_coordinates
 from .static import ComponentStaticProblem, _is_reference_object
 
 
@@ -250,19 +250,14 @@ def component_retarded_green(operator, sources, omega, eta: float, *, rtol: floa
     calls0 = op.action_calls
     out = []
     channels = []
-    sink_conj = torch.conj(sink).resolve_conj().contiguous()
     bases = arnoldi_channels(op.context.ops, [add.contiguous(), rem.contiguous()], shifts,
                              maximum_dimension=max_dim, residual_tolerance=rtol,
-                             minimum_dimension=min(16, max_dim), check_interval=8)
+                             minimum_dimension=min(16, max_dim), check_interval=8, sink=sink.contiguous())
     op.action_calls += sum(b.m for b in bases)
     for basis in bases:
         if not basis.converged:
             raise RuntimeError("a component EOM shifted solve failed to converge")
-        proj = torch.empty(basis.m, dtype=torch.complex128, device=dev)
-        vec.dots_c(basis.V, basis.m, sink_conj, proj)
-        proj = torch.conj(proj).resolve_conj()
-        green, resid = hessenberg_shifted(basis.H, basis.m, shifts, basis.beta, proj)
-        out.append((green.cpu().numpy(), resid.cpu().numpy()))
+        out.append((basis.green.cpu().numpy(), basis.residual.cpu().numpy()))
         channels.append(_Channel(basis, shifts))
     (ga, ra), (gr, rr) = out
     return ComponentRetardedGreen(

@@ -29,7 +29,8 @@ class ContractLevel(C.Structure):
 
 class WedgeStage(C.Structure):
     _fields_ = [("blocks", C.c_void_p), ("instances", C.c_void_p), ("tiles", C.c_void_p),
-                ("ntiles", C.c_int64), ("elements", C.c_void_p), ("digits", C.c_void_p)]
+                ("ntiles", C.c_int64), ("elements", C.c_void_p), ("digits", C.c_void_p), ("width", C.c_int32),
+                ("pad", C.c_int32)]
 
 
 class Action(C.Structure):
@@ -43,7 +44,7 @@ class StaticAction(C.Structure):
     _fields_ = [("action", Action), ("num_amplitudes", C.c_int64), ("tilde_ia", C.c_void_p),
                 ("tilde_ib", C.c_void_p), ("tilde_ca", C.c_void_p), ("tilde_cb", C.c_void_p),
                 ("canon", C.c_void_p), ("lam", C.c_void_p), ("col", C.c_void_p), ("pair", C.c_void_p),
-                ("scale", C.c_void_p)]
+                ("scale", C.c_void_p), ("pc_m4", C.c_void_p)]
 
 
 class EomAction(C.Structure):
@@ -61,16 +62,30 @@ class GmresArgs(C.Structure):
                 ("V", C.c_void_p), ("tmp", C.c_void_p), ("r", C.c_void_p), ("coeff", C.c_void_p),
                 ("partial", C.c_void_p), ("host", C.c_void_p), ("history", C.c_void_p),
                 ("history_capacity", C.c_int32), ("history_len", C.c_int32), ("info", C.c_int32),
-                ("matvecs", C.c_int32), ("use_f32", C.c_int32)]
+                ("matvecs", C.c_int32), ("use_f32", C.c_int32), ("work", C.c_void_p), ("counters", C.c_void_p),
+                ("slots", C.c_void_p), ("launches", C.c_int64), ("pc_m4_elem", C.c_void_p),
+                ("partial_capacity", C.c_int64)]
+
+
+class HessenbergStatus(C.Structure):
+    _fields_ = [("worst", C.c_uint64), ("first_break", C.c_int32), ("bad", C.c_int32)]
+
+
+class HessenbergState(C.Structure):
+    _fields_ = [("m_max", C.c_int32), ("nshift", C.c_int32), ("done", C.c_int32), ("pad", C.c_int32),
+                ("shifts", C.c_void_p), ("beta", C.c_double), ("breakdown_tol", C.c_double),
+                ("sinkproj_conj", C.c_void_p), ("rot_c", C.c_void_p), ("rot_s", C.c_void_p), ("vsink", C.c_void_p),
+                ("carry", C.c_void_p), ("accum", C.c_void_p), ("green", C.c_void_p), ("residual", C.c_void_p),
+                ("status", C.c_void_p)]
 
 
 class ArnoldiChannel(C.Structure):
-    _fields_ = [("sigma", C.c_void_p), ("b", C.c_void_p), ("V", C.c_void_p), ("Hcol", C.c_void_p), ("coeff", C.c_void_p),
-                ("partial", C.c_void_p), ("host", C.c_void_p), ("H", C.c_void_p), ("Hdev", C.c_void_p),
-                ("resid_dev", C.c_void_p), ("resid_host", C.c_void_p), ("check_dims", C.c_void_p),
-                ("check_res", C.c_void_p), ("check_capacity", C.c_int32), ("m", C.c_int32),
-                ("breakdown", C.c_int32), ("converged", C.c_int32), ("nchecks", C.c_int32), ("pad", C.c_int32),
-                ("beta", C.c_double), ("action_seconds", C.c_double)]
+    _fields_ = [("sigma", C.c_void_p), ("b", C.c_void_p), ("sink_conj", C.c_void_p), ("V", C.c_void_p),
+                ("Hcol", C.c_void_p), ("coeff", C.c_void_p), ("partial", C.c_void_p), ("host", C.c_void_p),
+                ("H", C.c_void_p), ("hess", HessenbergState), ("status_host", C.c_void_p), ("work", C.c_void_p),
+                ("counters", C.c_void_p), ("check_dims", C.c_void_p), ("check_res", C.c_void_p), ("check_capacity", C.c_int32),
+                ("m", C.c_int32), ("breakdown", C.c_int32), ("converged", C.c_int32), ("nchecks", C.c_int32),
+                ("pad", C.c_int32), ("beta", C.c_double), ("action_seconds", C.c_double), ("launches", C.c_int64)]
 
 
 EXPORTS = (
@@ -78,7 +93,7 @@ EXPORTS = (
     "c3l_wedge_eom_out", "c3l_wedge_source_out", "c3l_action_prepare", "c3l_static_apply", "c3l_eom_sigma",
     "c3l_multi_dot_scratch", "c3l_multi_dot_c", "c3l_multi_dot_r", "c3l_multi_axpy_c", "c3l_multi_axpy_r",
     "c3l_scale_c", "c3l_scale_r", "c3l_precondition", "c3l_hessenberg_shifted", "c3l_hessenberg_coordinates",
-    "c3l_hessenberg_coordinates_noalloc", "c3l_gmres", "c3l_arnoldi", "c3l_hessenberg_residual_f32",
+    "c3l_hessenberg_coordinates_noalloc", "c3l_gmres", "c3l_gmres_scratch", "c3l_arnoldi", "c3l_hessenberg_advance",
     "c3l_arnoldi_column", "c3l_static_apply_f32", "c3l_eom_sigma_f32", "c3l_action_prepare_f32", "c3l_downcast",
     "c3l_wedge_static_out_f32", "c3l_mlp_forward", "c3l_mlp_backward", "c3l_mlp_adam", "c3l_warm_features", "c3l_warm_apply", "c3l_version",
 )
@@ -118,7 +133,7 @@ def _declare(lib) -> None:
         "c3l_mlp_adam": [P, P, P, P, C.c_float, C.c_float, C.c_float, C.c_float, I32, P, P],
         "c3l_warm_features": [I64, P, P, P, P, P, P, D, D, P, P],
         "c3l_warm_apply": [I64, P, P, P, P, D, P, P],
-        "c3l_hessenberg_residual_f32": [P, I64, I32, P, I32, D, P, P],
+        "c3l_hessenberg_advance": [P, P, I64, I32, P],
         "c3l_arnoldi_column": [P, I32, P, I64, P, I64, I32, D, P],
         "c3l_arnoldi": [P, I32, I64, P, I32, I32, D, I32, I32, D, P],
     }
@@ -128,6 +143,8 @@ def _declare(lib) -> None:
         fn.restype = C.c_int
     lib.c3l_multi_dot_scratch.argtypes = [I32, I64]
     lib.c3l_multi_dot_scratch.restype = I64
+    lib.c3l_gmres_scratch.argtypes = [I32, I64]
+    lib.c3l_gmres_scratch.restype = I64
     lib.c3l_version.argtypes = []
     lib.c3l_version.restype = C.c_char_p
 
@@ -219,6 +236,7 @@ def wedge_stage(up: Uploader, stage) -> WedgeStage:
     st.ntiles = len(stage.tiles)
     st.elements = up.ptr(stage.elements) if stage.elements is not None else 0
     st.digits = up.ptr(stage.digits) if stage.digits is not None else 0
+    st.width = int(stage.width)
     return st
 
 

@@ -72,7 +72,7 @@ typedef struct {
 } c3l_block;
 
 /* A thread-block work unit: consecutive outputs of one block/task (<= 256 for
- * contraction tasks, <= 64 for wedge stages). */
+ * contraction tasks, <= the stage's width for wedge stages). */
 typedef struct {
     int32_t block;
     int32_t count;
@@ -92,6 +92,8 @@ typedef struct {
     int64_t ntiles;
     const int64_t* elements;  /* canonical stages: output vector positions */
     const int64_t* digits;    /* canonical stages: packed index digits      */
+    int32_t width;            /* outputs per tile: 8, 16, 32 or 64 (0: 64)  */
+    int32_t pad;
 } c3l_wedge_stage;
 
 /* ------------------------------------------------------------ primitives */
@@ -179,6 +181,10 @@ typedef struct {
     const int64_t* col;
     const int64_t* pair;
     const c3l_complex* scale;
+    /* optional (NULL: none): the rapidity preconditioner as one 2x2 block per
+     * output element, [elements][4] row-major, applied to the outputs in the
+     * output stage (the product M J of the Newton-Krylov inner solve) */
+    const double* pc_m4;
 } c3l_static_action;
 
 c3l_status c3l_static_apply(const c3l_static_action* action, const double* x, double* xout, void* stream);
@@ -246,10 +252,50 @@ c3l_status c3l_hessenberg_shifted(const c3l_complex* H, int64_t ldh, int32_t m, 
                                   int32_t nshift, double beta, const c3l_complex* sinkproj,
                                   c3l_complex* green, double* residual, void* stream);
 
-/* Single-precision residual-only variant for convergence checks: returns
- * residual[s] = |H[m, m-1] y_{m-1}| / beta with relative error ~cond * 1e-7. */
-c3l_status c3l_hessenberg_residual_f32(const c3l_complex* H, int64_t ldh, int32_t m, const c3l_complex* shifts,
-                                       int32_t nshift, double beta, double* residual, void* stream);
+/* Incremental shifted solves: the running state of (z_s I - H_m) y = beta e_1
+ * for all shifts while an Arnoldi basis grows.  The Givens rotations of the
+ * first j columns of z I - H do not change when columns are appended, so
+ * c3l_hessenberg_advance processes each new column once per shift and leaves,
+ * for the square system of dimension m,
+ *   green[s]    = sum_k p_k y_k           (if sinkproj_conj != NULL)
+ *   residual[s] = |h_{m,m-1} y_{m-1}| / beta
+ * (the quantities of c3l_hessenberg_shifted; ArnoldiResolvent.coefficients /
+ * _reduced_residuals, src/c3l/green/krylov.py:66-93, :257-281).  Over a whole
+ * run each shift costs one O(m^2/2) elimination, not one per check.
+ * The caller owns every buffer; the library fills shifts/nshift/beta/
+ * breakdown_tol when the state is driven by c3l_arnoldi.  Set done = 0 to
+ * start a new basis.  A column j with |h_{j+1,j}| <= breakdown_tol stops the
+ * advance there (status.first_break = j + 1; outputs are those of m = j + 1);
+ * the state is then final. */
+typedef struct {
+    unsigned long long worst;  /* bit pattern of max_s residual[s] (a non-negative double) */
+    int32_t first_break;       /* 1 + first breakdown column, 0: none */
+    int32_t bad;               /* nonzero: a non-finite residual or green value */
+} c3l_hessenberg_status;
+
+typedef struct {
+    int32_t m_max;                     /* capacity in columns                      */
+    int32_t nshift;
+    int32_t done;                      /* columns processed so far (host counter)  */
+    int32_t pad;
+    const c3l_complex* shifts;         /* device [nshift]                          */
+    double beta;
+    double breakdown_tol;
+    const c3l_complex* sinkproj_conj;  /* device [m_max]: conj(p_k), or NULL       */
+    double* rot_c;                     /* device [m_max][nshift]                   */
+    c3l_complex* rot_s;                /* device [m_max][nshift]                   */
+    c3l_complex* vsink;                /* device [m_max][nshift]                   */
+    c3l_complex* carry;                /* device [nshift]                          */
+    c3l_complex* accum;                /* device [nshift]                          */
+    c3l_complex* green;                /* device [nshift] output, or NULL          */
+    double* residual;                  /* device [nshift] output                   */
+    c3l_hessenberg_status* status;     /* device, rewritten by every call          */
+} c3l_hessenberg_state;
+
+/* Advances the state over columns [done, m) of the column-major Hessenberg
+ * Hc (column j at Hc + j*ldc holds rows 0..j+1; ldc >= m_max + 1). */
+c3l_status c3l_hessenberg_advance(c3l_hessenberg_state* state, const c3l_complex* Hc, int64_t ldc, int32_t m,
+                                  void* stream);
 
 /* Arnoldi column j on the device from the CGS2 coefficients
  * coeff = [c1 (k) | c2 (k) | |w'|^2]: Hc[j*ldc + i] = c1_i + c2_i (i < k),
@@ -269,10 +315,20 @@ c3l_status c3l_hessenberg_coordinates(const c3l_complex* H, int64_t ldh, int32_t
  * control flow (the solver of src/c3l/cc/component_solver.py:181-191): A is
  * the device JVP action, M the rapidity preconditioner.  Orthogonalization is
  * classical Gram-Schmidt twice on the device; the Givens updates run on the
- * host from one pinned read-back per inner iteration.
+ * host.  One inner iteration (JVP, preconditioner, CGS2, normalization) is a
+ * CUDA graph captured once per call and replayed with the step index kept in
+ * device memory; each iteration's Hessenberg column lands in its own slot of
+ * pinned host memory, so the host processes iteration j while the GPU runs
+ * iteration j + 1 (an iteration started after the stopping test passes is
+ * discarded).
+ * With pc_m4_elem (the preconditioner blocks in output-element order, see
+ * c3l_static_action.pc_m4) the preconditioner is applied inside the JVP's
+ * output stage instead of by a separate kernel.
  * Device buffers: V[(restart+1)*dim], tmp[dim], r[dim], x[dim] (output),
- * coeff[2*(restart+2)+3], partial[c3l_multi_dot_scratch(restart+1, dim)];
- * host: host[3*(restart+2)+2] (pinned), history[history_capacity]. */
+ * work[2*dim], counters[4] (int32), coeff[2*(restart+2)+3],
+ * partial[partial_capacity >= c3l_gmres_scratch(restart, dim)]; pinned host:
+ * host[3*(restart+2)+2], slots[restart*(restart+3)]; host: history[history_capacity].
+ * restart <= 254. */
 typedef struct {
     const c3l_static_action* jvp;
     int64_t nrep;
@@ -300,27 +356,38 @@ typedef struct {
     int32_t matvecs;
     /* input: nonzero applies the JVP with c3l_static_apply_f32 */
     int32_t use_f32;
+    double* work;
+    int32_t* counters;
+    double* slots;
+    /* output: kernels launched (graph nodes included) */
+    int64_t launches;
+    const double* pc_m4_elem;
+    int64_t partial_capacity;
 } c3l_gmres_args;
 
 c3l_status c3l_gmres(c3l_gmres_args* args, void* stream);
+/* Entries of the `partial` buffer c3l_gmres needs for (restart, dim) on the current device. */
+int64_t c3l_gmres_scratch(int32_t restart, int64_t dim);
 
 /* One Arnoldi channel (source vector and its own sigma workspace). */
 typedef struct {
     const c3l_eom_action* sigma;
     const c3l_complex* b;
-    c3l_complex* V;          /* device (m_max+1) x N, row-major        */
-    c3l_complex* Hcol;       /* device m_max x (m_max+1), column-major  */
-    c3l_complex* coeff;      /* device >= 2*(m_max+1)+1                */
-    c3l_complex* partial;    /* device c3l_multi_dot_scratch(m_max+1, N) */
-    c3l_complex* host;       /* pinned >= 2*(m_max+1)+1                */
-    c3l_complex* H;          /* host (m_max+1) x m_max, zeroed          */
-    c3l_complex* Hdev;       /* device (m_max+1) x m_max                */
-    double* resid_dev;       /* device [nshift]                         */
-    double* resid_host;      /* pinned [nshift]                         */
-    int32_t* check_dims;     /* host [check_capacity]                   */
-    double* check_res;       /* host [check_capacity]                   */
+    const c3l_complex* sink_conj;      /* device [N] conj(sink), or NULL: residuals only */
+    c3l_complex* V;                    /* device (m_max+1) x N, row-major        */
+    c3l_complex* Hcol;                 /* device m_max x (m_max+1), column-major  */
+    c3l_complex* coeff;                /* device >= 2*(m_max+1)+1                */
+    c3l_complex* partial;              /* device c3l_multi_dot_scratch(m_max+1, N) */
+    c3l_complex* host;                 /* pinned >= 2*(m_max+1)+1                */
+    c3l_complex* H;                    /* host (m_max+1) x m_max row-major, filled on return, or NULL */
+    c3l_hessenberg_state hess;         /* buffers (sinkproj_conj: device [m_max] when sink_conj is set) */
+    c3l_hessenberg_status* status_host;/* pinned                                  */
+    c3l_complex* work;                 /* device [2*N]                            */
+    int32_t* counters;                 /* device [4] (int32)                      */
+    int32_t* check_dims;               /* host [check_capacity]                   */
+    double* check_res;                 /* host [check_capacity]                   */
     int32_t check_capacity;
-    /* outputs */
+    /* outputs (hess.green / hess.residual hold the shifted solves at dimension m) */
     int32_t m;
     int32_t breakdown;
     int32_t converged;
@@ -328,16 +395,20 @@ typedef struct {
     int32_t pad;
     double beta;
     double action_seconds;
+    int64_t launches;                  /* kernels launched (graph nodes included) */
 } c3l_arnoldi_channel;
 
 /* CGS2 Arnoldi for (z I - K)^{-1} b on every channel, channel c on streams[c]
  * (src/c3l/green/krylov.py:284-417): stops a channel when the Arnoldi-relation
  * residual is <= tol for every shift (checked every check_interval steps from
  * min_dim on) or on breakdown (|h_{j+1,j}| <= breakdown_tol).  Steps run
- * without host synchronization between checks: each step's column of H is
- * formed on the device, and the host reads the new columns at each check.
- * Checks run in FP32 (c3l_hessenberg_residual_f32); a passing check is
- * confirmed in FP64 (c3l_hessenberg_shifted) before a channel stops. */
+ * without host synchronization between checks: one step (sigma, CGS2,
+ * column of H, normalization) is a CUDA graph captured once per call and
+ * replayed with the step index kept in device memory, and each check advances
+ * the channel's incremental
+ * shifted solves (c3l_hessenberg_advance, FP64) over the new columns and
+ * reads back one status word.  On return hess.green / hess.residual hold the
+ * Green function and residuals of the final dimension m. */
 c3l_status c3l_arnoldi(c3l_arnoldi_channel* channels, int32_t nchannels, int64_t N, const c3l_complex* shifts,
                        int32_t nshift, int32_t m_max, double tol, int32_t min_dim, int32_t check_interval,
                        double breakdown_tol, void* const* streams);

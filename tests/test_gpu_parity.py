@@ -8,6 +8,8 @@ reference's own CPU/device parity tests, tests/cc/test_component_jax.py).
 
 from __future__ import annotations
 
+import ctypes as C
+
 import numpy as np
 import pytest
 
@@ -164,6 +166,18 @@ def test_krylov_primitives_against_numpy(cuda_device):
     c = rng.normal(size=k) + 1j * rng.normal(size=k)
     vec.axpy_c(Vd, k, torch.from_numpy(c).to(cuda_device), -0.5 + 0.25j, wd)
     assert relerr(wd.cpu().numpy(), w + (-0.5 + 0.25j) * (c @ V)) < 1e-13
+    # long basis over a short vector (one block per row; 4 x 64 axpy blocks) and a
+    # long vector (two-pass reduction)
+    for kk, nn in ((70, 1947), (3, 10007)):
+        V2 = rng.normal(size=(kk, nn)) + 1j * rng.normal(size=(kk, nn))
+        w2 = rng.normal(size=nn) + 1j * rng.normal(size=nn)
+        V2d, w2d = torch.from_numpy(V2).to(cuda_device), torch.from_numpy(w2).to(cuda_device)
+        out2 = torch.empty(kk, dtype=torch.complex128, device=cuda_device)
+        vec.dots_c(V2d, kk, w2d, out2)
+        assert relerr(out2.cpu().numpy(), V2.conj() @ w2) < 1e-13
+        c2 = rng.normal(size=kk) + 1j * rng.normal(size=kk)
+        vec.axpy_c(V2d, kk, torch.from_numpy(c2).to(cuda_device), 0.75 - 0.5j, w2d)
+        assert relerr(w2d.cpu().numpy(), w2 + (0.75 - 0.5j) * (c2 @ V2)) < 1e-13
     Vr = rng.normal(size=(k, n))
     wr = rng.normal(size=n)
     outr = torch.empty(k, dtype=torch.float64, device=cuda_device)
@@ -181,16 +195,67 @@ def test_krylov_primitives_against_numpy(cuda_device):
     ys = [np.linalg.solve(z * np.eye(m) - H[:m, :m], e1) for z in shifts]
     assert relerr(green.cpu().numpy(), np.array([p @ y for y in ys])) < 1e-10
     assert relerr(resid.cpu().numpy(), np.array([abs(H[m, m - 1] * y[-1]) / 2.5 for y in ys])) < 1e-10
-    # single-precision convergence-check variant: same residuals to ~1e-4 relative
+
+
+def _advance(state, Hc, m_max, m, cuda_device):
     from c3lindblad_gb300 import runtime as rt
 
-    Hd = torch.from_numpy(np.ascontiguousarray(H[:m + 1, :m])).to(cuda_device)
-    r32 = torch.empty(shifts.size, dtype=torch.float64, device=cuda_device)
-    st = rt.lib().c3l_hessenberg_residual_f32(Hd.data_ptr(), m, m, torch.from_numpy(shifts).to(cuda_device).data_ptr(),
-                                              shifts.size, 2.5, r32.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    st = rt.lib().c3l_hessenberg_advance(C.byref(state), Hc.data_ptr(), m_max + 1, m,
+                                         torch.cuda.current_stream(cuda_device).cuda_stream)
     assert st == 0
-    want = np.array([abs(H[m, m - 1] * y[-1]) / 2.5 for y in ys])
-    assert np.max(np.abs(r32.cpu().numpy() - want) / want) < 1e-3
+
+
+def test_incremental_hessenberg_against_numpy(cuda_device):
+    """Column-incremental shifted solves agree with dense solves at every stop,
+    including stops inside a chunk and a breakdown column."""
+    from c3lindblad_gb300 import runtime as rt
+    from c3lindblad_gb300.krylov import HessenbergTracker
+
+    rng = np.random.default_rng(5)
+    m_max = 53
+    H = np.triu(rng.normal(size=(m_max + 1, m_max)) + 1j * rng.normal(size=(m_max + 1, m_max)), -1)
+    for j in range(m_max):
+        H[j + 1, j] = abs(H[j + 1, j]) + 0.5  # Arnoldi subdiagonals are real and positive
+    shifts = np.linspace(-3, 3, 23) + 0.1j
+    p = rng.normal(size=m_max) + 1j * rng.normal(size=m_max)
+    beta = 2.5
+    sd = torch.from_numpy(shifts).to(cuda_device)
+
+    def run(Hm, stops, brk=None):
+        Hc = torch.zeros((m_max, m_max + 1), dtype=torch.complex128)
+        for j in range(m_max):
+            Hc[j, :j + 2] = torch.from_numpy(Hm[:j + 2, j])
+        Hc = Hc.to(cuda_device)
+        tr = HessenbergTracker(m_max, sd, True)
+        tr.sinkproj_conj.copy_(torch.from_numpy(np.conj(p)))
+        state = rt.HessenbergState()
+        tr.fill(state)
+        state.beta, state.breakdown_tol = beta, 1e-14
+        for m in stops:
+            _advance(state, Hc, m_max, m, cuda_device)
+            torch.cuda.synchronize()
+            stat = tr.status.cpu().numpy()
+            mm = m if brk is None or brk >= m else brk + 1
+            assert int(stat[1] & 0xffffffff) == (0 if mm == m else brk + 1)
+            e1 = np.zeros(mm, complex)
+            e1[0] = beta
+            ys = [np.linalg.solve(z * np.eye(mm) - Hm[:mm, :mm], e1) for z in shifts]
+            want_g = np.array([p[:mm] @ y for y in ys])
+            want_r = np.array([abs(Hm[mm, mm - 1] * y[-1]) / beta for y in ys])
+            assert relerr(tr.green.cpu().numpy(), want_g) < 1e-10
+            if mm == m:
+                assert relerr(tr.residual.cpu().numpy(), want_r) < 1e-10
+                assert np.array([stat[0]]).view(np.float64)[0] == pytest.approx(want_r.max(), rel=1e-10)
+            else:
+                assert np.all(tr.residual.cpu().numpy() <= 1e-12)
+            if mm < m:
+                return
+
+    run(H, [16, 24, 29, 37, 53])
+    run(H, [3, 4, 12, 20, 21, 53])
+    Hb = H.copy()
+    Hb[31, 30] = 0.0  # breakdown at column 30
+    run(Hb, [16, 24, 36, 53], brk=30)
 
 
 # ------------------------------------------------------------ large fixtures

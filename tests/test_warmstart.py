@@ -114,7 +114,9 @@ def test_learned_warm_start_lowers_the_starting_residual_on_held_out_models(cuda
         ratios_learned.append(rl / r0)
         b = solve_component_ccsd(p, precision="mixed", warm_start=ws)
         assert b.converged and b.packed_residual_norm <= 1e-10
-        assert np.max(np.abs(a.amplitudes - b.amplitudes)) <= 1e-8 * np.max(np.abs(a.amplitudes))
+        # two Newton solves stopped by the same residual test agree to about
+        # cond(J) times the tolerance, not to rounding
+        assert np.max(np.abs(a.amplitudes - b.amplitudes)) <= 5e-8 * np.max(np.abs(a.amplitudes))
     assert len(ratios_learned) >= 4
     print(f"held-out starting residual / zero-guess residual: first-order {np.mean(ratios_first):.3f}, "
           f"learned {np.mean(ratios_learned):.3f}")
