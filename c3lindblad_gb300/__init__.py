@@ -20,13 +20,16 @@ from .response import (
     ComponentEOMContext,
     ComponentEOMProblem,
     ComponentEOMSources,
+    ArnoldiProjection,
     ComponentRetardedGreen,
+    ComponentRetardedMatrixArnoldiGreen,
     ComponentShiftedSolution,
     ComponentSigmaOperator,
     EOMCCSDProblem,
     component_eom_context,
     component_eom_sources,
     component_retarded_green,
+    component_retarded_matrix_green_arnoldi,
     eom_ccsd_problem,
 )
 
@@ -35,5 +38,6 @@ __all__ = [
     "NewtonKrylovStep", "component_static_jvp", "component_static_residual", "solve_component_ccsd",
     "ComponentEOMContext", "ComponentEOMProblem", "ComponentEOMSources", "ComponentRetardedGreen",
     "ComponentShiftedSolution", "ComponentSigmaOperator", "EOMCCSDProblem", "component_eom_context",
-    "component_eom_sources", "component_retarded_green", "eom_ccsd_problem",
+    "component_eom_sources", "component_retarded_green", "eom_ccsd_problem", "ArnoldiProjection",
+    "ComponentRetardedMatrixArnoldiGreen", "component_retarded_matrix_green_arnoldi",
 ]

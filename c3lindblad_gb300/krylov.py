@@ -130,10 +130,15 @@ def project_sink(vec: DeviceVectors, basis: ArnoldiBasis, sink: torch.Tensor) ->
 
 def reduced_coordinates(basis: ArnoldiBasis, shifts: torch.Tensor, chunk_bytes: int = 1 << 30) -> torch.Tensor:
     """Y[s, :m] with (z_s I - H_m) y = beta e_1, via caller-held R scratch."""
+    return hessenberg_coordinates(basis.H, basis.m, basis.beta, shifts, chunk_bytes)
+
+
+def hessenberg_coordinates(H: np.ndarray, m: int, beta: float, shifts: torch.Tensor,
+                           chunk_bytes: int = 1 << 30) -> torch.Tensor:
+    """Y[s, :m] with (z_s I - H[:m, :m]) y = beta e_1 (device), for a host Hessenberg H[:m+1, :m]."""
     dev = shifts.device
     lib = rt.lib()
-    m = basis.m
-    Hd = torch.from_numpy(np.ascontiguousarray(basis.H[:m + 1, :m])).to(dev)
+    Hd = torch.from_numpy(np.ascontiguousarray(H[:m + 1, :m])).to(dev)
     ns = shifts.numel()
     per = m * (m + 1) // 2
     chunk = max(1, min(ns, chunk_bytes // max(1, per * 16)))
@@ -142,7 +147,7 @@ def reduced_coordinates(basis: ArnoldiBasis, shifts: torch.Tensor, chunk_bytes: 
     for s0 in range(0, ns, chunk):
         s1 = min(ns, s0 + chunk)
         rt.check(lib.c3l_hessenberg_coordinates(Hd.data_ptr(), m, m, shifts[s0:s1].data_ptr(), s1 - s0,
-                                                float(basis.beta), scratch.data_ptr(), Y[s0:s1].data_ptr(),
+                                                float(beta), scratch.data_ptr(), Y[s0:s1].data_ptr(),
                                                 rt.stream_ptr(dev)), "hessenberg_coordinates")
         rt.LaunchCounter.add(1)
     return Y

@@ -9,8 +9,12 @@ and ``component_retarded_green`` (``:180-245``).
 ``component_retarded_green`` keeps the reference's signature and result
 type but replaces one restarted GMRES per frequency by one shift-invariant
 CGS2 Arnoldi basis per channel (the algorithm of ``src/c3l/green/krylov.py:284-417``),
-with the reduced shifted Hessenberg solves for every frequency in one launch.
-Per-frequency solution vectors are reconstructed lazily on first access.
+with the reduced shifted Hessenberg solves for every frequency advanced on the
+device as the basis grows.  Per-frequency solution vectors are reconstructed
+lazily on first access.  ``component_retarded_matrix_green_arnoldi`` is the
+many-source form (``src/c3l/cc/component_response.py:356-423, 550-625``): all
+addition/removal channels of all sources run as concurrent Arnoldi channels,
+and every sink row is contracted from each channel's basis.
 """
 
 from __future__ import annotations
@@ -23,7 +27,7 @@ import numpy as np
 import torch
 
 from . import runtime as rt
-from .krylov import DeviceVectors, arnoldi_channels, reduced_coordinates
+from .krylov import DeviceVectors, arnoldi_channels, hessenberg_coordinates, reduced_coordinates
 from .static import ComponentStaticProblem, _is_reference_object
 
 
@@ -266,3 +270,215 @@ def component_retarded_green(operator, sources, omega, eta: float, *, rtol: floa
         krylov_dimensions=tuple(ch.basis.m for ch in channels), component_action_calls=op.action_calls - calls0,
         wall_seconds=float(time.perf_counter() - started),
         peak_rss_kib=int(resource.getrusage(resource.RUSAGE_SELF).ru_maxrss), _channels=tuple(channels))
+
+
+# ===================================================== matrix Arnoldi response
+class ArnoldiProjection:
+    """One channel's projection K V_m = V_m H_m + h v_{m+1} e_m^T.
+
+    Mirrors ``ArnoldiResolvent`` (``src/c3l/green/krylov.py:28-254``); the basis
+    stays on the device (``basis`` copies it to the host on request, as the
+    reference's ``[N, m+1]`` matrix).
+    """
+
+    def __init__(self, channel_basis, residual_tolerance: float, peak_rss_kib: int):
+        b = channel_basis
+        self._V = b.V
+        self.hessenberg = b.H
+        self.source_norm = np.float64(b.beta)
+        self.breakdown = bool(b.breakdown)
+        self.check_dimensions = tuple(int(d) for d in b.check_dimensions)
+        self.check_maximum_relative_residuals = np.asarray(b.check_residuals, np.float64)
+        self.residual_tolerance = np.float64(residual_tolerance)
+        self.converged = bool(b.converged)
+        self.construction_wall_seconds = np.float64(b.wall_seconds)
+        self.action_wall_seconds = np.zeros(0, np.float64)
+        self.peak_rss_kib = int(peak_rss_kib)
+        self._final_residuals = b.residual
+
+    @property
+    def dimension(self) -> int:
+        return int(self.hessenberg.shape[1])
+
+    @property
+    def vector_dimension(self) -> int:
+        return int(self._V.shape[1])
+
+    @property
+    def terminal_coupling(self) -> complex:
+        m = self.dimension
+        return complex(self.hessenberg[m, m - 1])
+
+    @property
+    def basis(self) -> np.ndarray:
+        return self._V[:self.dimension + 1].cpu().numpy().T
+
+    def _dim(self, dimension):
+        m = self.dimension if dimension is None else dimension
+        if isinstance(m, bool) or not isinstance(m, (int, np.integer)):
+            raise TypeError("dimension must be an integer")
+        if not 1 <= m <= self.dimension:
+            raise ValueError("dimension must lie in [1, krylov_dimension]")
+        return int(m)
+
+    def _shifts(self, shifts) -> torch.Tensor:
+        z = np.asarray(shifts, dtype=np.complex128)
+        if z.ndim != 1 or z.size == 0 or not np.all(np.isfinite(z)):
+            raise ValueError("shifts must be a finite nonempty vector")
+        return torch.from_numpy(z.copy()).to(self._V.device)
+
+    def coefficients(self, shifts, *, dimension=None) -> np.ndarray:
+        """Reduced coordinates y(z) with (z - H_m) y = |b| e_1 (device solve)."""
+        m = self._dim(dimension)
+        Y = hessenberg_coordinates(self.hessenberg, m, float(self.source_norm), self._shifts(shifts))
+        return Y.cpu().numpy()
+
+    def residual_norms(self, shifts, *, dimension=None) -> np.ndarray:
+        m = self._dim(dimension)
+        reduced = self.coefficients(shifts, dimension=m)
+        return np.abs(self.hessenberg[m, m - 1] * reduced[:, -1]).astype(np.float64)
+
+    def relative_residuals(self, shifts, *, dimension=None) -> np.ndarray:
+        return self.residual_norms(shifts, dimension=dimension) / max(float(self.source_norm),
+                                                                      np.finfo(np.float64).tiny)
+
+    def solutions(self, shifts, *, dimension=None) -> np.ndarray:
+        m = self._dim(dimension)
+        Y = torch.from_numpy(self.coefficients(shifts, dimension=m)).to(self._V.device)
+        vec = DeviceVectors(self._V.device)
+        out = torch.zeros((Y.shape[0], self._V.shape[1]), dtype=torch.complex128, device=Y.device)
+        for s in range(Y.shape[0]):
+            vec.axpy_c(self._V, m, Y[s], 1.0, out[s])
+        return out.cpu().numpy()
+
+
+@dataclass(frozen=True)
+class ComponentRetardedMatrixArnoldiGreen:
+    omega: np.ndarray
+    eta: float
+    sites: tuple
+    addition: np.ndarray
+    removal: np.ndarray
+    retarded: np.ndarray
+    addition_projections: tuple
+    removal_projections: tuple
+    addition_relative_residuals: np.ndarray
+    removal_relative_residuals: np.ndarray
+    component_action_calls: int
+    component_action_wall_seconds: float
+    wall_seconds: float
+    peak_rss_kib: int
+
+
+def _validated_source_columns(operator, sources):
+    """component_response.py:496-516"""
+    columns = tuple(sources)
+    if not columns:
+        raise ValueError("at least one impurity source is required")
+    if len({item.site for item in columns}) != len(columns):
+        raise ValueError("impurity source sites must be unique")
+    if any(item.charge != columns[0].charge for item in columns):
+        raise ValueError("all impurity sources must use one response charge")
+    retained = np.asarray(columns[0].addition).size
+    for item in columns:
+        if (np.asarray(item.addition).shape != (retained,) or np.asarray(item.removal).shape != (retained,)
+                or np.asarray(item.sink).shape != (retained,)):
+            raise ValueError("impurity sources and sinks must share one retained basis")
+    if operator.dimension < retained:
+        raise ValueError("response operator is smaller than the retained sources")
+    return columns, retained
+
+
+def _validated_krylov_controls(operator, maximum, minimum, interval, tolerance):
+    """component_response.py:519-547"""
+    for v in (maximum, minimum, interval):
+        if isinstance(v, bool) or not isinstance(v, (int, np.integer)):
+            raise TypeError("Krylov dimensions and check_interval must be integers")
+    if maximum <= 0 or minimum <= 0 or interval <= 0 or not np.isfinite(tolerance) or tolerance <= 0.0:
+        raise ValueError("Krylov controls and residual tolerance must be positive")
+    maximum_dimension = int(min(maximum, operator.dimension, 4096))
+    minimum_dimension = int(min(minimum, maximum_dimension))
+    return maximum_dimension, minimum_dimension
+
+
+def component_retarded_matrix_green_arnoldi(operator, sources, omega, eta: float, *,
+                                            maximum_krylov_dimension: int = 320,
+                                            residual_tolerance: float = 1.0e-10,
+                                            minimum_krylov_dimension: int = 16,
+                                            check_interval: int = 8) -> ComponentRetardedMatrixArnoldiGreen:
+    """G^R_ab(omega) for every sink a and source b from one Arnoldi basis per source and channel.
+
+    Same inputs, controls, errors and result fields as the reference
+    (``src/c3l/cc/component_response.py:356-423``).  All 2 x len(sources)
+    channels run concurrently (one stream and sigma workspace each); for
+    channel b, ``values[:, a, b] = Y(z) (sink_a . V_m)^T`` with the reduced
+    coordinates Y solved on the device for every shift.
+    """
+    started = time.perf_counter()
+    if not hasattr(operator, "action_calls"):
+        raise TypeError("operator must be an instrumented ComponentSigmaOperator")
+    columns, retained = _validated_source_columns(operator, sources)
+    frequency = np.asarray(omega, dtype=np.float64)
+    broadening = float(eta)
+    if (frequency.ndim != 1 or frequency.size == 0 or not np.all(np.isfinite(frequency))
+            or not np.isfinite(broadening) or broadening <= 0.0):
+        raise ValueError("omega and positive eta must be finite")
+    max_dim, min_dim = _validated_krylov_controls(operator, maximum_krylov_dimension, minimum_krylov_dimension,
+                                                  check_interval, residual_tolerance)
+    ops = operator.context.ops
+    dev = ops.device
+    N = operator.dimension
+
+    def device_vec(item, which):
+        if item.device:
+            v = item.device[which]
+        else:
+            v = torch.from_numpy(np.asarray((item.addition, item.removal, item.sink)[which],
+                                            np.complex128).copy()).to(dev)
+        if v.numel() < N:
+            v = torch.cat([v, torch.zeros(N - v.numel(), dtype=torch.complex128, device=dev)])
+        return v.contiguous()
+
+    vectors = []
+    for item in columns:
+        vectors += [device_vec(item, 0), device_vec(item, 1)]
+    sinks = [device_vec(item, 2) for item in columns]
+    shifts = torch.from_numpy((frequency + 1j * broadening).astype(np.complex128)).to(dev)
+    action_seconds0 = operator.action_wall_seconds
+    t_action = time.perf_counter()
+    bases = arnoldi_channels(ops, vectors, shifts, maximum_dimension=max_dim,
+                             residual_tolerance=float(residual_tolerance), minimum_dimension=min_dim,
+                             check_interval=int(check_interval))
+    calls = sum(b.m for b in bases)
+    operator.action_calls += calls
+    operator.action_wall_seconds += time.perf_counter() - t_action
+    if not all(b.converged for b in bases):
+        raise RuntimeError("a component EOM matrix Arnoldi projection failed")
+    S = len(columns)
+    ns = frequency.size
+    values = [np.empty((ns, S, S), np.complex128), np.empty((ns, S, S), np.complex128)]
+    residuals = [np.empty((S, ns), np.float64), np.empty((S, ns), np.float64)]
+    vec = DeviceVectors(dev)
+    sink_conj = [torch.conj(s).resolve_conj().contiguous() for s in sinks]
+    for idx, basis in enumerate(bases):
+        b, kind = divmod(idx, 2)
+        m = basis.m
+        Y = reduced_coordinates(basis, shifts)                     # [ns, m]
+        for a in range(S):
+            # p_k = sink_a . v_k (bilinear), then values[s, a, b] = sum_k Y[s, k] p_k
+            pc = torch.empty(m, dtype=torch.complex128, device=dev)
+            vec.dots_c(basis.V, m, sink_conj[a], pc)               # conj(p)
+            g = torch.empty(ns, dtype=torch.complex128, device=dev)
+            vec.dots_c(Y, ns, pc, g)                               # conj(sum_k Y p)
+            values[kind][:, a, b] = np.conj(g.cpu().numpy())
+        residuals[kind][b] = basis.residual.cpu().numpy()
+    rss = int(resource.getrusage(resource.RUSAGE_SELF).ru_maxrss)
+    proj = [ArnoldiProjection(bb, residual_tolerance, rss) for bb in bases]
+    return ComponentRetardedMatrixArnoldiGreen(
+        omega=frequency, eta=broadening, sites=tuple(int(item.site) for item in columns),
+        addition=values[0], removal=values[1], retarded=values[0] + values[1],
+        addition_projections=tuple(proj[0::2]), removal_projections=tuple(proj[1::2]),
+        addition_relative_residuals=residuals[0], removal_relative_residuals=residuals[1],
+        component_action_calls=int(calls),
+        component_action_wall_seconds=float(operator.action_wall_seconds - action_seconds0),
+        wall_seconds=float(time.perf_counter() - started), peak_rss_kib=rss)

@@ -423,6 +423,46 @@ def compact_golden(path: Path) -> None:
     np.savez_compressed(path, **out)
 
 
+MATRIX_GREEN = dict(fixture="kanamori3x2", sites=(0, 1, 2), omega=np.linspace(-6.0, 6.0, 61), eta=0.2,
+                    maximum_krylov_dimension=1062)
+
+
+def export_matrix_green(path: Path) -> None:
+    """Matrix G^R_ab(omega) of the reference's one-sided Arnoldi driver
+    (component_retarded_matrix_green_arnoldi) for the three impurity orbitals
+    of the n = 9 Kanamori fixture, charge +1, at the fixture's fixed amplitudes."""
+    from c3l.cc.component_response import ComponentSigmaOperator, component_retarded_matrix_green_arnoldi
+    from c3l.cc.component_tensor import (
+        ComponentEOMProblem, ComponentStaticProblem, component_eom_context, component_eom_sources,
+    )
+    from c3l.cc.eom import eom_ccsd_problem
+
+    spec = MATRIX_GREEN
+    fx = FIXTURES[spec["fixture"]]
+    cc = build_problem(fx)
+    static = ComponentStaticProblem.compile(cc)
+    amplitudes = np.load(HERE / f"{spec['fixture']}.golden.npz")["eom_amplitudes"]
+    problem = ComponentEOMProblem.compile(eom_ccsd_problem(cc, response_spin=0), static, charge=1)
+    context = component_eom_context(problem, amplitudes)
+    op = ComponentSigmaOperator(context)
+    sources = [component_eom_sources(context, site=s) for s in spec["sites"]]
+    t0 = time.perf_counter()
+    res = component_retarded_matrix_green_arnoldi(op, sources, spec["omega"], spec["eta"],
+                                                  maximum_krylov_dimension=spec["maximum_krylov_dimension"])
+    seconds = time.perf_counter() - t0
+    np.savez_compressed(
+        path, omega=res.omega, eta=np.float64(res.eta), sites=np.asarray(res.sites, np.int64),
+        addition=res.addition, removal=res.removal, retarded=res.retarded,
+        addition_relative_residuals=res.addition_relative_residuals,
+        removal_relative_residuals=res.removal_relative_residuals,
+        addition_dimensions=np.asarray([p.dimension for p in res.addition_projections], np.int64),
+        removal_dimensions=np.asarray([p.dimension for p in res.removal_projections], np.int64),
+        maximum_krylov_dimension=np.int64(spec["maximum_krylov_dimension"]), seconds=np.float64(seconds),
+        action_calls=np.int64(res.component_action_calls))
+    print(f"  matrix green {seconds:.1f}s, dims {[p.dimension for p in res.addition_projections]} "
+          f"{[p.dimension for p in res.removal_projections]}", flush=True)
+
+
 def main() -> None:
     parser = argparse.ArgumentParser()
     parser.add_argument("--reference", default=str(HERE.parents[2] / "reference" / "src"))
@@ -431,6 +471,9 @@ def main() -> None:
     _import_reference(args.reference)
     if args.names == ["warmstart"]:
         export_warmstart_family(64, HERE / "warmstart_siam.npz")
+        return
+    if args.names == ["matrix"]:
+        export_matrix_green(HERE / f"{MATRIX_GREEN['fixture']}.matrix.npz")
         return
     names = args.names or list(FIXTURES)
     for name in names:

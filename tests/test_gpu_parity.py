@@ -150,6 +150,48 @@ def test_retarded_green_matches_reference(name, problems):
     assert np.linalg.norm(resid) / np.linalg.norm(src.addition) < 1e-8
 
 
+def test_matrix_green_arnoldi_matches_reference(problems):
+    """G^R_ab for the three impurity orbitals of the n = 9 Kanamori fixture
+    (charge +1, fixed amplitudes) against the reference's one-sided matrix
+    Arnoldi driver; all six channels run concurrently."""
+    import c3lindblad_gb300 as c3
+    from conftest import GOLDEN
+
+    spec, g, p = problems("kanamori3x2")
+    ref = np.load(GOLDEN / "kanamori3x2.matrix.npz")
+    ep = c3.ComponentEOMProblem.compile(c3.eom_ccsd_problem(p), p, 1)
+    ctx = c3.component_eom_context(ep, eom_amplitudes(g))
+    op = c3.ComponentSigmaOperator(ctx)
+    sources = [c3.component_eom_sources(ctx, site=int(s)) for s in ref["sites"]]
+    res = c3.component_retarded_matrix_green_arnoldi(
+        op, sources, ref["omega"], float(ref["eta"]), maximum_krylov_dimension=int(ref["maximum_krylov_dimension"]))
+    assert res.sites == tuple(int(s) for s in ref["sites"])
+    assert res.addition.shape == ref["addition"].shape
+    assert relerr(res.addition, ref["addition"]) < 1e-8
+    assert relerr(res.removal, ref["removal"]) < 1e-8
+    assert relerr(res.retarded, ref["retarded"]) < 1e-8
+    assert np.max(res.addition_relative_residuals) <= 1e-10
+    assert np.max(res.removal_relative_residuals) <= 1e-10
+    dims = [pr.dimension for pr in res.addition_projections + res.removal_projections]
+    want = list(ref["addition_dimensions"]) + list(ref["removal_dimensions"])
+    assert all(abs(a - b) <= 8 for a, b in zip(dims, want))
+    assert res.component_action_calls == sum(dims)
+    # a projection's reduced coordinates reproduce the shifted solve on the host
+    pr = res.addition_projections[1]
+    z = ref["omega"][:3] + 1j * float(ref["eta"])
+    Y = pr.coefficients(z)
+    m = pr.dimension
+    for i, zi in enumerate(z):
+        rhs = np.zeros(m, complex)
+        rhs[0] = pr.source_norm
+        y = np.linalg.solve(zi * np.eye(m) - pr.hessenberg[:m, :m], rhs)
+        assert relerr(Y[i], y) < 1e-9
+    with pytest.raises(ValueError):
+        c3.component_retarded_matrix_green_arnoldi(op, sources, ref["omega"], 0.0)
+    with pytest.raises(ValueError):
+        c3.component_retarded_matrix_green_arnoldi(op, [sources[0], sources[0]], ref["omega"], 0.1)
+
+
 def test_krylov_primitives_against_numpy(cuda_device):
     from c3lindblad_gb300.krylov import DeviceVectors, hessenberg_shifted
 
