@@ -31,6 +31,7 @@ from .response import (
     component_retarded_green,
     component_retarded_matrix_green_arnoldi,
     eom_ccsd_problem,
+    solve_component_shifted,
 )
 
 __all__ = [
@@ -39,5 +40,5 @@ __all__ = [
     "ComponentEOMContext", "ComponentEOMProblem", "ComponentEOMSources", "ComponentRetardedGreen",
     "ComponentShiftedSolution", "ComponentSigmaOperator", "EOMCCSDProblem", "component_eom_context",
     "component_eom_sources", "component_retarded_green", "eom_ccsd_problem", "ArnoldiProjection",
-    "ComponentRetardedMatrixArnoldiGreen", "component_retarded_matrix_green_arnoldi",
+    "ComponentRetardedMatrixArnoldiGreen", "component_retarded_matrix_green_arnoldi", "solve_component_shifted",
 ]

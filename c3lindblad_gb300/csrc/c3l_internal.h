@@ -37,6 +37,9 @@ int64_t row_dot_partial_size(const RowDot& p);  // entries of the partial buffer
 // out[r] = V[r]^H w (r < k) [and |w|^2 at r = k when self]
 c3l_status dot_rows_dev_c(const c3l_complex* V, int64_t ld, const int* cur, int self, const c3l_complex* w,
                           int64_t dim, const RowDot& p, c3l_complex* partial, c3l_complex* out, cudaStream_t s);
+// The same projections with FP32 products and sums (first CGS2 pass only).
+c3l_status dot_rows_f32acc_dev_c(const c3l_complex* V, int64_t ld, const int* cur, const c3l_complex* w, int64_t dim,
+                                 const RowDot& p, c3l_complex* out, cudaStream_t s);
 // Pass-2 projections with the Arnoldi column: c2[r] = V[r]^H w (r < k),
 // c2[k] = |w|^2, then h = sqrt(|w|^2 - |c2|^2), column j = k - 1 of Hc
 // (c1 + c2 | h), *hval = h and *next = k (done: zero between launches).

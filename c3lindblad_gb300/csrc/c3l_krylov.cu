@@ -266,6 +266,16 @@ __global__ void k_precondition(int64_t nrep, const double* __restrict__ m4, cons
     }
 }
 
+// out = inv * (z x - s) elementwise (s == NULL: 0; inv == NULL: 1)
+__global__ void k_shifted_combine(int64_t dim, double2 z, const double2* __restrict__ x, const double2* __restrict__ s,
+                                  const double2* __restrict__ inv, double2* __restrict__ out) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < dim; i += (int64_t)gridDim.x * blockDim.x) {
+        double2 v = cmul(z, x[i]);
+        if (s) v = make_double2(v.x - s[i].x, v.y - s[i].y);
+        out[i] = inv ? cmul(inv[i], v) : v;
+    }
+}
+
 unsigned axpy_grid(int64_t dim, int x = kAxX) {
     int64_t b = (dim + x - 1) / x;
     if (b > 8192) b = 8192;
@@ -431,14 +441,23 @@ __global__ void __launch_bounds__(kHessThreads) k_hessenberg_shifted(const doubl
 // Arnoldi run each shift costs one O(m^2/2) elimination instead of one per
 // check.
 //
-// Layout: one group of kAdvLanes lanes per shift; lane t advances column
-// j = cs + t of a chunk.  Rotations of earlier chunks are applied by all
-// lanes at once (phase A); inside the chunk the rotation of column cs + q is
-// formed by lane q and broadcast by warp shuffles to lanes t > q (phase B).
+// Layout: one warp per shift.  Lane (t, q) = (lane / kAdvSeg, lane % kAdvSeg)
+// advances column cs + t of a chunk of kAdvLanes new columns.  The rotations
+// of earlier columns (rows 0..cs-1, "phase A") are split into kAdvSeg
+// contiguous segments, one per lane q: a rotation step maps the carried entry
+// x affinely (x' = -conj(s) x - c h) and adds r v = (c x - s h) v to the sink
+// dot, so each lane composes its segment into x_out = A x_in + B and
+// dot += D x_in + E without knowing x_in, and the kAdvSeg lanes of a column
+// chain their maps in order.  Inside the chunk ("phase B") the rotation of
+// column cs + p is formed once (all lanes of column p compute it alike) and
+// broadcast by warp shuffles to the columns after it.
 constexpr int kAdvLanes = 8;
-constexpr int kAdvThreads = 32;
-constexpr int kAdvShiftsPerBlock = kAdvThreads / kAdvLanes;
+constexpr int kAdvSeg = 4;
+constexpr int kAdvWarps = 2;  // shifts per block
+constexpr int kAdvThreads = 32 * kAdvWarps;
+constexpr int kAdvShiftsPerBlock = kAdvWarps;
 constexpr int kAdvDepth = 4;
+static_assert(kAdvLanes * kAdvSeg == 32, "one warp per shift");
 
 // Entry (r, c) of z I - H for a column-major Hessenberg (column c at col).
 __device__ __forceinline__ double2 shifted_entry(const double2* __restrict__ col, int r, int c, double2 z) {
@@ -446,37 +465,50 @@ __device__ __forceinline__ double2 shifted_entry(const double2* __restrict__ col
     return (r == c) ? make_double2(z.x - h.x, z.y - h.y) : make_double2(-h.x, -h.y);
 }
 
+__device__ __forceinline__ double2 shfl2(double2 v, int src) {
+    return make_double2(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
+}
+
+__device__ __forceinline__ double2 cadd2(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+
 __global__ void __launch_bounds__(kAdvThreads) k_hessenberg_advance(
     const double2* __restrict__ Hc, int64_t ldc, int j0, int j1, const double2* __restrict__ shifts, int nshift,
     double beta, double btol, const double2* __restrict__ sinkc, double* __restrict__ rot_c,
     double2* __restrict__ rot_s, double2* __restrict__ vs, double2* __restrict__ carry, double2* __restrict__ accum,
     double2* __restrict__ green, double* __restrict__ residual, c3l_hessenberg_status* __restrict__ status) {
-    const unsigned full = 0xffffffffu;
-    const int lane = threadIdx.x & (kAdvLanes - 1);
-    const int sraw = blockIdx.x * kAdvShiftsPerBlock + (int)(threadIdx.x / kAdvLanes);
+    const int lane = threadIdx.x & 31;
+    const int t = lane / kAdvSeg;  // column of the chunk
+    const int q = lane % kAdvSeg;  // segment of the finalized rows
+    const int sraw = blockIdx.x * kAdvShiftsPerBlock + (int)(threadIdx.x >> 5);
     const bool live = sraw < nshift;
     const int sh = live ? sraw : nshift - 1;
+    const bool writer = live && q == 0;
     const double2 z = shifts[sh];
+    const double2 zero2 = make_double2(0.0, 0.0);
     double2 g = j0 == 0 ? make_double2(beta, 0.0) : carry[sh];
-    double2 acc = j0 == 0 ? make_double2(0.0, 0.0) : accum[sh];
+    double2 acc = j0 == 0 ? zero2 : accum[sh];
     bool stop = false;
     for (int cs = j0; cs < j1 && !stop; cs += kAdvLanes) {
-        const int c = min(cs + lane, j1 - 1);  // lanes past j1 shadow the last column (never stored)
+        const int c = min(cs + t, j1 - 1);  // lanes past j1 shadow the last column (never stored)
         const double2* col = Hc + (int64_t)c * ldc;
-        double2 x = shifted_entry(col, 0, c, z);
-        double2 dot = make_double2(0.0, 0.0);
-        // phase A: rotations of finalized columns.  Off the diagonal the entry
-        // is a = -h; the loads of a step do not depend on the arithmetic chain,
-        // so they are issued kAdvDepth steps ahead (register double buffer).
-        auto rotate_h = [&](double ci, double2 si, double2 h, double2 v) {
-            const double2 sh = cmul(si, h);
-            const double2 r = make_double2(fma(ci, x.x, -sh.x), fma(ci, x.y, -sh.y));
-            const double2 sx = cconjmul(si, x);  // conj(s) x
-            x = make_double2(fma(-ci, h.x, -sx.x), fma(-ci, h.y, -sx.y));
-            dot = make_double2(fma(r.x, v.x, fma(-r.y, v.y, dot.x)), fma(r.x, v.y, fma(r.y, v.x, dot.y)));
+        // ---- phase A: compose this lane's segment of rows [0, cs - 1) (never the diagonal: c >= cs)
+        const int offdiag = cs > 0 ? cs - 1 : 0;
+        const int seglen = (offdiag + kAdvSeg - 1) / kAdvSeg;
+        const int lo = min(offdiag, q * seglen);
+        const int hi = min(offdiag, lo + seglen);
+        double2 A = make_double2(1.0, 0.0), B = zero2, D = zero2, E = zero2;
+        auto step = [&](double ci, double2 si, double2 h, double2 v) {
+            // x_i = A x_in + B;  r_i = c x_i - s h;  x_{i+1} = -conj(s) x_i - c h
+            const double2 av = cmul(A, v);
+            D = make_double2(fma(ci, av.x, D.x), fma(ci, av.y, D.y));
+            const double2 sh2 = cmul(si, h);
+            const double2 rb = make_double2(fma(ci, B.x, -sh2.x), fma(ci, B.y, -sh2.y));
+            E = make_double2(fma(rb.x, v.x, fma(-rb.y, v.y, E.x)), fma(rb.x, v.y, fma(rb.y, v.x, E.y)));
+            const double2 sa = cconjmul(si, A);
+            A = make_double2(-sa.x, -sa.y);
+            const double2 sb = cconjmul(si, B);
+            B = make_double2(fma(-ci, h.x, -sb.x), fma(-ci, h.y, -sb.y));
         };
-        const double2 zero2 = make_double2(0.0, 0.0);
-        const int offdiag = cs - 1;  // steps i < cs - 1 never touch a diagonal entry (c >= cs)
         double bc[2][kAdvDepth];
         double2 bs[2][kAdvDepth], bv[2][kAdvDepth], bh[2][kAdvDepth];
         auto fetch = [&](int buf, int i0) {
@@ -489,47 +521,63 @@ __global__ void __launch_bounds__(kAdvThreads) k_hessenberg_advance(
                 bh[buf][u] = col[i0 + u + 1];
             }
         };
-        const int full_groups = offdiag > 0 ? offdiag / kAdvDepth : 0;
-        if (full_groups > 0) fetch(0, 0);
-        for (int gi = 0; gi < full_groups; gi += 2) {
-            if (gi + 1 < full_groups) fetch(1, (gi + 1) * kAdvDepth);
+        const int groups = (hi - lo) / kAdvDepth;
+        if (groups > 0) fetch(0, lo);
+        for (int gi = 0; gi < groups; gi += 2) {
+            if (gi + 1 < groups) fetch(1, lo + (gi + 1) * kAdvDepth);
 #pragma unroll
-            for (int u = 0; u < kAdvDepth; ++u) rotate_h(bc[0][u], bs[0][u], bh[0][u], bv[0][u]);
-            if (gi + 1 >= full_groups) break;
-            if (gi + 2 < full_groups) fetch(0, (gi + 2) * kAdvDepth);
+            for (int u = 0; u < kAdvDepth; ++u) step(bc[0][u], bs[0][u], bh[0][u], bv[0][u]);
+            if (gi + 1 >= groups) break;
+            if (gi + 2 < groups) fetch(0, lo + (gi + 2) * kAdvDepth);
 #pragma unroll
-            for (int u = 0; u < kAdvDepth; ++u) rotate_h(bc[1][u], bs[1][u], bh[1][u], bv[1][u]);
+            for (int u = 0; u < kAdvDepth; ++u) step(bc[1][u], bs[1][u], bh[1][u], bv[1][u]);
         }
-        for (int i = full_groups * kAdvDepth; i < offdiag; ++i) {
+        for (int i = lo + groups * kAdvDepth; i < hi; ++i) {
             const int64_t at = (int64_t)i * nshift + sh;
-            rotate_h(rot_c[at], rot_s[at], col[i + 1], sinkc ? vs[at] : zero2);
+            step(rot_c[at], rot_s[at], col[i + 1], sinkc ? vs[at] : zero2);
         }
-        if (cs > 0) {  // last finalized rotation: row cs may be this lane's diagonal
+        // chain the segments of this column in order (every lane of the column alike)
+        double2 x = shifted_entry(col, 0, c, z);
+        double2 dot = zero2;
+        const int base = t * kAdvSeg;
+#pragma unroll
+        for (int p = 0; p < kAdvSeg; ++p) {
+            const double2 Ap = shfl2(A, base + p), Bp = shfl2(B, base + p);
+            const double2 Dp = shfl2(D, base + p), Ep = shfl2(E, base + p);
+            dot = cadd2(dot, cadd2(cmul(Dp, x), Ep));
+            x = cadd2(cmul(Ap, x), Bp);
+        }
+        if (cs > 0) {  // last finalized rotation: row cs may be this column's diagonal
             const int64_t at = (int64_t)(cs - 1) * nshift + sh;
+            const double ci = rot_c[at];
+            const double2 si = rot_s[at];
             const double2 a = shifted_entry(col, cs, c, z);
-            const double2 h = make_double2(-a.x, -a.y);
-            rotate_h(rot_c[at], rot_s[at], h, sinkc ? vs[at] : zero2);
+            const double2 sa = cmul(si, a);
+            const double2 r = make_double2(fma(ci, x.x, sa.x), fma(ci, x.y, sa.y));
+            const double2 sx = cconjmul(si, x);
+            x = make_double2(fma(ci, a.x, -sx.x), fma(ci, a.y, -sx.y));
+            if (sinkc) {
+                const double2 v = vs[at];
+                dot = make_double2(fma(r.x, v.x, fma(-r.y, v.y, dot.x)), fma(r.x, v.y, fma(r.y, v.x, dot.y)));
+            }
         }
-        // phase B: columns of this chunk, one rotation per step
-        for (int q = 0; q < kAdvLanes; ++q) {
-            const int cq = cs + q;
+        // ---- phase B: columns of this chunk, one rotation per step
+        for (int p = 0; p < kAdvLanes; ++p) {
+            const int cq = cs + p;
             if (cq >= j1) break;
             const double2 hsub = Hc[(int64_t)cq * ldc + cq + 1];
             const bool brk = !(fabs(hsub.x) > btol);
             double fc = 0.0;
-            double2 fs = make_double2(0.0, 0.0), fv = make_double2(0.0, 0.0);
-            if (lane == q) {
-                const double2 u = sinkc ? make_double2(sinkc[cq].x, -sinkc[cq].y) : make_double2(0.0, 0.0);
+            double2 fs = zero2, fv = zero2;
+            if (t == p) {
+                const double2 u = sinkc ? make_double2(sinkc[cq].x, -sinkc[cq].y) : zero2;
                 const double2 num = make_double2(u.x - dot.x, u.y - dot.y);
                 if (cq == j1 - 1 || brk) {
                     const double2 y = cdiv(g, x);
                     const double res = hypot(hsub.x, hsub.y) * hypot(y.x, y.y) / beta;
                     double2 gr = acc;
-                    if (sinkc) {
-                        const double2 t = cmul(cdiv(num, x), g);
-                        gr = make_double2(acc.x + t.x, acc.y + t.y);
-                    }
-                    if (live) {
+                    if (sinkc) gr = cadd2(acc, cmul(cdiv(num, x), g));
+                    if (writer) {
                         residual[sh] = res;
                         if (green) green[sh] = gr;
                         if (isfinite(res) && isfinite(gr.x) && isfinite(gr.y)) {
@@ -542,11 +590,10 @@ __global__ void __launch_bounds__(kAdvThreads) k_hessenberg_advance(
                 }
                 if (!brk) {
                     givens_fast(x, make_double2(-hsub.x, -hsub.y), num, sinkc != nullptr, fc, fs, fv);
-                    const double2 t = cmul(fv, make_double2(fc * g.x, fc * g.y));
-                    acc = make_double2(acc.x + t.x, acc.y + t.y);
+                    acc = cadd2(acc, cmul(fv, make_double2(fc * g.x, fc * g.y)));
                     g = cconjmul(fs, g);
                     g = make_double2(-g.x, -g.y);
-                    if (live) {
+                    if (writer) {
                         const int64_t at = (int64_t)cq * nshift + sh;
                         rot_c[at] = fc;
                         rot_s[at] = fs;
@@ -558,17 +605,13 @@ __global__ void __launch_bounds__(kAdvThreads) k_hessenberg_advance(
                 stop = true;
                 break;
             }
-            const int src = (int)(threadIdx.x & ~(kAdvLanes - 1)) + q;
-            fc = __shfl_sync(full, fc, src);
-            fs.x = __shfl_sync(full, fs.x, src);
-            fs.y = __shfl_sync(full, fs.y, src);
-            fv.x = __shfl_sync(full, fv.x, src);
-            fv.y = __shfl_sync(full, fv.y, src);
-            g.x = __shfl_sync(full, g.x, src);
-            g.y = __shfl_sync(full, g.y, src);
-            acc.x = __shfl_sync(full, acc.x, src);
-            acc.y = __shfl_sync(full, acc.y, src);
-            if (lane > q) {
+            const int src = p * kAdvSeg;
+            fc = __shfl_sync(0xffffffffu, fc, src);
+            fs = shfl2(fs, src);
+            fv = shfl2(fv, src);
+            g = shfl2(g, src);
+            acc = shfl2(acc, src);
+            if (t > p) {
                 const double2 a = shifted_entry(col, cq + 1, c, z);
                 const double2 sa = cmul(fs, a);
                 const double2 r = make_double2(fma(fc, x.x, sa.x), fma(fc, x.y, sa.y));
@@ -766,6 +809,63 @@ __device__ void arnoldi_column_tail(const double2* __restrict__ c1, const double
 // *cur + 1, in segments of seglen; with one segment the block writes out[row]
 // directly, otherwise partial[row][seg].  COLUMN: the last block also forms
 // the Arnoldi column (single-segment case).
+// First CGS2 pass with FP32 products and sums (complex rows only): the second
+// pass, in FP64, measures and removes what the first left, and the column is
+// c1 + c2, so the Arnoldi relation and the orthogonality keep FP64 accuracy.
+__global__ void __launch_bounds__(kThreads) k_dot_rows_f32acc(const double2* __restrict__ V, int64_t ld, const int* cur,
+                                                              const double2* __restrict__ w, int64_t dim,
+                                                              double2* __restrict__ out) {
+    __shared__ float sm[2][32];
+    const int k = *cur + 1;
+    for (int row = blockIdx.x; row < k; row += gridDim.x) {
+        const double2* v = V + (int64_t)row * ld;
+        const int64_t step = blockDim.x;
+        float re = 0.0f, im = 0.0f;
+        int64_t i = threadIdx.x;
+        for (; i + 3 * step < dim; i += 4 * step) {
+            double2 a[4], b[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                a[u] = v[i + u * step];
+                b[u] = w[i + u * step];
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const float ax = (float)a[u].x, ay = (float)a[u].y, bx = (float)b[u].x, by = (float)b[u].y;
+                re = fmaf(ax, bx, fmaf(ay, by, re));
+                im = fmaf(ax, by, fmaf(-ay, bx, im));
+            }
+        }
+        for (; i < dim; i += step) {
+            const float ax = (float)v[i].x, ay = (float)v[i].y, bx = (float)w[i].x, by = (float)w[i].y;
+            re = fmaf(ax, bx, fmaf(ay, by, re));
+            im = fmaf(ax, by, fmaf(-ay, bx, im));
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            re += __shfl_down_sync(0xffffffffu, re, o);
+            im += __shfl_down_sync(0xffffffffu, im, o);
+        }
+        const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+        __syncthreads();
+        if (lane == 0) {
+            sm[0][wid] = re;
+            sm[1][wid] = im;
+        }
+        __syncthreads();
+        if (wid == 0) {
+            re = lane < (int)(blockDim.x >> 5) ? sm[0][lane] : 0.0f;
+            im = lane < (int)(blockDim.x >> 5) ? sm[1][lane] : 0.0f;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                re += __shfl_down_sync(0xffffffffu, re, o);
+                im += __shfl_down_sync(0xffffffffu, im, o);
+            }
+            if (lane == 0) out[row] = make_double2((double)re, (double)im);
+        }
+    }
+}
+
 template <typename T, bool COLUMN>
 __global__ void __launch_bounds__(kThreads) k_dot_rows_dev(const T* __restrict__ V, int64_t ld, const int* cur,
                                                            int self, const T* __restrict__ w, int64_t dim, int nseg,
@@ -1123,6 +1223,15 @@ c3l_status dot_rows_dev_c(const c3l_complex* V, int64_t ld, const int* cur, int 
                                         nullptr, nullptr, nullptr, 0, nullptr, nullptr, s);
 }
 
+c3l_status dot_rows_f32acc_dev_c(const c3l_complex* V, int64_t ld, const int* cur, const c3l_complex* w, int64_t dim,
+                                 const RowDot& p, c3l_complex* out, cudaStream_t s) {
+    if (!V || !cur || !w || !out || dim <= 0 || ld < dim) return C3L_ERR_ARGUMENT;
+    k_dot_rows_f32acc<<<p.grid, kThreads, 0, s>>>(reinterpret_cast<const double2*>(V), ld, cur,
+                                                 reinterpret_cast<const double2*>(w), dim,
+                                                 reinterpret_cast<double2*>(out));
+    return launch_status();
+}
+
 c3l_status dot_rows_column_dev_c(const c3l_complex* V, int64_t ld, const int* cur, int* next, const c3l_complex* w,
                                  int64_t dim, const RowDot& p, c3l_complex* partial, unsigned* done,
                                  const c3l_complex* c1, c3l_complex* c2, c3l_complex* Hc, int64_t ldc, double* hval,
@@ -1287,6 +1396,16 @@ c3l_status c3l_scale_r(int64_t dim, double a, const double* x, double* y, void* 
     if (dim < 0 || (dim > 0 && (!x || !y))) return C3L_ERR_ARGUMENT;
     if (dim == 0) return C3L_OK;
     k_scale_r<<<grid_for(dim), kThreads, 0, as_stream(stream)>>>(dim, a, x, y);
+    return launch_status();
+}
+
+c3l_status c3l_shifted_combine(int64_t dim, c3l_complex z, const c3l_complex* x, const c3l_complex* s,
+                               const c3l_complex* inv, c3l_complex* out, void* stream) {
+    if (dim < 0 || (dim > 0 && (!x || !out))) return C3L_ERR_ARGUMENT;
+    if (dim == 0) return C3L_OK;
+    k_shifted_combine<<<grid_for(dim), kThreads, 0, as_stream(stream)>>>(
+        dim, make_double2(z.re, z.im), reinterpret_cast<const double2*>(x), reinterpret_cast<const double2*>(s),
+        reinterpret_cast<const double2*>(inv), reinterpret_cast<double2*>(out));
     return launch_status();
 }
 

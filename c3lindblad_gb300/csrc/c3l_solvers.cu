@@ -123,6 +123,40 @@ struct OwnedEvents {
     }
 };
 
+// Complex plane rotation (LAPACK zlartg convention): real c, complex s with
+// c f + s g = r and -conj(s) f + c g = 0.
+void zlartg(c3l_complex f, c3l_complex g, double& c, c3l_complex& sn, c3l_complex& r) {
+    const double ng = std::hypot(g.re, g.im);
+    if (ng == 0.0) {
+        c = 1.0;
+        sn = {0.0, 0.0};
+        r = f;
+        return;
+    }
+    const double nf = std::hypot(f.re, f.im);
+    if (nf == 0.0) {
+        c = 0.0;
+        sn = {g.re / ng, -g.im / ng};
+        r = {ng, 0.0};
+        return;
+    }
+    const double rho = std::hypot(nf, ng);
+    c = nf / rho;
+    const c3l_complex ph{f.re / nf, f.im / nf};
+    const c3l_complex gc{g.re / rho, -g.im / rho};  // conj(g) / rho
+    sn = {ph.re * gc.re - ph.im * gc.im, ph.re * gc.im + ph.im * gc.re};
+    r = {ph.re * rho, ph.im * rho};
+}
+
+inline c3l_complex cmulh(c3l_complex a, c3l_complex b) { return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re}; }
+inline c3l_complex cconjh(c3l_complex a) { return {a.re, -a.im}; }
+inline c3l_complex caddh(c3l_complex a, c3l_complex b) { return {a.re + b.re, a.im + b.im}; }
+inline c3l_complex csubh(c3l_complex a, c3l_complex b) { return {a.re - b.re, a.im - b.im}; }
+inline c3l_complex cdivh(c3l_complex a, c3l_complex b) {
+    const double d = b.re * b.re + b.im * b.im;
+    return {(a.re * b.re + a.im * b.im) / d, (a.im * b.re - a.re * b.im) / d};
+}
+
 }  // namespace
 
 extern "C" {
@@ -328,6 +362,163 @@ c3l_status c3l_gmres(c3l_gmres_args* a, void* stream) {
     return C3L_OK;
 }
 
+c3l_status c3l_gmres_shifted(c3l_gmres_shifted_args* a, void* stream) {
+    if (!a || !a->sigma || !a->b || !a->x || !a->V || !a->tmp || !a->r || !a->coeff || !a->partial || !a->host ||
+        a->dim <= 0 || a->restart <= 0 || a->maxiter <= 0 || !(a->rtol >= 0.0) || !(a->atol >= 0.0))
+        return C3L_ERR_ARGUMENT;
+    cudaStream_t s = as_stream(stream);
+    const int64_t n = a->dim;
+    const int restart = (int)std::min<int64_t>(a->restart, n);
+    const double eps = 2.220446049250313e-16;
+    c3l_complex* V = a->V;
+    c3l_complex* host = a->host;
+    c3l_complex* coeff = a->coeff;
+    c3l_complex* ones = coeff + 2 * (restart + 2) + 2;
+    c3l_status st;
+    a->history_len = 0;
+    a->matvecs = 0;
+    a->launches = 0;
+    // A x = z x - sigma(x), then M (elementwise inverse of z - diag, or none)
+    auto apply = [&](const c3l_complex* in, c3l_complex* out, bool precondition) -> c3l_status {
+        a->matvecs += 1;
+        c3l_status q = c3l_eom_sigma(a->sigma, in, a->tmp, stream);
+        if (q) return q;
+        a->launches += a->sigma_launches + 1;
+        return c3l_shifted_combine(n, a->shift, in, a->tmp, precondition ? a->pc_inv : nullptr, out, stream);
+    };
+    auto psolve = [&](const c3l_complex* in, c3l_complex* out) -> c3l_status {
+        a->launches += 1;
+        return c3l_shifted_combine(n, c3l_complex{1.0, 0.0}, in, nullptr, a->pc_inv, out, stream);
+    };
+    auto norm = [&](const c3l_complex* v, double& out) -> c3l_status {
+        c3l_status q = c3l_multi_dot_c(v, n, 1, v, n, a->partial, coeff, stream);
+        if (q) return q;
+        a->launches += n > 8192 ? 2 : 1;
+        if ((q = d2h(host, coeff, sizeof(c3l_complex), s))) return q;
+        out = std::sqrt(std::max(host[0].re, 0.0));
+        return C3L_OK;
+    };
+    host[0] = {1.0, 0.0};
+    if (cudaMemcpyAsync(ones, host, sizeof(c3l_complex), cudaMemcpyHostToDevice, s) != cudaSuccess) return C3L_ERR_LAUNCH;
+    if (!a->use_x0 && cudaMemsetAsync(a->x, 0, n * sizeof(c3l_complex), s) != cudaSuccess) return C3L_ERR_LAUNCH;
+    double bnrm2;
+    if ((st = norm(a->b, bnrm2))) return st;
+    const double atol = std::max(a->atol, a->rtol * bnrm2);
+    a->info = 0;
+    if (bnrm2 == 0.0) {
+        return cudaMemcpyAsync(a->x, a->b, n * sizeof(c3l_complex), cudaMemcpyDeviceToDevice, s) == cudaSuccess
+                   ? C3L_OK : C3L_ERR_LAUNCH;
+    }
+    // SciPy scales the preconditioned tolerance by |M b|
+    if ((st = psolve(a->b, a->r))) return st;
+    double mb;
+    if ((st = norm(a->r, mb))) return st;
+    double ptol_max_factor = 1.0;
+    double ptol = mb * std::min(ptol_max_factor, atol / bnrm2);
+    // r = b - A x0 (or b)
+    auto residual = [&](double& out) -> c3l_status {
+        c3l_status q;
+        if (cudaMemcpyAsync(a->r, a->b, n * sizeof(c3l_complex), cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+            return C3L_ERR_LAUNCH;
+        if ((q = apply(a->x, V, false))) return q;  // V[0] as scratch for A x
+        if ((q = c3l_multi_axpy_c(V, n, 1, ones, c3l_complex{-1.0, 0.0}, a->r, n, stream))) return q;
+        a->launches += 1;
+        return norm(a->r, out);
+    };
+    double rnorm = bnrm2;
+    if (a->use_x0) {
+        if ((st = residual(rnorm))) return st;
+    } else if (cudaMemcpyAsync(a->r, a->b, n * sizeof(c3l_complex), cudaMemcpyDeviceToDevice, s) != cudaSuccess) {
+        return C3L_ERR_LAUNCH;
+    }
+    double presid = 0.0;
+    std::vector<c3l_complex> S(restart + 1), h((size_t)restart * (restart + 1)), gs(restart), y;
+    std::vector<double> gc(restart);
+    auto H = [&](int col, int row) -> c3l_complex& { return h[(size_t)col * (restart + 1) + row]; };
+    for (int iteration = 0; iteration < a->maxiter; ++iteration) {
+        if (iteration == 0 && rnorm <= atol) return C3L_OK;
+        if ((st = psolve(a->r, V))) return st;
+        double beta;
+        if ((st = norm(V, beta))) return st;
+        if ((st = c3l_scale_c(n, c3l_complex{1.0 / beta, 0.0}, V, V, stream))) return st;
+        a->launches += 1;
+        std::fill(S.begin(), S.end(), c3l_complex{0.0, 0.0});
+        std::fill(h.begin(), h.end(), c3l_complex{0.0, 0.0});
+        S[0] = {beta, 0.0};
+        bool breakdown = false;
+        int col = 0;
+        for (col = 0; col < restart; ++col) {
+            c3l_complex* w = V + (int64_t)(col + 1) * n;
+            if ((st = apply(V + (int64_t)col * n, w, true))) return st;
+            const int k = col + 1;
+            // CGS2: pass 1 with |w|^2 (row k is w itself), pass 2 with |w'|^2
+            if ((st = c3l_multi_dot_c(V, n, k + 1, w, n, a->partial, coeff, stream))) return st;
+            if ((st = c3l_multi_axpy_c(V, n, k, coeff, c3l_complex{-1.0, 0.0}, w, n, stream))) return st;
+            if ((st = c3l_multi_dot_c(V, n, k + 1, w, n, a->partial, coeff + k + 1, stream))) return st;
+            if ((st = c3l_multi_axpy_c(V, n, k, coeff + k + 1, c3l_complex{-1.0, 0.0}, w, n, stream))) return st;
+            a->launches += 2 * (n > 8192 ? 2 : 1) + 2;
+            if ((st = d2h(host, coeff, 2 * (k + 1) * sizeof(c3l_complex), s))) return st;
+            const double h0 = std::sqrt(std::max(host[k].re, 0.0));
+            double c2sq = 0.0;
+            for (int j = 0; j < k; ++j) c2sq += host[k + 1 + j].re * host[k + 1 + j].re + host[k + 1 + j].im * host[k + 1 + j].im;
+            const double h1 = std::sqrt(std::max(host[2 * k + 1].re - c2sq, 0.0));
+            for (int j = 0; j < k; ++j) H(col, j) = caddh(host[j], host[k + 1 + j]);
+            H(col, col + 1) = {h1, 0.0};
+            if (h1 <= eps * h0) {
+                H(col, col + 1) = {0.0, 0.0};
+                breakdown = true;
+            } else {
+                if ((st = c3l_scale_c(n, c3l_complex{1.0 / h1, 0.0}, w, w, stream))) return st;
+                a->launches += 1;
+            }
+            for (int j = 0; j < col; ++j) {
+                const c3l_complex n0 = H(col, j), n1 = H(col, j + 1);
+                H(col, j) = caddh(c3l_complex{gc[j] * n0.re, gc[j] * n0.im}, cmulh(gs[j], n1));
+                H(col, j + 1) = caddh(cmulh(c3l_complex{-gs[j].re, gs[j].im}, n0), c3l_complex{gc[j] * n1.re, gc[j] * n1.im});
+            }
+            double c;
+            c3l_complex sn, mag;
+            zlartg(H(col, col), H(col, col + 1), c, sn, mag);
+            gc[col] = c;
+            gs[col] = sn;
+            H(col, col) = mag;
+            H(col, col + 1) = {0.0, 0.0};
+            const c3l_complex t = cmulh(c3l_complex{-sn.re, sn.im}, S[col]);  // -conj(s) S[col]
+            S[col] = {c * S[col].re, c * S[col].im};
+            S[col + 1] = t;
+            presid = std::hypot(t.re, t.im);
+            if (a->history && a->history_len < a->history_capacity) a->history[a->history_len] = presid / bnrm2;
+            a->history_len += 1;
+            if (presid <= ptol || breakdown) break;
+        }
+        if (col == restart) col = restart - 1;
+        if (H(col, col).re == 0.0 && H(col, col).im == 0.0) S[col] = {0.0, 0.0};
+        y.assign(S.begin(), S.begin() + col + 1);
+        for (int k = col; k > 0; --k) {
+            if (y[k].re != 0.0 || y[k].im != 0.0) {
+                y[k] = cdivh(y[k], H(k, k));
+                const c3l_complex tk = y[k];
+                for (int j = 0; j < k; ++j) y[j] = csubh(y[j], cmulh(tk, H(k, j)));
+            }
+        }
+        if (y[0].re != 0.0 || y[0].im != 0.0) y[0] = cdivh(y[0], H(0, 0));
+        c3l_complex* yhost = host + 2 * (restart + 2) + 2;
+        std::copy(y.begin(), y.end(), yhost);
+        if (cudaMemcpyAsync(coeff, yhost, (col + 1) * sizeof(c3l_complex), cudaMemcpyHostToDevice, s) != cudaSuccess)
+            return C3L_ERR_LAUNCH;
+        if ((st = c3l_multi_axpy_c(V, n, col + 1, coeff, c3l_complex{1.0, 0.0}, a->x, n, stream))) return st;
+        a->launches += 1;
+        if ((st = residual(rnorm))) return st;
+        if (rnorm <= atol) break;
+        if (breakdown) break;
+        if (presid <= ptol) ptol_max_factor = std::max(eps, 0.25 * ptol_max_factor);
+        else ptol_max_factor = std::min(1.0, 1.5 * ptol_max_factor);
+        ptol = presid * std::min(ptol_max_factor, atol / rnorm);
+    }
+    a->info = rnorm <= atol ? 0 : a->maxiter;
+    return C3L_OK;
+}
+
 c3l_status c3l_arnoldi(c3l_arnoldi_channel* ch, int32_t nch, int64_t N, const c3l_complex* shifts, int32_t nshift,
                        int32_t m_max, double tol, int32_t min_dim, int32_t check_interval, double breakdown_tol,
                        void* const* streams) {
@@ -367,7 +558,8 @@ c3l_status c3l_arnoldi(c3l_arnoldi_channel* ch, int32_t nch, int64_t N, const c3
             int* next = q.counters + (1 - par);
             c3l_status r = c3l_eom_sigma(q.sigma, xnext, wfix, reinterpret_cast<void*>(cs));
             if (r) return r;
-            if ((r = c3l::dot_rows_dev_c(q.V, N, cur, 0, wfix, N, rd, q.partial, c1, cs))) return r;
+            // pass 1 in FP32 (pass 2 below is FP64 and removes what it leaves)
+            if ((r = c3l::dot_rows_f32acc_dev_c(q.V, N, cur, wfix, N, rd, c1, cs))) return r;
             if ((r = c3l::axpy_dev_c(q.V, N, cur, m_max, c1, c3l_complex{-1.0, 0.0}, wfix, N, cs))) return r;
             if ((r = c3l::dot_rows_column_dev_c(q.V, N, cur, next, wfix, N, rd, q.partial, done, c1, c2, q.Hcol, ldc,
                                                 hval, cs)))

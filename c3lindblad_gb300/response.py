@@ -19,6 +19,8 @@ and every sink row is contracted from each channel's basis.
 
 from __future__ import annotations
 
+import ctypes as C
+import dataclasses
 import resource
 import time
 from dataclasses import dataclass
@@ -160,14 +162,15 @@ class ComponentSigmaOperator:
 class ComponentShiftedSolution:
     """Per-frequency record; ``solution`` is reconstructed from the shared basis on demand."""
 
-    __slots__ = ("_channel", "_index", "converged", "info", "iterations", "true_relative_residual",
+    __slots__ = ("_channel", "_index", "_solution", "converged", "info", "iterations", "true_relative_residual",
                  "residual_history", "wall_seconds")
 
-    def __init__(self, channel, index, converged, iterations, residual, history, wall):
+    def __init__(self, channel, index, converged, iterations, residual, history, wall, *, solution=None, info=None):
         self._channel = channel
         self._index = index
+        self._solution = solution
         self.converged = converged
-        self.info = 0 if converged else 1
+        self.info = (0 if converged else 1) if info is None else int(info)
         self.iterations = iterations
         self.true_relative_residual = residual
         self.residual_history = history
@@ -175,6 +178,8 @@ class ComponentShiftedSolution:
 
     @property
     def solution(self) -> np.ndarray:
+        if self._solution is not None or self._channel is None:
+            return self._solution
         return self._channel.solutions()[self._index]
 
 
@@ -196,6 +201,137 @@ class _Channel:
         return self._solutions
 
 
+class _ShiftedGMRES:
+    """Device buffers of ``c3l_gmres_shifted`` for one operator and restart."""
+
+    def __init__(self, ops, restart: int):
+        dev = ops.device
+        n = ops.N
+        r = int(min(restart, n))
+        lib = rt.lib()
+        self.ops, self.restart = ops, r
+        self.V = torch.empty((r + 1, n), dtype=torch.complex128, device=dev)
+        self.tmp = torch.empty(n, dtype=torch.complex128, device=dev)
+        self.r = torch.empty(n, dtype=torch.complex128, device=dev)
+        self.coeff = torch.zeros(2 * (r + 2) + 4, dtype=torch.complex128, device=dev)
+        self.partial = torch.empty(max(int(lib.c3l_multi_dot_scratch(r + 1, n)), 1), dtype=torch.complex128,
+                                   device=dev)
+        self.host = torch.zeros(3 * (r + 2) + 4, dtype=torch.complex128).pin_memory()
+        self.history = np.zeros(8192, dtype=np.float64)
+        self.pc = torch.empty(n, dtype=torch.complex128, device=dev)
+
+    def solve(self, shift: complex, inverse: np.ndarray, b: torch.Tensor, x: torch.Tensor, *, rtol: float,
+              maxiter: int, use_x0: bool):
+        ops = self.ops
+        self.pc.copy_(torch.from_numpy(inverse))
+        a = rt.GmresShiftedArgs()
+        a.sigma = C.addressof(ops.sigma_action)
+        a.sigma_launches = int(ops.sigma_launches)
+        a.use_x0 = 1 if use_x0 else 0
+        a.dim = ops.N
+        a.shift = rt.cplx(shift)
+        a.pc_inv, a.b, a.x = self.pc.data_ptr(), b.data_ptr(), x.data_ptr()
+        a.rtol, a.atol = float(rtol), 0.0
+        a.restart, a.maxiter = self.restart, int(maxiter)
+        a.V, a.tmp, a.r = self.V.data_ptr(), self.tmp.data_ptr(), self.r.data_ptr()
+        a.coeff, a.partial, a.host = self.coeff.data_ptr(), self.partial.data_ptr(), self.host.data_ptr()
+        a.history, a.history_capacity = self.history.ctypes.data, self.history.size
+        rt.check(rt.lib().c3l_gmres_shifted(C.byref(a), rt.stream_ptr(ops.device)), "gmres_shifted")
+        rt.LaunchCounter.add(int(a.launches))
+        return int(a.info), list(self.history[:min(a.history_len, self.history.size)]), int(a.matvecs)
+
+
+def _true_relative_residual(ops, shift: complex, x: torch.Tensor, b: torch.Tensor, bnorm: float) -> float:
+    """|b - (z x - K x)| / |b| on the device (component_response.py:117-118)."""
+    lib = rt.lib()
+    kx = torch.empty_like(x)
+    ops.sigma(x, kx)
+    ax = torch.empty_like(x)
+    rt.check(lib.c3l_shifted_combine(x.numel(), rt.cplx(shift), x.data_ptr(), kx.data_ptr(), None, ax.data_ptr(),
+                                     rt.stream_ptr(ops.device)), "shifted_combine")
+    rt.LaunchCounter.add(1)
+    return float(torch.linalg.vector_norm(b - ax).item()) / max(bnorm, np.finfo(float).tiny)
+
+
+def _jacobi_inverse(diagonal: np.ndarray, shift: complex) -> np.ndarray:
+    """(z - diag)^{-1} with entries below sqrt(eps) left at 1 (component_response.py:88-93)."""
+    d = shift - diagonal
+    inverse = np.ones_like(d)
+    safe = np.abs(d) > np.sqrt(np.finfo(np.float64).eps)
+    inverse[safe] = 1.0 / d[safe]
+    return inverse
+
+
+def solve_component_shifted(operator, shift: complex, rhs, *, rtol: float = 1.0e-10, restart: int = 40,
+                            maxiter: int = 200, initial_solution=None) -> "ComponentShiftedSolution":
+    """Solve (z I - K) x = b by preconditioned restarted GMRES on the device.
+
+    Same signature, convergence rule and record as the reference
+    (``src/c3l/cc/component_response.py:72-128``): converged iff GMRES
+    reports success and the true relative residual is at most
+    max(10 rtol, 1e-12).
+    """
+    op = operator if isinstance(operator, ComponentSigmaOperator) else ComponentSigmaOperator(operator)
+    b = np.asarray(rhs, dtype=np.complex128)
+    if b.shape != (op.dimension,) or not np.all(np.isfinite(b)):
+        raise ValueError("shifted-response source has the wrong shape or is nonfinite")
+    ops = op.context.ops
+    dev = ops.device
+    started = time.perf_counter()
+    bd = torch.from_numpy(b.copy()).to(dev)
+    x = torch.zeros_like(bd)
+    if initial_solution is not None:
+        x.copy_(torch.from_numpy(np.asarray(initial_solution, dtype=np.complex128).copy()))
+    solver = _shifted_solver(op, restart)
+    z = complex(shift)
+    info, hist, matvecs = solver.solve(z, _jacobi_inverse(op.diagonal, z), bd, x, rtol=rtol, maxiter=maxiter,
+                                       use_x0=initial_solution is not None)
+    op.action_calls += matvecs + 1
+    true = _true_relative_residual(ops, z, x, bd, float(np.linalg.norm(b)))
+    return ComponentShiftedSolution(None, 0, bool(info == 0 and true <= max(10.0 * rtol, 1.0e-12)), len(hist), true,
+                                    tuple(hist), time.perf_counter() - started, solution=x.cpu().numpy(), info=info)
+
+
+def _shifted_solver(op, restart: int) -> _ShiftedGMRES:
+    cache = op.__dict__.setdefault("_shifted_solvers", {})
+    if restart not in cache:
+        cache[restart] = _ShiftedGMRES(op.context.ops, restart)
+    return cache[restart]
+
+
+def _retarded_green_gmres(op, add, rem, sink, freq, eta, rtol, restart, maxiter, started):
+    """The reference's per-frequency loop (component_response.py:200-233) on the device."""
+    ops = op.context.ops
+    solver = _shifted_solver(op, restart)
+    out = {}
+    for name, b in (("addition", add), ("removal", rem)):
+        x = torch.zeros_like(b)
+        bnorm = float(torch.linalg.vector_norm(b).item())
+        values = np.empty(freq.size, np.complex128)
+        records = []
+        for i, w in enumerate(freq):
+            z = complex(float(w), float(eta))
+            t0 = time.perf_counter()
+            info, hist, matvecs = solver.solve(z, _jacobi_inverse(op.diagonal, z), b, x, rtol=rtol, maxiter=maxiter,
+                                               use_x0=i > 0)
+            op.action_calls += matvecs + 1
+            true = _true_relative_residual(ops, z, x, b, bnorm)
+            converged = bool(info == 0 and true <= max(10.0 * rtol, 1.0e-12))
+            if not converged:
+                raise RuntimeError("a component EOM shifted solve failed to converge")
+            values[i] = complex(torch.dot(sink, x).item())
+            records.append(ComponentShiftedSolution(None, i, converged, len(hist), true, tuple(hist),
+                                                    time.perf_counter() - t0, solution=None, info=info))
+        out[name] = (values, records)
+    (ga, ra), (gr, rr) = out["addition"], out["removal"]
+    return ComponentRetardedGreen(
+        omega=freq, eta=float(eta), addition=ga, removal=gr, retarded=ga + gr,
+        addition_relative_residuals=np.array([r.true_relative_residual for r in ra]),
+        removal_relative_residuals=np.array([r.true_relative_residual for r in rr]),
+        krylov_dimensions=(), component_action_calls=0, wall_seconds=float(time.perf_counter() - started),
+        peak_rss_kib=int(resource.getrusage(resource.RUSAGE_SELF).ru_maxrss), _records_direct=(tuple(ra), tuple(rr)))
+
+
 @dataclass(frozen=True)
 class ComponentRetardedGreen:
     omega: np.ndarray
@@ -210,8 +346,11 @@ class ComponentRetardedGreen:
     wall_seconds: float
     peak_rss_kib: int
     _channels: tuple = ()
+    _records_direct: tuple = ()
 
     def _records(self, which: int):
+        if self._records_direct:
+            return self._records_direct[which]
         ch = self._channels[which]
         res = (self.addition_relative_residuals, self.removal_relative_residuals)[which]
         b = ch.basis
@@ -229,8 +368,16 @@ class ComponentRetardedGreen:
 
 
 def component_retarded_green(operator, sources, omega, eta: float, *, rtol: float = 1.0e-10, restart: int = 40,
-                             maxiter: int = 200) -> ComponentRetardedGreen:
-    """Addition and removal contributions to G^R(omega) (component_response.py:180-245)."""
+                             maxiter: int = 200, method: str = "arnoldi") -> ComponentRetardedGreen:
+    """Addition and removal contributions to G^R(omega) (component_response.py:180-245).
+
+    ``method="arnoldi"`` (default) solves every frequency from one CGS2
+    Arnoldi basis per channel; ``method="gmres"`` runs the reference's own
+    per-frequency loop (one preconditioned GMRES per frequency and channel,
+    started from the previous frequency's solution) with the same kernels.
+    """
+    if method not in ("arnoldi", "gmres"):
+        raise ValueError("method must be 'arnoldi' or 'gmres'")
     op = operator if isinstance(operator, ComponentSigmaOperator) else ComponentSigmaOperator(operator)
     started = time.perf_counter()
     freq = np.asarray(omega, dtype=np.float64)
@@ -248,6 +395,11 @@ def component_retarded_green(operator, sources, omega, eta: float, *, rtol: floa
     if add.numel() < N:
         pad = torch.zeros(N - add.numel(), dtype=torch.complex128, device=dev)
         add, rem, sink = (torch.cat([v, pad]) for v in (add, rem, sink))
+    if method == "gmres":
+        calls0 = op.action_calls
+        res = _retarded_green_gmres(op, add.contiguous(), rem.contiguous(), sink.contiguous(), freq, eta, rtol,
+                                    restart, maxiter, started)
+        return dataclasses.replace(res, component_action_calls=op.action_calls - calls0)
     shifts = torch.from_numpy((freq + 1j * float(eta)).astype(np.complex128)).to(dev)
     vec = DeviceVectors(dev)
     max_dim = int(min(N, restart * maxiter, 4096))

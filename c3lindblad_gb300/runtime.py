@@ -67,6 +67,16 @@ class GmresArgs(C.Structure):
                 ("partial_capacity", C.c_int64)]
 
 
+class GmresShiftedArgs(C.Structure):
+    _fields_ = [("sigma", C.c_void_p), ("sigma_launches", C.c_int32), ("use_x0", C.c_int32), ("dim", C.c_int64),
+                ("shift", Complex), ("pc_inv", C.c_void_p), ("b", C.c_void_p), ("x", C.c_void_p),
+                ("rtol", C.c_double), ("atol", C.c_double), ("restart", C.c_int32), ("maxiter", C.c_int32),
+                ("V", C.c_void_p), ("tmp", C.c_void_p), ("r", C.c_void_p), ("coeff", C.c_void_p),
+                ("partial", C.c_void_p), ("host", C.c_void_p), ("history", C.c_void_p),
+                ("history_capacity", C.c_int32), ("history_len", C.c_int32), ("info", C.c_int32),
+                ("matvecs", C.c_int32), ("launches", C.c_int64)]
+
+
 class HessenbergStatus(C.Structure):
     _fields_ = [("worst", C.c_uint64), ("first_break", C.c_int32), ("bad", C.c_int32)]
 
@@ -93,7 +103,7 @@ EXPORTS = (
     "c3l_wedge_eom_out", "c3l_wedge_source_out", "c3l_action_prepare", "c3l_static_apply", "c3l_eom_sigma",
     "c3l_multi_dot_scratch", "c3l_multi_dot_c", "c3l_multi_dot_r", "c3l_multi_axpy_c", "c3l_multi_axpy_r",
     "c3l_scale_c", "c3l_scale_r", "c3l_precondition", "c3l_hessenberg_shifted", "c3l_hessenberg_coordinates",
-    "c3l_hessenberg_coordinates_noalloc", "c3l_gmres", "c3l_gmres_scratch", "c3l_arnoldi", "c3l_hessenberg_advance",
+    "c3l_hessenberg_coordinates_noalloc", "c3l_gmres", "c3l_gmres_scratch", "c3l_gmres_shifted", "c3l_shifted_combine", "c3l_arnoldi", "c3l_hessenberg_advance",
     "c3l_arnoldi_column", "c3l_static_apply_f32", "c3l_eom_sigma_f32", "c3l_action_prepare_f32", "c3l_downcast",
     "c3l_wedge_static_out_f32", "c3l_mlp_forward", "c3l_mlp_backward", "c3l_mlp_adam", "c3l_warm_features", "c3l_warm_apply", "c3l_version",
 )
@@ -124,6 +134,8 @@ def _declare(lib) -> None:
         "c3l_hessenberg_coordinates": [P, I64, I32, P, I32, D, P, P, P],
         "c3l_hessenberg_coordinates_noalloc": [P, I64, I32, P, I32, D, P, P],
         "c3l_gmres": [P, P],
+        "c3l_gmres_shifted": [P, P],
+        "c3l_shifted_combine": [I64, Complex, P, P, P, P, P],
         "c3l_static_apply_f32": [P, P, P, P],
         "c3l_eom_sigma_f32": [P, P, P, P],
         "c3l_action_prepare_f32": [P, P, P],

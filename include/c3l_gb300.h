@@ -235,6 +235,12 @@ c3l_status c3l_multi_axpy_r(const double* V, int64_t ld, int32_t k, const double
 c3l_status c3l_scale_c(int64_t dim, c3l_complex a, const c3l_complex* x, c3l_complex* y, void* stream);
 c3l_status c3l_scale_r(int64_t dim, double a, const double* x, double* y, void* stream);
 
+/* out = inv * (z x - s) elementwise; s == NULL reads as 0 and inv == NULL as 1.
+ * The shifted operator and Jacobi preconditioner of
+ * src/c3l/cc/component_response.py:88-103 (A x = z x - K x, M = (z - diag)^{-1}). */
+c3l_status c3l_shifted_combine(int64_t dim, c3l_complex z, const c3l_complex* x, const c3l_complex* s,
+                               const c3l_complex* inv, c3l_complex* out, void* stream);
+
 /* Real preconditioner pack(unpack(x) / diag) as 2x2 blocks per tilde orbit
  * (src/c3l/cc/newton_krylov.py:158-192). m4: [nrep][4] row-major blocks. */
 c3l_status c3l_precondition(int64_t nrep, const double* m4, const int64_t* col, const int64_t* pair,
@@ -368,6 +374,47 @@ typedef struct {
 c3l_status c3l_gmres(c3l_gmres_args* args, void* stream);
 /* Entries of the `partial` buffer c3l_gmres needs for (restart, dim) on the current device. */
 int64_t c3l_gmres_scratch(int32_t restart, int64_t dim);
+
+/* Left-preconditioned restarted GMRES for one shifted EOM system
+ * (z I - K) x = b with SciPy's control flow (solve_component_shifted,
+ * src/c3l/cc/component_response.py:72-128): A x = z x - sigma(x) with the
+ * device sigma action, M = pc_inv elementwise (NULL: none), optional initial
+ * solution in x (use_x0).  CGS2 orthogonalization on the device, complex
+ * Givens updates (zlartg convention) on the host from one pinned read-back
+ * per inner iteration.  This is the reference's per-frequency algorithm; the
+ * batched form is c3l_arnoldi.
+ * Device buffers: V[(restart+1)*dim], tmp[dim], r[dim], x[dim],
+ * coeff[2*(restart+2)+3], partial[c3l_multi_dot_scratch(restart+1, dim)];
+ * pinned host: host[3*(restart+2)+3]; host: history[history_capacity]. */
+typedef struct {
+    const c3l_eom_action* sigma;
+    int32_t sigma_launches;  /* kernels per sigma call (for the launch count) */
+    int32_t use_x0;
+    int64_t dim;
+    c3l_complex shift;
+    const c3l_complex* pc_inv;
+    const c3l_complex* b;
+    c3l_complex* x;
+    double rtol;
+    double atol;
+    int32_t restart;
+    int32_t maxiter;
+    c3l_complex* V;
+    c3l_complex* tmp;
+    c3l_complex* r;
+    c3l_complex* coeff;
+    c3l_complex* partial;
+    c3l_complex* host;
+    double* history;
+    int32_t history_capacity;
+    /* outputs */
+    int32_t history_len;
+    int32_t info;
+    int32_t matvecs;
+    int64_t launches;
+} c3l_gmres_shifted_args;
+
+c3l_status c3l_gmres_shifted(c3l_gmres_shifted_args* args, void* stream);
 
 /* One Arnoldi channel (source vector and its own sigma workspace). */
 typedef struct {
