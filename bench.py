@@ -164,6 +164,14 @@ def run_gpu(args) -> dict:
     for _ in range(args.warmup):
         step(base, eom_problem)
     torch.cuda.synchronize()
+    if args.profile_step:
+        # one step inside an NVTX range "step" (for ncu --nvtx-include step/), then stop
+        t0 = time.perf_counter()
+        torch.cuda.nvtx.range_push("step")
+        step(base, eom_problem)
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
+        return {"profile_step_seconds": time.perf_counter() - t0, "workload": args.workload}
     if ws > 1:
         torch.distributed.barrier()
     times = []
@@ -409,6 +417,8 @@ def main() -> None:
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="siam10", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-step", action="store_true",
+                    help="run the warm-up steps and one step inside an NVTX range named 'step', then exit")
     args = ap.parse_args()
     out = run_reference(args) if args.impl == "reference" else run_gpu(args)
     if out is not None:

@@ -111,15 +111,11 @@ __device__ __forceinline__ void powers(int n, int64_t* pw) {
     for (int i = 1; i < 6; ++i) pw[i] = pw[i - 1] * n;
 }
 
+// One padded entry e of a contraction task: const + sum_j sign_j sum_m
+// vec_j[m] src_j[... m at axis_j ...] (interior products).
 template <typename C>
-__global__ void __launch_bounds__(kThreads) k_contract(c3l_contract_level lv, int n, const C* __restrict__ vectors,
-                                                        C* __restrict__ ws) {
-    const c3l_tile tile = lv.tiles[blockIdx.x];
-    if ((int)threadIdx.x >= tile.count) return;
-    const c3l_contract_task& task = lv.tasks[tile.block];
-    int64_t pw[6];
-    powers(n, pw);
-    const int64_t e = tile.start + threadIdx.x;
+__device__ __forceinline__ void contract_entry(const c3l_contract_task& task, int64_t e, int n, const int64_t* pw,
+                                               const C* __restrict__ vectors, C* __restrict__ ws) {
     C acc = Cx<C>::make(0.0, 0.0);
     if (task.const_off >= 0) acc = vectors[task.const_off + e];
     for (int j = 0; j < task.nsrc; ++j) {
@@ -145,6 +141,46 @@ __global__ void __launch_bounds__(kThreads) k_contract(c3l_contract_level lv, in
         acc.y = fma(sg, sum.y, acc.y);
     }
     ws[task.dst_off + e] = acc;
+}
+
+template <typename C>
+__global__ void __launch_bounds__(kThreads) k_contract(c3l_contract_level lv, int n, const C* __restrict__ vectors,
+                                                        C* __restrict__ ws) {
+    const c3l_tile tile = lv.tiles[blockIdx.x];
+    if ((int)threadIdx.x >= tile.count) return;
+    int64_t pw[6];
+    powers(n, pw);
+    contract_entry<C>(lv.tasks[tile.block], tile.start + threadIdx.x, n, pw, vectors, ws);
+}
+
+// The small trailing contraction levels (each a few tiles, each level
+// depending on the previous one) as one launch of one thread-block cluster:
+// the cluster's CTAs stride over a level's tiles, then meet at a hardware
+// cluster barrier (release/acquire) before the next level.  Every CTA reaches
+// every barrier.
+constexpr int kLevelCluster = 8;
+constexpr int kClusterLevelMaxTiles = kLevelCluster;  // one round per level
+
+struct LevelPack {
+    c3l_contract_level lv[C3L_MAX_LEVELS];
+    int first;
+    int count;
+};
+
+template <typename C>
+__global__ void __launch_bounds__(kThreads) k_contract_cluster(LevelPack pack, int n, const C* __restrict__ vectors,
+                                                                C* __restrict__ ws) {
+    int64_t pw[6];
+    powers(n, pw);
+    for (int l = pack.first; l < pack.first + pack.count; ++l) {
+        const c3l_contract_level lv = pack.lv[l];
+        for (int64_t t = blockIdx.x; t < lv.ntiles; t += gridDim.x) {
+            const c3l_tile tile = lv.tiles[t];
+            if ((int)threadIdx.x < tile.count)
+                contract_entry<C>(lv.tasks[tile.block], tile.start + threadIdx.x, n, pw, vectors, ws);
+        }
+        asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+    }
 }
 
 enum WedgeMode { kPadded = 0, kStatic = 1, kEom = 2, kSource = 3 };
@@ -284,11 +320,36 @@ inline unsigned grid_for(int64_t count) {
 
 template <typename C>
 c3l_status run_levels(const c3l_action* a, cudaStream_t s) {
-    for (int l = 0; l < a->nlevels; ++l) {
+    // levels [tail, nlevels) are all small: one cluster launch runs them
+    int tail = a->nlevels;
+    while (tail > 0 && a->levels[tail - 1].ntiles <= kClusterLevelMaxTiles) --tail;
+    if (a->nlevels - tail < 2) tail = a->nlevels;  // a single small level gains nothing
+    for (int l = 0; l < tail; ++l) {
         if (a->levels[l].ntiles <= 0) continue;
         k_contract<C><<<(unsigned)a->levels[l].ntiles, kThreads, 0, s>>>(a->levels[l], a->n,
                                                                         reinterpret_cast<const C*>(a->vectors),
                                                                         reinterpret_cast<C*>(a->ws));
+    }
+    if (tail < a->nlevels) {
+        LevelPack pack{};
+        for (int l = 0; l < a->nlevels; ++l) pack.lv[l] = a->levels[l];
+        pack.first = tail;
+        pack.count = a->nlevels - tail;
+        cudaLaunchConfig_t cfg{};
+        cfg.gridDim = dim3(kLevelCluster, 1, 1);
+        cfg.blockDim = dim3(kThreads, 1, 1);
+        cfg.dynamicSmemBytes = 0;
+        cfg.stream = s;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = kLevelCluster;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        if (cudaLaunchKernelEx(&cfg, k_contract_cluster<C>, pack, a->n, reinterpret_cast<const C*>(a->vectors),
+                               reinterpret_cast<C*>(a->ws)) != cudaSuccess)
+            return C3L_ERR_LAUNCH;
     }
     return launch_status();
 }

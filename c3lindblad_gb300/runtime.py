@@ -299,9 +299,17 @@ class LaunchCounter:
         return c
 
 
+CLUSTER_LEVEL_MAX_TILES = 8  # levels this small at the end of the list run as one cluster launch
+
+
 def action_launches(a: Action) -> int:
     k = 1 if a.scatter_count > 0 else 0
-    k += sum(1 for i in range(a.nlevels) if a.levels[i].ntiles > 0)
+    tail = a.nlevels
+    while tail > 0 and a.levels[tail - 1].ntiles <= CLUSTER_LEVEL_MAX_TILES:
+        tail -= 1
+    if a.nlevels - tail < 2:
+        tail = a.nlevels
+    k += sum(1 for i in range(tail) if a.levels[i].ntiles > 0) + (1 if tail < a.nlevels else 0)
     k += sum(1 for i in range(a.npadded) if a.padded[i].ntiles > 0)
     k += 1 if a.out.ntiles > 0 else 0
     return k

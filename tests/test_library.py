@@ -51,3 +51,25 @@ def test_bad_arguments_are_rejected_before_launch():
     assert lib.c3l_hessenberg_shifted(None, 4, 4, None, 1, 1.0, None, None, None, None) == 1
     assert lib.c3l_static_apply(None, None, None, None) == 1
     assert lib.c3l_eom_sigma(None, None, None, None) == 1
+
+
+def test_krylov_drivers_reject_bad_arguments_before_launch():
+    """The drivers and the incremental shifted solves validate their structs on the host."""
+    import ctypes as C
+
+    from c3lindblad_gb300 import runtime
+
+    lib = runtime.load_library()
+    assert lib.c3l_gmres(None, None) == 1
+    assert lib.c3l_gmres_shifted(None, None) == 1
+    assert lib.c3l_gmres_shifted(C.byref(runtime.GmresShiftedArgs()), None) == 1  # all pointers null
+    assert lib.c3l_arnoldi(None, 0, 10, None, 1, 4, 1e-10, 1, 8, 1e-14, None) == 1
+    assert lib.c3l_hessenberg_advance(None, None, 5, 4, None) == 1
+    st = runtime.HessenbergState()  # zero sizes and null buffers
+    assert lib.c3l_hessenberg_advance(C.byref(st), None, 5, 4, None) == 1
+    assert lib.c3l_shifted_combine(-1, runtime.cplx(1.0), None, None, None, None, None) == 1
+    assert lib.c3l_shifted_combine(0, runtime.cplx(1.0), None, None, None, None, None) == 0  # empty is a no-op
+    # capacity limits are stated in the header and enforced
+    assert lib.c3l_arnoldi(None, 1, 10, None, 1, 5000, 1e-10, 1, 8, 1e-14, None) == 1
+    assert lib.c3l_gmres_scratch(0, 10) == 0
+    assert lib.c3l_gmres_scratch(40, 20933) >= 42
