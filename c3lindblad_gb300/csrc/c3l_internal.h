@@ -77,4 +77,9 @@ c3l_status gm_axpy_dot(const double* V, int64_t ld, const int* cur, int* next, c
 c3l_status gm_scale(double* V, int64_t ld, const int* cur, const double* c2, const double* hval, double eps,
                     const double* w, int64_t n, const GmPlan& p, double* xnext, cudaStream_t s);
 
+// c3l_hessenberg_advance for several states in one launch (up to 16): the
+// rotation chains of all channels fill the GPU together.
+c3l_status hessenberg_advance_many(c3l_hessenberg_state* const* states, const c3l_complex* const* Hc,
+                                   const int64_t* ldc, const int32_t* m, int count, cudaStream_t s);
+
 }  // namespace c3l

@@ -13,6 +13,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <mutex>
 #include <type_traits>
 
@@ -346,6 +347,33 @@ __device__ __forceinline__ void givens_fast(double2 a, double2 b, double2 num, b
     }
 }
 
+// The same rotation and v = num / r from one reciprocal square root:
+// inv = 1 / (|a| rho) gives c = |a|^2 inv, s = a conj(b) inv and
+// 1 / r = conj(a) inv (r = a rho / |a|).  Falls back to the careful form
+// when |a|^2 rho^2 leaves the safe range.
+__device__ __forceinline__ void givens_one_rsqrt(double2 a, double2 b, double2 num, bool want_v, double& c,
+                                                 double2& s, double2& v) {
+    const double na2 = fma(a.x, a.x, a.y * a.y);
+    const double nb2 = fma(b.x, b.x, b.y * b.y);
+    const double q = na2 * (na2 + nb2);
+    if (!(q > 1e-290 && q < 1e290)) {
+        double2 r;
+        givens(a, b, c, s, r);
+        v = want_v ? cdiv(num, r) : make_double2(0.0, 0.0);
+        return;
+    }
+    const double inv = rsqrt(q);
+    c = na2 * inv;
+    const double2 ab = cconjmul(b, a);  // a conj(b)
+    s = make_double2(ab.x * inv, ab.y * inv);
+    if (want_v) {
+        const double2 t = cconjmul(a, num);  // conj(a) num
+        v = make_double2(t.x * inv, t.y * inv);
+    } else {
+        v = make_double2(0.0, 0.0);
+    }
+}
+
 // Streamed Givens QR of (z I - H_m) with the transposed forward solve
 // u = R^{-T} p, so that green = p^T y = sum_k u_k (Q^H beta e1)_k without
 // storing R.  Shared memory: w[m] (current working row), acc[m].  Thread 0
@@ -441,24 +469,6 @@ __global__ void __launch_bounds__(kHessThreads) k_hessenberg_shifted(const doubl
 // Arnoldi run each shift costs one O(m^2/2) elimination instead of one per
 // check.
 //
-// Layout: one warp per shift.  Lane (t, q) = (lane / kAdvSeg, lane % kAdvSeg)
-// advances column cs + t of a chunk of kAdvLanes new columns.  The rotations
-// of earlier columns (rows 0..cs-1, "phase A") are split into kAdvSeg
-// contiguous segments, one per lane q: a rotation step maps the carried entry
-// x affinely (x' = -conj(s) x - c h) and adds r v = (c x - s h) v to the sink
-// dot, so each lane composes its segment into x_out = A x_in + B and
-// dot += D x_in + E without knowing x_in, and the kAdvSeg lanes of a column
-// chain their maps in order.  Inside the chunk ("phase B") the rotation of
-// column cs + p is formed once (all lanes of column p compute it alike) and
-// broadcast by warp shuffles to the columns after it.
-constexpr int kAdvLanes = 8;
-constexpr int kAdvSeg = 4;
-constexpr int kAdvWarps = 2;  // shifts per block
-constexpr int kAdvThreads = 32 * kAdvWarps;
-constexpr int kAdvShiftsPerBlock = kAdvWarps;
-constexpr int kAdvDepth = 4;
-static_assert(kAdvLanes * kAdvSeg == 32, "one warp per shift");
-
 // Entry (r, c) of z I - H for a column-major Hessenberg (column c at col).
 __device__ __forceinline__ double2 shifted_entry(const double2* __restrict__ col, int r, int c, double2 z) {
     const double2 h = col[r];
@@ -471,102 +481,113 @@ __device__ __forceinline__ double2 shfl2(double2 v, int src) {
 
 __device__ __forceinline__ double2 cadd2(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
 
-__global__ void __launch_bounds__(kAdvThreads) k_hessenberg_advance(
-    const double2* __restrict__ Hc, int64_t ldc, int j0, int j1, const double2* __restrict__ shifts, int nshift,
-    double beta, double btol, const double2* __restrict__ sinkc, double* __restrict__ rot_c,
-    double2* __restrict__ rot_s, double2* __restrict__ vs, double2* __restrict__ carry, double2* __restrict__ accum,
-    double2* __restrict__ green, double* __restrict__ residual, c3l_hessenberg_status* __restrict__ status) {
+// Several channels' advances in one launch (blockIdx.y = channel), so that
+// the rotation chains of all channels fill the GPU together.  Layout: a warp
+// holds kMjShifts shifts x kMjLanes columns; lane t of a shift advances column
+// cs + t of a chunk, applying the finalized rotations of rows 0..cs-1 in
+// sequence (register double-buffered prefetch) and then the in-chunk
+// rotations, each formed by lane p and broadcast by shuffles.
+constexpr int kMjLanes = 8;
+constexpr int kMjShifts = 32 / kMjLanes;
+constexpr int kMjDepth = 4;
+constexpr int kMaxAdvJobs = 16;
+
+struct AdvJob {
+    const double2* Hc;
+    int64_t ldc;
+    int j0, j1;
+    const double2* shifts;
+    int nshift;
+    double beta, btol;
+    const double2* sinkc;
+    double* rot_c;
+    double2* rot_s;
+    double2* vs;
+    double2* carry;
+    double2* accum;
+    double2* green;
+    double* residual;
+    c3l_hessenberg_status* status;
+};
+
+struct AdvJobs {
+    AdvJob job[kMaxAdvJobs];
+    int count;
+};
+
+__global__ void __launch_bounds__(32) k_hessenberg_advance_jobs(AdvJobs jobs) {
+    const AdvJob& jb = jobs.job[blockIdx.y];
+    const double2* __restrict__ Hc = jb.Hc;
+    const int64_t ldc = jb.ldc;
+    const int j0 = jb.j0, j1 = jb.j1, nshift = jb.nshift;
+    const double2* __restrict__ sinkc = jb.sinkc;
+    const double* __restrict__ rot_c_r = jb.rot_c;
+    const double2* __restrict__ rot_s_r = jb.rot_s;
+    const double2* __restrict__ vs_r = jb.vs;
+    const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
-    const int t = lane / kAdvSeg;  // column of the chunk
-    const int q = lane % kAdvSeg;  // segment of the finalized rows
-    const int sraw = blockIdx.x * kAdvShiftsPerBlock + (int)(threadIdx.x >> 5);
+    const int t = lane & (kMjLanes - 1);
+    const int sraw = blockIdx.x * kMjShifts + (lane / kMjLanes);
+    if (blockIdx.x * kMjShifts >= nshift) return;  // whole block past this channel's shifts (uniform)
     const bool live = sraw < nshift;
     const int sh = live ? sraw : nshift - 1;
-    const bool writer = live && q == 0;
-    const double2 z = shifts[sh];
+    const double2 z = jb.shifts[sh];
     const double2 zero2 = make_double2(0.0, 0.0);
-    double2 g = j0 == 0 ? make_double2(beta, 0.0) : carry[sh];
-    double2 acc = j0 == 0 ? zero2 : accum[sh];
+    double2 g = j0 == 0 ? make_double2(jb.beta, 0.0) : jb.carry[sh];
+    double2 acc = j0 == 0 ? zero2 : jb.accum[sh];
     bool stop = false;
-    for (int cs = j0; cs < j1 && !stop; cs += kAdvLanes) {
+    for (int cs = j0; cs < j1 && !stop; cs += kMjLanes) {
         const int c = min(cs + t, j1 - 1);  // lanes past j1 shadow the last column (never stored)
         const double2* col = Hc + (int64_t)c * ldc;
-        // ---- phase A: compose this lane's segment of rows [0, cs - 1) (never the diagonal: c >= cs)
-        const int offdiag = cs > 0 ? cs - 1 : 0;
-        const int seglen = (offdiag + kAdvSeg - 1) / kAdvSeg;
-        const int lo = min(offdiag, q * seglen);
-        const int hi = min(offdiag, lo + seglen);
-        double2 A = make_double2(1.0, 0.0), B = zero2, D = zero2, E = zero2;
-        auto step = [&](double ci, double2 si, double2 h, double2 v) {
-            // x_i = A x_in + B;  r_i = c x_i - s h;  x_{i+1} = -conj(s) x_i - c h
-            const double2 av = cmul(A, v);
-            D = make_double2(fma(ci, av.x, D.x), fma(ci, av.y, D.y));
-            const double2 sh2 = cmul(si, h);
-            const double2 rb = make_double2(fma(ci, B.x, -sh2.x), fma(ci, B.y, -sh2.y));
-            E = make_double2(fma(rb.x, v.x, fma(-rb.y, v.y, E.x)), fma(rb.x, v.y, fma(rb.y, v.x, E.y)));
-            const double2 sa = cconjmul(si, A);
-            A = make_double2(-sa.x, -sa.y);
-            const double2 sb = cconjmul(si, B);
-            B = make_double2(fma(-ci, h.x, -sb.x), fma(-ci, h.y, -sb.y));
+        double2 x = shifted_entry(col, 0, c, z);
+        double2 dot = zero2;
+        // rows i < cs - 1 are off the diagonal (c >= cs): entry a = -h
+        auto rotate_h = [&](double ci, double2 si, double2 h, double2 v) {
+            const double2 shh = cmul(si, h);
+            const double2 r = make_double2(fma(ci, x.x, -shh.x), fma(ci, x.y, -shh.y));
+            const double2 sx = cconjmul(si, x);
+            x = make_double2(fma(-ci, h.x, -sx.x), fma(-ci, h.y, -sx.y));
+            dot = make_double2(fma(r.x, v.x, fma(-r.y, v.y, dot.x)), fma(r.x, v.y, fma(r.y, v.x, dot.y)));
         };
-        double bc[2][kAdvDepth];
-        double2 bs[2][kAdvDepth], bv[2][kAdvDepth], bh[2][kAdvDepth];
+        double bc[2][kMjDepth];
+        double2 bs[2][kMjDepth], bv[2][kMjDepth], bh[2][kMjDepth];
         auto fetch = [&](int buf, int i0) {
 #pragma unroll
-            for (int u = 0; u < kAdvDepth; ++u) {
+            for (int u = 0; u < kMjDepth; ++u) {
                 const int64_t at = (int64_t)(i0 + u) * nshift + sh;
-                bc[buf][u] = rot_c[at];
-                bs[buf][u] = rot_s[at];
-                bv[buf][u] = sinkc ? vs[at] : zero2;
+                bc[buf][u] = rot_c_r[at];
+                bs[buf][u] = rot_s_r[at];
+                bv[buf][u] = sinkc ? vs_r[at] : zero2;
                 bh[buf][u] = col[i0 + u + 1];
             }
         };
-        const int groups = (hi - lo) / kAdvDepth;
-        if (groups > 0) fetch(0, lo);
+        const int offdiag = cs > 0 ? cs - 1 : 0;
+        const int groups = offdiag / kMjDepth;
+        if (groups > 0) fetch(0, 0);
         for (int gi = 0; gi < groups; gi += 2) {
-            if (gi + 1 < groups) fetch(1, lo + (gi + 1) * kAdvDepth);
+            if (gi + 1 < groups) fetch(1, (gi + 1) * kMjDepth);
 #pragma unroll
-            for (int u = 0; u < kAdvDepth; ++u) step(bc[0][u], bs[0][u], bh[0][u], bv[0][u]);
+            for (int u = 0; u < kMjDepth; ++u) rotate_h(bc[0][u], bs[0][u], bh[0][u], bv[0][u]);
             if (gi + 1 >= groups) break;
-            if (gi + 2 < groups) fetch(0, lo + (gi + 2) * kAdvDepth);
+            if (gi + 2 < groups) fetch(0, (gi + 2) * kMjDepth);
 #pragma unroll
-            for (int u = 0; u < kAdvDepth; ++u) step(bc[1][u], bs[1][u], bh[1][u], bv[1][u]);
+            for (int u = 0; u < kMjDepth; ++u) rotate_h(bc[1][u], bs[1][u], bh[1][u], bv[1][u]);
         }
-        for (int i = lo + groups * kAdvDepth; i < hi; ++i) {
+        for (int i = groups * kMjDepth; i < offdiag; ++i) {
             const int64_t at = (int64_t)i * nshift + sh;
-            step(rot_c[at], rot_s[at], col[i + 1], sinkc ? vs[at] : zero2);
-        }
-        // chain the segments of this column in order (every lane of the column alike)
-        double2 x = shifted_entry(col, 0, c, z);
-        double2 dot = zero2;
-        const int base = t * kAdvSeg;
-#pragma unroll
-        for (int p = 0; p < kAdvSeg; ++p) {
-            const double2 Ap = shfl2(A, base + p), Bp = shfl2(B, base + p);
-            const double2 Dp = shfl2(D, base + p), Ep = shfl2(E, base + p);
-            dot = cadd2(dot, cadd2(cmul(Dp, x), Ep));
-            x = cadd2(cmul(Ap, x), Bp);
+            rotate_h(rot_c_r[at], rot_s_r[at], col[i + 1], sinkc ? vs_r[at] : zero2);
         }
         if (cs > 0) {  // last finalized rotation: row cs may be this column's diagonal
             const int64_t at = (int64_t)(cs - 1) * nshift + sh;
-            const double ci = rot_c[at];
-            const double2 si = rot_s[at];
             const double2 a = shifted_entry(col, cs, c, z);
-            const double2 sa = cmul(si, a);
-            const double2 r = make_double2(fma(ci, x.x, sa.x), fma(ci, x.y, sa.y));
-            const double2 sx = cconjmul(si, x);
-            x = make_double2(fma(ci, a.x, -sx.x), fma(ci, a.y, -sx.y));
-            if (sinkc) {
-                const double2 v = vs[at];
-                dot = make_double2(fma(r.x, v.x, fma(-r.y, v.y, dot.x)), fma(r.x, v.y, fma(r.y, v.x, dot.y)));
-            }
+            rotate_h(rot_c_r[at], rot_s_r[at], make_double2(-a.x, -a.y), sinkc ? vs_r[at] : zero2);
         }
-        // ---- phase B: columns of this chunk, one rotation per step
-        for (int p = 0; p < kAdvLanes; ++p) {
+        // in-chunk rotations
+        for (int p = 0; p < kMjLanes; ++p) {
             const int cq = cs + p;
             if (cq >= j1) break;
             const double2 hsub = Hc[(int64_t)cq * ldc + cq + 1];
-            const bool brk = !(fabs(hsub.x) > btol);
+            const bool brk = !(fabs(hsub.x) > jb.btol);
             double fc = 0.0;
             double2 fs = zero2, fv = zero2;
             if (t == p) {
@@ -574,30 +595,30 @@ __global__ void __launch_bounds__(kAdvThreads) k_hessenberg_advance(
                 const double2 num = make_double2(u.x - dot.x, u.y - dot.y);
                 if (cq == j1 - 1 || brk) {
                     const double2 y = cdiv(g, x);
-                    const double res = hypot(hsub.x, hsub.y) * hypot(y.x, y.y) / beta;
+                    const double res = hypot(hsub.x, hsub.y) * hypot(y.x, y.y) / jb.beta;
                     double2 gr = acc;
                     if (sinkc) gr = cadd2(acc, cmul(cdiv(num, x), g));
-                    if (writer) {
-                        residual[sh] = res;
-                        if (green) green[sh] = gr;
+                    if (live) {
+                        jb.residual[sh] = res;
+                        if (jb.green) jb.green[sh] = gr;
                         if (isfinite(res) && isfinite(gr.x) && isfinite(gr.y)) {
-                            atomicMax(&status->worst, (unsigned long long)__double_as_longlong(res));
+                            atomicMax(&jb.status->worst, (unsigned long long)__double_as_longlong(res));
                         } else {
-                            atomicExch(&status->bad, 1);
+                            atomicExch(&jb.status->bad, 1);
                         }
-                        if (brk) status->first_break = cq + 1;
+                        if (brk) jb.status->first_break = cq + 1;
                     }
                 }
                 if (!brk) {
-                    givens_fast(x, make_double2(-hsub.x, -hsub.y), num, sinkc != nullptr, fc, fs, fv);
+                    givens_one_rsqrt(x, make_double2(-hsub.x, -hsub.y), num, sinkc != nullptr, fc, fs, fv);
                     acc = cadd2(acc, cmul(fv, make_double2(fc * g.x, fc * g.y)));
                     g = cconjmul(fs, g);
                     g = make_double2(-g.x, -g.y);
-                    if (writer) {
+                    if (live) {
                         const int64_t at = (int64_t)cq * nshift + sh;
-                        rot_c[at] = fc;
-                        rot_s[at] = fs;
-                        vs[at] = fv;
+                        jb.rot_c[at] = fc;
+                        jb.rot_s[at] = fs;
+                        jb.vs[at] = fv;
                     }
                 }
             }
@@ -605,8 +626,8 @@ __global__ void __launch_bounds__(kAdvThreads) k_hessenberg_advance(
                 stop = true;
                 break;
             }
-            const int src = p * kAdvSeg;
-            fc = __shfl_sync(0xffffffffu, fc, src);
+            const int src = (lane & ~(kMjLanes - 1)) + p;
+            fc = __shfl_sync(full, fc, src);
             fs = shfl2(fs, src);
             fv = shfl2(fv, src);
             g = shfl2(g, src);
@@ -622,9 +643,9 @@ __global__ void __launch_bounds__(kAdvThreads) k_hessenberg_advance(
         }
         __syncwarp();
     }
-    if (lane == 0 && live) {
-        carry[sh] = g;
-        accum[sh] = acc;
+    if (t == 0 && live) {
+        jb.carry[sh] = g;
+        jb.accum[sh] = acc;
     }
 }
 
@@ -1314,6 +1335,50 @@ c3l_status gm_scale(double* V, int64_t ld, const int* cur, const double* c2, con
     return launch_status();
 }
 
+c3l_status hessenberg_advance_many(c3l_hessenberg_state* const* states, const c3l_complex* const* Hc,
+                                   const int64_t* ldc, const int32_t* m, int count, cudaStream_t s) {
+    if (count <= 0 || count > kMaxAdvJobs) return C3L_ERR_ARGUMENT;
+    AdvJobs jobs{};
+    int max_shifts = 0;
+    for (int i = 0; i < count; ++i) {
+        c3l_hessenberg_state* st = states[i];
+        if (!st || !Hc[i] || !st->shifts || !st->rot_c || !st->rot_s || !st->vsink || !st->carry || !st->accum ||
+            !st->residual || !st->status || st->nshift <= 0 || st->m_max <= 0 || !(st->beta > 0.0))
+            return C3L_ERR_ARGUMENT;
+        if (m[i] < st->done || m[i] > st->m_max || ldc[i] < (int64_t)st->m_max + 1 || st->done < 0)
+            return C3L_ERR_ARGUMENT;
+        if (cudaMemsetAsync(st->status, 0, sizeof(c3l_hessenberg_status), s) != cudaSuccess) return C3L_ERR_LAUNCH;
+        AdvJob& j = jobs.job[jobs.count];
+        if (m[i] == st->done) continue;  // nothing new: outputs stay those of the last call
+        j.Hc = reinterpret_cast<const double2*>(Hc[i]);
+        j.ldc = ldc[i];
+        j.j0 = st->done;
+        j.j1 = m[i];
+        j.shifts = reinterpret_cast<const double2*>(st->shifts);
+        j.nshift = st->nshift;
+        j.beta = st->beta;
+        j.btol = st->breakdown_tol;
+        j.sinkc = reinterpret_cast<const double2*>(st->sinkproj_conj);
+        j.rot_c = st->rot_c;
+        j.rot_s = reinterpret_cast<double2*>(st->rot_s);
+        j.vs = reinterpret_cast<double2*>(st->vsink);
+        j.carry = reinterpret_cast<double2*>(st->carry);
+        j.accum = reinterpret_cast<double2*>(st->accum);
+        j.green = reinterpret_cast<double2*>(st->green);
+        j.residual = st->residual;
+        j.status = st->status;
+        jobs.count += 1;
+        max_shifts = std::max(max_shifts, st->nshift);
+    }
+    if (jobs.count > 0) {
+        const dim3 grid((unsigned)((max_shifts + kMjShifts - 1) / kMjShifts), (unsigned)jobs.count, 1);
+        k_hessenberg_advance_jobs<<<grid, 32, 0, s>>>(jobs);
+        if (cudaGetLastError() != cudaSuccess) return C3L_ERR_LAUNCH;
+    }
+    for (int i = 0; i < count; ++i) states[i]->done = m[i];
+    return C3L_OK;
+}
+
 }  // namespace c3l
 
 extern "C" {
@@ -1481,23 +1546,11 @@ c3l_status c3l_hessenberg_coordinates_noalloc(const c3l_complex* H, int64_t ldh,
 
 c3l_status c3l_hessenberg_advance(c3l_hessenberg_state* st, const c3l_complex* Hc, int64_t ldc, int32_t m,
                                   void* stream) {
-    if (!st || !Hc || !st->shifts || !st->rot_c || !st->rot_s || !st->vsink || !st->carry || !st->accum ||
-        !st->residual || !st->status || st->nshift <= 0 || st->m_max <= 0 || !(st->beta > 0.0))
-        return C3L_ERR_ARGUMENT;
-    if (m < st->done || m > st->m_max || ldc < (int64_t)st->m_max + 1 || st->done < 0) return C3L_ERR_ARGUMENT;
-    cudaStream_t s = as_stream(stream);
-    if (cudaMemsetAsync(st->status, 0, sizeof(c3l_hessenberg_status), s) != cudaSuccess) return C3L_ERR_LAUNCH;
-    if (m == st->done) return C3L_OK;
-    const unsigned blocks = (unsigned)((st->nshift + kAdvShiftsPerBlock - 1) / kAdvShiftsPerBlock);
-    k_hessenberg_advance<<<blocks, kAdvThreads, 0, s>>>(
-        reinterpret_cast<const double2*>(Hc), ldc, st->done, m, reinterpret_cast<const double2*>(st->shifts),
-        st->nshift, st->beta, st->breakdown_tol, reinterpret_cast<const double2*>(st->sinkproj_conj), st->rot_c,
-        reinterpret_cast<double2*>(st->rot_s), reinterpret_cast<double2*>(st->vsink),
-        reinterpret_cast<double2*>(st->carry), reinterpret_cast<double2*>(st->accum),
-        reinterpret_cast<double2*>(st->green), st->residual, st->status);
-    if (cudaGetLastError() != cudaSuccess) return C3L_ERR_LAUNCH;
-    st->done = m;
-    return C3L_OK;
+    c3l_hessenberg_state* states[1] = {st};
+    const c3l_complex* hc[1] = {Hc};
+    const int64_t lds[1] = {ldc};
+    const int32_t ms[1] = {m};
+    return c3l::hessenberg_advance_many(states, hc, lds, ms, 1, as_stream(stream));
 }
 
 c3l_status c3l_arnoldi_column(const c3l_complex* coeff, int32_t k, c3l_complex* w, int64_t n, c3l_complex* Hc, int64_t ldc,

@@ -604,30 +604,65 @@ c3l_status c3l_arnoldi(c3l_arnoldi_channel* ch, int32_t nch, int64_t N, const c3
     }
     // advance the channel's shifted solves to dimension `upto` and read the
     // status word: worst residual, first breakdown column, non-finite flag
-    auto check = [&](c3l_arnoldi_channel& q, int c, int upto, double& worst, int& first_break) -> c3l_status {
-        void* stream = streams[c];
-        cudaStream_t s = as_stream(stream);
-        const int done = q.hess.done;
+    // Checks: the sink projections of the new rows on each channel's stream,
+    // then one launch advancing the shifted solves of every checked channel
+    // (on the first one's stream, after the others' work), then each channel
+    // reads back its status word: worst residual, first breakdown column,
+    // non-finite flag.
+    OwnedEvents ready;
+    if ((st = ready.create(nch + 1))) return st;
+    auto check_all = [&](const std::vector<int>& which, int upto, std::vector<double>& worst,
+                         std::vector<int>& first_break) -> c3l_status {
         c3l_status r;
-        if (q.sink_conj && upto > done) {
-            c3l_complex* out = const_cast<c3l_complex*>(q.hess.sinkproj_conj) + done;
-            if ((r = c3l_multi_dot_c(q.V + (int64_t)done * N, N, upto - done, q.sink_conj, N, q.partial, out, stream)))
-                return r;
-            q.launches += N > 8192 ? 2 : 1;
+        const int lead = which.front();
+        cudaStream_t ls = as_stream(streams[lead]);
+        std::vector<c3l_hessenberg_state*> states;
+        std::vector<const c3l_complex*> hcs;
+        std::vector<int64_t> lds;
+        std::vector<int32_t> ms;
+        for (int c : which) {
+            c3l_arnoldi_channel& q = ch[c];
+            const int done = q.hess.done;
+            if (q.sink_conj && upto > done) {
+                c3l_complex* out = const_cast<c3l_complex*>(q.hess.sinkproj_conj) + done;
+                if ((r = c3l_multi_dot_c(q.V + (int64_t)done * N, N, upto - done, q.sink_conj, N, q.partial, out,
+                                         streams[c])))
+                    return r;
+                q.launches += N > 8192 ? 2 : 1;
+            }
+            if (c != lead) {
+                if (cudaEventRecord(ready.ev[c], as_stream(streams[c])) != cudaSuccess ||
+                    cudaStreamWaitEvent(ls, ready.ev[c], 0) != cudaSuccess)
+                    return C3L_ERR_LAUNCH;
+            }
+            states.push_back(&q.hess);
+            hcs.push_back(q.Hcol);
+            lds.push_back(ldc);
+            ms.push_back(upto);
         }
-        if ((r = c3l_hessenberg_advance(&q.hess, q.Hcol, ldc, upto, stream))) return r;
-        q.launches += 1;
-        if ((r = d2h(q.status_host, q.hess.status, sizeof(c3l_hessenberg_status), s))) return r;
-        const c3l_hessenberg_status hs = *q.status_host;
-        if (hs.bad) return C3L_ERR_ARGUMENT;  // non-finite Arnoldi step
-        unsigned long long bits = hs.worst;
-        std::memcpy(&worst, &bits, sizeof(double));
-        first_break = hs.first_break - 1;
-        if (q.check_dims && q.nchecks < q.check_capacity) {
-            q.check_dims[q.nchecks] = first_break >= 0 ? first_break + 1 : upto;
-            q.check_res[q.nchecks] = worst;
+        if ((r = c3l::hessenberg_advance_many(states.data(), hcs.data(), lds.data(), ms.data(), (int)which.size(), ls)))
+            return r;
+        ch[lead].launches += 1;
+        if (cudaEventRecord(ready.ev[nch], ls) != cudaSuccess) return C3L_ERR_LAUNCH;
+        worst.assign(which.size(), 0.0);
+        first_break.assign(which.size(), -1);
+        for (size_t i = 0; i < which.size(); ++i) {
+            const int c = which[i];
+            c3l_arnoldi_channel& q = ch[c];
+            cudaStream_t cs = as_stream(streams[c]);
+            if (c != lead && cudaStreamWaitEvent(cs, ready.ev[nch], 0) != cudaSuccess) return C3L_ERR_LAUNCH;
+            if ((r = d2h(q.status_host, q.hess.status, sizeof(c3l_hessenberg_status), cs))) return r;
+            const c3l_hessenberg_status hs = *q.status_host;
+            if (hs.bad) return C3L_ERR_ARGUMENT;  // non-finite Arnoldi step
+            unsigned long long bits = hs.worst;
+            std::memcpy(&worst[i], &bits, sizeof(double));
+            first_break[i] = hs.first_break - 1;
+            if (q.check_dims && q.nchecks < q.check_capacity) {
+                q.check_dims[q.nchecks] = first_break[i] >= 0 ? first_break[i] + 1 : upto;
+                q.check_res[q.nchecks] = worst[i];
+            }
+            q.nchecks += 1;
         }
-        q.nchecks += 1;
         return C3L_OK;
     };
     auto settle = [&](c3l_arnoldi_channel& q, int first_break, double worst) {
@@ -665,14 +700,23 @@ c3l_status c3l_arnoldi(c3l_arnoldi_channel* ch, int32_t nch, int64_t N, const c3
             q.m = target;
         }
         j = target;
-        for (int c = 0; c < nch; ++c) {
-            if (!active[c]) continue;
-            c3l_arnoldi_channel& q = ch[c];
-            double worst;
-            int first_break;
-            if ((st = check(q, c, j, worst, first_break))) return st;
-            if (first_break >= 0 || worst <= tol || j == m_max) {
-                settle(q, first_break, worst);
+        std::vector<int> which;
+        for (int c = 0; c < nch; ++c)
+            if (active[c]) which.push_back(c);
+        std::vector<double> worst;
+        std::vector<int> first_break;
+        for (size_t b0 = 0; b0 < which.size(); b0 += 16) {  // at most 16 channels per launch
+            std::vector<int> part(which.begin() + b0, which.begin() + std::min(which.size(), b0 + 16));
+            std::vector<double> w;
+            std::vector<int> fb;
+            if ((st = check_all(part, j, w, fb))) return st;
+            worst.insert(worst.end(), w.begin(), w.end());
+            first_break.insert(first_break.end(), fb.begin(), fb.end());
+        }
+        for (size_t i = 0; i < which.size(); ++i) {
+            const int c = which[i];
+            if (first_break[i] >= 0 || worst[i] <= tol || j == m_max) {
+                settle(ch[c], first_break[i], worst[i]);
                 active[c] = 0;
                 remaining -= 1;
             }
