@@ -17,6 +17,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <memory>
 #include <vector>
 
 #include "c3l_gb300.h"
@@ -123,6 +124,31 @@ struct OwnedEvents {
     }
 };
 
+// Inner-iteration graphs of c3l_gmres kept between calls: valid while the
+// operator struct, the flags and every buffer pointer are the same.
+struct GmresGraphs {
+    c3l_static_action op{};
+    const double* pc_m4_elem = nullptr;
+    int32_t use_f32 = 0;
+    int64_t n = 0, nrep = 0;
+    int restart = 0;
+    const void* ptrs[10] = {};
+    StepGraph inner[2];
+    int64_t jvp_nodes = 0;
+
+    static void key_ptrs(const c3l_gmres_args* a, const void** out) {
+        const void* p[10] = {a->V, a->tmp, a->coeff, a->partial, a->work, a->counters, a->slots, a->pc_m4, a->pc_col,
+                             a->pc_pair};
+        for (int i = 0; i < 10; ++i) out[i] = p[i];
+    }
+    bool matches(const c3l_gmres_args* a, int rs) const {
+        const void* p[10];
+        key_ptrs(a, p);
+        return std::memcmp(&op, a->jvp, sizeof(op)) == 0 && pc_m4_elem == a->pc_m4_elem && use_f32 == a->use_f32 &&
+               n == a->dim && nrep == a->nrep && restart == rs && std::memcmp(ptrs, p, sizeof(ptrs)) == 0;
+    }
+};
+
 // Complex plane rotation (LAPACK zlartg convention): real c, complex s with
 // c f + s g = r and -conj(s) f + c g = 0.
 void zlartg(c3l_complex f, c3l_complex g, double& c, c3l_complex& sn, c3l_complex& r) {
@@ -160,6 +186,8 @@ inline c3l_complex cdivh(c3l_complex a, c3l_complex b) {
 }  // namespace
 
 extern "C" {
+
+void c3l_gmres_release(void* graph_cache) { delete static_cast<GmresGraphs*>(graph_cache); }
 
 int64_t c3l_gmres_scratch(int32_t restart, int64_t dim) {
     if (restart <= 0 || dim <= 0) return 0;
@@ -201,40 +229,55 @@ c3l_status c3l_gmres(c3l_gmres_args* a, void* stream) {
     if (R > C3L_GMRES_MAX_ROWS) return C3L_ERR_CAPACITY;
     const c3l::GmPlan gp = c3l::gm_plan(n, R, sm_count());
     if ((int64_t)gp.blocks * R > a->partial_capacity) return C3L_ERR_CAPACITY;
-    c3l_static_action fused;
-    const c3l_static_action* op = a->jvp;
-    if (a->pc_m4_elem) {
-        fused = *a->jvp;
-        fused.pc_m4 = a->pc_m4_elem;
-        op = &fused;
+    GmresGraphs* cache = static_cast<GmresGraphs*>(a->graph_cache);
+    std::unique_ptr<GmresGraphs> local;
+    if (!cache || !cache->matches(a, restart)) {
+        delete cache;
+        a->graph_cache = nullptr;
+        local.reset(new GmresGraphs());
+        GmresGraphs& gg = *local;
+        gg.op = *a->jvp;
+        gg.pc_m4_elem = a->pc_m4_elem;
+        gg.use_f32 = a->use_f32;
+        gg.n = n;
+        gg.nrep = a->nrep;
+        gg.restart = restart;
+        GmresGraphs::key_ptrs(a, gg.ptrs);
+        c3l_static_action fused = *a->jvp;
+        if (a->pc_m4_elem) fused.pc_m4 = a->pc_m4_elem;
+        const c3l_static_action* op = &fused;
+        OwnedStream cap;
+        if ((st = cap.create())) return st;
+        for (int par = 0; par < 2; ++par) {
+            const int* cur = a->counters + par;
+            int* next = a->counters + (1 - par);
+            st = gg.inner[par].capture(cap.s, [&](cudaStream_t cs) -> c3l_status {
+                void* csv = reinterpret_cast<void*>(cs);
+                c3l_status q;
+                if (a->pc_m4_elem) {
+                    q = a->use_f32 ? c3l_static_apply_f32(op, xcur, wfix, csv) : c3l_static_apply(op, xcur, wfix, csv);
+                    if (q) return q;
+                } else {
+                    q = a->use_f32 ? c3l_static_apply_f32(op, xcur, a->tmp, csv)
+                                   : c3l_static_apply(op, xcur, a->tmp, csv);
+                    if (q) return q;
+                    if ((q = c3l_precondition(a->nrep, a->pc_m4, a->pc_col, a->pc_pair, a->tmp, wfix, csv))) return q;
+                }
+                if ((q = c3l::gm_dot(V, n, cur, wfix, n, gp, a->partial, done, c1, cs))) return q;
+                if ((q = c3l::gm_axpy_dot(V, n, cur, next, c1, wfix, n, gp, a->partial, done, c2, hval, a->slots,
+                                          stride, cs)))
+                    return q;
+                return c3l::gm_scale(V, n, cur, c2, hval, eps, wfix, n, gp, xcur, cs);
+            });
+            if (st) return st;
+        }
+        // kernels of one operator application: the graph less the three CGS2 kernels
+        gg.jvp_nodes = gg.inner[0].nodes() - 3 - (a->pc_m4_elem ? 0 : 1);
+        cache = local.get();
+        if (a->keep_graphs) a->graph_cache = local.release();
     }
-    OwnedStream cap;
-    if ((st = cap.create())) return st;
-    StepGraph inner[2];
-    for (int par = 0; par < 2; ++par) {
-        const int* cur = a->counters + par;
-        int* next = a->counters + (1 - par);
-        st = inner[par].capture(cap.s, [&](cudaStream_t cs) -> c3l_status {
-            void* csv = reinterpret_cast<void*>(cs);
-            c3l_status q;
-            if (a->pc_m4_elem) {
-                q = a->use_f32 ? c3l_static_apply_f32(op, xcur, wfix, csv) : c3l_static_apply(op, xcur, wfix, csv);
-                if (q) return q;
-            } else {
-                q = a->use_f32 ? c3l_static_apply_f32(op, xcur, a->tmp, csv) : c3l_static_apply(op, xcur, a->tmp, csv);
-                if (q) return q;
-                if ((q = c3l_precondition(a->nrep, a->pc_m4, a->pc_col, a->pc_pair, a->tmp, wfix, csv))) return q;
-            }
-            if ((q = c3l::gm_dot(V, n, cur, wfix, n, gp, a->partial, done, c1, cs))) return q;
-            if ((q = c3l::gm_axpy_dot(V, n, cur, next, c1, wfix, n, gp, a->partial, done, c2, hval, a->slots, stride,
-                                      cs)))
-                return q;
-            return c3l::gm_scale(V, n, cur, c2, hval, eps, wfix, n, gp, xcur, cs);
-        });
-        if (st) return st;
-    }
-    // kernels of one operator application: the graph less the three CGS2 kernels
-    const int64_t jvp_nodes = inner[0].nodes() - 3 - (a->pc_m4_elem ? 0 : 1);
+    StepGraph* inner = cache->inner;
+    const int64_t jvp_nodes = cache->jvp_nodes;
     OwnedEvents ev;
     if ((st = ev.create(2))) return st;
     auto matvec = [&](const double* in, double* out) -> c3l_status {

@@ -175,6 +175,13 @@ class DeviceGMRES:
         self.counters = torch.zeros(4, dtype=torch.int32, device=dev)
         self.slots = torch.zeros(r * (r + 3) + 1, dtype=torch.float64).pin_memory()  # written by the GPU
         self.history = np.zeros(4096, dtype=np.float64)
+        self._graphs: dict = {}  # precision -> kept inner-iteration graphs
+        self._lib = lib
+
+    def __del__(self):
+        for handle in getattr(self, "_graphs", {}).values():
+            if handle:
+                self._lib.c3l_gmres_release(handle)
 
     def solve(self, b: torch.Tensor, x: torch.Tensor, *, rtol: float, atol: float, maxiter: int,
               single: bool = False):
@@ -195,7 +202,11 @@ class DeviceGMRES:
         a.work, a.counters, a.slots = self.work.data_ptr(), self.counters.data_ptr(), self.slots.data_ptr()
         a.pc_m4_elem = ops.pc_m4_elem.data_ptr()
         a.partial_capacity = self.partial.numel()
-        rt.check(rt.lib().c3l_gmres(C.byref(a), rt.stream_ptr(ops.device)), "gmres")
+        a.keep_graphs = 1
+        a.graph_cache = self._graphs.get(single)
+        st = rt.lib().c3l_gmres(C.byref(a), rt.stream_ptr(ops.device))
+        self._graphs[single] = a.graph_cache  # the call replaces a stale cache itself
+        rt.check(st, "gmres")
         hist = list(self.history[:min(a.history_len, self.history.size)])
         rt.LaunchCounter.add(int(a.launches))
         return int(a.info), hist, int(a.matvecs)

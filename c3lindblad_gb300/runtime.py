@@ -64,7 +64,8 @@ class GmresArgs(C.Structure):
                 ("history_capacity", C.c_int32), ("history_len", C.c_int32), ("info", C.c_int32),
                 ("matvecs", C.c_int32), ("use_f32", C.c_int32), ("work", C.c_void_p), ("counters", C.c_void_p),
                 ("slots", C.c_void_p), ("launches", C.c_int64), ("pc_m4_elem", C.c_void_p),
-                ("partial_capacity", C.c_int64)]
+                ("partial_capacity", C.c_int64), ("keep_graphs", C.c_int32), ("pad2", C.c_int32),
+                ("graph_cache", C.c_void_p)]
 
 
 class GmresShiftedArgs(C.Structure):
@@ -103,7 +104,7 @@ EXPORTS = (
     "c3l_wedge_eom_out", "c3l_wedge_source_out", "c3l_action_prepare", "c3l_static_apply", "c3l_eom_sigma",
     "c3l_multi_dot_scratch", "c3l_multi_dot_c", "c3l_multi_dot_r", "c3l_multi_axpy_c", "c3l_multi_axpy_r",
     "c3l_scale_c", "c3l_scale_r", "c3l_precondition", "c3l_hessenberg_shifted", "c3l_hessenberg_coordinates",
-    "c3l_hessenberg_coordinates_noalloc", "c3l_gmres", "c3l_gmres_scratch", "c3l_gmres_shifted", "c3l_shifted_combine", "c3l_arnoldi", "c3l_hessenberg_advance",
+    "c3l_hessenberg_coordinates_noalloc", "c3l_gmres", "c3l_gmres_scratch", "c3l_gmres_release", "c3l_gmres_shifted", "c3l_shifted_combine", "c3l_arnoldi", "c3l_hessenberg_advance",
     "c3l_arnoldi_column", "c3l_static_apply_f32", "c3l_eom_sigma_f32", "c3l_action_prepare_f32", "c3l_downcast",
     "c3l_wedge_static_out_f32", "c3l_mlp_forward", "c3l_mlp_backward", "c3l_mlp_adam", "c3l_warm_features", "c3l_warm_apply", "c3l_version",
 )
@@ -157,6 +158,8 @@ def _declare(lib) -> None:
     lib.c3l_multi_dot_scratch.restype = I64
     lib.c3l_gmres_scratch.argtypes = [I32, I64]
     lib.c3l_gmres_scratch.restype = I64
+    lib.c3l_gmres_release.argtypes = [P]
+    lib.c3l_gmres_release.restype = None
     lib.c3l_version.argtypes = []
     lib.c3l_version.restype = C.c_char_p
 

@@ -369,7 +369,17 @@ typedef struct {
     int64_t launches;
     const double* pc_m4_elem;
     int64_t partial_capacity;
+    /* in/out: with keep_graphs set, the captured inner-iteration graphs are
+     * kept in graph_cache and reused by later calls whose operator struct,
+     * flags and buffers are unchanged (NULL on the first call); release them
+     * with c3l_gmres_release.  keep_graphs = 0: captured per call. */
+    int32_t keep_graphs;
+    int32_t pad2;
+    void* graph_cache;
 } c3l_gmres_args;
+
+/* Frees graphs kept by c3l_gmres (NULL is a no-op). */
+void c3l_gmres_release(void* graph_cache);
 
 c3l_status c3l_gmres(c3l_gmres_args* args, void* stream);
 /* Entries of the `partial` buffer c3l_gmres needs for (restart, dim) on the current device. */

@@ -12,7 +12,7 @@ ROOT = Path(__file__).resolve().parents[1]
 
 def declared_symbols():
     text = (ROOT / "include" / "c3l_gb300.h").read_text()
-    return sorted(set(re.findall(r"^\s*(?:c3l_status|int64_t|const char\*)\s+(c3l_\w+)\s*\(", text, re.M)))
+    return sorted(set(re.findall(r"^\s*(?:c3l_status|int64_t|void|const char\*)\s+(c3l_\w+)\s*\(", text, re.M)))
 
 
 def test_header_declares_entry_points():
