@@ -65,17 +65,21 @@ struct GmPlan {
     unsigned scale_grid;
 };
 GmPlan gm_plan(int64_t n, int max_rows, int sms);
-// out[r] = V[r] . w (r < k), out[k] = |w|^2
+// Pass-1 partial projections: partial[block][r] = V[r] . w on the block's
+// segment (r < k), row k = |w|^2.  partial holds 2 x blocks x R doubles (pass 1
+// in the first half, pass 2 in the second); consumers reduce the partials
+// themselves in a fixed order, so no kernel waits for another block.
 c3l_status gm_dot(const double* V, int64_t ld, const int* cur, const double* w, int64_t n, const GmPlan& p,
-                  double* partial, unsigned* done, double* out, cudaStream_t s);
-// w -= V[0 : k]^T c1, then c2 as gm_dot; the last block writes
-// [c1 + c2 (k) | h | h0] to host-mapped slot j, hval = {h0, h} and *next = k
-c3l_status gm_axpy_dot(const double* V, int64_t ld, const int* cur, int* next, const double* c1, double* w, int64_t n,
-                       const GmPlan& p, double* partial, unsigned* done, double* c2, double* hval, double* slots,
-                       int stride, cudaStream_t s);
-// V[k] = xnext = (w - V[0 : k]^T c2) / h unless h <= eps h0
-c3l_status gm_scale(double* V, int64_t ld, const int* cur, const double* c2, const double* hval, double eps,
-                    const double* w, int64_t n, const GmPlan& p, double* xnext, cudaStream_t s);
+                  double* partial, cudaStream_t s);
+// c1 = reduced pass 1 (block 0 stores it), w -= V[0 : k]^T c1, pass-2 partials
+c3l_status gm_axpy_dot(const double* V, int64_t ld, const int* cur, double* c1, double* w, int64_t n, const GmPlan& p,
+                       double* partial, cudaStream_t s);
+// c2 = reduced pass 2, h0 = |w|, h = sqrt(|w'|^2 - |c2|^2); V[k] = xnext =
+// (w - V c2) / h unless h <= eps h0; block 0 writes [c1 + c2 (k) | h | h0] to
+// host-mapped slot j and *next = k
+c3l_status gm_scale(double* V, int64_t ld, const int* cur, int* next, const double* partial, const double* c1,
+                    double eps, const double* w, int64_t n, const GmPlan& p, double* xnext, double* slots, int stride,
+                    cudaStream_t s);
 
 // c3l_hessenberg_advance for several states in one launch (up to 16): the
 // rotation chains of all channels fill the GPU together.

@@ -1052,25 +1052,44 @@ __global__ void __launch_bounds__(X * Y) k_arnoldi_scale(double2* V, int64_t ld,
 // handles rows r8, r8 + 8, ...; its lanes stride the block's segment.
 constexpr int kGmWarps = kThreads / 32;
 
+// The rows of one warp (r = warp + kGmWarps q, q < kGmRowsPerWarp) are
+// streamed together: each column step loads w once and one entry per row, so
+// the loads of all rows are in flight at once.  Supports k + 1 <= 256 rows.
+constexpr int kGmRowsPerWarp = C3L_GMRES_MAX_ROWS / kGmWarps;
+
 __device__ __forceinline__ void gm_partials(const double* __restrict__ V, int64_t ld, int k,
                                             const double* __restrict__ w, int64_t lo, int64_t hi,
                                             double* __restrict__ partial, int R) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int r = warp; r <= k; r += kGmWarps) {
-        const double* v = r < k ? V + (int64_t)r * ld : w;
-        double s0 = 0.0, s1 = 0.0;
-        int64_t c = lo + lane;
-        for (; c + 32 < hi; c += 64) {
-            s0 = fma(v[c], w[c], s0);
-            s1 = fma(v[c + 32], w[c + 32], s1);
+    const int rows = (k + 1 - warp + kGmWarps - 1) / kGmWarps;  // rows of this warp (row k is w itself)
+    for (int q0 = 0; q0 < rows; q0 += 4) {
+        double acc[4] = {0.0, 0.0, 0.0, 0.0};
+        const double* v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int r = warp + kGmWarps * (q0 + u);
+            v[u] = (q0 + u < rows) ? (r < k ? V + (int64_t)r * ld : w) : w;
         }
-        if (c < hi) s0 = fma(v[c], w[c], s0);
-        const double t = warp_sum(s0 + s1);
-        if (lane == 0) partial[(int64_t)blockIdx.x * R + r] = t;
+        for (int64_t c = lo + lane; c < hi; c += 32) {
+            const double wc = w[c];
+            double e[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) e[u] = v[u][c];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) acc[u] = fma(e[u], wc, acc[u]);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const double t = warp_sum(acc[u]);
+            const int r = warp + kGmWarps * (q0 + u);
+            if (lane == 0 && q0 + u < rows) partial[(int64_t)blockIdx.x * R + r] = t;
+        }
     }
 }
 
-// out[r] = sum over blocks of partial[block][r], r <= k (fixed order)
+// out[r] = sum over blocks of partial[block][r], r <= k, reduced by every
+// block that needs it (fixed order: identical in every block, so all blocks
+// hold bitwise the same coefficients).
 __device__ __forceinline__ void gm_reduce(const double* __restrict__ partial, int R, int nb, int k,
                                           double* __restrict__ out) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1082,90 +1101,93 @@ __device__ __forceinline__ void gm_reduce(const double* __restrict__ partial, in
     }
 }
 
+// Pass-1 partial projections of the work vector: partial1[block][r].
 __global__ void __launch_bounds__(kThreads) k_gm_dot(const double* __restrict__ V, int64_t ld, const int* cur,
                                                      const double* __restrict__ w, int64_t n, int64_t seg,
-                                                     double* __restrict__ partial, int R, unsigned* done,
-                                                     double* __restrict__ out) {
+                                                     double* __restrict__ partial1, int R) {
     const int k = *cur + 1;
     const int64_t lo = (int64_t)blockIdx.x * seg;
-    gm_partials(V, ld, k, w, lo, min(n, lo + seg), partial, R);
-    if (last_block(done)) {
-        gm_reduce(partial, R, gridDim.x, k, out);
-        if (threadIdx.x == 0) *done = 0u;
-    }
+    gm_partials(V, ld, k, w, lo, min(n, lo + seg), partial1, R);
 }
 
-// w' = w - V c1 on the block's segment, then the pass-2 partials; the last
-// block reduces c2, forms h0 = |w|, h = sqrt(|w'|^2 - |c2|^2), writes the
-// column [c1 + c2 | h | h0] to host-mapped slot j and advances the counter.
+// c1 = reduced pass-1 projections (block 0 stores them), w' = w - V c1 on
+// the block's segment, then the pass-2 partials partial2[block][r].
 __global__ void __launch_bounds__(kThreads) k_gm_axpy_dot(const double* __restrict__ V, int64_t ld, const int* cur,
-                                                          int* next, const double* __restrict__ c1,
-                                                          double* __restrict__ w, int64_t n, int64_t seg,
-                                                          double* __restrict__ partial, int R, unsigned* done,
-                                                          double* __restrict__ c2, double* __restrict__ hval,
-                                                          double* __restrict__ slots, int stride) {
+                                                          const double* __restrict__ partial1,
+                                                          double* __restrict__ c1, double* __restrict__ w, int64_t n,
+                                                          int64_t seg, double* __restrict__ partial2, int R) {
     __shared__ double cs[C3L_GMRES_MAX_ROWS];
-    __shared__ double red[32];
     const int k = *cur + 1;
-    for (int r = threadIdx.x; r < k; r += blockDim.x) cs[r] = c1[r];
+    gm_reduce(partial1, R, gridDim.x, k, cs);
     __syncthreads();
+    if (blockIdx.x == 0)
+        for (int r = threadIdx.x; r <= k; r += blockDim.x) c1[r] = cs[r];
     const int64_t lo = (int64_t)blockIdx.x * seg;
     const int64_t hi = min(n, lo + seg);
     for (int64_t c = lo + threadIdx.x; c < hi; c += blockDim.x) {
-        double s0 = 0.0, s1 = 0.0;
+        double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
         int r = 0;
-        for (; r + 1 < k; r += 2) {
+        for (; r + 3 < k; r += 4) {
             s0 = fma(cs[r], V[(int64_t)r * ld + c], s0);
             s1 = fma(cs[r + 1], V[(int64_t)(r + 1) * ld + c], s1);
+            s2 = fma(cs[r + 2], V[(int64_t)(r + 2) * ld + c], s2);
+            s3 = fma(cs[r + 3], V[(int64_t)(r + 3) * ld + c], s3);
         }
-        if (r < k) s0 = fma(cs[r], V[(int64_t)r * ld + c], s0);
-        w[c] -= s0 + s1;
+        for (; r < k; ++r) s0 = fma(cs[r], V[(int64_t)r * ld + c], s0);
+        w[c] -= (s0 + s1) + (s2 + s3);
     }
     __syncthreads();
-    gm_partials(V, ld, k, w, lo, hi, partial, R);
-    if (last_block(done)) {
-        gm_reduce(partial, R, gridDim.x, k, c2);
-        __syncthreads();
+    gm_partials(V, ld, k, w, lo, hi, partial2, R);
+}
+
+// c2 = reduced pass-2 projections, h0 = |w| (from c1), h = sqrt(|w'|^2 -
+// |c2|^2); V[k] = xnext = (w' - V c2) / h unless h <= eps h0 (breakdown:
+// unscaled).  Block 0 writes the column [c1 + c2 | h | h0] to host-mapped
+// slot j and the step index of the other parity.
+__global__ void __launch_bounds__(kThreads) k_gm_scale(double* V, int64_t ld, const int* cur, int* next,
+                                                       const double* __restrict__ partial2, int R, int nb,
+                                                       const double* __restrict__ c1, double eps,
+                                                       const double* __restrict__ w, int64_t n,
+                                                       double* __restrict__ xnext, double* __restrict__ slots,
+                                                       int stride) {
+    __shared__ double cs[C3L_GMRES_MAX_ROWS];
+    __shared__ double hh[2];
+    const int k = *cur + 1;
+    gm_reduce(partial2, R, nb, k, cs);
+    __syncthreads();
+    if (threadIdx.x < 32) {
         double sq = 0.0;
-        for (int r = threadIdx.x; r < k; r += blockDim.x) sq = fma(c2[r], c2[r], sq);
-        sq = block_sum(sq, red);
-        const int j = k - 1;
-        double* slot = slots + (int64_t)j * stride;
-        for (int r = threadIdx.x; r < k; r += blockDim.x) slot[r] = c1[r] + c2[r];
+        for (int r = threadIdx.x; r < k; r += 32) sq = fma(cs[r], cs[r], sq);
+        sq = warp_sum(sq);
         if (threadIdx.x == 0) {
-            const double h0 = sqrt(fmax(c1[k], 0.0));
-            const double h = sqrt(fmax(c2[k] - sq, 0.0));
-            hval[0] = h0;
-            hval[1] = h;
+            hh[0] = sqrt(fmax(c1[k], 0.0));
+            hh[1] = sqrt(fmax(cs[k] - sq, 0.0));
+        }
+    }
+    __syncthreads();
+    const double h0 = hh[0], h = hh[1];
+    const double inv = h > eps * h0 ? 1.0 / h : 1.0;
+    if (blockIdx.x == 0) {
+        double* slot = slots + (int64_t)(k - 1) * stride;
+        for (int r = threadIdx.x; r < k; r += blockDim.x) slot[r] = c1[r] + cs[r];
+        if (threadIdx.x == 0) {
             slot[k] = h;
             slot[k + 1] = h0;
             *next = k;
-            *done = 0u;
         }
     }
-}
-
-// V[k] = xnext = (w' - V c2) / h unless h <= eps h0 (breakdown: unscaled)
-__global__ void __launch_bounds__(kThreads) k_gm_scale(double* V, int64_t ld, const int* cur,
-                                                       const double* __restrict__ c2, const double* __restrict__ hval,
-                                                       double eps, const double* __restrict__ w, int64_t n,
-                                                       double* __restrict__ xnext) {
-    __shared__ double cs[C3L_GMRES_MAX_ROWS];
-    const int k = *cur + 1;
-    for (int r = threadIdx.x; r < k; r += blockDim.x) cs[r] = c2[r];
-    __syncthreads();
-    const double h0 = hval[0], h = hval[1];
-    const double inv = h > eps * h0 ? 1.0 / h : 1.0;
     double* Vk = V + (int64_t)k * ld;
     for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
-        double s0 = 0.0, s1 = 0.0;
+        double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
         int r = 0;
-        for (; r + 1 < k; r += 2) {
+        for (; r + 3 < k; r += 4) {
             s0 = fma(cs[r], V[(int64_t)r * ld + c], s0);
             s1 = fma(cs[r + 1], V[(int64_t)(r + 1) * ld + c], s1);
+            s2 = fma(cs[r + 2], V[(int64_t)(r + 2) * ld + c], s2);
+            s3 = fma(cs[r + 3], V[(int64_t)(r + 3) * ld + c], s3);
         }
-        if (r < k) s0 = fma(cs[r], V[(int64_t)r * ld + c], s0);
-        const double x = (w[c] - (s0 + s1)) * inv;
+        for (; r < k; ++r) s0 = fma(cs[r], V[(int64_t)r * ld + c], s0);
+        const double x = (w[c] - ((s0 + s1) + (s2 + s3))) * inv;
         Vk[c] = x;
         xnext[c] = x;
     }
@@ -1311,27 +1333,27 @@ GmPlan gm_plan(int64_t n, int max_rows, int sms) {
 }
 
 c3l_status gm_dot(const double* V, int64_t ld, const int* cur, const double* w, int64_t n, const GmPlan& p,
-                  double* partial, unsigned* done, double* out, cudaStream_t s) {
-    if (!V || !cur || !w || !partial || !done || !out || n <= 0 || p.R > C3L_GMRES_MAX_ROWS) return C3L_ERR_ARGUMENT;
-    k_gm_dot<<<p.blocks, kThreads, 0, s>>>(V, ld, cur, w, n, p.seg, partial, p.R, done, out);
+                  double* partial, cudaStream_t s) {
+    if (!V || !cur || !w || !partial || n <= 0 || p.R > C3L_GMRES_MAX_ROWS) return C3L_ERR_ARGUMENT;
+    k_gm_dot<<<p.blocks, kThreads, 0, s>>>(V, ld, cur, w, n, p.seg, partial, p.R);
     return launch_status();
 }
 
-c3l_status gm_axpy_dot(const double* V, int64_t ld, const int* cur, int* next, const double* c1, double* w, int64_t n,
-                       const GmPlan& p, double* partial, unsigned* done, double* c2, double* hval, double* slots,
-                       int stride, cudaStream_t s) {
-    if (!V || !cur || !next || !c1 || !w || !partial || !done || !c2 || !hval || !slots || n <= 0 ||
-        p.R > C3L_GMRES_MAX_ROWS)
-        return C3L_ERR_ARGUMENT;
-    k_gm_axpy_dot<<<p.blocks, kThreads, 0, s>>>(V, ld, cur, next, c1, w, n, p.seg, partial, p.R, done, c2, hval, slots,
-                                                stride);
+c3l_status gm_axpy_dot(const double* V, int64_t ld, const int* cur, double* c1, double* w, int64_t n, const GmPlan& p,
+                       double* partial, cudaStream_t s) {
+    if (!V || !cur || !c1 || !w || !partial || n <= 0 || p.R > C3L_GMRES_MAX_ROWS) return C3L_ERR_ARGUMENT;
+    const int64_t half = (int64_t)p.blocks * p.R;
+    k_gm_axpy_dot<<<p.blocks, kThreads, 0, s>>>(V, ld, cur, partial, c1, w, n, p.seg, partial + half, p.R);
     return launch_status();
 }
 
-c3l_status gm_scale(double* V, int64_t ld, const int* cur, const double* c2, const double* hval, double eps,
-                    const double* w, int64_t n, const GmPlan& p, double* xnext, cudaStream_t s) {
-    if (!V || !cur || !c2 || !hval || !w || !xnext || n <= 0) return C3L_ERR_ARGUMENT;
-    k_gm_scale<<<p.scale_grid, kThreads, 0, s>>>(V, ld, cur, c2, hval, eps, w, n, xnext);
+c3l_status gm_scale(double* V, int64_t ld, const int* cur, int* next, const double* partial, const double* c1,
+                    double eps, const double* w, int64_t n, const GmPlan& p, double* xnext, double* slots, int stride,
+                    cudaStream_t s) {
+    if (!V || !cur || !next || !partial || !c1 || !w || !xnext || !slots || n <= 0) return C3L_ERR_ARGUMENT;
+    const int64_t half = (int64_t)p.blocks * p.R;
+    k_gm_scale<<<p.scale_grid, kThreads, 0, s>>>(V, ld, cur, next, partial + half, p.R, (int)p.blocks, c1, eps, w, n,
+                                                 xnext, slots, stride);
     return launch_status();
 }
 

@@ -193,7 +193,7 @@ int64_t c3l_gmres_scratch(int32_t restart, int64_t dim) {
     if (restart <= 0 || dim <= 0) return 0;
     const int r = (int)std::min<int64_t>(restart, dim);
     const c3l::GmPlan gp = c3l::gm_plan(dim, r + 2, sm_count());
-    return (int64_t)gp.blocks * (r + 2);
+    return 2 * (int64_t)gp.blocks * (r + 2);
 }
 
 c3l_status c3l_gmres(c3l_gmres_args* a, void* stream) {
@@ -221,14 +221,11 @@ c3l_status c3l_gmres(c3l_gmres_args* a, void* stream) {
     double* xcur = a->work;
     double* wfix = a->work + n;
     const int R = restart + 2;
-    double* c1 = coeff;
-    double* c2 = coeff + R;
-    double* hval = coeff + 2 * R;
-    unsigned* done = reinterpret_cast<unsigned*>(a->counters + 2);
+    double* c1 = coeff;  // reduced pass-1 projections (k + 1)
     const int stride = restart + 3;
     if (R > C3L_GMRES_MAX_ROWS) return C3L_ERR_CAPACITY;
     const c3l::GmPlan gp = c3l::gm_plan(n, R, sm_count());
-    if ((int64_t)gp.blocks * R > a->partial_capacity) return C3L_ERR_CAPACITY;
+    if (2 * (int64_t)gp.blocks * R > a->partial_capacity) return C3L_ERR_CAPACITY;
     GmresGraphs* cache = static_cast<GmresGraphs*>(a->graph_cache);
     std::unique_ptr<GmresGraphs> local;
     if (!cache || !cache->matches(a, restart)) {
@@ -263,11 +260,9 @@ c3l_status c3l_gmres(c3l_gmres_args* a, void* stream) {
                     if (q) return q;
                     if ((q = c3l_precondition(a->nrep, a->pc_m4, a->pc_col, a->pc_pair, a->tmp, wfix, csv))) return q;
                 }
-                if ((q = c3l::gm_dot(V, n, cur, wfix, n, gp, a->partial, done, c1, cs))) return q;
-                if ((q = c3l::gm_axpy_dot(V, n, cur, next, c1, wfix, n, gp, a->partial, done, c2, hval, a->slots,
-                                          stride, cs)))
-                    return q;
-                return c3l::gm_scale(V, n, cur, c2, hval, eps, wfix, n, gp, xcur, cs);
+                if ((q = c3l::gm_dot(V, n, cur, wfix, n, gp, a->partial, cs))) return q;
+                if ((q = c3l::gm_axpy_dot(V, n, cur, c1, wfix, n, gp, a->partial, cs))) return q;
+                return c3l::gm_scale(V, n, cur, next, a->partial, c1, eps, wfix, n, gp, xcur, a->slots, stride, cs);
             });
             if (st) return st;
         }

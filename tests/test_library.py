@@ -73,3 +73,10 @@ def test_krylov_drivers_reject_bad_arguments_before_launch():
     assert lib.c3l_arnoldi(None, 1, 10, None, 1, 5000, 1e-10, 1, 8, 1e-14, None) == 1
     assert lib.c3l_gmres_scratch(0, 10) == 0
     assert lib.c3l_gmres_scratch(40, 20933) >= 42
+
+
+def test_gmres_graph_release_accepts_null():
+    from c3lindblad_gb300 import runtime
+
+    lib = runtime.load_library()
+    lib.c3l_gmres_release(None)  # no-op
