@@ -158,8 +158,7 @@ __global__ void __launch_bounds__(kThreads) k_contract(c3l_contract_level lv, in
 // the cluster's CTAs stride over a level's tiles, then meet at a hardware
 // cluster barrier (release/acquire) before the next level.  Every CTA reaches
 // every barrier.
-constexpr int kLevelCluster = 8;
-constexpr int kClusterLevelMaxTiles = kLevelCluster;  // one round per level
+constexpr int kLevelClusterMax = 16;  // non-portable cluster size where the device allows it
 
 struct LevelPack {
     c3l_contract_level lv[C3L_MAX_LEVELS];
@@ -318,11 +317,40 @@ inline unsigned grid_for(int64_t count) {
     return (unsigned)b;
 }
 
+// Cluster size for k_contract_cluster<C>: 16 CTAs where the device can
+// schedule such a cluster (checked once per process), else the portable 8.
+template <typename C>
+int level_cluster_size() {
+    static int size = 0;
+    if (size) return size;
+    int chosen = 8;
+    const void* fn = (const void*)k_contract_cluster<C>;
+    if (cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess) {
+        cudaLaunchConfig_t cfg{};
+        cfg.gridDim = dim3(kLevelClusterMax, 1, 1);
+        cfg.blockDim = dim3(kThreads, 1, 1);
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = kLevelClusterMax;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        int clusters = 0;
+        if (cudaOccupancyMaxActiveClusters(&clusters, fn, &cfg) == cudaSuccess && clusters >= 1)
+            chosen = kLevelClusterMax;
+    }
+    cudaGetLastError();  // a refused query leaves no error behind
+    size = chosen;
+    return size;
+}
+
 template <typename C>
 c3l_status run_levels(const c3l_action* a, cudaStream_t s) {
-    // levels [tail, nlevels) are all small: one cluster launch runs them
+    // levels [tail, nlevels) each fit one round of the cluster: one cluster launch runs them
+    const int cluster = level_cluster_size<C>();
     int tail = a->nlevels;
-    while (tail > 0 && a->levels[tail - 1].ntiles <= kClusterLevelMaxTiles) --tail;
+    while (tail > 0 && a->levels[tail - 1].ntiles <= cluster) --tail;
     if (a->nlevels - tail < 2) tail = a->nlevels;  // a single small level gains nothing
     for (int l = 0; l < tail; ++l) {
         if (a->levels[l].ntiles <= 0) continue;
@@ -336,13 +364,13 @@ c3l_status run_levels(const c3l_action* a, cudaStream_t s) {
         pack.first = tail;
         pack.count = a->nlevels - tail;
         cudaLaunchConfig_t cfg{};
-        cfg.gridDim = dim3(kLevelCluster, 1, 1);
+        cfg.gridDim = dim3(cluster, 1, 1);
         cfg.blockDim = dim3(kThreads, 1, 1);
         cfg.dynamicSmemBytes = 0;
         cfg.stream = s;
         cudaLaunchAttribute attr[1];
         attr[0].id = cudaLaunchAttributeClusterDimension;
-        attr[0].val.clusterDim.x = kLevelCluster;
+        attr[0].val.clusterDim.x = cluster;
         attr[0].val.clusterDim.y = 1;
         attr[0].val.clusterDim.z = 1;
         cfg.attrs = attr;

@@ -302,7 +302,8 @@ class LaunchCounter:
         return c
 
 
-CLUSTER_LEVEL_MAX_TILES = 8  # levels this small at the end of the list run as one cluster launch
+CLUSTER_LEVEL_MAX_TILES = 16  # levels this small at the end of the list run as one cluster launch
+                              # (16-CTA clusters on GB300; the count is an estimate where only 8 are allowed)
 
 
 def action_launches(a: Action) -> int:
