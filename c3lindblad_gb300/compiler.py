@@ -450,13 +450,7 @@ class Builder:
                 idx = np.flatnonzero(eb == b)
                 if idx.size:
                     ranges.append((b, int(idx[0]), int(idx[-1]) + 1))
-        # the widest tile that still gives every SM several blocks
-        width = WEDGE_WIDTHS[-1]
-        for w in WEDGE_WIDTHS:
-            if sum(-(-(hi - lo) // w) for _, lo, hi in ranges) >= WEDGE_MIN_TILES:
-                width = w
-                break
-        tiles = [(b, min(width, hi - s), s) for b, lo, hi in ranges for s in range(lo, hi, width)]
+        width, tiles = _tiles_for(ranges)
         tarr = np.zeros(len(tiles), TILE_DTYPE)
         for i, (b, c, s) in enumerate(tiles):
             tarr[i] = (b, c, s)
@@ -490,6 +484,37 @@ class Builder:
             levels[cls] = lv
         return Program(self.n, self.ws, self.vectors.reshape(-1), self.source_offsets, levels,
                        self.stage_data, self.atom_offsets, self.rest_offsets)
+
+
+def _tiles_for(ranges):
+    """The widest tile that still gives every SM several blocks, and the tiles."""
+    width = WEDGE_WIDTHS[-1]
+    for w in WEDGE_WIDTHS:
+        if sum(-(-(hi - lo) // w) for _, lo, hi in ranges) >= WEDGE_MIN_TILES:
+            width = w
+            break
+    return width, [(b, min(width, hi - s), s) for b, lo, hi in ranges for s in range(lo, hi, width)]
+
+
+def merge_padded(stages: list, n: int) -> "Stage":
+    """One launch for several padded stages of an action.  Padded stages read
+    atoms only and write disjoint workspace blocks, so their blocks can share
+    a grid; the instance ranges and tile block indices are rebased."""
+    blocks = np.concatenate([st.blocks for st in stages]).copy()
+    inst = np.concatenate([st.instances for st in stages])
+    b0 = i0 = 0
+    for st in stages:
+        nb = st.blocks.size
+        blocks[b0:b0 + nb]["inst_begin"] += i0
+        blocks[b0:b0 + nb]["inst_end"] += i0
+        b0 += nb
+        i0 += st.instances.size
+    ranges = [(b, 0, n ** int(blocks[b]["deg"])) for b in range(blocks.size)]
+    width, tiles = _tiles_for(ranges)
+    tarr = np.zeros(len(tiles), TILE_DTYPE)
+    for i, t in enumerate(tiles):
+        tarr[i] = t
+    return Stage("+".join(st.name for st in stages), "padded", blocks, inst, tarr, width=width)
 
 
 def _group_by_anchor(terms: dict):

@@ -268,6 +268,14 @@ def build_action(up: Uploader, program, vectors_ptr: int, ws: torch.Tensor, leve
         a.levels[i].tiles = up.ptr(lv.tiles)
         a.levels[i].ntiles = len(lv.tiles)
     stages = [program.stages[nm] for nm in padded_names if nm in program.stages]
+    if len(stages) > 1:  # independent padded stages share one launch
+        from .compiler import merge_padded
+
+        key = tuple(st.name for st in stages)
+        cache = program.__dict__.setdefault("_merged_padded", {})
+        if key not in cache:
+            cache[key] = merge_padded(stages, program.n)
+        stages = [cache[key]]
     if len(stages) > 4:
         raise C3LError("too many padded stages")
     a.npadded = len(stages)
