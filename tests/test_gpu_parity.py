@@ -228,6 +228,15 @@ def test_matrix_green_arnoldi_matches_reference(problems):
         rhs[0] = pr.source_norm
         y = np.linalg.solve(zi * np.eye(m) - pr.hessenberg[:m, :m], rhs)
         assert relerr(Y[i], y) < 1e-9
+    # the device basis is orthonormal and satisfies K V_m = V_{m+1} H to FP64
+    # rounding (a single FP64 pass where |w'| >= |w| / sqrt(2), the DGKS test,
+    # let the orthogonality decay to 1e-8 over this basis)
+    for pr in (res.addition_projections[0], res.removal_projections[2]):
+        V = pr.basis
+        m = pr.dimension
+        assert np.max(np.abs(V.conj().T @ V - np.eye(m + 1))) < 1e-12
+        KV = np.stack([op.matvec(V[:, j]) for j in range(m)], axis=1)
+        assert np.linalg.norm(KV - V @ pr.hessenberg) / np.linalg.norm(pr.hessenberg) < 1e-13
     with pytest.raises(ValueError):
         c3.component_retarded_matrix_green_arnoldi(op, sources, ref["omega"], 0.0)
     with pytest.raises(ValueError):
