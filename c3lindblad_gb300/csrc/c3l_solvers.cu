@@ -640,20 +640,20 @@ c3l_status c3l_arnoldi(c3l_arnoldi_channel* ch, int32_t nch, int64_t N, const c3
         q.hess.done = 0;
         if (!q.sink_conj) q.hess.sinkproj_conj = nullptr;
     }
-    // advance the channel's shifted solves to dimension `upto` and read the
-    // status word: worst residual, first breakdown column, non-finite flag
     // Checks: the sink projections of the new rows on each channel's stream,
-    // then one launch advancing the shifted solves of every checked channel
-    // (on the first one's stream, after the others' work), then each channel
-    // reads back its status word: worst residual, first breakdown column,
-    // non-finite flag.
+    // then, on a check stream of the driver's own, one launch advancing the
+    // shifted solves of every checked channel and the read-back of each
+    // status word (worst residual, first breakdown column, non-finite flag).
+    // While a check runs, the channels already take their next steps: a
+    // channel that the check stops keeps the dimension checked, and the steps
+    // taken beyond it are discarded (they write only basis rows and Hessenberg
+    // columns past that dimension).
     OwnedEvents ready;
-    if ((st = ready.create(nch + 1))) return st;
-    auto check_all = [&](const std::vector<int>& which, int upto, std::vector<double>& worst,
-                         std::vector<int>& first_break) -> c3l_status {
+    if ((st = ready.create(nch))) return st;
+    OwnedStream chk;
+    if ((st = chk.create())) return st;
+    auto enqueue_check = [&](const std::vector<int>& which, int upto) -> c3l_status {
         c3l_status r;
-        const int lead = which.front();
-        cudaStream_t ls = as_stream(streams[lead]);
         std::vector<c3l_hessenberg_state*> states;
         std::vector<const c3l_complex*> hcs;
         std::vector<int64_t> lds;
@@ -668,39 +668,22 @@ c3l_status c3l_arnoldi(c3l_arnoldi_channel* ch, int32_t nch, int64_t N, const c3
                     return r;
                 q.launches += N > 8192 ? 2 : 1;
             }
-            if (c != lead) {
-                if (cudaEventRecord(ready.ev[c], as_stream(streams[c])) != cudaSuccess ||
-                    cudaStreamWaitEvent(ls, ready.ev[c], 0) != cudaSuccess)
-                    return C3L_ERR_LAUNCH;
-            }
+            if (cudaEventRecord(ready.ev[c], as_stream(streams[c])) != cudaSuccess ||
+                cudaStreamWaitEvent(chk.s, ready.ev[c], 0) != cudaSuccess)
+                return C3L_ERR_LAUNCH;
             states.push_back(&q.hess);
             hcs.push_back(q.Hcol);
             lds.push_back(ldc);
             ms.push_back(upto);
         }
-        if ((r = c3l::hessenberg_advance_many(states.data(), hcs.data(), lds.data(), ms.data(), (int)which.size(), ls)))
+        if ((r = c3l::hessenberg_advance_many(states.data(), hcs.data(), lds.data(), ms.data(), (int)which.size(),
+                                              chk.s)))
             return r;
-        ch[lead].launches += 1;
-        if (cudaEventRecord(ready.ev[nch], ls) != cudaSuccess) return C3L_ERR_LAUNCH;
-        worst.assign(which.size(), 0.0);
-        first_break.assign(which.size(), -1);
-        for (size_t i = 0; i < which.size(); ++i) {
-            const int c = which[i];
-            c3l_arnoldi_channel& q = ch[c];
-            cudaStream_t cs = as_stream(streams[c]);
-            if (c != lead && cudaStreamWaitEvent(cs, ready.ev[nch], 0) != cudaSuccess) return C3L_ERR_LAUNCH;
-            if ((r = d2h(q.status_host, q.hess.status, sizeof(c3l_hessenberg_status), cs))) return r;
-            const c3l_hessenberg_status hs = *q.status_host;
-            if (hs.bad) return C3L_ERR_ARGUMENT;  // non-finite Arnoldi step
-            unsigned long long bits = hs.worst;
-            std::memcpy(&worst[i], &bits, sizeof(double));
-            first_break[i] = hs.first_break - 1;
-            if (q.check_dims && q.nchecks < q.check_capacity) {
-                q.check_dims[q.nchecks] = first_break[i] >= 0 ? first_break[i] + 1 : upto;
-                q.check_res[q.nchecks] = worst[i];
-            }
-            q.nchecks += 1;
-        }
+        ch[which.front()].launches += 1;
+        for (int c : which)
+            if (cudaMemcpyAsync(ch[c].status_host, ch[c].hess.status, sizeof(c3l_hessenberg_status),
+                                cudaMemcpyDeviceToHost, chk.s) != cudaSuccess)
+                return C3L_ERR_LAUNCH;
         return C3L_OK;
     };
     auto settle = [&](c3l_arnoldi_channel& q, int first_break, double worst) {
@@ -711,53 +694,75 @@ c3l_status c3l_arnoldi(c3l_arnoldi_channel* ch, int32_t nch, int64_t N, const c3
         q.converged = worst <= tol ? 1 : 0;
     };
     auto due = [&](int k) { return k >= min_dim && (k % check_interval == 0 || k == m_max); };
-    int remaining = nch;
-    int j = 0;  // steps taken by every active channel
-    while (j < m_max && remaining > 0) {
-        int target = j + 1;
-        while (!due(target)) ++target;  // terminates: due(m_max) holds
-        const int steps = target - j;
+    auto next_due = [&](int k) {
+        int t = k + 1;
+        while (!due(t)) ++t;  // terminates: due(m_max) holds
+        return t;
+    };
+    // every active channel takes the steps launched .. upto
+    int launched = 0;
+    auto launch_to = [&](int upto) -> c3l_status {
         for (int c = 0; c < nch; ++c) {
             if (!active[c]) continue;
             c3l_arnoldi_channel& q = ch[c];
             cudaStream_t s = as_stream(streams[c]);
-            int left = steps;
-            int at = j;  // steps taken so far: the parity of the next step
+            int left = upto - launched;
+            int at = launched;  // steps taken so far: the parity of the next step
             while (left >= check_interval) {
                 const StepGraph& g = interval[2 * c + (at & 1)];
-                if ((st = g.launch(s))) return st;
+                c3l_status r = g.launch(s);
+                if (r) return r;
                 q.launches += g.nodes();
                 left -= check_interval;
                 at += check_interval;
             }
             for (; left > 0; --left, ++at) {
                 const StepGraph& g = one[2 * c + (at & 1)];
-                if ((st = g.launch(s))) return st;
+                c3l_status r = g.launch(s);
+                if (r) return r;
                 q.launches += g.nodes();
             }
-            q.m = target;
         }
-        j = target;
+        launched = upto;
+        return C3L_OK;
+    };
+    int remaining = nch;
+    if ((st = launch_to(next_due(0)))) return st;
+    while (remaining > 0) {
+        const int target = launched;  // dimension of this check
         std::vector<int> which;
         for (int c = 0; c < nch; ++c)
             if (active[c]) which.push_back(c);
-        std::vector<double> worst;
-        std::vector<int> first_break;
         for (size_t b0 = 0; b0 < which.size(); b0 += 16) {  // at most 16 channels per launch
             std::vector<int> part(which.begin() + b0, which.begin() + std::min(which.size(), b0 + 16));
-            std::vector<double> w;
-            std::vector<int> fb;
-            if ((st = check_all(part, j, w, fb))) return st;
-            worst.insert(worst.end(), w.begin(), w.end());
-            first_break.insert(first_break.end(), fb.begin(), fb.end());
+            if ((st = enqueue_check(part, target))) return st;
         }
-        for (size_t i = 0; i < which.size(); ++i) {
-            const int c = which[i];
-            if (first_break[i] >= 0 || worst[i] <= tol || j == m_max) {
-                settle(ch[c], first_break[i], worst[i]);
+        if (target < m_max && (st = launch_to(next_due(target)))) return st;
+        if (cudaStreamSynchronize(chk.s) != cudaSuccess) return C3L_ERR_LAUNCH;
+        bool bad = false;
+        for (int c : which) {
+            c3l_arnoldi_channel& q = ch[c];
+            const c3l_hessenberg_status hs = *q.status_host;
+            bad = bad || hs.bad != 0;
+            double worst;
+            unsigned long long bits = hs.worst;
+            std::memcpy(&worst, &bits, sizeof(double));
+            const int first_break = hs.first_break - 1;
+            if (q.check_dims && q.nchecks < q.check_capacity) {
+                q.check_dims[q.nchecks] = first_break >= 0 ? first_break + 1 : target;
+                q.check_res[q.nchecks] = worst;
+            }
+            q.nchecks += 1;
+            q.m = target;
+            if (first_break >= 0 || worst <= tol || target == m_max) {
+                settle(q, first_break, worst);
                 active[c] = 0;
                 remaining -= 1;
             }
+        }
+        if (bad) {  // non-finite Arnoldi step: let the steps in flight finish first
+            for (int c = 0; c < nch; ++c) cudaStreamSynchronize(as_stream(streams[c]));
+            return C3L_ERR_ARGUMENT;
         }
     }
     // host copy of H[:m+1, :m] (row-major, leading dimension m_max)
