@@ -261,8 +261,8 @@ def run_gpu(args) -> dict:
         "ms_per_step": t_step * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
         "dtype": "c128", "data": "synthetic",
         "config": {"workload": args.workload, "description": wl["label"],
-                   "precision": "mixed: FP32 inner JVPs in GMRES, FP64 residuals/refinement; FP64 sigma and "
-                                "Arnoldi (first CGS2 pass FP32, second FP64)",
+                   "precision": "mixed: FP32 inner JVPs and FP32 Krylov basis in GMRES (inner tolerance >= 1e-5), FP64 "
+                                "residuals/refinement; FP64 sigma and Arnoldi (first CGS2 pass FP32, second FP64)",
                    "plain_fp64_seconds": t_unbatched,
                    "plain_fp64_form": "FP64 inner JVPs, the reference's per-frequency preconditioned GMRES for "
                                       "every omega and channel (batching off), zero initial amplitudes",

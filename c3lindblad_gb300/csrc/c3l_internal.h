@@ -80,6 +80,21 @@ c3l_status gm_axpy_dot(const double* V, int64_t ld, const int* cur, double* c1, 
 c3l_status gm_scale(double* V, int64_t ld, const int* cur, int* next, const double* partial, const double* c1,
                     double eps, const double* w, int64_t n, const GmPlan& p, double* xnext, double* slots, int stride,
                     cudaStream_t s);
+// The same step over an FP32 basis (inner solves with the FP32 operator): wf
+// (n floats) receives the work vector in FP32 and is updated in place; the
+// partials and c1 are floats (c1: k + 1 entries); the slot column stays FP64.
+c3l_status gm_dot_f32(const float* V, int64_t ld, const int* cur, const double* w, float* wf, int64_t n,
+                      const GmPlan& p, float* partial, cudaStream_t s);
+c3l_status gm_axpy_dot_f32(const float* V, int64_t ld, const int* cur, float* c1, float* wf, int64_t n,
+                           const GmPlan& p, float* partial, cudaStream_t s);
+c3l_status gm_scale_f32(float* V, int64_t ld, const int* cur, int* next, const float* partial, const float* c1,
+                        double eps, const float* wf, int64_t n, const GmPlan& p, double* xnext, double* slots,
+                        int stride, cudaStream_t s);
+// V0 = (float)(a r) and x = V0 (FP64 copy)
+c3l_status gm_start_f32(int64_t n, double a, const double* r, float* V0, double* x, cudaStream_t s);
+// x += V[0 : k]^T y (FP32 rows, FP64 arithmetic)
+c3l_status gm_update_f32(const float* V, int64_t ld, int k, const double* y, double* x, int64_t n, cudaStream_t s);
+
 
 // c3l_hessenberg_advance for several states in one launch (up to 16): the
 // rotation chains of all channels fill the GPU together.

@@ -52,6 +52,11 @@ __device__ __forceinline__ double warp_sum(double v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
     return v;
 }
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
 
 // Block-wide sum of one double; result valid in thread 0.
 __device__ double block_sum(double v, double* smem) {
@@ -1193,6 +1198,163 @@ __global__ void __launch_bounds__(kThreads) k_gm_scale(double* V, int64_t ld, co
     }
 }
 
+// ------------------------------------------ GMRES CGS2 step, FP32 basis
+// The same three kernels for an inner solve whose operator is FP32 (the
+// FP32 JVP): the basis rows, the work vector after the operator and all
+// products and sums are FP32; the Hessenberg column goes to the host in FP64.
+// Partial sums are floats in the same [block][R] layout.
+
+__device__ __forceinline__ void gm_partials_f(const float* __restrict__ V, int64_t ld, int k,
+                                              const float* __restrict__ w, int64_t lo, int64_t hi,
+                                              float* __restrict__ partial, int R) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int rows = (k + 1 - warp + kGmWarps - 1) / kGmWarps;  // rows of this warp (row k is w itself)
+    for (int q0 = 0; q0 < rows; q0 += 4) {
+        float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        const float* v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int r = warp + kGmWarps * (q0 + u);
+            v[u] = (q0 + u < rows) ? (r < k ? V + (int64_t)r * ld : w) : w;
+        }
+        for (int64_t c = lo + lane; c < hi; c += 32) {
+            const float wc = w[c];
+            float e[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) e[u] = v[u][c];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) acc[u] = fmaf(e[u], wc, acc[u]);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const float t = warp_sum(acc[u]);
+            const int r = warp + kGmWarps * (q0 + u);
+            if (lane == 0 && q0 + u < rows) partial[(int64_t)blockIdx.x * R + r] = t;
+        }
+    }
+}
+
+__device__ __forceinline__ void gm_reduce_f(const float* __restrict__ partial, int R, int nb, int k,
+                                            float* __restrict__ out) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int r = warp; r <= k; r += kGmWarps) {
+        float s = 0.0f;
+        for (int b = lane; b < nb; b += 32) s += partial[(int64_t)b * R + r];
+        s = warp_sum(s);
+        if (lane == 0) out[r] = s;
+    }
+}
+
+// wf = (float) w on the block's segment, then the pass-1 partials.
+__global__ void __launch_bounds__(kThreads) k_gm_dot_f(const float* __restrict__ V, int64_t ld, const int* cur,
+                                                       const double* __restrict__ w, float* __restrict__ wf,
+                                                       int64_t n, int64_t seg, float* __restrict__ partial1, int R) {
+    const int k = *cur + 1;
+    const int64_t lo = (int64_t)blockIdx.x * seg;
+    const int64_t hi = min(n, lo + seg);
+    for (int64_t c = lo + threadIdx.x; c < hi; c += blockDim.x) wf[c] = (float)w[c];
+    __syncthreads();
+    gm_partials_f(V, ld, k, wf, lo, hi, partial1, R);
+}
+
+__global__ void __launch_bounds__(kThreads) k_gm_axpy_dot_f(const float* __restrict__ V, int64_t ld, const int* cur,
+                                                            const float* __restrict__ partial1,
+                                                            float* __restrict__ c1, float* __restrict__ wf,
+                                                            int64_t n, int64_t seg, float* __restrict__ partial2,
+                                                            int R) {
+    __shared__ float cs[C3L_GMRES_MAX_ROWS];
+    const int k = *cur + 1;
+    gm_reduce_f(partial1, R, gridDim.x, k, cs);
+    __syncthreads();
+    if (blockIdx.x == 0)
+        for (int r = threadIdx.x; r <= k; r += blockDim.x) c1[r] = cs[r];
+    const int64_t lo = (int64_t)blockIdx.x * seg;
+    const int64_t hi = min(n, lo + seg);
+    for (int64_t c = lo + threadIdx.x; c < hi; c += blockDim.x) {
+        float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f, s3 = 0.0f;
+        int r = 0;
+        for (; r + 3 < k; r += 4) {
+            s0 = fmaf(cs[r], V[(int64_t)r * ld + c], s0);
+            s1 = fmaf(cs[r + 1], V[(int64_t)(r + 1) * ld + c], s1);
+            s2 = fmaf(cs[r + 2], V[(int64_t)(r + 2) * ld + c], s2);
+            s3 = fmaf(cs[r + 3], V[(int64_t)(r + 3) * ld + c], s3);
+        }
+        for (; r < k; ++r) s0 = fmaf(cs[r], V[(int64_t)r * ld + c], s0);
+        wf[c] -= (s0 + s1) + (s2 + s3);
+    }
+    __syncthreads();
+    gm_partials_f(V, ld, k, wf, lo, hi, partial2, R);
+}
+
+__global__ void __launch_bounds__(kThreads) k_gm_scale_f(float* V, int64_t ld, const int* cur, int* next,
+                                                         const float* __restrict__ partial2, int R, int nb,
+                                                         const float* __restrict__ c1, double eps,
+                                                         const float* __restrict__ wf, int64_t n,
+                                                         double* __restrict__ xnext, double* __restrict__ slots,
+                                                         int stride) {
+    __shared__ float cs[C3L_GMRES_MAX_ROWS];
+    __shared__ float hh[2];
+    const int k = *cur + 1;
+    gm_reduce_f(partial2, R, nb, k, cs);
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        float sq = 0.0f;
+        for (int r = threadIdx.x; r < k; r += 32) sq = fmaf(cs[r], cs[r], sq);
+        sq = warp_sum(sq);
+        if (threadIdx.x == 0) {
+            hh[0] = sqrtf(fmaxf(c1[k], 0.0f));
+            hh[1] = sqrtf(fmaxf(cs[k] - sq, 0.0f));
+        }
+    }
+    __syncthreads();
+    const float h0 = hh[0], h = hh[1];
+    const float inv = (double)h > eps * (double)h0 ? 1.0f / h : 1.0f;
+    if (blockIdx.x == 0) {
+        double* slot = slots + (int64_t)(k - 1) * stride;
+        for (int r = threadIdx.x; r < k; r += blockDim.x) slot[r] = (double)c1[r] + (double)cs[r];
+        if (threadIdx.x == 0) {
+            slot[k] = h;
+            slot[k + 1] = h0;
+            *next = k;
+        }
+    }
+    float* Vk = V + (int64_t)k * ld;
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+        float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f, s3 = 0.0f;
+        int r = 0;
+        for (; r + 3 < k; r += 4) {
+            s0 = fmaf(cs[r], V[(int64_t)r * ld + c], s0);
+            s1 = fmaf(cs[r + 1], V[(int64_t)(r + 1) * ld + c], s1);
+            s2 = fmaf(cs[r + 2], V[(int64_t)(r + 2) * ld + c], s2);
+            s3 = fmaf(cs[r + 3], V[(int64_t)(r + 3) * ld + c], s3);
+        }
+        for (; r < k; ++r) s0 = fmaf(cs[r], V[(int64_t)r * ld + c], s0);
+        const float x = (wf[c] - ((s0 + s1) + (s2 + s3))) * inv;
+        Vk[c] = x;
+        xnext[c] = (double)x;
+    }
+}
+
+// V0 = (float)(a r) and x = V0 in FP64: the first row of an FP32 basis.
+__global__ void k_gm_start_f(int64_t n, double a, const double* __restrict__ r, float* __restrict__ V0,
+                             double* __restrict__ x) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float v = (float)(a * r[i]);
+        V0[i] = v;
+        x[i] = (double)v;
+    }
+}
+
+// x += V[0 : k]^T y over an FP32 basis (FP64 products and sums).
+__global__ void k_gm_update_f(const float* __restrict__ V, int64_t ld, int k, const double* __restrict__ y,
+                              double* __restrict__ x, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double s = 0.0;
+        for (int r = 0; r < k; ++r) s = fma(y[r], (double)V[(int64_t)r * ld + i], s);
+        x[i] += s;
+    }
+}
+
 // Fixed scratch for c3l_hessenberg_coordinates_noalloc: the packed R factors
 // of the shifted solves live here instead of in caller-provided memory.  The
 // array is part of the library's device image, so every GPU that loads the
@@ -1354,6 +1516,43 @@ c3l_status gm_scale(double* V, int64_t ld, const int* cur, int* next, const doub
     const int64_t half = (int64_t)p.blocks * p.R;
     k_gm_scale<<<p.scale_grid, kThreads, 0, s>>>(V, ld, cur, next, partial + half, p.R, (int)p.blocks, c1, eps, w, n,
                                                  xnext, slots, stride);
+    return launch_status();
+}
+
+c3l_status gm_dot_f32(const float* V, int64_t ld, const int* cur, const double* w, float* wf, int64_t n,
+                      const GmPlan& p, float* partial, cudaStream_t s) {
+    if (!V || !cur || !w || !wf || !partial || n <= 0 || p.R > C3L_GMRES_MAX_ROWS) return C3L_ERR_ARGUMENT;
+    k_gm_dot_f<<<p.blocks, kThreads, 0, s>>>(V, ld, cur, w, wf, n, p.seg, partial, p.R);
+    return launch_status();
+}
+
+c3l_status gm_axpy_dot_f32(const float* V, int64_t ld, const int* cur, float* c1, float* wf, int64_t n,
+                           const GmPlan& p, float* partial, cudaStream_t s) {
+    if (!V || !cur || !c1 || !wf || !partial || n <= 0 || p.R > C3L_GMRES_MAX_ROWS) return C3L_ERR_ARGUMENT;
+    const int64_t half = (int64_t)p.blocks * p.R;
+    k_gm_axpy_dot_f<<<p.blocks, kThreads, 0, s>>>(V, ld, cur, partial, c1, wf, n, p.seg, partial + half, p.R);
+    return launch_status();
+}
+
+c3l_status gm_scale_f32(float* V, int64_t ld, const int* cur, int* next, const float* partial, const float* c1,
+                        double eps, const float* wf, int64_t n, const GmPlan& p, double* xnext, double* slots,
+                        int stride, cudaStream_t s) {
+    if (!V || !cur || !next || !partial || !c1 || !wf || !xnext || !slots || n <= 0) return C3L_ERR_ARGUMENT;
+    const int64_t half = (int64_t)p.blocks * p.R;
+    k_gm_scale_f<<<p.scale_grid, kThreads, 0, s>>>(V, ld, cur, next, partial + half, p.R, (int)p.blocks, c1, eps, wf,
+                                                   n, xnext, slots, stride);
+    return launch_status();
+}
+
+c3l_status gm_start_f32(int64_t n, double a, const double* r, float* V0, double* x, cudaStream_t s) {
+    if (!r || !V0 || !x || n <= 0) return C3L_ERR_ARGUMENT;
+    k_gm_start_f<<<grid_for(n), kThreads, 0, s>>>(n, a, r, V0, x);
+    return launch_status();
+}
+
+c3l_status gm_update_f32(const float* V, int64_t ld, int k, const double* y, double* x, int64_t n, cudaStream_t s) {
+    if (!V || !y || !x || n <= 0 || k <= 0 || ld < n) return C3L_ERR_ARGUMENT;
+    k_gm_update_f<<<grid_for(n), kThreads, 0, s>>>(V, ld, k, y, x, n);
     return launch_status();
 }
 

@@ -129,7 +129,7 @@ struct OwnedEvents {
 struct GmresGraphs {
     c3l_static_action op{};
     const double* pc_m4_elem = nullptr;
-    int32_t use_f32 = 0;
+    int32_t use_f32 = 0, basis_f32 = 0;
     int64_t n = 0, nrep = 0;
     int restart = 0;
     const void* ptrs[10] = {};
@@ -145,7 +145,7 @@ struct GmresGraphs {
         const void* p[10];
         key_ptrs(a, p);
         return std::memcmp(&op, a->jvp, sizeof(op)) == 0 && pc_m4_elem == a->pc_m4_elem && use_f32 == a->use_f32 &&
-               n == a->dim && nrep == a->nrep && restart == rs && std::memcmp(ptrs, p, sizeof(ptrs)) == 0;
+               basis_f32 == a->basis_f32 && n == a->dim && nrep == a->nrep && restart == rs && std::memcmp(ptrs, p, sizeof(ptrs)) == 0;
     }
 };
 
@@ -199,8 +199,7 @@ int64_t c3l_gmres_scratch(int32_t restart, int64_t dim) {
 c3l_status c3l_gmres(c3l_gmres_args* a, void* stream) {
     if (!a || !a->jvp || !a->b || !a->x || !a->V || !a->tmp || !a->r || !a->coeff || !a->partial || !a->host ||
         !a->pc_m4 || !a->pc_col || !a->pc_pair || !a->work || !a->counters || !a->slots || a->dim <= 0 ||
-        a->partial_capacity <= 0 ||
-        a->restart <= 0 || a->maxiter <= 0)
+        a->partial_capacity <= 0 || a->restart <= 0 || a->maxiter <= 0 || (a->basis_f32 && !a->use_f32))
         return C3L_ERR_ARGUMENT;
     cudaStream_t s = as_stream(stream);
     const int64_t n = a->dim;
@@ -222,6 +221,12 @@ c3l_status c3l_gmres(c3l_gmres_args* a, void* stream) {
     double* wfix = a->work + n;
     const int R = restart + 2;
     double* c1 = coeff;  // reduced pass-1 projections (k + 1)
+    // FP32 basis: rows of n floats, then the FP32 work vector, inside V
+    const bool f32b = a->basis_f32 != 0;
+    float* Vf = reinterpret_cast<float*>(V);
+    float* wf = Vf + (int64_t)(restart + 1) * n;
+    float* c1f = reinterpret_cast<float*>(coeff);
+    float* pf = reinterpret_cast<float*>(a->partial);
     const int stride = restart + 3;
     if (R > C3L_GMRES_MAX_ROWS) return C3L_ERR_CAPACITY;
     const c3l::GmPlan gp = c3l::gm_plan(n, R, sm_count());
@@ -236,6 +241,7 @@ c3l_status c3l_gmres(c3l_gmres_args* a, void* stream) {
         gg.op = *a->jvp;
         gg.pc_m4_elem = a->pc_m4_elem;
         gg.use_f32 = a->use_f32;
+        gg.basis_f32 = a->basis_f32;
         gg.n = n;
         gg.nrep = a->nrep;
         gg.restart = restart;
@@ -259,6 +265,11 @@ c3l_status c3l_gmres(c3l_gmres_args* a, void* stream) {
                                    : c3l_static_apply(op, xcur, a->tmp, csv);
                     if (q) return q;
                     if ((q = c3l_precondition(a->nrep, a->pc_m4, a->pc_col, a->pc_pair, a->tmp, wfix, csv))) return q;
+                }
+                if (f32b) {
+                    if ((q = c3l::gm_dot_f32(Vf, n, cur, wfix, wf, n, gp, pf, cs))) return q;
+                    if ((q = c3l::gm_axpy_dot_f32(Vf, n, cur, c1f, wf, n, gp, pf, cs))) return q;
+                    return c3l::gm_scale_f32(Vf, n, cur, next, pf, c1f, eps, wf, n, gp, xcur, a->slots, stride, cs);
                 }
                 if ((q = c3l::gm_dot(V, n, cur, wfix, n, gp, a->partial, cs))) return q;
                 if ((q = c3l::gm_axpy_dot(V, n, cur, c1, wfix, n, gp, a->partial, cs))) return q;
@@ -314,13 +325,19 @@ c3l_status c3l_gmres(c3l_gmres_args* a, void* stream) {
     auto H = [&](int col, int row) -> double& { return h[(size_t)col * (restart + 1) + row]; };
     for (int iteration = 0; iteration < a->maxiter; ++iteration) {
         if (iteration == 0 && bnrm2 < atol) return C3L_OK;
-        if ((st = psolve(a->r, V))) return st;
         double beta;
-        if ((st = norm(V, beta))) return st;
-        if ((st = c3l_scale_r(n, 1.0 / beta, V, V, stream))) return st;
-        if (cudaMemcpyAsync(xcur, V, n * sizeof(double), cudaMemcpyDeviceToDevice, s) != cudaSuccess ||
-            cudaMemsetAsync(a->counters, 0, 4 * sizeof(int32_t), s) != cudaSuccess)
-            return C3L_ERR_LAUNCH;
+        if (f32b) {
+            if ((st = psolve(a->r, a->tmp))) return st;
+            if ((st = norm(a->tmp, beta))) return st;
+            if ((st = c3l::gm_start_f32(n, 1.0 / beta, a->tmp, Vf, xcur, s))) return st;
+        } else {
+            if ((st = psolve(a->r, V))) return st;
+            if ((st = norm(V, beta))) return st;
+            if ((st = c3l_scale_r(n, 1.0 / beta, V, V, stream))) return st;
+            if (cudaMemcpyAsync(xcur, V, n * sizeof(double), cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+                return C3L_ERR_LAUNCH;
+        }
+        if (cudaMemsetAsync(a->counters, 0, 4 * sizeof(int32_t), s) != cudaSuccess) return C3L_ERR_LAUNCH;
         a->launches += 1;  // scale
         std::fill(S.begin(), S.end(), 0.0);
         std::fill(h.begin(), h.end(), 0.0);
@@ -384,7 +401,9 @@ c3l_status c3l_gmres(c3l_gmres_args* a, void* stream) {
         std::copy(y.begin(), y.end(), yhost);
         if (cudaMemcpyAsync(coeff, yhost, (col + 1) * sizeof(double), cudaMemcpyHostToDevice, s) != cudaSuccess)
             return C3L_ERR_LAUNCH;
-        if ((st = c3l_multi_axpy_r(V, n, col + 1, coeff, 1.0, a->x, n, stream))) return st;
+        if ((st = f32b ? c3l::gm_update_f32(Vf, n, col + 1, coeff, a->x, n, s)
+                       : c3l_multi_axpy_r(V, n, col + 1, coeff, 1.0, a->x, n, stream)))
+            return st;
         if ((st = matvec(a->x, a->tmp))) return st;
         if (cudaMemcpyAsync(a->r, a->b, n * sizeof(double), cudaMemcpyDeviceToDevice, s) != cudaSuccess) return C3L_ERR_LAUNCH;
         if ((st = c3l_multi_axpy_r(a->tmp, n, 1, ones, -1.0, a->r, n, stream))) return st;

@@ -184,11 +184,14 @@ class DeviceGMRES:
                 self._lib.c3l_gmres_release(handle)
 
     def solve(self, b: torch.Tensor, x: torch.Tensor, *, rtol: float, atol: float, maxiter: int,
-              single: bool = False):
+              single: bool = False, basis_f32: bool = False):
+        """One Newton correction solve; ``single`` applies the FP32 JVP, and
+        ``basis_f32`` (with ``single``) also keeps the Krylov basis in FP32."""
         ops = self.ops
         a = rt.GmresArgs()
         a.jvp = C.addressof(ops.jvp32_action if single else ops.jvp_action)
         a.use_f32 = 1 if single else 0
+        a.basis_f32 = 1 if (single and basis_f32) else 0
         a.nrep = ops.nrep
         a.pc_m4, a.pc_col, a.pc_pair = ops.pc_m4.data_ptr(), ops.pc_col.data_ptr(), ops.pc_pair.data_ptr()
         a.dim = ops.D
@@ -203,9 +206,10 @@ class DeviceGMRES:
         a.pc_m4_elem = ops.pc_m4_elem.data_ptr()
         a.partial_capacity = self.partial.numel()
         a.keep_graphs = 1
-        a.graph_cache = self._graphs.get(single)
+        key = (single, bool(a.basis_f32))
+        a.graph_cache = self._graphs.get(key)
         st = rt.lib().c3l_gmres(C.byref(a), rt.stream_ptr(ops.device))
-        self._graphs[single] = a.graph_cache  # the call replaces a stale cache itself
+        self._graphs[key] = a.graph_cache  # the call replaces a stale cache itself
         rt.check(st, "gmres")
         hist = list(self.history[:min(a.history_len, self.history.size)])
         rt.LaunchCounter.add(int(a.launches))

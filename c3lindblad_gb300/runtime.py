@@ -64,7 +64,7 @@ class GmresArgs(C.Structure):
                 ("history_capacity", C.c_int32), ("history_len", C.c_int32), ("info", C.c_int32),
                 ("matvecs", C.c_int32), ("use_f32", C.c_int32), ("work", C.c_void_p), ("counters", C.c_void_p),
                 ("slots", C.c_void_p), ("launches", C.c_int64), ("pc_m4_elem", C.c_void_p),
-                ("partial_capacity", C.c_int64), ("keep_graphs", C.c_int32), ("pad2", C.c_int32),
+                ("partial_capacity", C.c_int64), ("keep_graphs", C.c_int32), ("basis_f32", C.c_int32),
                 ("graph_cache", C.c_void_p)]
 
 

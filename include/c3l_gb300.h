@@ -374,7 +374,10 @@ typedef struct {
      * flags and buffers are unchanged (NULL on the first call); release them
      * with c3l_gmres_release.  keep_graphs = 0: captured per call. */
     int32_t keep_graphs;
-    int32_t pad2;
+    /* input: nonzero (with use_f32) keeps the Krylov basis in FP32 and runs
+     * CGS2 in FP32; V then holds (restart+1)*dim floats of rows followed by
+     * a dim-float work vector (within the same allocation). */
+    int32_t basis_f32;
     void* graph_cache;
 } c3l_gmres_args;
 
