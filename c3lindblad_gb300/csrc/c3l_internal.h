@@ -34,26 +34,43 @@ struct RowDot {
 RowDot row_dot_plan(int max_rows, int64_t dim, int sms);
 int64_t row_dot_partial_size(const RowDot& p);  // entries of the partial buffer
 
-// out[r] = V[r]^H w (r < k) [and |w|^2 at r = k when self]
-c3l_status dot_rows_dev_c(const c3l_complex* V, int64_t ld, const int* cur, int self, const c3l_complex* w,
-                          int64_t dim, const RowDot& p, c3l_complex* partial, c3l_complex* out, cudaStream_t s);
-// The same projections with FP32 products and sums (first CGS2 pass only).
-c3l_status dot_rows_f32acc_dev_c(const c3l_complex* V, int64_t ld, const int* cur, const c3l_complex* w, int64_t dim,
-                                 const RowDot& p, c3l_complex* out, cudaStream_t s);
-// Pass-2 projections with the Arnoldi column: c2[r] = V[r]^H w (r < k),
-// c2[k] = |w|^2, then h = sqrt(|w|^2 - |c2|^2), column j = k - 1 of Hc
-// (c1 + c2 | h), *hval = h and *next = k (done: zero between launches).
-c3l_status dot_rows_column_dev_c(const c3l_complex* V, int64_t ld, const int* cur, int* next, const c3l_complex* w,
-                                 int64_t dim, const RowDot& p, c3l_complex* partial, unsigned* done,
-                                 const c3l_complex* c1, c3l_complex* c2, c3l_complex* Hc, int64_t ldc, double* hval,
-                                 cudaStream_t s);
-// w += alpha * V[0 : k]^T c
-c3l_status axpy_dev_c(const c3l_complex* V, int64_t ld, const int* cur, int max_k, const c3l_complex* c,
-                      c3l_complex alpha, c3l_complex* w, int64_t dim, cudaStream_t s);
+// One Arnoldi step's CGS2 for a batch of channels in one launch per kernel
+// (blockIdx.y = channel).  Per channel: basis V (rows of ld), work vector w
+// (the operator's output, updated in place), next input xnext, projections
+// c1 and c2 (k + 1 entries each), h, Hessenberg columns Hc (leading dimension
+// ldc), the pass-2 partials (when the plan has several segments) and the
+// counters {step index by parity, done (zero between launches), stop}.  A
+// channel whose stop counter is nonzero is skipped by every kernel.
+struct ArnoldiBatch {
+    int nb;
+    double2* V[C3L_MAX_BATCH];
+    double2* w[C3L_MAX_BATCH];
+    double2* xnext[C3L_MAX_BATCH];
+    double2* c1[C3L_MAX_BATCH];
+    double2* c2[C3L_MAX_BATCH];
+    double* hval[C3L_MAX_BATCH];
+    int32_t* counters[C3L_MAX_BATCH];
+    double2* Hc[C3L_MAX_BATCH];
+    double2* partial[C3L_MAX_BATCH];
+};
+// pass 1 (FP32 products): c1[r] = V[r]^H w, r < k = counters[par] + 1
+c3l_status arnoldi_dot1(const ArnoldiBatch& bt, int par, int64_t ld, int64_t dim, const RowDot& p, cudaStream_t s);
+// w -= V[0 : k]^T c1
+c3l_status arnoldi_axpy1(const ArnoldiBatch& bt, int par, int64_t ld, int max_k, int64_t dim, cudaStream_t s);
+// pass 2 (FP64): c2[r] = V[r]^H w, c2[k] = |w|^2, h = sqrt(|w|^2 - |c2|^2),
+// column k - 1 of Hc = (c1 + c2 | h), *hval = h, counters[1 - par] = k
+c3l_status arnoldi_dot2(const ArnoldiBatch& bt, int par, int64_t ld, int64_t dim, const RowDot& p, int64_t ldc,
+                        cudaStream_t s);
 // V[k] = xnext = (w - V[0 : k]^T c2) / h (unscaled when h <= tol)
-c3l_status arnoldi_scale_dev(c3l_complex* V, int64_t ld, const int* cur, int max_k, const c3l_complex* c2,
-                             const double* hval, double tol, const c3l_complex* w, int64_t n, c3l_complex* xnext,
-                             cudaStream_t s);
+c3l_status arnoldi_scale(const ArnoldiBatch& bt, int par, int64_t ld, int max_k, double tol, int64_t n,
+                         cudaStream_t s);
+
+// The sigma action on a batch of vectors (actions[b] share one program and
+// differ in their workspace); an entry whose stop flag is set is skipped.
+c3l_status eom_sigma_batch(const c3l_eom_action* actions, int nb, const c3l_complex* const* xin,
+                           c3l_complex* const* out, const int32_t* const* stop, cudaStream_t s);
+// True when two sigma actions run the same program (they may differ in ws).
+bool same_sigma_program(const c3l_eom_action& a, const c3l_eom_action& b);
 
 // GMRES (real) step: a short basis over a long vector.  Blocks own column
 // segments for all rows; partial sums partial[block][R] are reduced by the

@@ -811,53 +811,41 @@ __device__ __forceinline__ bool last_block(unsigned* done) {
     return last;
 }
 
-// Arnoldi column from the reduced projections (run by one block): c2 holds
-// the pass-2 projections (k) followed by |w'|^2, so h = sqrt(|w'|^2 - |c2|^2);
-// H[:k+1, j] = c1 + c2 | h goes to column j of Hc, h to hval, and the step
-// counter of the other parity to k.
-__device__ void arnoldi_column_tail(const double2* __restrict__ c1, const double2* __restrict__ c2, int k,
-                                    double2* __restrict__ Hc, int64_t ldc, double* __restrict__ hval, int* next) {
-    __shared__ double red[32];
-    double sq = 0.0;
-    for (int i = threadIdx.x; i < k; i += blockDim.x) sq = fma(c2[i].x, c2[i].x, fma(c2[i].y, c2[i].y, sq));
-    sq = block_sum(sq, red);
-    double2* col = Hc + (int64_t)(k - 1) * ldc;
-    for (int i = threadIdx.x; i < k; i += blockDim.x) col[i] = make_double2(c1[i].x + c2[i].x, c1[i].y + c2[i].y);
-    if (threadIdx.x == 0) {
-        const double h = sqrt(fmax(c2[k].x - sq, 0.0));
-        col[k] = make_double2(h, 0.0);
-        *hval = h;
-        *next = k;
-    }
-}
+// ------------------------------------------------ Arnoldi (complex) step
+// Device-indexed CGS2 of the Arnoldi step for a batch of channels
+// (blockIdx.y = channel, each with its own basis, work vectors, projections
+// and counters {step index by parity, done, stop}); a channel whose stop flag
+// is set does nothing.  k = *cur + 1 basis rows of dimension dim.
 
-// Rows [0, k) of V (plus the vector itself when self) dotted with w, k =
-// *cur + 1, in segments of seglen; with one segment the block writes out[row]
-// directly, otherwise partial[row][seg].  COLUMN: the last block also forms
-// the Arnoldi column (single-segment case).
-// First CGS2 pass with FP32 products and sums (complex rows only): the second
-// pass, in FP64, measures and removes what the first left, and the column is
-// c1 + c2, so the Arnoldi relation and the orthogonality keep FP64 accuracy.
-__global__ void __launch_bounds__(kThreads) k_dot_rows_f32acc(const double2* __restrict__ V, int64_t ld, const int* cur,
-                                                              const double2* __restrict__ w, int64_t dim,
-                                                              double2* __restrict__ out) {
+__device__ __forceinline__ bool arn_stopped(const c3l::ArnoldiBatch& bt) { return bt.counters[blockIdx.y][3] != 0; }
+
+// Pass 1 with FP32 products and sums: c1[r] = V[r]^H w (one block per row).
+// The second pass, in FP64, measures and removes what the first left, and the
+// column is c1 + c2, so the Arnoldi relation and the orthogonality keep FP64
+// accuracy.
+__global__ void __launch_bounds__(kThreads) k_arn_dot1(c3l::ArnoldiBatch bt, int par, int64_t ld, int64_t dim) {
     __shared__ float sm[2][32];
-    const int k = *cur + 1;
+    if (arn_stopped(bt)) return;
+    const int b = blockIdx.y;
+    const double2* __restrict__ V = bt.V[b];
+    const double2* __restrict__ w = bt.w[b];
+    double2* __restrict__ out = bt.c1[b];
+    const int k = bt.counters[b][par] + 1;
     for (int row = blockIdx.x; row < k; row += gridDim.x) {
         const double2* v = V + (int64_t)row * ld;
         const int64_t step = blockDim.x;
         float re = 0.0f, im = 0.0f;
         int64_t i = threadIdx.x;
         for (; i + 3 * step < dim; i += 4 * step) {
-            double2 a[4], b[4];
+            double2 a[4], c[4];
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
                 a[u] = v[i + u * step];
-                b[u] = w[i + u * step];
+                c[u] = w[i + u * step];
             }
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
-                const float ax = (float)a[u].x, ay = (float)a[u].y, bx = (float)b[u].x, by = (float)b[u].y;
+                const float ax = (float)a[u].x, ay = (float)a[u].y, bx = (float)c[u].x, by = (float)c[u].y;
                 re = fmaf(ax, bx, fmaf(ay, by, re));
                 im = fmaf(ax, by, fmaf(-ay, bx, im));
             }
@@ -892,156 +880,161 @@ __global__ void __launch_bounds__(kThreads) k_dot_rows_f32acc(const double2* __r
     }
 }
 
-template <typename T, bool COLUMN>
-__global__ void __launch_bounds__(kThreads) k_dot_rows_dev(const T* __restrict__ V, int64_t ld, const int* cur,
-                                                           int self, const T* __restrict__ w, int64_t dim, int nseg,
-                                                           int64_t seglen, T* __restrict__ partial,
-                                                           T* __restrict__ out, unsigned* done,
-                                                           const T* __restrict__ c1, T* __restrict__ Hc, int64_t ldc,
-                                                           double* __restrict__ hval, int* next) {
+// t = V[0 : k]^T c for the block's X entries (Y partial rows, reduced in
+// shared memory); valid in threadIdx.y == 0.
+template <int X, int Y>
+__device__ __forceinline__ double2 arn_combine(const double2* __restrict__ V, int64_t ld, int k,
+                                               const double2* __restrict__ c, int64_t i, int64_t dim,
+                                               double2 (&part)[Y][X]) {
+    double2 s = make_double2(0.0, 0.0);
+    if (i < dim) {
+        int j = threadIdx.y;
+        for (; j + 3 * Y < k; j += 4 * Y) {  // four independent loads in flight
+            double2 cj[4], v[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                cj[u] = c[j + u * Y];
+                v[u] = V[(int64_t)(j + u * Y) * ld + i];
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) axpy_acc(s, cj[u], v[u]);
+        }
+        for (; j < k; j += Y) axpy_acc(s, c[j], V[(int64_t)j * ld + i]);
+    }
+    part[threadIdx.y][threadIdx.x] = s;
+    __syncthreads();
+    for (int h = Y / 2; h > 0; h >>= 1) {
+        if ((int)threadIdx.y < h) {
+            double2 t = part[threadIdx.y][threadIdx.x];
+            dot_acc_plain(t, part[threadIdx.y + h][threadIdx.x]);
+            part[threadIdx.y][threadIdx.x] = t;
+        }
+        __syncthreads();
+    }
+    return part[0][threadIdx.x];
+}
+
+// First update: w -= V c1.
+template <int X, int Y>
+__global__ void __launch_bounds__(X * Y) k_arn_axpy(c3l::ArnoldiBatch bt, int par, int64_t ld, int64_t dim) {
+    __shared__ double2 part[Y][X];
+    if (arn_stopped(bt)) return;
+    const int b = blockIdx.y;
+    const int k = bt.counters[b][par] + 1;
+    double2* __restrict__ w = bt.w[b];
+    for (int64_t base = (int64_t)blockIdx.x * X; base < dim; base += (int64_t)gridDim.x * X) {
+        const int64_t i = base + threadIdx.x;
+        const double2 t = arn_combine<X, Y>(bt.V[b], ld, k, bt.c1[b], i, dim, part);
+        if (threadIdx.y == 0 && i < dim) w[i] = make_double2(w[i].x - t.x, w[i].y - t.y);
+        __syncthreads();
+    }
+}
+
+// Arnoldi column from the reduced projections (run by one block): c2 holds
+// the pass-2 projections (k) followed by |w'|^2, so h = sqrt(|w'|^2 - |c2|^2);
+// H[:k+1, j] = c1 + c2 | h goes to column j of Hc, h to hval, and the step
+// counter of the other parity to k.
+__device__ void arnoldi_column_tail(const double2* __restrict__ c1, const double2* __restrict__ c2, int k,
+                                    double2* __restrict__ Hc, int64_t ldc, double* __restrict__ hval, int* next) {
+    __shared__ double red[32];
+    double sq = 0.0;
+    for (int i = threadIdx.x; i < k; i += blockDim.x) sq = fma(c2[i].x, c2[i].x, fma(c2[i].y, c2[i].y, sq));
+    sq = block_sum(sq, red);
+    double2* col = Hc + (int64_t)(k - 1) * ldc;
+    for (int i = threadIdx.x; i < k; i += blockDim.x) col[i] = make_double2(c1[i].x + c2[i].x, c1[i].y + c2[i].y);
+    if (threadIdx.x == 0) {
+        const double h = sqrt(fmax(c2[k].x - sq, 0.0));
+        col[k] = make_double2(h, 0.0);
+        *hval = h;
+        *next = k;
+    }
+}
+
+// Pass 2 in FP64: rows [0, k) and the vector itself (|w'|^2) in nseg segments
+// of seglen, one block per (row, segment) item; with one segment the block
+// writes c2[row] and the block that finishes last forms the column, otherwise
+// it writes partial[row][seg] for k_arn_dot2_final.  Every block reaches the
+// last-block count.
+__global__ void __launch_bounds__(kThreads) k_arn_dot2(c3l::ArnoldiBatch bt, int par, int64_t ld, int64_t dim,
+                                                       int nseg, int64_t seglen, int64_t ldc) {
     __shared__ double sm[32];
-    const int k = *cur + 1;
-    const int items = (k + self) * nseg;
+    if (arn_stopped(bt)) return;
+    const int b = blockIdx.y;
+    const double2* __restrict__ V = bt.V[b];
+    const double2* __restrict__ w = bt.w[b];
+    int32_t* ctr = bt.counters[b];
+    const int k = ctr[par] + 1;
+    const int items = (k + 1) * nseg;
     for (int item = blockIdx.x; item < items; item += gridDim.x) {
         const int row = item / nseg;
         const int seg = item - row * nseg;
-        const T* v = row < k ? V + (int64_t)row * ld : w;
+        const double2* v = row < k ? V + (int64_t)row * ld : w;
         const int64_t lo = (int64_t)seg * seglen;
         const int64_t hi = min(dim, lo + seglen);
         const int64_t step = blockDim.x;
-        T acc;
-        zero(acc);
+        double2 acc = make_double2(0.0, 0.0);
         int64_t i = lo + threadIdx.x;
         for (; i + 3 * step < hi; i += 4 * step) {
-            T a[4], b[4];
+            double2 a[4], c[4];
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
                 a[u] = v[i + u * step];
-                b[u] = w[i + u * step];
+                c[u] = w[i + u * step];
             }
 #pragma unroll
-            for (int u = 0; u < 4; ++u) dot_acc(acc, a[u], b[u]);
+            for (int u = 0; u < 4; ++u) dot_acc(acc, a[u], c[u]);
         }
         for (; i < hi; i += step) dot_acc(acc, v[i], w[i]);
         acc = block_sum_t(acc, sm);
         if (threadIdx.x == 0) {
-            if (nseg == 1) out[row] = acc;
-            else partial[(int64_t)row * nseg + seg] = acc;
+            if (nseg == 1) bt.c2[b][row] = acc;
+            else bt.partial[b][(int64_t)row * nseg + seg] = acc;
         }
     }
-    if (COLUMN) {
-        if (last_block(done)) {
-            if constexpr (std::is_same<T, double2>::value) arnoldi_column_tail(c1, out, k, Hc, ldc, hval, next);
-            if (threadIdx.x == 0) *done = 0u;
-        }
+    if (nseg == 1 && last_block(reinterpret_cast<unsigned*>(ctr + 2))) {
+        arnoldi_column_tail(bt.c1[b], bt.c2[b], k, bt.Hc[b], ldc, bt.hval[b], ctr + (1 - par));
+        if (threadIdx.x == 0) ctr[2] = 0;
     }
 }
 
-template <typename T, bool COLUMN>
-__global__ void __launch_bounds__(kThreads) k_dot_final_dev(const T* __restrict__ partial, const int* cur, int self,
-                                                            int nseg, T* __restrict__ out, unsigned* done,
-                                                            const T* __restrict__ c1, T* __restrict__ Hc,
-                                                            int64_t ldc, double* __restrict__ hval, int* next) {
+__global__ void __launch_bounds__(kThreads) k_arn_dot2_final(c3l::ArnoldiBatch bt, int par, int nseg, int64_t ldc) {
     __shared__ double sm[32];
-    const int k = *cur + 1;
-    const int rows = k + self;
-    for (int row = blockIdx.x; row < rows; row += gridDim.x) {
-        T acc;
-        zero(acc);
-        for (int b = threadIdx.x; b < nseg; b += blockDim.x) dot_acc_plain(acc, partial[(int64_t)row * nseg + b]);
+    if (arn_stopped(bt)) return;
+    const int b = blockIdx.y;
+    int32_t* ctr = bt.counters[b];
+    const int k = ctr[par] + 1;
+    const double2* __restrict__ partial = bt.partial[b];
+    for (int row = blockIdx.x; row <= k; row += gridDim.x) {
+        double2 acc = make_double2(0.0, 0.0);
+        for (int q = threadIdx.x; q < nseg; q += blockDim.x) dot_acc_plain(acc, partial[(int64_t)row * nseg + q]);
         acc = block_sum_t(acc, sm);
-        if (threadIdx.x == 0) out[row] = acc;
+        if (threadIdx.x == 0) bt.c2[b][row] = acc;
     }
-    if (COLUMN) {
-        if (last_block(done)) {
-            if constexpr (std::is_same<T, double2>::value) arnoldi_column_tail(c1, out, k, Hc, ldc, hval, next);
-            if (threadIdx.x == 0) *done = 0u;
-        }
+    if (last_block(reinterpret_cast<unsigned*>(ctr + 2))) {
+        arnoldi_column_tail(bt.c1[b], bt.c2[b], k, bt.Hc[b], ldc, bt.hval[b], ctr + (1 - par));
+        if (threadIdx.x == 0) ctr[2] = 0;
     }
 }
 
-template <typename T, int X, int Y>
-__global__ void __launch_bounds__(X * Y) k_axpy_dev(const T* __restrict__ V, int64_t ld, const int* cur,
-                                                     const T* __restrict__ c, T alpha, T* __restrict__ w,
-                                                     int64_t dim) {
-    __shared__ T part[Y][X];
-    const int k = *cur + 1;
-    for (int64_t base = (int64_t)blockIdx.x * X; base < dim; base += (int64_t)gridDim.x * X) {
-        const int64_t i = base + threadIdx.x;
-        T s;
-        zero(s);
-        if (i < dim) {
-            int j = threadIdx.y;
-            for (; j + 3 * Y < k; j += 4 * Y) {
-                T cj[4], v[4];
-#pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    cj[u] = c[j + u * Y];
-                    v[u] = V[(int64_t)(j + u * Y) * ld + i];
-                }
-#pragma unroll
-                for (int u = 0; u < 4; ++u) axpy_acc(s, cj[u], v[u]);
-            }
-            for (; j < k; j += Y) axpy_acc(s, c[j], V[(int64_t)j * ld + i]);
-        }
-        part[threadIdx.y][threadIdx.x] = s;
-        __syncthreads();
-        for (int h = Y / 2; h > 0; h >>= 1) {
-            if ((int)threadIdx.y < h) {
-                T o = part[threadIdx.y + h][threadIdx.x];
-                T cur2 = part[threadIdx.y][threadIdx.x];
-                dot_acc_plain(cur2, o);
-                part[threadIdx.y][threadIdx.x] = cur2;
-            }
-            __syncthreads();
-        }
-        if (threadIdx.y == 0 && i < dim) w[i] = add_scaled(w[i], alpha, part[0][threadIdx.x]);
-        __syncthreads();
-    }
-}
-
-// Second Arnoldi update and normalization: V[k] = xnext = (w' - V c2) / h,
-// unscaled when h <= tol (breakdown, detected by the shifted solves).
+// Second update and normalization: V[k] = xnext = (w' - V c2) / h, unscaled
+// when h <= tol (breakdown, detected by the shifted solves).  Reads the step
+// index from `cur` of the parity (the column tail already wrote `next`).
 template <int X, int Y>
-__global__ void __launch_bounds__(X * Y) k_arnoldi_scale(double2* V, int64_t ld, const int* cur,
-                                                          const double2* __restrict__ c2,
-                                                          const double* __restrict__ hval, double tol,
-                                                          const double2* __restrict__ w, int64_t n,
-                                                          double2* __restrict__ xnext) {
+__global__ void __launch_bounds__(X * Y) k_arn_scale(c3l::ArnoldiBatch bt, int par, int64_t ld, int64_t n,
+                                                     double tol) {
     __shared__ double2 part[Y][X];
-    const int k = *cur + 1;
-    const double h = *hval;
+    if (arn_stopped(bt)) return;
+    const int b = blockIdx.y;
+    const int k = bt.counters[b][par] + 1;
+    const double h = *bt.hval[b];
     const double inv = h > tol ? 1.0 / h : 1.0;
-    double2* Vk = V + (int64_t)k * ld;
+    double2* Vk = bt.V[b] + (int64_t)k * ld;
+    const double2* __restrict__ w = bt.w[b];
+    double2* __restrict__ xnext = bt.xnext[b];
     for (int64_t base = (int64_t)blockIdx.x * X; base < n; base += (int64_t)gridDim.x * X) {
         const int64_t i = base + threadIdx.x;
-        double2 s = make_double2(0.0, 0.0);
-        if (i < n) {
-            int j = threadIdx.y;
-            for (; j + 3 * Y < k; j += 4 * Y) {
-                double2 cj[4], v[4];
-#pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    cj[u] = c2[j + u * Y];
-                    v[u] = V[(int64_t)(j + u * Y) * ld + i];
-                }
-#pragma unroll
-                for (int u = 0; u < 4; ++u) axpy_acc(s, cj[u], v[u]);
-            }
-            for (; j < k; j += Y) axpy_acc(s, c2[j], V[(int64_t)j * ld + i]);
-        }
-        part[threadIdx.y][threadIdx.x] = s;
-        __syncthreads();
-        for (int hh = Y / 2; hh > 0; hh >>= 1) {
-            if ((int)threadIdx.y < hh) {
-                double2 c = part[threadIdx.y][threadIdx.x];
-                dot_acc_plain(c, part[threadIdx.y + hh][threadIdx.x]);
-                part[threadIdx.y][threadIdx.x] = c;
-            }
-            __syncthreads();
-        }
+        const double2 t = arn_combine<X, Y>(bt.V[b], ld, k, bt.c2[b], i, n, part);
         if (threadIdx.y == 0 && i < n) {
-            const double2 t = part[0][threadIdx.x];
             const double2 x = make_double2((w[i].x - t.x) * inv, (w[i].y - t.y) * inv);
             Vk[i] = x;
             xnext[i] = x;
@@ -1401,81 +1394,44 @@ RowDot row_dot_plan(int max_rows, int64_t dim, int sms) {
 
 int64_t row_dot_partial_size(const RowDot& p) { return p.nseg == 1 ? 0 : (int64_t)p.max_rows * p.nseg; }
 
-template <typename T, bool COLUMN>
-static c3l_status dot_rows_dev(const T* V, int64_t ld, const int* cur, int self, const T* w, int64_t dim,
-                               const RowDot& p, T* partial, T* out, unsigned* done, const T* c1, T* Hc, int64_t ldc,
-                               double* hval, int* next, cudaStream_t s) {
-    if (!V || !cur || !w || !out || dim <= 0 || ld < dim || (p.nseg > 1 && !partial)) return C3L_ERR_ARGUMENT;
-    if (COLUMN && (!done || !c1 || !Hc || !hval || !next)) return C3L_ERR_ARGUMENT;
-    if (p.nseg == 1) {
-        k_dot_rows_dev<T, COLUMN><<<p.grid, kThreads, 0, s>>>(V, ld, cur, self, w, dim, 1, p.seglen, partial, out,
-                                                             done, c1, Hc, ldc, hval, next);
-    } else {
-        k_dot_rows_dev<T, false><<<p.grid, kThreads, 0, s>>>(V, ld, cur, self, w, dim, p.nseg, p.seglen, partial,
-                                                            out, nullptr, nullptr, nullptr, 0, nullptr, nullptr);
+static bool valid_batch(const ArnoldiBatch& bt, bool with_partial) {
+    if (bt.nb < 1 || bt.nb > C3L_MAX_BATCH) return false;
+    for (int b = 0; b < bt.nb; ++b)
+        if (!bt.V[b] || !bt.w[b] || !bt.xnext[b] || !bt.c1[b] || !bt.c2[b] || !bt.hval[b] || !bt.counters[b] ||
+            !bt.Hc[b] || (with_partial && !bt.partial[b]))
+            return false;
+    return true;
+}
+
+c3l_status arnoldi_dot1(const ArnoldiBatch& bt, int par, int64_t ld, int64_t dim, const RowDot& p, cudaStream_t s) {
+    if (!valid_batch(bt, false) || dim <= 0 || ld < dim || (par & ~1)) return C3L_ERR_ARGUMENT;
+    k_arn_dot1<<<dim3(p.grid, (unsigned)bt.nb), kThreads, 0, s>>>(bt, par, ld, dim);
+    return launch_status();
+}
+
+c3l_status arnoldi_axpy1(const ArnoldiBatch& bt, int par, int64_t ld, int max_k, int64_t dim, cudaStream_t s) {
+    if (!valid_batch(bt, false) || dim <= 0 || ld < dim || (par & ~1)) return C3L_ERR_ARGUMENT;
+    (void)max_k;
+    k_arn_axpy<kAxX, kAxY><<<dim3(axpy_grid(dim), (unsigned)bt.nb), dim3(kAxX, kAxY), 0, s>>>(bt, par, ld, dim);
+    return launch_status();
+}
+
+c3l_status arnoldi_dot2(const ArnoldiBatch& bt, int par, int64_t ld, int64_t dim, const RowDot& p, int64_t ldc,
+                        cudaStream_t s) {
+    if (!valid_batch(bt, p.nseg > 1) || dim <= 0 || ld < dim || (par & ~1)) return C3L_ERR_ARGUMENT;
+    k_arn_dot2<<<dim3(p.grid, (unsigned)bt.nb), kThreads, 0, s>>>(bt, par, ld, dim, p.nseg, p.seglen, ldc);
+    if (p.nseg > 1) {
         const unsigned g = (unsigned)(p.max_rows > 1024 ? 1024 : p.max_rows);
-        k_dot_final_dev<T, COLUMN><<<g, kThreads, 0, s>>>(partial, cur, self, p.nseg, out, done, c1, Hc, ldc, hval,
-                                                          next);
+        k_arn_dot2_final<<<dim3(g, (unsigned)bt.nb), kThreads, 0, s>>>(bt, par, p.nseg, ldc);
     }
     return launch_status();
 }
 
-c3l_status dot_rows_dev_c(const c3l_complex* V, int64_t ld, const int* cur, int self, const c3l_complex* w,
-                          int64_t dim, const RowDot& p, c3l_complex* partial, c3l_complex* out, cudaStream_t s) {
-    return dot_rows_dev<double2, false>(reinterpret_cast<const double2*>(V), ld, cur, self,
-                                        reinterpret_cast<const double2*>(w), dim, p,
-                                        reinterpret_cast<double2*>(partial), reinterpret_cast<double2*>(out),
-                                        nullptr, nullptr, nullptr, 0, nullptr, nullptr, s);
-}
-
-c3l_status dot_rows_f32acc_dev_c(const c3l_complex* V, int64_t ld, const int* cur, const c3l_complex* w, int64_t dim,
-                                 const RowDot& p, c3l_complex* out, cudaStream_t s) {
-    if (!V || !cur || !w || !out || dim <= 0 || ld < dim) return C3L_ERR_ARGUMENT;
-    k_dot_rows_f32acc<<<p.grid, kThreads, 0, s>>>(reinterpret_cast<const double2*>(V), ld, cur,
-                                                 reinterpret_cast<const double2*>(w), dim,
-                                                 reinterpret_cast<double2*>(out));
-    return launch_status();
-}
-
-c3l_status dot_rows_column_dev_c(const c3l_complex* V, int64_t ld, const int* cur, int* next, const c3l_complex* w,
-                                 int64_t dim, const RowDot& p, c3l_complex* partial, unsigned* done,
-                                 const c3l_complex* c1, c3l_complex* c2, c3l_complex* Hc, int64_t ldc, double* hval,
-                                 cudaStream_t s) {
-    return dot_rows_dev<double2, true>(reinterpret_cast<const double2*>(V), ld, cur, 1,
-                                       reinterpret_cast<const double2*>(w), dim, p,
-                                       reinterpret_cast<double2*>(partial), reinterpret_cast<double2*>(c2), done,
-                                       reinterpret_cast<const double2*>(c1), reinterpret_cast<double2*>(Hc), ldc,
-                                       hval, next, s);
-}
-
-c3l_status axpy_dev_c(const c3l_complex* V, int64_t ld, const int* cur, int max_k, const c3l_complex* c,
-                      c3l_complex alpha, c3l_complex* w, int64_t dim, cudaStream_t s) {
-    if (!V || !cur || !c || !w || dim <= 0 || ld < dim) return C3L_ERR_ARGUMENT;
-    const double2* Vd = reinterpret_cast<const double2*>(V);
-    const double2* cd = reinterpret_cast<const double2*>(c);
-    const double2 al = make_double2(alpha.re, alpha.im);
-    double2* wd = reinterpret_cast<double2*>(w);
-    if (max_k >= kAxYLong)
-        k_axpy_dev<double2, kAxXLong, kAxYLong><<<axpy_grid(dim, kAxXLong), dim3(kAxXLong, kAxYLong), 0, s>>>(
-            Vd, ld, cur, cd, al, wd, dim);
-    else
-        k_axpy_dev<double2, kAxX, kAxY><<<axpy_grid(dim), dim3(kAxX, kAxY), 0, s>>>(Vd, ld, cur, cd, al, wd, dim);
-    return launch_status();
-}
-
-c3l_status arnoldi_scale_dev(c3l_complex* V, int64_t ld, const int* cur, int max_k, const c3l_complex* c2,
-                             const double* hval, double tol, const c3l_complex* w, int64_t n, c3l_complex* xnext,
-                             cudaStream_t s) {
-    if (!V || !cur || !c2 || !hval || !w || !xnext || n <= 0 || ld < n) return C3L_ERR_ARGUMENT;
-    double2* Vd = reinterpret_cast<double2*>(V);
-    const double2* cd = reinterpret_cast<const double2*>(c2);
-    const double2* wd = reinterpret_cast<const double2*>(w);
-    double2* xd = reinterpret_cast<double2*>(xnext);
-    if (max_k >= kAxYLong)
-        k_arnoldi_scale<kAxXLong, kAxYLong><<<axpy_grid(n, kAxXLong), dim3(kAxXLong, kAxYLong), 0, s>>>(
-            Vd, ld, cur, cd, hval, tol, wd, n, xd);
-    else
-        k_arnoldi_scale<kAxX, kAxY><<<axpy_grid(n), dim3(kAxX, kAxY), 0, s>>>(Vd, ld, cur, cd, hval, tol, wd, n, xd);
+c3l_status arnoldi_scale(const ArnoldiBatch& bt, int par, int64_t ld, int max_k, double tol, int64_t n,
+                         cudaStream_t s) {
+    if (!valid_batch(bt, false) || n <= 0 || ld < n || (par & ~1)) return C3L_ERR_ARGUMENT;
+    (void)max_k;
+    k_arn_scale<kAxX, kAxY><<<dim3(axpy_grid(n), (unsigned)bt.nb), dim3(kAxX, kAxY), 0, s>>>(bt, par, ld, n, tol);
     return launch_status();
 }
 

@@ -594,38 +594,72 @@ c3l_status c3l_arnoldi(c3l_arnoldi_channel* ch, int32_t nch, int64_t N, const c3
     const c3l::RowDot rd = c3l::row_dot_plan(m_max + 1, N, sm_count());
     if (c3l::row_dot_partial_size(rd) > c3l_multi_dot_scratch(m_max + 1, N)) return C3L_ERR_CAPACITY;
     c3l_status st;
-    // one Arnoldi step per channel as a graph: xnext -> sigma -> wfix, CGS2
-    // against V[0..j] (the pass-2 projections also form column j of H and
-    // h), V[j+1] = xnext = w'' / h.  The step index alternates between two
-    // counters: graphs exist for both parities, and `interval` chains
-    // check_interval steps starting at either parity.
+    // Channels whose sigma actions run the same program step together in a
+    // group: one Arnoldi step of the whole group is one graph, every kernel
+    // serving all of its channels (blockIdx.y = channel), on the stream of the
+    // group's first channel.  Step: xnext -> sigma -> wfix, CGS2 against
+    // V[0..j] (the pass-2 projections also form column j of H and h), V[j+1]
+    // = xnext = w'' / h.  The step index alternates between two counters per
+    // channel: graphs exist for both parities, and `interval` chains
+    // check_interval steps starting at either parity.  A channel that has
+    // stopped is skipped through its stop counter.
+    std::vector<std::vector<int>> groups;
+    std::vector<int> group_of(nch, 0);
+    for (int c = 0; c < nch; ++c) {
+        int g = -1;
+        for (size_t i = 0; i < groups.size() && g < 0; ++i)
+            if ((int)groups[i].size() < C3L_MAX_BATCH && c3l::same_sigma_program(*ch[groups[i][0]].sigma, *ch[c].sigma))
+                g = (int)i;
+        if (g < 0) {
+            g = (int)groups.size();
+            groups.emplace_back();
+        }
+        groups[g].push_back(c);
+        group_of[c] = g;
+    }
+    const int ng = (int)groups.size();
+    auto chan_stream = [&](int c) { return as_stream(streams[groups[group_of[c]].front()]); };
+    auto d2 = [](c3l_complex* p) { return reinterpret_cast<double2*>(p); };
     OwnedStream cap;
     if ((st = cap.create())) return st;
-    std::vector<StepGraph> one(2 * nch), interval(2 * nch);
-    for (int c = 0; c < nch; ++c) {
-        c3l_arnoldi_channel& q = ch[c];
-        c3l_complex* xnext = q.work;
-        c3l_complex* wfix = q.work + N;
-        c3l_complex* c1 = q.coeff;
-        c3l_complex* c2 = q.coeff + (m_max + 1);
-        double* hval = reinterpret_cast<double*>(q.coeff + 2 * (m_max + 1));
-        unsigned* done = reinterpret_cast<unsigned*>(q.counters + 2);
+    std::vector<StepGraph> one(2 * ng), interval(2 * ng);
+    for (int g = 0; g < ng; ++g) {
+        const std::vector<int>& mem = groups[g];
+        const int nb = (int)mem.size();
+        c3l::ArnoldiBatch bt{};
+        bt.nb = nb;
+        std::vector<c3l_eom_action> acts(nb);
+        std::vector<const c3l_complex*> xin(nb);
+        std::vector<c3l_complex*> out(nb);
+        std::vector<const int32_t*> stop(nb);
+        for (int i = 0; i < nb; ++i) {
+            c3l_arnoldi_channel& q = ch[mem[i]];
+            acts[i] = *q.sigma;
+            xin[i] = q.work;
+            out[i] = q.work + N;
+            stop[i] = q.counters + 3;
+            bt.V[i] = d2(q.V);
+            bt.w[i] = d2(q.work + N);
+            bt.xnext[i] = d2(q.work);
+            bt.c1[i] = d2(q.coeff);
+            bt.c2[i] = d2(q.coeff + (m_max + 1));
+            bt.hval[i] = reinterpret_cast<double*>(q.coeff + 2 * (m_max + 1));
+            bt.counters[i] = q.counters;
+            bt.Hc[i] = d2(q.Hcol);
+            bt.partial[i] = d2(q.partial);
+        }
         auto step = [&](cudaStream_t cs, int par) -> c3l_status {
-            const int* cur = q.counters + par;
-            int* next = q.counters + (1 - par);
-            c3l_status r = c3l_eom_sigma(q.sigma, xnext, wfix, reinterpret_cast<void*>(cs));
+            c3l_status r = c3l::eom_sigma_batch(acts.data(), nb, xin.data(), out.data(), stop.data(), cs);
             if (r) return r;
-            // pass 1 in FP32 (pass 2 below is FP64 and removes what it leaves)
-            if ((r = c3l::dot_rows_f32acc_dev_c(q.V, N, cur, wfix, N, rd, c1, cs))) return r;
-            if ((r = c3l::axpy_dev_c(q.V, N, cur, m_max, c1, c3l_complex{-1.0, 0.0}, wfix, N, cs))) return r;
-            if ((r = c3l::dot_rows_column_dev_c(q.V, N, cur, next, wfix, N, rd, q.partial, done, c1, c2, q.Hcol, ldc,
-                                                hval, cs)))
-                return r;
-            return c3l::arnoldi_scale_dev(q.V, N, cur, m_max, c2, hval, breakdown_tol, wfix, N, xnext, cs);
+            // pass 1 in FP32 (pass 2 is FP64 and removes what it leaves)
+            if ((r = c3l::arnoldi_dot1(bt, par, N, N, rd, cs))) return r;
+            if ((r = c3l::arnoldi_axpy1(bt, par, N, m_max, N, cs))) return r;
+            if ((r = c3l::arnoldi_dot2(bt, par, N, N, rd, ldc, cs))) return r;
+            return c3l::arnoldi_scale(bt, par, N, m_max, breakdown_tol, N, cs);
         };
         for (int par = 0; par < 2; ++par) {
-            if ((st = one[2 * c + par].capture(cap.s, [&](cudaStream_t cs) { return step(cs, par); }))) return st;
-            if ((st = interval[2 * c + par].capture(cap.s, [&](cudaStream_t cs) -> c3l_status {
+            if ((st = one[2 * g + par].capture(cap.s, [&](cudaStream_t cs) { return step(cs, par); }))) return st;
+            if ((st = interval[2 * g + par].capture(cap.s, [&](cudaStream_t cs) -> c3l_status {
                      for (int i = 0; i < check_interval; ++i) {
                          const c3l_status r = step(cs, (par + i) & 1);
                          if (r) return r;
@@ -638,19 +672,20 @@ c3l_status c3l_arnoldi(c3l_arnoldi_channel* ch, int32_t nch, int64_t N, const c3
     std::vector<int> active(nch, 1);
     for (int c = 0; c < nch; ++c) {
         c3l_arnoldi_channel& q = ch[c];
-        cudaStream_t s = as_stream(streams[c]);
+        cudaStream_t s = chan_stream(c);
+        void* sv = reinterpret_cast<void*>(s);
         q.m = 0;
         q.breakdown = 0;
         q.converged = 0;
         q.nchecks = 0;
         q.action_seconds = 0.0;
         q.launches = 0;
-        if ((st = c3l_multi_dot_c(q.b, N, 1, q.b, N, q.partial, q.coeff, streams[c]))) return st;
+        if ((st = c3l_multi_dot_c(q.b, N, 1, q.b, N, q.partial, q.coeff, sv))) return st;
         if ((st = d2h(q.host, q.coeff, sizeof(c3l_complex), s))) return st;
         q.beta = std::sqrt(std::max(q.host[0].re, 0.0));
         if (!(q.beta > 0.0) || !std::isfinite(q.beta)) return C3L_ERR_ARGUMENT;
-        if ((st = c3l_scale_c(N, c3l_complex{1.0 / q.beta, 0.0}, q.b, q.V, streams[c]))) return st;
-        if ((st = c3l_scale_c(N, c3l_complex{1.0 / q.beta, 0.0}, q.b, q.work, streams[c]))) return st;
+        if ((st = c3l_scale_c(N, c3l_complex{1.0 / q.beta, 0.0}, q.b, q.V, sv))) return st;
+        if ((st = c3l_scale_c(N, c3l_complex{1.0 / q.beta, 0.0}, q.b, q.work, sv))) return st;
         if (cudaMemsetAsync(q.counters, 0, 4 * sizeof(int32_t), s) != cudaSuccess) return C3L_ERR_LAUNCH;
         q.launches += (N > 8192 ? 2 : 1) + 2;
         q.hess.shifts = shifts;
@@ -683,11 +718,11 @@ c3l_status c3l_arnoldi(c3l_arnoldi_channel* ch, int32_t nch, int64_t N, const c3
             if (q.sink_conj && upto > done) {
                 c3l_complex* out = const_cast<c3l_complex*>(q.hess.sinkproj_conj) + done;
                 if ((r = c3l_multi_dot_c(q.V + (int64_t)done * N, N, upto - done, q.sink_conj, N, q.partial, out,
-                                         streams[c])))
+                                         reinterpret_cast<void*>(chan_stream(c)))))
                     return r;
                 q.launches += N > 8192 ? 2 : 1;
             }
-            if (cudaEventRecord(ready.ev[c], as_stream(streams[c])) != cudaSuccess ||
+            if (cudaEventRecord(ready.ev[c], chan_stream(c)) != cudaSuccess ||
                 cudaStreamWaitEvent(chk.s, ready.ev[c], 0) != cudaSuccess)
                 return C3L_ERR_LAUNCH;
             states.push_back(&q.hess);
@@ -718,17 +753,19 @@ c3l_status c3l_arnoldi(c3l_arnoldi_channel* ch, int32_t nch, int64_t N, const c3
         while (!due(t)) ++t;  // terminates: due(m_max) holds
         return t;
     };
-    // every active channel takes the steps launched .. upto
+    // every group with an active channel takes the steps launched .. upto
     int launched = 0;
     auto launch_to = [&](int upto) -> c3l_status {
-        for (int c = 0; c < nch; ++c) {
-            if (!active[c]) continue;
-            c3l_arnoldi_channel& q = ch[c];
-            cudaStream_t s = as_stream(streams[c]);
+        for (int gi = 0; gi < ng; ++gi) {
+            bool any = false;
+            for (int c : groups[gi]) any = any || active[c];
+            if (!any) continue;
+            c3l_arnoldi_channel& q = ch[groups[gi].front()];  // launches counted once per group
+            cudaStream_t s = chan_stream(groups[gi].front());
             int left = upto - launched;
             int at = launched;  // steps taken so far: the parity of the next step
             while (left >= check_interval) {
-                const StepGraph& g = interval[2 * c + (at & 1)];
+                const StepGraph& g = interval[2 * gi + (at & 1)];
                 c3l_status r = g.launch(s);
                 if (r) return r;
                 q.launches += g.nodes();
@@ -736,7 +773,7 @@ c3l_status c3l_arnoldi(c3l_arnoldi_channel* ch, int32_t nch, int64_t N, const c3
                 at += check_interval;
             }
             for (; left > 0; --left, ++at) {
-                const StepGraph& g = one[2 * c + (at & 1)];
+                const StepGraph& g = one[2 * gi + (at & 1)];
                 c3l_status r = g.launch(s);
                 if (r) return r;
                 q.launches += g.nodes();
@@ -777,10 +814,12 @@ c3l_status c3l_arnoldi(c3l_arnoldi_channel* ch, int32_t nch, int64_t N, const c3
                 settle(q, first_break, worst);
                 active[c] = 0;
                 remaining -= 1;
+                // later steps of the group skip this channel
+                if (cudaMemsetAsync(q.counters + 3, 1, 1, chan_stream(c)) != cudaSuccess) return C3L_ERR_LAUNCH;
             }
         }
         if (bad) {  // non-finite Arnoldi step: let the steps in flight finish first
-            for (int c = 0; c < nch; ++c) cudaStreamSynchronize(as_stream(streams[c]));
+            for (int c = 0; c < nch; ++c) cudaStreamSynchronize(chan_stream(c));
             return C3L_ERR_ARGUMENT;
         }
     }
@@ -788,7 +827,7 @@ c3l_status c3l_arnoldi(c3l_arnoldi_channel* ch, int32_t nch, int64_t N, const c3
     for (int c = 0; c < nch; ++c) {
         c3l_arnoldi_channel& q = ch[c];
         if (!q.H || q.m <= 0) continue;
-        cudaStream_t s = as_stream(streams[c]);
+        cudaStream_t s = chan_stream(c);
         const int m = q.m;
         std::vector<c3l_complex> cols((size_t)m * (m + 1));
         if (cudaMemcpy2DAsync(cols.data(), (m + 1) * sizeof(c3l_complex), q.Hcol, ldc * sizeof(c3l_complex),

@@ -21,9 +21,11 @@
 // Instances of one output block are staged through shared memory and split
 // over four thread groups.
 #include <cuda_runtime.h>
+#include <cstring>
 #include <stdint.h>
 
 #include "c3l_gb300.h"
+#include "c3l_internal.h"
 
 namespace {
 
@@ -72,6 +74,24 @@ inline c3l_status launch_status() {
     return cudaGetLastError() == cudaSuccess ? C3L_OK : C3L_ERR_LAUNCH;
 }
 
+// Entries of a batched launch (blockIdx.y = entry): the same program over
+// separate workspaces, inputs and outputs; an entry whose stop flag is set
+// does nothing.  Unbatched launches use entry 0 only.
+template <typename C>
+struct Batch {
+    C* ws[C3L_MAX_BATCH];
+    const double2* in[C3L_MAX_BATCH];   // scatter source and output-stage input
+    double2* out[C3L_MAX_BATCH];        // complex output-stage destination
+    const int32_t* stop[C3L_MAX_BATCH];
+    int nb;
+};
+
+template <typename C>
+__device__ __forceinline__ bool batch_stopped(const Batch<C>& bt) {
+    const int32_t* f = bt.stop[blockIdx.y];
+    return f && *f;
+}
+
 __global__ void k_tilde_unpack(int64_t dim, const double* __restrict__ x, const int64_t* __restrict__ ia,
                                const int64_t* __restrict__ ib, const double2* __restrict__ ca,
                                const double2* __restrict__ cb, double2* __restrict__ t) {
@@ -86,7 +106,10 @@ __global__ void k_tilde_unpack(int64_t dim, const double* __restrict__ x, const 
 
 template <typename C>
 __global__ void k_scatter(int64_t count, const int64_t* __restrict__ dst, const int64_t* __restrict__ pos,
-                          const double* __restrict__ sign, const double2* __restrict__ vec, C* __restrict__ ws) {
+                          const double* __restrict__ sign, Batch<C> bt) {
+    if (batch_stopped(bt)) return;
+    const double2* __restrict__ vec = bt.in[blockIdx.y];
+    C* __restrict__ ws = bt.ws[blockIdx.y];
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < count; e += (int64_t)gridDim.x * blockDim.x) {
         const double s = sign[e];
         double2 v = make_double2(0.0, 0.0);
@@ -145,7 +168,9 @@ __device__ __forceinline__ void contract_entry(const c3l_contract_task& task, in
 
 template <typename C>
 __global__ void __launch_bounds__(kThreads) k_contract(c3l_contract_level lv, int n, const C* __restrict__ vectors,
-                                                        C* __restrict__ ws) {
+                                                        Batch<C> bt) {
+    if (batch_stopped(bt)) return;
+    C* __restrict__ ws = bt.ws[blockIdx.y];
     const c3l_tile tile = lv.tiles[blockIdx.x];
     if ((int)threadIdx.x >= tile.count) return;
     int64_t pw[6];
@@ -157,7 +182,8 @@ __global__ void __launch_bounds__(kThreads) k_contract(c3l_contract_level lv, in
 // depending on the previous one) as one launch of one thread-block cluster:
 // the cluster's CTAs stride over a level's tiles, then meet at a hardware
 // cluster barrier (release/acquire) before the next level.  Every CTA reaches
-// every barrier.
+// every barrier.  Batch entries are separate clusters (blockIdx.y); a stopped
+// entry's CTAs all return before the first barrier.
 constexpr int kLevelClusterMax = 16;  // non-portable cluster size where the device allows it
 
 struct LevelPack {
@@ -168,7 +194,9 @@ struct LevelPack {
 
 template <typename C>
 __global__ void __launch_bounds__(kThreads) k_contract_cluster(LevelPack pack, int n, const C* __restrict__ vectors,
-                                                                C* __restrict__ ws) {
+                                                                Batch<C> bt) {
+    if (batch_stopped(bt)) return;
+    C* __restrict__ ws = bt.ws[blockIdx.y];
     int64_t pw[6];
     powers(n, pw);
     for (int l = pack.first; l < pack.first + pack.count; ++l) {
@@ -184,14 +212,14 @@ __global__ void __launch_bounds__(kThreads) k_contract_cluster(LevelPack pack, i
 
 enum WedgeMode { kPadded = 0, kStatic = 1, kEom = 2, kSource = 3 };
 
+// Output-stage constants; the per-entry input (src) and complex destination
+// come from the batch.
 struct Epilogue {
     const double2* lam;
-    const double2* src;
     const int64_t* col;
     const int64_t* pair;
     const double2* scale;
     double* xout;
-    double2* cout;
     double2 cscale;
     const double* m4;  // static outputs: optional 2x2 preconditioner block per element
 };
@@ -205,8 +233,10 @@ __device__ __forceinline__ double2 dmul(double2 a, double2 b) {
 // i % kWG) and the groups' partial sums are added in shared memory.  Narrow
 // tiles (small kWE) put more blocks on the GPU when a stage has few outputs.
 template <int MODE, typename C, int kWE>
-__global__ void __launch_bounds__(kThreads) k_wedge(c3l_wedge_stage st, int n, C* ws, Epilogue ep) {
+__global__ void __launch_bounds__(kThreads) k_wedge(c3l_wedge_stage st, int n, Batch<C> bt, Epilogue ep) {
     constexpr int kWG = kThreads / kWE;
+    if (batch_stopped(bt)) return;
+    C* __restrict__ ws = bt.ws[blockIdx.y];
     __shared__ c3l_instance sinst[kInstChunk];
     __shared__ C red[kWG][kWE];
     const c3l_tile tile = st.tiles[blockIdx.x];
@@ -268,7 +298,7 @@ __global__ void __launch_bounds__(kThreads) k_wedge(c3l_wedge_stage st, int n, C
     } else if (MODE == kStatic) {
         const int64_t mu = st.elements[e];
         const double2 a = to_d2(acc);
-        const double2 lam = ep.lam[e], src = ep.src[mu];
+        const double2 lam = ep.lam[e], src = bt.in[blockIdx.y][mu];
         const double2 s = make_double2(fma(lam.x, src.x, fma(-lam.y, src.y, a.x)), fma(lam.x, src.y, fma(lam.y, src.x, a.y)));
         const double2 r = make_double2(s.y, -s.x);  // -i * s
         const double2 v = dmul(r, ep.scale[e]);
@@ -288,23 +318,34 @@ __global__ void __launch_bounds__(kThreads) k_wedge(c3l_wedge_stage st, int n, C
     } else if (MODE == kEom) {
         const int64_t mu = st.elements[e];
         const double2 a = to_d2(acc);
-        const double2 lam = ep.lam[e], src = ep.src[mu];
-        ep.cout[mu] = make_double2(fma(lam.x, src.x, fma(-lam.y, src.y, a.x)), fma(lam.x, src.y, fma(lam.y, src.x, a.y)));
+        const double2 lam = ep.lam[e], src = bt.in[blockIdx.y][mu];
+        bt.out[blockIdx.y][mu] =
+            make_double2(fma(lam.x, src.x, fma(-lam.y, src.y, a.x)), fma(lam.x, src.y, fma(lam.y, src.x, a.y)));
     } else {
         const int64_t mu = st.elements[e];
-        ep.cout[mu] = dmul(ep.cscale, to_d2(acc));
+        bt.out[blockIdx.y][mu] = dmul(ep.cscale, to_d2(acc));
     }
 }
 
+template <typename C>
+Batch<C> single(C* ws, const double2* in = nullptr, double2* out = nullptr) {
+    Batch<C> bt{};
+    bt.ws[0] = ws;
+    bt.in[0] = in;
+    bt.out[0] = out;
+    bt.nb = 1;
+    return bt;
+}
+
 template <int MODE, typename C>
-c3l_status launch_wedge(const c3l_wedge_stage& st, int n, C* ws, const Epilogue& ep, cudaStream_t s) {
-    const unsigned grid = (unsigned)st.ntiles;
+c3l_status launch_wedge(const c3l_wedge_stage& st, int n, const Batch<C>& bt, const Epilogue& ep, cudaStream_t s) {
+    const dim3 grid((unsigned)st.ntiles, (unsigned)bt.nb);
     switch (st.width) {
-        case 8: k_wedge<MODE, C, 8><<<grid, kThreads, 0, s>>>(st, n, ws, ep); break;
-        case 16: k_wedge<MODE, C, 16><<<grid, kThreads, 0, s>>>(st, n, ws, ep); break;
-        case 32: k_wedge<MODE, C, 32><<<grid, kThreads, 0, s>>>(st, n, ws, ep); break;
+        case 8: k_wedge<MODE, C, 8><<<grid, kThreads, 0, s>>>(st, n, bt, ep); break;
+        case 16: k_wedge<MODE, C, 16><<<grid, kThreads, 0, s>>>(st, n, bt, ep); break;
+        case 32: k_wedge<MODE, C, 32><<<grid, kThreads, 0, s>>>(st, n, bt, ep); break;
         case 0:
-        case 64: k_wedge<MODE, C, 64><<<grid, kThreads, 0, s>>>(st, n, ws, ep); break;
+        case 64: k_wedge<MODE, C, 64><<<grid, kThreads, 0, s>>>(st, n, bt, ep); break;
         default: return C3L_ERR_ARGUMENT;
     }
     return launch_status();
@@ -346,17 +387,17 @@ int level_cluster_size() {
 }
 
 template <typename C>
-c3l_status run_levels(const c3l_action* a, cudaStream_t s) {
+c3l_status run_levels(const c3l_action* a, const Batch<C>& bt, cudaStream_t s) {
     // levels [tail, nlevels) each fit one round of the cluster: one cluster launch runs them
     const int cluster = level_cluster_size<C>();
     int tail = a->nlevels;
     while (tail > 0 && a->levels[tail - 1].ntiles <= cluster) --tail;
     if (a->nlevels - tail < 2) tail = a->nlevels;  // a single small level gains nothing
+    const C* vectors = reinterpret_cast<const C*>(a->vectors);
     for (int l = 0; l < tail; ++l) {
         if (a->levels[l].ntiles <= 0) continue;
-        k_contract<C><<<(unsigned)a->levels[l].ntiles, kThreads, 0, s>>>(a->levels[l], a->n,
-                                                                        reinterpret_cast<const C*>(a->vectors),
-                                                                        reinterpret_cast<C*>(a->ws));
+        k_contract<C><<<dim3((unsigned)a->levels[l].ntiles, (unsigned)bt.nb), kThreads, 0, s>>>(a->levels[l], a->n,
+                                                                                              vectors, bt);
     }
     if (tail < a->nlevels) {
         LevelPack pack{};
@@ -364,7 +405,7 @@ c3l_status run_levels(const c3l_action* a, cudaStream_t s) {
         pack.first = tail;
         pack.count = a->nlevels - tail;
         cudaLaunchConfig_t cfg{};
-        cfg.gridDim = dim3(cluster, 1, 1);
+        cfg.gridDim = dim3(cluster, (unsigned)bt.nb, 1);
         cfg.blockDim = dim3(kThreads, 1, 1);
         cfg.dynamicSmemBytes = 0;
         cfg.stream = s;
@@ -375,30 +416,28 @@ c3l_status run_levels(const c3l_action* a, cudaStream_t s) {
         attr[0].val.clusterDim.z = 1;
         cfg.attrs = attr;
         cfg.numAttrs = 1;
-        if (cudaLaunchKernelEx(&cfg, k_contract_cluster<C>, pack, a->n, reinterpret_cast<const C*>(a->vectors),
-                               reinterpret_cast<C*>(a->ws)) != cudaSuccess)
+        if (cudaLaunchKernelEx(&cfg, k_contract_cluster<C>, pack, a->n, vectors, bt) != cudaSuccess)
             return C3L_ERR_LAUNCH;
     }
     return launch_status();
 }
 
 template <typename C>
-c3l_status run_padded(const c3l_action* a, cudaStream_t s) {
+c3l_status run_padded(const c3l_action* a, const Batch<C>& bt, cudaStream_t s) {
     Epilogue ep{};
     for (int p = 0; p < a->npadded; ++p) {
         if (a->padded[p].ntiles <= 0) continue;
-        const c3l_status st = launch_wedge<kPadded, C>(a->padded[p], a->n, reinterpret_cast<C*>(a->ws), ep, s);
+        const c3l_status st = launch_wedge<kPadded, C>(a->padded[p], a->n, bt, ep, s);
         if (st) return st;
     }
     return C3L_OK;
 }
 
 template <typename C>
-c3l_status scatter(const c3l_action* a, const c3l_complex* vec, cudaStream_t s) {
+c3l_status scatter(const c3l_action* a, const Batch<C>& bt, cudaStream_t s) {
     if (a->scatter_count <= 0) return C3L_OK;
-    k_scatter<C><<<grid_for(a->scatter_count), kThreads, 0, s>>>(a->scatter_count, a->scatter_dst, a->scatter_pos,
-                                                               a->scatter_sign, reinterpret_cast<const double2*>(vec),
-                                                               reinterpret_cast<C*>(a->ws));
+    k_scatter<C><<<dim3(grid_for(a->scatter_count), (unsigned)bt.nb), kThreads, 0, s>>>(
+        a->scatter_count, a->scatter_dst, a->scatter_pos, a->scatter_sign, bt);
     return launch_status();
 }
 
@@ -407,12 +446,14 @@ bool valid_action(const c3l_action* a) {
            a->npadded >= 0 && a->npadded <= C3L_MAX_STAGES;
 }
 
+// The batch's input vectors through the scatter, the atom levels and the
+// padded stages of a program.
 template <typename C>
-c3l_status action_prepare(const c3l_action* action, const c3l_complex* t, cudaStream_t s) {
-    c3l_status st = scatter<C>(action, t, s);
+c3l_status action_prepare(const c3l_action* action, const Batch<C>& bt, cudaStream_t s) {
+    c3l_status st = scatter<C>(action, bt, s);
     if (st) return st;
-    if ((st = run_levels<C>(action, s))) return st;
-    return run_padded<C>(action, s);
+    if ((st = run_levels<C>(action, bt, s))) return st;
+    return run_padded<C>(action, bt, s);
 }
 
 template <typename C>
@@ -424,34 +465,63 @@ c3l_status static_apply(const c3l_static_action* sa, const double* x, double* xo
     c3l_status st = c3l_tilde_unpack(sa->num_amplitudes, x, sa->tilde_ia, sa->tilde_ib, sa->tilde_ca, sa->tilde_cb,
                                      sa->canon, stream);
     if (st) return st;
-    if ((st = action_prepare<C>(&sa->action, sa->canon, s))) return st;
+    const Batch<C> bt = single<C>(reinterpret_cast<C*>(sa->action.ws), reinterpret_cast<const double2*>(sa->canon));
+    if ((st = action_prepare<C>(&sa->action, bt, s))) return st;
     if (sa->action.out.ntiles <= 0) return C3L_OK;
     Epilogue ep{};
     ep.lam = reinterpret_cast<const double2*>(sa->lam);
-    ep.src = reinterpret_cast<const double2*>(sa->canon);
     ep.col = sa->col;
     ep.pair = sa->pair;
     ep.scale = reinterpret_cast<const double2*>(sa->scale);
     ep.xout = xout;
     ep.m4 = sa->pc_m4;
-    return launch_wedge<kStatic, C>(sa->action.out, sa->action.n, reinterpret_cast<C*>(sa->action.ws), ep, s);
+    return launch_wedge<kStatic, C>(sa->action.out, sa->action.n, bt, ep, s);
+}
+
+// Two actions run the same program when they differ only in the workspace.
+bool same_program(const c3l_action& a, const c3l_action& b) {
+    c3l_action x = a, y = b;
+    x.ws = nullptr;
+    y.ws = nullptr;
+    return std::memcmp(&x, &y, sizeof(c3l_action)) == 0;
 }
 
 template <typename C>
-c3l_status eom_sigma(const c3l_eom_action* ea, const c3l_complex* xin, c3l_complex* out, void* stream) {
-    if (!ea || !xin || !out || !valid_action(&ea->action) || !ea->lam) return C3L_ERR_ARGUMENT;
-    cudaStream_t s = as_stream(stream);
-    c3l_status st = action_prepare<C>(&ea->action, xin, s);
+c3l_status eom_sigma(const c3l_eom_action* ea, int nb, const c3l_complex* const* xin, c3l_complex* const* out,
+                     const int32_t* const* stop, cudaStream_t s) {
+    if (!ea || nb < 1 || nb > C3L_MAX_BATCH || !xin || !out) return C3L_ERR_ARGUMENT;
+    Batch<C> bt{};
+    bt.nb = nb;
+    for (int b = 0; b < nb; ++b) {
+        if (!xin[b] || !out[b] || !valid_action(&ea[b].action) || !ea[b].lam) return C3L_ERR_ARGUMENT;
+        if (b > 0 && (!same_program(ea[b].action, ea[0].action) || ea[b].lam != ea[0].lam)) return C3L_ERR_ARGUMENT;
+        bt.ws[b] = reinterpret_cast<C*>(ea[b].action.ws);
+        bt.in[b] = reinterpret_cast<const double2*>(xin[b]);
+        bt.out[b] = reinterpret_cast<double2*>(out[b]);
+        bt.stop[b] = stop ? stop[b] : nullptr;
+    }
+    c3l_status st = action_prepare<C>(&ea[0].action, bt, s);
     if (st) return st;
-    if (ea->action.out.ntiles <= 0) return C3L_OK;
+    if (ea[0].action.out.ntiles <= 0) return C3L_OK;
     Epilogue ep{};
-    ep.lam = reinterpret_cast<const double2*>(ea->lam);
-    ep.src = reinterpret_cast<const double2*>(xin);
-    ep.cout = reinterpret_cast<double2*>(out);
-    return launch_wedge<kEom, C>(ea->action.out, ea->action.n, reinterpret_cast<C*>(ea->action.ws), ep, s);
+    ep.lam = reinterpret_cast<const double2*>(ea[0].lam);
+    return launch_wedge<kEom, C>(ea[0].action.out, ea[0].action.n, bt, ep, s);
 }
 
 }  // namespace
+
+namespace c3l {
+
+c3l_status eom_sigma_batch(const c3l_eom_action* actions, int nb, const c3l_complex* const* xin,
+                           c3l_complex* const* out, const int32_t* const* stop, cudaStream_t s) {
+    return eom_sigma<double2>(actions, nb, xin, out, stop, s);
+}
+
+bool same_sigma_program(const c3l_eom_action& a, const c3l_eom_action& b) {
+    return same_program(a.action, b.action) && a.lam == b.lam;
+}
+
+}  // namespace c3l
 
 extern "C" {
 
@@ -470,7 +540,7 @@ c3l_status c3l_scatter_padded(int64_t count, const int64_t* dst, const int64_t* 
     if (count < 0 || (count > 0 && (!dst || !pos || !sign || !vec || !ws))) return C3L_ERR_ARGUMENT;
     if (count == 0) return C3L_OK;
     k_scatter<double2><<<grid_for(count), kThreads, 0, as_stream(stream)>>>(
-        count, dst, pos, sign, reinterpret_cast<const double2*>(vec), reinterpret_cast<double2*>(ws));
+        count, dst, pos, sign, single<double2>(reinterpret_cast<double2*>(ws), reinterpret_cast<const double2*>(vec)));
     return launch_status();
 }
 
@@ -487,7 +557,7 @@ c3l_status c3l_contract(const c3l_contract_level* level, int32_t n, const c3l_co
     if (!level || !vectors || !ws || n <= 0 || n > 255) return C3L_ERR_ARGUMENT;
     if (level->ntiles <= 0) return C3L_OK;
     k_contract<double2><<<(unsigned)level->ntiles, kThreads, 0, as_stream(stream)>>>(
-        *level, n, reinterpret_cast<const double2*>(vectors), reinterpret_cast<double2*>(ws));
+        *level, n, reinterpret_cast<const double2*>(vectors), single<double2>(reinterpret_cast<double2*>(ws)));
     return launch_status();
 }
 
@@ -495,7 +565,8 @@ c3l_status c3l_wedge_padded(const c3l_wedge_stage* stage, int32_t n, c3l_complex
     if (!stage || !ws || n <= 0 || n > 255) return C3L_ERR_ARGUMENT;
     if (stage->ntiles <= 0) return C3L_OK;
     Epilogue ep{};
-    return launch_wedge<kPadded, double2>(*stage, n, reinterpret_cast<double2*>(ws), ep, as_stream(stream));
+    return launch_wedge<kPadded, double2>(*stage, n, single<double2>(reinterpret_cast<double2*>(ws)), ep,
+                                          as_stream(stream));
 }
 
 c3l_status c3l_wedge_static_out(const c3l_wedge_stage* stage, int32_t n, const c3l_complex* ws, const c3l_complex* lam,
@@ -505,13 +576,14 @@ c3l_status c3l_wedge_static_out(const c3l_wedge_stage* stage, int32_t n, const c
     if (stage->ntiles <= 0) return C3L_OK;
     Epilogue ep{};
     ep.lam = reinterpret_cast<const double2*>(lam);
-    ep.src = reinterpret_cast<const double2*>(src);
     ep.col = col;
     ep.pair = pair;
     ep.scale = reinterpret_cast<const double2*>(scale);
     ep.xout = xout;
-    return launch_wedge<kStatic, double2>(*stage, n, const_cast<double2*>(reinterpret_cast<const double2*>(ws)), ep,
-                                          as_stream(stream));
+    return launch_wedge<kStatic, double2>(
+        *stage, n,
+        single<double2>(const_cast<double2*>(reinterpret_cast<const double2*>(ws)), reinterpret_cast<const double2*>(src)),
+        ep, as_stream(stream));
 }
 
 c3l_status c3l_wedge_static_out_f32(const c3l_wedge_stage* stage, int32_t n, const c3l_complex32* ws,
@@ -521,13 +593,14 @@ c3l_status c3l_wedge_static_out_f32(const c3l_wedge_stage* stage, int32_t n, con
     if (stage->ntiles <= 0) return C3L_OK;
     Epilogue ep{};
     ep.lam = reinterpret_cast<const double2*>(lam);
-    ep.src = reinterpret_cast<const double2*>(src);
     ep.col = col;
     ep.pair = pair;
     ep.scale = reinterpret_cast<const double2*>(scale);
     ep.xout = xout;
-    return launch_wedge<kStatic, float2>(*stage, n, const_cast<float2*>(reinterpret_cast<const float2*>(ws)), ep,
-                                         as_stream(stream));
+    return launch_wedge<kStatic, float2>(
+        *stage, n,
+        single<float2>(const_cast<float2*>(reinterpret_cast<const float2*>(ws)), reinterpret_cast<const double2*>(src)),
+        ep, as_stream(stream));
 }
 
 c3l_status c3l_wedge_eom_out(const c3l_wedge_stage* stage, int32_t n, const c3l_complex* ws, const c3l_complex* lam,
@@ -536,10 +609,11 @@ c3l_status c3l_wedge_eom_out(const c3l_wedge_stage* stage, int32_t n, const c3l_
     if (stage->ntiles <= 0) return C3L_OK;
     Epilogue ep{};
     ep.lam = reinterpret_cast<const double2*>(lam);
-    ep.src = reinterpret_cast<const double2*>(xin);
-    ep.cout = reinterpret_cast<double2*>(out);
-    return launch_wedge<kEom, double2>(*stage, n, const_cast<double2*>(reinterpret_cast<const double2*>(ws)), ep,
-                                       as_stream(stream));
+    return launch_wedge<kEom, double2>(*stage, n,
+                                       single<double2>(const_cast<double2*>(reinterpret_cast<const double2*>(ws)),
+                                                       reinterpret_cast<const double2*>(xin),
+                                                       reinterpret_cast<double2*>(out)),
+                                       ep, as_stream(stream));
 }
 
 c3l_status c3l_wedge_source_out(const c3l_wedge_stage* stage, int32_t n, const c3l_complex* ws, c3l_complex scale,
@@ -548,19 +622,25 @@ c3l_status c3l_wedge_source_out(const c3l_wedge_stage* stage, int32_t n, const c
     if (stage->ntiles <= 0) return C3L_OK;
     Epilogue ep{};
     ep.cscale = make_double2(scale.re, scale.im);
-    ep.cout = reinterpret_cast<double2*>(out);
-    return launch_wedge<kSource, double2>(*stage, n, const_cast<double2*>(reinterpret_cast<const double2*>(ws)), ep,
-                                          as_stream(stream));
+    return launch_wedge<kSource, double2>(
+        *stage, n,
+        single<double2>(const_cast<double2*>(reinterpret_cast<const double2*>(ws)), nullptr,
+                        reinterpret_cast<double2*>(out)),
+        ep, as_stream(stream));
 }
 
 c3l_status c3l_action_prepare(const c3l_action* action, const c3l_complex* t, void* stream) {
     if (!valid_action(action) || !t) return C3L_ERR_ARGUMENT;
-    return action_prepare<double2>(action, t, as_stream(stream));
+    return action_prepare<double2>(
+        action, single<double2>(reinterpret_cast<double2*>(action->ws), reinterpret_cast<const double2*>(t)),
+        as_stream(stream));
 }
 
 c3l_status c3l_action_prepare_f32(const c3l_action* action, const c3l_complex* t, void* stream) {
     if (!valid_action(action) || !t) return C3L_ERR_ARGUMENT;
-    return action_prepare<float2>(action, t, as_stream(stream));
+    return action_prepare<float2>(
+        action, single<float2>(reinterpret_cast<float2*>(action->ws), reinterpret_cast<const double2*>(t)),
+        as_stream(stream));
 }
 
 c3l_status c3l_static_apply(const c3l_static_action* sa, const double* x, double* xout, void* stream) {
@@ -572,11 +652,16 @@ c3l_status c3l_static_apply_f32(const c3l_static_action* sa, const double* x, do
 }
 
 c3l_status c3l_eom_sigma(const c3l_eom_action* ea, const c3l_complex* xin, c3l_complex* out, void* stream) {
-    return eom_sigma<double2>(ea, xin, out, stream);
+    return eom_sigma<double2>(ea, 1, &xin, &out, nullptr, as_stream(stream));
 }
 
 c3l_status c3l_eom_sigma_f32(const c3l_eom_action* ea, const c3l_complex* xin, c3l_complex* out, void* stream) {
-    return eom_sigma<float2>(ea, xin, out, stream);
+    return eom_sigma<float2>(ea, 1, &xin, &out, nullptr, as_stream(stream));
+}
+
+c3l_status c3l_eom_sigma_batch(const c3l_eom_action* actions, int32_t nb, const c3l_complex* const* xin,
+                               c3l_complex* const* out, void* stream) {
+    return eom_sigma<double2>(actions, nb, xin, out, nullptr, as_stream(stream));
 }
 
 const char* c3l_version(void) { return "c3l_gb300 0.2.0 (sm_103a, fp64/fp32 complex programs)"; }

@@ -102,6 +102,7 @@ class ArnoldiChannel(C.Structure):
 EXPORTS = (
     "c3l_tilde_unpack", "c3l_scatter_padded", "c3l_contract", "c3l_wedge_padded", "c3l_wedge_static_out",
     "c3l_wedge_eom_out", "c3l_wedge_source_out", "c3l_action_prepare", "c3l_static_apply", "c3l_eom_sigma",
+    "c3l_eom_sigma_batch",
     "c3l_multi_dot_scratch", "c3l_multi_dot_c", "c3l_multi_dot_r", "c3l_multi_axpy_c", "c3l_multi_axpy_r",
     "c3l_scale_c", "c3l_scale_r", "c3l_precondition", "c3l_hessenberg_shifted", "c3l_hessenberg_coordinates",
     "c3l_hessenberg_coordinates_noalloc", "c3l_gmres", "c3l_gmres_scratch", "c3l_gmres_release", "c3l_gmres_shifted", "c3l_shifted_combine", "c3l_arnoldi", "c3l_hessenberg_advance",
@@ -124,6 +125,7 @@ def _declare(lib) -> None:
         "c3l_action_prepare": [P, P, P],
         "c3l_static_apply": [P, P, P, P],
         "c3l_eom_sigma": [P, P, P, P],
+        "c3l_eom_sigma_batch": [P, I32, P, P, P],
         "c3l_multi_dot_c": [P, I64, I32, P, I64, P, P, P],
         "c3l_multi_dot_r": [P, I64, I32, P, I64, P, P, P],
         "c3l_multi_axpy_c": [P, I64, I32, P, Complex, P, I64, P],
@@ -217,6 +219,7 @@ class Uploader:
     def __init__(self, device):
         self.device = device
         self.keep: list = []
+        self._tables: dict = {}  # id(array) -> (array, device copy): one upload per table
 
     def raw(self, arr: np.ndarray) -> torch.Tensor:
         a = np.ascontiguousarray(arr)
@@ -233,11 +236,18 @@ class Uploader:
         return t
 
     def ptr(self, arr) -> int:
+        """Device address of a (read-only) program table, uploaded once: actions
+        built from the same tables share them, which batched launches require."""
         if arr is None:
             return 0
         if len(arr) == 0:
             return 0
-        return self.raw(arr).data_ptr()
+        hit = self._tables.get(id(arr))
+        if hit is not None and hit[0] is arr:
+            return hit[1].data_ptr()
+        t = self.raw(arr)
+        self._tables[id(arr)] = (arr, t)
+        return t.data_ptr()
 
 
 def wedge_stage(up: Uploader, stage) -> WedgeStage:

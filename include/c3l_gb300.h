@@ -145,6 +145,7 @@ c3l_status c3l_wedge_source_out(const c3l_wedge_stage* stage, int32_t n, const c
 
 #define C3L_MAX_LEVELS 8
 #define C3L_MAX_STAGES 4
+#define C3L_MAX_BATCH 8
 
 /* One operation = unpack/scatter, atom levels, padded stages, output stage. */
 typedef struct {
@@ -197,6 +198,12 @@ typedef struct {
 } c3l_eom_action;
 
 c3l_status c3l_eom_sigma(const c3l_eom_action* action, const c3l_complex* xin, c3l_complex* out, void* stream);
+
+/* The sigma action of one operator on nb <= C3L_MAX_BATCH vectors in one
+ * launch per kernel: actions[b] differ only in their workspace (the same
+ * program tables and lam), xin[b] -> out[b] (host arrays of device pointers). */
+c3l_status c3l_eom_sigma_batch(const c3l_eom_action* actions, int32_t nb, const c3l_complex* const* xin,
+                               c3l_complex* const* out, void* stream);
 
 /* Single-precision variants: the action's `vectors` and `ws` point to
  * complex FP32 copies (c3l_complex32) of the factor-vector table and of the

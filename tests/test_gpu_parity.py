@@ -447,3 +447,35 @@ def test_newton_correction_gmres_fp32_operator(basis_f32, problems, cuda_device)
     ops.jvp(s, js)  # FP64 operator
     defect = (js + r).cpu().numpy()
     assert np.linalg.norm(defect) <= 2 * rtol * np.linalg.norm(r.cpu().numpy())
+
+
+def test_batched_sigma_matches_single_calls(problems, cuda_device):
+    """c3l_eom_sigma_batch over three channel workspaces gives, bit for bit,
+    the single-vector c3l_eom_sigma of each vector (same kernels, one launch
+    per kernel for the batch)."""
+    import c3lindblad_gb300 as c3
+    from c3lindblad_gb300 import runtime as rt
+
+    spec, g, p = problems("siam10")
+    ep = c3.ComponentEOMProblem.compile(c3.eom_ccsd_problem(p), p, 1)
+    ctx = c3.component_eom_context(ep, g["solution_amplitudes"])
+    ops = ctx.ops
+    ops.ensure_channels(3)
+    N = ops.N
+    rng = np.random.default_rng(3)
+    xs = [torch.from_numpy(rng.normal(size=N) + 1j * rng.normal(size=N)).to(cuda_device) for _ in range(3)]
+    outs = [torch.empty_like(x) for x in xs]
+    acts = (rt.EomAction * 3)(*[ops.sigma_actions[i] for i in range(3)])
+    xin = (C.c_void_p * 3)(*[x.data_ptr() for x in xs])
+    xo = (C.c_void_p * 3)(*[o.data_ptr() for o in outs])
+    lib = rt.lib()
+    rt.check(lib.c3l_eom_sigma_batch(acts, 3, xin, xo, rt.stream_ptr(cuda_device)), "sigma batch")
+    for x, o in zip(xs, outs):
+        want = torch.empty_like(x)
+        ops.sigma(x, want)
+        assert torch.equal(o, want)
+    # workspaces of different programs are refused
+    other = c3.ComponentEOMProblem.compile(c3.eom_ccsd_problem(p), p, -1)
+    octx = c3.component_eom_context(other, g["solution_amplitudes"])
+    mixed = (rt.EomAction * 2)(ops.sigma_actions[0], octx.ops.sigma_action)
+    assert lib.c3l_eom_sigma_batch(mixed, 2, xin, xo, rt.stream_ptr(cuda_device)) == 1
