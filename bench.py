@@ -271,7 +271,8 @@ def run_gpu(args) -> dict:
                    "green_rel_err_mixed_vs_fp64": mixed_vs_fp64,
                    "green_rel_err_unbatched_vs_batched_fp64": unbatched_vs_fp64,
                    "batched_omega": "one CGS2 Arnoldi basis per channel for all omega (graph-replayed steps, "
-                                    "incremental FP64 shifted solves); addition/removal channels on two streams",
+                                    "incremental FP64 shifted solves); addition and removal channels stepped together, "
+                                    "one launch per kernel for both",
                    "warm_start": "off: the learned guess lowers the starting residual but not the Newton work "
                                  "on this family",
                    "l2": "flushed between steps (256 MB write)",

@@ -92,15 +92,45 @@ __device__ __forceinline__ bool batch_stopped(const Batch<C>& bt) {
     return f && *f;
 }
 
+__device__ __forceinline__ double2 tilde_value(const double* __restrict__ x, const int64_t* __restrict__ ia,
+                                               const int64_t* __restrict__ ib, const double2* __restrict__ ca,
+                                               const double2* __restrict__ cb, int64_t i) {
+    const double xa = x[ia[i]];
+    const double xb = x[ib[i]];
+    const double2 a = ca[i];
+    const double2 b = cb[i];
+    return make_double2(fma(a.x, xa, b.x * xb), fma(a.y, xa, b.y * xb));
+}
+
 __global__ void k_tilde_unpack(int64_t dim, const double* __restrict__ x, const int64_t* __restrict__ ia,
                                const int64_t* __restrict__ ib, const double2* __restrict__ ca,
                                const double2* __restrict__ cb, double2* __restrict__ t) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < dim; i += (int64_t)gridDim.x * blockDim.x) {
-        const double xa = x[ia[i]];
-        const double xb = x[ib[i]];
-        const double2 a = ca[i];
-        const double2 b = cb[i];
-        t[i] = make_double2(fma(a.x, xa, b.x * xb), fma(a.y, xa, b.y * xb));
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < dim; i += (int64_t)gridDim.x * blockDim.x)
+        t[i] = tilde_value(x, ia, ib, ca, cb, i);
+}
+
+// The tilde unpack and the scatter into padded blocks in one launch: t[i]
+// for the canonical vector (read again by the output stage) and, per scatter
+// entry, ws[dst[e]] = sign[e] t[pos[e]] computed from x directly (the same
+// arithmetic as k_tilde_unpack followed by k_scatter).
+template <typename C>
+__global__ void k_unpack_scatter(int64_t dim, const double* __restrict__ x, const int64_t* __restrict__ ia,
+                                 const int64_t* __restrict__ ib, const double2* __restrict__ ca,
+                                 const double2* __restrict__ cb, double2* __restrict__ t, int64_t count,
+                                 const int64_t* __restrict__ dst, const int64_t* __restrict__ pos,
+                                 const double* __restrict__ sign, C* __restrict__ ws) {
+    const int64_t n = dim > count ? dim : count;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        if (i < dim) t[i] = tilde_value(x, ia, ib, ca, cb, i);
+        if (i < count) {
+            const double sg = sign[i];
+            double2 v = make_double2(0.0, 0.0);
+            if (sg != 0.0) {
+                const double2 u = tilde_value(x, ia, ib, ca, cb, pos[i]);
+                v = make_double2(sg * u.x, sg * u.y);
+            }
+            ws[dst[i]] = Cx<C>::make(v.x, v.y);
+        }
     }
 }
 
@@ -462,11 +492,17 @@ c3l_status static_apply(const c3l_static_action* sa, const double* x, double* xo
         !sa->tilde_ca || !sa->tilde_cb || !sa->lam || !sa->col || !sa->pair || !sa->scale || sa->num_amplitudes <= 0)
         return C3L_ERR_ARGUMENT;
     cudaStream_t s = as_stream(stream);
-    c3l_status st = c3l_tilde_unpack(sa->num_amplitudes, x, sa->tilde_ia, sa->tilde_ib, sa->tilde_ca, sa->tilde_cb,
-                                     sa->canon, stream);
+    const c3l_action* a = &sa->action;
+    const Batch<C> bt = single<C>(reinterpret_cast<C*>(a->ws), reinterpret_cast<const double2*>(sa->canon));
+    const int64_t n = sa->num_amplitudes > a->scatter_count ? sa->num_amplitudes : a->scatter_count;
+    k_unpack_scatter<C><<<grid_for(n), kThreads, 0, s>>>(
+        sa->num_amplitudes, x, sa->tilde_ia, sa->tilde_ib, reinterpret_cast<const double2*>(sa->tilde_ca),
+        reinterpret_cast<const double2*>(sa->tilde_cb), reinterpret_cast<double2*>(sa->canon), a->scatter_count,
+        a->scatter_dst, a->scatter_pos, a->scatter_sign, reinterpret_cast<C*>(a->ws));
+    c3l_status st = launch_status();
     if (st) return st;
-    const Batch<C> bt = single<C>(reinterpret_cast<C*>(sa->action.ws), reinterpret_cast<const double2*>(sa->canon));
-    if ((st = action_prepare<C>(&sa->action, bt, s))) return st;
+    if ((st = run_levels<C>(a, bt, s))) return st;
+    if ((st = run_padded<C>(a, bt, s))) return st;
     if (sa->action.out.ntiles <= 0) return C3L_OK;
     Epilogue ep{};
     ep.lam = reinterpret_cast<const double2*>(sa->lam);

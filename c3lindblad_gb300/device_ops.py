@@ -80,9 +80,9 @@ class DeviceStatic:
         self.cjvp_stage = rt.wedge_stage(up, prog.stages["jvp_all"])
         self.cjvp_lam = up.raw(plan.lam_all_jvp)
         self.launches = {
-            "residual": 1 + rt.action_launches(self.res_action.action),
-            "linearize": 1 + rt.action_launches(self.lin_action.action),
-            "jvp": 1 + rt.action_launches(self.jvp_action.action),
+            "residual": rt.static_launches(self.res_action.action),
+            "linearize": rt.static_launches(self.lin_action.action),
+            "jvp": rt.static_launches(self.jvp_action.action),
         }
         m4, self.preconditioner_diagnostics = plan.preconditioner_table()
         self.pc_m4 = up.raw(m4)

@@ -324,6 +324,11 @@ CLUSTER_LEVEL_MAX_TILES = 16  # levels this small at the end of the list run as 
                               # (16-CTA clusters on GB300; the count is an estimate where only 8 are allowed)
 
 
+def static_launches(a: Action) -> int:
+    """Kernels of one c3l_static_apply: the fused unpack/scatter replaces the scatter."""
+    return action_launches(a) + (0 if a.scatter_count > 0 else 1)
+
+
 def action_launches(a: Action) -> int:
     k = 1 if a.scatter_count > 0 else 0
     tail = a.nlevels
