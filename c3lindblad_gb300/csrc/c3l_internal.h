@@ -52,8 +52,10 @@ struct ArnoldiBatch {
     int32_t* counters[C3L_MAX_BATCH];
     double2* Hc[C3L_MAX_BATCH];
     double2* partial[C3L_MAX_BATCH];
+    float2* V32[C3L_MAX_BATCH];   // FP32 copy of the basis rows (written with each row)
+    float2* w32[C3L_MAX_BATCH];   // FP32 copy of the operator output (written by the sigma)
 };
-// pass 1 (FP32 products): c1[r] = V[r]^H w, r < k = counters[par] + 1
+// pass 1 (FP32, from the FP32 copies V32 and w32): c1[r] = V[r]^H w, r < k = counters[par] + 1
 c3l_status arnoldi_dot1(const ArnoldiBatch& bt, int par, int64_t ld, int64_t dim, const RowDot& p, cudaStream_t s);
 // w -= V[0 : k]^T c1
 c3l_status arnoldi_axpy1(const ArnoldiBatch& bt, int par, int64_t ld, int max_k, int64_t dim, cudaStream_t s);
@@ -61,14 +63,16 @@ c3l_status arnoldi_axpy1(const ArnoldiBatch& bt, int par, int64_t ld, int max_k,
 // column k - 1 of Hc = (c1 + c2 | h), *hval = h, counters[1 - par] = k
 c3l_status arnoldi_dot2(const ArnoldiBatch& bt, int par, int64_t ld, int64_t dim, const RowDot& p, int64_t ldc,
                         cudaStream_t s);
-// V[k] = xnext = (w - V[0 : k]^T c2) / h (unscaled when h <= tol)
+// V[k] = xnext = (w - V[0 : k]^T c2) / h (unscaled when h <= tol), V32[k] = (float) V[k]
 c3l_status arnoldi_scale(const ArnoldiBatch& bt, int par, int64_t ld, int max_k, double tol, int64_t n,
                          cudaStream_t s);
 
 // The sigma action on a batch of vectors (actions[b] share one program and
 // differ in their workspace); an entry whose stop flag is set is skipped.
+// out32 (may be null, or hold null entries): an FP32 copy of each output.
 c3l_status eom_sigma_batch(const c3l_eom_action* actions, int nb, const c3l_complex* const* xin,
-                           c3l_complex* const* out, const int32_t* const* stop, cudaStream_t s);
+                           c3l_complex* const* out, c3l_complex32* const* out32, const int32_t* const* stop,
+                           cudaStream_t s);
 // True when two sigma actions run the same program (they may differ in ws).
 bool same_sigma_program(const c3l_eom_action& a, const c3l_eom_action& b);
 

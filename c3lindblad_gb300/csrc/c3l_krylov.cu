@@ -819,25 +819,26 @@ __device__ __forceinline__ bool last_block(unsigned* done) {
 
 __device__ __forceinline__ bool arn_stopped(const c3l::ArnoldiBatch& bt) { return bt.counters[blockIdx.y][3] != 0; }
 
-// Pass 1 with FP32 products and sums: c1[r] = V[r]^H w (one block per row).
-// The second pass, in FP64, measures and removes what the first left, and the
-// column is c1 + c2, so the Arnoldi relation and the orthogonality keep FP64
-// accuracy.
+// Pass 1 in FP32 from the FP32 copies of the basis rows and of w: c1[r] =
+// V[r]^H w (one block per row).  The second pass, in FP64, measures and
+// removes what the first left, and the column is c1 + c2, so the Arnoldi
+// relation and the orthogonality keep FP64 accuracy; this pass leaves the
+// FP64 pipe to the others.
 __global__ void __launch_bounds__(kThreads) k_arn_dot1(c3l::ArnoldiBatch bt, int par, int64_t ld, int64_t dim) {
     __shared__ float sm[2][32];
     if (arn_stopped(bt)) return;
     const int b = blockIdx.y;
-    const double2* __restrict__ V = bt.V[b];
-    const double2* __restrict__ w = bt.w[b];
+    const float2* __restrict__ V = bt.V32[b];
+    const float2* __restrict__ w = bt.w32[b];
     double2* __restrict__ out = bt.c1[b];
     const int k = bt.counters[b][par] + 1;
     for (int row = blockIdx.x; row < k; row += gridDim.x) {
-        const double2* v = V + (int64_t)row * ld;
+        const float2* v = V + (int64_t)row * ld;
         const int64_t step = blockDim.x;
         float re = 0.0f, im = 0.0f;
         int64_t i = threadIdx.x;
         for (; i + 3 * step < dim; i += 4 * step) {
-            double2 a[4], c[4];
+            float2 a[4], c[4];
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
                 a[u] = v[i + u * step];
@@ -845,15 +846,14 @@ __global__ void __launch_bounds__(kThreads) k_arn_dot1(c3l::ArnoldiBatch bt, int
             }
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
-                const float ax = (float)a[u].x, ay = (float)a[u].y, bx = (float)c[u].x, by = (float)c[u].y;
-                re = fmaf(ax, bx, fmaf(ay, by, re));
-                im = fmaf(ax, by, fmaf(-ay, bx, im));
+                re = fmaf(a[u].x, c[u].x, fmaf(a[u].y, c[u].y, re));
+                im = fmaf(a[u].x, c[u].y, fmaf(-a[u].y, c[u].x, im));
             }
         }
         for (; i < dim; i += step) {
-            const float ax = (float)v[i].x, ay = (float)v[i].y, bx = (float)w[i].x, by = (float)w[i].y;
-            re = fmaf(ax, bx, fmaf(ay, by, re));
-            im = fmaf(ax, by, fmaf(-ay, bx, im));
+            const float2 a = v[i], c = w[i];
+            re = fmaf(a.x, c.x, fmaf(a.y, c.y, re));
+            im = fmaf(a.x, c.y, fmaf(-a.y, c.x, im));
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
@@ -1029,6 +1029,7 @@ __global__ void __launch_bounds__(X * Y) k_arn_scale(c3l::ArnoldiBatch bt, int p
     const double h = *bt.hval[b];
     const double inv = h > tol ? 1.0 / h : 1.0;
     double2* Vk = bt.V[b] + (int64_t)k * ld;
+    float2* V32k = bt.V32[b] + (int64_t)k * ld;
     const double2* __restrict__ w = bt.w[b];
     double2* __restrict__ xnext = bt.xnext[b];
     for (int64_t base = (int64_t)blockIdx.x * X; base < n; base += (int64_t)gridDim.x * X) {
@@ -1037,6 +1038,7 @@ __global__ void __launch_bounds__(X * Y) k_arn_scale(c3l::ArnoldiBatch bt, int p
         if (threadIdx.y == 0 && i < n) {
             const double2 x = make_double2((w[i].x - t.x) * inv, (w[i].y - t.y) * inv);
             Vk[i] = x;
+            V32k[i] = make_float2((float)x.x, (float)x.y);
             xnext[i] = x;
         }
         __syncthreads();
@@ -1398,7 +1400,7 @@ static bool valid_batch(const ArnoldiBatch& bt, bool with_partial) {
     if (bt.nb < 1 || bt.nb > C3L_MAX_BATCH) return false;
     for (int b = 0; b < bt.nb; ++b)
         if (!bt.V[b] || !bt.w[b] || !bt.xnext[b] || !bt.c1[b] || !bt.c2[b] || !bt.hval[b] || !bt.counters[b] ||
-            !bt.Hc[b] || (with_partial && !bt.partial[b]))
+            !bt.Hc[b] || !bt.V32[b] || !bt.w32[b] || (with_partial && !bt.partial[b]))
             return false;
     return true;
 }

@@ -586,7 +586,7 @@ c3l_status c3l_arnoldi(c3l_arnoldi_channel* ch, int32_t nch, int64_t N, const c3
         const c3l_arnoldi_channel& q = ch[c];
         const c3l_hessenberg_state& h = q.hess;
         if (!q.sigma || !q.b || !q.V || !q.Hcol || !q.coeff || !q.partial || !q.host || !q.status_host || !q.work ||
-            !q.counters || !h.rot_c || !h.rot_s || !h.vsink || !h.carry || !h.accum || !h.residual || !h.status ||
+            !q.counters || !q.V32 || !q.work32 || !h.rot_c || !h.rot_s || !h.vsink || !h.carry || !h.accum || !h.residual || !h.status ||
             h.m_max < m_max || h.nshift != nshift || (q.sink_conj && !h.sinkproj_conj))
             return C3L_ERR_ARGUMENT;
     }
@@ -631,12 +631,14 @@ c3l_status c3l_arnoldi(c3l_arnoldi_channel* ch, int32_t nch, int64_t N, const c3
         std::vector<c3l_eom_action> acts(nb);
         std::vector<const c3l_complex*> xin(nb);
         std::vector<c3l_complex*> out(nb);
+        std::vector<c3l_complex32*> out32(nb);
         std::vector<const int32_t*> stop(nb);
         for (int i = 0; i < nb; ++i) {
             c3l_arnoldi_channel& q = ch[mem[i]];
             acts[i] = *q.sigma;
             xin[i] = q.work;
             out[i] = q.work + N;
+            out32[i] = q.work32;
             stop[i] = q.counters + 3;
             bt.V[i] = d2(q.V);
             bt.w[i] = d2(q.work + N);
@@ -647,9 +649,11 @@ c3l_status c3l_arnoldi(c3l_arnoldi_channel* ch, int32_t nch, int64_t N, const c3
             bt.counters[i] = q.counters;
             bt.Hc[i] = d2(q.Hcol);
             bt.partial[i] = d2(q.partial);
+            bt.V32[i] = reinterpret_cast<float2*>(q.V32);
+            bt.w32[i] = reinterpret_cast<float2*>(q.work32);
         }
         auto step = [&](cudaStream_t cs, int par) -> c3l_status {
-            c3l_status r = c3l::eom_sigma_batch(acts.data(), nb, xin.data(), out.data(), stop.data(), cs);
+            c3l_status r = c3l::eom_sigma_batch(acts.data(), nb, xin.data(), out.data(), out32.data(), stop.data(), cs);
             if (r) return r;
             // pass 1 in FP32 (pass 2 is FP64 and removes what it leaves)
             if ((r = c3l::arnoldi_dot1(bt, par, N, N, rd, cs))) return r;
@@ -685,9 +689,10 @@ c3l_status c3l_arnoldi(c3l_arnoldi_channel* ch, int32_t nch, int64_t N, const c3
         q.beta = std::sqrt(std::max(q.host[0].re, 0.0));
         if (!(q.beta > 0.0) || !std::isfinite(q.beta)) return C3L_ERR_ARGUMENT;
         if ((st = c3l_scale_c(N, c3l_complex{1.0 / q.beta, 0.0}, q.b, q.V, sv))) return st;
+        if ((st = c3l_downcast(N, q.V, q.V32, sv))) return st;
         if ((st = c3l_scale_c(N, c3l_complex{1.0 / q.beta, 0.0}, q.b, q.work, sv))) return st;
         if (cudaMemsetAsync(q.counters, 0, 4 * sizeof(int32_t), s) != cudaSuccess) return C3L_ERR_LAUNCH;
-        q.launches += (N > 8192 ? 2 : 1) + 2;
+        q.launches += (N > 8192 ? 2 : 1) + 3;
         q.hess.shifts = shifts;
         q.hess.beta = q.beta;
         q.hess.breakdown_tol = breakdown_tol;

@@ -82,6 +82,7 @@ struct Batch {
     C* ws[C3L_MAX_BATCH];
     const double2* in[C3L_MAX_BATCH];   // scatter source and output-stage input
     double2* out[C3L_MAX_BATCH];        // complex output-stage destination
+    float2* out32[C3L_MAX_BATCH];       // optional FP32 copy of the EOM output
     const int32_t* stop[C3L_MAX_BATCH];
     int nb;
 };
@@ -349,8 +350,11 @@ __global__ void __launch_bounds__(kThreads) k_wedge(c3l_wedge_stage st, int n, B
         const int64_t mu = st.elements[e];
         const double2 a = to_d2(acc);
         const double2 lam = ep.lam[e], src = bt.in[blockIdx.y][mu];
-        bt.out[blockIdx.y][mu] =
+        const double2 o =
             make_double2(fma(lam.x, src.x, fma(-lam.y, src.y, a.x)), fma(lam.x, src.y, fma(lam.y, src.x, a.y)));
+        bt.out[blockIdx.y][mu] = o;
+        float2* o32 = bt.out32[blockIdx.y];
+        if (o32) o32[mu] = make_float2((float)o.x, (float)o.y);
     } else {
         const int64_t mu = st.elements[e];
         bt.out[blockIdx.y][mu] = dmul(ep.cscale, to_d2(acc));
@@ -524,7 +528,7 @@ bool same_program(const c3l_action& a, const c3l_action& b) {
 
 template <typename C>
 c3l_status eom_sigma(const c3l_eom_action* ea, int nb, const c3l_complex* const* xin, c3l_complex* const* out,
-                     const int32_t* const* stop, cudaStream_t s) {
+                     c3l_complex32* const* out32, const int32_t* const* stop, cudaStream_t s) {
     if (!ea || nb < 1 || nb > C3L_MAX_BATCH || !xin || !out) return C3L_ERR_ARGUMENT;
     Batch<C> bt{};
     bt.nb = nb;
@@ -535,6 +539,7 @@ c3l_status eom_sigma(const c3l_eom_action* ea, int nb, const c3l_complex* const*
         bt.in[b] = reinterpret_cast<const double2*>(xin[b]);
         bt.out[b] = reinterpret_cast<double2*>(out[b]);
         bt.stop[b] = stop ? stop[b] : nullptr;
+        bt.out32[b] = out32 ? reinterpret_cast<float2*>(out32[b]) : nullptr;
     }
     c3l_status st = action_prepare<C>(&ea[0].action, bt, s);
     if (st) return st;
@@ -549,8 +554,9 @@ c3l_status eom_sigma(const c3l_eom_action* ea, int nb, const c3l_complex* const*
 namespace c3l {
 
 c3l_status eom_sigma_batch(const c3l_eom_action* actions, int nb, const c3l_complex* const* xin,
-                           c3l_complex* const* out, const int32_t* const* stop, cudaStream_t s) {
-    return eom_sigma<double2>(actions, nb, xin, out, stop, s);
+                           c3l_complex* const* out, c3l_complex32* const* out32, const int32_t* const* stop,
+                           cudaStream_t s) {
+    return eom_sigma<double2>(actions, nb, xin, out, out32, stop, s);
 }
 
 bool same_sigma_program(const c3l_eom_action& a, const c3l_eom_action& b) {
@@ -688,16 +694,16 @@ c3l_status c3l_static_apply_f32(const c3l_static_action* sa, const double* x, do
 }
 
 c3l_status c3l_eom_sigma(const c3l_eom_action* ea, const c3l_complex* xin, c3l_complex* out, void* stream) {
-    return eom_sigma<double2>(ea, 1, &xin, &out, nullptr, as_stream(stream));
+    return eom_sigma<double2>(ea, 1, &xin, &out, nullptr, nullptr, as_stream(stream));
 }
 
 c3l_status c3l_eom_sigma_f32(const c3l_eom_action* ea, const c3l_complex* xin, c3l_complex* out, void* stream) {
-    return eom_sigma<float2>(ea, 1, &xin, &out, nullptr, as_stream(stream));
+    return eom_sigma<float2>(ea, 1, &xin, &out, nullptr, nullptr, as_stream(stream));
 }
 
 c3l_status c3l_eom_sigma_batch(const c3l_eom_action* actions, int32_t nb, const c3l_complex* const* xin,
                                c3l_complex* const* out, void* stream) {
-    return eom_sigma<double2>(actions, nb, xin, out, nullptr, as_stream(stream));
+    return eom_sigma<double2>(actions, nb, xin, out, nullptr, nullptr, as_stream(stream));
 }
 
 const char* c3l_version(void) { return "c3l_gb300 0.2.0 (sm_103a, fp64/fp32 complex programs)"; }

@@ -451,6 +451,8 @@ typedef struct {
     c3l_hessenberg_status* status_host;/* pinned                                  */
     c3l_complex* work;                 /* device [2*N]                            */
     int32_t* counters;                 /* device [4] (int32)                      */
+    c3l_complex32* V32;                /* device (m_max+1) x N: FP32 copy of the basis rows */
+    c3l_complex32* work32;             /* device [N]: FP32 copy of each sigma output        */
     int32_t* check_dims;               /* host [check_capacity]                   */
     double* check_res;                 /* host [check_capacity]                   */
     int32_t check_capacity;
