@@ -165,8 +165,12 @@ __device__ __forceinline__ void powers(int n, int64_t* pw) {
     for (int i = 1; i < 6; ++i) pw[i] = pw[i - 1] * n;
 }
 
+constexpr int kContractChunk = 16;  // source and factor loads issued together per entry
+
 // One padded entry e of a contraction task: const + sum_j sign_j sum_m
-// vec_j[m] src_j[... m at axis_j ...] (interior products).
+// vec_j[m] src_j[... m at axis_j ...] (interior products).  Each chunk of up
+// to 16 strided source entries and their factor entries is loaded before any
+// is used, so the loads' latencies overlap.
 template <typename C>
 __device__ __forceinline__ void contract_entry(const c3l_contract_task& task, int64_t e, int n, const int64_t* pw,
                                                const C* __restrict__ vectors, C* __restrict__ ws) {
@@ -179,17 +183,23 @@ __device__ __forceinline__ void contract_entry(const c3l_contract_task& task, in
         const int64_t lo = e - hi * low;
         const C* src = ws + task.src_off[j] + hi * low * n + lo;
         const C* vec = vectors + task.vec_off[j];
-        // four independent partial sums keep four loads in flight
-        C s0 = Cx<C>::make(0.0, 0.0), s1 = s0, s2 = s0, s3 = s0;
-        int m = 0;
-        for (; m + 3 < n; m += 4) {
-            s0 = cfma(vec[m], src[m * low], s0);
-            s1 = cfma(vec[m + 1], src[(m + 1) * low], s1);
-            s2 = cfma(vec[m + 2], src[(m + 2) * low], s2);
-            s3 = cfma(vec[m + 3], src[(m + 3) * low], s3);
+        C sum = Cx<C>::make(0.0, 0.0);
+        for (int m0 = 0; m0 < n; m0 += kContractChunk) {
+            C v[kContractChunk], f[kContractChunk];
+#pragma unroll
+            for (int u = 0; u < kContractChunk; ++u)
+                if (m0 + u < n) {
+                    v[u] = src[(int64_t)(m0 + u) * low];
+                    f[u] = vec[m0 + u];
+                }
+            C s0 = Cx<C>::make(0.0, 0.0), s1 = s0;
+#pragma unroll
+            for (int u = 0; u < kContractChunk; u += 2) {
+                if (m0 + u < n) s0 = cfma(f[u], v[u], s0);
+                if (m0 + u + 1 < n) s1 = cfma(f[u + 1], v[u + 1], s1);
+            }
+            sum = cadd(sum, cadd(s0, s1));
         }
-        for (; m < n; ++m) s0 = cfma(vec[m], src[m * low], s0);
-        const C sum = cadd(cadd(s0, s1), cadd(s2, s3));
         const typename Cx<C>::R sg = (typename Cx<C>::R)task.sign[j];
         acc.x = fma(sg, sum.x, acc.x);
         acc.y = fma(sg, sum.y, acc.y);
