@@ -219,11 +219,12 @@ __global__ void __launch_bounds__(kThreads) k_contract(c3l_contract_level lv, in
     contract_entry<C>(lv.tasks[tile.block], tile.start + threadIdx.x, n, pw, vectors, ws);
 }
 
-// The small trailing contraction levels (each a few tiles, each level
-// depending on the previous one) as one launch of one thread-block cluster:
-// the cluster's CTAs stride over a level's tiles, then meet at a hardware
-// cluster barrier (release/acquire) before the next level.  Every CTA reaches
-// every barrier.  Batch entries are separate clusters (blockIdx.y); a stopped
+// The small trailing contraction levels (each at most one tile per CTA, each
+// level depending on the previous one) as one launch of one thread-block
+// cluster: CTA c computes tile c of each level, then the cluster meets at a
+// hardware cluster barrier (release/acquire) before the next level.  Every
+// CTA reaches every barrier (the level loop's bounds are the same in all
+// CTAs).  Batch entries are separate clusters (blockIdx.y); a stopped
 // entry's CTAs all return before the first barrier.
 constexpr int kLevelClusterMax = 16;  // non-portable cluster size where the device allows it
 
@@ -238,16 +239,36 @@ __global__ void __launch_bounds__(kThreads) k_contract_cluster(LevelPack pack, i
                                                                 Batch<C> bt) {
     if (batch_stopped(bt)) return;
     C* __restrict__ ws = bt.ws[blockIdx.y];
+    // Every level has at most gridDim.x tiles (the launcher's condition), so a
+    // CTA owns at most one tile per level: its tiles and their tasks are
+    // fetched for all levels at once, before the first level runs.
+    __shared__ c3l_tile stile[C3L_MAX_LEVELS];
+    __shared__ c3l_contract_task stask[C3L_MAX_LEVELS];
+    static_assert(sizeof(c3l_contract_task) % sizeof(int64_t) == 0, "task records are copied as 8-byte words");
+    constexpr int kTaskWords = sizeof(c3l_contract_task) / sizeof(int64_t);
+    if ((int)threadIdx.x < pack.count) {
+        const c3l_contract_level& lv = pack.lv[pack.first + threadIdx.x];
+        c3l_tile t{};
+        if ((int64_t)blockIdx.x < lv.ntiles) t = lv.tiles[blockIdx.x];
+        stile[threadIdx.x] = t;
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < pack.count * kTaskWords; q += blockDim.x) {
+        const int l = q / kTaskWords;
+        if ((int64_t)blockIdx.x < pack.lv[pack.first + l].ntiles)
+            reinterpret_cast<int64_t*>(&stask[l])[q - l * kTaskWords] =
+                reinterpret_cast<const int64_t*>(&pack.lv[pack.first + l].tasks[stile[l].block])[q - l * kTaskWords];
+    }
+    __syncthreads();
     int64_t pw[6];
     powers(n, pw);
-    for (int l = pack.first; l < pack.first + pack.count; ++l) {
-        const c3l_contract_level lv = pack.lv[l];
-        for (int64_t t = blockIdx.x; t < lv.ntiles; t += gridDim.x) {
-            const c3l_tile tile = lv.tiles[t];
-            if ((int)threadIdx.x < tile.count)
-                contract_entry<C>(lv.tasks[tile.block], tile.start + threadIdx.x, n, pw, vectors, ws);
-        }
-        asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+    for (int i = 0; i < pack.count; ++i) {
+        if ((int64_t)blockIdx.x < pack.lv[pack.first + i].ntiles && (int)threadIdx.x < stile[i].count)
+            contract_entry<C>(stask[i], stile[i].start + threadIdx.x, n, pw, vectors, ws);
+        // the next level reads this one's outputs; after the last level the
+        // kernel's end publishes them (no shared memory of other CTAs is used)
+        if (i + 1 < pack.count)
+            asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
     }
 }
 
