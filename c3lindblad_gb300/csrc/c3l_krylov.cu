@@ -19,6 +19,7 @@
 
 #include "c3l_gb300.h"
 #include "c3l_internal.h"
+#include "c3l_pdl.h"
 
 namespace {
 
@@ -826,7 +827,9 @@ __device__ __forceinline__ bool arn_stopped(const c3l::ArnoldiBatch& bt) { retur
 // FP64 pipe to the others.
 __global__ void __launch_bounds__(kThreads) k_arn_dot1(c3l::ArnoldiBatch bt, int par, int64_t ld, int64_t dim) {
     __shared__ float sm[2][32];
+    c3l::pdl_launch_dependents();
     if (arn_stopped(bt)) return;
+    c3l::pdl_wait();
     const int b = blockIdx.y;
     const float2* __restrict__ V = bt.V32[b];
     const float2* __restrict__ w = bt.w32[b];
@@ -918,7 +921,9 @@ __device__ __forceinline__ double2 arn_combine(const double2* __restrict__ V, in
 template <int X, int Y>
 __global__ void __launch_bounds__(X * Y) k_arn_axpy(c3l::ArnoldiBatch bt, int par, int64_t ld, int64_t dim) {
     __shared__ double2 part[Y][X];
+    c3l::pdl_launch_dependents();
     if (arn_stopped(bt)) return;
+    c3l::pdl_wait();
     const int b = blockIdx.y;
     const int k = bt.counters[b][par] + 1;
     double2* __restrict__ w = bt.w[b];
@@ -958,7 +963,9 @@ __device__ void arnoldi_column_tail(const double2* __restrict__ c1, const double
 __global__ void __launch_bounds__(kThreads) k_arn_dot2(c3l::ArnoldiBatch bt, int par, int64_t ld, int64_t dim,
                                                        int nseg, int64_t seglen, int64_t ldc) {
     __shared__ double sm[32];
+    c3l::pdl_launch_dependents();
     if (arn_stopped(bt)) return;
+    c3l::pdl_wait();
     const int b = blockIdx.y;
     const double2* __restrict__ V = bt.V[b];
     const double2* __restrict__ w = bt.w[b];
@@ -999,7 +1006,9 @@ __global__ void __launch_bounds__(kThreads) k_arn_dot2(c3l::ArnoldiBatch bt, int
 
 __global__ void __launch_bounds__(kThreads) k_arn_dot2_final(c3l::ArnoldiBatch bt, int par, int nseg, int64_t ldc) {
     __shared__ double sm[32];
+    c3l::pdl_launch_dependents();
     if (arn_stopped(bt)) return;
+    c3l::pdl_wait();
     const int b = blockIdx.y;
     int32_t* ctr = bt.counters[b];
     const int k = ctr[par] + 1;
@@ -1023,7 +1032,9 @@ template <int X, int Y>
 __global__ void __launch_bounds__(X * Y) k_arn_scale(c3l::ArnoldiBatch bt, int par, int64_t ld, int64_t n,
                                                      double tol) {
     __shared__ double2 part[Y][X];
+    c3l::pdl_launch_dependents();
     if (arn_stopped(bt)) return;
+    c3l::pdl_wait();
     const int b = blockIdx.y;
     const int k = bt.counters[b][par] + 1;
     const double h = *bt.hval[b];
@@ -1244,6 +1255,8 @@ __device__ __forceinline__ void gm_reduce_f(const float* __restrict__ partial, i
 __global__ void __launch_bounds__(kThreads) k_gm_dot_f(const float* __restrict__ V, int64_t ld, const int* cur,
                                                        const double* __restrict__ w, float* __restrict__ wf,
                                                        int64_t n, int64_t seg, float* __restrict__ partial1, int R) {
+    c3l::pdl_launch_dependents();
+    c3l::pdl_wait();
     const int k = *cur + 1;
     const int64_t lo = (int64_t)blockIdx.x * seg;
     const int64_t hi = min(n, lo + seg);
@@ -1257,6 +1270,8 @@ __global__ void __launch_bounds__(kThreads) k_gm_axpy_dot_f(const float* __restr
                                                             float* __restrict__ c1, float* __restrict__ wf,
                                                             int64_t n, int64_t seg, float* __restrict__ partial2,
                                                             int R) {
+    c3l::pdl_launch_dependents();
+    c3l::pdl_wait();
     __shared__ float cs[C3L_GMRES_MAX_ROWS];
     const int k = *cur + 1;
     gm_reduce_f(partial1, R, gridDim.x, k, cs);
@@ -1287,6 +1302,8 @@ __global__ void __launch_bounds__(kThreads) k_gm_scale_f(float* V, int64_t ld, c
                                                          const float* __restrict__ wf, int64_t n,
                                                          double* __restrict__ xnext, double* __restrict__ slots,
                                                          int stride) {
+    c3l::pdl_launch_dependents();
+    c3l::pdl_wait();
     __shared__ float cs[C3L_GMRES_MAX_ROWS];
     __shared__ float hh[2];
     const int k = *cur + 1;
@@ -1407,34 +1424,32 @@ static bool valid_batch(const ArnoldiBatch& bt, bool with_partial) {
 
 c3l_status arnoldi_dot1(const ArnoldiBatch& bt, int par, int64_t ld, int64_t dim, const RowDot& p, cudaStream_t s) {
     if (!valid_batch(bt, false) || dim <= 0 || ld < dim || (par & ~1)) return C3L_ERR_ARGUMENT;
-    k_arn_dot1<<<dim3(p.grid, (unsigned)bt.nb), kThreads, 0, s>>>(bt, par, ld, dim);
-    return launch_status();
+    return launch_pdl(k_arn_dot1, dim3(p.grid, (unsigned)bt.nb), dim3(kThreads), 0, s, 0, false, bt, par, ld, dim);
 }
 
 c3l_status arnoldi_axpy1(const ArnoldiBatch& bt, int par, int64_t ld, int max_k, int64_t dim, cudaStream_t s) {
     if (!valid_batch(bt, false) || dim <= 0 || ld < dim || (par & ~1)) return C3L_ERR_ARGUMENT;
     (void)max_k;
-    k_arn_axpy<kAxX, kAxY><<<dim3(axpy_grid(dim), (unsigned)bt.nb), dim3(kAxX, kAxY), 0, s>>>(bt, par, ld, dim);
-    return launch_status();
+    return launch_pdl(k_arn_axpy<kAxX, kAxY>, dim3(axpy_grid(dim), (unsigned)bt.nb), dim3(kAxX, kAxY), 0, s, 0, false, bt, par,
+                      ld, dim);
 }
 
 c3l_status arnoldi_dot2(const ArnoldiBatch& bt, int par, int64_t ld, int64_t dim, const RowDot& p, int64_t ldc,
                         cudaStream_t s) {
     if (!valid_batch(bt, p.nseg > 1) || dim <= 0 || ld < dim || (par & ~1)) return C3L_ERR_ARGUMENT;
-    k_arn_dot2<<<dim3(p.grid, (unsigned)bt.nb), kThreads, 0, s>>>(bt, par, ld, dim, p.nseg, p.seglen, ldc);
-    if (p.nseg > 1) {
-        const unsigned g = (unsigned)(p.max_rows > 1024 ? 1024 : p.max_rows);
-        k_arn_dot2_final<<<dim3(g, (unsigned)bt.nb), kThreads, 0, s>>>(bt, par, p.nseg, ldc);
-    }
-    return launch_status();
+    c3l_status r = launch_pdl(k_arn_dot2, dim3(p.grid, (unsigned)bt.nb), dim3(kThreads), 0, s, 0, false, bt, par, ld, dim,
+                              p.nseg, p.seglen, ldc);
+    if (r || p.nseg == 1) return r;
+    const unsigned g = (unsigned)(p.max_rows > 1024 ? 1024 : p.max_rows);
+    return launch_pdl(k_arn_dot2_final, dim3(g, (unsigned)bt.nb), dim3(kThreads), 0, s, 0, false, bt, par, p.nseg, ldc);
 }
 
 c3l_status arnoldi_scale(const ArnoldiBatch& bt, int par, int64_t ld, int max_k, double tol, int64_t n,
                          cudaStream_t s) {
     if (!valid_batch(bt, false) || n <= 0 || ld < n || (par & ~1)) return C3L_ERR_ARGUMENT;
     (void)max_k;
-    k_arn_scale<kAxX, kAxY><<<dim3(axpy_grid(n), (unsigned)bt.nb), dim3(kAxX, kAxY), 0, s>>>(bt, par, ld, n, tol);
-    return launch_status();
+    return launch_pdl(k_arn_scale<kAxX, kAxY>, dim3(axpy_grid(n), (unsigned)bt.nb), dim3(kAxX, kAxY), 0, s, 0, false, bt, par,
+                      ld, n, tol);
 }
 
 GmPlan gm_plan(int64_t n, int max_rows, int sms) {
@@ -1480,16 +1495,15 @@ c3l_status gm_scale(double* V, int64_t ld, const int* cur, int* next, const doub
 c3l_status gm_dot_f32(const float* V, int64_t ld, const int* cur, const double* w, float* wf, int64_t n,
                       const GmPlan& p, float* partial, cudaStream_t s) {
     if (!V || !cur || !w || !wf || !partial || n <= 0 || p.R > C3L_GMRES_MAX_ROWS) return C3L_ERR_ARGUMENT;
-    k_gm_dot_f<<<p.blocks, kThreads, 0, s>>>(V, ld, cur, w, wf, n, p.seg, partial, p.R);
-    return launch_status();
+    return launch_pdl(k_gm_dot_f, dim3(p.blocks), dim3(kThreads), 0, s, 0, true, V, ld, cur, w, wf, n, p.seg, partial, p.R);
 }
 
 c3l_status gm_axpy_dot_f32(const float* V, int64_t ld, const int* cur, float* c1, float* wf, int64_t n,
                            const GmPlan& p, float* partial, cudaStream_t s) {
     if (!V || !cur || !c1 || !wf || !partial || n <= 0 || p.R > C3L_GMRES_MAX_ROWS) return C3L_ERR_ARGUMENT;
     const int64_t half = (int64_t)p.blocks * p.R;
-    k_gm_axpy_dot_f<<<p.blocks, kThreads, 0, s>>>(V, ld, cur, partial, c1, wf, n, p.seg, partial + half, p.R);
-    return launch_status();
+    return launch_pdl(k_gm_axpy_dot_f, dim3(p.blocks), dim3(kThreads), 0, s, 0, true, V, ld, cur, (const float*)partial, c1,
+                      wf, n, p.seg, partial + half, p.R);
 }
 
 c3l_status gm_scale_f32(float* V, int64_t ld, const int* cur, int* next, const float* partial, const float* c1,
@@ -1497,9 +1511,8 @@ c3l_status gm_scale_f32(float* V, int64_t ld, const int* cur, int* next, const f
                         int stride, cudaStream_t s) {
     if (!V || !cur || !next || !partial || !c1 || !wf || !xnext || !slots || n <= 0) return C3L_ERR_ARGUMENT;
     const int64_t half = (int64_t)p.blocks * p.R;
-    k_gm_scale_f<<<p.scale_grid, kThreads, 0, s>>>(V, ld, cur, next, partial + half, p.R, (int)p.blocks, c1, eps, wf,
-                                                   n, xnext, slots, stride);
-    return launch_status();
+    return launch_pdl(k_gm_scale_f, dim3(p.scale_grid), dim3(kThreads), 0, s, 0, true, V, ld, cur, next,
+                      (const float*)(partial + half), p.R, (int)p.blocks, c1, eps, wf, n, xnext, slots, stride);
 }
 
 c3l_status gm_start_f32(int64_t n, double a, const double* r, float* V0, double* x, cudaStream_t s) {

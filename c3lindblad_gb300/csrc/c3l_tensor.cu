@@ -26,6 +26,7 @@
 
 #include "c3l_gb300.h"
 #include "c3l_internal.h"
+#include "c3l_pdl.h"
 
 namespace {
 
@@ -85,6 +86,7 @@ struct Batch {
     float2* out32[C3L_MAX_BATCH];       // optional FP32 copy of the EOM output
     const int32_t* stop[C3L_MAX_BATCH];
     int nb;
+    bool pdl;  // launch with programmatic dependent launch (the static operator's path)
 };
 
 template <typename C>
@@ -120,6 +122,8 @@ __global__ void k_unpack_scatter(int64_t dim, const double* __restrict__ x, cons
                                  const double2* __restrict__ cb, double2* __restrict__ t, int64_t count,
                                  const int64_t* __restrict__ dst, const int64_t* __restrict__ pos,
                                  const double* __restrict__ sign, C* __restrict__ ws) {
+    c3l::pdl_launch_dependents();
+    c3l::pdl_wait();
     const int64_t n = dim > count ? dim : count;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         if (i < dim) t[i] = tilde_value(x, ia, ib, ca, cb, i);
@@ -138,7 +142,9 @@ __global__ void k_unpack_scatter(int64_t dim, const double* __restrict__ x, cons
 template <typename C>
 __global__ void k_scatter(int64_t count, const int64_t* __restrict__ dst, const int64_t* __restrict__ pos,
                           const double* __restrict__ sign, Batch<C> bt) {
+    c3l::pdl_launch_dependents();
     if (batch_stopped(bt)) return;
+    c3l::pdl_wait();
     const double2* __restrict__ vec = bt.in[blockIdx.y];
     C* __restrict__ ws = bt.ws[blockIdx.y];
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < count; e += (int64_t)gridDim.x * blockDim.x) {
@@ -210,13 +216,16 @@ __device__ __forceinline__ void contract_entry(const c3l_contract_task& task, in
 template <typename C>
 __global__ void __launch_bounds__(kThreads) k_contract(c3l_contract_level lv, int n, const C* __restrict__ vectors,
                                                         Batch<C> bt) {
+    c3l::pdl_launch_dependents();
     if (batch_stopped(bt)) return;
     C* __restrict__ ws = bt.ws[blockIdx.y];
     const c3l_tile tile = lv.tiles[blockIdx.x];
     if ((int)threadIdx.x >= tile.count) return;
+    const c3l_contract_task task = lv.tasks[tile.block];  // program tables: read before the wait
     int64_t pw[6];
     powers(n, pw);
-    contract_entry<C>(lv.tasks[tile.block], tile.start + threadIdx.x, n, pw, vectors, ws);
+    c3l::pdl_wait();
+    contract_entry<C>(task, tile.start + threadIdx.x, n, pw, vectors, ws);
 }
 
 // The small trailing contraction levels (each at most one tile per CTA, each
@@ -237,6 +246,7 @@ struct LevelPack {
 template <typename C>
 __global__ void __launch_bounds__(kThreads) k_contract_cluster(LevelPack pack, int n, const C* __restrict__ vectors,
                                                                 Batch<C> bt) {
+    c3l::pdl_launch_dependents();
     if (batch_stopped(bt)) return;
     C* __restrict__ ws = bt.ws[blockIdx.y];
     // Every level has at most gridDim.x tiles (the launcher's condition), so a
@@ -262,6 +272,7 @@ __global__ void __launch_bounds__(kThreads) k_contract_cluster(LevelPack pack, i
     __syncthreads();
     int64_t pw[6];
     powers(n, pw);
+    c3l::pdl_wait();  // the tables above are constant; the workspace is not
     for (int i = 0; i < pack.count; ++i) {
         if ((int64_t)blockIdx.x < pack.lv[pack.first + i].ntiles && (int)threadIdx.x < stile[i].count)
             contract_entry<C>(stask[i], stile[i].start + threadIdx.x, n, pw, vectors, ws);
@@ -297,6 +308,7 @@ __device__ __forceinline__ double2 dmul(double2 a, double2 b) {
 template <int MODE, typename C, int kWE>
 __global__ void __launch_bounds__(kThreads) k_wedge(c3l_wedge_stage st, int n, Batch<C> bt, Epilogue ep) {
     constexpr int kWG = kThreads / kWE;
+    c3l::pdl_launch_dependents();
     if (batch_stopped(bt)) return;
     C* __restrict__ ws = bt.ws[blockIdx.y];
     __shared__ c3l_instance sinst[kInstChunk];
@@ -324,16 +336,25 @@ __global__ void __launch_bounds__(kThreads) k_wedge(c3l_wedge_stage st, int n, B
         }
     }
     C acc = Cx<C>::make(0.0, 0.0);
+    // cooperative copy of cnt instances from `base` (8-byte words); the first
+    // chunk is staged before the wait (instances are program tables)
+    auto stage = [&](int64_t base, int cnt) {
+        const int64_t* src = reinterpret_cast<const int64_t*>(st.instances + base);
+        int64_t* dst = reinterpret_cast<int64_t*>(sinst);
+        const int words = cnt * (int)(sizeof(c3l_instance) / 8);
+        for (int w = threadIdx.x; w < words; w += blockDim.x) dst[w] = src[w];
+    };
+    {
+        const int64_t left = blk.inst_end - blk.inst_begin;
+        if (left > 0) stage(blk.inst_begin, left < kInstChunk ? (int)left : kInstChunk);
+    }
+    c3l::pdl_wait();
     for (int64_t base = blk.inst_begin; base < blk.inst_end; base += kInstChunk) {
         const int64_t left = blk.inst_end - base;
         const int cnt = left < kInstChunk ? (int)left : kInstChunk;
-        __syncthreads();
-        {
-            // cooperative copy of cnt instances (8-byte words)
-            const int64_t* src = reinterpret_cast<const int64_t*>(st.instances + base);
-            int64_t* dst = reinterpret_cast<int64_t*>(sinst);
-            const int words = cnt * (int)(sizeof(c3l_instance) / 8);
-            for (int w = threadIdx.x; w < words; w += blockDim.x) dst[w] = src[w];
+        if (base != blk.inst_begin) {
+            __syncthreads();  // the previous chunk has been used
+            stage(base, cnt);
         }
         __syncthreads();
         if (active) {
@@ -406,14 +427,13 @@ template <int MODE, typename C>
 c3l_status launch_wedge(const c3l_wedge_stage& st, int n, const Batch<C>& bt, const Epilogue& ep, cudaStream_t s) {
     const dim3 grid((unsigned)st.ntiles, (unsigned)bt.nb);
     switch (st.width) {
-        case 8: k_wedge<MODE, C, 8><<<grid, kThreads, 0, s>>>(st, n, bt, ep); break;
-        case 16: k_wedge<MODE, C, 16><<<grid, kThreads, 0, s>>>(st, n, bt, ep); break;
-        case 32: k_wedge<MODE, C, 32><<<grid, kThreads, 0, s>>>(st, n, bt, ep); break;
+        case 8: return c3l::launch_pdl(k_wedge<MODE, C, 8>, grid, dim3(kThreads), 0, s, 0, bt.pdl, st, n, bt, ep);
+        case 16: return c3l::launch_pdl(k_wedge<MODE, C, 16>, grid, dim3(kThreads), 0, s, 0, bt.pdl, st, n, bt, ep);
+        case 32: return c3l::launch_pdl(k_wedge<MODE, C, 32>, grid, dim3(kThreads), 0, s, 0, bt.pdl, st, n, bt, ep);
         case 0:
-        case 64: k_wedge<MODE, C, 64><<<grid, kThreads, 0, s>>>(st, n, bt, ep); break;
+        case 64: return c3l::launch_pdl(k_wedge<MODE, C, 64>, grid, dim3(kThreads), 0, s, 0, bt.pdl, st, n, bt, ep);
         default: return C3L_ERR_ARGUMENT;
     }
-    return launch_status();
 }
 
 inline unsigned grid_for(int64_t count) {
@@ -461,28 +481,18 @@ c3l_status run_levels(const c3l_action* a, const Batch<C>& bt, cudaStream_t s) {
     const C* vectors = reinterpret_cast<const C*>(a->vectors);
     for (int l = 0; l < tail; ++l) {
         if (a->levels[l].ntiles <= 0) continue;
-        k_contract<C><<<dim3((unsigned)a->levels[l].ntiles, (unsigned)bt.nb), kThreads, 0, s>>>(a->levels[l], a->n,
-                                                                                              vectors, bt);
+        const c3l_status r = c3l::launch_pdl(k_contract<C>, dim3((unsigned)a->levels[l].ntiles, (unsigned)bt.nb),
+                                             dim3(kThreads), 0, s, 0, bt.pdl, a->levels[l], a->n, vectors, bt);
+        if (r) return r;
     }
     if (tail < a->nlevels) {
         LevelPack pack{};
         for (int l = 0; l < a->nlevels; ++l) pack.lv[l] = a->levels[l];
         pack.first = tail;
         pack.count = a->nlevels - tail;
-        cudaLaunchConfig_t cfg{};
-        cfg.gridDim = dim3(cluster, (unsigned)bt.nb, 1);
-        cfg.blockDim = dim3(kThreads, 1, 1);
-        cfg.dynamicSmemBytes = 0;
-        cfg.stream = s;
-        cudaLaunchAttribute attr[1];
-        attr[0].id = cudaLaunchAttributeClusterDimension;
-        attr[0].val.clusterDim.x = cluster;
-        attr[0].val.clusterDim.y = 1;
-        attr[0].val.clusterDim.z = 1;
-        cfg.attrs = attr;
-        cfg.numAttrs = 1;
-        if (cudaLaunchKernelEx(&cfg, k_contract_cluster<C>, pack, a->n, vectors, bt) != cudaSuccess)
-            return C3L_ERR_LAUNCH;
+        const c3l_status r = c3l::launch_pdl(k_contract_cluster<C>, dim3(cluster, (unsigned)bt.nb, 1), dim3(kThreads),
+                                             0, s, (unsigned)cluster, bt.pdl, pack, a->n, vectors, bt);
+        if (r) return r;
     }
     return launch_status();
 }
@@ -501,9 +511,8 @@ c3l_status run_padded(const c3l_action* a, const Batch<C>& bt, cudaStream_t s) {
 template <typename C>
 c3l_status scatter(const c3l_action* a, const Batch<C>& bt, cudaStream_t s) {
     if (a->scatter_count <= 0) return C3L_OK;
-    k_scatter<C><<<dim3(grid_for(a->scatter_count), (unsigned)bt.nb), kThreads, 0, s>>>(
-        a->scatter_count, a->scatter_dst, a->scatter_pos, a->scatter_sign, bt);
-    return launch_status();
+    return c3l::launch_pdl(k_scatter<C>, dim3(grid_for(a->scatter_count), (unsigned)bt.nb), dim3(kThreads), 0, s, 0,
+                           bt.pdl, a->scatter_count, a->scatter_dst, a->scatter_pos, a->scatter_sign, bt);
 }
 
 bool valid_action(const c3l_action* a) {
@@ -528,13 +537,15 @@ c3l_status static_apply(const c3l_static_action* sa, const double* x, double* xo
         return C3L_ERR_ARGUMENT;
     cudaStream_t s = as_stream(stream);
     const c3l_action* a = &sa->action;
-    const Batch<C> bt = single<C>(reinterpret_cast<C*>(a->ws), reinterpret_cast<const double2*>(sa->canon));
+    Batch<C> bt = single<C>(reinterpret_cast<C*>(a->ws), reinterpret_cast<const double2*>(sa->canon));
+    bt.pdl = true;
     const int64_t n = sa->num_amplitudes > a->scatter_count ? sa->num_amplitudes : a->scatter_count;
-    k_unpack_scatter<C><<<grid_for(n), kThreads, 0, s>>>(
-        sa->num_amplitudes, x, sa->tilde_ia, sa->tilde_ib, reinterpret_cast<const double2*>(sa->tilde_ca),
+    c3l_status st = c3l::launch_pdl(
+        k_unpack_scatter<C>, dim3(grid_for(n)), dim3(kThreads), 0, s, 0, true, sa->num_amplitudes, x,
+        (const int64_t*)sa->tilde_ia, (const int64_t*)sa->tilde_ib, reinterpret_cast<const double2*>(sa->tilde_ca),
         reinterpret_cast<const double2*>(sa->tilde_cb), reinterpret_cast<double2*>(sa->canon), a->scatter_count,
-        a->scatter_dst, a->scatter_pos, a->scatter_sign, reinterpret_cast<C*>(a->ws));
-    c3l_status st = launch_status();
+        (const int64_t*)a->scatter_dst, (const int64_t*)a->scatter_pos, (const double*)a->scatter_sign,
+        reinterpret_cast<C*>(a->ws));
     if (st) return st;
     if ((st = run_levels<C>(a, bt, s))) return st;
     if ((st = run_padded<C>(a, bt, s))) return st;
