@@ -827,8 +827,7 @@ __device__ __forceinline__ bool arn_stopped(const c3l::ArnoldiBatch& bt) { retur
 // FP64 pipe to the others.
 __global__ void __launch_bounds__(kThreads) k_arn_dot1(c3l::ArnoldiBatch bt, int par, int64_t ld, int64_t dim) {
     __shared__ float sm[2][32];
-    c3l::pdl_launch_dependents();
-    if (arn_stopped(bt)) return;
+    if (arn_stopped(bt)) return;  // dependents launch as the blocks exit
     c3l::pdl_wait();
     const int b = blockIdx.y;
     const float2* __restrict__ V = bt.V32[b];
@@ -921,8 +920,7 @@ __device__ __forceinline__ double2 arn_combine(const double2* __restrict__ V, in
 template <int X, int Y>
 __global__ void __launch_bounds__(X * Y) k_arn_axpy(c3l::ArnoldiBatch bt, int par, int64_t ld, int64_t dim) {
     __shared__ double2 part[Y][X];
-    c3l::pdl_launch_dependents();
-    if (arn_stopped(bt)) return;
+    if (arn_stopped(bt)) return;  // dependents launch as the blocks exit
     c3l::pdl_wait();
     const int b = blockIdx.y;
     const int k = bt.counters[b][par] + 1;
@@ -963,8 +961,7 @@ __device__ void arnoldi_column_tail(const double2* __restrict__ c1, const double
 __global__ void __launch_bounds__(kThreads) k_arn_dot2(c3l::ArnoldiBatch bt, int par, int64_t ld, int64_t dim,
                                                        int nseg, int64_t seglen, int64_t ldc) {
     __shared__ double sm[32];
-    c3l::pdl_launch_dependents();
-    if (arn_stopped(bt)) return;
+    if (arn_stopped(bt)) return;  // dependents launch as the blocks exit
     c3l::pdl_wait();
     const int b = blockIdx.y;
     const double2* __restrict__ V = bt.V[b];
@@ -1006,8 +1003,7 @@ __global__ void __launch_bounds__(kThreads) k_arn_dot2(c3l::ArnoldiBatch bt, int
 
 __global__ void __launch_bounds__(kThreads) k_arn_dot2_final(c3l::ArnoldiBatch bt, int par, int nseg, int64_t ldc) {
     __shared__ double sm[32];
-    c3l::pdl_launch_dependents();
-    if (arn_stopped(bt)) return;
+    if (arn_stopped(bt)) return;  // dependents launch as the blocks exit
     c3l::pdl_wait();
     const int b = blockIdx.y;
     int32_t* ctr = bt.counters[b];
@@ -1032,8 +1028,7 @@ template <int X, int Y>
 __global__ void __launch_bounds__(X * Y) k_arn_scale(c3l::ArnoldiBatch bt, int par, int64_t ld, int64_t n,
                                                      double tol) {
     __shared__ double2 part[Y][X];
-    c3l::pdl_launch_dependents();
-    if (arn_stopped(bt)) return;
+    if (arn_stopped(bt)) return;  // dependents launch as the blocks exit
     c3l::pdl_wait();
     const int b = blockIdx.y;
     const int k = bt.counters[b][par] + 1;
@@ -1208,19 +1203,26 @@ __global__ void __launch_bounds__(kThreads) k_gm_scale(double* V, int64_t ld, co
 // The same three kernels for an inner solve whose operator is FP32 (the
 // FP32 JVP): the basis rows, the work vector after the operator and all
 // products and sums are FP32; the Hessenberg column goes to the host in FP64.
-// Partial sums are floats in the same [block][R] layout.
+// Partial sums are floats in the same [block][R] layout.  Blocks of 1024
+// threads: 32 warps share the projection rows, and the updates w -= V c run
+// 256 columns x 4 row groups (each thread a quarter of the rows, the groups
+// added in shared memory in a fixed order), so no thread walks all k rows.
+constexpr int kGmfThreads = 1024;
+constexpr int kGmfWarps = kGmfThreads / 32;
+constexpr int kGmfCols = 256;
+constexpr int kGmfGroups = kGmfThreads / kGmfCols;
 
 __device__ __forceinline__ void gm_partials_f(const float* __restrict__ V, int64_t ld, int k,
                                               const float* __restrict__ w, int64_t lo, int64_t hi,
                                               float* __restrict__ partial, int R) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int rows = (k + 1 - warp + kGmWarps - 1) / kGmWarps;  // rows of this warp (row k is w itself)
+    const int rows = (k + 1 - warp + kGmfWarps - 1) / kGmfWarps;  // rows of this warp (row k is w itself)
     for (int q0 = 0; q0 < rows; q0 += 4) {
         float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
         const float* v[4];
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
-            const int r = warp + kGmWarps * (q0 + u);
+            const int r = warp + kGmfWarps * (q0 + u);
             v[u] = (q0 + u < rows) ? (r < k ? V + (int64_t)r * ld : w) : w;
         }
         for (int64_t c = lo + lane; c < hi; c += 32) {
@@ -1234,7 +1236,7 @@ __device__ __forceinline__ void gm_partials_f(const float* __restrict__ V, int64
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
             const float t = warp_sum(acc[u]);
-            const int r = warp + kGmWarps * (q0 + u);
+            const int r = warp + kGmfWarps * (q0 + u);
             if (lane == 0 && q0 + u < rows) partial[(int64_t)blockIdx.x * R + r] = t;
         }
     }
@@ -1243,7 +1245,7 @@ __device__ __forceinline__ void gm_partials_f(const float* __restrict__ V, int64
 __device__ __forceinline__ void gm_reduce_f(const float* __restrict__ partial, int R, int nb, int k,
                                             float* __restrict__ out) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int r = warp; r <= k; r += kGmWarps) {
+    for (int r = warp; r <= k; r += kGmfWarps) {
         float s = 0.0f;
         for (int b = lane; b < nb; b += 32) s += partial[(int64_t)b * R + r];
         s = warp_sum(s);
@@ -1251,10 +1253,40 @@ __device__ __forceinline__ void gm_reduce_f(const float* __restrict__ partial, i
     }
 }
 
+// t = sum_{r < k} c[r] V[r][col] for the thread's column (col valid when
+// `ok`), each row group a quarter of the rows; the result is valid in row
+// group 0.  Every thread of the block calls it (it synchronizes).
+__device__ __forceinline__ float gm_combine_f(const float* __restrict__ V, int64_t ld, int k,
+                                              const float* __restrict__ c, int64_t col, bool ok,
+                                              float (*red)[kGmfCols]) {
+    const int g = threadIdx.x / kGmfCols, cl = threadIdx.x % kGmfCols;
+    float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f, s3 = 0.0f;
+    if (ok) {
+        constexpr int G = kGmfGroups;
+        int r = g;
+        for (; r + 3 * G < k; r += 4 * G) {
+            s0 = fmaf(c[r], V[(int64_t)r * ld + col], s0);
+            s1 = fmaf(c[r + G], V[(int64_t)(r + G) * ld + col], s1);
+            s2 = fmaf(c[r + 2 * G], V[(int64_t)(r + 2 * G) * ld + col], s2);
+            s3 = fmaf(c[r + 3 * G], V[(int64_t)(r + 3 * G) * ld + col], s3);
+        }
+        for (; r < k; r += G) s0 = fmaf(c[r], V[(int64_t)r * ld + col], s0);
+    }
+    red[g][cl] = (s0 + s1) + (s2 + s3);
+    __syncthreads();
+    float t = 0.0f;
+    if (g == 0) {
+#pragma unroll
+        for (int q = 0; q < kGmfGroups; ++q) t += red[q][cl];
+    }
+    return t;
+}
+
 // wf = (float) w on the block's segment, then the pass-1 partials.
-__global__ void __launch_bounds__(kThreads) k_gm_dot_f(const float* __restrict__ V, int64_t ld, const int* cur,
-                                                       const double* __restrict__ w, float* __restrict__ wf,
-                                                       int64_t n, int64_t seg, float* __restrict__ partial1, int R) {
+__global__ void __launch_bounds__(kGmfThreads) k_gm_dot_f(const float* __restrict__ V, int64_t ld, const int* cur,
+                                                          const double* __restrict__ w, float* __restrict__ wf,
+                                                          int64_t n, int64_t seg, float* __restrict__ partial1,
+                                                          int R) {
     c3l::pdl_launch_dependents();
     c3l::pdl_wait();
     const int k = *cur + 1;
@@ -1265,14 +1297,15 @@ __global__ void __launch_bounds__(kThreads) k_gm_dot_f(const float* __restrict__
     gm_partials_f(V, ld, k, wf, lo, hi, partial1, R);
 }
 
-__global__ void __launch_bounds__(kThreads) k_gm_axpy_dot_f(const float* __restrict__ V, int64_t ld, const int* cur,
-                                                            const float* __restrict__ partial1,
-                                                            float* __restrict__ c1, float* __restrict__ wf,
-                                                            int64_t n, int64_t seg, float* __restrict__ partial2,
-                                                            int R) {
+__global__ void __launch_bounds__(kGmfThreads) k_gm_axpy_dot_f(const float* __restrict__ V, int64_t ld,
+                                                               const int* cur, const float* __restrict__ partial1,
+                                                               float* __restrict__ c1, float* __restrict__ wf,
+                                                               int64_t n, int64_t seg, float* __restrict__ partial2,
+                                                               int R) {
     c3l::pdl_launch_dependents();
     c3l::pdl_wait();
     __shared__ float cs[C3L_GMRES_MAX_ROWS];
+    __shared__ float red[kGmfGroups][kGmfCols];
     const int k = *cur + 1;
     gm_reduce_f(partial1, R, gridDim.x, k, cs);
     __syncthreads();
@@ -1280,31 +1313,26 @@ __global__ void __launch_bounds__(kThreads) k_gm_axpy_dot_f(const float* __restr
         for (int r = threadIdx.x; r <= k; r += blockDim.x) c1[r] = cs[r];
     const int64_t lo = (int64_t)blockIdx.x * seg;
     const int64_t hi = min(n, lo + seg);
-    for (int64_t c = lo + threadIdx.x; c < hi; c += blockDim.x) {
-        float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f, s3 = 0.0f;
-        int r = 0;
-        for (; r + 3 < k; r += 4) {
-            s0 = fmaf(cs[r], V[(int64_t)r * ld + c], s0);
-            s1 = fmaf(cs[r + 1], V[(int64_t)(r + 1) * ld + c], s1);
-            s2 = fmaf(cs[r + 2], V[(int64_t)(r + 2) * ld + c], s2);
-            s3 = fmaf(cs[r + 3], V[(int64_t)(r + 3) * ld + c], s3);
-        }
-        for (; r < k; ++r) s0 = fmaf(cs[r], V[(int64_t)r * ld + c], s0);
-        wf[c] -= (s0 + s1) + (s2 + s3);
+    const int g = threadIdx.x / kGmfCols, cl = threadIdx.x % kGmfCols;
+    for (int64_t base = lo; base < hi; base += kGmfCols) {
+        const int64_t col = base + cl;
+        const float t = gm_combine_f(V, ld, k, cs, col, col < hi, red);
+        if (g == 0 && col < hi) wf[col] -= t;
+        __syncthreads();  // red is reused; the new wf is visible to the partials below
     }
-    __syncthreads();
     gm_partials_f(V, ld, k, wf, lo, hi, partial2, R);
 }
 
-__global__ void __launch_bounds__(kThreads) k_gm_scale_f(float* V, int64_t ld, const int* cur, int* next,
-                                                         const float* __restrict__ partial2, int R, int nb,
-                                                         const float* __restrict__ c1, double eps,
-                                                         const float* __restrict__ wf, int64_t n,
-                                                         double* __restrict__ xnext, double* __restrict__ slots,
-                                                         int stride) {
+__global__ void __launch_bounds__(kGmfThreads) k_gm_scale_f(float* V, int64_t ld, const int* cur, int* next,
+                                                            const float* __restrict__ partial2, int R, int nb,
+                                                            const float* __restrict__ c1, double eps,
+                                                            const float* __restrict__ wf, int64_t n,
+                                                            double* __restrict__ xnext, double* __restrict__ slots,
+                                                            int stride) {
     c3l::pdl_launch_dependents();
     c3l::pdl_wait();
     __shared__ float cs[C3L_GMRES_MAX_ROWS];
+    __shared__ float red[kGmfGroups][kGmfCols];
     __shared__ float hh[2];
     const int k = *cur + 1;
     gm_reduce_f(partial2, R, nb, k, cs);
@@ -1331,19 +1359,16 @@ __global__ void __launch_bounds__(kThreads) k_gm_scale_f(float* V, int64_t ld, c
         }
     }
     float* Vk = V + (int64_t)k * ld;
-    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
-        float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f, s3 = 0.0f;
-        int r = 0;
-        for (; r + 3 < k; r += 4) {
-            s0 = fmaf(cs[r], V[(int64_t)r * ld + c], s0);
-            s1 = fmaf(cs[r + 1], V[(int64_t)(r + 1) * ld + c], s1);
-            s2 = fmaf(cs[r + 2], V[(int64_t)(r + 2) * ld + c], s2);
-            s3 = fmaf(cs[r + 3], V[(int64_t)(r + 3) * ld + c], s3);
+    const int g = threadIdx.x / kGmfCols, cl = threadIdx.x % kGmfCols;
+    for (int64_t base = (int64_t)blockIdx.x * kGmfCols; base < n; base += (int64_t)gridDim.x * kGmfCols) {
+        const int64_t col = base + cl;
+        const float t = gm_combine_f(V, ld, k, cs, col, col < n, red);
+        if (g == 0 && col < n) {
+            const float x = (wf[col] - t) * inv;
+            Vk[col] = x;
+            xnext[col] = (double)x;
         }
-        for (; r < k; ++r) s0 = fmaf(cs[r], V[(int64_t)r * ld + c], s0);
-        const float x = (wf[c] - ((s0 + s1) + (s2 + s3))) * inv;
-        Vk[c] = x;
-        xnext[c] = (double)x;
+        __syncthreads();  // red is reused
     }
 }
 
@@ -1424,31 +1449,31 @@ static bool valid_batch(const ArnoldiBatch& bt, bool with_partial) {
 
 c3l_status arnoldi_dot1(const ArnoldiBatch& bt, int par, int64_t ld, int64_t dim, const RowDot& p, cudaStream_t s) {
     if (!valid_batch(bt, false) || dim <= 0 || ld < dim || (par & ~1)) return C3L_ERR_ARGUMENT;
-    return launch_pdl(k_arn_dot1, dim3(p.grid, (unsigned)bt.nb), dim3(kThreads), 0, s, 0, false, bt, par, ld, dim);
+    return launch_pdl(k_arn_dot1, dim3(p.grid, (unsigned)bt.nb), dim3(kThreads), 0, s, 0, true, bt, par, ld, dim);
 }
 
 c3l_status arnoldi_axpy1(const ArnoldiBatch& bt, int par, int64_t ld, int max_k, int64_t dim, cudaStream_t s) {
     if (!valid_batch(bt, false) || dim <= 0 || ld < dim || (par & ~1)) return C3L_ERR_ARGUMENT;
     (void)max_k;
-    return launch_pdl(k_arn_axpy<kAxX, kAxY>, dim3(axpy_grid(dim), (unsigned)bt.nb), dim3(kAxX, kAxY), 0, s, 0, false, bt, par,
+    return launch_pdl(k_arn_axpy<kAxX, kAxY>, dim3(axpy_grid(dim), (unsigned)bt.nb), dim3(kAxX, kAxY), 0, s, 0, true, bt, par,
                       ld, dim);
 }
 
 c3l_status arnoldi_dot2(const ArnoldiBatch& bt, int par, int64_t ld, int64_t dim, const RowDot& p, int64_t ldc,
                         cudaStream_t s) {
     if (!valid_batch(bt, p.nseg > 1) || dim <= 0 || ld < dim || (par & ~1)) return C3L_ERR_ARGUMENT;
-    c3l_status r = launch_pdl(k_arn_dot2, dim3(p.grid, (unsigned)bt.nb), dim3(kThreads), 0, s, 0, false, bt, par, ld, dim,
+    c3l_status r = launch_pdl(k_arn_dot2, dim3(p.grid, (unsigned)bt.nb), dim3(kThreads), 0, s, 0, true, bt, par, ld, dim,
                               p.nseg, p.seglen, ldc);
     if (r || p.nseg == 1) return r;
     const unsigned g = (unsigned)(p.max_rows > 1024 ? 1024 : p.max_rows);
-    return launch_pdl(k_arn_dot2_final, dim3(g, (unsigned)bt.nb), dim3(kThreads), 0, s, 0, false, bt, par, p.nseg, ldc);
+    return launch_pdl(k_arn_dot2_final, dim3(g, (unsigned)bt.nb), dim3(kThreads), 0, s, 0, true, bt, par, p.nseg, ldc);
 }
 
 c3l_status arnoldi_scale(const ArnoldiBatch& bt, int par, int64_t ld, int max_k, double tol, int64_t n,
                          cudaStream_t s) {
     if (!valid_batch(bt, false) || n <= 0 || ld < n || (par & ~1)) return C3L_ERR_ARGUMENT;
     (void)max_k;
-    return launch_pdl(k_arn_scale<kAxX, kAxY>, dim3(axpy_grid(n), (unsigned)bt.nb), dim3(kAxX, kAxY), 0, s, 0, false, bt, par,
+    return launch_pdl(k_arn_scale<kAxX, kAxY>, dim3(axpy_grid(n), (unsigned)bt.nb), dim3(kAxX, kAxY), 0, s, 0, true, bt, par,
                       ld, n, tol);
 }
 
@@ -1495,14 +1520,14 @@ c3l_status gm_scale(double* V, int64_t ld, const int* cur, int* next, const doub
 c3l_status gm_dot_f32(const float* V, int64_t ld, const int* cur, const double* w, float* wf, int64_t n,
                       const GmPlan& p, float* partial, cudaStream_t s) {
     if (!V || !cur || !w || !wf || !partial || n <= 0 || p.R > C3L_GMRES_MAX_ROWS) return C3L_ERR_ARGUMENT;
-    return launch_pdl(k_gm_dot_f, dim3(p.blocks), dim3(kThreads), 0, s, 0, true, V, ld, cur, w, wf, n, p.seg, partial, p.R);
+    return launch_pdl(k_gm_dot_f, dim3(p.blocks), dim3(kGmfThreads), 0, s, 0, true, V, ld, cur, w, wf, n, p.seg, partial, p.R);
 }
 
 c3l_status gm_axpy_dot_f32(const float* V, int64_t ld, const int* cur, float* c1, float* wf, int64_t n,
                            const GmPlan& p, float* partial, cudaStream_t s) {
     if (!V || !cur || !c1 || !wf || !partial || n <= 0 || p.R > C3L_GMRES_MAX_ROWS) return C3L_ERR_ARGUMENT;
     const int64_t half = (int64_t)p.blocks * p.R;
-    return launch_pdl(k_gm_axpy_dot_f, dim3(p.blocks), dim3(kThreads), 0, s, 0, true, V, ld, cur, (const float*)partial, c1,
+    return launch_pdl(k_gm_axpy_dot_f, dim3(p.blocks), dim3(kGmfThreads), 0, s, 0, true, V, ld, cur, (const float*)partial, c1,
                       wf, n, p.seg, partial + half, p.R);
 }
 
@@ -1511,7 +1536,7 @@ c3l_status gm_scale_f32(float* V, int64_t ld, const int* cur, int* next, const f
                         int stride, cudaStream_t s) {
     if (!V || !cur || !next || !partial || !c1 || !wf || !xnext || !slots || n <= 0) return C3L_ERR_ARGUMENT;
     const int64_t half = (int64_t)p.blocks * p.R;
-    return launch_pdl(k_gm_scale_f, dim3(p.scale_grid), dim3(kThreads), 0, s, 0, true, V, ld, cur, next,
+    return launch_pdl(k_gm_scale_f, dim3(p.scale_grid), dim3(kGmfThreads), 0, s, 0, true, V, ld, cur, next,
                       (const float*)(partial + half), p.R, (int)p.blocks, c1, eps, wf, n, xnext, slots, stride);
 }
 

@@ -86,7 +86,8 @@ struct Batch {
     float2* out32[C3L_MAX_BATCH];       // optional FP32 copy of the EOM output
     const int32_t* stop[C3L_MAX_BATCH];
     int nb;
-    bool pdl;  // launch with programmatic dependent launch (the static operator's path)
+    bool pdl;         // launch with programmatic dependent launch
+    bool pdl_at_exit; // dependents launch only as the blocks exit (no early trigger)
 };
 
 template <typename C>
@@ -142,7 +143,7 @@ __global__ void k_unpack_scatter(int64_t dim, const double* __restrict__ x, cons
 template <typename C>
 __global__ void k_scatter(int64_t count, const int64_t* __restrict__ dst, const int64_t* __restrict__ pos,
                           const double* __restrict__ sign, Batch<C> bt) {
-    c3l::pdl_launch_dependents();
+    if (!bt.pdl_at_exit) c3l::pdl_launch_dependents();
     if (batch_stopped(bt)) return;
     c3l::pdl_wait();
     const double2* __restrict__ vec = bt.in[blockIdx.y];
@@ -216,7 +217,7 @@ __device__ __forceinline__ void contract_entry(const c3l_contract_task& task, in
 template <typename C>
 __global__ void __launch_bounds__(kThreads) k_contract(c3l_contract_level lv, int n, const C* __restrict__ vectors,
                                                         Batch<C> bt) {
-    c3l::pdl_launch_dependents();
+    if (!bt.pdl_at_exit) c3l::pdl_launch_dependents();
     if (batch_stopped(bt)) return;
     C* __restrict__ ws = bt.ws[blockIdx.y];
     const c3l_tile tile = lv.tiles[blockIdx.x];
@@ -246,7 +247,7 @@ struct LevelPack {
 template <typename C>
 __global__ void __launch_bounds__(kThreads) k_contract_cluster(LevelPack pack, int n, const C* __restrict__ vectors,
                                                                 Batch<C> bt) {
-    c3l::pdl_launch_dependents();
+    if (!bt.pdl_at_exit) c3l::pdl_launch_dependents();
     if (batch_stopped(bt)) return;
     C* __restrict__ ws = bt.ws[blockIdx.y];
     // Every level has at most gridDim.x tiles (the launcher's condition), so a
@@ -308,7 +309,7 @@ __device__ __forceinline__ double2 dmul(double2 a, double2 b) {
 template <int MODE, typename C, int kWE>
 __global__ void __launch_bounds__(kThreads) k_wedge(c3l_wedge_stage st, int n, Batch<C> bt, Epilogue ep) {
     constexpr int kWG = kThreads / kWE;
-    c3l::pdl_launch_dependents();
+    if (!bt.pdl_at_exit) c3l::pdl_launch_dependents();
     if (batch_stopped(bt)) return;
     C* __restrict__ ws = bt.ws[blockIdx.y];
     __shared__ c3l_instance sinst[kInstChunk];
@@ -570,10 +571,12 @@ bool same_program(const c3l_action& a, const c3l_action& b) {
 
 template <typename C>
 c3l_status eom_sigma(const c3l_eom_action* ea, int nb, const c3l_complex* const* xin, c3l_complex* const* out,
-                     c3l_complex32* const* out32, const int32_t* const* stop, cudaStream_t s) {
+                     c3l_complex32* const* out32, const int32_t* const* stop, cudaStream_t s, bool pdl = false) {
     if (!ea || nb < 1 || nb > C3L_MAX_BATCH || !xin || !out) return C3L_ERR_ARGUMENT;
     Batch<C> bt{};
     bt.nb = nb;
+    bt.pdl = pdl;
+    bt.pdl_at_exit = true;
     for (int b = 0; b < nb; ++b) {
         if (!xin[b] || !out[b] || !valid_action(&ea[b].action) || !ea[b].lam) return C3L_ERR_ARGUMENT;
         if (b > 0 && (!same_program(ea[b].action, ea[0].action) || ea[b].lam != ea[0].lam)) return C3L_ERR_ARGUMENT;
@@ -598,7 +601,7 @@ namespace c3l {
 c3l_status eom_sigma_batch(const c3l_eom_action* actions, int nb, const c3l_complex* const* xin,
                            c3l_complex* const* out, c3l_complex32* const* out32, const int32_t* const* stop,
                            cudaStream_t s) {
-    return eom_sigma<double2>(actions, nb, xin, out, out32, stop, s);
+    return eom_sigma<double2>(actions, nb, xin, out, out32, stop, s, true);
 }
 
 bool same_sigma_program(const c3l_eom_action& a, const c3l_eom_action& b) {
