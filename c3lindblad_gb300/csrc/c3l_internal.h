@@ -63,7 +63,8 @@ c3l_status arnoldi_axpy1(const ArnoldiBatch& bt, int par, int64_t ld, int max_k,
 // column k - 1 of Hc = (c1 + c2 | h), *hval = h, counters[1 - par] = k
 c3l_status arnoldi_dot2(const ArnoldiBatch& bt, int par, int64_t ld, int64_t dim, const RowDot& p, int64_t ldc,
                         cudaStream_t s);
-// V[k] = xnext = (w - V[0 : k]^T c2) / h (unscaled when h <= tol), V32[k] = (float) V[k]
+// V[k] = xnext = (w - V[0 : k]^T c2) / h (unscaled when h <= tol), V32[k] = (float) V[k];
+// V c2 from FP32 products of the FP32 rows (c2 is the small second-pass correction)
 c3l_status arnoldi_scale(const ArnoldiBatch& bt, int par, int64_t ld, int max_k, double tol, int64_t n,
                          cudaStream_t s);
 

@@ -1022,27 +1022,70 @@ __global__ void __launch_bounds__(kThreads) k_arn_dot2_final(c3l::ArnoldiBatch b
 }
 
 // Second update and normalization: V[k] = xnext = (w' - V c2) / h, unscaled
-// when h <= tol (breakdown, detected by the shifted solves).  Reads the step
-// index from `cur` of the parity (the column tail already wrote `next`).
+// when h <= tol (breakdown, detected by the shifted solves); V32[k] gets its
+// FP32 copy.  c2 is the small correction left by the FP32 first pass (about
+// 1e-7 |w'|), so V c2 is formed with FP32 products from the FP32 rows: its
+// error, about 6e-8 |V c2|, is near 1e-14 |w|; the subtraction and the
+// scaling are FP64.  The projections c2 stay FP64 in the Hessenberg column.
+// Reads the step index from `cur` of the parity (the column tail already
+// wrote `next`).
 template <int X, int Y>
 __global__ void __launch_bounds__(X * Y) k_arn_scale(c3l::ArnoldiBatch bt, int par, int64_t ld, int64_t n,
                                                      double tol) {
-    __shared__ double2 part[Y][X];
+    __shared__ float2 part[Y][X];
+    __shared__ float2 cf[C3L_MAX_HESSENBERG];
     if (arn_stopped(bt)) return;  // dependents launch as the blocks exit
     c3l::pdl_wait();
     const int b = blockIdx.y;
     const int k = bt.counters[b][par] + 1;
     const double h = *bt.hval[b];
     const double inv = h > tol ? 1.0 / h : 1.0;
+    const int tid = threadIdx.y * X + threadIdx.x;
+    for (int r = tid; r < k; r += X * Y) {
+        const double2 c = bt.c2[b][r];
+        cf[r] = make_float2((float)c.x, (float)c.y);
+    }
+    __syncthreads();
+    const float2* __restrict__ V32 = bt.V32[b];
     double2* Vk = bt.V[b] + (int64_t)k * ld;
     float2* V32k = bt.V32[b] + (int64_t)k * ld;
     const double2* __restrict__ w = bt.w[b];
     double2* __restrict__ xnext = bt.xnext[b];
     for (int64_t base = (int64_t)blockIdx.x * X; base < n; base += (int64_t)gridDim.x * X) {
         const int64_t i = base + threadIdx.x;
-        const double2 t = arn_combine<X, Y>(bt.V[b], ld, k, bt.c2[b], i, n, part);
+        float2 s = make_float2(0.0f, 0.0f);
+        if (i < n) {
+            int j = threadIdx.y;
+            for (; j + 3 * Y < k; j += 4 * Y) {
+                float2 v[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) v[u] = V32[(int64_t)(j + u * Y) * ld + i];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const float2 c = cf[j + u * Y];
+                    s.x = fmaf(c.x, v[u].x, fmaf(-c.y, v[u].y, s.x));
+                    s.y = fmaf(c.x, v[u].y, fmaf(c.y, v[u].x, s.y));
+                }
+            }
+            for (; j < k; j += Y) {
+                const float2 c = cf[j], v = V32[(int64_t)j * ld + i];
+                s.x = fmaf(c.x, v.x, fmaf(-c.y, v.y, s.x));
+                s.y = fmaf(c.x, v.y, fmaf(c.y, v.x, s.y));
+            }
+        }
+        part[threadIdx.y][threadIdx.x] = s;
+        __syncthreads();
+        for (int hh = Y / 2; hh > 0; hh >>= 1) {
+            if ((int)threadIdx.y < hh) {
+                const float2 o = part[threadIdx.y + hh][threadIdx.x];
+                part[threadIdx.y][threadIdx.x].x += o.x;
+                part[threadIdx.y][threadIdx.x].y += o.y;
+            }
+            __syncthreads();
+        }
         if (threadIdx.y == 0 && i < n) {
-            const double2 x = make_double2((w[i].x - t.x) * inv, (w[i].y - t.y) * inv);
+            const float2 t = part[0][threadIdx.x];
+            const double2 x = make_double2((w[i].x - (double)t.x) * inv, (w[i].y - (double)t.y) * inv);
             Vk[i] = x;
             V32k[i] = make_float2((float)x.x, (float)x.y);
             xnext[i] = x;
@@ -1472,7 +1515,7 @@ c3l_status arnoldi_dot2(const ArnoldiBatch& bt, int par, int64_t ld, int64_t dim
 c3l_status arnoldi_scale(const ArnoldiBatch& bt, int par, int64_t ld, int max_k, double tol, int64_t n,
                          cudaStream_t s) {
     if (!valid_batch(bt, false) || n <= 0 || ld < n || (par & ~1)) return C3L_ERR_ARGUMENT;
-    (void)max_k;
+    if (max_k > C3L_MAX_HESSENBERG) return C3L_ERR_CAPACITY;  // c2 is staged in shared memory
     return launch_pdl(k_arn_scale<kAxX, kAxY>, dim3(axpy_grid(n), (unsigned)bt.nb), dim3(kAxX, kAxY), 0, s, 0, true, bt, par,
                       ld, n, tol);
 }
