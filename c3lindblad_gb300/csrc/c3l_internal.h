@@ -53,18 +53,22 @@ struct ArnoldiBatch {
     double2* Hc[C3L_MAX_BATCH];
     double2* partial[C3L_MAX_BATCH];
     float2* V32[C3L_MAX_BATCH];   // FP32 copy of the basis rows (written with each row)
-    float2* w32[C3L_MAX_BATCH];   // FP32 copy of the operator output (written by the sigma)
+    float2* w32[C3L_MAX_BATCH];   // FP32 copy of the operator output (sigma), then of w' (first update)
+    float2* V32lo[C3L_MAX_BATCH]; // V - V32 in FP32: rows as FP32 (hi, lo) pairs
+    float2* w32lo[C3L_MAX_BATCH]; // w' - w32 in FP32 (first update)
 };
 // pass 1 (FP32, from the FP32 copies V32 and w32): c1[r] = V[r]^H w, r < k = counters[par] + 1
 c3l_status arnoldi_dot1(const ArnoldiBatch& bt, int par, int64_t ld, int64_t dim, const RowDot& p, cudaStream_t s);
-// w -= V[0 : k]^T c1
+// w -= V[0 : k]^T c1 (FP64); (w32, w32lo) receive the FP32 (hi, lo) pair of the result
 c3l_status arnoldi_axpy1(const ArnoldiBatch& bt, int par, int64_t ld, int max_k, int64_t dim, cudaStream_t s);
-// pass 2 (FP64): c2[r] = V[r]^H w, c2[k] = |w|^2, h = sqrt(|w|^2 - |c2|^2),
+// pass 2 (double-float products and sums on the FP32 pipe from the (hi, lo)
+// pairs of the rows and of w, finished in FP64): c2[r] = V[r]^H w, c2[k] = |w|^2, h = sqrt(|w|^2 - |c2|^2),
 // column k - 1 of Hc = (c1 + c2 | h), *hval = h, counters[1 - par] = k
 c3l_status arnoldi_dot2(const ArnoldiBatch& bt, int par, int64_t ld, int64_t dim, const RowDot& p, int64_t ldc,
                         cudaStream_t s);
 // V[k] = xnext = (w - V[0 : k]^T c2) / h (unscaled when h <= tol), V32[k] = (float) V[k];
-// V c2 from FP32 products of the FP32 rows (c2 is the small second-pass correction)
+// V c2 from FP32 products of the FP32 rows (c2 is the small second-pass correction);
+// V32lo[k] = (float)(V[k] - V32[k])
 c3l_status arnoldi_scale(const ArnoldiBatch& bt, int par, int64_t ld, int max_k, double tol, int64_t n,
                          cudaStream_t s);
 
@@ -112,6 +116,8 @@ c3l_status gm_axpy_dot_f32(const float* V, int64_t ld, const int* cur, float* c1
 c3l_status gm_scale_f32(float* V, int64_t ld, const int* cur, int* next, const float* partial, const float* c1,
                         double eps, const float* wf, int64_t n, const GmPlan& p, double* xnext, double* slots,
                         int stride, cudaStream_t s);
+// FP32 (hi, lo) pair of a complex FP64 vector: hi = (float) x, lo = (float)(x - hi)
+c3l_status split_c(int64_t n, const c3l_complex* x, c3l_complex32* hi, c3l_complex32* lo, cudaStream_t s);
 // V0 = (float)(a r) and x = V0 (FP64 copy)
 c3l_status gm_start_f32(int64_t n, double a, const double* r, float* V0, double* x, cudaStream_t s);
 // x += V[0 : k]^T y (FP32 rows, FP64 arithmetic)

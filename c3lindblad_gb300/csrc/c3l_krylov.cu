@@ -820,6 +820,34 @@ __device__ __forceinline__ bool last_block(unsigned* done) {
 
 __device__ __forceinline__ bool arn_stopped(const c3l::ArnoldiBatch& bt) { return bt.counters[blockIdx.y][3] != 0; }
 
+// Double-float arithmetic on the FP32 pipe (a value is an unevaluated sum hi + lo
+// of two floats).  two_sum is Knuth's error-free addition, the product split
+// p + e = a_hi b_hi uses one FMA (Dekker's product with a fused multiply-add);
+// the cross terms a_hi b_lo + a_lo b_hi are added to the error term and
+// a_lo b_lo (2^-48 relative) is dropped.  The _rn intrinsics keep the compiler
+// from contracting the additions into FMAs, which would break the
+// transformations.
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+// (S, C) += (ahi + alo)(bhi + blo)
+__device__ __forceinline__ void df_mac(float& S, float& C, float ahi, float alo, float bhi, float blo) {
+    const float p = __fmul_rn(ahi, bhi);
+    float e = fmaf(ahi, bhi, -p);
+    e = fmaf(ahi, blo, fmaf(alo, bhi, e));
+    float s, t;
+    two_sum(S, p, s, t);
+    S = s;
+    C = __fadd_rn(C, __fadd_rn(t, e));
+}
+// FP32 (hi, lo) pair of a double
+__device__ __forceinline__ void split_d(double x, float& hi, float& lo) {
+    hi = (float)x;
+    lo = (float)(x - (double)hi);
+}
+
 // Pass 1 in FP32 from the FP32 copies of the basis rows and of w: c1[r] =
 // V[r]^H w (one block per row).  The second pass, in FP64, measures and
 // removes what the first left, and the column is c1 + c2, so the Arnoldi
@@ -928,7 +956,15 @@ __global__ void __launch_bounds__(X * Y) k_arn_axpy(c3l::ArnoldiBatch bt, int pa
     for (int64_t base = (int64_t)blockIdx.x * X; base < dim; base += (int64_t)gridDim.x * X) {
         const int64_t i = base + threadIdx.x;
         const double2 t = arn_combine<X, Y>(bt.V[b], ld, k, bt.c1[b], i, dim, part);
-        if (threadIdx.y == 0 && i < dim) w[i] = make_double2(w[i].x - t.x, w[i].y - t.y);
+        if (threadIdx.y == 0 && i < dim) {
+            const double2 x = make_double2(w[i].x - t.x, w[i].y - t.y);
+            w[i] = x;
+            float2 hi, lo;
+            split_d(x.x, hi.x, lo.x);
+            split_d(x.y, hi.y, lo.y);
+            bt.w32[b][i] = hi;
+            bt.w32lo[b][i] = lo;
+        }
         __syncthreads();
     }
 }
@@ -953,10 +989,13 @@ __device__ void arnoldi_column_tail(const double2* __restrict__ c1, const double
     }
 }
 
-// Pass 2 in FP64: rows [0, k) and the vector itself (|w'|^2) in nseg segments
-// of seglen, one block per (row, segment) item; with one segment the block
-// writes c2[row] and the block that finishes last forms the column, otherwise
-// it writes partial[row][seg] for k_arn_dot2_final.  Every block reaches the
+// Pass 2: rows [0, k) and the vector itself (|w'|^2) in nseg segments of
+// seglen, one block per (row, segment) item.  Each thread accumulates its
+// entries of conj(V[row]) w' in double-float from the FP32 (hi, lo) pairs of
+// the row and of w' (error about 4e-15 of sum |V_i| |w'_i| <= |w'|), and the
+// block adds the threads' sums in FP64.  With one segment the block writes
+// c2[row] and the block that finishes last forms the column, otherwise it
+// writes partial[row][seg] for k_arn_dot2_final.  Every block reaches the
 // last-block count.
 __global__ void __launch_bounds__(kThreads) k_arn_dot2(c3l::ArnoldiBatch bt, int par, int64_t ld, int64_t dim,
                                                        int nseg, int64_t seglen, int64_t ldc) {
@@ -964,31 +1003,30 @@ __global__ void __launch_bounds__(kThreads) k_arn_dot2(c3l::ArnoldiBatch bt, int
     if (arn_stopped(bt)) return;  // dependents launch as the blocks exit
     c3l::pdl_wait();
     const int b = blockIdx.y;
-    const double2* __restrict__ V = bt.V[b];
-    const double2* __restrict__ w = bt.w[b];
+    const float2* __restrict__ Vh = bt.V32[b];
+    const float2* __restrict__ Vl = bt.V32lo[b];
+    const float2* __restrict__ wh = bt.w32[b];
+    const float2* __restrict__ wl = bt.w32lo[b];
     int32_t* ctr = bt.counters[b];
     const int k = ctr[par] + 1;
     const int items = (k + 1) * nseg;
     for (int item = blockIdx.x; item < items; item += gridDim.x) {
         const int row = item / nseg;
         const int seg = item - row * nseg;
-        const double2* v = row < k ? V + (int64_t)row * ld : w;
+        const float2* vh = row < k ? Vh + (int64_t)row * ld : wh;
+        const float2* vl = row < k ? Vl + (int64_t)row * ld : wl;
         const int64_t lo = (int64_t)seg * seglen;
         const int64_t hi = min(dim, lo + seglen);
-        const int64_t step = blockDim.x;
-        double2 acc = make_double2(0.0, 0.0);
-        int64_t i = lo + threadIdx.x;
-        for (; i + 3 * step < hi; i += 4 * step) {
-            double2 a[4], c[4];
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                a[u] = v[i + u * step];
-                c[u] = w[i + u * step];
-            }
-#pragma unroll
-            for (int u = 0; u < 4; ++u) dot_acc(acc, a[u], c[u]);
+        // conj(v) w = (vx wx + vy wy) + i (vx wy - vy wx)
+        float rS = 0.0f, rC = 0.0f, iS = 0.0f, iC = 0.0f;
+        for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+            const float2 ah = vh[i], al = vl[i], bh = wh[i], bl = wl[i];
+            df_mac(rS, rC, ah.x, al.x, bh.x, bl.x);
+            df_mac(rS, rC, ah.y, al.y, bh.y, bl.y);
+            df_mac(iS, iC, ah.x, al.x, bh.y, bl.y);
+            df_mac(iS, iC, -ah.y, -al.y, bh.x, bl.x);
         }
-        for (; i < hi; i += step) dot_acc(acc, v[i], w[i]);
+        double2 acc = make_double2((double)rS + (double)rC, (double)iS + (double)iC);
         acc = block_sum_t(acc, sm);
         if (threadIdx.x == 0) {
             if (nseg == 1) bt.c2[b][row] = acc;
@@ -1087,7 +1125,11 @@ __global__ void __launch_bounds__(X * Y) k_arn_scale(c3l::ArnoldiBatch bt, int p
             const float2 t = part[0][threadIdx.x];
             const double2 x = make_double2((w[i].x - (double)t.x) * inv, (w[i].y - (double)t.y) * inv);
             Vk[i] = x;
-            V32k[i] = make_float2((float)x.x, (float)x.y);
+            float2 xh, xl;
+            split_d(x.x, xh.x, xl.x);
+            split_d(x.y, xh.y, xl.y);
+            V32k[i] = xh;
+            bt.V32lo[b][(int64_t)k * ld + i] = xl;
             xnext[i] = x;
         }
         __syncthreads();
@@ -1415,6 +1457,18 @@ __global__ void __launch_bounds__(kGmfThreads) k_gm_scale_f(float* V, int64_t ld
     }
 }
 
+// FP32 (hi, lo) pair of a complex FP64 vector.
+__global__ void k_split_c(int64_t n, const double2* __restrict__ x, float2* __restrict__ hi, float2* __restrict__ lo) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double2 v = x[i];
+        float2 h, l;
+        split_d(v.x, h.x, l.x);
+        split_d(v.y, h.y, l.y);
+        hi[i] = h;
+        lo[i] = l;
+    }
+}
+
 // V0 = (float)(a r) and x = V0 in FP64: the first row of an FP32 basis.
 __global__ void k_gm_start_f(int64_t n, double a, const double* __restrict__ r, float* __restrict__ V0,
                              double* __restrict__ x) {
@@ -1485,7 +1539,8 @@ static bool valid_batch(const ArnoldiBatch& bt, bool with_partial) {
     if (bt.nb < 1 || bt.nb > C3L_MAX_BATCH) return false;
     for (int b = 0; b < bt.nb; ++b)
         if (!bt.V[b] || !bt.w[b] || !bt.xnext[b] || !bt.c1[b] || !bt.c2[b] || !bt.hval[b] || !bt.counters[b] ||
-            !bt.Hc[b] || !bt.V32[b] || !bt.w32[b] || (with_partial && !bt.partial[b]))
+            !bt.Hc[b] || !bt.V32[b] || !bt.w32[b] || !bt.V32lo[b] || !bt.w32lo[b] ||
+            (with_partial && !bt.partial[b]))
             return false;
     return true;
 }
@@ -1581,6 +1636,13 @@ c3l_status gm_scale_f32(float* V, int64_t ld, const int* cur, int* next, const f
     const int64_t half = (int64_t)p.blocks * p.R;
     return launch_pdl(k_gm_scale_f, dim3(p.scale_grid), dim3(kGmfThreads), 0, s, 0, true, V, ld, cur, next,
                       (const float*)(partial + half), p.R, (int)p.blocks, c1, eps, wf, n, xnext, slots, stride);
+}
+
+c3l_status split_c(int64_t n, const c3l_complex* x, c3l_complex32* hi, c3l_complex32* lo, cudaStream_t s) {
+    if (!x || !hi || !lo || n <= 0) return C3L_ERR_ARGUMENT;
+    k_split_c<<<grid_for(n), kThreads, 0, s>>>(n, reinterpret_cast<const double2*>(x), reinterpret_cast<float2*>(hi),
+                                               reinterpret_cast<float2*>(lo));
+    return launch_status();
 }
 
 c3l_status gm_start_f32(int64_t n, double a, const double* r, float* V0, double* x, cudaStream_t s) {

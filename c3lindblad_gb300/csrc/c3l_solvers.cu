@@ -586,7 +586,7 @@ c3l_status c3l_arnoldi(c3l_arnoldi_channel* ch, int32_t nch, int64_t N, const c3
         const c3l_arnoldi_channel& q = ch[c];
         const c3l_hessenberg_state& h = q.hess;
         if (!q.sigma || !q.b || !q.V || !q.Hcol || !q.coeff || !q.partial || !q.host || !q.status_host || !q.work ||
-            !q.counters || !q.V32 || !q.work32 || !h.rot_c || !h.rot_s || !h.vsink || !h.carry || !h.accum || !h.residual || !h.status ||
+            !q.counters || !q.V32 || !q.work32 || !q.V32lo || !q.work32lo || !h.rot_c || !h.rot_s || !h.vsink || !h.carry || !h.accum || !h.residual || !h.status ||
             h.m_max < m_max || h.nshift != nshift || (q.sink_conj && !h.sinkproj_conj))
             return C3L_ERR_ARGUMENT;
     }
@@ -651,6 +651,8 @@ c3l_status c3l_arnoldi(c3l_arnoldi_channel* ch, int32_t nch, int64_t N, const c3
             bt.partial[i] = d2(q.partial);
             bt.V32[i] = reinterpret_cast<float2*>(q.V32);
             bt.w32[i] = reinterpret_cast<float2*>(q.work32);
+            bt.V32lo[i] = reinterpret_cast<float2*>(q.V32lo);
+            bt.w32lo[i] = reinterpret_cast<float2*>(q.work32lo);
         }
         auto step = [&](cudaStream_t cs, int par) -> c3l_status {
             c3l_status r = c3l::eom_sigma_batch(acts.data(), nb, xin.data(), out.data(), out32.data(), stop.data(), cs);
@@ -689,7 +691,7 @@ c3l_status c3l_arnoldi(c3l_arnoldi_channel* ch, int32_t nch, int64_t N, const c3
         q.beta = std::sqrt(std::max(q.host[0].re, 0.0));
         if (!(q.beta > 0.0) || !std::isfinite(q.beta)) return C3L_ERR_ARGUMENT;
         if ((st = c3l_scale_c(N, c3l_complex{1.0 / q.beta, 0.0}, q.b, q.V, sv))) return st;
-        if ((st = c3l_downcast(N, q.V, q.V32, sv))) return st;
+        if ((st = c3l::split_c(N, q.V, q.V32, q.V32lo, s))) return st;
         if ((st = c3l_scale_c(N, c3l_complex{1.0 / q.beta, 0.0}, q.b, q.work, sv))) return st;
         if (cudaMemsetAsync(q.counters, 0, 4 * sizeof(int32_t), s) != cudaSuccess) return C3L_ERR_LAUNCH;
         q.launches += (N > 8192 ? 2 : 1) + 3;

@@ -278,6 +278,8 @@ def arnoldi_channels(ops, sources, shifts: torch.Tensor, *, maximum_dimension: i
             "counters": torch.zeros(4, dtype=torch.int32, device=dev),
             "V32": torch.empty((m_max + 1, N), dtype=torch.complex64, device=dev),
             "work32": torch.empty(N, dtype=torch.complex64, device=dev),
+            "V32lo": torch.empty((m_max + 1, N), dtype=torch.complex64, device=dev),
+            "work32lo": torch.empty(N, dtype=torch.complex64, device=dev),
             "b": b,
         }
         d["cres"] = np.zeros(d["cdims"].size, dtype=np.float64)
@@ -291,6 +293,7 @@ def arnoldi_channels(ops, sources, shifts: torch.Tensor, *, maximum_dimension: i
         q.status_host = d["hess"].status_host.data_ptr()
         q.work, q.counters = d["work"].data_ptr(), d["counters"].data_ptr()
         q.V32, q.work32 = d["V32"].data_ptr(), d["work32"].data_ptr()
+        q.V32lo, q.work32lo = d["V32lo"].data_ptr(), d["work32lo"].data_ptr()
         q.check_dims, q.check_res, q.check_capacity = d["cdims"].ctypes.data, d["cres"].ctypes.data, d["cdims"].size
     for st in streams:
         st.wait_stream(cur)

@@ -453,6 +453,8 @@ typedef struct {
     int32_t* counters;                 /* device [4] (int32)                      */
     c3l_complex32* V32;                /* device (m_max+1) x N: FP32 copy of the basis rows */
     c3l_complex32* work32;             /* device [N]: FP32 copy of each sigma output        */
+    c3l_complex32* V32lo;              /* device (m_max+1) x N: V - V32 in FP32 (low parts) */
+    c3l_complex32* work32lo;           /* device [N]: low part of the updated work vector   */
     int32_t* check_dims;               /* host [check_capacity]                   */
     double* check_res;                 /* host [check_capacity]                   */
     int32_t check_capacity;
