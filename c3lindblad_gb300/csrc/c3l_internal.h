@@ -59,7 +59,8 @@ struct ArnoldiBatch {
 };
 // pass 1 (FP32, from the FP32 copies V32 and w32): c1[r] = V[r]^H w, r < k = counters[par] + 1
 c3l_status arnoldi_dot1(const ArnoldiBatch& bt, int par, int64_t ld, int64_t dim, const RowDot& p, cudaStream_t s);
-// w -= V[0 : k]^T c1 (FP64); (w32, w32lo) receive the FP32 (hi, lo) pair of the result
+// w -= V[0 : k]^T c1 (double-float products and sums from the FP32 (hi, lo) rows, FP64
+// subtraction); (w32, w32lo) receive the FP32 (hi, lo) pair of the result
 c3l_status arnoldi_axpy1(const ArnoldiBatch& bt, int par, int64_t ld, int max_k, int64_t dim, cudaStream_t s);
 // pass 2 (double-float products and sums on the FP32 pipe from the (hi, lo)
 // pairs of the rows and of w, finished in FP64): c2[r] = V[r]^H w, c2[k] = |w|^2, h = sqrt(|w|^2 - |c2|^2),

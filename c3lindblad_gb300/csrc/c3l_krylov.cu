@@ -910,53 +910,56 @@ __global__ void __launch_bounds__(kThreads) k_arn_dot1(c3l::ArnoldiBatch bt, int
     }
 }
 
-// t = V[0 : k]^T c for the block's X entries (Y partial rows, reduced in
-// shared memory); valid in threadIdx.y == 0.
-template <int X, int Y>
-__device__ __forceinline__ double2 arn_combine(const double2* __restrict__ V, int64_t ld, int k,
-                                               const double2* __restrict__ c, int64_t i, int64_t dim,
-                                               double2 (&part)[Y][X]) {
-    double2 s = make_double2(0.0, 0.0);
-    if (i < dim) {
-        int j = threadIdx.y;
-        for (; j + 3 * Y < k; j += 4 * Y) {  // four independent loads in flight
-            double2 cj[4], v[4];
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                cj[u] = c[j + u * Y];
-                v[u] = V[(int64_t)(j + u * Y) * ld + i];
-            }
-#pragma unroll
-            for (int u = 0; u < 4; ++u) axpy_acc(s, cj[u], v[u]);
-        }
-        for (; j < k; j += Y) axpy_acc(s, c[j], V[(int64_t)j * ld + i]);
-    }
-    part[threadIdx.y][threadIdx.x] = s;
-    __syncthreads();
-    for (int h = Y / 2; h > 0; h >>= 1) {
-        if ((int)threadIdx.y < h) {
-            double2 t = part[threadIdx.y][threadIdx.x];
-            dot_acc_plain(t, part[threadIdx.y + h][threadIdx.x]);
-            part[threadIdx.y][threadIdx.x] = t;
-        }
-        __syncthreads();
-    }
-    return part[0][threadIdx.x];
-}
-
-// First update: w -= V c1.
+// First update: w' = w - V c1, in double-float on the FP32 pipe.  c1 comes from
+// the FP32 first pass, so every coefficient is exactly a float; each product
+// c1_r V_r splits exactly (one FMA) against the row's FP32 (hi, lo) pair, the
+// products are summed by TwoSum per row group, the groups' sums are finished
+// in FP64, and the subtraction from w is FP64 (error about 4e-15 of
+// sum |c1_r V_r,i|, i.e. near 1e-14 |w|).  The FP32 (hi, lo) pair of w' goes
+// to (w32, w32lo) for the second projections.
 template <int X, int Y>
 __global__ void __launch_bounds__(X * Y) k_arn_axpy(c3l::ArnoldiBatch bt, int par, int64_t ld, int64_t dim) {
     __shared__ double2 part[Y][X];
+    __shared__ float2 cf[C3L_MAX_HESSENBERG];
     if (arn_stopped(bt)) return;  // dependents launch as the blocks exit
     c3l::pdl_wait();
     const int b = blockIdx.y;
     const int k = bt.counters[b][par] + 1;
+    const int tid = threadIdx.y * X + threadIdx.x;
+    for (int r = tid; r < k; r += X * Y) {
+        const double2 c = bt.c1[b][r];
+        cf[r] = make_float2((float)c.x, (float)c.y);  // exact: c1 holds FP32 sums
+    }
+    __syncthreads();
+    const float2* __restrict__ Vh = bt.V32[b];
+    const float2* __restrict__ Vl = bt.V32lo[b];
     double2* __restrict__ w = bt.w[b];
     for (int64_t base = (int64_t)blockIdx.x * X; base < dim; base += (int64_t)gridDim.x * X) {
         const int64_t i = base + threadIdx.x;
-        const double2 t = arn_combine<X, Y>(bt.V[b], ld, k, bt.c1[b], i, dim, part);
+        // c v = (cx vx - cy vy) + i (cx vy + cy vx)
+        float rS = 0.0f, rC = 0.0f, iS = 0.0f, iC = 0.0f;
+        if (i < dim) {
+            for (int j = threadIdx.y; j < k; j += Y) {
+                const float2 c = cf[j];
+                const float2 vh = Vh[(int64_t)j * ld + i], vl = Vl[(int64_t)j * ld + i];
+                df_mac(rS, rC, c.x, 0.0f, vh.x, vl.x);
+                df_mac(rS, rC, -c.y, 0.0f, vh.y, vl.y);
+                df_mac(iS, iC, c.x, 0.0f, vh.y, vl.y);
+                df_mac(iS, iC, c.y, 0.0f, vh.x, vl.x);
+            }
+        }
+        part[threadIdx.y][threadIdx.x] = make_double2((double)rS + (double)rC, (double)iS + (double)iC);
+        __syncthreads();
+        for (int h = Y / 2; h > 0; h >>= 1) {
+            if ((int)threadIdx.y < h) {
+                double2 t = part[threadIdx.y][threadIdx.x];
+                dot_acc_plain(t, part[threadIdx.y + h][threadIdx.x]);
+                part[threadIdx.y][threadIdx.x] = t;
+            }
+            __syncthreads();
+        }
         if (threadIdx.y == 0 && i < dim) {
+            const double2 t = part[0][threadIdx.x];
             const double2 x = make_double2(w[i].x - t.x, w[i].y - t.y);
             w[i] = x;
             float2 hi, lo;
@@ -1552,7 +1555,7 @@ c3l_status arnoldi_dot1(const ArnoldiBatch& bt, int par, int64_t ld, int64_t dim
 
 c3l_status arnoldi_axpy1(const ArnoldiBatch& bt, int par, int64_t ld, int max_k, int64_t dim, cudaStream_t s) {
     if (!valid_batch(bt, false) || dim <= 0 || ld < dim || (par & ~1)) return C3L_ERR_ARGUMENT;
-    (void)max_k;
+    if (max_k > C3L_MAX_HESSENBERG) return C3L_ERR_CAPACITY;  // c1 is staged in shared memory
     return launch_pdl(k_arn_axpy<kAxX, kAxY>, dim3(axpy_grid(dim), (unsigned)bt.nb), dim3(kAxX, kAxY), 0, s, 0, true, bt, par,
                       ld, dim);
 }
