@@ -842,6 +842,22 @@ __device__ __forceinline__ void df_mac(float& S, float& C, float ahi, float alo,
     S = s;
     C = __fadd_rn(C, __fadd_rn(t, e));
 }
+// (S, C) += (S2, C2)
+__device__ __forceinline__ void df_add(float& S, float& C, float S2, float C2) {
+    float s, t;
+    two_sum(S, S2, s, t);
+    S = s;
+    C = __fadd_rn(C, __fadd_rn(C2, t));
+}
+// double-float sum over the warp, valid in lane 0
+__device__ __forceinline__ void df_warp_sum(float& S, float& C) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float S2 = __shfl_down_sync(0xffffffffu, S, o);
+        const float C2 = __shfl_down_sync(0xffffffffu, C, o);
+        df_add(S, C, S2, C2);
+    }
+}
 // FP32 (hi, lo) pair of a double
 __device__ __forceinline__ void split_d(double x, float& hi, float& lo) {
     hi = (float)x;
@@ -1002,7 +1018,7 @@ __device__ void arnoldi_column_tail(const double2* __restrict__ c1, const double
 // last-block count.
 __global__ void __launch_bounds__(kThreads) k_arn_dot2(c3l::ArnoldiBatch bt, int par, int64_t ld, int64_t dim,
                                                        int nseg, int64_t seglen, int64_t ldc) {
-    __shared__ double sm[32];
+    __shared__ float sm[4][kThreads / 32];
     if (arn_stopped(bt)) return;  // dependents launch as the blocks exit
     c3l::pdl_wait();
     const int b = blockIdx.y;
@@ -1029,11 +1045,31 @@ __global__ void __launch_bounds__(kThreads) k_arn_dot2(c3l::ArnoldiBatch bt, int
             df_mac(iS, iC, ah.x, al.x, bh.y, bl.y);
             df_mac(iS, iC, -ah.y, -al.y, bh.x, bl.x);
         }
-        double2 acc = make_double2((double)rS + (double)rC, (double)iS + (double)iC);
-        acc = block_sum_t(acc, sm);
-        if (threadIdx.x == 0) {
-            if (nseg == 1) bt.c2[b][row] = acc;
-            else bt.partial[b][(int64_t)row * nseg + seg] = acc;
+        // the block's sum in double-float, FP64 only for the result
+        df_warp_sum(rS, rC);
+        df_warp_sum(iS, iC);
+        const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+        __syncthreads();  // sm is free (previous item)
+        if (lane == 0) {
+            sm[0][wid] = rS;
+            sm[1][wid] = rC;
+            sm[2][wid] = iS;
+            sm[3][wid] = iC;
+        }
+        __syncthreads();
+        if (wid == 0) {
+            const bool in = lane < (int)(blockDim.x >> 5);
+            rS = in ? sm[0][lane] : 0.0f;
+            rC = in ? sm[1][lane] : 0.0f;
+            iS = in ? sm[2][lane] : 0.0f;
+            iC = in ? sm[3][lane] : 0.0f;
+            df_warp_sum(rS, rC);
+            df_warp_sum(iS, iC);
+            if (lane == 0) {
+                const double2 acc = make_double2((double)rS + (double)rC, (double)iS + (double)iC);
+                if (nseg == 1) bt.c2[b][row] = acc;
+                else bt.partial[b][(int64_t)row * nseg + seg] = acc;
+            }
         }
     }
     if (nseg == 1 && last_block(reinterpret_cast<unsigned*>(ctr + 2))) {
