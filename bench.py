@@ -262,7 +262,9 @@ def run_gpu(args) -> dict:
         "dtype": "c128", "data": "synthetic",
         "config": {"workload": args.workload, "description": wl["label"],
                    "precision": "mixed: FP32 inner JVPs and FP32 Krylov basis in GMRES (inner tolerance >= 1e-5), FP64 "
-                                "residuals/refinement; FP64 sigma and Arnoldi (first CGS2 pass FP32, second FP64)",
+                                "residuals/refinement; FP64 sigma; Arnoldi CGS2 with FP32 first projections and "
+                                "double-float (FP32-pipe) updates and second projections, FP64 Hessenberg "
+                                "column and shifted solves",
                    "plain_fp64_seconds": t_unbatched,
                    "plain_fp64_form": "FP64 inner JVPs, the reference's per-frequency preconditioned GMRES for "
                                       "every omega and channel (batching off), zero initial amplitudes",
