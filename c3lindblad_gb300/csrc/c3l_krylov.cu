@@ -955,7 +955,24 @@ __global__ void __launch_bounds__(X * Y) k_arn_axpy(c3l::ArnoldiBatch bt, int pa
         // c v = (cx vx - cy vy) + i (cx vy + cy vx)
         float rS = 0.0f, rC = 0.0f, iS = 0.0f, iC = 0.0f;
         if (i < dim) {
-            for (int j = threadIdx.y; j < k; j += Y) {
+            int j = threadIdx.y;
+            for (; j + 3 * Y < k; j += 4 * Y) {  // eight loads in flight
+                float2 vh[4], vl[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    vh[u] = Vh[(int64_t)(j + u * Y) * ld + i];
+                    vl[u] = Vl[(int64_t)(j + u * Y) * ld + i];
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const float2 c = cf[j + u * Y];
+                    df_mac(rS, rC, c.x, 0.0f, vh[u].x, vl[u].x);
+                    df_mac(rS, rC, -c.y, 0.0f, vh[u].y, vl[u].y);
+                    df_mac(iS, iC, c.x, 0.0f, vh[u].y, vl[u].y);
+                    df_mac(iS, iC, c.y, 0.0f, vh[u].x, vl[u].x);
+                }
+            }
+            for (; j < k; j += Y) {
                 const float2 c = cf[j];
                 const float2 vh = Vh[(int64_t)j * ld + i], vl = Vl[(int64_t)j * ld + i];
                 df_mac(rS, rC, c.x, 0.0f, vh.x, vl.x);
@@ -1038,7 +1055,26 @@ __global__ void __launch_bounds__(kThreads) k_arn_dot2(c3l::ArnoldiBatch bt, int
         const int64_t hi = min(dim, lo + seglen);
         // conj(v) w = (vx wx + vy wy) + i (vx wy - vy wx)
         float rS = 0.0f, rC = 0.0f, iS = 0.0f, iC = 0.0f;
-        for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+        const int64_t step = blockDim.x;
+        int64_t i = lo + threadIdx.x;
+        for (; i + 3 * step < hi; i += 4 * step) {  // sixteen loads in flight
+            float2 ah[4], al[4], bh[4], bl[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                ah[u] = vh[i + u * step];
+                al[u] = vl[i + u * step];
+                bh[u] = wh[i + u * step];
+                bl[u] = wl[i + u * step];
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                df_mac(rS, rC, ah[u].x, al[u].x, bh[u].x, bl[u].x);
+                df_mac(rS, rC, ah[u].y, al[u].y, bh[u].y, bl[u].y);
+                df_mac(iS, iC, ah[u].x, al[u].x, bh[u].y, bl[u].y);
+                df_mac(iS, iC, -ah[u].y, -al[u].y, bh[u].x, bl[u].x);
+            }
+        }
+        for (; i < hi; i += step) {
             const float2 ah = vh[i], al = vl[i], bh = wh[i], bl = wl[i];
             df_mac(rS, rC, ah.x, al.x, bh.x, bl.x);
             df_mac(rS, rC, ah.y, al.y, bh.y, bl.y);
