@@ -479,3 +479,35 @@ def test_batched_sigma_matches_single_calls(problems, cuda_device):
     octx = c3.component_eom_context(other, g["solution_amplitudes"])
     mixed = (rt.EomAction * 2)(ops.sigma_actions[0], octx.ops.sigma_action)
     assert lib.c3l_eom_sigma_batch(mixed, 2, xin, xo, rt.stream_ptr(cuda_device)) == 1
+
+
+@pytest.mark.parametrize("name", golden_names(compact=True))
+def test_arnoldi_basis_long_vectors(name, problems, cuda_device):
+    """The Arnoldi step at N > 8192 (segmented second projections and their
+    final reduction, double-float updates from rows that stream from HBM):
+    the device bases of the n = 27 Kanamori charge +1 operator (addition and
+    removal channels stepped together) are orthonormal and satisfy
+    K V_m = V_{m+1} H to FP64-level rounding."""
+    import c3lindblad_gb300 as c3
+    from c3lindblad_gb300.krylov import arnoldi_channels
+
+    spec, g, p = problems(name)
+    T, _ = _fixed_inputs(p.plan, float(g["scale"]))
+    ep = c3.ComponentEOMProblem.compile(c3.eom_ccsd_problem(p), p, 1)
+    ctx = c3.component_eom_context(ep, T)
+    op = c3.ComponentSigmaOperator(ctx)
+    N = op.dimension
+    assert N > 8192
+    src = c3.component_eom_sources(ctx, site=0)
+    vecs = [torch.from_numpy(np.ascontiguousarray(v)).to(cuda_device) for v in (src.addition, src.removal)]
+    shifts = torch.tensor([0.1 + 0.5j, -1.0 + 0.5j], dtype=torch.complex128, device=cuda_device)
+    m = 48
+    bases = arnoldi_channels(ctx.ops, vecs, shifts, maximum_dimension=m, residual_tolerance=1e-30,
+                             minimum_dimension=m, check_interval=16)
+    for basis in bases:
+        assert basis.m == m
+        V = basis.V[:m + 1].cpu().numpy().T
+        H = basis.H[:m + 1, :m]
+        assert np.max(np.abs(V.conj().T @ V - np.eye(m + 1))) < 1e-12
+        KV = np.stack([op.matvec(V[:, j]) for j in range(m)], axis=1)
+        assert np.linalg.norm(KV - V @ H) / np.linalg.norm(H) < 1e-13
