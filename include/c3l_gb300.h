@@ -469,17 +469,22 @@ typedef struct {
     int64_t launches;                  /* kernels launched (graph nodes included) */
 } c3l_arnoldi_channel;
 
-/* CGS2 Arnoldi for (z I - K)^{-1} b on every channel, channel c on streams[c]
+/* CGS2 Arnoldi for (z I - K)^{-1} b on every channel
  * (src/c3l/green/krylov.py:284-417): stops a channel when the Arnoldi-relation
  * residual is <= tol for every shift (checked every check_interval steps from
- * min_dim on) or on breakdown (|h_{j+1,j}| <= breakdown_tol).  Steps run
- * without host synchronization between checks: one step (sigma, CGS2,
- * column of H, normalization) is a CUDA graph captured once per call and
- * replayed with the step index kept in device memory, and each check advances
- * the channel's incremental
- * shifted solves (c3l_hessenberg_advance, FP64) over the new columns and
- * reads back one status word.  On return hess.green / hess.residual hold the
- * Green function and residuals of the final dimension m. */
+ * min_dim on) or on breakdown (|h_{j+1,j}| <= breakdown_tol).  Channels whose
+ * sigma actions run the same program (up to C3L_MAX_BATCH) step together on
+ * the stream of their first channel: one step (sigma, CGS2, column of H,
+ * normalization) for all of them is a CUDA graph captured once per call and
+ * replayed with the step indices kept in device memory.  Each check advances
+ * the incremental shifted solves (c3l_hessenberg_advance, FP64) over the new
+ * columns on a stream of the driver's own while the channels take their next
+ * steps, and reads back one status word per channel.  CGS2 arithmetic: FP32
+ * first projections from the FP32 copies V32/work32; first update and second
+ * projections in double-float from the (V32, V32lo) and (work32, work32lo)
+ * pairs; second update V c2 with FP32 products; FP64 subtractions, scaling
+ * and Hessenberg column.  On return hess.green / hess.residual hold the Green
+ * function and residuals of the final dimension m. */
 c3l_status c3l_arnoldi(c3l_arnoldi_channel* channels, int32_t nchannels, int64_t N, const c3l_complex* shifts,
                        int32_t nshift, int32_t m_max, double tol, int32_t min_dim, int32_t check_interval,
                        double breakdown_tol, void* const* streams);
