@@ -185,10 +185,11 @@ __device__ __forceinline__ void contract_entry(const c3l_contract_task& task, in
     if (task.const_off >= 0) acc = vectors[task.const_off + e];
     for (int j = 0; j < task.nsrc; ++j) {
         const int axis = task.axis[j];
-        const int64_t low = pw[task.deg - axis];
-        const int64_t hi = e / low;
-        const int64_t lo = e - hi * low;
-        const C* src = ws + task.src_off[j] + hi * low * n + lo;
+        // entries of a padded block are below n^4 < 2^32 (n <= 255): 32-bit division
+        const uint32_t low = (uint32_t)pw[task.deg - axis];
+        const uint32_t hi = (uint32_t)e / low;
+        const uint32_t lo = (uint32_t)e - hi * low;
+        const C* src = ws + task.src_off[j] + (int64_t)hi * low * n + lo;
         const C* vec = vectors + task.vec_off[j];
         C sum = Cx<C>::make(0.0, 0.0);
         for (int m0 = 0; m0 < n; m0 += kContractChunk) {
@@ -325,15 +326,35 @@ __global__ void __launch_bounds__(kThreads) k_wedge(c3l_wedge_stage st, int n, B
     int dig[4] = {0, 0, 0, 0};
     if (active) {
         if (MODE == kPadded) {
-            int64_t r = e;
+            uint32_t r = (uint32_t)e;  // below n^4 < 2^32
             for (int c = blk.deg - 1; c >= 0; --c) {
-                dig[c] = (int)(r % n);
-                r /= n;
+                const uint32_t q = r / (uint32_t)n;
+                dig[c] = (int)(r - q * (uint32_t)n);
+                r = q;
             }
         } else {
             const int64_t packed = st.digits[e];
 #pragma unroll
             for (int c = 0; c < 4; ++c) dig[c] = (int)((packed >> (8 * c)) & 0xFF);
+        }
+    }
+    // the epilogue's table entries of group 0's output, fetched before the
+    // instance loop (and, being program tables, before the wait)
+    const bool ep_thread = MODE != kPadded && active && gy == 0;
+    int64_t mu = 0, ecol = 0, epair = 0;
+    double2 elam = make_double2(0.0, 0.0), escale = make_double2(0.0, 0.0);
+    double em4[4] = {0.0, 0.0, 0.0, 0.0};
+    if (ep_thread) {
+        mu = st.elements[e];
+        if (MODE == kStatic || MODE == kEom) elam = ep.lam[e];
+        if (MODE == kStatic) {
+            escale = ep.scale[e];
+            ecol = ep.col[e];
+            epair = ep.pair[e];
+            if (ep.m4) {
+#pragma unroll
+                for (int q = 0; q < 4; ++q) em4[q] = ep.m4[4 * e + q];
+            }
         }
     }
     C acc = Cx<C>::make(0.0, 0.0);
@@ -350,6 +371,8 @@ __global__ void __launch_bounds__(kThreads) k_wedge(c3l_wedge_stage st, int n, B
         if (left > 0) stage(blk.inst_begin, left < kInstChunk ? (int)left : kInstChunk);
     }
     c3l::pdl_wait();
+    double2 esrc = make_double2(0.0, 0.0);  // the operator's input at the output (issued before the loop)
+    if ((MODE == kStatic || MODE == kEom) && ep_thread) esrc = bt.in[blockIdx.y][mu];
     for (int64_t base = blk.inst_begin; base < blk.inst_end; base += kInstChunk) {
         const int64_t left = blk.inst_end - base;
         const int cnt = left < kInstChunk ? (int)left : kInstChunk;
@@ -380,36 +403,32 @@ __global__ void __launch_bounds__(kThreads) k_wedge(c3l_wedge_stage st, int n, B
     if (MODE == kPadded) {
         ws[blk.out_off + e] = acc;
     } else if (MODE == kStatic) {
-        const int64_t mu = st.elements[e];
         const double2 a = to_d2(acc);
-        const double2 lam = ep.lam[e], src = bt.in[blockIdx.y][mu];
+        const double2 lam = elam, src = esrc;
         const double2 s = make_double2(fma(lam.x, src.x, fma(-lam.y, src.y, a.x)), fma(lam.x, src.y, fma(lam.y, src.x, a.y)));
         const double2 r = make_double2(s.y, -s.x);  // -i * s
-        const double2 v = dmul(r, ep.scale[e]);
-        const int64_t c = ep.col[e];
+        const double2 v = dmul(r, escale);
+        const int64_t c = ecol;
         if (ep.m4) {  // fused preconditioner: y = M [x_c, x_c+1] (pack(unpack(.)/diag))
-            const double* m = ep.m4 + 4 * e;
-            if (ep.pair[e]) {
-                ep.xout[c] = fma(m[0], v.x, m[1] * r.y);
-                ep.xout[c + 1] = fma(m[2], v.x, m[3] * r.y);
+            if (epair) {
+                ep.xout[c] = fma(em4[0], v.x, em4[1] * r.y);
+                ep.xout[c + 1] = fma(em4[2], v.x, em4[3] * r.y);
             } else {
-                ep.xout[c] = m[0] * v.x;
+                ep.xout[c] = em4[0] * v.x;
             }
         } else {
             ep.xout[c] = v.x;
-            if (ep.pair[e]) ep.xout[c + 1] = r.y;
+            if (epair) ep.xout[c + 1] = r.y;
         }
     } else if (MODE == kEom) {
-        const int64_t mu = st.elements[e];
         const double2 a = to_d2(acc);
-        const double2 lam = ep.lam[e], src = bt.in[blockIdx.y][mu];
+        const double2 lam = elam, src = esrc;
         const double2 o =
             make_double2(fma(lam.x, src.x, fma(-lam.y, src.y, a.x)), fma(lam.x, src.y, fma(lam.y, src.x, a.y)));
         bt.out[blockIdx.y][mu] = o;
         float2* o32 = bt.out32[blockIdx.y];
         if (o32) o32[mu] = make_float2((float)o.x, (float)o.y);
     } else {
-        const int64_t mu = st.elements[e];
         bt.out[blockIdx.y][mu] = dmul(ep.cscale, to_d2(acc));
     }
 }
