@@ -124,16 +124,53 @@ __global__ void k_unpack_scatter(int64_t dim, const double* __restrict__ x, cons
                                  const int64_t* __restrict__ dst, const int64_t* __restrict__ pos,
                                  const double* __restrict__ sign, C* __restrict__ ws) {
     c3l::pdl_launch_dependents();
-    c3l::pdl_wait();
     const int64_t n = dim > count ? dim : count;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int64_t i0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    // the thread's first entry: every index and coefficient is a program table,
+    // read before the wait; x (the previous kernel's output) after it
+    int64_t a0 = 0, b0 = 0, pa = 0, pb = 0, d0 = 0;
+    double2 ca0 = make_double2(0.0, 0.0), cb0 = ca0, cap = ca0, cbp = ca0;
+    double sg = 0.0;
+    if (i0 < dim) {
+        a0 = ia[i0];
+        b0 = ib[i0];
+        ca0 = ca[i0];
+        cb0 = cb[i0];
+    }
+    if (i0 < count) {
+        sg = sign[i0];
+        d0 = dst[i0];
+        if (sg != 0.0) {
+            const int64_t p = pos[i0];
+            pa = ia[p];
+            pb = ib[p];
+            cap = ca[p];
+            cbp = cb[p];
+        }
+    }
+    c3l::pdl_wait();
+    if (i0 < dim) {
+        const double xa = x[a0], xb = x[b0];
+        t[i0] = make_double2(fma(ca0.x, xa, cb0.x * xb), fma(ca0.y, xa, cb0.y * xb));
+    }
+    if (i0 < count) {
+        double2 v = make_double2(0.0, 0.0);
+        if (sg != 0.0) {
+            const double xa = x[pa], xb = x[pb];
+            const double2 u = make_double2(fma(cap.x, xa, cbp.x * xb), fma(cap.y, xa, cbp.y * xb));
+            v = make_double2(sg * u.x, sg * u.y);
+        }
+        ws[d0] = Cx<C>::make(v.x, v.y);
+    }
+    for (int64_t i = i0 + stride; i < n; i += stride) {  // grids smaller than n (not the usual launch)
         if (i < dim) t[i] = tilde_value(x, ia, ib, ca, cb, i);
         if (i < count) {
-            const double sg = sign[i];
+            const double s2 = sign[i];
             double2 v = make_double2(0.0, 0.0);
-            if (sg != 0.0) {
+            if (s2 != 0.0) {
                 const double2 u = tilde_value(x, ia, ib, ca, cb, pos[i]);
-                v = make_double2(sg * u.x, sg * u.y);
+                v = make_double2(s2 * u.x, s2 * u.y);
             }
             ws[dst[i]] = Cx<C>::make(v.x, v.y);
         }
@@ -145,10 +182,27 @@ __global__ void k_scatter(int64_t count, const int64_t* __restrict__ dst, const 
                           const double* __restrict__ sign, Batch<C> bt) {
     if (!bt.pdl_at_exit) c3l::pdl_launch_dependents();
     if (batch_stopped(bt)) return;
-    c3l::pdl_wait();
     const double2* __restrict__ vec = bt.in[blockIdx.y];
     C* __restrict__ ws = bt.ws[blockIdx.y];
-    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < count; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t e0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    // the first entry's table values before the wait, the vector after it
+    double s0 = 0.0;
+    int64_t p0 = 0, d0 = 0;
+    if (e0 < count) {
+        s0 = sign[e0];
+        p0 = pos[e0];
+        d0 = dst[e0];
+    }
+    c3l::pdl_wait();
+    if (e0 < count) {
+        double2 v = make_double2(0.0, 0.0);
+        if (s0 != 0.0) {
+            const double2 u = vec[p0];
+            v = make_double2(s0 * u.x, s0 * u.y);
+        }
+        ws[d0] = Cx<C>::make(v.x, v.y);
+    }
+    for (int64_t e = e0 + (int64_t)gridDim.x * blockDim.x; e < count; e += (int64_t)gridDim.x * blockDim.x) {
         const double s = sign[e];
         double2 v = make_double2(0.0, 0.0);
         if (s != 0.0) {
