@@ -177,16 +177,22 @@ class DeviceStatic:
 class DeviceEOM:
     """Sigma action of one (spin, charge) EOM block at fixed amplitudes."""
 
-    def __init__(self, plan: EOMPlan, amplitudes: torch.Tensor, device=None):
+    def __init__(self, plan: EOMPlan, amplitudes: torch.Tensor, device=None, tables: dict | None = None):
+        """``tables``: a dict (device -> Uploader) owned by the EOM problem, so that
+        contexts of one problem share its uploaded program tables."""
         self.device = rt.require_cuda(device)
         self.lib = rt.lib()
         self.plan = plan
         prog = plan.program
-        up = rt.Uploader(self.device)
+        if tables is None:
+            tables = {}
+        up = tables.get(self.device)
+        if up is None:
+            up = tables[self.device] = rt.Uploader(self.device)
         self._up = up
         self.N = plan.dimension
-        self.vec = up.raw(prog.vectors)
-        self.lam = up.raw(plan.lam_sigma)
+        self.vec = up.table(prog.vectors)
+        self.lam = up.table(plan.lam_sigma)
         self.amplitudes = amplitudes.to(self.device, torch.complex128).contiguous()
         self.workspaces: list = []
         self.sigma_actions: list = []

@@ -60,6 +60,7 @@ class ComponentEOMProblem:
         self.response_spin = int(response_spin)
         self.charge = int(charge)
         self._plan = None
+        self._tables = {}  # device -> Uploader holding this problem's program tables (shared by contexts)
 
     @classmethod
     def compile(cls, problem, static, charge: int) -> "ComponentEOMProblem":
@@ -93,7 +94,7 @@ class ComponentEOMContext:
             if arr.shape != (st.num_amplitudes,) or not np.all(np.isfinite(arr)):
                 raise ValueError("component vector has the wrong shape or is nonfinite")
             t = torch.from_numpy(arr.copy())
-        self.ops = DeviceEOM(problem.plan, t, st._device)
+        self.ops = DeviceEOM(problem.plan, t, st._device, tables=problem._tables)
         self.amplitudes = self.ops.amplitudes
 
 

@@ -237,6 +237,15 @@ class Uploader:
         self.keep.append(t)
         return t
 
+    def table(self, arr) -> torch.Tensor:
+        """Device copy of a (read-only) program table, uploaded once per array."""
+        hit = self._tables.get(id(arr))
+        if hit is not None and hit[0] is arr:
+            return hit[1]
+        t = self.raw(arr)
+        self._tables[id(arr)] = (arr, t)
+        return t
+
     def ptr(self, arr) -> int:
         """Device address of a (read-only) program table, uploaded once: actions
         built from the same tables share them, which batched launches require."""
@@ -244,12 +253,7 @@ class Uploader:
             return 0
         if len(arr) == 0:
             return 0
-        hit = self._tables.get(id(arr))
-        if hit is not None and hit[0] is arr:
-            return hit[1].data_ptr()
-        t = self.raw(arr)
-        self._tables[id(arr)] = (arr, t)
-        return t.data_ptr()
+        return self.table(arr).data_ptr()
 
 
 def wedge_stage(up: Uploader, stage) -> WedgeStage:
