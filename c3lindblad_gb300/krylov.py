@@ -90,10 +90,12 @@ class DeviceVectors:
 # ================================================================= Arnoldi
 @dataclass
 class ArnoldiBasis:
-    """Krylov basis V (rows) and Hessenberg H of K V_m = V_m H_m + h v e_m^T."""
+    """Krylov basis V (rows) and Hessenberg H of K V_m = V_m H_m + h v e_m^T.
+
+    H stays on the device (``Hcol``: column j in row j) until it is first read."""
 
     V: torch.Tensor          # [m+1, N] complex (device)
-    H: np.ndarray            # [m+1, m] complex (host)
+    Hcol: torch.Tensor       # [m_max, m_max+1] complex (device): Hcol[j, :j+2] = H[:j+2, j]
     beta: float
     m: int
     breakdown: bool
@@ -104,6 +106,15 @@ class ArnoldiBasis:
     wall_seconds: float
     green: torch.Tensor | None = None     # [nshift] sink . y at dimension m (device)
     residual: torch.Tensor | None = None  # [nshift] Arnoldi-relation residuals at m (device)
+    _H: np.ndarray | None = None
+
+    @property
+    def H(self) -> np.ndarray:
+        """[m+1, m] complex Hessenberg matrix (host copy, made on first use)."""
+        if self._H is None:
+            m = self.m
+            self._H = np.ascontiguousarray(self.Hcol[:m, :m + 1].cpu().numpy().T)
+        return self._H
 
 
 def hessenberg_shifted(H: np.ndarray, m: int, shifts: torch.Tensor, beta: float, sinkproj: torch.Tensor | None):
@@ -271,7 +282,6 @@ def arnoldi_channels(ops, sources, shifts: torch.Tensor, *, maximum_dimension: i
             "partial": torch.empty(max(int(lib.c3l_multi_dot_scratch(m_max + 1, N)), 1), dtype=torch.complex128,
                                    device=dev),
             "host": torch.zeros(2 * (m_max + 1) + 2, dtype=torch.complex128).pin_memory(),
-            "H": np.zeros((m_max + 1, m_max), dtype=np.complex128),
             "cdims": np.zeros(m_max // max(check_interval, 1) + 4, dtype=np.int32),
             "hess": HessenbergTracker(m_max, shifts, sink is not None),
             "work": torch.empty(2 * N, dtype=torch.complex128, device=dev),
@@ -288,7 +298,7 @@ def arnoldi_channels(ops, sources, shifts: torch.Tensor, *, maximum_dimension: i
         q.sigma = C.addressof(ops.sigma_actions[c])
         q.b, q.sink_conj = b.data_ptr(), rt.ptr(sink_conj)
         q.V, q.Hcol, q.coeff = d["V"].data_ptr(), d["Hcol"].data_ptr(), d["coeff"].data_ptr()
-        q.partial, q.host, q.H = d["partial"].data_ptr(), d["host"].data_ptr(), d["H"].ctypes.data
+        q.partial, q.host, q.H = d["partial"].data_ptr(), d["host"].data_ptr(), None  # H stays on the device
         d["hess"].fill(q.hess)
         q.status_host = d["hess"].status_host.data_ptr()
         q.work, q.counters = d["work"].data_ptr(), d["counters"].data_ptr()
@@ -309,7 +319,7 @@ def arnoldi_channels(ops, sources, shifts: torch.Tensor, *, maximum_dimension: i
         m = int(q.m)
         nchk = min(int(q.nchecks), d["cdims"].size)
         rt.LaunchCounter.add(int(q.launches))
-        out.append(ArnoldiBasis(d["V"], d["H"][:m + 1, :m].copy(), float(q.beta), m, bool(q.breakdown),
+        out.append(ArnoldiBasis(d["V"], d["Hcol"], float(q.beta), m, bool(q.breakdown),
                                 list(d["cdims"][:nchk]), list(d["cres"][:nchk]), bool(q.converged),
                                 float(q.action_seconds), time.perf_counter() - started,
                                 d["hess"].green, d["hess"].residual))
