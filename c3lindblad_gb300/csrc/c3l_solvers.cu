@@ -93,6 +93,7 @@ class StepGraph {
         return exec_ && cudaGraphLaunch(exec_, s) == cudaSuccess ? C3L_OK : C3L_ERR_LAUNCH;
     }
     int64_t nodes() const { return nodes_; }
+    bool captured() const { return exec_ != nullptr; }
 
   private:
     cudaGraph_t graph_ = nullptr;
@@ -622,24 +623,36 @@ c3l_status c3l_arnoldi(c3l_arnoldi_channel* ch, int32_t nch, int64_t N, const c3
     auto d2 = [](c3l_complex* p) { return reinterpret_cast<double2*>(p); };
     OwnedStream cap;
     if ((st = cap.create())) return st;
-    std::vector<StepGraph> one(2 * ng), interval(2 * ng);
+    // per-group launch data, kept for the whole call: graphs are captured on
+    // first use (checks at multiples of check_interval launch only the
+    // interval graph of one parity)
+    struct GroupStep {
+        c3l::ArnoldiBatch bt{};
+        std::vector<c3l_eom_action> acts;
+        std::vector<const c3l_complex*> xin;
+        std::vector<c3l_complex*> out;
+        std::vector<c3l_complex32*> out32;
+        std::vector<const int32_t*> stop;
+    };
+    std::vector<GroupStep> gsteps(ng);
     for (int g = 0; g < ng; ++g) {
         const std::vector<int>& mem = groups[g];
         const int nb = (int)mem.size();
-        c3l::ArnoldiBatch bt{};
-        bt.nb = nb;
-        std::vector<c3l_eom_action> acts(nb);
-        std::vector<const c3l_complex*> xin(nb);
-        std::vector<c3l_complex*> out(nb);
-        std::vector<c3l_complex32*> out32(nb);
-        std::vector<const int32_t*> stop(nb);
+        GroupStep& gs = gsteps[g];
+        gs.bt.nb = nb;
+        gs.acts.resize(nb);
+        gs.xin.resize(nb);
+        gs.out.resize(nb);
+        gs.out32.resize(nb);
+        gs.stop.resize(nb);
         for (int i = 0; i < nb; ++i) {
             c3l_arnoldi_channel& q = ch[mem[i]];
-            acts[i] = *q.sigma;
-            xin[i] = q.work;
-            out[i] = q.work + N;
-            out32[i] = q.work32;
-            stop[i] = q.counters + 3;
+            gs.acts[i] = *q.sigma;
+            gs.xin[i] = q.work;
+            gs.out[i] = q.work + N;
+            gs.out32[i] = q.work32;
+            gs.stop[i] = q.counters + 3;
+            c3l::ArnoldiBatch& bt = gs.bt;
             bt.V[i] = d2(q.V);
             bt.w[i] = d2(q.work + N);
             bt.xnext[i] = d2(q.work);
@@ -654,27 +667,34 @@ c3l_status c3l_arnoldi(c3l_arnoldi_channel* ch, int32_t nch, int64_t N, const c3
             bt.V32lo[i] = reinterpret_cast<float2*>(q.V32lo);
             bt.w32lo[i] = reinterpret_cast<float2*>(q.work32lo);
         }
-        auto step = [&](cudaStream_t cs, int par) -> c3l_status {
-            c3l_status r = c3l::eom_sigma_batch(acts.data(), nb, xin.data(), out.data(), out32.data(), stop.data(), cs);
-            if (r) return r;
-            // pass 1 in FP32 (pass 2 is FP64 and removes what it leaves)
-            if ((r = c3l::arnoldi_dot1(bt, par, N, N, rd, cs))) return r;
-            if ((r = c3l::arnoldi_axpy1(bt, par, N, m_max, N, cs))) return r;
-            if ((r = c3l::arnoldi_dot2(bt, par, N, N, rd, ldc, cs))) return r;
-            return c3l::arnoldi_scale(bt, par, N, m_max, breakdown_tol, N, cs);
-        };
-        for (int par = 0; par < 2; ++par) {
-            if ((st = one[2 * g + par].capture(cap.s, [&](cudaStream_t cs) { return step(cs, par); }))) return st;
-            if ((st = interval[2 * g + par].capture(cap.s, [&](cudaStream_t cs) -> c3l_status {
-                     for (int i = 0; i < check_interval; ++i) {
-                         const c3l_status r = step(cs, (par + i) & 1);
-                         if (r) return r;
-                     }
-                     return C3L_OK;
-                 })))
-                return st;
-        }
     }
+    auto step = [&](const GroupStep& gs, cudaStream_t cs, int par) -> c3l_status {
+        c3l_status r = c3l::eom_sigma_batch(gs.acts.data(), gs.bt.nb, gs.xin.data(), gs.out.data(), gs.out32.data(),
+                                            gs.stop.data(), cs);
+        if (r) return r;
+        if ((r = c3l::arnoldi_dot1(gs.bt, par, N, N, rd, cs))) return r;
+        if ((r = c3l::arnoldi_axpy1(gs.bt, par, N, m_max, N, cs))) return r;
+        if ((r = c3l::arnoldi_dot2(gs.bt, par, N, N, rd, ldc, cs))) return r;
+        return c3l::arnoldi_scale(gs.bt, par, N, m_max, breakdown_tol, N, cs);
+    };
+    std::vector<StepGraph> one(2 * ng), interval(2 * ng);
+    // the graph of group g: `steps` steps (1 or check_interval) from parity par
+    auto graph = [&](int g, int par, bool chained, const StepGraph** out) -> c3l_status {
+        StepGraph& sg = chained ? interval[2 * g + par] : one[2 * g + par];
+        if (!sg.captured()) {
+            const int steps = chained ? check_interval : 1;
+            c3l_status r = sg.capture(cap.s, [&](cudaStream_t cs) -> c3l_status {
+                for (int i = 0; i < steps; ++i) {
+                    const c3l_status q = step(gsteps[g], cs, (par + i) & 1);
+                    if (q) return q;
+                }
+                return C3L_OK;
+            });
+            if (r) return r;
+        }
+        *out = &sg;
+        return C3L_OK;
+    };
     std::vector<int> active(nch, 1);
     for (int c = 0; c < nch; ++c) {
         c3l_arnoldi_channel& q = ch[c];
@@ -772,18 +792,18 @@ c3l_status c3l_arnoldi(c3l_arnoldi_channel* ch, int32_t nch, int64_t N, const c3
             int left = upto - launched;
             int at = launched;  // steps taken so far: the parity of the next step
             while (left >= check_interval) {
-                const StepGraph& g = interval[2 * gi + (at & 1)];
-                c3l_status r = g.launch(s);
-                if (r) return r;
-                q.launches += g.nodes();
+                const StepGraph* g = nullptr;
+                c3l_status r = graph(gi, at & 1, true, &g);
+                if (r || (r = g->launch(s))) return r;
+                q.launches += g->nodes();
                 left -= check_interval;
                 at += check_interval;
             }
             for (; left > 0; --left, ++at) {
-                const StepGraph& g = one[2 * gi + (at & 1)];
-                c3l_status r = g.launch(s);
-                if (r) return r;
-                q.launches += g.nodes();
+                const StepGraph* g = nullptr;
+                c3l_status r = graph(gi, at & 1, false, &g);
+                if (r || (r = g->launch(s))) return r;
+                q.launches += g->nodes();
             }
         }
         launched = upto;
