@@ -56,6 +56,12 @@ struct ArnoldiBatch {
     float2* w32[C3L_MAX_BATCH];   // FP32 copy of the operator output (sigma), then of w' (first update)
     float2* V32lo[C3L_MAX_BATCH]; // V - V32 in FP32: rows as FP32 (hi, lo) pairs
     float2* w32lo[C3L_MAX_BATCH]; // w' - w32 in FP32 (first update)
+    // optional: the sigma's padded input, written by the second update for the
+    // next step (xws null: the sigma scatters its input itself)
+    double2* xws[C3L_MAX_BATCH];
+    const int64_t* xoff;          // [N + 1] entries of input element i: [xoff[i], xoff[i+1])
+    const int64_t* xdst;
+    const double* xsign;
 };
 // pass 1 (FP32, from the FP32 copies V32 and w32): c1[r] = V[r]^H w, r < k = counters[par] + 1
 c3l_status arnoldi_dot1(const ArnoldiBatch& bt, int par, int64_t ld, int64_t dim, const RowDot& p, cudaStream_t s);
@@ -76,9 +82,11 @@ c3l_status arnoldi_scale(const ArnoldiBatch& bt, int par, int64_t ld, int max_k,
 // The sigma action on a batch of vectors (actions[b] share one program and
 // differ in their workspace); an entry whose stop flag is set is skipped.
 // out32 (may be null, or hold null entries): an FP32 copy of each output.
+// skip_scatter: the padded input blocks are already written (by the Arnoldi
+// step that formed xin).
 c3l_status eom_sigma_batch(const c3l_eom_action* actions, int nb, const c3l_complex* const* xin,
                            c3l_complex* const* out, c3l_complex32* const* out32, const int32_t* const* stop,
-                           cudaStream_t s);
+                           cudaStream_t s, bool skip_scatter = false);
 // True when two sigma actions run the same program (they may differ in ws).
 bool same_sigma_program(const c3l_eom_action& a, const c3l_eom_action& b);
 

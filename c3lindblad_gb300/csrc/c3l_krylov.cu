@@ -1164,9 +1164,15 @@ __global__ void __launch_bounds__(X * Y) k_arn_scale(c3l::ArnoldiBatch bt, int p
     float2* V32k = bt.V32[b] + (int64_t)k * ld;
     const double2* __restrict__ w = bt.w[b];
     double2* __restrict__ xnext = bt.xnext[b];
+    double2* __restrict__ xws = bt.xws[b];
     for (int64_t base = (int64_t)blockIdx.x * X; base < n; base += (int64_t)gridDim.x * X) {
         const int64_t i = base + threadIdx.x;
         float2 s = make_float2(0.0f, 0.0f);
+        int64_t q0 = 0, q1 = 0;  // the element's scatter entries (program table)
+        if (xws && threadIdx.y == 0 && i < n) {
+            q0 = bt.xoff[i];
+            q1 = bt.xoff[i + 1];
+        }
         if (i < n) {
             int j = threadIdx.y;
             for (; j + 3 * Y < k; j += 4 * Y) {
@@ -1206,6 +1212,12 @@ __global__ void __launch_bounds__(X * Y) k_arn_scale(c3l::ArnoldiBatch bt, int p
             V32k[i] = xh;
             bt.V32lo[b][(int64_t)k * ld + i] = xl;
             xnext[i] = x;
+            if (xws) {  // the next sigma's padded input entries of element i
+                for (int64_t q = q0; q < q1; ++q) {
+                    const double sg = bt.xsign[q];
+                    xws[bt.xdst[q]] = make_double2(sg * x.x, sg * x.y);
+                }
+            }
         }
         __syncthreads();
     }

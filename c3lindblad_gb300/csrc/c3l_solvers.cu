@@ -633,6 +633,7 @@ c3l_status c3l_arnoldi(c3l_arnoldi_channel* ch, int32_t nch, int64_t N, const c3
         std::vector<c3l_complex*> out;
         std::vector<c3l_complex32*> out32;
         std::vector<const int32_t*> stop;
+        bool fused_scatter = false;
     };
     std::vector<GroupStep> gsteps(ng);
     for (int g = 0; g < ng; ++g) {
@@ -667,10 +668,25 @@ c3l_status c3l_arnoldi(c3l_arnoldi_channel* ch, int32_t nch, int64_t N, const c3
             bt.V32lo[i] = reinterpret_cast<float2*>(q.V32lo);
             bt.w32lo[i] = reinterpret_cast<float2*>(q.work32lo);
         }
+        // the second update writes the next sigma's padded input when every
+        // channel of the group supplies the scatter grouped by element
+        bool fused = true;
+        for (int i = 0; i < nb; ++i) {
+            const c3l_arnoldi_channel& q = ch[mem[i]];
+            fused = fused && q.xscatter_offsets && q.xscatter_dst && q.xscatter_sign;
+        }
+        gs.fused_scatter = fused;
+        if (fused) {
+            const c3l_arnoldi_channel& q0 = ch[mem[0]];
+            gs.bt.xoff = q0.xscatter_offsets;
+            gs.bt.xdst = q0.xscatter_dst;
+            gs.bt.xsign = q0.xscatter_sign;
+            for (int i = 0; i < nb; ++i) gs.bt.xws[i] = reinterpret_cast<double2*>(ch[mem[i]].sigma->action.ws);
+        }
     }
     auto step = [&](const GroupStep& gs, cudaStream_t cs, int par) -> c3l_status {
         c3l_status r = c3l::eom_sigma_batch(gs.acts.data(), gs.bt.nb, gs.xin.data(), gs.out.data(), gs.out32.data(),
-                                            gs.stop.data(), cs);
+                                            gs.stop.data(), cs, gs.fused_scatter);
         if (r) return r;
         if ((r = c3l::arnoldi_dot1(gs.bt, par, N, N, rd, cs))) return r;
         if ((r = c3l::arnoldi_axpy1(gs.bt, par, N, m_max, N, cs))) return r;
@@ -713,6 +729,13 @@ c3l_status c3l_arnoldi(c3l_arnoldi_channel* ch, int32_t nch, int64_t N, const c3
         if ((st = c3l_scale_c(N, c3l_complex{1.0 / q.beta, 0.0}, q.b, q.V, sv))) return st;
         if ((st = c3l::split_c(N, q.V, q.V32, q.V32lo, s))) return st;
         if ((st = c3l_scale_c(N, c3l_complex{1.0 / q.beta, 0.0}, q.b, q.work, sv))) return st;
+        if (gsteps[group_of[c]].fused_scatter) {  // the first sigma's padded input (zero entries included)
+            const c3l_action& a = q.sigma->action;
+            if ((st = c3l_scatter_padded(a.scatter_count, a.scatter_dst, a.scatter_pos, a.scatter_sign, q.work, a.ws,
+                                         sv)))
+                return st;
+            q.launches += 1;
+        }
         if (cudaMemsetAsync(q.counters, 0, 4 * sizeof(int32_t), s) != cudaSuccess) return C3L_ERR_LAUNCH;
         q.launches += (N > 8192 ? 2 : 1) + 3;
         q.hess.shifts = shifts;

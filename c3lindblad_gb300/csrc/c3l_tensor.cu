@@ -644,7 +644,8 @@ bool same_program(const c3l_action& a, const c3l_action& b) {
 
 template <typename C>
 c3l_status eom_sigma(const c3l_eom_action* ea, int nb, const c3l_complex* const* xin, c3l_complex* const* out,
-                     c3l_complex32* const* out32, const int32_t* const* stop, cudaStream_t s, bool pdl = false) {
+                     c3l_complex32* const* out32, const int32_t* const* stop, cudaStream_t s, bool pdl = false,
+                     bool skip_scatter = false) {
     if (!ea || nb < 1 || nb > C3L_MAX_BATCH || !xin || !out) return C3L_ERR_ARGUMENT;
     Batch<C> bt{};
     bt.nb = nb;
@@ -659,8 +660,10 @@ c3l_status eom_sigma(const c3l_eom_action* ea, int nb, const c3l_complex* const*
         bt.stop[b] = stop ? stop[b] : nullptr;
         bt.out32[b] = out32 ? reinterpret_cast<float2*>(out32[b]) : nullptr;
     }
-    c3l_status st = action_prepare<C>(&ea[0].action, bt, s);
+    c3l_status st = skip_scatter ? C3L_OK : scatter<C>(&ea[0].action, bt, s);
     if (st) return st;
+    if ((st = run_levels<C>(&ea[0].action, bt, s))) return st;
+    if ((st = run_padded<C>(&ea[0].action, bt, s))) return st;
     if (ea[0].action.out.ntiles <= 0) return C3L_OK;
     Epilogue ep{};
     ep.lam = reinterpret_cast<const double2*>(ea[0].lam);
@@ -673,8 +676,8 @@ namespace c3l {
 
 c3l_status eom_sigma_batch(const c3l_eom_action* actions, int nb, const c3l_complex* const* xin,
                            c3l_complex* const* out, c3l_complex32* const* out32, const int32_t* const* stop,
-                           cudaStream_t s) {
-    return eom_sigma<double2>(actions, nb, xin, out, out32, stop, s, true);
+                           cudaStream_t s, bool skip_scatter) {
+    return eom_sigma<double2>(actions, nb, xin, out, out32, stop, s, true, skip_scatter);
 }
 
 bool same_sigma_program(const c3l_eom_action& a, const c3l_eom_action& b) {

@@ -202,6 +202,20 @@ class DeviceEOM:
         self.sigma_launches = rt.action_launches(self.sigma_action.action)
         self.diagonal = torch.from_numpy(plan.diagonal.copy()).to(self.device)
 
+    def input_scatter_csr(self):
+        """(offsets[N+1], dst, sign) device tables: the nonzero entries of the
+        sigma's input scatter grouped by input element (uploaded once)."""
+        csr = self.plan.__dict__.get("_x_scatter_csr")
+        if csr is None:
+            sc = self.plan.scatter_X
+            keep = np.nonzero(sc.sign != 0.0)[0]
+            order = keep[np.argsort(sc.pos[keep], kind="stable")]
+            offsets = np.zeros(self.N + 1, dtype=np.int64)
+            np.add.at(offsets, sc.pos[order] + 1, 1)
+            csr = (np.cumsum(offsets), sc.dst[order].astype(np.int64), sc.sign[order].astype(np.float64))
+            self.plan.__dict__["_x_scatter_csr"] = csr
+        return tuple(self._up.table(a) for a in csr)
+
     def ensure_channels(self, count: int) -> None:
         """One workspace (amplitude part prepared) per concurrently used channel."""
         prog = self.plan.program

@@ -273,6 +273,7 @@ def arnoldi_channels(ops, sources, shifts: torch.Tensor, *, maximum_dimension: i
     streams = [torch.cuda.Stream(device=dev) for _ in range(nch)]
     cur = torch.cuda.current_stream(dev)
     sink_conj = torch.conj(sink).resolve_conj().contiguous() if sink is not None else None
+    xcsr = ops.input_scatter_csr()
     per = []
     for c, b in enumerate(sources):
         d = {
@@ -304,6 +305,7 @@ def arnoldi_channels(ops, sources, shifts: torch.Tensor, *, maximum_dimension: i
         q.work, q.counters = d["work"].data_ptr(), d["counters"].data_ptr()
         q.V32, q.work32 = d["V32"].data_ptr(), d["work32"].data_ptr()
         q.V32lo, q.work32lo = d["V32lo"].data_ptr(), d["work32lo"].data_ptr()
+        q.xscatter_offsets, q.xscatter_dst, q.xscatter_sign = (t.data_ptr() for t in xcsr)
         q.check_dims, q.check_res, q.check_capacity = d["cdims"].ctypes.data, d["cres"].ctypes.data, d["cdims"].size
     for st in streams:
         st.wait_stream(cur)

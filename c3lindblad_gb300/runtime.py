@@ -95,7 +95,8 @@ class ArnoldiChannel(C.Structure):
                 ("Hcol", C.c_void_p), ("coeff", C.c_void_p), ("partial", C.c_void_p), ("host", C.c_void_p),
                 ("H", C.c_void_p), ("hess", HessenbergState), ("status_host", C.c_void_p), ("work", C.c_void_p),
                 ("counters", C.c_void_p), ("V32", C.c_void_p), ("work32", C.c_void_p), ("V32lo", C.c_void_p),
-                ("work32lo", C.c_void_p), ("check_dims", C.c_void_p),
+                ("work32lo", C.c_void_p), ("xscatter_offsets", C.c_void_p), ("xscatter_dst", C.c_void_p),
+                ("xscatter_sign", C.c_void_p), ("check_dims", C.c_void_p),
                 ("check_res", C.c_void_p), ("check_capacity", C.c_int32),
                 ("m", C.c_int32), ("breakdown", C.c_int32), ("converged", C.c_int32), ("nchecks", C.c_int32),
                 ("pad", C.c_int32), ("beta", C.c_double), ("action_seconds", C.c_double), ("launches", C.c_int64)]

@@ -455,6 +455,14 @@ typedef struct {
     c3l_complex32* work32;             /* device [N]: FP32 copy of each sigma output        */
     c3l_complex32* V32lo;              /* device (m_max+1) x N: V - V32 in FP32 (low parts) */
     c3l_complex32* work32lo;           /* device [N]: low part of the updated work vector   */
+    /* optional (NULL: the sigma scatters its input itself): the nonzero entries
+     * of the sigma's input scatter (sigma->action.scatter_*) grouped by input
+     * element, so that each step writes the next step's padded input blocks
+     * as it forms V[j+1]: entries [xscatter_offsets[i], xscatter_offsets[i+1])
+     * are ws[xscatter_dst[e]] = xscatter_sign[e] * x[i]. */
+    const int64_t* xscatter_offsets;   /* device [N + 1] */
+    const int64_t* xscatter_dst;
+    const double* xscatter_sign;
     int32_t* check_dims;               /* host [check_capacity]                   */
     double* check_res;                 /* host [check_capacity]                   */
     int32_t check_capacity;
