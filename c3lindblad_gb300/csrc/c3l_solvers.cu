@@ -324,16 +324,20 @@ c3l_status c3l_gmres(c3l_gmres_args* a, void* stream) {
     double presid = 0.0;
     std::vector<double> S(restart + 1), h((size_t)restart * (restart + 1)), gc(restart), gs(restart), y;
     auto H = [&](int col, int row) -> double& { return h[(size_t)col * (restart + 1) + row]; };
+    // M r of the next cycle goes to tmp (FP32 basis) or V[0] (FP64 basis); its
+    // norm is read together with |r| at the end of each cycle
+    double* mr = f32b ? a->tmp : V;
+    double beta_next = -1.0;
     for (int iteration = 0; iteration < a->maxiter; ++iteration) {
         if (iteration == 0 && bnrm2 < atol) return C3L_OK;
-        double beta;
+        double beta = beta_next;
+        if (beta < 0.0) {
+            if ((st = psolve(a->r, mr))) return st;
+            if ((st = norm(mr, beta))) return st;
+        }
         if (f32b) {
-            if ((st = psolve(a->r, a->tmp))) return st;
-            if ((st = norm(a->tmp, beta))) return st;
             if ((st = c3l::gm_start_f32(n, 1.0 / beta, a->tmp, Vf, xcur, s))) return st;
         } else {
-            if ((st = psolve(a->r, V))) return st;
-            if ((st = norm(V, beta))) return st;
             if ((st = c3l_scale_r(n, 1.0 / beta, V, V, stream))) return st;
             if (cudaMemcpyAsync(xcur, V, n * sizeof(double), cudaMemcpyDeviceToDevice, s) != cudaSuccess)
                 return C3L_ERR_LAUNCH;
@@ -409,7 +413,15 @@ c3l_status c3l_gmres(c3l_gmres_args* a, void* stream) {
         if (cudaMemcpyAsync(a->r, a->b, n * sizeof(double), cudaMemcpyDeviceToDevice, s) != cudaSuccess) return C3L_ERR_LAUNCH;
         if ((st = c3l_multi_axpy_r(a->tmp, n, 1, ones, -1.0, a->r, n, stream))) return st;
         a->launches += 2 + jvp_nodes;  // two axpys and the JVP
-        if ((st = norm(a->r, rnorm))) return st;
+        // |r| and, for the next cycle, M r and |M r|: one read-back
+        if ((st = psolve(a->r, mr))) return st;
+        if ((st = c3l_multi_dot_r(a->r, n, 1, a->r, n, a->partial, coeff, stream)) ||
+            (st = c3l_multi_dot_r(mr, n, 1, mr, n, a->partial, coeff + 1, stream)))
+            return st;
+        a->launches += 4;
+        if ((st = d2h(host, coeff, 2 * sizeof(double), s))) return st;
+        rnorm = std::sqrt(std::max(host[0], 0.0));
+        beta_next = std::sqrt(std::max(host[1], 0.0));
         if (rnorm <= atol) break;
         if (breakdown) break;
         if (presid <= ptol) ptol_max_factor = std::max(eps, 0.25 * ptol_max_factor);
