@@ -427,18 +427,19 @@ def test_single_precision_jvp_tracks_fp64(problems, cuda_device):
     assert 0 < err < 1e-5
 
 
-@pytest.mark.parametrize("basis_f32", [False, True])
-def test_newton_correction_gmres_fp32_operator(basis_f32, problems, cuda_device):
+@pytest.mark.parametrize("basis_f32,restart", [(False, 30), (True, 30), (True, 70)])
+def test_newton_correction_gmres_fp32_operator(basis_f32, restart, problems, cuda_device):
     """c3l_gmres with the FP32 JVP, with an FP64 or an FP32 Krylov basis: the
     correction meets the requested relative tolerance of the FP64 system
-    M J s = -M r (left preconditioned) up to the FP32 operator's accuracy."""
+    M J s = -M r (left preconditioned) up to the FP32 operator's accuracy;
+    restart 70 takes the FP32 basis past 64 rows."""
     spec, g, p = problems("siam10")
     ops = p.ops
     x = torch.from_numpy(g["fixed_variables"]).to(cuda_device)
     r = torch.empty_like(x)
     ops.linearize(x, r)
     ops.to_single()
-    solver = p.gmres_solver(30)
+    solver = p.gmres_solver(restart)
     s = torch.zeros_like(x)
     rtol = 1e-4
     info, hist, matvecs = solver.solve(-r, s, rtol=rtol, atol=0.0, maxiter=40, single=True, basis_f32=basis_f32)
