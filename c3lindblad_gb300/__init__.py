@@ -23,13 +23,20 @@ from .response import (
     ArnoldiProjection,
     ComponentRetardedGreen,
     ComponentRetardedMatrixArnoldiGreen,
+    ComponentRetardedMatrixGreen,
+    ComponentRetardedMatrixTime,
+    ComponentShiftedMatrixArnoldiGreen,
     ComponentShiftedSolution,
     ComponentSigmaOperator,
     EOMCCSDProblem,
     component_eom_context,
     component_eom_sources,
     component_retarded_green,
+    component_retarded_matrix_green,
     component_retarded_matrix_green_arnoldi,
+    component_retarded_matrix_green_shifts,
+    component_retarded_matrix_time,
+    component_retarded_time,
     eom_ccsd_problem,
     solve_component_shifted,
 )
@@ -41,4 +48,7 @@ __all__ = [
     "ComponentShiftedSolution", "ComponentSigmaOperator", "EOMCCSDProblem", "component_eom_context",
     "component_eom_sources", "component_retarded_green", "eom_ccsd_problem", "ArnoldiProjection",
     "ComponentRetardedMatrixArnoldiGreen", "component_retarded_matrix_green_arnoldi", "solve_component_shifted",
+    "ComponentRetardedMatrixGreen", "ComponentRetardedMatrixTime", "ComponentShiftedMatrixArnoldiGreen",
+    "component_retarded_matrix_green", "component_retarded_matrix_green_shifts", "component_retarded_matrix_time",
+    "component_retarded_time",
 ]

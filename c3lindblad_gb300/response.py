@@ -504,6 +504,88 @@ class ArnoldiProjection:
             vec.axpy_c(self._V, m, Y[s], 1.0, out[s])
         return out.cpu().numpy()
 
+    def projected_rows(self, rows: torch.Tensor, m: int) -> np.ndarray:
+        """P[a, k] = rows[a] . v_k (bilinear) for k < m, from the device basis."""
+        vec = DeviceVectors(self._V.device)
+        out = torch.empty((rows.shape[0], m), dtype=torch.complex128, device=self._V.device)
+        for a in range(rows.shape[0]):
+            vec.dots_c(self._V, m, torch.conj(rows[a]).resolve_conj().contiguous(), out[a])
+        return np.conj(out.cpu().numpy())
+
+    def time_coefficients(self, time_points, *, dimension=None) -> np.ndarray:
+        """exp(-i H_m t) |b| e_1 on a time grid (``krylov.py:134-176``): SciPy's
+        ``expm_multiply`` on the m x m Hessenberg matrix, one call for a uniform
+        grid, one per time otherwise."""
+        from scipy.sparse.linalg import expm_multiply
+
+        t = np.asarray(time_points, dtype=np.float64)
+        if t.ndim != 1 or t.size == 0 or not np.all(np.isfinite(t)):
+            raise ValueError("time must be a finite nonempty vector")
+        m = self._dim(dimension)
+        H = self.hessenberg[:m, :m]
+        rhs = np.zeros(m, dtype=np.complex128)
+        rhs[0] = self.source_norm
+        if t.size == 1:
+            reduced = expm_multiply(-1j * float(t[0]) * H, rhs)[None, :]
+        elif np.allclose(np.diff(t), t[1] - t[0], atol=1.0e-14, rtol=1.0e-14):
+            reduced = expm_multiply(-1j * H, rhs, start=float(t[0]), stop=float(t[-1]), num=t.size, endpoint=True)
+        else:
+            reduced = np.asarray([expm_multiply(-1j * float(v) * H, rhs) for v in t], dtype=np.complex128)
+        return np.asarray(reduced, dtype=np.complex128)
+
+    def time_residual_norms(self, time_points, *, dimension=None) -> np.ndarray:
+        """|h_{m+1,m} e_m^T exp(-i H_m t) |b| e_1|: the propagator's own residual."""
+        m = self._dim(dimension)
+        reduced = self.time_coefficients(time_points, dimension=m)
+        return np.abs(self.hessenberg[m, m - 1] * reduced[:, -1]).astype(np.float64)
+
+    def relative_time_residuals(self, time_points, *, dimension=None) -> np.ndarray:
+        return self.time_residual_norms(time_points, dimension=dimension) / max(float(self.source_norm),
+                                                                                np.finfo(np.float64).tiny)
+
+    def transfer(self, shifts, sink, *, dimension=None) -> np.ndarray:
+        """sink . x(z) at the full projection or one saved prefix (``krylov.py:210-224``)."""
+        row = np.asarray(sink, dtype=np.complex128)
+        if row.shape != (self.vector_dimension,) or not np.all(np.isfinite(row)):
+            raise ValueError("sink must match the full vector dimension")
+        m = self._dim(dimension)
+        reduced = self.coefficients(shifts, dimension=m)
+        rows = torch.from_numpy(row.copy()).to(self._V.device)[None, :]
+        return np.asarray(reduced @ self.projected_rows(rows, m)[0], dtype=np.complex128)
+
+    @property
+    def orthogonality_defect(self) -> np.float64:
+        """|V_m^H V_m - I|_F / m (``krylov.py:392-399``), formed on the device on first use."""
+        if getattr(self, "_orth", None) is None:
+            m = self.dimension
+            vec = DeviceVectors(self._V.device)
+            gram = torch.empty((m, m), dtype=torch.complex128, device=self._V.device)
+            for k in range(m):
+                vec.dots_c(self._V, m, self._V[k], gram[k])  # gram[k, j] = conj(v_j) . v_k
+            g = gram.cpu().numpy().T
+            self._orth = np.float64(np.linalg.norm(g - np.eye(m), ord="fro") / max(float(m), 1.0))
+        return self._orth
+
+    def to_dict(self) -> dict:
+        return {
+            "krylov_dimension": self.dimension,
+            "full_vector_dimension": self.vector_dimension,
+            "source_norm": float(self.source_norm),
+            "terminal_coupling_absolute": float(abs(self.terminal_coupling)),
+            "orthogonality_defect": float(self.orthogonality_defect),
+            "action_wall_seconds": [float(v) for v in self.action_wall_seconds],
+            "action_wall_seconds_total": float(np.sum(self.action_wall_seconds)),
+            "construction_wall_seconds": float(self.construction_wall_seconds),
+            "peak_rss_kib": self.peak_rss_kib,
+            "breakdown": self.breakdown,
+            "check_dimensions": list(self.check_dimensions),
+            "check_maximum_relative_residuals": [float(v) for v in self.check_maximum_relative_residuals],
+            "maximum_relative_residual": float(self.check_maximum_relative_residuals[-1]),
+            "residual_tolerance": float(self.residual_tolerance),
+            "converged": self.converged,
+            "method": "two_pass_one_sided_Arnoldi_shift_invariant_resolvent",
+        }
+
 
 @dataclass(frozen=True)
 class ComponentRetardedMatrixArnoldiGreen:
@@ -578,37 +660,53 @@ def component_retarded_matrix_green_arnoldi(operator, sources, omega, eta: float
         raise ValueError("omega and positive eta must be finite")
     max_dim, min_dim = _validated_krylov_controls(operator, maximum_krylov_dimension, minimum_krylov_dimension,
                                                   check_interval, residual_tolerance)
+    r = _matrix_arnoldi_response(operator, columns, (frequency + 1j * broadening).astype(np.complex128),
+                                 max_dim, min_dim, float(residual_tolerance), int(check_interval))
+    return ComponentRetardedMatrixArnoldiGreen(
+        omega=frequency, eta=broadening, sites=r["sites"], addition=r["values"][0], removal=r["values"][1],
+        retarded=r["values"][0] + r["values"][1], addition_projections=r["projections"][0],
+        removal_projections=r["projections"][1], addition_relative_residuals=r["residuals"][0],
+        removal_relative_residuals=r["residuals"][1], component_action_calls=r["calls"],
+        component_action_wall_seconds=r["action_seconds"], wall_seconds=float(time.perf_counter() - started),
+        peak_rss_kib=r["rss"])
+
+
+def _padded_source(item, which: int, N: int, dev) -> torch.Tensor:
+    """Addition (0), removal (1) or sink (2) of a source column on the device, zero-padded to N."""
+    if item.device:
+        v = item.device[which]
+    else:
+        v = torch.from_numpy(np.asarray((item.addition, item.removal, item.sink)[which], np.complex128).copy()).to(dev)
+    if v.numel() < N:
+        v = torch.cat([v, torch.zeros(N - v.numel(), dtype=torch.complex128, device=dev)])
+    return v.contiguous()
+
+
+def _matrix_arnoldi_response(operator, columns, shifts: np.ndarray, max_dim: int, min_dim: int, tolerance: float,
+                             interval: int) -> dict:
+    """One Arnoldi basis per source and channel, all channels concurrent, every sink
+    row contracted from each basis (``component_response.py:550-625``): for channel
+    b, ``values[:, a, b] = Y(z) (sink_a . V_m)^T`` with the reduced coordinates Y
+    solved on the device for every shift."""
     ops = operator.context.ops
     dev = ops.device
     N = operator.dimension
-
-    def device_vec(item, which):
-        if item.device:
-            v = item.device[which]
-        else:
-            v = torch.from_numpy(np.asarray((item.addition, item.removal, item.sink)[which],
-                                            np.complex128).copy()).to(dev)
-        if v.numel() < N:
-            v = torch.cat([v, torch.zeros(N - v.numel(), dtype=torch.complex128, device=dev)])
-        return v.contiguous()
-
     vectors = []
     for item in columns:
-        vectors += [device_vec(item, 0), device_vec(item, 1)]
-    sinks = [device_vec(item, 2) for item in columns]
-    shifts = torch.from_numpy((frequency + 1j * broadening).astype(np.complex128)).to(dev)
+        vectors += [_padded_source(item, 0, N, dev), _padded_source(item, 1, N, dev)]
+    sinks = [_padded_source(item, 2, N, dev) for item in columns]
+    z = torch.from_numpy(np.ascontiguousarray(shifts, dtype=np.complex128)).to(dev)
     action_seconds0 = operator.action_wall_seconds
     t_action = time.perf_counter()
-    bases = arnoldi_channels(ops, vectors, shifts, maximum_dimension=max_dim,
-                             residual_tolerance=float(residual_tolerance), minimum_dimension=min_dim,
-                             check_interval=int(check_interval))
+    bases = arnoldi_channels(ops, vectors, z, maximum_dimension=max_dim, residual_tolerance=tolerance,
+                             minimum_dimension=min_dim, check_interval=interval)
     calls = sum(b.m for b in bases)
     operator.action_calls += calls
     operator.action_wall_seconds += time.perf_counter() - t_action
     if not all(b.converged for b in bases):
         raise RuntimeError("a component EOM matrix Arnoldi projection failed")
     S = len(columns)
-    ns = frequency.size
+    ns = shifts.size
     values = [np.empty((ns, S, S), np.complex128), np.empty((ns, S, S), np.complex128)]
     residuals = [np.empty((S, ns), np.float64), np.empty((S, ns), np.float64)]
     vec = DeviceVectors(dev)
@@ -616,7 +714,7 @@ def component_retarded_matrix_green_arnoldi(operator, sources, omega, eta: float
     for idx, basis in enumerate(bases):
         b, kind = divmod(idx, 2)
         m = basis.m
-        Y = reduced_coordinates(basis, shifts)                     # [ns, m]
+        Y = reduced_coordinates(basis, z)                          # [ns, m]
         for a in range(S):
             # p_k = sink_a . v_k (bilinear), then values[s, a, b] = sum_k Y[s, k] p_k
             pc = torch.empty(m, dtype=torch.complex128, device=dev)
@@ -626,12 +724,273 @@ def component_retarded_matrix_green_arnoldi(operator, sources, omega, eta: float
             values[kind][:, a, b] = np.conj(g.cpu().numpy())
         residuals[kind][b] = basis.residual.cpu().numpy()
     rss = int(resource.getrusage(resource.RUSAGE_SELF).ru_maxrss)
-    proj = [ArnoldiProjection(bb, residual_tolerance, rss) for bb in bases]
-    return ComponentRetardedMatrixArnoldiGreen(
-        omega=frequency, eta=broadening, sites=tuple(int(item.site) for item in columns),
-        addition=values[0], removal=values[1], retarded=values[0] + values[1],
-        addition_projections=tuple(proj[0::2]), removal_projections=tuple(proj[1::2]),
-        addition_relative_residuals=residuals[0], removal_relative_residuals=residuals[1],
-        component_action_calls=int(calls),
-        component_action_wall_seconds=float(operator.action_wall_seconds - action_seconds0),
-        wall_seconds=float(time.perf_counter() - started), peak_rss_kib=rss)
+    proj = [ArnoldiProjection(bb, tolerance, rss) for bb in bases]
+    return {"sites": tuple(int(item.site) for item in columns), "values": values, "residuals": residuals,
+            "projections": (tuple(proj[0::2]), tuple(proj[1::2])), "calls": int(calls),
+            "action_seconds": float(operator.action_wall_seconds - action_seconds0), "rss": rss}
+
+
+@dataclass(frozen=True)
+class ComponentShiftedMatrixArnoldiGreen:
+    """``retarded[k, a, b]`` = G^R_ab(z_k), sink a, source b (``component_response.py:427-446``)."""
+    shifts: np.ndarray
+    sites: tuple
+    addition: np.ndarray
+    removal: np.ndarray
+    retarded: np.ndarray
+    addition_projections: tuple
+    removal_projections: tuple
+    addition_relative_residuals: np.ndarray
+    removal_relative_residuals: np.ndarray
+    action_calls: int
+    wall_seconds: float
+    peak_rss_kib: int
+
+
+def component_retarded_matrix_green_shifts(operator, sources, shifts, *, maximum_krylov_dimension: int = 320,
+                                           residual_tolerance: float = 1.0e-10, minimum_krylov_dimension: int = 16,
+                                           check_interval: int = 8) -> ComponentShiftedMatrixArnoldiGreen:
+    """G^R(z) at complex shifts with Im z > 0 (``component_response.py:449-493``):
+    the matrix Arnoldi response without the omega + i eta restriction, so
+    imaginary-axis points share one Krylov space per source with real-axis
+    points.  Same inputs, controls, errors and result fields as the reference."""
+    started = time.perf_counter()
+    if not hasattr(operator, "action_calls"):
+        raise TypeError("operator must be an instrumented ComponentSigmaOperator")
+    columns, _ = _validated_source_columns(operator, sources)
+    z = np.asarray(shifts, dtype=np.complex128)
+    if z.ndim != 1 or z.size == 0 or not np.all(np.isfinite(z)) or np.any(z.imag <= 0.0):
+        raise ValueError("shifts must be finite with positive imaginary parts")
+    max_dim, min_dim = _validated_krylov_controls(operator, maximum_krylov_dimension, minimum_krylov_dimension,
+                                                  check_interval, residual_tolerance)
+    r = _matrix_arnoldi_response(operator, columns, z, max_dim, min_dim, float(residual_tolerance),
+                                 int(check_interval))
+    return ComponentShiftedMatrixArnoldiGreen(
+        shifts=np.asarray(z, dtype=np.complex128), sites=r["sites"], addition=r["values"][0],
+        removal=r["values"][1], retarded=r["values"][0] + r["values"][1], addition_projections=r["projections"][0],
+        removal_projections=r["projections"][1], addition_relative_residuals=r["residuals"][0],
+        removal_relative_residuals=r["residuals"][1], action_calls=r["calls"],
+        wall_seconds=float(time.perf_counter() - started), peak_rss_kib=r["rss"])
+
+
+# ============================================================ time domain
+def _arnoldi_projections(operator, vectors, shifts: np.ndarray, max_dim: int, tolerance: float):
+    """``arnoldi_resolvent`` with the time drivers' controls (minimum dimension
+    min(16, N), check interval min(8, N)) for several source vectors at once;
+    one action call per basis vector, as the reference counts them."""
+    ops = operator.context.ops
+    N = operator.dimension
+    z = torch.from_numpy(np.ascontiguousarray(shifts, dtype=np.complex128)).to(ops.device)
+    t0 = time.perf_counter()
+    bases = arnoldi_channels(ops, vectors, z, maximum_dimension=max_dim, residual_tolerance=tolerance,
+                             minimum_dimension=min(16, N), check_interval=min(8, N))
+    operator.action_calls += sum(b.m for b in bases)
+    operator.action_wall_seconds += time.perf_counter() - t0
+    rss = int(resource.getrusage(resource.RUSAGE_SELF).ru_maxrss)
+    return [ArnoldiProjection(b, tolerance, rss) for b in bases]
+
+
+def component_retarded_time(operator, sources, time_points, *, maximum_krylov_dimension: int = 160,
+                            residual_tolerance: float = 1.0e-11) -> np.ndarray:
+    """-i sink . exp(-i K t) (addition + removal) for t >= 0 (``component_response.py:628-663``).
+
+    One Arnoldi basis of the combined source (stopping test at the probe shift
+    z = i, as in the reference) is built on the device; the propagator acts on
+    the m x m Hessenberg matrix (SciPy's ``expm`` per time, as the reference).
+    """
+    from scipy.linalg import expm
+
+    t = np.asarray(time_points, dtype=np.float64)
+    N = operator.dimension
+    dev = operator.context.ops.device
+    source = _padded_source(sources, 0, N, dev) + _padded_source(sources, 1, N, dev)
+    sink = _padded_source(sources, 2, N, dev)
+    proj = _arnoldi_projections(operator, [source.contiguous()], np.asarray([1j], np.complex128),
+                                int(min(maximum_krylov_dimension, N)), float(residual_tolerance))[0]
+    m = proj.dimension
+    H = proj.hessenberg[:m, :m]
+    reduced_source = np.zeros(m, dtype=np.complex128)
+    reduced_source[0] = proj.source_norm
+    projected_sink = proj.projected_rows(sink[None, :], m)[0]
+    out = np.empty(t.size, dtype=np.complex128)
+    for i, value in enumerate(t):
+        out[i] = -1j * (projected_sink @ (expm(-1j * float(value) * H) @ reduced_source))
+    return out
+
+
+@dataclass(frozen=True)
+class ComponentRetardedMatrixTime:
+    """Direct-time impurity Green matrix from one basis per source column (``component_response.py:666-682``)."""
+    time: np.ndarray
+    sites: tuple
+    addition: np.ndarray
+    removal: np.ndarray
+    retarded: np.ndarray
+    channel_sum_defect: float
+    combined_projections: tuple
+    addition_projections: tuple
+    removal_projections: tuple
+    combined_relative_time_residuals: np.ndarray
+    addition_relative_time_residuals: np.ndarray
+    removal_relative_time_residuals: np.ndarray
+    wall_seconds: float
+    peak_rss_kib: int
+
+
+def _matrix_time_from_projections(projections, sinks: torch.Tensor, t: np.ndarray) -> np.ndarray:
+    """out[:, a, b] = -i exp(-i H t) |b| e_1 . (sink_a . V_m) (``component_response.py:685-699``)."""
+    out = np.empty((t.size, sinks.shape[0], len(projections)), dtype=np.complex128)
+    for b, proj in enumerate(projections):
+        m = proj.dimension
+        projected = proj.projected_rows(sinks, m)              # [S, m]
+        out[:, :, b] = -1j * (proj.time_coefficients(t) @ projected.T)
+    return out
+
+
+def component_retarded_matrix_time(operator, sources, time_points, validation_shifts, *,
+                                   maximum_krylov_dimension: int = 160, residual_tolerance: float = 1.0e-11,
+                                   include_channels: bool = True) -> ComponentRetardedMatrixTime:
+    """All sink rows from one combined-source basis per source orbital, plus the
+    separate addition/removal bases when ``include_channels`` (the channel-sum
+    diagnostic).  Same inputs, errors and result fields as the reference
+    (``component_response.py:702-815``); all bases run as concurrent device
+    channels."""
+    started = time.perf_counter()
+    columns = tuple(sources)
+    if not columns:
+        raise ValueError("at least one impurity source is required")
+    if len({item.site for item in columns}) != len(columns):
+        raise ValueError("impurity source sites must be unique")
+    if any(item.charge != columns[0].charge for item in columns):
+        raise ValueError("all impurity sources must use one response charge")
+    retained = np.asarray(columns[0].addition).size
+    for item in columns:
+        if (np.asarray(item.addition).shape != (retained,) or np.asarray(item.removal).shape != (retained,)
+                or np.asarray(item.sink).shape != (retained,)):
+            raise ValueError("impurity sources and sinks must share one retained basis")
+    if operator.dimension < retained:
+        raise ValueError("response operator is smaller than the retained sources")
+    t = np.asarray(time_points, dtype=np.float64)
+    z = np.asarray(validation_shifts, dtype=np.complex128)
+    if (t.ndim != 1 or t.size == 0 or np.any(t < 0.0) or not np.all(np.isfinite(t)) or z.ndim != 1 or z.size == 0
+            or not np.all(np.isfinite(z))):
+        raise ValueError("time and validation shifts must be finite nonempty vectors")
+    N = operator.dimension
+    dev = operator.context.ops.device
+    sinks = torch.stack([_padded_source(item, 2, N, dev) for item in columns])
+    vectors = [(_padded_source(item, 0, N, dev) + _padded_source(item, 1, N, dev)).contiguous() for item in columns]
+    if include_channels:
+        vectors += [_padded_source(item, 0, N, dev) for item in columns]
+        vectors += [_padded_source(item, 1, N, dev) for item in columns]
+    proj = _arnoldi_projections(operator, vectors, z, int(min(maximum_krylov_dimension, N)),
+                                float(residual_tolerance))
+    S = len(columns)
+    combined = tuple(proj[:S])
+    retarded = _matrix_time_from_projections(combined, sinks, t)
+    combined_res = np.asarray([p.relative_time_residuals(t) for p in combined], dtype=np.float64)
+    if include_channels:
+        add_p, rem_p = tuple(proj[S:2 * S]), tuple(proj[2 * S:])
+        addition = _matrix_time_from_projections(add_p, sinks, t)
+        removal = _matrix_time_from_projections(rem_p, sinks, t)
+        add_res = np.asarray([p.relative_time_residuals(t) for p in add_p], dtype=np.float64)
+        rem_res = np.asarray([p.relative_time_residuals(t) for p in rem_p], dtype=np.float64)
+        defect = float(np.max(abs(retarded - addition - removal)))
+    else:
+        add_p = rem_p = ()
+        add_res = np.empty((0, t.size), dtype=np.float64)
+        rem_res = np.empty((0, t.size), dtype=np.float64)
+        addition = np.full_like(retarded, np.nan + 1j * np.nan)
+        removal = np.full_like(retarded, np.nan + 1j * np.nan)
+        defect = float("nan")
+    return ComponentRetardedMatrixTime(
+        time=t, sites=tuple(int(item.site) for item in columns), addition=addition, removal=removal,
+        retarded=retarded, channel_sum_defect=defect, combined_projections=combined, addition_projections=add_p,
+        removal_projections=rem_p, combined_relative_time_residuals=combined_res,
+        addition_relative_time_residuals=add_res, removal_relative_time_residuals=rem_res,
+        wall_seconds=float(time.perf_counter() - started),
+        peak_rss_kib=int(resource.getrusage(resource.RUSAGE_SELF).ru_maxrss))
+
+
+# ============================================= matrix response, GMRES form
+@dataclass(frozen=True)
+class ComponentRetardedMatrixGreen:
+    """Frequency-domain Green matrix from one response solve per source column
+    and frequency (``component_response.py:145-158``)."""
+    omega: np.ndarray
+    eta: float
+    sites: tuple
+    addition: np.ndarray
+    removal: np.ndarray
+    retarded: np.ndarray
+    addition_solutions: tuple
+    removal_solutions: tuple
+    wall_seconds: float
+    peak_rss_kib: int
+
+
+def component_retarded_matrix_green(operator, sources, omega, eta: float, *, rtol: float = 1.0e-10,
+                                    restart: int = 40, maxiter: int = 200) -> ComponentRetardedMatrixGreen:
+    """All sink rows with one addition/removal solve per source column and frequency
+    (``component_response.py:248-353``): preconditioned restarted GMRES on the
+    device (``c3l_gmres_shifted``), each frequency started from the previous
+    frequency's solution, every sink contracted with the same solutions.  Axes
+    ``(omega, sink_site, source_site)``; a solve that misses the convergence
+    rule of ``solve_component_shifted`` raises."""
+    columns = tuple(sources)
+    if not columns:
+        raise ValueError("at least one impurity source is required")
+    if len({item.site for item in columns}) != len(columns):
+        raise ValueError("impurity source sites must be unique")
+    if any(item.charge != columns[0].charge for item in columns):
+        raise ValueError("all impurity sources must use one response charge")
+    retained = np.asarray(columns[0].addition).size
+    for item in columns:
+        if (np.asarray(item.addition).shape != (retained,) or np.asarray(item.removal).shape != (retained,)
+                or np.asarray(item.sink).shape != (retained,)):
+            raise ValueError("impurity sources and sinks must share one retained basis")
+    if operator.dimension < retained:
+        raise ValueError("response operator is smaller than the retained sources")
+    frequency = np.asarray(omega, dtype=np.float64)
+    broadening = float(eta)
+    if (frequency.ndim != 1 or frequency.size == 0 or not np.all(np.isfinite(frequency))
+            or not np.isfinite(broadening) or broadening <= 0.0):
+        raise ValueError("omega and positive eta must be finite")
+    op = operator if isinstance(operator, ComponentSigmaOperator) else ComponentSigmaOperator(operator)
+    ops = op.context.ops
+    dev = ops.device
+    N = op.dimension
+    S = len(columns)
+    started = time.perf_counter()
+    sinks_conj = torch.stack([torch.conj(_padded_source(item, 2, N, dev)).resolve_conj() for item in columns])
+    shape = (frequency.size, S, S)
+    values = [np.empty(shape, np.complex128), np.empty(shape, np.complex128)]
+    records = [[], []]
+    solver = _shifted_solver(op, restart)
+    vec = DeviceVectors(dev)
+    row = torch.empty(S, dtype=torch.complex128, device=dev)
+    for b, item in enumerate(columns):
+        for kind in (0, 1):
+            rhs = _padded_source(item, kind, N, dev)
+            bnorm = float(torch.linalg.vector_norm(rhs).item())
+            x = torch.zeros_like(rhs)
+            per = []
+            for i, w in enumerate(frequency):
+                z = complex(float(w), broadening)
+                t0 = time.perf_counter()
+                info, hist, matvecs = solver.solve(z, _jacobi_inverse(op.diagonal, z), rhs, x, rtol=rtol,
+                                                   maxiter=maxiter, use_x0=i > 0)
+                op.action_calls += matvecs + 1
+                true = _true_relative_residual(ops, z, x, rhs, bnorm)
+                converged = bool(info == 0 and true <= max(10.0 * rtol, 1.0e-12))
+                if not converged:
+                    raise RuntimeError("a component EOM matrix shifted solve failed")
+                vec.dots_c(sinks_conj, S, x, row)                 # sink_a . x (bilinear)
+                values[kind][i, :, b] = row.cpu().numpy()
+                per.append(ComponentShiftedSolution(None, i, converged, len(hist), true, tuple(hist),
+                                                    time.perf_counter() - t0, solution=x.cpu().numpy(), info=info))
+            records[kind].append(tuple(per))
+    return ComponentRetardedMatrixGreen(
+        omega=frequency, eta=broadening, sites=tuple(int(item.site) for item in columns), addition=values[0],
+        removal=values[1], retarded=values[0] + values[1], addition_solutions=tuple(records[0]),
+        removal_solutions=tuple(records[1]), wall_seconds=float(time.perf_counter() - started),
+        peak_rss_kib=int(resource.getrusage(resource.RUSAGE_SELF).ru_maxrss))

@@ -17,7 +17,9 @@ reference's own setup code, runs the reference's CPU hot path and writes:
 
 The GPU machine never runs this script; only the ``.npz`` files travel.
 
-Usage: ``python tests/golden/make_fixtures.py [--reference SRC] [names...]``
+Usage: ``python tests/golden/make_fixtures.py [--reference SRC] [names...]``;
+``... matrix``, ``... warmstart`` and ``... drivers [names...]`` write the
+matrix-response, warm-start and response-driver fixtures.
 """
 
 from __future__ import annotations
@@ -463,6 +465,78 @@ def export_matrix_green(path: Path) -> None:
           f"{[p.dimension for p in res.removal_projections]}", flush=True)
 
 
+DRIVERS = {
+    # fixture: source sites, GMRES matrix frequencies/eta, shifts (Matsubara points
+    # i(2k+1)pi/beta and real-axis points omega + i eta), time grid, time validation shifts
+    "twosrc": dict(sites=(0, 1), gmres_omega=np.linspace(-2.0, 2.0, 9), gmres_eta=0.1,
+                   shifts=np.r_[1j * (2 * np.arange(6) + 1) * np.pi / 8.0, np.linspace(-2.0, 2.0, 5) + 0.1j],
+                   time=np.linspace(0.0, 12.0, 49), validation=np.linspace(-2.0, 2.0, 5) + 0.1j),
+    "siam10": dict(sites=(0,), gmres_omega=np.asarray([-1.0, 0.0, 1.5]), gmres_eta=0.2,
+                   shifts=np.r_[1j * (2 * np.arange(6) + 1) * np.pi / 10.0, np.linspace(-8.0, 8.0, 41) + 0.5j],
+                   time=np.linspace(0.0, 20.0, 81), validation=np.linspace(-4.0, 4.0, 9) + 0.2j),
+}
+
+
+def export_drivers(name: str, path: Path) -> None:
+    """The reference's other response drivers on a fixture's converged
+    amplitudes, charge +1: component_retarded_matrix_green (one GMRES solve per
+    source, channel and frequency), component_retarded_matrix_green_shifts
+    (complex shifts), component_retarded_time (first site) and
+    component_retarded_matrix_time (with the separate channels)."""
+    from c3l.cc.component_response import (
+        ComponentSigmaOperator, component_retarded_matrix_green, component_retarded_matrix_green_shifts,
+        component_retarded_matrix_time, component_retarded_time,
+    )
+    from c3l.cc.component_tensor import (
+        ComponentEOMProblem, ComponentStaticProblem, component_eom_context, component_eom_sources,
+    )
+    from c3l.cc.eom import eom_ccsd_problem
+
+    spec = DRIVERS[name]
+    cc = build_problem(FIXTURES[name])
+    static = ComponentStaticProblem.compile(cc)
+    golden = np.load(HERE / f"{name}.golden.npz")
+    amplitudes = golden["eom_amplitudes" if "eom_amplitudes" in golden.files else "solution_amplitudes"]
+    problem = ComponentEOMProblem.compile(eom_ccsd_problem(cc, response_spin=0), static, charge=1)
+    context = component_eom_context(problem, amplitudes)
+    sources = [component_eom_sources(context, site=s) for s in spec["sites"]]
+    out: dict = {"sites": np.asarray(spec["sites"], np.int64)}
+    t0 = time.perf_counter()
+    op = ComponentSigmaOperator(context)
+    mg = component_retarded_matrix_green(op, sources, spec["gmres_omega"], spec["gmres_eta"])
+    out.update(gmres_omega=mg.omega, gmres_eta=np.float64(mg.eta), gmres_addition=mg.addition,
+               gmres_removal=mg.removal, gmres_retarded=mg.retarded, gmres_calls=np.int64(op.action_calls),
+               gmres_seconds=np.float64(time.perf_counter() - t0))
+    t0 = time.perf_counter()
+    op = ComponentSigmaOperator(context)
+    sh = component_retarded_matrix_green_shifts(op, sources, spec["shifts"])
+    out.update(shifts=sh.shifts, shifts_addition=sh.addition, shifts_removal=sh.removal,
+               shifts_retarded=sh.retarded, shifts_addition_relative_residuals=sh.addition_relative_residuals,
+               shifts_removal_relative_residuals=sh.removal_relative_residuals,
+               shifts_addition_dimensions=np.asarray([p.dimension for p in sh.addition_projections], np.int64),
+               shifts_removal_dimensions=np.asarray([p.dimension for p in sh.removal_projections], np.int64),
+               shifts_action_calls=np.int64(sh.action_calls), shifts_seconds=np.float64(time.perf_counter() - t0))
+    t0 = time.perf_counter()
+    op = ComponentSigmaOperator(context)
+    out["time"] = spec["time"]
+    out["time_retarded"] = component_retarded_time(op, sources[0], spec["time"])
+    out["time_calls"] = np.int64(op.action_calls)
+    out["time_seconds"] = np.float64(time.perf_counter() - t0)
+    t0 = time.perf_counter()
+    op = ComponentSigmaOperator(context)
+    mt = component_retarded_matrix_time(op, sources, spec["time"], spec["validation"])
+    out.update(validation_shifts=spec["validation"], mtime_retarded=mt.retarded, mtime_addition=mt.addition,
+               mtime_removal=mt.removal, mtime_channel_sum_defect=np.float64(mt.channel_sum_defect),
+               mtime_combined_relative_time_residuals=mt.combined_relative_time_residuals,
+               mtime_addition_relative_time_residuals=mt.addition_relative_time_residuals,
+               mtime_removal_relative_time_residuals=mt.removal_relative_time_residuals,
+               mtime_combined_dimensions=np.asarray([p.dimension for p in mt.combined_projections], np.int64),
+               mtime_calls=np.int64(op.action_calls), mtime_seconds=np.float64(time.perf_counter() - t0))
+    np.savez_compressed(path, **out)
+    print(f"  [{name}] drivers: gmres {out['gmres_seconds']:.1f}s shifts {out['shifts_seconds']:.1f}s "
+          f"time {out['time_seconds']:.1f}s matrix time {out['mtime_seconds']:.1f}s", flush=True)
+
+
 def main() -> None:
     parser = argparse.ArgumentParser()
     parser.add_argument("--reference", default=str(HERE.parents[2] / "reference" / "src"))
@@ -474,6 +548,10 @@ def main() -> None:
         return
     if args.names == ["matrix"]:
         export_matrix_green(HERE / f"{MATRIX_GREEN['fixture']}.matrix.npz")
+        return
+    if args.names and args.names[0] == "drivers":
+        for name in args.names[1:] or list(DRIVERS):
+            export_drivers(name, HERE / f"{name}.drivers.npz")
         return
     names = args.names or list(FIXTURES)
     for name in names:

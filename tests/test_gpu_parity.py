@@ -512,3 +512,69 @@ def test_arnoldi_basis_long_vectors(name, problems, cuda_device):
         assert np.max(np.abs(V.conj().T @ V - np.eye(m + 1))) < 1e-12
         KV = np.stack([op.matvec(V[:, j]) for j in range(m)], axis=1)
         assert np.linalg.norm(KV - V @ H) / np.linalg.norm(H) < 1e-13
+
+
+@pytest.mark.parametrize("name", ["twosrc", "siam10"])
+def test_response_drivers_match_reference(name, problems):
+    """The reference's other response drivers (charge +1, converged amplitudes)
+    against its own outputs: the GMRES matrix response (one solve per source,
+    channel and frequency), the matrix response at complex shifts (Matsubara
+    and real-axis points), the time-domain propagation of one source and the
+    time-domain matrix with its separate channels.  Frequency-domain values
+    1e-8 relative (the G^R contract); Krylov dimensions within one check
+    interval; time-domain values 1e-7 relative (the Krylov spaces agree to
+    FP64 rounding, which the propagator carries to t = 20)."""
+    import c3lindblad_gb300 as c3
+    from conftest import GOLDEN
+
+    spec, g, p = problems(name)
+    ref = np.load(GOLDEN / f"{name}.drivers.npz")
+    ep = c3.ComponentEOMProblem.compile(c3.eom_ccsd_problem(p), p, 1)
+    ctx = c3.component_eom_context(ep, eom_amplitudes(g))
+    sources = [c3.component_eom_sources(ctx, site=int(s)) for s in ref["sites"]]
+    S = len(sources)
+    errors = {}
+
+    op = c3.ComponentSigmaOperator(ctx)
+    mg = c3.component_retarded_matrix_green(op, sources, ref["gmres_omega"], float(ref["gmres_eta"]))
+    assert mg.retarded.shape == (ref["gmres_omega"].size, S, S)
+    errors["gmres"] = relerr(mg.retarded, ref["gmres_retarded"])
+    errors["gmres_addition"] = relerr(mg.addition, ref["gmres_addition"])
+    assert all(r.converged for rows in mg.addition_solutions + mg.removal_solutions for r in rows)
+    assert mg.addition_solutions[0][0].solution.shape == (op.dimension,)
+
+    op = c3.ComponentSigmaOperator(ctx)
+    sh = c3.component_retarded_matrix_green_shifts(op, sources, ref["shifts"])
+    errors["shifts"] = relerr(sh.retarded, ref["shifts_retarded"])
+    errors["shifts_removal"] = relerr(sh.removal, ref["shifts_removal"])
+    dims = [pr.dimension for pr in sh.addition_projections + sh.removal_projections]
+    want = list(ref["shifts_addition_dimensions"]) + list(ref["shifts_removal_dimensions"])
+    assert all(abs(a - b) <= 8 for a, b in zip(dims, want)), (dims, want)
+    assert sh.action_calls == sum(dims) == op.action_calls
+    assert np.max(sh.addition_relative_residuals) <= 1e-10
+
+    op = c3.ComponentSigmaOperator(ctx)
+    tr = c3.component_retarded_time(op, sources[0], ref["time"])
+    errors["time"] = relerr(tr, ref["time_retarded"])
+    assert abs(op.action_calls - int(ref["time_calls"])) <= 8
+
+    op = c3.ComponentSigmaOperator(ctx)
+    mt = c3.component_retarded_matrix_time(op, sources, ref["time"], ref["validation_shifts"])
+    errors["matrix_time"] = relerr(mt.retarded, ref["mtime_retarded"])
+    errors["matrix_time_addition"] = relerr(mt.addition, ref["mtime_addition"])
+    assert [pr.dimension for pr in mt.combined_projections] == list(ref["mtime_combined_dimensions"]) or all(
+        abs(a - b) <= 8 for a, b in zip([pr.dimension for pr in mt.combined_projections],
+                                        ref["mtime_combined_dimensions"]))
+    assert mt.combined_relative_time_residuals.shape == (S, ref["time"].size)
+    assert mt.channel_sum_defect <= max(10 * float(ref["mtime_channel_sum_defect"]), 1e-12)
+    print(name, {k: f"{v:.2e}" for k, v in errors.items()})
+    for k in ("gmres", "gmres_addition", "shifts", "shifts_removal"):
+        assert errors[k] < 1e-8, (k, errors[k])
+    for k in ("time", "matrix_time", "matrix_time_addition"):
+        assert errors[k] < 1e-7, (k, errors[k])
+    # the projection's transfer and orthogonality diagnostics
+    pr = sh.addition_projections[0]
+    sink = np.concatenate([sources[0].sink, np.zeros(op.dimension - sources[0].sink.size, complex)])
+    assert relerr(pr.transfer(ref["shifts"][:4], sink), sh.addition[:4, 0, 0]) < 1e-10
+    assert pr.orthogonality_defect < 1e-12
+    assert pr.to_dict()["krylov_dimension"] == pr.dimension
