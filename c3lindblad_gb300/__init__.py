@@ -16,6 +16,7 @@ from .static import (
     component_static_residual,
     solve_component_ccsd,
 )
+from .matsubara import MatsubaraGreen, MatsubaraGrid, component_matsubara_green, matsubara_grid
 from .response import (
     ComponentEOMContext,
     ComponentEOMProblem,
@@ -50,5 +51,5 @@ __all__ = [
     "ComponentRetardedMatrixArnoldiGreen", "component_retarded_matrix_green_arnoldi", "solve_component_shifted",
     "ComponentRetardedMatrixGreen", "ComponentRetardedMatrixTime", "ComponentShiftedMatrixArnoldiGreen",
     "component_retarded_matrix_green", "component_retarded_matrix_green_shifts", "component_retarded_matrix_time",
-    "component_retarded_time",
+    "component_retarded_time", "MatsubaraGreen", "MatsubaraGrid", "component_matsubara_green", "matsubara_grid",
 ]

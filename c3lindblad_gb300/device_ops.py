@@ -21,6 +21,24 @@ def _cz(n: int, device) -> torch.Tensor:
     return torch.zeros(max(n, 1), dtype=torch.complex128, device=device)
 
 
+def _preconditioner_tables(plan: StaticPlan):
+    """(M blocks per representative, diagnostics, the same blocks in the JVP
+    output stage's element order for the fused M J): a function of the
+    compiled plan, formed once per plan."""
+    cached = plan.__dict__.get("_pc_tables")
+    if cached is None:
+        m4, diagnostics = plan.preconditioner_table()
+        t = plan.tilde
+        rep_of = np.full(plan.num_amplitudes, -1, np.int64)
+        rep_of[t.rep_pos] = np.arange(t.rep_pos.size)
+        elem_rep = rep_of[plan.program.stages["jvp"].elements]
+        if np.any(elem_rep < 0):
+            raise rt.C3LError("JVP output elements must be tilde representatives")
+        cached = (m4, diagnostics, np.ascontiguousarray(m4[elem_rep]))
+        plan.__dict__["_pc_tables"] = cached
+    return cached
+
+
 class DeviceStatic:
     """Residual, linearization and exact JVP in real tilde coordinates."""
 
@@ -35,68 +53,63 @@ class DeviceStatic:
         self.A = plan.num_amplitudes
         self.ws_lin = _cz(prog.ws_size, self.device)
         self.ws_res = _cz(prog.ws_size, self.device)
-        vec = up.raw(prog.vectors)
-        self.vec = vec
-        t = plan.tilde
-        ia, ib = up.raw(t.idx_a), up.raw(t.idx_b)
-        ca, cb = up.raw(t.coef_a), up.raw(t.coef_b)
-        self.canon_T = _cz(self.A, self.device)
-        self.canon_R = _cz(self.A, self.device)
-        self.canon_V = _cz(self.A, self.device)
+        with up.batch():  # every table of the static actions in one copy per arena chunk (no launch inside)
+            vec = up.raw(prog.vectors)
+            self.vec = vec
+            t = plan.tilde
+            ia, ib = up.raw(t.idx_a), up.raw(t.idx_b)
+            ca, cb = up.raw(t.coef_a), up.raw(t.coef_b)
+            self.canon_T = _cz(self.A, self.device)
+            self.canon_R = _cz(self.A, self.device)
+            self.canon_V = _cz(self.A, self.device)
 
-        def static_action(ws, levels_cls, padded, out, scatter, canon, ep, vectors=vec):
-            sa = rt.StaticAction()
-            sa.action = rt.build_action(up, prog, vectors.data_ptr(), ws, levels_cls, padded, out, scatter)
-            sa.num_amplitudes = self.A
-            sa.tilde_ia, sa.tilde_ib = ia.data_ptr(), ib.data_ptr()
-            sa.tilde_ca, sa.tilde_cb = ca.data_ptr(), cb.data_ptr()
-            sa.canon = canon.data_ptr()
-            sa.lam = up.ptr(ep["lam"])
-            sa.col = up.ptr(ep["col"])
-            sa.pair = up.ptr(ep["pair"])
-            sa.scale = up.ptr(ep["scale"])
-            return sa
+            def static_action(ws, levels_cls, padded, out, scatter, canon, ep, vectors=vec):
+                sa = rt.StaticAction()
+                sa.action = rt.build_action(up, prog, vectors.data_ptr(), ws, levels_cls, padded, out, scatter)
+                sa.num_amplitudes = self.A
+                sa.tilde_ia, sa.tilde_ib = ia.data_ptr(), ib.data_ptr()
+                sa.tilde_ca, sa.tilde_cb = ca.data_ptr(), cb.data_ptr()
+                sa.canon = canon.data_ptr()
+                sa.lam = up.ptr(ep["lam"])
+                sa.col = up.ptr(ep["col"])
+                sa.pair = up.ptr(ep["pair"])
+                sa.scale = up.ptr(ep["scale"])
+                return sa
 
-        self.res_action = static_action(self.ws_res, "T", ["res_rest_T", "res_scalar"], "res", plan.scatter_T,
-                                        self.canon_R, plan.epilogue)
-        self.lin_action = static_action(self.ws_lin, "T", ["res_rest_T", "res_scalar", "jvp_rest_T"], "res",
-                                        plan.scatter_T, self.canon_T, plan.epilogue)
-        self.jvp_action = static_action(self.ws_lin, "V", ["jvp_rest_V", "jvp_scalar"], "jvp", plan.scatter_V,
-                                        self.canon_V, plan.epilogue_jvp)
-        # single-precision twin of the JVP (inner operator of the mixed-precision solve)
-        self.vec32 = up.raw(prog.vectors.astype(np.complex64))
-        self.ws32_lin = torch.zeros(max(prog.ws_size, 1), dtype=torch.complex64, device=self.device)
-        self.jvp32_action = static_action(self.ws32_lin, "V", ["jvp_rest_V", "jvp_scalar"], "jvp", plan.scatter_V,
-                                          self.canon_V, plan.epilogue_jvp, vectors=self.vec32)
-        # complex outputs at every coordinate (arbitrary complex amplitudes)
-        self.cres_action = rt.build_action(up, prog, vec.data_ptr(), self.ws_res, "T", ["res_rest_T", "res_scalar"],
-                                           None, plan.scatter_T)
-        self.cres_stage = rt.wedge_stage(up, prog.stages["res_all"])
-        self.cres_lam = up.raw(plan.lam_all)
-        self.clin_action = rt.build_action(up, prog, vec.data_ptr(), self.ws_lin, "T", ["jvp_rest_T"], None,
-                                           plan.scatter_T)
-        self.cjvp_action = rt.build_action(up, prog, vec.data_ptr(), self.ws_lin, "V", ["jvp_rest_V", "jvp_scalar"],
-                                           None, plan.scatter_V)
-        self.cjvp_stage = rt.wedge_stage(up, prog.stages["jvp_all"])
-        self.cjvp_lam = up.raw(plan.lam_all_jvp)
-        self.launches = {
-            "residual": rt.static_launches(self.res_action.action),
-            "linearize": rt.static_launches(self.lin_action.action),
-            "jvp": rt.static_launches(self.jvp_action.action),
-        }
-        m4, self.preconditioner_diagnostics = plan.preconditioner_table()
-        self.pc_m4 = up.raw(m4)
-        self.pc_col = up.raw(t.rep_col)
-        self.pc_pair = up.raw(t.rep_pair)
-        # the same blocks in the JVP output stage's element order (fused M J)
-        rep_of = np.full(plan.num_amplitudes, -1, np.int64)
-        rep_of[t.rep_pos] = np.arange(t.rep_pos.size)
-        elem_rep = rep_of[prog.stages["jvp"].elements]
-        if np.any(elem_rep < 0):
-            raise rt.C3LError("JVP output elements must be tilde representatives")
-        self.pc_m4_elem = up.raw(np.ascontiguousarray(m4[elem_rep]))
-        self.nrep = int(t.rep_pos.size)
-        self.ia, self.ib, self.ca, self.cb = ia, ib, ca, cb
+            self.res_action = static_action(self.ws_res, "T", ["res_rest_T", "res_scalar"], "res", plan.scatter_T,
+                                            self.canon_R, plan.epilogue)
+            self.lin_action = static_action(self.ws_lin, "T", ["res_rest_T", "res_scalar", "jvp_rest_T"], "res",
+                                            plan.scatter_T, self.canon_T, plan.epilogue)
+            self.jvp_action = static_action(self.ws_lin, "V", ["jvp_rest_V", "jvp_scalar"], "jvp", plan.scatter_V,
+                                            self.canon_V, plan.epilogue_jvp)
+            # single-precision twin of the JVP (inner operator of the mixed-precision solve)
+            self.vec32 = up.raw(prog.vectors.astype(np.complex64))
+            self.ws32_lin = torch.zeros(max(prog.ws_size, 1), dtype=torch.complex64, device=self.device)
+            self.jvp32_action = static_action(self.ws32_lin, "V", ["jvp_rest_V", "jvp_scalar"], "jvp", plan.scatter_V,
+                                              self.canon_V, plan.epilogue_jvp, vectors=self.vec32)
+            # complex outputs at every coordinate (arbitrary complex amplitudes)
+            self.cres_action = rt.build_action(up, prog, vec.data_ptr(), self.ws_res, "T", ["res_rest_T", "res_scalar"],
+                                               None, plan.scatter_T)
+            self.cres_stage = rt.wedge_stage(up, prog.stages["res_all"])
+            self.cres_lam = up.raw(plan.lam_all)
+            self.clin_action = rt.build_action(up, prog, vec.data_ptr(), self.ws_lin, "T", ["jvp_rest_T"], None,
+                                               plan.scatter_T)
+            self.cjvp_action = rt.build_action(up, prog, vec.data_ptr(), self.ws_lin, "V", ["jvp_rest_V", "jvp_scalar"],
+                                               None, plan.scatter_V)
+            self.cjvp_stage = rt.wedge_stage(up, prog.stages["jvp_all"])
+            self.cjvp_lam = up.raw(plan.lam_all_jvp)
+            self.launches = {
+                "residual": rt.static_launches(self.res_action.action),
+                "linearize": rt.static_launches(self.lin_action.action),
+                "jvp": rt.static_launches(self.jvp_action.action),
+            }
+            m4, self.preconditioner_diagnostics, m4_elem = _preconditioner_tables(plan)
+            self.pc_m4 = up.raw(m4)
+            self.pc_col = up.raw(t.rep_col)
+            self.pc_pair = up.raw(t.rep_pair)
+            self.pc_m4_elem = up.raw(m4_elem)
+            self.nrep = int(t.rep_pos.size)
+            self.ia, self.ib, self.ca, self.cb = ia, ib, ca, cb
 
     def _stream(self) -> int:
         return rt.stream_ptr(self.device)
@@ -191,8 +204,9 @@ class DeviceEOM:
             up = tables[self.device] = rt.Uploader(self.device)
         self._up = up
         self.N = plan.dimension
-        self.vec = up.table(prog.vectors)
-        self.lam = up.table(plan.lam_sigma)
+        with up.batch():
+            self.vec = up.table(prog.vectors)
+            self.lam = up.table(plan.lam_sigma)
         self.amplitudes = amplitudes.to(self.device, torch.complex128).contiguous()
         self.workspaces: list = []
         self.sigma_actions: list = []
@@ -220,16 +234,21 @@ class DeviceEOM:
         """One workspace (amplitude part prepared) per concurrently used channel."""
         prog = self.plan.program
         up = self._up
-        while len(self.workspaces) < count:
-            ws = _cz(prog.ws_size, self.device)
-            ctx = rt.build_action(up, prog, self.vec.data_ptr(), ws, "T", ["sigma_rest_T"], None, self.plan.scatter_T)
+        built = []
+        with up.batch():  # tables sent when the block ends, before the context launches below
+            while len(self.workspaces) + len(built) < count:
+                ws = _cz(prog.ws_size, self.device)
+                ctx = rt.build_action(up, prog, self.vec.data_ptr(), ws, "T", ["sigma_rest_T"], None,
+                                      self.plan.scatter_T)
+                ea = rt.EomAction()
+                ea.action = rt.build_action(up, prog, self.vec.data_ptr(), ws, "X", ["sigma_rest_X"], "sigma",
+                                            self.plan.scatter_X)
+                ea.lam = self.lam.data_ptr()
+                built.append((ws, ctx, ea))
+        for ws, ctx, ea in built:
             rt.check(self.lib.c3l_action_prepare(C.byref(ctx), self.amplitudes.data_ptr(), rt.stream_ptr(self.device)),
                      "EOM context")
             rt.LaunchCounter.add(rt.action_launches(ctx))
-            ea = rt.EomAction()
-            ea.action = rt.build_action(up, prog, self.vec.data_ptr(), ws, "X", ["sigma_rest_X"], "sigma",
-                                        self.plan.scatter_X)
-            ea.lam = self.lam.data_ptr()
             self.workspaces.append(ws)
             self.sigma_actions.append(ea)
 
@@ -246,15 +265,17 @@ class DeviceEOM:
         prog = sp.program
         up = self._up
         ws = _cz(prog.ws_size, self.device)
-        vec = up.raw(prog.vectors)
-        act = rt.build_action(up, prog, vec.data_ptr(), ws, "T", ["add_rest_T", "rem_rest_T"], None, sp.scatter_T)
+        with up.batch():  # tables sent when the block ends, before the launches below
+            vec = up.raw(prog.vectors)
+            act = rt.build_action(up, prog, vec.data_ptr(), ws, "T", ["add_rest_T", "rem_rest_T"], None,
+                                  sp.scatter_T)
+            stages = [rt.wedge_stage(up, prog.stages.get(nm)) for nm in ("add", "rem")]
         s = rt.stream_ptr(self.device)
         rt.check(self.lib.c3l_action_prepare(C.byref(act), self.amplitudes.data_ptr(), s), "EOM source context")
         rt.LaunchCounter.add(rt.action_launches(act))
         outs = []
-        for nm, scale in (("add", sp.source_scale[0]), ("rem", sp.source_scale[1])):
+        for st, scale in zip(stages, sp.source_scale[:2]):
             out = _cz(self.N, self.device)
-            st = rt.wedge_stage(up, prog.stages.get(nm))
             rt.check(self.lib.c3l_wedge_source_out(C.byref(st), prog.n, ws.data_ptr(), rt.cplx(scale), out.data_ptr(), s),
                      "EOM source")
             rt.LaunchCounter.add(1)

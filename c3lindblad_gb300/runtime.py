@@ -7,6 +7,7 @@ computes on the host: when the library or a GPU is missing the calls raise.
 
 from __future__ import annotations
 
+import contextlib
 import ctypes as C
 from pathlib import Path
 
@@ -217,24 +218,88 @@ def cplx(z: complex) -> Complex:
 
 
 class Uploader:
-    """Keeps device copies of host tables alive and hands out raw pointers."""
+    """Keeps device copies of host tables alive and hands out raw pointers.
+
+    Inside ``with uploader.batch():`` tables are placed in a device arena
+    (their addresses are known at once) and sent in one copy per arena chunk
+    when the block ends; no kernel may read them before the block has ended.
+    Outside a batch every table is copied immediately."""
+
+    _CHUNK = 4 << 20
+    _ALIGN = 256
 
     def __init__(self, device):
         self.device = device
         self.keep: list = []
         self._tables: dict = {}  # id(array) -> (array, device copy): one upload per table
+        self._pending = None     # [(device byte view, host bytes)] inside a batch
+        self._arena = None
+        self._used = 0
+
+    @contextlib.contextmanager
+    def batch(self):
+        if self._pending is not None:  # nested: the outer block sends
+            yield self
+            return
+        self._pending, self._arena, self._used = [], None, 0
+        cached = set(self._tables)
+        try:
+            yield self
+            self._send(self._pending)
+        except BaseException:
+            for key in set(self._tables) - cached:  # never hand out a table that was not sent
+                del self._tables[key]
+            raise
+        finally:
+            self._pending, self._arena, self._used = None, None, 0
+
+    def _send(self, pending) -> None:
+        groups: dict = {}
+        for dst, host in pending:  # by arena chunk (or own allocation)
+            base = dst.untyped_storage().data_ptr()
+            groups.setdefault(base, []).append((dst, host))
+        for items in groups.values():
+            if len(items) == 1:
+                dst, host = items[0]
+                dst.copy_(torch.from_numpy(host.copy()))
+                continue
+            chunk = items[0][0]
+            base = chunk.untyped_storage().data_ptr()
+            end = max(d.data_ptr() - base + d.numel() for d, _ in items)
+            stage = np.empty(end, dtype=np.uint8)
+            for d, h in items:
+                off = d.data_ptr() - base
+                stage[off:off + h.size] = h
+            whole = torch.empty(0, dtype=torch.uint8, device=self.device).set_(chunk.untyped_storage(), 0, (end,))
+            whole.copy_(torch.from_numpy(stage))
 
     def raw(self, arr: np.ndarray) -> torch.Tensor:
         a = np.ascontiguousarray(arr)
         if a.dtype.names is not None or a.dtype == np.int8:
-            host = torch.from_numpy(a.view(np.uint8).reshape(-1).copy())
+            flat = a.view(np.uint8).reshape(-1)
         elif a.dtype == np.complex128:
-            host = torch.from_numpy(a.view(np.float64).reshape(-1).copy())
+            flat = a.view(np.float64).reshape(-1)
         elif a.dtype == np.complex64:
-            host = torch.from_numpy(a.view(np.float32).reshape(-1).copy())
+            flat = a.view(np.float32).reshape(-1)
         else:
-            host = torch.from_numpy(a.reshape(-1).copy())
-        t = host.to(self.device, non_blocking=False)
+            flat = a.reshape(-1)
+        if self._pending is None:
+            t = torch.from_numpy(flat.copy()).to(self.device, non_blocking=False)
+        else:
+            dtype = torch.from_numpy(flat[:0].copy()).dtype
+            nbytes = int(flat.nbytes)
+            need = max(self._ALIGN, (nbytes + self._ALIGN - 1) // self._ALIGN * self._ALIGN)
+            if need > self._CHUNK // 2:
+                dst = torch.empty(need, dtype=torch.uint8, device=self.device)[:nbytes]
+            else:
+                if self._arena is None or self._used + need > self._CHUNK:
+                    self._arena = torch.empty(self._CHUNK, dtype=torch.uint8, device=self.device)
+                    self._used = 0
+                dst = self._arena[self._used:self._used + nbytes]
+                self._used += need
+            t = dst.view(dtype).view(flat.shape)
+            if nbytes:
+                self._pending.append((dst, flat.view(np.uint8).reshape(-1)))
         self.keep.append(t)
         return t
 

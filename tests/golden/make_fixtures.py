@@ -470,10 +470,10 @@ DRIVERS = {
     # i(2k+1)pi/beta and real-axis points omega + i eta), time grid, time validation shifts
     "twosrc": dict(sites=(0, 1), gmres_omega=np.linspace(-2.0, 2.0, 9), gmres_eta=0.1,
                    shifts=np.r_[1j * (2 * np.arange(6) + 1) * np.pi / 8.0, np.linspace(-2.0, 2.0, 5) + 0.1j],
-                   time=np.linspace(0.0, 12.0, 49), validation=np.linspace(-2.0, 2.0, 5) + 0.1j),
+                   time=np.linspace(0.0, 12.0, 49), validation=np.linspace(-2.0, 2.0, 5) + 0.1j, beta=8.0, n_iw=6),
     "siam10": dict(sites=(0,), gmres_omega=np.asarray([-1.0, 0.0, 1.5]), gmres_eta=0.2,
                    shifts=np.r_[1j * (2 * np.arange(6) + 1) * np.pi / 10.0, np.linspace(-8.0, 8.0, 41) + 0.5j],
-                   time=np.linspace(0.0, 20.0, 81), validation=np.linspace(-4.0, 4.0, 9) + 0.2j),
+                   time=np.linspace(0.0, 20.0, 81), validation=np.linspace(-4.0, 4.0, 9) + 0.2j, beta=10.0, n_iw=16),
 }
 
 
@@ -482,7 +482,8 @@ def export_drivers(name: str, path: Path) -> None:
     amplitudes, charge +1: component_retarded_matrix_green (one GMRES solve per
     source, channel and frequency), component_retarded_matrix_green_shifts
     (complex shifts), component_retarded_time (first site) and
-    component_retarded_matrix_time (with the separate channels)."""
+    component_retarded_matrix_time (with the separate channels), and
+    component_matsubara_green on a symmetric explicit Matsubara grid."""
     from c3l.cc.component_response import (
         ComponentSigmaOperator, component_retarded_matrix_green, component_retarded_matrix_green_shifts,
         component_retarded_matrix_time, component_retarded_time,
@@ -532,6 +533,14 @@ def export_drivers(name: str, path: Path) -> None:
                mtime_removal_relative_time_residuals=mt.removal_relative_time_residuals,
                mtime_combined_dimensions=np.asarray([p.dimension for p in mt.combined_projections], np.int64),
                mtime_calls=np.int64(op.action_calls), mtime_seconds=np.float64(time.perf_counter() - t0))
+    from c3l.matsubara.grid import matsubara_grid
+    from c3l.matsubara.solver import component_matsubara_green
+
+    grid = matsubara_grid(spec["beta"], n_iw=spec["n_iw"])
+    op = ComponentSigmaOperator(context)
+    mats = component_matsubara_green(op, sources, grid)
+    out.update(matsubara_beta=np.float64(grid.beta), matsubara_indices=grid.indices, matsubara_green=mats.green,
+               matsubara_max_relative_residual=np.float64(mats.max_relative_residual))
     np.savez_compressed(path, **out)
     print(f"  [{name}] drivers: gmres {out['gmres_seconds']:.1f}s shifts {out['shifts_seconds']:.1f}s "
           f"time {out['time_seconds']:.1f}s matrix time {out['mtime_seconds']:.1f}s", flush=True)

@@ -572,6 +572,13 @@ def test_response_drivers_match_reference(name, problems):
         assert errors[k] < 1e-8, (k, errors[k])
     for k in ("time", "matrix_time", "matrix_time_addition"):
         assert errors[k] < 1e-7, (k, errors[k])
+    # the Matsubara grid form (the complex-shift driver at i|omega_n|)
+    op = c3.ComponentSigmaOperator(ctx)
+    grid = c3.matsubara_grid(float(ref["matsubara_beta"]), indices=ref["matsubara_indices"])
+    mats = c3.component_matsubara_green(op, sources, grid)
+    assert mats.green.shape == ref["matsubara_green"].shape
+    assert relerr(mats.green, ref["matsubara_green"]) < 1e-8
+    assert mats.max_relative_residual <= 1e-10
     # the projection's transfer and orthogonality diagnostics
     pr = sh.addition_projections[0]
     sink = np.concatenate([sources[0].sink, np.zeros(op.dimension - sources[0].sink.size, complex)])

@@ -5,6 +5,7 @@ from __future__ import annotations
 import re
 from pathlib import Path
 
+import numpy as np
 import pytest
 
 ROOT = Path(__file__).resolve().parents[1]
@@ -80,3 +81,52 @@ def test_gmres_graph_release_accepts_null():
 
     lib = runtime.load_library()
     lib.c3l_gmres_release(None)  # no-op
+
+
+def test_uploader_batch_places_every_table_byte_for_byte():
+    """Tables uploaded inside ``Uploader.batch()`` share arena chunks and are sent
+    in one copy per chunk when the block ends: every table must arrive intact
+    (dtype, shape, bytes), whatever its type, size or alignment (run on the CPU
+    device: the same placement and copy logic as on the GPU)."""
+    import torch
+    from c3lindblad_gb300 import runtime as rt
+
+    rng = np.random.default_rng(11)
+    rec = np.zeros(7, dtype=[("a", "<i8"), ("b", "<f8"), ("c", "i1")])
+    rec["a"] = np.arange(7)
+    rec["b"] = rng.normal(size=7)
+    arrays = [
+        rng.integers(-5, 5, size=1000).astype(np.int64),
+        rng.normal(size=333),
+        (rng.normal(size=17) + 1j * rng.normal(size=17)).astype(np.complex128),
+        (rng.normal(size=9) + 1j * rng.normal(size=9)).astype(np.complex64),
+        rng.integers(-3, 3, size=13).astype(np.int8),
+        rec,
+        np.zeros(0, np.int32),
+        rng.integers(0, 2, size=5).astype(bool),
+        rng.normal(size=(3, 5)),                               # 2-D
+        rng.integers(0, 9, size=(rt.Uploader._CHUNK // 8)),    # larger than half a chunk: own allocation
+        rng.normal(size=rt.Uploader._CHUNK // 16),              # fills half a chunk: opens a second chunk
+        np.arange(3, dtype=np.uint16),
+    ]
+    up = rt.Uploader(torch.device("cpu"))
+    with up.batch():
+        outs = [up.raw(a) for a in arrays]
+        cached = up.table(arrays[1])
+    assert up.table(arrays[1]) is cached
+    for a, t in zip(arrays, outs):
+        host = np.ascontiguousarray(a)
+        assert t.numel() * t.element_size() == host.nbytes
+        assert t.cpu().numpy().tobytes() == host.tobytes()
+    # a failed block leaves no cached table behind
+    fresh = np.arange(5.0)
+    try:
+        with up.batch():
+            up.table(fresh)
+            raise RuntimeError("stop")
+    except RuntimeError:
+        pass
+    assert id(fresh) not in up._tables
+    # outside a batch: immediate copies
+    t = up.raw(arrays[0])
+    assert t.numpy().tobytes() == arrays[0].tobytes()

@@ -97,3 +97,30 @@ def test_time_coefficients_match_the_matrix_exponential(grid):
         proj.time_coefficients([np.inf])
     with pytest.raises(ValueError):
         proj.time_coefficients(t, dimension=13)
+
+
+def test_matsubara_grid_maps_upper_values_and_checks_the_lattice():
+    grid = c3.matsubara_grid(5.0, n_iw=3)
+    assert list(grid.indices) == [-3, -2, -1, 0, 1, 2]
+    assert np.allclose(grid.upper_shifts, 1j * np.array([1, 3, 5]) * np.pi / 5.0)
+    rng = np.random.default_rng(2)
+    upper = rng.normal(size=(3, 2, 2)) + 1j * rng.normal(size=(3, 2, 2))
+    full = grid.from_upper(upper)
+    # n = -1 and n = 0 share |2n + 1| = 1: G(-i w) = G(i w)^dagger
+    assert np.array_equal(full[3], upper[0])
+    assert np.array_equal(full[2], upper[0].conj().T)
+    assert np.array_equal(full[0], upper[2].conj().T)
+    scalar = grid.from_upper(upper[:, 0, 0])
+    assert scalar[1] == np.conj(upper[1, 0, 0])
+    same = c3.matsubara_grid(5.0, omega_n=grid.iw)
+    assert np.array_equal(same.indices, grid.indices)
+    with pytest.raises(ValueError, match="fermionic"):
+        c3.matsubara_grid(5.0, omega_n=[2 * np.pi / 5.0])
+    with pytest.raises(ValueError, match="exactly one"):
+        c3.matsubara_grid(5.0, n_iw=2, indices=[0])
+    with pytest.raises(ValueError, match="unique"):
+        c3.matsubara_grid(5.0, indices=[0, 0])
+    with pytest.raises(ValueError, match="shape"):
+        grid.from_upper(np.zeros(4))
+    with pytest.raises(TypeError):
+        c3.component_matsubara_green(_operator(12), _sources(1, 12), object())
