@@ -252,8 +252,11 @@ def run_gpu(args) -> dict:
         torch.cuda.synchronize()
         e2e_times.append(e0.elapsed_time(e1) / 1000.0)
         if k == 0:
+            # the static and EOM program tables, the converged amplitudes sent to the EOM
+            # context, the EOM diagonal, the sink and the shift grid
             h2d = sum(t.numel() * t.element_size() for t in problem.ops._up.keep)
-            h2d += sum(t.numel() * t.element_size() for t in res2._channels[0].basis.V[:0])  # none
+            h2d += sum(t.numel() * t.element_size() for up in eomp._tables.values() for t in up.keep)
+            h2d += sol2.amplitudes.nbytes + 16 * eomp.dimension * 2 + 16 * omega.size
             d2h = sol2.amplitudes.nbytes + sol2.variables.nbytes + res2.retarded.nbytes * 3
     e2e = float(np.mean(e2e_times))
 
