@@ -118,6 +118,17 @@ def _dist():
     return ws, rank, local
 
 
+def _max_over_ranks(value: float, device) -> float:
+    """The largest of the ranks' values (every rank receives it): the job's
+    step time is its slowest replica's."""
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def _flush_l2(torch, buf):
     buf.add_(1.0)
 
@@ -223,10 +234,7 @@ def run_gpu(args) -> dict:
     rt.LaunchCounter.reset()
     unbatched_vs_fp64 = float(np.max(np.abs(res_u.retarded - res64.retarded)) / np.max(np.abs(res64.retarded)))
     if ws > 1:
-        import torch.distributed as dist
-        tt = torch.tensor([t_step], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_step = float(tt.item())
+        t_step = _max_over_ranks(t_step, dev)
 
     # accuracy against the reference FP64 run (subset of the grid it computed)
     amp_err = float(np.max(np.abs(sol.amplitudes - gold["solution_amplitudes"])) /

@@ -304,6 +304,9 @@ def _retarded_green_gmres(op, add, rem, sink, freq, eta, rtol, restart, maxiter,
     """The reference's per-frequency loop (component_response.py:200-233) on the device."""
     ops = op.context.ops
     solver = _shifted_solver(op, restart)
+    vec = DeviceVectors(ops.device)
+    sink_conj = torch.conj(sink).resolve_conj().reshape(1, -1).contiguous()
+    gval = torch.empty(1, dtype=torch.complex128, device=ops.device)
     out = {}
     for name, b in (("addition", add), ("removal", rem)):
         x = torch.zeros_like(b)
@@ -320,7 +323,8 @@ def _retarded_green_gmres(op, add, rem, sink, freq, eta, rtol, restart, maxiter,
             converged = bool(info == 0 and true <= max(10.0 * rtol, 1.0e-12))
             if not converged:
                 raise RuntimeError("a component EOM shifted solve failed to converge")
-            values[i] = complex(torch.dot(sink, x).item())
+            vec.dots_c(sink_conj, 1, x, gval)                   # sink . x (bilinear)
+            values[i] = complex(gval.item())
             records.append(ComponentShiftedSolution(None, i, converged, len(hist), true, tuple(hist),
                                                     time.perf_counter() - t0, solution=None, info=info))
         out[name] = (values, records)
@@ -856,20 +860,7 @@ def component_retarded_matrix_time(operator, sources, time_points, validation_sh
     (``component_response.py:702-815``); all bases run as concurrent device
     channels."""
     started = time.perf_counter()
-    columns = tuple(sources)
-    if not columns:
-        raise ValueError("at least one impurity source is required")
-    if len({item.site for item in columns}) != len(columns):
-        raise ValueError("impurity source sites must be unique")
-    if any(item.charge != columns[0].charge for item in columns):
-        raise ValueError("all impurity sources must use one response charge")
-    retained = np.asarray(columns[0].addition).size
-    for item in columns:
-        if (np.asarray(item.addition).shape != (retained,) or np.asarray(item.removal).shape != (retained,)
-                or np.asarray(item.sink).shape != (retained,)):
-            raise ValueError("impurity sources and sinks must share one retained basis")
-    if operator.dimension < retained:
-        raise ValueError("response operator is smaller than the retained sources")
+    columns, _ = _validated_source_columns(operator, sources)
     t = np.asarray(time_points, dtype=np.float64)
     z = np.asarray(validation_shifts, dtype=np.complex128)
     if (t.ndim != 1 or t.size == 0 or np.any(t < 0.0) or not np.all(np.isfinite(t)) or z.ndim != 1 or z.size == 0
@@ -936,20 +927,7 @@ def component_retarded_matrix_green(operator, sources, omega, eta: float, *, rto
     frequency's solution, every sink contracted with the same solutions.  Axes
     ``(omega, sink_site, source_site)``; a solve that misses the convergence
     rule of ``solve_component_shifted`` raises."""
-    columns = tuple(sources)
-    if not columns:
-        raise ValueError("at least one impurity source is required")
-    if len({item.site for item in columns}) != len(columns):
-        raise ValueError("impurity source sites must be unique")
-    if any(item.charge != columns[0].charge for item in columns):
-        raise ValueError("all impurity sources must use one response charge")
-    retained = np.asarray(columns[0].addition).size
-    for item in columns:
-        if (np.asarray(item.addition).shape != (retained,) or np.asarray(item.removal).shape != (retained,)
-                or np.asarray(item.sink).shape != (retained,)):
-            raise ValueError("impurity sources and sinks must share one retained basis")
-    if operator.dimension < retained:
-        raise ValueError("response operator is smaller than the retained sources")
+    columns, _ = _validated_source_columns(operator, sources)
     frequency = np.asarray(omega, dtype=np.float64)
     broadening = float(eta)
     if (frequency.ndim != 1 or frequency.size == 0 or not np.all(np.isfinite(frequency))
