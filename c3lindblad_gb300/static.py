@@ -288,6 +288,12 @@ def _acceptable_inexact_newton_step(r_norm: float, merit_slope: float, defect_no
 # last step still leaves the Newton residual near 2e-13, far below the
 # 1e-10 convergence test.
 MIXED_GMRES_FLOOR = 1.0e-5
+# Mixed precision, last steps: the inner solve needs to shrink the residual only
+# to the outer tolerance, so a step whose residual is already near it may stop
+# at MIXED_TARGET_SAFETY * tolerance / |r| (capped by the policy's largest
+# relative tolerance).  The FP64 residual still decides convergence; a step
+# that falls short is followed by another Newton step.
+MIXED_TARGET_SAFETY = 0.05
 
 
 def solve_component_ccsd(problem, initial_amplitudes=None, *, policy: NewtonKrylovPolicy | None = None,
@@ -305,9 +311,10 @@ def solve_component_ccsd(problem, initial_amplitudes=None, *, policy: NewtonKryl
 
     ``precision="mixed"`` applies the JVP inside GMRES with FP32 contractions
     and keeps the GMRES basis in FP32 (the GMRES tolerance is floored at
-    ``MIXED_GMRES_FLOOR``) while every residual, the line search and the true
-    linear defect stay FP64 -- iterative refinement, so the converged
-    amplitudes meet the same FP64 residual tolerance.
+    ``MIXED_GMRES_FLOOR`` and may rise to ``MIXED_TARGET_SAFETY`` times the
+    outer tolerance over |r| near convergence) while every residual, the
+    line search and the true linear defect stay FP64 -- iterative refinement,
+    so the converged amplitudes meet the same FP64 residual tolerance.
     """
     if precision not in ("fp64", "mixed"):
         raise ValueError("precision must be 'fp64' or 'mixed'")
@@ -374,7 +381,10 @@ def solve_component_ccsd(problem, initial_amplitudes=None, *, policy: NewtonKryl
         lin_tol = forcing_tolerance(norm, controls, previous_norm=prev_norm, previous_tolerance=prev_tol)
         lin_atol = 0.0 if controls.forcing_strategy == "legacy" else controls.gmres_absolute_tolerance_factor * controls.tolerance
         vec.scale_r(-1.0, r, negr)
-        gm_rtol = max(lin_tol, MIXED_GMRES_FLOOR) if mixed else lin_tol
+        gm_rtol = lin_tol
+        if mixed:
+            sufficient = min(controls.maximum_gmres_relative_tolerance, MIXED_TARGET_SAFETY * controls.tolerance / norm)
+            gm_rtol = max(lin_tol, MIXED_GMRES_FLOOR, sufficient)
         info, gm_history, gm_matvecs = solver.solve(negr, step, rtol=gm_rtol, atol=lin_atol,
                                                     maxiter=controls.gmres_maximum_restart_cycles, single=mixed,
                                                     basis_f32=mixed)
