@@ -276,7 +276,7 @@ def run_gpu(args) -> dict:
         "ms_per_step": t_step * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
         "dtype": "c128", "data": "synthetic",
         "config": {"workload": args.workload, "description": wl["label"],
-                   "precision": "mixed: FP32 inner JVPs and FP32 Krylov basis in GMRES (inner tolerance >= 1e-5), FP64 "
+                   "precision": "mixed: FP32 inner JVPs and FP32 Krylov basis in GMRES (inner tolerance >= 1e-5, and up to 0.05 x tolerance / |r| near convergence), FP64 "
                                 "residuals/refinement; FP64 sigma; Arnoldi CGS2 with FP32 first projections and "
                                 "double-float (FP32-pipe) updates and second projections, FP64 Hessenberg "
                                 "column and shifted solves",
