@@ -24,6 +24,7 @@ import dataclasses
 import resource
 import time
 from dataclasses import dataclass
+from time import perf_counter
 
 import numpy as np
 import torch
@@ -516,13 +517,13 @@ class ArnoldiProjection:
             vec.dots_c(self._V, m, torch.conj(rows[a]).resolve_conj().contiguous(), out[a])
         return np.conj(out.cpu().numpy())
 
-    def time_coefficients(self, time_points, *, dimension=None) -> np.ndarray:
+    def time_coefficients(self, time, *, dimension=None) -> np.ndarray:
         """exp(-i H_m t) |b| e_1 on a time grid (``krylov.py:134-176``): SciPy's
         ``expm_multiply`` on the m x m Hessenberg matrix, one call for a uniform
         grid, one per time otherwise."""
         from scipy.sparse.linalg import expm_multiply
 
-        t = np.asarray(time_points, dtype=np.float64)
+        t = np.asarray(time, dtype=np.float64)
         if t.ndim != 1 or t.size == 0 or not np.all(np.isfinite(t)):
             raise ValueError("time must be a finite nonempty vector")
         m = self._dim(dimension)
@@ -537,14 +538,14 @@ class ArnoldiProjection:
             reduced = np.asarray([expm_multiply(-1j * float(v) * H, rhs) for v in t], dtype=np.complex128)
         return np.asarray(reduced, dtype=np.complex128)
 
-    def time_residual_norms(self, time_points, *, dimension=None) -> np.ndarray:
+    def time_residual_norms(self, time, *, dimension=None) -> np.ndarray:
         """|h_{m+1,m} e_m^T exp(-i H_m t) |b| e_1|: the propagator's own residual."""
         m = self._dim(dimension)
-        reduced = self.time_coefficients(time_points, dimension=m)
+        reduced = self.time_coefficients(time, dimension=m)
         return np.abs(self.hessenberg[m, m - 1] * reduced[:, -1]).astype(np.float64)
 
-    def relative_time_residuals(self, time_points, *, dimension=None) -> np.ndarray:
-        return self.time_residual_norms(time_points, dimension=dimension) / max(float(self.source_norm),
+    def relative_time_residuals(self, time, *, dimension=None) -> np.ndarray:
+        return self.time_residual_norms(time, dimension=dimension) / max(float(self.source_norm),
                                                                                 np.finfo(np.float64).tiny)
 
     def transfer(self, shifts, sink, *, dimension=None) -> np.ndarray:
@@ -794,7 +795,7 @@ def _arnoldi_projections(operator, vectors, shifts: np.ndarray, max_dim: int, to
     return [ArnoldiProjection(b, tolerance, rss) for b in bases]
 
 
-def component_retarded_time(operator, sources, time_points, *, maximum_krylov_dimension: int = 160,
+def component_retarded_time(operator, sources, time, *, maximum_krylov_dimension: int = 160,
                             residual_tolerance: float = 1.0e-11) -> np.ndarray:
     """-i sink . exp(-i K t) (addition + removal) for t >= 0 (``component_response.py:628-663``).
 
@@ -804,7 +805,7 @@ def component_retarded_time(operator, sources, time_points, *, maximum_krylov_di
     """
     from scipy.linalg import expm
 
-    t = np.asarray(time_points, dtype=np.float64)
+    t = np.asarray(time, dtype=np.float64)
     N = operator.dimension
     dev = operator.context.ops.device
     source = _padded_source(sources, 0, N, dev) + _padded_source(sources, 1, N, dev)
@@ -851,7 +852,7 @@ def _matrix_time_from_projections(projections, sinks: torch.Tensor, t: np.ndarra
     return out
 
 
-def component_retarded_matrix_time(operator, sources, time_points, validation_shifts, *,
+def component_retarded_matrix_time(operator, sources, time, validation_shifts, *,
                                    maximum_krylov_dimension: int = 160, residual_tolerance: float = 1.0e-11,
                                    include_channels: bool = True) -> ComponentRetardedMatrixTime:
     """All sink rows from one combined-source basis per source orbital, plus the
@@ -859,9 +860,9 @@ def component_retarded_matrix_time(operator, sources, time_points, validation_sh
     diagnostic).  Same inputs, errors and result fields as the reference
     (``component_response.py:702-815``); all bases run as concurrent device
     channels."""
-    started = time.perf_counter()
+    started = perf_counter()
     columns, _ = _validated_source_columns(operator, sources)
-    t = np.asarray(time_points, dtype=np.float64)
+    t = np.asarray(time, dtype=np.float64)
     z = np.asarray(validation_shifts, dtype=np.complex128)
     if (t.ndim != 1 or t.size == 0 or np.any(t < 0.0) or not np.all(np.isfinite(t)) or z.ndim != 1 or z.size == 0
             or not np.all(np.isfinite(z))):
@@ -898,7 +899,7 @@ def component_retarded_matrix_time(operator, sources, time_points, validation_sh
         retarded=retarded, channel_sum_defect=defect, combined_projections=combined, addition_projections=add_p,
         removal_projections=rem_p, combined_relative_time_residuals=combined_res,
         addition_relative_time_residuals=add_res, removal_relative_time_residuals=rem_res,
-        wall_seconds=float(time.perf_counter() - started),
+        wall_seconds=float(perf_counter() - started),
         peak_rss_kib=int(resource.getrusage(resource.RUSAGE_SELF).ru_maxrss))
 
 
