@@ -563,3 +563,48 @@ def retarded_green_dense(eom: OracleEOM, site: int, omega, eta: float):
 
 def amplitude_count(n: int) -> int:
     return 2 * n * n + 2 * comb(n, 2) ** 2 + n ** 4
+
+
+def matrix_green_dense(eom: OracleEOM, sites, shifts):
+    """G_ab(z) = sink_a . (z - K)^{-1} source_b for the addition and removal
+    channels at complex shifts, by dense solves (the quantity of
+    component_response.py:248-353 and 449-493).  Returns (addition, removal),
+    each [len(shifts), len(sites), len(sites)] with axes (z, sink, source)."""
+    A = dense_matrix(eom)
+    I = np.eye(eom.dimension)
+    cols = [eom.sources(s) for s in sites]
+    sinks = np.vstack([c[2] for c in cols])
+    add = np.vstack([c[0] for c in cols]).T
+    rem = np.vstack([c[1] for c in cols]).T
+    z = np.asarray(shifts, dtype=np.complex128)
+    S = len(cols)
+    rhs = np.hstack([add, rem])
+    ga = np.empty((z.size, S, S), dtype=np.complex128)
+    gr = np.empty_like(ga)
+    for k, zk in enumerate(z):
+        g = sinks @ np.linalg.solve(zk * I - A, rhs)  # one factorization for both channels
+        ga[k], gr[k] = g[:, :S], g[:, S:]
+    return ga, gr
+
+
+def matrix_time_dense(eom: OracleEOM, sites, times):
+    """-i sink_a . exp(-i K t) source_b for the combined (addition + removal),
+    addition and removal sources (the quantity of component_response.py:628-663
+    and 685-815), by dense matrix exponentials.  Each result is
+    [len(times), len(sites), len(sites)]."""
+    from scipy.linalg import expm
+
+    A = dense_matrix(eom)
+    cols = [eom.sources(s) for s in sites]
+    sinks = np.vstack([c[2] for c in cols])
+    add = np.vstack([c[0] for c in cols]).T
+    rem = np.vstack([c[1] for c in cols]).T
+    t = np.asarray(times, dtype=np.float64)
+    out = [np.empty((t.size, len(cols), len(cols)), dtype=np.complex128) for _ in range(3)]
+    for k, tk in enumerate(t):
+        P = expm(-1j * tk * A)
+        pa, pr = P @ add, P @ rem
+        out[1][k] = -1j * (sinks @ pa)
+        out[2][k] = -1j * (sinks @ pr)
+        out[0][k] = out[1][k] + out[2][k]
+    return tuple(out)

@@ -87,3 +87,43 @@ def test_single_mode_known_answer():
     sink = np.array([1.0, 0.0])
     g = np.array([sink @ np.linalg.solve(x * np.eye(2) - A, src) for x in w])
     assert np.allclose(g, 1.0 / (w - 0.3 + 1.1j), atol=1e-12)
+
+
+@pytest.mark.parametrize("name", ["twosrc", "siam10"])
+def test_oracle_response_drivers_match_reference(name):
+    """Dense forms of the reference's other response drivers (GMRES matrix
+    response, complex shifts, Matsubara grid, time propagation) against the
+    reference's own outputs on the converged amplitudes, charge +1 (the
+    fixtures of ``make_fixtures.py drivers``).  siam10 (EOM dimension 1,947)
+    checks the frequency-domain drivers on every fourth shift; its 160-vector
+    time-domain bases did not converge in the reference, so only twosrc
+    checks the propagators."""
+    import c3lindblad_gb300 as c3
+    from conftest import GOLDEN
+
+    spec, g = load(name)
+    d = np.load(GOLDEN / f"{name}.drivers.npz")
+    eom = oc.OracleEOM(oc.OracleProblem(spec.as_dict()), eom_amplitudes(g), 0, 1)
+    sites = [int(s) for s in d["sites"]]
+    ga, gr = oc.matrix_green_dense(eom, sites, d["gmres_omega"] + 1j * float(d["gmres_eta"]))
+    assert relerr(ga, d["gmres_addition"]) < 1e-10
+    assert relerr(ga + gr, d["gmres_retarded"]) < 1e-10
+    every = 1 if eom.dimension <= 100 else 4
+    sa, sr = oc.matrix_green_dense(eom, sites, d["shifts"][::every])
+    assert relerr(sa, d["shifts_addition"][::every]) < 1e-10
+    assert relerr(sr, d["shifts_removal"][::every]) < 1e-10
+    grid = c3.matsubara_grid(float(d["matsubara_beta"]), indices=d["matsubara_indices"])
+    upper = grid.upper_shifts[::every]
+    ma, mr = oc.matrix_green_dense(eom, sites, upper)
+    if every == 1:
+        assert relerr(grid.from_upper(ma + mr), d["matsubara_green"]) < 1e-10
+    else:  # the grid points n >= 0 of the checked shifts
+        pos = [int(np.flatnonzero((grid.indices >= 0) & (2 * grid.indices + 1 == round(z.imag * grid.beta / np.pi)))[0])
+               for z in upper]
+        assert relerr(ma + mr, d["matsubara_green"][pos]) < 1e-10
+    if eom.dimension <= 100:
+        comb, add, rem = oc.matrix_time_dense(eom, sites, d["time"])
+        assert relerr(comb[:, 0, 0], d["time_retarded"]) < 1e-10
+        assert relerr(comb, d["mtime_retarded"]) < 1e-10
+        assert relerr(add, d["mtime_addition"]) < 1e-10
+        assert relerr(rem, d["mtime_removal"]) < 1e-10
