@@ -10,11 +10,13 @@ from .static import (
     ComponentCCSolution,
     ComponentStaticAction,
     ComponentStaticProblem,
+    ContinuationStage,
     NewtonKrylovPolicy,
     NewtonKrylovStep,
     component_static_jvp,
     component_static_residual,
     solve_component_ccsd,
+    solve_component_ccsd_continuation,
 )
 from .matsubara import MatsubaraGreen, MatsubaraGrid, component_matsubara_green, matsubara_grid
 from .response import (
@@ -52,4 +54,5 @@ __all__ = [
     "ComponentRetardedMatrixGreen", "ComponentRetardedMatrixTime", "ComponentShiftedMatrixArnoldiGreen",
     "component_retarded_matrix_green", "component_retarded_matrix_green_shifts", "component_retarded_matrix_time",
     "component_retarded_time", "MatsubaraGreen", "MatsubaraGrid", "component_matsubara_green", "matsubara_grid",
+    "ContinuationStage", "solve_component_ccsd_continuation",
 ]

@@ -75,6 +75,14 @@ BLOCK_DTYPE = np.dtype([
 
 TILE_DTYPE = np.dtype([("block", np.int32), ("count", np.int32), ("start", np.int64)], align=True)
 
+# Pair GEMMs of an output stage: group g computes P_g[i, j] = sum_k A_k[i] R_k[j]
+# over its anchors k (rows aoff[k] .. + M and roff[k] .. + N of the workspace),
+# P_g row-major M x N at offset p_off of the pair buffer that follows the workspace.
+PAIR_GROUP_DTYPE = np.dtype([("p_off", np.int64), ("kbegin", np.int64), ("kend", np.int64),
+                             ("M", np.int32), ("N", np.int32)], align=True)
+PAIR_TILE_DTYPE = np.dtype([("group", np.int32), ("m0", np.int32), ("n0", np.int32), ("pad", np.int32)], align=True)
+PAIR_TILE = 64    # P entries per tile side
+
 
 def _e(g: int) -> tuple:
     return tuple(1 if h == g else 0 for h in range(4))
@@ -279,6 +287,23 @@ class Stage:
     digits: np.ndarray | None = None     # canonical: int32 packed index digits
     element_block: np.ndarray | None = None
     width: int = 64                      # outputs per tile
+    pair_relative: bool = False          # instance offsets count from the pair buffer (fixed in finish)
+
+
+@dataclass
+class PairProgram:
+    """The GEMMs feeding a ``<name>_pairs`` gather stage (offsets into the pair buffer)."""
+
+    groups: np.ndarray        # PAIR_GROUP_DTYPE
+    aoff: np.ndarray          # int64 workspace offsets of anchor rows
+    roff: np.ndarray          # int64 workspace offsets of rest rows
+    tiles: np.ndarray         # PAIR_TILE_DTYPE
+    size: int                 # pair-buffer entries
+
+    @property
+    def macs(self) -> int:
+        g = self.groups
+        return int(np.sum((g["kend"] - g["kbegin"]) * g["M"].astype(np.int64) * g["N"].astype(np.int64)))
 
 
 @dataclass
@@ -297,6 +322,8 @@ class Program:
     stages: dict = field(default_factory=dict)   # name -> Stage
     atom_offsets: dict = field(default_factory=dict)
     rest_offsets: dict = field(default_factory=dict)
+    pairs: dict = field(default_factory=dict)    # stage name -> PairProgram
+    pair_size: int = 0                           # pair-buffer entries (after the workspace)
 
 
 class Builder:
@@ -321,6 +348,8 @@ class Builder:
                 self.vectors[f, 1, g] = ann[f, g * n:(g + 1) * n]
         self.levels: dict = defaultdict(lambda: defaultdict(list))
         self.stage_data: dict = {}
+        self.pairs: dict = {}
+        self.pair_size = 0
 
     def vec_off(self, f: int, kind: int, g: int) -> int:
         return ((f * 2 + kind) * 4 + g) * self.n
@@ -482,8 +511,13 @@ class Builder:
                     tarr[i] = t
                 lv.append(ContractLevel(tasks, tarr))
             levels[cls] = lv
+        for st in self.stage_data.values():
+            if st.pair_relative:
+                nf = st.instances["nfac"]
+                st.instances["fac_off"][nf > 0, 0] += self.ws
+                st.pair_relative = False
         return Program(self.n, self.ws, self.vectors.reshape(-1), self.source_offsets, levels,
-                       self.stage_data, self.atom_offsets, self.rest_offsets)
+                       self.stage_data, self.atom_offsets, self.rest_offsets, self.pairs, self.pair_size)
 
 
 def _tiles_for(ranges):
@@ -543,13 +577,14 @@ def _digits(coords: Coordinates, positions: np.ndarray) -> np.ndarray:
 
 
 def compile_output(builder: Builder, name: str, terms: dict, coords: Coordinates,
-                   positions: np.ndarray, rest_stage: str, scalar_stage: str | None, extra=()):
+                   positions: np.ndarray, rest_stage: str, scalar_stage: str | None, extra=(), pairs: bool = False):
     """Emit rest stage(s) and the canonical output stage(s) for a term set.
 
     ``positions``: vector positions (in ``coords``) to evaluate, any order; the
     stage stores them grouped by block.  ``extra``: further canonical stages
     ``(stage_name, positions, scale)`` sharing the same rest forms, with every
-    instance coefficient multiplied by ``scale``.  Returns the offset of the
+    instance coefficient multiplied by ``scale``.  ``pairs``: also emit the
+    GEMM form of the main stage (``compile_pairs``).  Returns the offset of the
     scalar (degree-zero) output in the workspace or -1.
     """
     sym = builder.sym
@@ -621,7 +656,66 @@ def compile_output(builder: Builder, name: str, terms: dict, coords: Coordinates
         rows_scaled = [(o, d, [(c * scale, f) for c, f in rows]) for o, d, rows in block_rows]
         builder.emit_stage(stage_name, "canonical", rows_scaled, elements=pos, digits=_digits(coords, pos),
                            element_block=blk)
+        if pairs and stage_name == name:
+            compile_pairs(builder, name, rest_info, coords, pos, blk)
     return scalar_off
+
+
+def compile_pairs(builder: Builder, name: str, rest_info: dict, coords: Coordinates, pos: np.ndarray,
+                  blk: np.ndarray) -> None:
+    """GEMM form of a canonical output stage: stage ``<name>_pairs`` and ``builder.pairs[name]``.
+
+    The stage's output at an element of block K is sum over anchors a and
+    anchor blocks ka of shuffle-signed products A_a[ka](...) R_a[K - ka](...)
+    (``compile_output``).  For fixed (K, ka) the shuffles do not depend on the
+    anchor, so the products are first summed over the anchors as one padded
+    GEMM P[i, j] = sum_a A_a[ka][i] R_a[K - ka][j] (i over n^|ka|, j over
+    n^|K - ka| entries), and the element reads one signed entry of P per
+    shuffle: a single-factor instance of degree |K| whose axes are the
+    anchor's axes followed by the rest's.  The elements (and so the epilogue
+    tables) are those of the instance stage, in the same order.
+    """
+    sym = builder.sym
+    n = builder.n
+    groups = []        # (block, ka, kr, [(aoff, roff)])
+    for b, key in enumerate(coords.keys):
+        by_ka: dict = defaultdict(list)
+        for (anchor, D), offs in rest_info.items():
+            if D != sum(key):
+                continue
+            aoffs = builder.atom_offsets[anchor]
+            for ka in sorted(sym.blocks(anchor)):
+                kr = _sub(key, ka)
+                if min(kr) < 0 or kr not in offs:
+                    continue
+                by_ka[ka].append((aoffs[ka], offs[kr]))
+        for ka in sorted(by_ka):
+            groups.append((b, ka, _sub(key, ka), by_ka[ka]))
+    garr = np.zeros(len(groups), PAIR_GROUP_DTYPE)
+    aoff, roff, tiles = [], [], []
+    block_rows = [(-1, sum(k), []) for k in coords.keys]
+    base = builder.pair_size
+    p = base
+    for g, (b, ka, kr, rows) in enumerate(groups):
+        M, N = n ** sum(ka), n ** sum(kr)
+        garr[g] = (p, len(aoff), len(aoff) + len(rows), M, N)
+        aoff.extend(r[0] for r in rows)
+        roff.extend(r[1] for r in rows)
+        for m0 in range(0, M, PAIR_TILE):
+            for n0 in range(0, N, PAIR_TILE):
+                tiles.append((g, m0, n0, 0))
+        key = coords.keys[b]
+        for sign, lists in multi_shuffles(key, [ka, kr]):
+            block_rows[b][2].append((complex(sign), [(p, sum(key), lists[0] + lists[1])]))
+        p += M * N
+    tarr = np.zeros(len(tiles), PAIR_TILE_DTYPE)
+    for i, t in enumerate(tiles):
+        tarr[i] = t
+    builder.pairs[name] = PairProgram(garr, np.asarray(aoff, np.int64), np.asarray(roff, np.int64), tarr, p - base)
+    builder.pair_size = p
+    builder.emit_stage(f"{name}_pairs", "canonical", block_rows, elements=pos, digits=_digits(coords, pos),
+                       element_block=blk)
+    builder.stage_data[f"{name}_pairs"].pair_relative = True
 
 
 # ================================================================ front ends

@@ -18,7 +18,7 @@
 #include "c3l_gb300.h"
 
 // largest GMRES basis (restart + 2 rows of projections) of the device step
-#define C3L_GMRES_MAX_ROWS 256
+#define C3L_GMRES_MAX_ROWS 1024
 
 namespace c3l {
 

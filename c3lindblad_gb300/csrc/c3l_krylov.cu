@@ -1230,10 +1230,9 @@ __global__ void __launch_bounds__(X * Y) k_arn_scale(c3l::ArnoldiBatch bt, int p
 // handles rows r8, r8 + 8, ...; its lanes stride the block's segment.
 constexpr int kGmWarps = kThreads / 32;
 
-// The rows of one warp (r = warp + kGmWarps q, q < kGmRowsPerWarp) are
+// The rows of one warp (r = warp + kGmWarps q) are
 // streamed together: each column step loads w once and one entry per row, so
-// the loads of all rows are in flight at once.  Supports k + 1 <= 256 rows.
-constexpr int kGmRowsPerWarp = C3L_GMRES_MAX_ROWS / kGmWarps;
+// the loads of all rows are in flight at once.  Supports k + 1 <= C3L_GMRES_MAX_ROWS rows.
 
 __device__ __forceinline__ void gm_partials(const double* __restrict__ V, int64_t ld, int k,
                                             const double* __restrict__ w, int64_t lo, int64_t hi,

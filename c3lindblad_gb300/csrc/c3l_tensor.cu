@@ -339,6 +339,104 @@ __global__ void __launch_bounds__(kThreads) k_contract_cluster(LevelPack pack, i
     }
 }
 
+// Pair GEMMs (c3l_pair_program): one thread block computes a 64 x 64 tile of
+// P_g = sum_k A_k^T R_k, whose operand rows A_k = ws[aoff[k] ...] and
+// R_k = ws[roff[k] ...] sit anywhere in the workspace (atoms and rest forms).
+// Chunks of 8 anchors are staged through shared memory (the next chunk's
+// rows are loaded into registers while the current one is multiplied); each
+// thread accumulates a 4 x 4 block of complex entries (rows tm + 16 i,
+// columns tn + 16 j), so every shared-memory read feeds four complex FMAs.
+constexpr int kPairTile = 64;
+constexpr int kPairChunk = 8;
+constexpr int kPairThreads = 256;
+static_assert(kPairThreads == 4 * kPairTile, "the loader covers 4 rows of a chunk per pass");
+
+template <typename C>
+__global__ void __launch_bounds__(kPairThreads) k_pair_gemm(c3l_pair_program pp, Batch<C> bt) {
+    if (!bt.pdl_at_exit) c3l::pdl_launch_dependents();
+    if (batch_stopped(bt)) return;
+    C* __restrict__ ws = bt.ws[blockIdx.y];
+    __shared__ C sa[kPairChunk][kPairTile];
+    __shared__ C sr[kPairChunk][kPairTile];
+    const c3l_pair_tile t = pp.tiles[blockIdx.x];
+    const c3l_pair_group g = pp.groups[t.group];
+    const int tm = threadIdx.x / 16, tn = threadIdx.x % 16;
+    const int lc = threadIdx.x % kPairTile, lr = threadIdx.x / kPairTile;  // loader: rows lr, lr + 4
+    const bool a_ok = t.m0 + lc < g.M, r_ok = t.n0 + lc < g.N;
+    const C zero = Cx<C>::make(0.0, 0.0);
+    // operand row offsets are program tables: the first chunk's before the wait
+    int64_t ao[2] = {-1, -1}, ro[2] = {-1, -1};
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+        const int64_t k = g.kbegin + lr + 4 * u;
+        if (k < g.kend) {
+            ao[u] = pp.aoff[k];
+            ro[u] = pp.roff[k];
+        }
+    }
+    c3l::pdl_wait();
+    C av[2], rv[2];
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+        av[u] = (ao[u] >= 0 && a_ok) ? ws[ao[u] + t.m0 + lc] : zero;
+        rv[u] = (ro[u] >= 0 && r_ok) ? ws[ro[u] + t.n0 + lc] : zero;
+    }
+    C acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = zero;
+    for (int64_t k0 = g.kbegin; k0 < g.kend; k0 += kPairChunk) {
+        __syncthreads();  // the previous chunk has been used
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            sa[lr + 4 * u][lc] = av[u];
+            sr[lr + 4 * u][lc] = rv[u];
+        }
+        __syncthreads();
+        // the next chunk's rows, in flight during this chunk's products
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            const int64_t k = k0 + kPairChunk + lr + 4 * u;
+            const bool ok = k < g.kend;
+            av[u] = (ok && a_ok) ? ws[pp.aoff[k] + t.m0 + lc] : zero;
+            rv[u] = (ok && r_ok) ? ws[pp.roff[k] + t.n0 + lc] : zero;
+        }
+#pragma unroll
+        for (int r = 0; r < kPairChunk; ++r) {
+            C a[4], b[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                a[i] = sa[r][tm + 16 * i];
+                b[i] = sr[r][tn + 16 * i];
+            }
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) acc[i][j] = cfma(a[i], b[j], acc[i][j]);
+        }
+    }
+    C* __restrict__ P = ws + pp.base + g.p_off;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const int m = t.m0 + tm + 16 * i;
+        if (m >= g.M) continue;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int nn = t.n0 + tn + 16 * j;
+            if (nn < g.N) P[(int64_t)m * g.N + nn] = acc[i][j];
+        }
+    }
+}
+
+template <typename C>
+c3l_status run_pairs(const c3l_pair_program& pp, const Batch<C>& bt, cudaStream_t s) {
+    if (pp.ntiles <= 0) return C3L_OK;
+    if (!pp.groups || !pp.aoff || !pp.roff || !pp.tiles || pp.base < 0) return C3L_ERR_ARGUMENT;
+    return c3l::launch_pdl(k_pair_gemm<C>, dim3((unsigned)pp.ntiles, (unsigned)bt.nb), dim3(kPairThreads), 0, s, 0,
+                           bt.pdl, pp, bt);
+}
+
 enum WedgeMode { kPadded = 0, kStatic = 1, kEom = 2, kSource = 3 };
 
 // Output-stage constants; the per-entry input (src) and complex destination
@@ -351,6 +449,7 @@ struct Epilogue {
     double* xout;
     double2 cscale;
     const double* m4;  // static outputs: optional 2x2 preconditioner block per element
+    double iscale;     // static outputs: factor of the product part (the homotopy scale)
 };
 
 __device__ __forceinline__ double2 dmul(double2 a, double2 b) {
@@ -457,7 +556,8 @@ __global__ void __launch_bounds__(kThreads) k_wedge(c3l_wedge_stage st, int n, B
     if (MODE == kPadded) {
         ws[blk.out_off + e] = acc;
     } else if (MODE == kStatic) {
-        const double2 a = to_d2(acc);
+        const double2 a0 = to_d2(acc);
+        const double2 a = make_double2(ep.iscale * a0.x, ep.iscale * a0.y);
         const double2 lam = elam, src = esrc;
         const double2 s = make_double2(fma(lam.x, src.x, fma(-lam.y, src.y, a.x)), fma(lam.x, src.y, fma(lam.y, src.x, a.y)));
         const double2 r = make_double2(s.y, -s.x);  // -i * s
@@ -607,7 +707,8 @@ c3l_status action_prepare(const c3l_action* action, const Batch<C>& bt, cudaStre
 template <typename C>
 c3l_status static_apply(const c3l_static_action* sa, const double* x, double* xout, void* stream) {
     if (!sa || !x || !xout || !valid_action(&sa->action) || !sa->canon || !sa->tilde_ia || !sa->tilde_ib ||
-        !sa->tilde_ca || !sa->tilde_cb || !sa->lam || !sa->col || !sa->pair || !sa->scale || sa->num_amplitudes <= 0)
+        !sa->tilde_ca || !sa->tilde_cb || !sa->lam || !sa->col || !sa->pair || !sa->scale || sa->num_amplitudes <= 0 ||
+        !(sa->interaction_scale >= 0.0 && sa->interaction_scale <= 1.0))
         return C3L_ERR_ARGUMENT;
     cudaStream_t s = as_stream(stream);
     const c3l_action* a = &sa->action;
@@ -623,6 +724,7 @@ c3l_status static_apply(const c3l_static_action* sa, const double* x, double* xo
     if (st) return st;
     if ((st = run_levels<C>(a, bt, s))) return st;
     if ((st = run_padded<C>(a, bt, s))) return st;
+    if ((st = run_pairs<C>(a->pairs, bt, s))) return st;
     if (sa->action.out.ntiles <= 0) return C3L_OK;
     Epilogue ep{};
     ep.lam = reinterpret_cast<const double2*>(sa->lam);
@@ -631,6 +733,7 @@ c3l_status static_apply(const c3l_static_action* sa, const double* x, double* xo
     ep.scale = reinterpret_cast<const double2*>(sa->scale);
     ep.xout = xout;
     ep.m4 = sa->pc_m4;
+    ep.iscale = sa->interaction_scale;
     return launch_wedge<kStatic, C>(sa->action.out, sa->action.n, bt, ep, s);
 }
 
@@ -664,6 +767,7 @@ c3l_status eom_sigma(const c3l_eom_action* ea, int nb, const c3l_complex* const*
     if (st) return st;
     if ((st = run_levels<C>(&ea[0].action, bt, s))) return st;
     if ((st = run_padded<C>(&ea[0].action, bt, s))) return st;
+    if ((st = run_pairs<C>(ea[0].action.pairs, bt, s))) return st;
     if (ea[0].action.out.ntiles <= 0) return C3L_OK;
     Epilogue ep{};
     ep.lam = reinterpret_cast<const double2*>(ea[0].lam);
@@ -743,6 +847,7 @@ c3l_status c3l_wedge_static_out(const c3l_wedge_stage* stage, int32_t n, const c
     ep.pair = pair;
     ep.scale = reinterpret_cast<const double2*>(scale);
     ep.xout = xout;
+    ep.iscale = 1.0;
     return launch_wedge<kStatic, double2>(
         *stage, n,
         single<double2>(const_cast<double2*>(reinterpret_cast<const double2*>(ws)), reinterpret_cast<const double2*>(src)),
@@ -760,6 +865,7 @@ c3l_status c3l_wedge_static_out_f32(const c3l_wedge_stage* stage, int32_t n, con
     ep.pair = pair;
     ep.scale = reinterpret_cast<const double2*>(scale);
     ep.xout = xout;
+    ep.iscale = 1.0;
     return launch_wedge<kStatic, float2>(
         *stage, n,
         single<float2>(const_cast<float2*>(reinterpret_cast<const float2*>(ws)), reinterpret_cast<const double2*>(src)),
@@ -777,6 +883,16 @@ c3l_status c3l_wedge_eom_out(const c3l_wedge_stage* stage, int32_t n, const c3l_
                                                        reinterpret_cast<const double2*>(xin),
                                                        reinterpret_cast<double2*>(out)),
                                        ep, as_stream(stream));
+}
+
+c3l_status c3l_pair_gemm(const c3l_pair_program* program, c3l_complex* ws, void* stream) {
+    if (!program || !ws) return C3L_ERR_ARGUMENT;
+    return run_pairs<double2>(*program, single<double2>(reinterpret_cast<double2*>(ws)), as_stream(stream));
+}
+
+c3l_status c3l_pair_gemm_f32(const c3l_pair_program* program, c3l_complex32* ws, void* stream) {
+    if (!program || !ws) return C3L_ERR_ARGUMENT;
+    return run_pairs<float2>(*program, single<float2>(reinterpret_cast<float2*>(ws)), as_stream(stream));
 }
 
 c3l_status c3l_wedge_source_out(const c3l_wedge_stage* stage, int32_t n, const c3l_complex* ws, c3l_complex scale,

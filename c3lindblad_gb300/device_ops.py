@@ -63,9 +63,9 @@ class DeviceStatic:
             self.canon_R = _cz(self.A, self.device)
             self.canon_V = _cz(self.A, self.device)
 
-            def static_action(ws, levels_cls, padded, out, scatter, canon, ep, vectors=vec):
+            def static_action(ws, levels_cls, padded, out, scatter, canon, ep, vectors=vec, pairs=None):
                 sa = rt.StaticAction()
-                sa.action = rt.build_action(up, prog, vectors.data_ptr(), ws, levels_cls, padded, out, scatter)
+                sa.action = rt.build_action(up, prog, vectors.data_ptr(), ws, levels_cls, padded, out, scatter, pairs)
                 sa.num_amplitudes = self.A
                 sa.tilde_ia, sa.tilde_ib = ia.data_ptr(), ib.data_ptr()
                 sa.tilde_ca, sa.tilde_cb = ca.data_ptr(), cb.data_ptr()
@@ -74,6 +74,7 @@ class DeviceStatic:
                 sa.col = up.ptr(ep["col"])
                 sa.pair = up.ptr(ep["pair"])
                 sa.scale = up.ptr(ep["scale"])
+                sa.interaction_scale = 1.0
                 return sa
 
             self.res_action = static_action(self.ws_res, "T", ["res_rest_T", "res_scalar"], "res", plan.scatter_T,
@@ -82,11 +83,16 @@ class DeviceStatic:
                                             plan.scatter_T, self.canon_T, plan.epilogue)
             self.jvp_action = static_action(self.ws_lin, "V", ["jvp_rest_V", "jvp_scalar"], "jvp", plan.scatter_V,
                                             self.canon_V, plan.epilogue_jvp)
-            # single-precision twin of the JVP (inner operator of the mixed-precision solve)
+            # single-precision twin of the JVP (inner operator of the mixed-precision solve):
+            # its output stage sums the anchor ^ rest products as pair GEMMs into the
+            # pair buffer that follows the FP32 workspace, then gathers them
             self.vec32 = up.raw(prog.vectors.astype(np.complex64))
-            self.ws32_lin = torch.zeros(max(prog.ws_size, 1), dtype=torch.complex64, device=self.device)
-            self.jvp32_action = static_action(self.ws32_lin, "V", ["jvp_rest_V", "jvp_scalar"], "jvp", plan.scatter_V,
-                                              self.canon_V, plan.epilogue_jvp, vectors=self.vec32)
+            self.ws32_lin = torch.zeros(max(prog.ws_size + prog.pair_size, 1), dtype=torch.complex64,
+                                        device=self.device)
+            pairs = "jvp" if "jvp" in prog.pairs else None
+            self.jvp32_action = static_action(self.ws32_lin, "V", ["jvp_rest_V", "jvp_scalar"],
+                                              "jvp_pairs" if pairs else "jvp", plan.scatter_V, self.canon_V,
+                                              plan.epilogue_jvp, vectors=self.vec32, pairs=pairs)
             # complex outputs at every coordinate (arbitrary complex amplitudes)
             self.cres_action = rt.build_action(up, prog, vec.data_ptr(), self.ws_res, "T", ["res_rest_T", "res_scalar"],
                                                None, plan.scatter_T)
@@ -102,6 +108,7 @@ class DeviceStatic:
                 "residual": rt.static_launches(self.res_action.action),
                 "linearize": rt.static_launches(self.lin_action.action),
                 "jvp": rt.static_launches(self.jvp_action.action),
+                "jvp32": rt.static_launches(self.jvp32_action.action),
             }
             m4, self.preconditioner_diagnostics, m4_elem = _preconditioner_tables(plan)
             self.pc_m4 = up.raw(m4)
@@ -113,6 +120,19 @@ class DeviceStatic:
 
     def _stream(self) -> int:
         return rt.stream_ptr(self.device)
+
+    @property
+    def interaction_scale(self) -> float:
+        return float(self.res_action.interaction_scale)
+
+    def set_interaction_scale(self, s: float) -> None:
+        """Scale the product part of the residual and JVP (the homotopy
+        ``L0(K_ref) + s [L - L0(K_ref)]`` at the compiled HF reference)."""
+        s = float(s)
+        if not 0.0 <= s <= 1.0:
+            raise ValueError("interaction scale must lie in [0, 1]")
+        for a in (self.res_action, self.lin_action, self.jvp_action, self.jvp32_action):
+            a.interaction_scale = s
 
     def _apply(self, action, x: torch.Tensor, out: torch.Tensor, what: str, launches: int) -> None:
         if x.dtype != torch.float64 or out.dtype != torch.float64 or x.numel() != self.D or out.numel() != self.D:
@@ -134,7 +154,7 @@ class DeviceStatic:
 
     def to_single(self) -> None:
         """Copy the linearization workspace into its FP32 twin (after ``linearize``)."""
-        rt.check(self.lib.c3l_downcast(self.ws_lin.numel(), self.ws_lin.data_ptr(), self.ws32_lin.data_ptr(),
+        rt.check(self.lib.c3l_downcast(self.plan.program.ws_size, self.ws_lin.data_ptr(), self.ws32_lin.data_ptr(),
                                        self._stream()), "downcast")
         rt.LaunchCounter.add(1)
 
@@ -144,7 +164,7 @@ class DeviceStatic:
             raise ValueError(f"jvp32: expected float64 vectors of length {self.D}")
         rt.check(self.lib.c3l_static_apply_f32(C.byref(self.jvp32_action), v.data_ptr(), out.data_ptr(),
                                                self._stream()), "static JVP (fp32)")
-        rt.LaunchCounter.add(self.launches["jvp"])
+        rt.LaunchCounter.add(self.launches["jvp32"])
 
     def precondition(self, x: torch.Tensor, out: torch.Tensor) -> None:
         rt.check(self.lib.c3l_precondition(self.nrep, self.pc_m4.data_ptr(), self.pc_col.data_ptr(),
@@ -164,7 +184,7 @@ class DeviceStatic:
         ws = self.ws_res if which == "res" else self.ws_lin
         if off < 0:
             return 0j
-        return complex(-1j * ws[off].item())
+        return complex(-1j * self.interaction_scale * ws[off].item())
 
     # ---------------------------------------------- complex-amplitude actions
     def residual_complex(self, t: torch.Tensor, out: torch.Tensor) -> complex:

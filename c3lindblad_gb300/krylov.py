@@ -175,7 +175,7 @@ class DeviceGMRES:
         self.restart = int(min(restart, n))
         r = self.restart
         lib = rt.lib()
-        self.V = torch.empty((r + 1, n), dtype=torch.float64, device=dev)
+        self._basis: dict = {}  # basis_f32 -> the basis buffer (allocated on first use)
         self.tmp = torch.empty(n, dtype=torch.float64, device=dev)
         self.r = torch.empty(n, dtype=torch.float64, device=dev)
         self.coeff = torch.zeros(2 * (r + 2) + 4, dtype=torch.float64, device=dev)
@@ -190,9 +190,31 @@ class DeviceGMRES:
         self._lib = lib
 
     def __del__(self):
-        for handle in getattr(self, "_graphs", {}).values():
+        self.release_graphs()
+
+    def release_graphs(self) -> None:
+        for key, handle in list(getattr(self, "_graphs", {}).items()):
             if handle:
                 self._lib.c3l_gmres_release(handle)
+            self._graphs[key] = None
+
+    def basis(self, basis_f32: bool) -> torch.Tensor:
+        """The Krylov basis: restart + 1 rows of FP64, or (FP32 basis) restart + 1
+        FP32 rows plus the FP32 work vector.  Only the precision in use is held."""
+        got = self._basis.get(basis_f32)
+        if got is None:
+            r, n = self.restart, self.ops.D
+            for key in list(self._basis):  # the other precision's basis and the graphs that point at it
+                self.release_graphs()
+                del self._basis[key]
+            doubles = ((r + 2) * n + 1) // 2 if basis_f32 else (r + 1) * n
+            got = torch.empty(doubles, dtype=torch.float64, device=self.ops.device)
+            self._basis[basis_f32] = got
+        return got
+
+    @property
+    def nbytes(self) -> int:
+        return sum(t.numel() * t.element_size() for t in self._basis.values())
 
     def solve(self, b: torch.Tensor, x: torch.Tensor, *, rtol: float, atol: float, maxiter: int,
               single: bool = False, basis_f32: bool = False):
@@ -209,7 +231,7 @@ class DeviceGMRES:
         a.b, a.x = b.data_ptr(), x.data_ptr()
         a.rtol, a.atol = float(rtol), float(atol)
         a.restart, a.maxiter = self.restart, int(maxiter)
-        a.V, a.tmp, a.r = self.V.data_ptr(), self.tmp.data_ptr(), self.r.data_ptr()
+        a.V, a.tmp, a.r = self.basis(bool(a.basis_f32)).data_ptr(), self.tmp.data_ptr(), self.r.data_ptr()
         a.coeff, a.partial, a.host = self.coeff.data_ptr(), self.partial.data_ptr(), self.host.data_ptr()
         a.history = self.history.ctypes.data
         a.history_capacity = self.history.size

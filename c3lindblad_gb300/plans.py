@@ -60,8 +60,9 @@ class StaticPlan:
         # complex outputs -i(...) at every coordinate (arbitrary amplitudes)
         self.res_scalar_off = compile_output(b, "res", self.res_terms, coords, rep, "res_rest", "res_scalar",
                                              extra=(("res_all", allpos, -1j),))
+        # the inner JVP of the mixed solve reads its outputs through pair GEMMs
         self.jvp_scalar_off = compile_output(b, "jvp", self.jvp_terms, coords, rep, "jvp_rest", "jvp_scalar",
-                                             extra=(("jvp_all", allpos, -1j),))
+                                             extra=(("jvp_all", allpos, -1j),), pairs=True)
         self.program = b.finish()
         self.scatter_T = _scatter_table(coords, self.program.source_offsets["T"])
         self.scatter_V = _scatter_table(coords, self.program.source_offsets["V"])

@@ -28,6 +28,11 @@ class ContractLevel(C.Structure):
     _fields_ = [("tasks", C.c_void_p), ("tiles", C.c_void_p), ("ntiles", C.c_int64)]
 
 
+class PairProgram(C.Structure):
+    _fields_ = [("groups", C.c_void_p), ("aoff", C.c_void_p), ("roff", C.c_void_p), ("tiles", C.c_void_p),
+                ("ntiles", C.c_int64), ("base", C.c_int64)]
+
+
 class WedgeStage(C.Structure):
     _fields_ = [("blocks", C.c_void_p), ("instances", C.c_void_p), ("tiles", C.c_void_p),
                 ("ntiles", C.c_int64), ("elements", C.c_void_p), ("digits", C.c_void_p), ("width", C.c_int32),
@@ -38,14 +43,15 @@ class Action(C.Structure):
     _fields_ = [("n", C.c_int32), ("nlevels", C.c_int32), ("npadded", C.c_int32), ("pad", C.c_int32),
                 ("vectors", C.c_void_p), ("ws", C.c_void_p), ("scatter_count", C.c_int64),
                 ("scatter_dst", C.c_void_p), ("scatter_pos", C.c_void_p), ("scatter_sign", C.c_void_p),
-                ("levels", ContractLevel * 8), ("padded", WedgeStage * 4), ("out", WedgeStage)]
+                ("levels", ContractLevel * 8), ("padded", WedgeStage * 4), ("pairs", PairProgram),
+                ("out", WedgeStage)]
 
 
 class StaticAction(C.Structure):
     _fields_ = [("action", Action), ("num_amplitudes", C.c_int64), ("tilde_ia", C.c_void_p),
                 ("tilde_ib", C.c_void_p), ("tilde_ca", C.c_void_p), ("tilde_cb", C.c_void_p),
                 ("canon", C.c_void_p), ("lam", C.c_void_p), ("col", C.c_void_p), ("pair", C.c_void_p),
-                ("scale", C.c_void_p), ("pc_m4", C.c_void_p)]
+                ("scale", C.c_void_p), ("pc_m4", C.c_void_p), ("interaction_scale", C.c_double)]
 
 
 class EomAction(C.Structure):
@@ -111,7 +117,7 @@ EXPORTS = (
     "c3l_scale_c", "c3l_scale_r", "c3l_precondition", "c3l_hessenberg_shifted", "c3l_hessenberg_coordinates",
     "c3l_hessenberg_coordinates_noalloc", "c3l_gmres", "c3l_gmres_scratch", "c3l_gmres_release", "c3l_gmres_shifted", "c3l_shifted_combine", "c3l_arnoldi", "c3l_hessenberg_advance",
     "c3l_arnoldi_column", "c3l_static_apply_f32", "c3l_eom_sigma_f32", "c3l_action_prepare_f32", "c3l_downcast",
-    "c3l_wedge_static_out_f32", "c3l_mlp_forward", "c3l_mlp_backward", "c3l_mlp_adam", "c3l_warm_features", "c3l_warm_apply", "c3l_version",
+    "c3l_wedge_static_out_f32", "c3l_pair_gemm", "c3l_pair_gemm_f32", "c3l_mlp_forward", "c3l_mlp_backward", "c3l_mlp_adam", "c3l_warm_features", "c3l_warm_apply", "c3l_version",
 )
 
 
@@ -147,6 +153,8 @@ def _declare(lib) -> None:
         "c3l_eom_sigma_f32": [P, P, P, P],
         "c3l_action_prepare_f32": [P, P, P],
         "c3l_downcast": [I64, P, P, P],
+        "c3l_pair_gemm": [P, P, P],
+        "c3l_pair_gemm_f32": [P, P, P],
         "c3l_mlp_forward": [I64, P, P, P, P],
         "c3l_mlp_backward": [I64, P, P, P, C.c_float, P, P, P, P],
         "c3l_mlp_adam": [P, P, P, P, C.c_float, C.c_float, C.c_float, C.c_float, I32, P, P],
@@ -337,8 +345,28 @@ def wedge_stage(up: Uploader, stage) -> WedgeStage:
     return st
 
 
+def pair_program(up: Uploader, program, name: str | None) -> PairProgram:
+    """The pair GEMMs feeding stage ``<name>_pairs`` (none when ``name`` is None)."""
+    pp = PairProgram()
+    pairs = program.pairs.get(name) if name else None
+    if pairs is None or pairs.tiles.size == 0:
+        pp.ntiles = 0
+        return pp
+    pp.groups = up.ptr(pairs.groups)
+    pp.aoff = up.ptr(pairs.aoff)
+    pp.roff = up.ptr(pairs.roff)
+    pp.tiles = up.ptr(pairs.tiles)
+    pp.ntiles = pairs.tiles.size
+    pp.base = program.ws_size
+    return pp
+
+
 def build_action(up: Uploader, program, vectors_ptr: int, ws: torch.Tensor, levels_cls: str | None,
-                 padded_names: list, out_name: str | None, scatter) -> Action:
+                 padded_names: list, out_name: str | None, scatter, pairs: str | None = None) -> Action:
+    """``pairs``: run the pair GEMMs of that stage before the output stage
+    (``ws`` then holds the workspace followed by the pair buffer)."""
+    if pairs is not None and ws.numel() < program.ws_size + program.pair_size:
+        raise C3LError("the workspace has no room for the pair buffer")
     a = Action()
     a.n = program.n
     levels = program.levels.get(levels_cls, []) if levels_cls else []
@@ -364,6 +392,7 @@ def build_action(up: Uploader, program, vectors_ptr: int, ws: torch.Tensor, leve
     for i, s in enumerate(stages):
         a.padded[i] = wedge_stage(up, s)
     a.out = wedge_stage(up, program.stages.get(out_name) if out_name else None)
+    a.pairs = pair_program(up, program, pairs)
     a.vectors = vectors_ptr
     a.ws = ws.data_ptr()
     if scatter is not None:
@@ -410,5 +439,6 @@ def action_launches(a: Action) -> int:
         tail = a.nlevels
     k += sum(1 for i in range(tail) if a.levels[i].ntiles > 0) + (1 if tail < a.nlevels else 0)
     k += sum(1 for i in range(a.npadded) if a.padded[i].ntiles > 0)
+    k += 1 if a.pairs.ntiles > 0 else 0
     k += 1 if a.out.ntiles > 0 else 0
     return k

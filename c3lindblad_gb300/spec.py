@@ -110,16 +110,28 @@ class ProblemSpec:
 
     # ------------------------------------------------------- reference adapter
     @classmethod
-    def from_reference(cls, static_problem) -> "ProblemSpec":
+    def from_reference(cls, static_problem, recipe: str = "reference") -> "ProblemSpec":
         """Lower a reference ``ComponentStaticProblem`` (needs the reference package).
 
-        Reads ``static_problem.oracle`` (a ``FactorizedCCProblem``): its
-        products, rapidities and normal-mode reference.
+        Reads ``static_problem.oracle`` (a ``FactorizedCCProblem``,
+        ``src/c3l/cc/component_tensor.py:1276-1298``).
+        """
+        return cls.from_factorized(static_problem.oracle, recipe)
+
+    @classmethod
+    def from_factorized(cls, cc, recipe: str = "reference") -> "ProblemSpec":
+        """Lower the parts of a reference ``FactorizedCCProblem`` the hot path reads.
+
+        ``cc`` needs ``model``, ``reference``, ``products`` and ``rapidities``
+        (``src/c3l/cc/factorized.py:70-110``); the cluster masks and the
+        amplitude tilde map are not read, since this package derives both
+        from ``n`` and the mode-level tilde map.  Factors are numbered in
+        first-use order over the products (written order), then the physical
+        operators of every site and spin (``src/c3l/ci/matrix_free.py:95-139``).
         """
         from c3l.ci.matrix_free import physical_mode_operator
         from c3l.ci.tilde import tilde_map_from_references
 
-        cc = static_problem.oracle
         if cc.model.symmetry != "spin":
             raise ValueError("only the spinful (up/down conserving) layout is supported")
         n = cc.model.n_sites
@@ -160,5 +172,5 @@ class ProblemSpec:
             product_coefficients=pc, product_factors=pf, product_lengths=pl,
             rapidities=np.asarray(cc.rapidities, complex),
             mode_partner=np.asarray(det.partners, np.int64), mode_phase=np.asarray(det.factors, complex),
-            source_factor=src, impurity_site=int(cc.model.impurity_site), recipe="reference",
+            source_factor=src, impurity_site=int(cc.model.impurity_site), recipe=recipe,
         )

@@ -180,7 +180,7 @@ class ComponentStaticProblem:
             cc = problem.oracle if hasattr(problem, "coordinates") else problem
             if getattr(cc, "level", "CCSD") != "CCSD":
                 raise ValueError("the component backend currently implements CCSD only")
-            return cls(ProblemSpec.from_reference(cc), device=device, oracle=cc)
+            return cls(ProblemSpec.from_factorized(cc), device=device, oracle=cc)
         raise TypeError("unsupported problem type")
 
     @property
@@ -294,12 +294,15 @@ MIXED_GMRES_FLOOR = 1.0e-5
 # relative tolerance).  The FP64 residual still decides convergence; a step
 # that falls short is followed by another Newton step.
 MIXED_TARGET_SAFETY = 0.05
+# GMRES bases larger than this are released when a solve returns (a 960-vector
+# basis of a 65-site problem holds 102 GB); smaller ones stay for the next solve.
+KEEP_GMRES_BYTES = 8 << 30
 
 
 def solve_component_ccsd(problem, initial_amplitudes=None, *, policy: NewtonKrylovPolicy | None = None,
                          rank6_tile_size: int = 4096, compute_rank6: bool = False,
                          accepted_step_callback: Callable | None = None, warm_start=None,
-                         precision: str = "fp64") -> ComponentCCSolution:
+                         precision: str = "fp64", interaction_scale: float = 1.0) -> ComponentCCSolution:
     """Solve the tilde-real CCSD equations with device residuals and JVPs.
 
     Control flow, forcing terms, Armijo backtracking and the final
@@ -315,6 +318,11 @@ def solve_component_ccsd(problem, initial_amplitudes=None, *, policy: NewtonKryl
     outer tolerance over |r| near convergence) while every residual, the
     line search and the true linear defect stay FP64 -- iterative refinement,
     so the converged amplitudes meet the same FP64 residual tolerance.
+
+    ``interaction_scale`` s solves the reference's homotopy model
+    ``L0(K_ref) + s [L - L0(K_ref)]`` at the problem's own HF reference
+    (``src/c3l/models.py:516-549``): the same products with every coefficient
+    times s, so the compiled program is reused with its product part scaled.
     """
     if precision not in ("fp64", "mixed"):
         raise ValueError("precision must be 'fp64' or 'mixed'")
@@ -324,6 +332,19 @@ def solve_component_ccsd(problem, initial_amplitudes=None, *, policy: NewtonKryl
     controls = NewtonKrylovPolicy() if policy is None else policy
     p = _as_problem(problem)
     ops = p.ops
+    ops.set_interaction_scale(interaction_scale)
+    try:
+        return _solve(p, ops, controls, initial_amplitudes, accepted_step_callback, warm_start, precision)
+    finally:
+        ops.set_interaction_scale(1.0)
+        for key, solver in list(p.__dict__.get("_gmres", {}).items()):
+            if solver.nbytes > KEEP_GMRES_BYTES:
+                solver.release_graphs()
+                del p.__dict__["_gmres"][key]
+
+
+def _solve(p, ops, controls, initial_amplitudes, accepted_step_callback, warm_start, precision):
+    mixed = precision == "mixed"
     dev = ops.device
     vec = DeviceVectors(dev)
     started = time.perf_counter()
@@ -449,3 +470,49 @@ def solve_component_ccsd(problem, initial_amplitudes=None, *, policy: NewtonKryl
         peak_rss_kib=int(resource.getrusage(resource.RUSAGE_SELF).ru_maxrss),
         gpu_launches=rt.LaunchCounter.count - launches0, warm_start=warm_label,
     )
+
+
+# Interaction scales of the reference's continuation driver
+# (examples/junction/gpu_timing.py:30-31).
+CONTINUATION_SCALES = (0.5, 0.75, 1.0)
+
+
+@dataclass(frozen=True, slots=True)
+class ContinuationStage:
+    scale: float
+    seconds: float
+    residual: float
+    iterations: int
+    jvp_evaluations: int
+    residual_evaluations: int
+
+
+def solve_component_ccsd_continuation(problem, scales=CONTINUATION_SCALES, initial_amplitudes=None, *,
+                                      policy: NewtonKrylovPolicy | None = None, precision: str = "fp64",
+                                      tolerance: float = 1.0e-10):
+    """Static CCSD by continuation in the interaction scale.
+
+    The reference's production driver for strongly interacting impurities
+    solves the homotopy models ``L0(K_ref) + s [L - L0(K_ref)]`` at one HF
+    reference for s = 0.5, 0.75, 1, each started from the previous root, and
+    stops with ``RuntimeError`` when a stage does not converge
+    (``examples/junction/gpu_timing.py:46-64``, problems from
+    ``examples/shared/saved_reference.py:43-59``).  Returns the last stage's
+    ``ComponentCCSolution`` and one ``ContinuationStage`` record per stage.
+    """
+    values = tuple(float(s) for s in scales)
+    if not values or values[-1] != 1.0 or any(not 0.0 < s <= 1.0 for s in values):
+        raise ValueError("continuation scales must lie in (0, 1] and end at 1")
+    initial = initial_amplitudes
+    records = []
+    solution = None
+    for s in values:
+        started = time.perf_counter()
+        solution = solve_component_ccsd(problem, initial, policy=policy, precision=precision, interaction_scale=s)
+        residual = solution.packed_residual_norm
+        if not solution.converged or not np.isfinite(residual) or residual > tolerance:
+            raise RuntimeError(f"Static solve failed at interaction scale {s}: {residual}")
+        initial = solution.amplitudes
+        records.append(ContinuationStage(s, time.perf_counter() - started, float(residual), solution.iterations,
+                                         solution.jvp_evaluations, solution.residual_evaluations))
+    return solution, tuple(records)

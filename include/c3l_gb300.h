@@ -96,6 +96,37 @@ typedef struct {
     int32_t pad;
 } c3l_wedge_stage;
 
+/* Pair GEMMs of an output stage (the anchor ^ rest sums of
+ * src/c3l/cc/component_tensor.py:869-898 regrouped by anchor block): group g
+ * computes P_g[i][j] = sum_{k in [kbegin, kend)} ws[aoff[k] + i] ws[roff[k] + j]
+ * for i < M, j < N into ws[pair_base + p_off + i N + j], pair_base being the
+ * first entry after the workspace proper.  The output stage then reads one
+ * signed entry of P per shuffle. */
+typedef struct {
+    int64_t p_off;
+    int64_t kbegin;
+    int64_t kend;
+    int32_t M;
+    int32_t N;
+} c3l_pair_group;
+
+/* One thread block: the 64 x 64 entries of group `group` starting at (m0, n0). */
+typedef struct {
+    int32_t group;
+    int32_t m0;
+    int32_t n0;
+    int32_t pad;
+} c3l_pair_tile;
+
+typedef struct {
+    const c3l_pair_group* groups;
+    const int64_t* aoff;
+    const int64_t* roff;
+    const c3l_pair_tile* tiles;
+    int64_t ntiles;
+    int64_t base;             /* pair_base: P entries are ws[base + p_off + ...] */
+} c3l_pair_program;
+
 /* ------------------------------------------------------------ primitives */
 
 /* t[mu] = ca[mu] x[ia[mu]] + cb[mu] x[ib[mu]]  (TildeMap.unpack,
@@ -137,6 +168,11 @@ c3l_status c3l_wedge_eom_out(const c3l_wedge_stage* stage, int32_t n, const c3l_
                              const c3l_complex* lam, const c3l_complex* xin, c3l_complex* out,
                              void* stream);
 
+/* The pair GEMMs alone over a complex FP64 / FP32 workspace (the P blocks
+ * are written at ws[program->base + p_off ...]). */
+c3l_status c3l_pair_gemm(const c3l_pair_program* program, c3l_complex* ws, void* stream);
+c3l_status c3l_pair_gemm_f32(const c3l_pair_program* program, c3l_complex32* ws, void* stream);
+
 /* EOM sources: out[mu] = scale * V  (src/c3l/cc/component_tensor.py:2788-2798). */
 c3l_status c3l_wedge_source_out(const c3l_wedge_stage* stage, int32_t n, const c3l_complex* ws,
                                 c3l_complex scale, c3l_complex* out, void* stream);
@@ -161,6 +197,7 @@ typedef struct {
     const double* scatter_sign;
     c3l_contract_level levels[C3L_MAX_LEVELS];
     c3l_wedge_stage padded[C3L_MAX_STAGES];
+    c3l_pair_program pairs;   /* ntiles 0: none; else run before `out`, which reads P */
     c3l_wedge_stage out;
 } c3l_action;
 
@@ -186,6 +223,12 @@ typedef struct {
      * output element, [elements][4] row-major, applied to the outputs in the
      * output stage (the product M J of the Newton-Krylov inner solve) */
     const double* pc_m4;
+    /* factor s multiplying the product part: xout = -i pack(Lambda x + s V(x)).
+     * 1 is the problem as compiled; s < 1 is the reference's homotopy model
+     * L0(K_ref) + s [L - L0(K_ref)] at a fixed HF reference
+     * (src/c3l/models.py:516-549), whose products are the compiled ones with
+     * every coefficient times s (examples/junction/gpu_timing.py:30-31). */
+    double interaction_scale;
 } c3l_static_action;
 
 c3l_status c3l_static_apply(const c3l_static_action* action, const double* x, double* xout, void* stream);
@@ -545,7 +588,9 @@ c3l_status c3l_warm_apply(int64_t nrep, const int64_t* col, const int64_t* pair,
  *
  * The first call on each device looks up the array's device address (with
  * that device current) and caches it; make that first call before any stream
- * capture.  Every call shares the one array and leaves its contents behind;
+ * capture.  The cached address belongs to the device's primary context:
+ * resetting the device (cudaDeviceReset) while the library stays loaded is
+ * not supported, since later calls would use the old context's address.  Every call shares the one array and leaves its contents behind;
  * each call writes every scratch entry it reads, so nothing has to start at
  * zero.  Calls that overlap on the GPU (other streams, other host threads)
  * race on the array: serialize them.  No cudaMalloc or cudaFree is called. */

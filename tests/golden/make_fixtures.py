@@ -19,7 +19,8 @@ The GPU machine never runs this script; only the ``.npz`` files travel.
 
 Usage: ``python tests/golden/make_fixtures.py [--reference SRC] [names...]``;
 ``... matrix``, ``... warmstart`` and ``... drivers [names...]`` write the
-matrix-response, warm-start and response-driver fixtures.
+matrix-response, warm-start and response-driver fixtures; ``... spec
+[names...]`` writes the specs of ``SPEC_ONLY`` (no reference outputs).
 """
 
 from __future__ import annotations
@@ -138,6 +139,47 @@ def model_kanamori(norb: int, modes_per_orbital: int, seed: int):
     )
 
 
+def model_general(norb: int, modes_per_orbital: int, seed: int):
+    """General-interaction impurity: ``norb`` orbitals with a seeded Gaussian
+    spatial tensor U_abcd (scale 0.5) made Hermitian and permutation-symmetric
+    (U_abcd = U_badc = conj(U_dcba)), lowered to spin-orbital terms by the
+    reference's ``interaction_from_spatial_tensor`` (``_static_schema.py:77``);
+    a GOE impurity one-body block (scale 0.3) and seeded pseudomode baths per
+    orbital drawn as for the single-impurity model (T = 0.1, mu = 0)."""
+    from c3l import FermionicLindbladModel
+    from c3l.cc._static_schema import interaction_from_spatial_tensor
+    from c3l.interactions import SparseTwoBodyInteraction
+
+    rng = np.random.default_rng(seed)
+    K = rng.normal(0.0, 0.5, (norb,) * 4)
+    K = 0.5 * (K + K.transpose(1, 0, 3, 2))
+    K = 0.5 * (K + K.transpose(3, 2, 1, 0).conj())
+    terms = interaction_from_spatial_tensor(K)
+    nm = modes_per_orbital
+    n = norb * (1 + nm)
+    E = np.zeros((n, n), complex)
+    loss = np.zeros(n)
+    gain = np.zeros(n)
+    A = rng.normal(0.0, 0.3, (norb, norb))
+    E[:norb, :norb] = (A + A.T) / np.sqrt(2.0)
+    for o in range(norb):
+        eb = rng.uniform(-3, 3, nm)
+        V = rng.normal(0, 0.3, nm)
+        r = rng.uniform(0.05, 0.5, nm)
+        f = 1 / (np.exp(eb / 0.1) + 1)
+        s = slice(norb + o * nm, norb + (o + 1) * nm)
+        E[s, s] = np.diag(eb)
+        E[o, s] = V
+        E[s, o] = V
+        loss[s] = r * (1 - f)
+        gain[s] = r * f
+    inter = SparseTwoBodyInteraction(2 * n, terms.terms)
+    return FermionicLindbladModel(
+        E, np.diag(loss), np.diag(gain), U=0.0,
+        interaction_sites=tuple(range(norb)), two_body_interaction=inter,
+    )
+
+
 def _restricted_reference(model):
     from c3l.ci.reference import full_hartree_fock_reference
     from c3l.gaussian_mean_field import solve_ghf
@@ -168,7 +210,65 @@ FIXTURES = {
                         omega=None, eta=0.02, solve=False, eom=True),
     "kanamori3x8": dict(model=lambda: model_kanamori(3, 8, 2), recipe="restricted_ghf", scale=1e-3,
                         omega=None, eta=0.02, solve=False, eom=True),
+    # the general-interaction (5 orbitals, seeded U_abcd) model with one
+    # pseudomode per orbital: the product structure of the 12-mode workload
+    # (1,650 four-factor products + 100 counterterms over 40 factors) at n = 10.
+    # The reference needs 41 s per JVP here, so its own Newton solve is out of
+    # reach; the goldens (actions, sources, G^R) are taken at the fixed amplitudes
+    "gen5x1": dict(model=lambda: model_general(5, 1, 0), recipe="restricted_ghf", scale=1e-3,
+                   omega=np.linspace(-12.0, 12.0, 4096)[::128], eta=0.02, solve=False, eom=True),
 }
+
+# specs only (no reference hot-path run): the 12-mode general-interaction model
+# (n = 65), built without the cluster masks
+SPEC_ONLY = {
+    "gen5x12": dict(model=lambda: model_general(5, 12, 0), recipe="restricted_ghf"),
+}
+
+
+def light_problem(model, reference):
+    """The fields of the reference's ``FactorizedCCProblem`` that a spec reads
+    (model, reference, products, rapidities), built by the reference's own
+    product constructors but without the cluster masks and amplitude tilde map
+    (``src/c3l/cc/factorized.py:336-414``).  Those are Python loops over every
+    amplitude, too slow at n = 65; the package derives both itself.  The
+    one-body counterterm loop for an unregulated reference restates
+    ``factorized.py:383-414``."""
+    from types import SimpleNamespace
+
+    from c3l.cc.factorized import _quadratic_dissipation_counterterms
+    from c3l.ci.matrix_free import FactorizedModeProduct, _interaction_products, physical_mode_operator
+
+    products = list(_interaction_products(reference))
+    if reference.reference_gamma_loss is not None:
+        products.extend(_quadratic_dissipation_counterterms(model, reference))
+    else:
+        E = np.asarray(model.E)
+        blocks = tuple(E - np.asarray(b) for b in reference.one_body_blocks)
+        for i in range(model.n_sites):
+            for j in range(model.n_sites):
+                for spin, delta in enumerate(blocks):
+                    if delta[i, j] == 0.0:
+                        continue
+                    op = lambda site, ch: physical_mode_operator(reference, site, spin, ch)
+                    products.append(FactorizedModeProduct(
+                        f"quadratic_counter:c_{i}_{spin}_dagger_c_{j}_{spin}", complex(delta[i, j]),
+                        (op(i, "c_dagger"), op(j, "c"))))
+                    products.append(FactorizedModeProduct(
+                        f"quadratic_counter:-tilde_c_{i}_{spin}_dagger_tilde_c_{j}_{spin}", -complex(delta[j, i]),
+                        (op(i, "tilde_c_dagger"), op(j, "tilde_c"))))
+    rapidities = np.asarray(
+        tuple(v for block in reference.mode_references for v in block.rapidities), dtype=np.complex128)
+    return SimpleNamespace(model=model, reference=reference, products=tuple(products), rapidities=rapidities)
+
+
+def build_reference(spec):
+    """The HF reference of a fixture recipe (as ``factorized_cc_problem`` builds it)."""
+    model = spec["model"]()
+    recipe = spec["recipe"]
+    if recipe == "restricted_ghf":
+        return model, _restricted_reference(model)
+    raise ValueError(f"mask-free build supports the restricted GHF recipe only, not {recipe}")
 
 
 def build_problem(spec):
@@ -189,62 +289,15 @@ def build_problem(spec):
 
 
 def export_spec(cc, path: Path, recipe: str) -> dict:
-    """Write the self-contained problem description."""
-    from c3l.ci.matrix_free import physical_mode_operator
-    from c3l.ci.tilde import tilde_map_from_references
+    """Write the self-contained problem description, lowered by the package's
+    own ``ProblemSpec.from_factorized`` (the path ``ComponentStaticProblem.compile``
+    takes for a reference object)."""
+    sys.path.insert(0, str(HERE.parents[1]))
+    from c3lindblad_gb300.spec import ProblemSpec
 
-    n = cc.model.n_sites
-    M = 4 * n
-    keys: dict = {}
-    creators: list = []
-    annihilators: list = []
-
-    def factor_index(op) -> int:
-        key = op.components
-        if key not in keys:
-            c = np.zeros(M, complex)
-            a = np.zeros(M, complex)
-            for kind, mode, coefficient in key:
-                (c if kind == "create" else a)[mode] += coefficient
-            keys[key] = len(creators)
-            creators.append(c)
-            annihilators.append(a)
-        return keys[key]
-
-    maxlen = max(len(p.factors) for p in cc.products)
-    prod_factors = -np.ones((len(cc.products), maxlen), np.int64)
-    prod_len = np.zeros(len(cc.products), np.int64)
-    prod_coef = np.zeros(len(cc.products), complex)
-    for i, p in enumerate(cc.products):
-        prod_coef[i] = p.coefficient
-        prod_len[i] = len(p.factors)
-        for j, f in enumerate(p.factors):
-            prod_factors[i, j] = factor_index(f)
-    nprod_factors = len(creators)
-    # physical operators used by the EOM sources/sink (reference
-    # component_tensor.py:2816-2858), for every site and spin
-    channels = ("c", "c_dagger", "tilde_c", "tilde_c_dagger")
-    src_index = -np.ones((n, 2, 4), np.int64)
-    for site in range(n):
-        for spin in range(2):
-            for k, ch in enumerate(channels):
-                src_index[site, spin, k] = factor_index(physical_mode_operator(cc.reference, site, spin, ch))
-    det = tilde_map_from_references(cc.reference.up, cc.reference.down)
-    out = dict(
-        n=np.int64(n),
-        creators=np.asarray(creators),
-        annihilators=np.asarray(annihilators),
-        product_coefficients=prod_coef,
-        product_factors=prod_factors,
-        product_lengths=prod_len,
-        product_factor_count=np.int64(nprod_factors),
-        rapidities=np.asarray(cc.rapidities, complex),
-        mode_partner=np.asarray(det.partners, np.int64),
-        mode_phase=np.asarray(det.factors, complex),
-        source_factor=src_index,
-        impurity_site=np.int64(cc.model.impurity_site),
-        recipe=np.array(recipe),
-    )
+    spec = ProblemSpec.from_factorized(cc, recipe)
+    out = spec.as_dict()
+    out["product_factor_count"] = np.int64(int(np.max(spec.product_factors)) + 1)
     np.savez_compressed(path, **out)
     return out
 
@@ -557,6 +610,15 @@ def main() -> None:
         return
     if args.names == ["matrix"]:
         export_matrix_green(HERE / f"{MATRIX_GREEN['fixture']}.matrix.npz")
+        return
+    if args.names and args.names[0] == "spec":
+        for name in args.names[1:] or list(SPEC_ONLY):
+            t0 = time.perf_counter()
+            model, reference = build_reference(SPEC_ONLY[name])
+            cc = light_problem(model, reference)
+            export_spec(cc, HERE / f"{name}.spec.npz", SPEC_ONLY[name]["recipe"])
+            print(f"[{name}] n={model.n_sites} products={len(cc.products)} spec {time.perf_counter() - t0:.1f}s",
+                  flush=True)
         return
     if args.names and args.names[0] == "drivers":
         for name in args.names[1:] or list(DRIVERS):

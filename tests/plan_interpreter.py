@@ -73,6 +73,21 @@ def run_padded(program, name: str, ws: np.ndarray) -> None:
         ws[blk["out_off"] + np.arange(size)] = _eval_instances(stage, b, _digits_padded(size, deg, n), ws, n)
 
 
+def run_pairs(program, name: str, ws: np.ndarray) -> np.ndarray:
+    """The pair GEMMs of stage ``name``: returns the workspace followed by the
+    pair buffer (what the ``<name>_pairs`` gather stage reads)."""
+    pp = program.pairs[name]
+    out = np.concatenate([ws, np.zeros(program.pair_size, np.complex128)])
+    base = program.ws_size
+    for g in pp.groups:
+        M, N = int(g["M"]), int(g["N"])
+        k = np.arange(int(g["kbegin"]), int(g["kend"]))
+        A = ws[pp.aoff[k][:, None] + np.arange(M)[None, :]]
+        R = ws[pp.roff[k][:, None] + np.arange(N)[None, :]]
+        out[base + int(g["p_off"]) + np.arange(M * N)] = (A.T @ R).reshape(-1)
+    return out
+
+
 def run_canonical(program, name: str, ws: np.ndarray) -> np.ndarray:
     """Returns the interaction value at every element of the stage (stage order)."""
     stage = program.stages[name]

@@ -16,7 +16,7 @@ from conftest import eom_amplitudes, golden_names, load, relerr
 from c3lindblad_gb300 import compiler, layout
 from c3lindblad_gb300.plans import EOMPlan, StaticPlan
 from oracle import component_oracle as oc
-from plan_interpreter import InterpretedEOM, InterpretedStatic
+from plan_interpreter import InterpretedEOM, InterpretedStatic, run_canonical, run_pairs
 
 
 @pytest.fixture(scope="module")
@@ -80,6 +80,27 @@ def test_compiled_residual_and_jvp(name, plans):
     assert abs(jref - g["jvp_reference"]) < 1e-12 * max(1.0, abs(g["jvp_reference"]))
 
 
+@pytest.mark.parametrize("name", golden_names())
+def test_pair_gemm_stage_matches_instance_stage(name, plans):
+    """The GEMM form of the JVP output (pair GEMMs + gather) equals the
+    instance form on the same workspace, and so the reference's JVP."""
+    spec, g, plan = plans(name)
+    it = InterpretedStatic(plan)
+    it.residual(g["fixed_variables"], linearize=True)
+    it.jvp(g["fixed_direction_variables"])
+    prog = plan.program
+    want = run_canonical(prog, "jvp", it.ws)
+    got = run_canonical(prog, "jvp_pairs", run_pairs(prog, "jvp", it.ws))
+    assert relerr(got, want) < 1e-13
+    pp = prog.pairs["jvp"]
+    assert pp.size == prog.pair_size and pp.tiles["group"].max() == pp.groups.size - 1
+    # every tile lies inside its group's P block
+    gr = pp.groups[pp.tiles["group"]]
+    assert np.all(pp.tiles["m0"] < gr["M"]) and np.all(pp.tiles["n0"] < gr["N"])
+    assert np.all(pp.groups["p_off"] + pp.groups["M"].astype(np.int64) * pp.groups["N"] <= prog.pair_size)
+    assert np.all(pp.aoff >= 0) and np.all(pp.roff >= 0) and np.all(pp.aoff < prog.ws_size)
+
+
 @pytest.mark.parametrize("name", golden_names(with_eom=True))
 @pytest.mark.parametrize("charge", [1, -1])
 def test_compiled_sigma_and_sources(name, charge, plans):
@@ -114,8 +135,16 @@ def test_program_table_layouts_match_c_structs():
     class Tile(ctypes.Structure):
         _fields_ = [("block", ctypes.c_int32), ("count", ctypes.c_int32), ("start", ctypes.c_int64)]
 
+    class PairGroup(ctypes.Structure):
+        _fields_ = [("p_off", ctypes.c_int64), ("kbegin", ctypes.c_int64), ("kend", ctypes.c_int64),
+                    ("M", ctypes.c_int32), ("N", ctypes.c_int32)]
+
+    class PairTile(ctypes.Structure):
+        _fields_ = [("group", ctypes.c_int32), ("m0", ctypes.c_int32), ("n0", ctypes.c_int32), ("pad", ctypes.c_int32)]
+
     for dt, cs in ((compiler.CONTRACT_DTYPE, Task), (compiler.INSTANCE_DTYPE, Inst),
-                   (compiler.BLOCK_DTYPE, Block), (compiler.TILE_DTYPE, Tile)):
+                   (compiler.BLOCK_DTYPE, Block), (compiler.TILE_DTYPE, Tile),
+                   (compiler.PAIR_GROUP_DTYPE, PairGroup), (compiler.PAIR_TILE_DTYPE, PairTile)):
         assert dt.itemsize == ctypes.sizeof(cs)
         for name, *_ in cs._fields_:
             assert dt.fields[name][1] == getattr(cs, name).offset, name

@@ -411,8 +411,10 @@ def test_mixed_precision_solve_meets_fp64_tolerance(name, problems):
     assert relerr(sol.amplitudes, g["solution_amplitudes"]) < 1e-8
 
 
-def test_single_precision_jvp_tracks_fp64(problems, cuda_device):
-    spec, g, p = problems("siam10")
+@pytest.mark.parametrize("name", golden_names())
+def test_single_precision_jvp_tracks_fp64(name, problems, cuda_device):
+    """The FP32 JVP (its output stage summed by the pair GEMMs) against the FP64 one."""
+    spec, g, p = problems(name)
     ops = p.ops
     x = torch.from_numpy(g["fixed_variables"]).to(cuda_device)
     d = torch.from_numpy(g["fixed_direction_variables"]).to(cuda_device)

@@ -1,0 +1,83 @@
+"""The pair-GEMM kernel (``c3l_pair_gemm`` / ``_f32``) against NumPy.
+
+Each group multiplies K gathered operand rows: P[i, j] = sum_k A_k[i] R_k[j]
+with A_k = ws[aoff[k] : aoff[k] + M] and R_k = ws[roff[k] : roff[k] + N].  The
+shapes cover ragged tiles (M, N not multiples of 64), single rows and columns,
+chunks of fewer than 8 anchors, and rows shared between groups.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from c3lindblad_gb300 import compiler
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+SHAPES = [(1, 1, 1), (3, 7, 2), (64, 64, 8), (65, 65, 9), (130, 17, 23), (1, 300, 5), (300, 1, 5),
+          (197, 201, 37), (4225, 65, 3)]
+
+
+def _program(rng, ws_size: int):
+    groups = np.zeros(len(SHAPES), compiler.PAIR_GROUP_DTYPE)
+    aoff, roff, tiles = [], [], []
+    p = 0
+    for g, (M, N, K) in enumerate(SHAPES):
+        groups[g] = (p, len(aoff), len(aoff) + K, M, N)
+        aoff.extend(int(v) for v in rng.integers(0, ws_size - M + 1, K))
+        roff.extend(int(v) for v in rng.integers(0, ws_size - N + 1, K))
+        for m0 in range(0, M, compiler.PAIR_TILE):
+            for n0 in range(0, N, compiler.PAIR_TILE):
+                tiles.append((g, m0, n0, 0))
+        p += M * N
+    t = np.zeros(len(tiles), compiler.PAIR_TILE_DTYPE)
+    for i, row in enumerate(tiles):
+        t[i] = row
+    return groups, np.asarray(aoff, np.int64), np.asarray(roff, np.int64), t, p
+
+
+def _expected(ws, groups, aoff, roff):
+    out = []
+    for g in groups:
+        k = np.arange(int(g["kbegin"]), int(g["kend"]))
+        A = ws[aoff[k][:, None] + np.arange(int(g["M"]))[None, :]]
+        R = ws[roff[k][:, None] + np.arange(int(g["N"]))[None, :]]
+        out.append((A.T @ R).reshape(-1))
+    return np.concatenate(out)
+
+
+@pytest.mark.parametrize("dtype", ["f64", "f32"])
+def test_pair_gemm_matches_numpy(dtype, cuda_device):
+    from c3lindblad_gb300 import runtime as rt
+
+    lib = rt.lib()
+    rng = np.random.default_rng(7)
+    ws_size = 20000
+    groups, aoff, roff, tiles, psize = _program(rng, ws_size)
+    ws = rng.normal(size=ws_size) + 1j * rng.normal(size=ws_size)
+    want = _expected(ws, groups, aoff, roff)
+    cdt = torch.complex128 if dtype == "f64" else torch.complex64
+    buf = torch.full((ws_size + psize,), complex("nan"), dtype=cdt, device=cuda_device)
+    buf[:ws_size] = torch.from_numpy(ws).to(cuda_device, cdt)
+    keep = [torch.from_numpy(a.view(np.uint8).copy()).to(cuda_device) for a in (groups, aoff, roff, tiles)]
+    pp = rt.PairProgram()
+    pp.groups, pp.aoff, pp.roff, pp.tiles = (k.data_ptr() for k in keep)
+    pp.ntiles = tiles.size
+    pp.base = ws_size
+    fn = lib.c3l_pair_gemm if dtype == "f64" else lib.c3l_pair_gemm_f32
+    assert fn(C.byref(pp), buf.data_ptr(), torch.cuda.current_stream(cuda_device).cuda_stream) == 0
+    torch.cuda.synchronize(cuda_device)
+    got = buf[ws_size:].cpu().numpy().astype(np.complex128)
+    assert np.all(np.isfinite(got))  # every P entry written
+    # per-entry bound: |error| <= c eps sum_k |A_k[i]| |R_k[j]|
+    tol = 1e-13 if dtype == "f64" else 3e-6
+    scale = _expected(np.abs(ws), groups, aoff, roff).real
+    assert np.all(np.abs(got - want) <= tol * scale)
+    # the workspace itself is untouched
+    assert np.array_equal(buf[:ws_size].cpu().numpy().astype(np.complex128),
+                          ws if dtype == "f64" else ws.astype(np.complex64).astype(np.complex128))

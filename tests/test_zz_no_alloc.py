@@ -21,9 +21,13 @@ pytestmark = pytest.mark.gpu
 torch = pytest.importorskip("torch")
 
 
-def _problem(rng, m: int, nshift: int):
-    H = np.triu(rng.normal(size=(m + 1, m)) + 1j * rng.normal(size=(m + 1, m)), -1)
-    H[np.arange(1, m + 1), np.arange(m)] = np.abs(H[np.arange(1, m + 1), np.arange(m)]) + 0.5
+def _problem(rng, m: int, nshift: int, scale: float = 1.0, damping: float = 0.0):
+    """A Hessenberg matrix with positive subdiagonal; ``damping`` moves its
+    diagonal to Im = -damping, as for a dissipative operator, which keeps
+    z I - H well conditioned for the shifts (Im z = 0.05) at large m."""
+    H = scale * np.triu(rng.normal(size=(m + 1, m)) + 1j * rng.normal(size=(m + 1, m)), -1)
+    H[np.arange(1, m + 1), np.arange(m)] = np.abs(H[np.arange(1, m + 1), np.arange(m)]) + 0.5 * scale
+    H[np.arange(m), np.arange(m)] -= 1j * damping
     shifts = np.linspace(-4.0, 4.0, nshift) + 0.05j
     return H, shifts
 
@@ -34,10 +38,13 @@ def test_noalloc_coordinates_match_allocating_entry_point(cuda_device):
     lib = runtime.load_library()
     stream = torch.cuda.current_stream(cuda_device).cuda_stream
     rng = np.random.default_rng(2024)
-    # two calls in a row; the second problem is larger, so stale scratch from the
-    # first call would show up in its result
-    for m, nshift, beta in ((40, 29, 1.7), (96, 53, 0.6)):
-        H, shifts = _problem(rng, m, nshift)
+    # calls in a row; each problem is larger than the one before, so stale
+    # scratch from an earlier call would show up in its result.  The last one
+    # needs 60 * 400 * 401 / 2 entries, more than the fixed scratch holds, so
+    # its shifts run in three chunks (26, 26, 8) that reuse the array in order.
+    for m, nshift, beta, scale, damping in ((40, 29, 1.7, 1.0, 0.0), (96, 53, 0.6, 1.0, 0.0),
+                                            (400, 60, 1.1, 0.1, 1.0)):
+        H, shifts = _problem(rng, m, nshift, scale, damping)
         Hd = torch.from_numpy(np.ascontiguousarray(H)).to(cuda_device)
         zd = torch.from_numpy(shifts).to(cuda_device)
         scratch = torch.empty(nshift * m * (m + 1) // 2, dtype=torch.complex128, device=cuda_device)
