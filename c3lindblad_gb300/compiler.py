@@ -323,7 +323,7 @@ class Program:
     atom_offsets: dict = field(default_factory=dict)
     rest_offsets: dict = field(default_factory=dict)
     pairs: dict = field(default_factory=dict)    # stage name -> PairProgram
-    pair_size: int = 0                           # pair-buffer entries (after the workspace)
+    pair_size: int = 0                           # pair-buffer entries (after the workspace): the largest program
 
 
 class Builder:
@@ -694,8 +694,7 @@ def compile_pairs(builder: Builder, name: str, rest_info: dict, coords: Coordina
     garr = np.zeros(len(groups), PAIR_GROUP_DTYPE)
     aoff, roff, tiles = [], [], []
     block_rows = [(-1, sum(k), []) for k in coords.keys]
-    base = builder.pair_size
-    p = base
+    p = 0  # every program's P blocks start at the pair buffer's first entry
     for g, (b, ka, kr, rows) in enumerate(groups):
         M, N = n ** sum(ka), n ** sum(kr)
         garr[g] = (p, len(aoff), len(aoff) + len(rows), M, N)
@@ -711,8 +710,8 @@ def compile_pairs(builder: Builder, name: str, rest_info: dict, coords: Coordina
     tarr = np.zeros(len(tiles), PAIR_TILE_DTYPE)
     for i, t in enumerate(tiles):
         tarr[i] = t
-    builder.pairs[name] = PairProgram(garr, np.asarray(aoff, np.int64), np.asarray(roff, np.int64), tarr, p - base)
-    builder.pair_size = p
+    builder.pairs[name] = PairProgram(garr, np.asarray(aoff, np.int64), np.asarray(roff, np.int64), tarr, p)
+    builder.pair_size = max(builder.pair_size, p)
     builder.emit_stage(f"{name}_pairs", "canonical", block_rows, elements=pos, digits=_digits(coords, pos),
                        element_block=blk)
     builder.stage_data[f"{name}_pairs"].pair_relative = True

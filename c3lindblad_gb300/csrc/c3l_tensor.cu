@@ -22,10 +22,12 @@
 // over four thread groups.
 #include <cuda_runtime.h>
 #include <cstring>
+#include <type_traits>
 #include <stdint.h>
 
 #include "c3l_gb300.h"
 #include "c3l_internal.h"
+#include "c3l_df.h"
 #include "c3l_pdl.h"
 
 namespace {
@@ -429,12 +431,115 @@ __global__ void __launch_bounds__(kPairThreads) k_pair_gemm(c3l_pair_program pp,
     }
 }
 
+// The pair GEMMs of an FP64 workspace in double-float arithmetic on the FP32
+// pipe.  Operand entries are split into FP32 (hi, lo) pairs as they are
+// staged (complex: re hi, re lo, im hi, im lo); each real product is formed
+// to about 2^-46 (Dekker's product with one FMA, df_mac) and summed by
+// TwoSum into a (sum, correction) pair per real component, finished in FP64
+// when P is written.  The result differs from an FP64 GEMM by about 1e-14 of
+// sum_k |A_k[i]| |R_k[j]|, at several times the FP64 pipe's rate.
+__global__ void __launch_bounds__(kPairThreads) k_pair_gemm_df(c3l_pair_program pp, Batch<double2> bt) {
+    if (!bt.pdl_at_exit) c3l::pdl_launch_dependents();
+    if (batch_stopped(bt)) return;
+    double2* __restrict__ ws = bt.ws[blockIdx.y];
+    __shared__ float4 sa[kPairChunk][kPairTile];
+    __shared__ float4 sr[kPairChunk][kPairTile];
+    const c3l_pair_tile t = pp.tiles[blockIdx.x];
+    const c3l_pair_group g = pp.groups[t.group];
+    const int tm = threadIdx.x / 16, tn = threadIdx.x % 16;
+    const int lc = threadIdx.x % kPairTile, lr = threadIdx.x / kPairTile;
+    const bool a_ok = t.m0 + lc < g.M, r_ok = t.n0 + lc < g.N;
+    const double2 zero = make_double2(0.0, 0.0);
+    int64_t ao[2] = {-1, -1}, ro[2] = {-1, -1};
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+        const int64_t k = g.kbegin + lr + 4 * u;
+        if (k < g.kend) {
+            ao[u] = pp.aoff[k];
+            ro[u] = pp.roff[k];
+        }
+    }
+    c3l::pdl_wait();
+    double2 av[2], rv[2];
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+        av[u] = (ao[u] >= 0 && a_ok) ? ws[ao[u] + t.m0 + lc] : zero;
+        rv[u] = (ro[u] >= 0 && r_ok) ? ws[ro[u] + t.n0 + lc] : zero;
+    }
+    // (re sum, re correction, im sum, im correction) of each of the thread's 4 x 4 entries
+    float4 acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    auto split = [](double2 v) {
+        float4 q;
+        split_d(v.x, q.x, q.y);
+        split_d(v.y, q.z, q.w);
+        return q;
+    };
+    for (int64_t k0 = g.kbegin; k0 < g.kend; k0 += kPairChunk) {
+        __syncthreads();
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            sa[lr + 4 * u][lc] = split(av[u]);
+            sr[lr + 4 * u][lc] = split(rv[u]);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            const int64_t k = k0 + kPairChunk + lr + 4 * u;
+            const bool ok = k < g.kend;
+            av[u] = (ok && a_ok) ? ws[pp.aoff[k] + t.m0 + lc] : zero;
+            rv[u] = (ok && r_ok) ? ws[pp.roff[k] + t.n0 + lc] : zero;
+        }
+#pragma unroll 2
+        for (int r = 0; r < kPairChunk; ++r) {
+            float4 a[4], b[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                a[i] = sa[r][tm + 16 * i];
+                b[i] = sr[r][tn + 16 * i];
+            }
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    float4& c = acc[i][j];
+                    // re += ar br - ai bi, im += ar bi + ai br
+                    df_mac(c.x, c.y, a[i].x, a[i].y, b[j].x, b[j].y);
+                    df_mac(c.x, c.y, -a[i].z, -a[i].w, b[j].z, b[j].w);
+                    df_mac(c.z, c.w, a[i].x, a[i].y, b[j].z, b[j].w);
+                    df_mac(c.z, c.w, a[i].z, a[i].w, b[j].x, b[j].y);
+                }
+        }
+    }
+    double2* __restrict__ P = ws + pp.base + g.p_off;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const int m = t.m0 + tm + 16 * i;
+        if (m >= g.M) continue;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int nn = t.n0 + tn + 16 * j;
+            const float4 c = acc[i][j];
+            if (nn < g.N) P[(int64_t)m * g.N + nn] = make_double2((double)c.x + (double)c.y, (double)c.z + (double)c.w);
+        }
+    }
+}
+
+// FP64 workspaces run the double-float kernel unless `fp64_pipe` asks for the
+// plain FP64 one (kept for parity checks of the double-float sums).
 template <typename C>
-c3l_status run_pairs(const c3l_pair_program& pp, const Batch<C>& bt, cudaStream_t s) {
+c3l_status run_pairs(const c3l_pair_program& pp, const Batch<C>& bt, cudaStream_t s, bool fp64_pipe = false) {
     if (pp.ntiles <= 0) return C3L_OK;
     if (!pp.groups || !pp.aoff || !pp.roff || !pp.tiles || pp.base < 0) return C3L_ERR_ARGUMENT;
-    return c3l::launch_pdl(k_pair_gemm<C>, dim3((unsigned)pp.ntiles, (unsigned)bt.nb), dim3(kPairThreads), 0, s, 0,
-                           bt.pdl, pp, bt);
+    const dim3 grid((unsigned)pp.ntiles, (unsigned)bt.nb);
+    if constexpr (std::is_same<C, double2>::value) {
+        if (!fp64_pipe)
+            return c3l::launch_pdl(k_pair_gemm_df, grid, dim3(kPairThreads), 0, s, 0, bt.pdl, pp, bt);
+    }
+    return c3l::launch_pdl(k_pair_gemm<C>, grid, dim3(kPairThreads), 0, s, 0, bt.pdl, pp, bt);
 }
 
 enum WedgeMode { kPadded = 0, kStatic = 1, kEom = 2, kSource = 3 };
@@ -886,6 +991,11 @@ c3l_status c3l_wedge_eom_out(const c3l_wedge_stage* stage, int32_t n, const c3l_
 }
 
 c3l_status c3l_pair_gemm(const c3l_pair_program* program, c3l_complex* ws, void* stream) {
+    if (!program || !ws) return C3L_ERR_ARGUMENT;
+    return run_pairs<double2>(*program, single<double2>(reinterpret_cast<double2*>(ws)), as_stream(stream), true);
+}
+
+c3l_status c3l_pair_gemm_df(const c3l_pair_program* program, c3l_complex* ws, void* stream) {
     if (!program || !ws) return C3L_ERR_ARGUMENT;
     return run_pairs<double2>(*program, single<double2>(reinterpret_cast<double2*>(ws)), as_stream(stream));
 }

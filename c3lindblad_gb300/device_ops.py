@@ -51,8 +51,10 @@ class DeviceStatic:
         self._up = up
         self.D = plan.num_variables
         self.A = plan.num_amplitudes
-        self.ws_lin = _cz(prog.ws_size, self.device)
-        self.ws_res = _cz(prog.ws_size, self.device)
+        # FP64 workspaces: the workspace, then the pair buffer of the residual's output
+        # stage (double-float pair GEMMs)
+        self.ws_lin = _cz(prog.ws_size + prog.pair_size, self.device)
+        self.ws_res = _cz(prog.ws_size + prog.pair_size, self.device)
         with up.batch():  # every table of the static actions in one copy per arena chunk (no launch inside)
             vec = up.raw(prog.vectors)
             self.vec = vec
@@ -77,10 +79,13 @@ class DeviceStatic:
                 sa.interaction_scale = 1.0
                 return sa
 
-            self.res_action = static_action(self.ws_res, "T", ["res_rest_T", "res_scalar"], "res", plan.scatter_T,
-                                            self.canon_R, plan.epilogue)
-            self.lin_action = static_action(self.ws_lin, "T", ["res_rest_T", "res_scalar", "jvp_rest_T"], "res",
-                                            plan.scatter_T, self.canon_T, plan.epilogue)
+            rp = "res" if "res" in prog.pairs else None
+            self.res_action = static_action(self.ws_res, "T", ["res_rest_T", "res_scalar"],
+                                            "res_pairs" if rp else "res", plan.scatter_T, self.canon_R, plan.epilogue,
+                                            pairs=rp)
+            self.lin_action = static_action(self.ws_lin, "T", ["res_rest_T", "res_scalar", "jvp_rest_T"],
+                                            "res_pairs" if rp else "res", plan.scatter_T, self.canon_T, plan.epilogue,
+                                            pairs=rp)
             self.jvp_action = static_action(self.ws_lin, "V", ["jvp_rest_V", "jvp_scalar"], "jvp", plan.scatter_V,
                                             self.canon_V, plan.epilogue_jvp)
             # single-precision twin of the JVP (inner operator of the mixed-precision solve):
@@ -255,14 +260,16 @@ class DeviceEOM:
         prog = self.plan.program
         up = self._up
         built = []
+        pairs = "sigma" if "sigma" in prog.pairs else None
         with up.batch():  # tables sent when the block ends, before the context launches below
             while len(self.workspaces) + len(built) < count:
-                ws = _cz(prog.ws_size, self.device)
+                # the workspace, then (pair GEMMs) the pair buffer the output stage reads
+                ws = _cz(prog.ws_size + (prog.pair_size if pairs else 0), self.device)
                 ctx = rt.build_action(up, prog, self.vec.data_ptr(), ws, "T", ["sigma_rest_T"], None,
                                       self.plan.scatter_T)
                 ea = rt.EomAction()
-                ea.action = rt.build_action(up, prog, self.vec.data_ptr(), ws, "X", ["sigma_rest_X"], "sigma",
-                                            self.plan.scatter_X)
+                ea.action = rt.build_action(up, prog, self.vec.data_ptr(), ws, "X", ["sigma_rest_X"],
+                                            "sigma_pairs" if pairs else "sigma", self.plan.scatter_X, pairs)
                 ea.lam = self.lam.data_ptr()
                 built.append((ws, ctx, ea))
         for ws, ctx, ea in built:

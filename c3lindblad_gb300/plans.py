@@ -59,7 +59,7 @@ class StaticPlan:
         # real-coordinate outputs at tilde representatives (Newton path) and
         # complex outputs -i(...) at every coordinate (arbitrary amplitudes)
         self.res_scalar_off = compile_output(b, "res", self.res_terms, coords, rep, "res_rest", "res_scalar",
-                                             extra=(("res_all", allpos, -1j),))
+                                             extra=(("res_all", allpos, -1j),), pairs=True)
         # the inner JVP of the mixed solve reads its outputs through pair GEMMs
         self.jvp_scalar_off = compile_output(b, "jvp", self.jvp_terms, coords, rep, "jvp_rest", "jvp_scalar",
                                              extra=(("jvp_all", allpos, -1j),), pairs=True)
@@ -143,7 +143,8 @@ class EOMPlan:
         b.add_source("T", static.coords.keys)
         b.add_source("X", coords.keys)
         allpos = np.arange(coords.dimension)
-        compile_output(b, "sigma", self.sigma_terms, coords, allpos, "sigma_rest", None)
+        # the output stage sums its anchor ^ rest products as pair GEMMs
+        compile_output(b, "sigma", self.sigma_terms, coords, allpos, "sigma_rest", None, pairs=True)
         self.program = b.finish()
         self.scatter_T = _scatter_table(static.coords, self.program.source_offsets["T"])
         self.scatter_X = _scatter_table(coords, self.program.source_offsets["X"])

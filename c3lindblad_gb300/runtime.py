@@ -117,7 +117,7 @@ EXPORTS = (
     "c3l_scale_c", "c3l_scale_r", "c3l_precondition", "c3l_hessenberg_shifted", "c3l_hessenberg_coordinates",
     "c3l_hessenberg_coordinates_noalloc", "c3l_gmres", "c3l_gmres_scratch", "c3l_gmres_release", "c3l_gmres_shifted", "c3l_shifted_combine", "c3l_arnoldi", "c3l_hessenberg_advance",
     "c3l_arnoldi_column", "c3l_static_apply_f32", "c3l_eom_sigma_f32", "c3l_action_prepare_f32", "c3l_downcast",
-    "c3l_wedge_static_out_f32", "c3l_pair_gemm", "c3l_pair_gemm_f32", "c3l_mlp_forward", "c3l_mlp_backward", "c3l_mlp_adam", "c3l_warm_features", "c3l_warm_apply", "c3l_version",
+    "c3l_wedge_static_out_f32", "c3l_pair_gemm", "c3l_pair_gemm_df", "c3l_pair_gemm_f32", "c3l_mlp_forward", "c3l_mlp_backward", "c3l_mlp_adam", "c3l_warm_features", "c3l_warm_apply", "c3l_version",
 )
 
 
@@ -154,6 +154,7 @@ def _declare(lib) -> None:
         "c3l_action_prepare_f32": [P, P, P],
         "c3l_downcast": [I64, P, P, P],
         "c3l_pair_gemm": [P, P, P],
+        "c3l_pair_gemm_df": [P, P, P],
         "c3l_pair_gemm_f32": [P, P, P],
         "c3l_mlp_forward": [I64, P, P, P, P],
         "c3l_mlp_backward": [I64, P, P, P, C.c_float, P, P, P, P],

@@ -11,7 +11,7 @@ from __future__ import annotations
 
 import resource
 import time
-from dataclasses import dataclass
+from dataclasses import dataclass, field
 from pathlib import Path
 from typing import Callable
 
@@ -146,6 +146,9 @@ class ComponentCCSolution:
     peak_rss_kib: int
     gpu_launches: int = 0
     warm_start: str = "none"
+    # the amplitudes as the device vector they were unpacked into (an EOM
+    # context built from it needs no host round trip)
+    device_amplitudes: object = field(default=None, repr=False, compare=False)
 
 
 # ----------------------------------------------------------------- problem
@@ -468,7 +471,7 @@ def _solve(p, ops, controls, initial_amplitudes, accepted_step_callback, warm_st
         residual_evaluations=residual_evaluations, jvp_evaluations=jvp_evaluations, history=tuple(history),
         preconditioner=pre, wall_seconds=float(time.perf_counter() - started),
         peak_rss_kib=int(resource.getrusage(resource.RUSAGE_SELF).ru_maxrss),
-        gpu_launches=rt.LaunchCounter.count - launches0, warm_start=warm_label,
+        gpu_launches=rt.LaunchCounter.count - launches0, warm_start=warm_label, device_amplitudes=amp,
     )
 
 

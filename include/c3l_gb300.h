@@ -168,9 +168,13 @@ c3l_status c3l_wedge_eom_out(const c3l_wedge_stage* stage, int32_t n, const c3l_
                              const c3l_complex* lam, const c3l_complex* xin, c3l_complex* out,
                              void* stream);
 
-/* The pair GEMMs alone over a complex FP64 / FP32 workspace (the P blocks
- * are written at ws[program->base + p_off ...]). */
+/* The pair GEMMs alone over a complex workspace (the P blocks are written at
+ * ws[program->base + p_off ...]): c3l_pair_gemm on the FP64 pipe,
+ * c3l_pair_gemm_df in double-float arithmetic on the FP32 pipe (FP32 (hi, lo)
+ * pairs, about 1e-14 relative; what the FP64 actions run), c3l_pair_gemm_f32
+ * over an FP32 workspace. */
 c3l_status c3l_pair_gemm(const c3l_pair_program* program, c3l_complex* ws, void* stream);
+c3l_status c3l_pair_gemm_df(const c3l_pair_program* program, c3l_complex* ws, void* stream);
 c3l_status c3l_pair_gemm_f32(const c3l_pair_program* program, c3l_complex32* ws, void* stream);
 
 /* EOM sources: out[mu] = scale * V  (src/c3l/cc/component_tensor.py:2788-2798). */

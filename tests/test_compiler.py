@@ -89,16 +89,31 @@ def test_pair_gemm_stage_matches_instance_stage(name, plans):
     it.residual(g["fixed_variables"], linearize=True)
     it.jvp(g["fixed_direction_variables"])
     prog = plan.program
-    want = run_canonical(prog, "jvp", it.ws)
-    got = run_canonical(prog, "jvp_pairs", run_pairs(prog, "jvp", it.ws))
+    for stage in ("res", "jvp"):  # the residual's stage reads the same workspace
+        want = run_canonical(prog, stage, it.ws)
+        got = run_canonical(prog, f"{stage}_pairs", run_pairs(prog, stage, it.ws))
+        assert relerr(got, want) < 1e-13
+        pp = prog.pairs[stage]
+        assert pp.size <= prog.pair_size and pp.tiles["group"].max() == pp.groups.size - 1
+        # every tile lies inside its group's P block, every block inside the buffer
+        gr = pp.groups[pp.tiles["group"]]
+        assert np.all(pp.tiles["m0"] < gr["M"]) and np.all(pp.tiles["n0"] < gr["N"])
+        assert np.all(pp.groups["p_off"] + pp.groups["M"].astype(np.int64) * pp.groups["N"] <= prog.pair_size)
+        assert np.all(pp.aoff >= 0) and np.all(pp.roff >= 0) and np.all(pp.aoff < prog.ws_size)
+
+
+@pytest.mark.parametrize("name", golden_names(with_eom=True))
+@pytest.mark.parametrize("charge", [1, -1])
+def test_sigma_pair_gemm_stage_matches_instance_stage(name, charge, plans):
+    spec, g, plan = plans(name)
+    tag = "p" if charge == 1 else "m"
+    ep = EOMPlan(plan, 0, charge)
+    it = InterpretedEOM(ep, eom_amplitudes(g))
+    it.sigma(g[f"eom{tag}_probe"])
+    prog = ep.program
+    want = run_canonical(prog, "sigma", it.ws)
+    got = run_canonical(prog, "sigma_pairs", run_pairs(prog, "sigma", it.ws))
     assert relerr(got, want) < 1e-13
-    pp = prog.pairs["jvp"]
-    assert pp.size == prog.pair_size and pp.tiles["group"].max() == pp.groups.size - 1
-    # every tile lies inside its group's P block
-    gr = pp.groups[pp.tiles["group"]]
-    assert np.all(pp.tiles["m0"] < gr["M"]) and np.all(pp.tiles["n0"] < gr["N"])
-    assert np.all(pp.groups["p_off"] + pp.groups["M"].astype(np.int64) * pp.groups["N"] <= prog.pair_size)
-    assert np.all(pp.aoff >= 0) and np.all(pp.roff >= 0) and np.all(pp.aoff < prog.ws_size)
 
 
 @pytest.mark.parametrize("name", golden_names(with_eom=True))

@@ -1,4 +1,4 @@
-"""The pair-GEMM kernel (``c3l_pair_gemm`` / ``_f32``) against NumPy.
+"""The pair-GEMM kernels (``c3l_pair_gemm`` / ``_df`` / ``_f32``) against NumPy.
 
 Each group multiplies K gathered operand rows: P[i, j] = sum_k A_k[i] R_k[j]
 with A_k = ws[aoff[k] : aoff[k] + M] and R_k = ws[roff[k] : roff[k] + N].  The
@@ -51,7 +51,7 @@ def _expected(ws, groups, aoff, roff):
     return np.concatenate(out)
 
 
-@pytest.mark.parametrize("dtype", ["f64", "f32"])
+@pytest.mark.parametrize("dtype", ["f64", "df", "f32"])
 def test_pair_gemm_matches_numpy(dtype, cuda_device):
     from c3lindblad_gb300 import runtime as rt
 
@@ -61,7 +61,7 @@ def test_pair_gemm_matches_numpy(dtype, cuda_device):
     groups, aoff, roff, tiles, psize = _program(rng, ws_size)
     ws = rng.normal(size=ws_size) + 1j * rng.normal(size=ws_size)
     want = _expected(ws, groups, aoff, roff)
-    cdt = torch.complex128 if dtype == "f64" else torch.complex64
+    cdt = torch.complex64 if dtype == "f32" else torch.complex128
     buf = torch.full((ws_size + psize,), complex("nan"), dtype=cdt, device=cuda_device)
     buf[:ws_size] = torch.from_numpy(ws).to(cuda_device, cdt)
     keep = [torch.from_numpy(a.view(np.uint8).copy()).to(cuda_device) for a in (groups, aoff, roff, tiles)]
@@ -69,15 +69,16 @@ def test_pair_gemm_matches_numpy(dtype, cuda_device):
     pp.groups, pp.aoff, pp.roff, pp.tiles = (k.data_ptr() for k in keep)
     pp.ntiles = tiles.size
     pp.base = ws_size
-    fn = lib.c3l_pair_gemm if dtype == "f64" else lib.c3l_pair_gemm_f32
+    fn = {"f64": lib.c3l_pair_gemm, "df": lib.c3l_pair_gemm_df, "f32": lib.c3l_pair_gemm_f32}[dtype]
     assert fn(C.byref(pp), buf.data_ptr(), torch.cuda.current_stream(cuda_device).cuda_stream) == 0
     torch.cuda.synchronize(cuda_device)
     got = buf[ws_size:].cpu().numpy().astype(np.complex128)
     assert np.all(np.isfinite(got))  # every P entry written
     # per-entry bound: |error| <= c eps sum_k |A_k[i]| |R_k[j]|
-    tol = 1e-13 if dtype == "f64" else 3e-6
+    # FP64: reassociation only; double-float: products to 2^-46 and TwoSum sums
+    tol = {"f64": 1e-13, "df": 1e-12, "f32": 3e-6}[dtype]
     scale = _expected(np.abs(ws), groups, aoff, roff).real
     assert np.all(np.abs(got - want) <= tol * scale)
     # the workspace itself is untouched
     assert np.array_equal(buf[:ws_size].cpu().numpy().astype(np.complex128),
-                          ws if dtype == "f64" else ws.astype(np.complex64).astype(np.complex128))
+                          ws if dtype != "f32" else ws.astype(np.complex64).astype(np.complex128))
