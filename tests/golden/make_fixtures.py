@@ -18,9 +18,10 @@ reference's own setup code, runs the reference's CPU hot path and writes:
 The GPU machine never runs this script; only the ``.npz`` files travel.
 
 Usage: ``python tests/golden/make_fixtures.py [--reference SRC] [names...]``;
-``... matrix``, ``... warmstart`` and ``... drivers [names...]`` write the
-matrix-response, warm-start and response-driver fixtures; ``... spec
-[names...]`` writes the specs of ``SPEC_ONLY`` (no reference outputs).
+``... matrix [fixtures...]``, ``... warmstart``, ``... drivers [names...]`` and
+``... ed`` write the matrix-response, warm-start, response-driver and
+exact-diagonalisation fixtures; ``... spec [names...]`` writes the specs of
+``SPEC_ONLY`` (no reference outputs).
 """
 
 from __future__ import annotations
@@ -203,7 +204,7 @@ FIXTURES = {
     "twosrc": dict(model=model_twosrc, recipe="legacy_half_filled:0.3", scale=5e-4,
                    omega=np.linspace(-2.0, 2.0, 17), eta=0.1, solve=True),
     "siam10": dict(model=lambda: model_siam(10, 0), recipe="legacy_half_filled:0.5", scale=1e-3,
-                   omega=np.linspace(-8.0, 8.0, 1001)[::50], eta=0.0, solve=True),
+                   omega=np.linspace(-8.0, 8.0, 1001), eta=0.0, solve=True),
     # the reference's Newton solve does not converge on these Kanamori draws from
     # zero amplitudes, so EOM parity uses the fixed amplitudes instead
     "kanamori3x2": dict(model=lambda: model_kanamori(3, 2, 2), recipe="restricted_ghf", scale=1e-3,
@@ -478,26 +479,49 @@ def compact_golden(path: Path) -> None:
     np.savez_compressed(path, **out)
 
 
-MATRIX_GREEN = dict(fixture="kanamori3x2", sites=(0, 1, 2), omega=np.linspace(-6.0, 6.0, 61), eta=0.2,
-                    maximum_krylov_dimension=1062)
+MATRIX_GREEN = {
+    # n = 9 Kanamori: charge +1
+    "kanamori3x2": dict(sites=(0, 1, 2), omega=np.linspace(-6.0, 6.0, 61), eta=0.2, maximum_krylov_dimension=1062,
+                        charges=(1,)),
+    # n = 27 Kanamori (the three-orbital, eight-mode workload's model): charge +1 and -1,
+    # eta = 0.02 on a short grid of [-10, 10]
+    "kanamori3x8": dict(sites=(0, 1, 2), omega=np.linspace(-10.0, 10.0, 41), eta=0.02, maximum_krylov_dimension=1600,
+                        charges=(1, -1)),
+}
 
 
-def export_matrix_green(path: Path) -> None:
+def export_matrix_green(fixture: str) -> None:
     """Matrix G^R_ab(omega) of the reference's one-sided Arnoldi driver
     (component_retarded_matrix_green_arnoldi) for the three impurity orbitals
-    of the n = 9 Kanamori fixture, charge +1, at the fixture's fixed amplitudes."""
+    of a Kanamori fixture at the fixture's fixed amplitudes, written to
+    ``<fixture>.matrix.npz`` (charge +1) and ``<fixture>.matrix_m.npz`` (charge -1)."""
     from c3l.cc.component_response import ComponentSigmaOperator, component_retarded_matrix_green_arnoldi
     from c3l.cc.component_tensor import (
         ComponentEOMProblem, ComponentStaticProblem, component_eom_context, component_eom_sources,
     )
     from c3l.cc.eom import eom_ccsd_problem
 
-    spec = MATRIX_GREEN
-    fx = FIXTURES[spec["fixture"]]
+    spec = MATRIX_GREEN[fixture]
+    fx = FIXTURES[fixture]
     cc = build_problem(fx)
     static = ComponentStaticProblem.compile(cc)
-    amplitudes = np.load(HERE / f"{spec['fixture']}.golden.npz")["eom_amplitudes"]
-    problem = ComponentEOMProblem.compile(eom_ccsd_problem(cc, response_spin=0), static, charge=1)
+    golden = np.load(HERE / f"{fixture}.golden.npz")
+    if "eom_amplitudes" in golden.files:
+        amplitudes = golden["eom_amplitudes"]
+    else:  # compact golden: the fixed amplitudes from their formula
+        idx = np.arange(cc.num_variables, dtype=np.float64)
+        amplitudes = cc.tilde.unpack(fx["scale"] * np.cos(idx + 0.13))
+    for charge in spec["charges"]:
+        _export_matrix_charge(fixture, spec, cc, static, amplitudes, charge)
+
+
+def _export_matrix_charge(fixture, spec, cc, static, amplitudes, charge) -> None:
+    from c3l.cc.component_response import ComponentSigmaOperator, component_retarded_matrix_green_arnoldi
+    from c3l.cc.component_tensor import ComponentEOMProblem, component_eom_context, component_eom_sources
+    from c3l.cc.eom import eom_ccsd_problem
+
+    path = HERE / (f"{fixture}.matrix.npz" if charge == 1 else f"{fixture}.matrix_m.npz")
+    problem = ComponentEOMProblem.compile(eom_ccsd_problem(cc, response_spin=0), static, charge=charge)
     context = component_eom_context(problem, amplitudes)
     op = ComponentSigmaOperator(context)
     sources = [component_eom_sources(context, site=s) for s in spec["sites"]]
@@ -506,7 +530,7 @@ def export_matrix_green(path: Path) -> None:
                                                   maximum_krylov_dimension=spec["maximum_krylov_dimension"])
     seconds = time.perf_counter() - t0
     np.savez_compressed(
-        path, omega=res.omega, eta=np.float64(res.eta), sites=np.asarray(res.sites, np.int64),
+        path, charge=np.int64(charge), omega=res.omega, eta=np.float64(res.eta), sites=np.asarray(res.sites, np.int64),
         addition=res.addition, removal=res.removal, retarded=res.retarded,
         addition_relative_residuals=res.addition_relative_residuals,
         removal_relative_residuals=res.removal_relative_residuals,
@@ -599,6 +623,55 @@ def export_drivers(name: str, path: Path) -> None:
           f"time {out['time_seconds']:.1f}s matrix time {out['mtime_seconds']:.1f}s", flush=True)
 
 
+ED_CHECK = dict(fixture="readme", omega=np.linspace(-4.0, 4.0, 161), eta=0.1)
+
+
+def export_ed(path: Path) -> None:
+    """Exact Lindblad-ED G^R of the README model and the reference's CCSD-EOM
+    (S1 + S3) G^R on the same grid: the exact-diagonalisation check of the
+    reference's examples/basic/01_ccsd_eom.py (ED by its examples/siam_ed
+    sector code, no dense Liouvillian), run here once by the reference."""
+    from c3l.cc.component_response import ComponentSigmaOperator, component_retarded_green
+    from c3l.cc.component_solver import solve_component_ccsd
+    from c3l.cc.component_tensor import (
+        ComponentEOMProblem, ComponentStaticProblem, component_eom_context, component_eom_sources,
+    )
+    from c3l.cc.eom import eom_ccsd_problem
+
+    sys.path.insert(0, str(Path(sys.modules["c3l"].__file__).resolve().parents[2] / "examples"))
+    from siam_ed.physical_sparse import (
+        compile_physical_sector_operator, physical_density_action, physical_response_action,
+        physical_response_vectors, solve_trace_fixed_static,
+    )
+    from siam_ed.sparse_response import sparse_direct_resolvent
+
+    fx = FIXTURES[ED_CHECK["fixture"]]
+    omega, eta = ED_CHECK["omega"], ED_CHECK["eta"]
+    cc = build_problem(fx)
+    model = cc.model
+    static = ComponentStaticProblem.compile(cc)
+    sol = solve_component_ccsd(static)
+    problem = ComponentEOMProblem.compile(eom_ccsd_problem(cc, response_spin=0), static, charge=1)
+    context = component_eom_context(problem, sol.amplitudes)
+    op = ComponentSigmaOperator(context)
+    green = component_retarded_green(op, component_eom_sources(context), omega, eta)
+    density = compile_physical_sector_operator(physical_density_action(model), maximum_bytes=1 << 30)
+    ness = solve_trace_fixed_static(density)
+    response = compile_physical_sector_operator(physical_response_action(model, spin=0, charge=1),
+                                                maximum_bytes=1 << 30)
+    vectors = physical_response_vectors(density.action.sector, ness.coefficients,
+                                        model.orbital_index(model.impurity_site, 0))
+    sources = np.column_stack((vectors.creation_left, vectors.creation_right))
+    ed = sparse_direct_resolvent(response, sources, omega.astype(np.complex128) + 1j * eta,
+                                 verification_operator=response.action)
+    channels = ed.transfer(vectors.annihilation_sink)[:, 0, :]
+    g_ed = channels[:, 0] + channels[:, 1]
+    dev = float(np.max(np.abs(green.retarded - g_ed)) / np.max(np.abs(g_ed)))
+    np.savez_compressed(path, omega=omega, eta=np.float64(eta), green_ed=g_ed, green_cc_reference=green.retarded,
+                        cc_vs_ed_relative=np.float64(dev))
+    print(f"  ED check: CCSD-EOM vs ED max relative deviation {dev:.3e}", flush=True)
+
+
 def main() -> None:
     parser = argparse.ArgumentParser()
     parser.add_argument("--reference", default=str(HERE.parents[2] / "reference" / "src"))
@@ -608,8 +681,12 @@ def main() -> None:
     if args.names == ["warmstart"]:
         export_warmstart_family(64, HERE / "warmstart_siam.npz")
         return
-    if args.names == ["matrix"]:
-        export_matrix_green(HERE / f"{MATRIX_GREEN['fixture']}.matrix.npz")
+    if args.names and args.names[0] == "matrix":
+        for fixture in args.names[1:] or ["kanamori3x2"]:
+            export_matrix_green(fixture)
+        return
+    if args.names == ["ed"]:
+        export_ed(HERE / f"{ED_CHECK['fixture']}.ed.npz")
         return
     if args.names and args.names[0] == "spec":
         for name in args.names[1:] or list(SPEC_ONLY):

@@ -587,3 +587,23 @@ def test_response_drivers_match_reference(name, problems):
     assert relerr(pr.transfer(ref["shifts"][:4], sink), sh.addition[:4, 0, 0]) < 1e-10
     assert pr.orthogonality_defect < 1e-12
     assert pr.to_dict()["krylov_dimension"] == pr.dimension
+
+
+def test_exact_diagonalisation_check_readme(problems):
+    """The exact-diagonalisation check of the tiny README model
+    (examples/basic/01_ccsd_eom.py of the reference): the device CCSD-EOM G^R
+    matches the reference's CC values to 1e-8 and so differs from the exact
+    Lindblad ED G^R by the reference's own CCSD truncation error."""
+    import c3lindblad_gb300 as c3
+    from conftest import GOLDEN
+
+    spec, g, p = problems("readme")
+    ed = np.load(GOLDEN / "readme.ed.npz")
+    sol = c3.solve_component_ccsd(p)
+    assert sol.converged
+    ep = c3.ComponentEOMProblem.compile(c3.eom_ccsd_problem(p), p, 1)
+    ctx = c3.component_eom_context(ep, sol.amplitudes)
+    res = c3.component_retarded_green(c3.ComponentSigmaOperator(ctx), c3.component_eom_sources(ctx), ed["omega"],
+                                      float(ed["eta"]))
+    assert relerr(res.retarded, ed["green_cc_reference"]) < 1e-8
+    assert abs(relerr(res.retarded, ed["green_ed"]) - float(ed["cc_vs_ed_relative"])) <= 1e-7

@@ -5,7 +5,7 @@ from __future__ import annotations
 import numpy as np
 import pytest
 
-from conftest import eom_amplitudes, golden_names, load, relerr
+from conftest import GOLDEN as GOLDEN_DIR, eom_amplitudes, golden_names, load, relerr
 from oracle import component_oracle as oc
 
 
@@ -127,3 +127,17 @@ def test_oracle_response_drivers_match_reference(name):
         assert relerr(comb, d["mtime_retarded"]) < 1e-10
         assert relerr(add, d["mtime_addition"]) < 1e-10
         assert relerr(rem, d["mtime_removal"]) < 1e-10
+
+
+def test_oracle_green_matches_reference_on_the_ed_check_grid():
+    """The README model's G^R (eta = 0.1, 161 omega) against the reference's
+    CCSD-EOM values of its exact-diagonalisation check, and that check's own
+    CCSD-vs-ED deviation (the truncation error, 7.7e-3 relative)."""
+    spec, g = load("readme")
+    ed = np.load(GOLDEN_DIR / "readme.ed.npz")
+    p = oc.OracleProblem(spec.as_dict())
+    eom = oc.OracleEOM(p, g["solution_amplitudes"], 0, 1)
+    _, _, gr = oc.retarded_green_dense(eom, spec.impurity_site, ed["omega"], float(ed["eta"]))
+    assert relerr(gr, ed["green_cc_reference"]) < 1e-8
+    dev = relerr(gr, ed["green_ed"])
+    assert abs(dev - float(ed["cc_vs_ed_relative"])) <= 1e-7
