@@ -62,7 +62,7 @@ WORKLOADS = {
                     label="5 orbitals x 12 pseudomodes, seeded general U_abcd (n=65, 26,511,875 amplitudes, S13 dim "
                           "409,890); 10 sources (5 orbitals x 2 spins, charge +1) x 4096 omega in [-12,12], eta=0.02"),
     "config3": dict(spec="kanamori3x8", omega=(-10.0, 10.0, 2001), eta=0.02, sites=(0, 1, 2), spins=(0, 1),
-                    charges=(1, -1), scales=(0.5, 0.75, 1.0), policy=CONTINUATION_POLICY, golden="kanamori3x8",
+                    charges=(1, -1), scales=(0.5, 0.75, 1.0), policy=CONTINUATION_POLICY, golden=None,
                     similar="kanamori3x2",
                     label="3-orbital Kanamori U=2 J=0.3, 8 pseudomodes per orbital (n=27, 779,301 amplitudes, S13 dim "
                           "29,187); 6 sources (3 orbitals x 2 spins) x charge +1/-1 x 2001 omega in [-10,10], eta=0.02"),
@@ -255,9 +255,10 @@ def _timed(torch, stream, fn, flush):
 
 
 def reference_errors(pipe: Pipeline, sol, greens) -> dict:
-    """Errors against the reference's own FP64 outputs on this workload, where
-    goldens exist: the converged amplitudes and G^R (scalar goldens), or the
-    diagonal of the reference's matrix G^R at its frequencies (matrix goldens)."""
+    """Errors against the reference's own FP64 outputs on this workload where
+    the reference's solve converged (converged amplitudes and G^R at the
+    golden's frequencies).  The larger workloads are pinned at fixed
+    amplitudes by the GPU tests instead."""
     out = {}
     name = pipe.wl["golden"]
     if not name:
@@ -272,21 +273,6 @@ def reference_errors(pipe: Pipeline, sol, greens) -> dict:
             idx = [int(np.argmin(np.abs(pipe.omega - w))) for w in g["green_omega"]]
             out["green_rel_err_vs_reference"] = _rel(res.retarded[idx], g["green_retarded"])
             out["green_reference_points"] = len(idx)
-    for charge, suffix in ((1, ""), (-1, "_m")):
-        mfile = GOLDEN / f"{name}.matrix{suffix}.npz"
-        if not mfile.exists() or abs(pipe.eta - float(np.load(mfile)["eta"])) > 0:
-            continue
-        m = np.load(mfile)
-        idx = [int(np.argmin(np.abs(pipe.omega - w))) for w in m["omega"]]
-        if np.max(np.abs(pipe.omega[idx] - m["omega"])) > 1e-12:
-            continue
-        errs = []
-        for a, site in enumerate(m["sites"]):
-            key = (0, charge, int(site))
-            if key in greens:
-                errs.append(_rel(greens[key].retarded[idx], m["retarded"][:, a, a]))
-        if errs:
-            out[f"green_rel_err_vs_reference_charge{charge:+d}"] = max(errs)
     return out
 
 

@@ -81,7 +81,8 @@ TILE_DTYPE = np.dtype([("block", np.int32), ("count", np.int32), ("start", np.in
 PAIR_GROUP_DTYPE = np.dtype([("p_off", np.int64), ("kbegin", np.int64), ("kend", np.int64),
                              ("M", np.int32), ("N", np.int32)], align=True)
 PAIR_TILE_DTYPE = np.dtype([("group", np.int32), ("m0", np.int32), ("n0", np.int32), ("pad", np.int32)], align=True)
-PAIR_TILE = 64    # P entries per tile side
+PAIR_TILE = 64    # P entries per tile side (CUDA-core kernels)
+PAIR_TILE_TC = (128, 64)  # tensor-core tiles: rows (tensor-memory lanes) x columns
 
 
 def _e(g: int) -> tuple:
@@ -297,8 +298,9 @@ class PairProgram:
     groups: np.ndarray        # PAIR_GROUP_DTYPE
     aoff: np.ndarray          # int64 workspace offsets of anchor rows
     roff: np.ndarray          # int64 workspace offsets of rest rows
-    tiles: np.ndarray         # PAIR_TILE_DTYPE
+    tiles: np.ndarray         # PAIR_TILE_DTYPE (PAIR_TILE x PAIR_TILE)
     size: int                 # pair-buffer entries
+    tiles_tc: np.ndarray | None = None  # PAIR_TILE_DTYPE (PAIR_TILE_TC)
 
     @property
     def macs(self) -> int:
@@ -710,7 +712,12 @@ def compile_pairs(builder: Builder, name: str, rest_info: dict, coords: Coordina
     tarr = np.zeros(len(tiles), PAIR_TILE_DTYPE)
     for i, t in enumerate(tiles):
         tarr[i] = t
-    builder.pairs[name] = PairProgram(garr, np.asarray(aoff, np.int64), np.asarray(roff, np.int64), tarr, p)
+    tc = [(g, m0, n0, 0) for g, (b, ka, kr, rows) in enumerate(groups)
+          for m0 in range(0, int(garr[g]["M"]), PAIR_TILE_TC[0]) for n0 in range(0, int(garr[g]["N"]), PAIR_TILE_TC[1])]
+    tcarr = np.zeros(len(tc), PAIR_TILE_DTYPE)
+    for i, t in enumerate(tc):
+        tcarr[i] = t
+    builder.pairs[name] = PairProgram(garr, np.asarray(aoff, np.int64), np.asarray(roff, np.int64), tarr, p, tcarr)
     builder.pair_size = max(builder.pair_size, p)
     builder.emit_stage(f"{name}_pairs", "canonical", block_rows, elements=pos, digits=_digits(coords, pos),
                        element_block=blk)

@@ -133,6 +133,9 @@ c3l_status gm_start_f32(int64_t n, double a, const double* r, float* V0, double*
 c3l_status gm_update_f32(const float* V, int64_t ld, int k, const double* y, double* x, int64_t n, cudaStream_t s);
 
 
+// The FP32 pair GEMMs of a program on the tcgen05 tensor cores (c3l_tcgen05.cu).
+c3l_status pair_gemm_tc(const c3l_pair_program& pp, float2* ws, bool pdl, cudaStream_t s);
+
 // c3l_hessenberg_advance for several states in one launch (up to 16): the
 // rotation chains of all channels fill the GPU together.
 c3l_status hessenberg_advance_many(c3l_hessenberg_state* const* states, const c3l_complex* const* Hc,

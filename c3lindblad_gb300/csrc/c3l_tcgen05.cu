@@ -1,0 +1,292 @@
+// Pair GEMMs of the FP32 (inner-solve) JVP on the fifth-generation tensor
+// cores (tcgen05, sm_103a), split-TF32.
+//
+// A pair group computes P[i][j] = sum_k A_k[i] R_k[j] over its anchors k, with
+// complex operand rows gathered from the workspace (c3l_pair_program).  A
+// thread block owns a 128 x 64 tile of P.  Per chunk of 8 anchors its threads
+// load the operand rows (coalesced along i and j), split every real
+// component x into TF32 parts hi = tf32(x), lo = x - hi, and store them in
+// shared memory in the K-major, no-swizzle core-matrix layout the MMA reads
+// (8 rows x 16 bytes per core matrix).  One thread then issues the chunk's
+// twelve tcgen05.mma.kind::tf32 (M = 128, N = 64, K = 8) into two FP32
+// accumulators in tensor memory:
+//
+//   D_re += Ar Br - Ai Bi,   D_im += Ar Bi + Ai Br,
+//   each real product as hi hi + hi lo + lo hi (the lo lo term, 2^-22
+//   relative, is dropped), -Ai Bi by the MMA's negate-A bit,
+//
+// and commits them to the chunk's stage barrier, while the threads stage the
+// next chunk into the other buffer.  The error per product is about 2^-21
+// relative, the accuracy of the FP32 operands themselves.  The epilogue reads
+// the accumulators with tcgen05.ld (warp w owns tensor-memory lanes 32w ..
+// 32w + 31, i.e. tile rows) and writes P.
+//
+// Every wait on a barrier is bounded; a block whose wait runs out writes 1
+// to the program's status word (when given), skips the epilogue, frees its
+// tensor memory and returns.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "c3l_gb300.h"
+#include "c3l_internal.h"
+#include "c3l_pdl.h"
+
+namespace {
+
+constexpr int kTcM = 128;        // tile rows = tensor-memory lanes
+constexpr int kTcN = 64;         // tile columns per accumulator
+constexpr int kTcK = 8;          // anchors per MMA (32 bytes of TF32)
+constexpr int kTcThreads = 128;  // one warpgroup
+constexpr int kTcStages = 2;
+constexpr int kATile = kTcM * kTcK * 4;  // 4 KB: one TF32 part of the anchor tile
+constexpr int kBTile = kTcN * kTcK * 4;  // 2 KB: one TF32 part of the rest tile
+constexpr int kStageBytes = 4 * kATile + 4 * kBTile;
+constexpr int kTmemCols = 4 * kTcN;      // D_re in columns [0, 64), D_im in [64, 128); allocation 256
+constexpr int kAlign = 1024;
+constexpr int kSmemBytes = kAlign + kTcStages * kStageBytes + 64;
+constexpr uint32_t kWaitLimit = 1u << 22;  // try_wait rounds before a block gives up
+static_assert(kTcThreads == kTcM, "one thread per tile row stages the anchor tile");
+
+// Byte offset of (row r, k) in a K-major no-swizzle operand tile: core
+// matrices of 8 rows x 16 bytes (4 TF32), the next 4 k at +128 bytes (the
+// descriptor's leading-dimension offset), the next 8 rows at +256 bytes (its
+// stride offset).
+__device__ __forceinline__ uint32_t kmajor_off(int r, int k) {
+    return (uint32_t)((r >> 3) * 256 + (k >> 2) * 128 + (r & 7) * 16 + (k & 3) * 4);
+}
+
+// Shared-memory matrix descriptor: start address, leading-dimension byte
+// offset 128, stride byte offset 256 (both in 16-byte units), descriptor
+// version 1 (bits 46-47), base offset 0, no swizzle.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr) {
+    return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)(128 >> 4) << 16) | ((uint64_t)(256 >> 4) << 32) |
+           ((uint64_t)1 << 46);
+}
+
+// Instruction descriptor of tcgen05.mma.kind::tf32: D F32 (bits 4-5 = 1), A and
+// B TF32 (bits 7-9, 10-12 = 2), optional negate A (bit 13), both K-major
+// (bits 15-16 = 0), N >> 3 (bits 17-22), M >> 4 (bits 24-28).
+__host__ __device__ constexpr uint32_t idesc_tf32(bool neg_a) {
+    return (1u << 4) | (2u << 7) | (2u << 10) | ((neg_a ? 1u : 0u) << 13) | ((uint32_t)(kTcN >> 3) << 17) |
+           ((uint32_t)(kTcM >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_tf32(uint32_t dtmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(dtmem),
+        "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t mbar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
+    for (uint32_t i = 0; i < kWaitLimit; ++i) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}\n"
+            : "=r"(done)
+            : "r"(mbar), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ uint32_t tf32_hi(float x) {
+    uint32_t h;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(x));
+    return h;
+}
+
+// hi and lo TF32 parts of x (lo = x - hi is exact in FP32)
+__device__ __forceinline__ void tf32_split(float x, float& hi, float& lo) {
+    hi = __uint_as_float(tf32_hi(x));
+    lo = __fsub_rn(x, hi);
+}
+
+__device__ __forceinline__ void st_shared_v4(uint32_t addr, float a, float b, float c, float d) {
+    asm volatile("st.shared.v4.f32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "f"(a), "f"(b), "f"(c), "f"(d) : "memory");
+}
+
+// 32 lanes x 16 columns of 32 bits: this thread's lane, columns [col, col + 16)
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__global__ void __launch_bounds__(kTcThreads) k_pair_gemm_tc(c3l_pair_program pp, float2* __restrict__ ws, int pdl) {
+    extern __shared__ uint8_t dsmem[];
+    if (pdl) c3l::pdl_launch_dependents();
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const uint32_t raw = (uint32_t)__cvta_generic_to_shared(dsmem);
+    const uint32_t sbase = (raw + kAlign - 1) & ~(uint32_t)(kAlign - 1);
+    const uint32_t mbar0 = sbase + kTcStages * kStageBytes;  // two 8-byte barriers
+    const uint32_t slot = mbar0 + 16;                        // tensor-memory address
+    const c3l_pair_tile t = pp.tiles_tc[blockIdx.x];
+    const c3l_pair_group g = pp.groups[t.group];
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(slot),
+                     "r"(kTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        for (int s = 0; s < kTcStages; ++s)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar0 + 8 * s) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    uint32_t tmem;
+    asm volatile("ld.shared.b32 %0, [%1];" : "=r"(tmem) : "r"(slot) : "memory");
+    c3l::pdl_wait();
+
+    const int64_t nk = g.kend - g.kbegin;
+    const int nchunks = (int)((nk + kTcK - 1) / kTcK);
+    const bool a_ok = t.m0 + tid < g.M;
+    const int bcol = tid & (kTcN - 1), bk0 = (tid >> 6) * 4;  // rest tile: column, first of 4 anchors
+    const bool b_ok = t.n0 + bcol < g.N;
+    bool ok = true;
+    for (int c = 0; c < nchunks; ++c) {
+        const int s = c & 1;
+        const int64_t k0 = g.kbegin + (int64_t)c * kTcK;
+        // the stage's previous MMAs (chunk c - 2) must be done before it is rewritten
+        if (c >= kTcStages) ok = mbar_wait(mbar0 + 8 * s, (uint32_t)(((c - kTcStages) >> 1) & 1));
+        if (!__syncthreads_and(ok)) {
+            ok = false;
+            break;
+        }
+        const uint32_t st = sbase + s * kStageBytes;
+        // anchor tile: this thread's row, the chunk's 8 anchors
+        float ar[kTcK], ai[kTcK];
+#pragma unroll
+        for (int k = 0; k < kTcK; ++k) {
+            float2 v = make_float2(0.0f, 0.0f);
+            if (a_ok && k0 + k < g.kend) v = ws[pp.aoff[k0 + k] + t.m0 + tid];
+            ar[k] = v.x;
+            ai[k] = v.y;
+        }
+#pragma unroll
+        for (int half = 0; half < 2; ++half) {
+            float h[4], l[4], hi2[4], li[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                tf32_split(ar[4 * half + q], h[q], l[q]);
+                tf32_split(ai[4 * half + q], hi2[q], li[q]);
+            }
+            const uint32_t off = kmajor_off(tid, 4 * half);
+            st_shared_v4(st + 0 * kATile + off, h[0], h[1], h[2], h[3]);
+            st_shared_v4(st + 1 * kATile + off, l[0], l[1], l[2], l[3]);
+            st_shared_v4(st + 2 * kATile + off, hi2[0], hi2[1], hi2[2], hi2[3]);
+            st_shared_v4(st + 3 * kATile + off, li[0], li[1], li[2], li[3]);
+        }
+        // rest tile: this thread's column, 4 of the chunk's anchors
+        {
+            float h[4], l[4], hi2[4], li[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                float2 v = make_float2(0.0f, 0.0f);
+                const int64_t k = k0 + bk0 + q;
+                if (b_ok && k < g.kend) v = ws[pp.roff[k] + t.n0 + bcol];
+                tf32_split(v.x, h[q], l[q]);
+                tf32_split(v.y, hi2[q], li[q]);
+            }
+            const uint32_t off = kmajor_off(bcol, bk0);
+            const uint32_t bt = st + 4 * kATile;
+            st_shared_v4(bt + 0 * kBTile + off, h[0], h[1], h[2], h[3]);
+            st_shared_v4(bt + 1 * kBTile + off, l[0], l[1], l[2], l[3]);
+            st_shared_v4(bt + 2 * kBTile + off, hi2[0], hi2[1], hi2[2], hi2[3]);
+            st_shared_v4(bt + 3 * kBTile + off, li[0], li[1], li[2], li[3]);
+        }
+        // the generic-proxy stores become visible to the tensor cores' reads
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint64_t arh = smem_desc(st), arl = smem_desc(st + kATile), aih = smem_desc(st + 2 * kATile),
+                           ail = smem_desc(st + 3 * kATile);
+            const uint32_t bb = st + 4 * kATile;
+            const uint64_t brh = smem_desc(bb), brl = smem_desc(bb + kBTile), bih = smem_desc(bb + 2 * kBTile),
+                           bil = smem_desc(bb + 3 * kBTile);
+            const uint32_t dre = tmem, dim = tmem + kTcN;
+            const uint32_t pos = idesc_tf32(false), neg = idesc_tf32(true);
+            const uint32_t first = c > 0 ? 1u : 0u;
+            mma_tf32(dre, arh, brh, pos, first);
+            mma_tf32(dre, arh, brl, pos, 1u);
+            mma_tf32(dre, arl, brh, pos, 1u);
+            mma_tf32(dre, aih, bih, neg, 1u);
+            mma_tf32(dre, aih, bil, neg, 1u);
+            mma_tf32(dre, ail, bih, neg, 1u);
+            mma_tf32(dim, arh, bih, pos, first);
+            mma_tf32(dim, arh, bil, pos, 1u);
+            mma_tf32(dim, arl, bih, pos, 1u);
+            mma_tf32(dim, aih, brh, pos, 1u);
+            mma_tf32(dim, aih, brl, pos, 1u);
+            mma_tf32(dim, ail, brh, pos, 1u);
+            mma_commit(mbar0 + 8 * s);
+        }
+    }
+    // the last chunk's commit covers every MMA issued before it
+    if (ok && nchunks > 0) ok = mbar_wait(mbar0 + 8 * ((nchunks - 1) & 1), (uint32_t)(((nchunks - 1) >> 1) & 1));
+    ok = __syncthreads_and(ok);
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (ok && nchunks > 0) {
+        const int row = warp * 32 + lane;
+        const int m = t.m0 + row;
+        float2* __restrict__ P = ws + pp.base + g.p_off;
+#pragma unroll 1
+        for (int c0 = 0; c0 < kTcN; c0 += 16) {
+            float re[16], im[16];
+            const uint32_t lanes = (uint32_t)(warp * 32) << 16;
+            tmem_ld16(tmem + lanes + c0, re);
+            tmem_ld16(tmem + lanes + kTcN + c0, im);
+            if (m < g.M) {
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    const int nn = t.n0 + c0 + j;
+                    if (nn < g.N) P[(int64_t)m * g.N + nn] = make_float2(re[j], im[j]);
+                }
+            }
+        }
+    } else if (!ok && tid == 0 && pp.status) {
+        atomicExch(pp.status, 1);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
+}
+
+}  // namespace
+
+namespace c3l {
+
+c3l_status pair_gemm_tc(const c3l_pair_program& pp, float2* ws, bool pdl, cudaStream_t s) {
+    if (pp.ntiles_tc <= 0) return C3L_OK;
+    if (!pp.groups || !pp.aoff || !pp.roff || !pp.tiles_tc || pp.base < 0 || !ws) return C3L_ERR_ARGUMENT;
+    static bool configured = false;
+    if (!configured) {
+        if (cudaFuncSetAttribute(k_pair_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes) !=
+            cudaSuccess)
+            return C3L_ERR_LAUNCH;
+        configured = true;
+    }
+    return launch_pdl(k_pair_gemm_tc, dim3((unsigned)pp.ntiles_tc), dim3(kTcThreads), (size_t)kSmemBytes, s, 0, pdl,
+                      pp, ws, pdl ? 1 : 0);
+}
+
+}  // namespace c3l

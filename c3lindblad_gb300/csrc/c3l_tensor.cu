@@ -535,6 +535,12 @@ c3l_status run_pairs(const c3l_pair_program& pp, const Batch<C>& bt, cudaStream_
     if (pp.ntiles <= 0) return C3L_OK;
     if (!pp.groups || !pp.aoff || !pp.roff || !pp.tiles || pp.base < 0) return C3L_ERR_ARGUMENT;
     const dim3 grid((unsigned)pp.ntiles, (unsigned)bt.nb);
+    if constexpr (std::is_same<C, float2>::value) {
+        if (pp.kernel == C3L_PAIR_TCGEN05 && pp.ntiles_tc > 0) {
+            if (bt.nb != 1) return C3L_ERR_ARGUMENT;
+            return c3l::pair_gemm_tc(pp, bt.ws[0], bt.pdl, s);
+        }
+    }
     if constexpr (std::is_same<C, double2>::value) {
         if (!fp64_pipe)
             return c3l::launch_pdl(k_pair_gemm_df, grid, dim3(kPairThreads), 0, s, 0, bt.pdl, pp, bt);
@@ -998,6 +1004,11 @@ c3l_status c3l_pair_gemm(const c3l_pair_program* program, c3l_complex* ws, void*
 c3l_status c3l_pair_gemm_df(const c3l_pair_program* program, c3l_complex* ws, void* stream) {
     if (!program || !ws) return C3L_ERR_ARGUMENT;
     return run_pairs<double2>(*program, single<double2>(reinterpret_cast<double2*>(ws)), as_stream(stream));
+}
+
+c3l_status c3l_pair_gemm_tc(const c3l_pair_program* program, c3l_complex32* ws, void* stream) {
+    if (!program || !ws) return C3L_ERR_ARGUMENT;
+    return c3l::pair_gemm_tc(*program, reinterpret_cast<float2*>(ws), false, as_stream(stream));
 }
 
 c3l_status c3l_pair_gemm_f32(const c3l_pair_program* program, c3l_complex32* ws, void* stream) {

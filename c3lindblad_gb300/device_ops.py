@@ -9,12 +9,19 @@ sequence of one action through a single C-ABI call
 from __future__ import annotations
 
 import ctypes as C
+import os
 
 import numpy as np
 import torch
 
 from . import runtime as rt
 from .plans import EOMPlan, SourcePlan, StaticPlan
+
+
+def pair_kernel() -> int:
+    """The kernel of the FP32 JVP's pair GEMMs: C3L_PAIR_KERNEL=tcgen05 selects
+    the tensor-core kernel, anything else the CUDA-core kernel."""
+    return rt.PAIR_TCGEN05 if os.environ.get("C3L_PAIR_KERNEL", "simt") == "tcgen05" else rt.PAIR_SIMT
 
 
 def _cz(n: int, device) -> torch.Tensor:
@@ -65,9 +72,12 @@ class DeviceStatic:
             self.canon_R = _cz(self.A, self.device)
             self.canon_V = _cz(self.A, self.device)
 
-            def static_action(ws, levels_cls, padded, out, scatter, canon, ep, vectors=vec, pairs=None):
+            self.pair_status = torch.zeros(1, dtype=torch.int32, device=self.device)
+
+            def static_action(ws, levels_cls, padded, out, scatter, canon, ep, vectors=vec, pairs=None, kernel=0):
                 sa = rt.StaticAction()
-                sa.action = rt.build_action(up, prog, vectors.data_ptr(), ws, levels_cls, padded, out, scatter, pairs)
+                sa.action = rt.build_action(up, prog, vectors.data_ptr(), ws, levels_cls, padded, out, scatter, pairs,
+                                            kernel, self.pair_status.data_ptr())
                 sa.num_amplitudes = self.A
                 sa.tilde_ia, sa.tilde_ib = ia.data_ptr(), ib.data_ptr()
                 sa.tilde_ca, sa.tilde_cb = ca.data_ptr(), cb.data_ptr()
@@ -95,9 +105,11 @@ class DeviceStatic:
             self.ws32_lin = torch.zeros(max(prog.ws_size + prog.pair_size, 1), dtype=torch.complex64,
                                         device=self.device)
             pairs = "jvp" if "jvp" in prog.pairs else None
+            self.pair_kernel = pair_kernel()
             self.jvp32_action = static_action(self.ws32_lin, "V", ["jvp_rest_V", "jvp_scalar"],
                                               "jvp_pairs" if pairs else "jvp", plan.scatter_V, self.canon_V,
-                                              plan.epilogue_jvp, vectors=self.vec32, pairs=pairs)
+                                              plan.epilogue_jvp, vectors=self.vec32, pairs=pairs,
+                                              kernel=self.pair_kernel)
             # complex outputs at every coordinate (arbitrary complex amplitudes)
             self.cres_action = rt.build_action(up, prog, vec.data_ptr(), self.ws_res, "T", ["res_rest_T", "res_scalar"],
                                                None, plan.scatter_T)
@@ -170,6 +182,12 @@ class DeviceStatic:
         rt.check(self.lib.c3l_static_apply_f32(C.byref(self.jvp32_action), v.data_ptr(), out.data_ptr(),
                                                self._stream()), "static JVP (fp32)")
         rt.LaunchCounter.add(self.launches["jvp32"])
+
+    def check_device_status(self) -> None:
+        """Raise if a tensor-core pair GEMM block gave up waiting for its MMAs."""
+        if int(self.pair_status.item()) != 0:
+            self.pair_status.zero_()
+            raise rt.C3LError("a tensor-core pair GEMM timed out waiting for its MMAs")
 
     def precondition(self, x: torch.Tensor, out: torch.Tensor) -> None:
         rt.check(self.lib.c3l_precondition(self.nrep, self.pc_m4.data_ptr(), self.pc_col.data_ptr(),

@@ -30,7 +30,11 @@ class ContractLevel(C.Structure):
 
 class PairProgram(C.Structure):
     _fields_ = [("groups", C.c_void_p), ("aoff", C.c_void_p), ("roff", C.c_void_p), ("tiles", C.c_void_p),
-                ("ntiles", C.c_int64), ("base", C.c_int64)]
+                ("ntiles", C.c_int64), ("base", C.c_int64), ("tiles_tc", C.c_void_p), ("ntiles_tc", C.c_int64),
+                ("status", C.c_void_p), ("kernel", C.c_int32), ("pad", C.c_int32)]
+
+
+PAIR_SIMT, PAIR_TCGEN05 = 0, 1
 
 
 class WedgeStage(C.Structure):
@@ -117,7 +121,7 @@ EXPORTS = (
     "c3l_scale_c", "c3l_scale_r", "c3l_precondition", "c3l_hessenberg_shifted", "c3l_hessenberg_coordinates",
     "c3l_hessenberg_coordinates_noalloc", "c3l_gmres", "c3l_gmres_scratch", "c3l_gmres_release", "c3l_gmres_shifted", "c3l_shifted_combine", "c3l_arnoldi", "c3l_hessenberg_advance",
     "c3l_arnoldi_column", "c3l_static_apply_f32", "c3l_eom_sigma_f32", "c3l_action_prepare_f32", "c3l_downcast",
-    "c3l_wedge_static_out_f32", "c3l_pair_gemm", "c3l_pair_gemm_df", "c3l_pair_gemm_f32", "c3l_mlp_forward", "c3l_mlp_backward", "c3l_mlp_adam", "c3l_warm_features", "c3l_warm_apply", "c3l_version",
+    "c3l_wedge_static_out_f32", "c3l_pair_gemm", "c3l_pair_gemm_df", "c3l_pair_gemm_f32", "c3l_pair_gemm_tc", "c3l_mlp_forward", "c3l_mlp_backward", "c3l_mlp_adam", "c3l_warm_features", "c3l_warm_apply", "c3l_version",
 )
 
 
@@ -155,6 +159,7 @@ def _declare(lib) -> None:
         "c3l_downcast": [I64, P, P, P],
         "c3l_pair_gemm": [P, P, P],
         "c3l_pair_gemm_df": [P, P, P],
+        "c3l_pair_gemm_tc": [P, P, P],
         "c3l_pair_gemm_f32": [P, P, P],
         "c3l_mlp_forward": [I64, P, P, P, P],
         "c3l_mlp_backward": [I64, P, P, P, C.c_float, P, P, P, P],
@@ -346,8 +351,9 @@ def wedge_stage(up: Uploader, stage) -> WedgeStage:
     return st
 
 
-def pair_program(up: Uploader, program, name: str | None) -> PairProgram:
-    """The pair GEMMs feeding stage ``<name>_pairs`` (none when ``name`` is None)."""
+def pair_program(up: Uploader, program, name: str | None, kernel: int = PAIR_SIMT, status: int = 0) -> PairProgram:
+    """The pair GEMMs feeding stage ``<name>_pairs`` (none when ``name`` is None);
+    ``kernel`` PAIR_TCGEN05 runs an FP32 workspace's GEMMs on the tensor cores."""
     pp = PairProgram()
     pairs = program.pairs.get(name) if name else None
     if pairs is None or pairs.tiles.size == 0:
@@ -359,11 +365,17 @@ def pair_program(up: Uploader, program, name: str | None) -> PairProgram:
     pp.tiles = up.ptr(pairs.tiles)
     pp.ntiles = pairs.tiles.size
     pp.base = program.ws_size
+    if pairs.tiles_tc is not None and pairs.tiles_tc.size:
+        pp.tiles_tc = up.ptr(pairs.tiles_tc)
+        pp.ntiles_tc = pairs.tiles_tc.size
+    pp.kernel = int(kernel)
+    pp.status = int(status)
     return pp
 
 
 def build_action(up: Uploader, program, vectors_ptr: int, ws: torch.Tensor, levels_cls: str | None,
-                 padded_names: list, out_name: str | None, scatter, pairs: str | None = None) -> Action:
+                 padded_names: list, out_name: str | None, scatter, pairs: str | None = None,
+                 pair_kernel: int = PAIR_SIMT, pair_status: int = 0) -> Action:
     """``pairs``: run the pair GEMMs of that stage before the output stage
     (``ws`` then holds the workspace followed by the pair buffer)."""
     if pairs is not None and ws.numel() < program.ws_size + program.pair_size:
@@ -393,7 +405,7 @@ def build_action(up: Uploader, program, vectors_ptr: int, ws: torch.Tensor, leve
     for i, s in enumerate(stages):
         a.padded[i] = wedge_stage(up, s)
     a.out = wedge_stage(up, program.stages.get(out_name) if out_name else None)
-    a.pairs = pair_program(up, program, pairs)
+    a.pairs = pair_program(up, program, pairs, pair_kernel, pair_status)
     a.vectors = vectors_ptr
     a.ws = ws.data_ptr()
     if scatter is not None:

@@ -413,6 +413,8 @@ def _solve(p, ops, controls, initial_amplitudes, accepted_step_callback, warm_st
                                                     maxiter=controls.gmres_maximum_restart_cycles, single=mixed,
                                                     basis_f32=mixed)
         jvp_count[0] += gm_matvecs
+        if mixed:
+            ops.check_device_status()
         matvec(step, jstep)
         # linear defect J s + r, merit slope r . J s, step norm
         vec.dots_r(r, 1, jstep, scal[0:1])

@@ -118,6 +118,12 @@ typedef struct {
     int32_t pad;
 } c3l_pair_tile;
 
+/* kernel: C3L_PAIR_SIMT runs the CUDA-core kernels over `tiles` (64 x 64);
+ * C3L_PAIR_TCGEN05 runs FP32 workspaces on the tensor cores over `tiles_tc`
+ * (128 x 64, split-TF32, c3l_pair_gemm_tc); status (optional) receives 1 if
+ * a tensor-core block gave up waiting for its MMAs. */
+#define C3L_PAIR_SIMT 0
+#define C3L_PAIR_TCGEN05 1
 typedef struct {
     const c3l_pair_group* groups;
     const int64_t* aoff;
@@ -125,6 +131,11 @@ typedef struct {
     const c3l_pair_tile* tiles;
     int64_t ntiles;
     int64_t base;             /* pair_base: P entries are ws[base + p_off + ...] */
+    const c3l_pair_tile* tiles_tc;
+    int64_t ntiles_tc;
+    int32_t* status;
+    int32_t kernel;
+    int32_t pad;
 } c3l_pair_program;
 
 /* ------------------------------------------------------------ primitives */
@@ -176,6 +187,10 @@ c3l_status c3l_wedge_eom_out(const c3l_wedge_stage* stage, int32_t n, const c3l_
 c3l_status c3l_pair_gemm(const c3l_pair_program* program, c3l_complex* ws, void* stream);
 c3l_status c3l_pair_gemm_df(const c3l_pair_program* program, c3l_complex* ws, void* stream);
 c3l_status c3l_pair_gemm_f32(const c3l_pair_program* program, c3l_complex32* ws, void* stream);
+/* The FP32 pair GEMMs on the tcgen05 tensor cores (split-TF32: three TF32 MMAs
+ * per real product, FP32 accumulation in tensor memory; about 5e-7 relative
+ * per product), over program->tiles_tc. */
+c3l_status c3l_pair_gemm_tc(const c3l_pair_program* program, c3l_complex32* ws, void* stream);
 
 /* EOM sources: out[mu] = scale * V  (src/c3l/cc/component_tensor.py:2788-2798). */
 c3l_status c3l_wedge_source_out(const c3l_wedge_stage* stage, int32_t n, const c3l_complex* ws,

@@ -243,6 +243,34 @@ def test_matrix_green_arnoldi_matches_reference(problems):
         c3.component_retarded_matrix_green_arnoldi(op, [sources[0], sources[0]], ref["omega"], 0.1)
 
 
+@pytest.mark.parametrize("suffix,charge", [("", 1), ("_m", -1)])
+def test_matrix_green_arnoldi_large_fixture(suffix, charge, problems):
+    """n = 27 Kanamori (the three-orbital, eight-mode model; EOM dimension
+    29,187), eta = 0.02: the device matrix response against the reference's
+    one-sided matrix Arnoldi driver at the fixture's fixed amplitudes, both
+    charges."""
+    import c3lindblad_gb300 as c3
+    from conftest import GOLDEN
+
+    path = GOLDEN / f"kanamori3x8.matrix{suffix}.npz"
+    if not path.exists():
+        pytest.skip("matrix golden not generated")
+    ref = np.load(path)
+    spec, g, p = problems("kanamori3x8")
+    T, _ = _fixed_inputs(p.plan, float(g["scale"]))
+    ep = c3.ComponentEOMProblem.compile(c3.eom_ccsd_problem(p), p, charge)
+    ctx = c3.component_eom_context(ep, T)
+    op = c3.ComponentSigmaOperator(ctx)
+    sources = [c3.component_eom_sources(ctx, site=int(s)) for s in ref["sites"]]
+    res = c3.component_retarded_matrix_green_arnoldi(
+        op, sources, ref["omega"], float(ref["eta"]), maximum_krylov_dimension=int(ref["maximum_krylov_dimension"]))
+    assert relerr(res.addition, ref["addition"]) < 1e-8
+    assert relerr(res.removal, ref["removal"]) < 1e-8
+    assert relerr(res.retarded, ref["retarded"]) < 1e-8
+    assert np.max(res.addition_relative_residuals) <= 1e-10
+    assert np.max(res.removal_relative_residuals) <= 1e-10
+
+
 def test_krylov_primitives_against_numpy(cuda_device):
     from c3lindblad_gb300.krylov import DeviceVectors, hessenberg_shifted
 
@@ -411,10 +439,16 @@ def test_mixed_precision_solve_meets_fp64_tolerance(name, problems):
     assert relerr(sol.amplitudes, g["solution_amplitudes"]) < 1e-8
 
 
+@pytest.mark.parametrize("kernel", ["simt", "tcgen05"])
 @pytest.mark.parametrize("name", golden_names())
-def test_single_precision_jvp_tracks_fp64(name, problems, cuda_device):
-    """The FP32 JVP (its output stage summed by the pair GEMMs) against the FP64 one."""
-    spec, g, p = problems(name)
+def test_single_precision_jvp_tracks_fp64(name, kernel, cuda_device, monkeypatch):
+    """The FP32 JVP (its output stage summed by the pair GEMMs, on the CUDA
+    cores or the tcgen05 tensor cores) against the FP64 one."""
+    import c3lindblad_gb300 as c3
+
+    monkeypatch.setenv("C3L_PAIR_KERNEL", kernel)
+    spec, g = load(name)
+    p = c3.ComponentStaticProblem.compile(spec, device=cuda_device)
     ops = p.ops
     x = torch.from_numpy(g["fixed_variables"]).to(cuda_device)
     d = torch.from_numpy(g["fixed_direction_variables"]).to(cuda_device)
@@ -425,6 +459,7 @@ def test_single_precision_jvp_tracks_fp64(name, problems, cuda_device):
     j32 = torch.empty_like(x)
     ops.jvp(d, j64)
     ops.jvp32(d, j32)
+    ops.check_device_status()
     err = relerr(j32.cpu().numpy(), j64.cpu().numpy())
     assert 0 < err < 1e-5
 

@@ -1,4 +1,4 @@
-"""The pair-GEMM kernels (``c3l_pair_gemm`` / ``_df`` / ``_f32``) against NumPy.
+"""The pair-GEMM kernels (``c3l_pair_gemm`` / ``_df`` / ``_f32`` / ``_tc``) against NumPy.
 
 Each group multiplies K gathered operand rows: P[i, j] = sum_k A_k[i] R_k[j]
 with A_k = ws[aoff[k] : aoff[k] + M] and R_k = ws[roff[k] : roff[k] + N].  The
@@ -25,7 +25,7 @@ SHAPES = [(1, 1, 1), (3, 7, 2), (64, 64, 8), (65, 65, 9), (130, 17, 23), (1, 300
 
 def _program(rng, ws_size: int):
     groups = np.zeros(len(SHAPES), compiler.PAIR_GROUP_DTYPE)
-    aoff, roff, tiles = [], [], []
+    aoff, roff, tiles, tiles_tc = [], [], [], []
     p = 0
     for g, (M, N, K) in enumerate(SHAPES):
         groups[g] = (p, len(aoff), len(aoff) + K, M, N)
@@ -34,11 +34,18 @@ def _program(rng, ws_size: int):
         for m0 in range(0, M, compiler.PAIR_TILE):
             for n0 in range(0, N, compiler.PAIR_TILE):
                 tiles.append((g, m0, n0, 0))
+        for m0 in range(0, M, compiler.PAIR_TILE_TC[0]):
+            for n0 in range(0, N, compiler.PAIR_TILE_TC[1]):
+                tiles_tc.append((g, m0, n0, 0))
         p += M * N
-    t = np.zeros(len(tiles), compiler.PAIR_TILE_DTYPE)
-    for i, row in enumerate(tiles):
-        t[i] = row
-    return groups, np.asarray(aoff, np.int64), np.asarray(roff, np.int64), t, p
+
+    def table(rows):
+        t = np.zeros(len(rows), compiler.PAIR_TILE_DTYPE)
+        for i, row in enumerate(rows):
+            t[i] = row
+        return t
+
+    return groups, np.asarray(aoff, np.int64), np.asarray(roff, np.int64), table(tiles), table(tiles_tc), p
 
 
 def _expected(ws, groups, aoff, roff):
@@ -51,34 +58,40 @@ def _expected(ws, groups, aoff, roff):
     return np.concatenate(out)
 
 
-@pytest.mark.parametrize("dtype", ["f64", "df", "f32"])
+@pytest.mark.parametrize("dtype", ["f64", "df", "f32", "tc"])
 def test_pair_gemm_matches_numpy(dtype, cuda_device):
     from c3lindblad_gb300 import runtime as rt
 
     lib = rt.lib()
     rng = np.random.default_rng(7)
     ws_size = 20000
-    groups, aoff, roff, tiles, psize = _program(rng, ws_size)
+    groups, aoff, roff, tiles, tiles_tc, psize = _program(rng, ws_size)
     ws = rng.normal(size=ws_size) + 1j * rng.normal(size=ws_size)
     want = _expected(ws, groups, aoff, roff)
-    cdt = torch.complex64 if dtype == "f32" else torch.complex128
+    cdt = torch.complex64 if dtype in ("f32", "tc") else torch.complex128
     buf = torch.full((ws_size + psize,), complex("nan"), dtype=cdt, device=cuda_device)
     buf[:ws_size] = torch.from_numpy(ws).to(cuda_device, cdt)
-    keep = [torch.from_numpy(a.view(np.uint8).copy()).to(cuda_device) for a in (groups, aoff, roff, tiles)]
+    keep = [torch.from_numpy(a.view(np.uint8).copy()).to(cuda_device) for a in (groups, aoff, roff, tiles, tiles_tc)]
+    status = torch.zeros(1, dtype=torch.int32, device=cuda_device)
     pp = rt.PairProgram()
-    pp.groups, pp.aoff, pp.roff, pp.tiles = (k.data_ptr() for k in keep)
+    pp.groups, pp.aoff, pp.roff, pp.tiles, pp.tiles_tc = (k.data_ptr() for k in keep)
     pp.ntiles = tiles.size
+    pp.ntiles_tc = tiles_tc.size
     pp.base = ws_size
-    fn = {"f64": lib.c3l_pair_gemm, "df": lib.c3l_pair_gemm_df, "f32": lib.c3l_pair_gemm_f32}[dtype]
+    pp.status = status.data_ptr()
+    fn = {"f64": lib.c3l_pair_gemm, "df": lib.c3l_pair_gemm_df, "f32": lib.c3l_pair_gemm_f32,
+          "tc": lib.c3l_pair_gemm_tc}[dtype]
     assert fn(C.byref(pp), buf.data_ptr(), torch.cuda.current_stream(cuda_device).cuda_stream) == 0
     torch.cuda.synchronize(cuda_device)
     got = buf[ws_size:].cpu().numpy().astype(np.complex128)
     assert np.all(np.isfinite(got))  # every P entry written
     # per-entry bound: |error| <= c eps sum_k |A_k[i]| |R_k[j]|
-    # FP64: reassociation only; double-float: products to 2^-46 and TwoSum sums
-    tol = {"f64": 1e-13, "df": 1e-12, "f32": 3e-6}[dtype]
+    assert int(status.item()) == 0
+    # FP64: reassociation only; double-float: products to 2^-46 and TwoSum sums;
+    # FP32 and split-TF32 (three TF32 MMAs per real product): about 2^-21 per product
+    tol = {"f64": 1e-13, "df": 1e-12, "f32": 3e-6, "tc": 3e-6}[dtype]
     scale = _expected(np.abs(ws), groups, aoff, roff).real
     assert np.all(np.abs(got - want) <= tol * scale)
     # the workspace itself is untouched
     assert np.array_equal(buf[:ws_size].cpu().numpy().astype(np.complex128),
-                          ws if dtype != "f32" else ws.astype(np.complex64).astype(np.complex128))
+                          ws if dtype not in ("f32", "tc") else ws.astype(np.complex64).astype(np.complex128))
