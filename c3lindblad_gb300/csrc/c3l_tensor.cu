@@ -686,7 +686,8 @@ __global__ void __launch_bounds__(kThreads) k_wedge(c3l_wedge_stage st, int n, B
             if (epair) ep.xout[c + 1] = r.y;
         }
     } else if (MODE == kEom) {
-        const double2 a = to_d2(acc);
+        const double2 a0 = to_d2(acc);
+        const double2 a = make_double2(ep.iscale * a0.x, ep.iscale * a0.y);
         const double2 lam = elam, src = esrc;
         const double2 o =
             make_double2(fma(lam.x, src.x, fma(-lam.y, src.y, a.x)), fma(lam.x, src.y, fma(lam.y, src.x, a.y)));
@@ -867,7 +868,10 @@ c3l_status eom_sigma(const c3l_eom_action* ea, int nb, const c3l_complex* const*
     bt.pdl_at_exit = true;
     for (int b = 0; b < nb; ++b) {
         if (!xin[b] || !out[b] || !valid_action(&ea[b].action) || !ea[b].lam) return C3L_ERR_ARGUMENT;
-        if (b > 0 && (!same_program(ea[b].action, ea[0].action) || ea[b].lam != ea[0].lam)) return C3L_ERR_ARGUMENT;
+        if (b > 0 && (!same_program(ea[b].action, ea[0].action) || ea[b].lam != ea[0].lam ||
+                      ea[b].interaction_scale != ea[0].interaction_scale))
+            return C3L_ERR_ARGUMENT;
+        if (!(ea[b].interaction_scale >= 0.0 && ea[b].interaction_scale <= 1.0)) return C3L_ERR_ARGUMENT;
         bt.ws[b] = reinterpret_cast<C*>(ea[b].action.ws);
         bt.in[b] = reinterpret_cast<const double2*>(xin[b]);
         bt.out[b] = reinterpret_cast<double2*>(out[b]);
@@ -882,6 +886,7 @@ c3l_status eom_sigma(const c3l_eom_action* ea, int nb, const c3l_complex* const*
     if (ea[0].action.out.ntiles <= 0) return C3L_OK;
     Epilogue ep{};
     ep.lam = reinterpret_cast<const double2*>(ea[0].lam);
+    ep.iscale = ea[0].interaction_scale;
     return launch_wedge<kEom, C>(ea[0].action.out, ea[0].action.n, bt, ep, s);
 }
 
@@ -896,7 +901,7 @@ c3l_status eom_sigma_batch(const c3l_eom_action* actions, int nb, const c3l_comp
 }
 
 bool same_sigma_program(const c3l_eom_action& a, const c3l_eom_action& b) {
-    return same_program(a.action, b.action) && a.lam == b.lam;
+    return same_program(a.action, b.action) && a.lam == b.lam && a.interaction_scale == b.interaction_scale;
 }
 
 }  // namespace c3l
@@ -989,6 +994,7 @@ c3l_status c3l_wedge_eom_out(const c3l_wedge_stage* stage, int32_t n, const c3l_
     if (stage->ntiles <= 0) return C3L_OK;
     Epilogue ep{};
     ep.lam = reinterpret_cast<const double2*>(lam);
+    ep.iscale = 1.0;
     return launch_wedge<kEom, double2>(*stage, n,
                                        single<double2>(const_cast<double2*>(reinterpret_cast<const double2*>(ws)),
                                                        reinterpret_cast<const double2*>(xin),

@@ -18,10 +18,22 @@ from . import runtime as rt
 from .plans import EOMPlan, SourcePlan, StaticPlan
 
 
+PAIR_KERNELS = {"simt": rt.PAIR_SIMT, "tcgen05": rt.PAIR_TCGEN05}
+# the kernel used before (or without) tuning
+PAIR_KERNEL_DEFAULT = "simt"
+
+
+def pair_kernel_setting() -> str:
+    """C3L_PAIR_KERNEL: 'simt' or 'tcgen05' forces the FP32 JVP's pair-GEMM
+    kernel; 'auto' lets the first mixed-precision solve time both and keep the
+    faster (``DeviceStatic.tune_pair_kernel``)."""
+    v = os.environ.get("C3L_PAIR_KERNEL", PAIR_KERNEL_DEFAULT)
+    return v if v in ("simt", "tcgen05", "auto") else PAIR_KERNEL_DEFAULT
+
+
 def pair_kernel() -> int:
-    """The kernel of the FP32 JVP's pair GEMMs: C3L_PAIR_KERNEL=tcgen05 selects
-    the tensor-core kernel, anything else the CUDA-core kernel."""
-    return rt.PAIR_TCGEN05 if os.environ.get("C3L_PAIR_KERNEL", "simt") == "tcgen05" else rt.PAIR_SIMT
+    v = pair_kernel_setting()
+    return PAIR_KERNELS[PAIR_KERNEL_DEFAULT if v == "auto" else v]
 
 
 def _cz(n: int, device) -> torch.Tensor:
@@ -106,6 +118,7 @@ class DeviceStatic:
                                         device=self.device)
             pairs = "jvp" if "jvp" in prog.pairs else None
             self.pair_kernel = pair_kernel()
+            self.pair_tuning = None  # {kernel: ms} once tuned
             self.jvp32_action = static_action(self.ws32_lin, "V", ["jvp_rest_V", "jvp_scalar"],
                                               "jvp_pairs" if pairs else "jvp", plan.scatter_V, self.canon_V,
                                               plan.epilogue_jvp, vectors=self.vec32, pairs=pairs,
@@ -183,6 +196,41 @@ class DeviceStatic:
                                                self._stream()), "static JVP (fp32)")
         rt.LaunchCounter.add(self.launches["jvp32"])
 
+    @property
+    def pair_kernel_name(self) -> str:
+        return {v: k for k, v in PAIR_KERNELS.items()}[int(self.jvp32_action.action.pairs.kernel)]
+
+    def tune_pair_kernel(self, reps: int = 3) -> dict:
+        """Project autotuner of the FP32 JVP's contraction tiles: times the JVP
+        (after ``to_single``) with each pair-GEMM kernel -- CUDA cores on 64 x 64
+        tiles, tcgen05 tensor cores on 128 x 64 tiles -- and keeps the faster.
+        Returns {kernel: milliseconds}.  Both kernels sum in FP32 (the
+        tensor-core one in split TF32), so the choice does not move the JVP
+        beyond FP32 rounding."""
+        if self.jvp32_action.action.pairs.ntiles <= 0:
+            return {}
+        times = {}
+        v = torch.zeros(self.D, dtype=torch.float64, device=self.device)
+        v[:: max(self.D // 97, 1)] = 1.0
+        out = torch.empty_like(v)
+        for name, k in PAIR_KERNELS.items():
+            self.jvp32_action.action.pairs.kernel = k
+            self.jvp32(v, out)  # first launch: function attributes, caches
+            torch.cuda.synchronize(self.device)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(reps):
+                self.jvp32(v, out)
+            e1.record()
+            torch.cuda.synchronize(self.device)
+            self.check_device_status()
+            times[name] = e0.elapsed_time(e1) / reps
+        best = min(times, key=times.get)
+        self.jvp32_action.action.pairs.kernel = PAIR_KERNELS[best]
+        self.pair_tuning = times
+        return times
+
     def check_device_status(self) -> None:
         """Raise if a tensor-core pair GEMM block gave up waiting for its MMAs."""
         if int(self.pair_status.item()) != 0:
@@ -233,9 +281,15 @@ class DeviceStatic:
 class DeviceEOM:
     """Sigma action of one (spin, charge) EOM block at fixed amplitudes."""
 
-    def __init__(self, plan: EOMPlan, amplitudes: torch.Tensor, device=None, tables: dict | None = None):
+    def __init__(self, plan: EOMPlan, amplitudes: torch.Tensor, device=None, tables: dict | None = None,
+                 interaction_scale: float = 1.0):
         """``tables``: a dict (device -> Uploader) owned by the EOM problem, so that
-        contexts of one problem share its uploaded program tables."""
+        contexts of one problem share its uploaded program tables.
+        ``interaction_scale``: the product part's factor (the homotopy model
+        the amplitudes were solved at)."""
+        if not 0.0 <= float(interaction_scale) <= 1.0:
+            raise ValueError("interaction scale must lie in [0, 1]")
+        self.interaction_scale = float(interaction_scale)
         self.device = rt.require_cuda(device)
         self.lib = rt.lib()
         self.plan = plan
@@ -289,6 +343,7 @@ class DeviceEOM:
                 ea.action = rt.build_action(up, prog, self.vec.data_ptr(), ws, "X", ["sigma_rest_X"],
                                             "sigma_pairs" if pairs else "sigma", self.plan.scatter_X, pairs)
                 ea.lam = self.lam.data_ptr()
+                ea.interaction_scale = self.interaction_scale
                 built.append((ws, ctx, ea))
         for ws, ctx, ea in built:
             rt.check(self.lib.c3l_action_prepare(C.byref(ctx), self.amplitudes.data_ptr(), rt.stream_ptr(self.device)),

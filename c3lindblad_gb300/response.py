@@ -84,7 +84,10 @@ class ComponentEOMProblem:
 class ComponentEOMContext:
     """Sigma action at fixed amplitudes (device workspace prepared once)."""
 
-    def __init__(self, problem: ComponentEOMProblem, amplitudes):
+    def __init__(self, problem: ComponentEOMProblem, amplitudes, *, interaction_scale: float = 1.0):
+        """``interaction_scale``: the homotopy scale the amplitudes solve
+        (``solve_component_ccsd(..., interaction_scale=s)``); the sigma
+        action's product part is scaled by it."""
         from .device_ops import DeviceEOM
         self.problem = problem
         st = problem.static
@@ -95,15 +98,15 @@ class ComponentEOMContext:
             if arr.shape != (st.num_amplitudes,) or not np.all(np.isfinite(arr)):
                 raise ValueError("component vector has the wrong shape or is nonfinite")
             t = torch.from_numpy(arr.copy())
-        self.ops = DeviceEOM(problem.plan, t, st._device, tables=problem._tables)
+        self.ops = DeviceEOM(problem.plan, t, st._device, tables=problem._tables, interaction_scale=interaction_scale)
         self.amplitudes = self.ops.amplitudes
 
 
-def component_eom_context(problem, amplitudes) -> ComponentEOMContext:
+def component_eom_context(problem, amplitudes, *, interaction_scale: float = 1.0) -> ComponentEOMContext:
     if _is_reference_object(problem):
         static = ComponentStaticProblem.compile(problem.static)
         problem = ComponentEOMProblem(static, problem.oracle.response_spin, problem.charge)
-    return ComponentEOMContext(problem, amplitudes)
+    return ComponentEOMContext(problem, amplitudes, interaction_scale=interaction_scale)
 
 
 @dataclass

@@ -59,7 +59,7 @@ class StaticAction(C.Structure):
 
 
 class EomAction(C.Structure):
-    _fields_ = [("action", Action), ("lam", C.c_void_p)]
+    _fields_ = [("action", Action), ("lam", C.c_void_p), ("interaction_scale", C.c_double)]
 
 
 class Complex(C.Structure):

@@ -9,6 +9,7 @@ Drop-in counterparts of the reference's
 
 from __future__ import annotations
 
+import dataclasses
 import resource
 import time
 from dataclasses import dataclass, field
@@ -149,6 +150,8 @@ class ComponentCCSolution:
     # the amplitudes as the device vector they were unpacked into (an EOM
     # context built from it needs no host round trip)
     device_amplitudes: object = field(default=None, repr=False, compare=False)
+    # the homotopy scale of the model these amplitudes solve (1: the problem as compiled)
+    interaction_scale: float = 1.0
 
 
 # ----------------------------------------------------------------- problem
@@ -337,7 +340,8 @@ def solve_component_ccsd(problem, initial_amplitudes=None, *, policy: NewtonKryl
     ops = p.ops
     ops.set_interaction_scale(interaction_scale)
     try:
-        return _solve(p, ops, controls, initial_amplitudes, accepted_step_callback, warm_start, precision)
+        sol = _solve(p, ops, controls, initial_amplitudes, accepted_step_callback, warm_start, precision)
+        return dataclasses.replace(sol, interaction_scale=float(interaction_scale))
     finally:
         ops.set_interaction_scale(1.0)
         for key, solver in list(p.__dict__.get("_gmres", {}).items()):
@@ -391,11 +395,15 @@ def _solve(p, ops, controls, initial_amplitudes, accepted_step_callback, warm_st
         jvp_count[0] += 1
         ops.jvp(v, out)
 
+    from .device_ops import pair_kernel_setting
+
     for iteration in range(controls.maximum_newton_iterations + 1):
         ops.linearize(x, r)
         residual_evaluations += 1
         if mixed:
             ops.to_single()
+            if ops.pair_tuning is None and pair_kernel_setting() == "auto":
+                ops.tune_pair_kernel()
         norm = vec.norm_r(r)
         if norm <= controls.tolerance:
             converged = True
@@ -500,14 +508,15 @@ def solve_component_ccsd_continuation(problem, scales=CONTINUATION_SCALES, initi
     The reference's production driver for strongly interacting impurities
     solves the homotopy models ``L0(K_ref) + s [L - L0(K_ref)]`` at one HF
     reference for s = 0.5, 0.75, 1, each started from the previous root, and
-    stops with ``RuntimeError`` when a stage does not converge
+    stops with ``RuntimeError`` when a stage does not converge; the last scale
+    is the model solved (1: the problem as compiled)
     (``examples/junction/gpu_timing.py:46-64``, problems from
     ``examples/shared/saved_reference.py:43-59``).  Returns the last stage's
     ``ComponentCCSolution`` and one ``ContinuationStage`` record per stage.
     """
     values = tuple(float(s) for s in scales)
-    if not values or values[-1] != 1.0 or any(not 0.0 < s <= 1.0 for s in values):
-        raise ValueError("continuation scales must lie in (0, 1] and end at 1")
+    if not values or any(not 0.0 < s <= 1.0 for s in values) or list(values) != sorted(values):
+        raise ValueError("continuation scales must increase within (0, 1]")
     initial = initial_amplitudes
     records = []
     solution = None

@@ -257,6 +257,9 @@ c3l_status c3l_static_apply(const c3l_static_action* action, const double* x, do
 typedef struct {
     c3l_action action;
     const c3l_complex* lam;
+    /* factor s of the product part, out = lam x + s V(x): the EOM block of the
+     * homotopy model at interaction scale s (see c3l_static_action) */
+    double interaction_scale;
 } c3l_eom_action;
 
 c3l_status c3l_eom_sigma(const c3l_eom_action* action, const c3l_complex* xin, c3l_complex* out, void* stream);

@@ -642,3 +642,40 @@ def test_exact_diagonalisation_check_readme(problems):
                                       float(ed["eta"]))
     assert relerr(res.retarded, ed["green_cc_reference"]) < 1e-8
     assert abs(relerr(res.retarded, ed["green_ed"]) - float(ed["cc_vs_ed_relative"])) <= 1e-7
+
+
+@pytest.mark.parametrize("name", ["readme", "twosrc", "kanamori3x2"])
+def test_interaction_scale_is_the_homotopy_model(name, problems, cuda_device):
+    """Residual, JVP and EOM sigma with the product part scaled by s equal the
+    oracle's on the spec with every product coefficient times s (the
+    reference's homotopy model at one HF reference)."""
+    import dataclasses
+
+    import c3lindblad_gb300 as c3
+    from oracle import component_oracle as oc
+
+    spec, g, p = problems(name)
+    s = 0.6
+    orc = oc.OracleProblem(dataclasses.replace(spec, product_coefficients=spec.product_coefficients * s).as_dict())
+    T = orc.tilde.unpack(g["fixed_variables"])
+    D = orc.tilde.unpack(g["fixed_direction_variables"])
+    ops = p.ops
+    x = torch.from_numpy(g["fixed_variables"]).to(cuda_device)
+    d = torch.from_numpy(g["fixed_direction_variables"]).to(cuda_device)
+    r = torch.empty_like(x)
+    j = torch.empty_like(x)
+    ops.set_interaction_scale(s)
+    try:
+        ops.residual(x, r)
+        ops.linearize(x, torch.empty_like(x))
+        ops.jvp(d, j)
+    finally:
+        ops.set_interaction_scale(1.0)
+    assert relerr(r.cpu().numpy(), _packed(p.plan, orc.residual(T)[0])) < 1e-12
+    assert relerr(j.cpu().numpy(), _packed(p.plan, orc.jvp(T, D)[0])) < 1e-12
+    ep = c3.ComponentEOMProblem.compile(c3.eom_ccsd_problem(p), p, 1)
+    ctx = c3.component_eom_context(ep, T, interaction_scale=s)
+    op = c3.ComponentSigmaOperator(ctx)
+    k = np.arange(op.dimension, dtype=np.float64)
+    probe = np.cos(0.7 * k + 0.2) + 1j * np.sin(0.3 * k - 0.1)
+    assert relerr(op.matvec(probe), oc.OracleEOM(orc, T, 0, 1).sigma(probe)) < 1e-12
