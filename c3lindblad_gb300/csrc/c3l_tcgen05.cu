@@ -8,8 +8,8 @@
 // component x into TF32 parts hi = tf32(x), lo = x - hi, and store them in
 // shared memory in the K-major, no-swizzle core-matrix layout the MMA reads
 // (8 rows x 16 bytes per core matrix).  One thread then issues the chunk's
-// twelve tcgen05.mma.kind::tf32 (M = 128, N = 64, K = 8) into two FP32
-// accumulators in tensor memory:
+// tcgen05.mma.kind::tf32 (M = 128, N = 64, K = 8; twelve per 8 anchors) into
+// two FP32 accumulators in tensor memory:
 //
 //   D_re += Ar Br - Ai Bi,   D_im += Ar Bi + Ai Br,
 //   each real product as hi hi + hi lo + lo hi (the lo lo term, 2^-22
@@ -36,31 +36,35 @@ namespace {
 constexpr int kTcM = 128;        // tile rows = tensor-memory lanes
 constexpr int kTcN = 64;         // tile columns per accumulator
 constexpr int kTcK = 8;          // anchors per MMA (32 bytes of TF32)
+constexpr int kTcChunk = 16;     // anchors per stage: two MMA K-steps
 constexpr int kTcThreads = 128;  // one warpgroup
 constexpr int kTcStages = 2;
-constexpr int kATile = kTcM * kTcK * 4;  // 4 KB: one TF32 part of the anchor tile
-constexpr int kBTile = kTcN * kTcK * 4;  // 2 KB: one TF32 part of the rest tile
-constexpr int kStageBytes = 4 * kATile + 4 * kBTile;
-constexpr int kTmemCols = 4 * kTcN;      // D_re in columns [0, 64), D_im in [64, 128); allocation 256
+constexpr int kRowBytes = kTcChunk * 4;               // one tile row's TF32 entries of a stage
+constexpr int kATile = kTcM * kRowBytes;              // 8 KB: one TF32 part of the anchor tile
+constexpr int kBTile = kTcN * kRowBytes;              // 4 KB: one TF32 part of the rest tile
+constexpr int kStageBytes = 4 * kATile + 4 * kBTile;  // 48 KB
+constexpr int kTmemCols = 2 * kTcN;                   // D_re in columns [0, 64), D_im in [64, 128)
 constexpr int kAlign = 1024;
 constexpr int kSmemBytes = kAlign + kTcStages * kStageBytes + 64;
 constexpr uint32_t kWaitLimit = 1u << 22;  // try_wait rounds before a block gives up
+constexpr int kBPerThread = kTcN * kTcChunk / kTcThreads;  // rest entries staged per thread
 static_assert(kTcThreads == kTcM, "one thread per tile row stages the anchor tile");
+static_assert(kBPerThread == 8, "the rest tile's staging covers 8 anchors per thread");
 
-// Byte offset of (row r, k) in a K-major no-swizzle operand tile: core
-// matrices of 8 rows x 16 bytes (4 TF32), the next 4 k at +128 bytes (the
-// descriptor's leading-dimension offset), the next 8 rows at +256 bytes (its
-// stride offset).
+// Byte offset of (row r, k) in a K-major no-swizzle operand tile of kTcChunk
+// anchors: core matrices of 8 rows x 16 bytes (4 TF32), the next 4 k at +128
+// bytes (the descriptor's leading-dimension offset), the next 8 rows at
+// +8 * kRowBytes (its stride offset).  MMA K-step j starts at +256 j.
 __device__ __forceinline__ uint32_t kmajor_off(int r, int k) {
-    return (uint32_t)((r >> 3) * 256 + (k >> 2) * 128 + (r & 7) * 16 + (k & 3) * 4);
+    return (uint32_t)((r >> 3) * (8 * kRowBytes) + (k >> 2) * 128 + (r & 7) * 16 + (k & 3) * 4);
 }
 
 // Shared-memory matrix descriptor: start address, leading-dimension byte
-// offset 128, stride byte offset 256 (both in 16-byte units), descriptor
-// version 1 (bits 46-47), base offset 0, no swizzle.
+// offset 128, stride byte offset 8 * kRowBytes (both in 16-byte units),
+// descriptor version 1 (bits 46-47), base offset 0, no swizzle.
 __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr) {
-    return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)(128 >> 4) << 16) | ((uint64_t)(256 >> 4) << 32) |
-           ((uint64_t)1 << 46);
+    return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)(128 >> 4) << 16) |
+           ((uint64_t)((8 * kRowBytes) >> 4) << 32) | ((uint64_t)1 << 46);
 }
 
 // Instruction descriptor of tcgen05.mma.kind::tf32: D F32 (bits 4-5 = 1), A and
@@ -103,10 +107,12 @@ __device__ __forceinline__ uint32_t tf32_hi(float x) {
     return h;
 }
 
-// hi and lo TF32 parts of x (lo = x - hi is exact in FP32)
+// hi and lo TF32 parts of x: hi = tf32(x), lo = tf32(x - hi) (x - hi is exact
+// in FP32; rounding it here keeps the tensor core's own truncation of the
+// operand from biasing long sums)
 __device__ __forceinline__ void tf32_split(float x, float& hi, float& lo) {
     hi = __uint_as_float(tf32_hi(x));
-    lo = __fsub_rn(x, hi);
+    lo = __uint_as_float(tf32_hi(__fsub_rn(x, hi)));
 }
 
 __device__ __forceinline__ void st_shared_v4(uint32_t addr, float a, float b, float c, float d) {
@@ -156,14 +162,27 @@ __global__ void __launch_bounds__(kTcThreads) k_pair_gemm_tc(c3l_pair_program pp
     c3l::pdl_wait();
 
     const int64_t nk = g.kend - g.kbegin;
-    const int nchunks = (int)((nk + kTcK - 1) / kTcK);
+    const int nchunks = (int)((nk + kTcChunk - 1) / kTcChunk);
     const bool a_ok = t.m0 + tid < g.M;
-    const int bcol = tid & (kTcN - 1), bk0 = (tid >> 6) * 4;  // rest tile: column, first of 4 anchors
+    const int bcol = tid & (kTcN - 1), bk0 = (tid >> 6) * kBPerThread;  // rest tile: column, first anchor
     const bool b_ok = t.n0 + bcol < g.N;
+    // the operand rows of one chunk, loaded one chunk ahead of their staging
+    float2 av[kTcChunk], bv[kBPerThread];
+    auto load = [&](int c) {
+        const int64_t k0 = g.kbegin + (int64_t)c * kTcChunk;
+#pragma unroll
+        for (int k = 0; k < kTcChunk; ++k)
+            av[k] = (a_ok && k0 + k < g.kend) ? ws[pp.aoff[k0 + k] + t.m0 + tid] : make_float2(0.0f, 0.0f);
+#pragma unroll
+        for (int q = 0; q < kBPerThread; ++q) {
+            const int64_t k = k0 + bk0 + q;
+            bv[q] = (b_ok && k < g.kend) ? ws[pp.roff[k] + t.n0 + bcol] : make_float2(0.0f, 0.0f);
+        }
+    };
+    if (nchunks > 0) load(0);
     bool ok = true;
     for (int c = 0; c < nchunks; ++c) {
         const int s = c & 1;
-        const int64_t k0 = g.kbegin + (int64_t)c * kTcK;
         // the stage's previous MMAs (chunk c - 2) must be done before it is rewritten
         if (c >= kTcStages) ok = mbar_wait(mbar0 + 8 * s, (uint32_t)(((c - kTcStages) >> 1) & 1));
         if (!__syncthreads_and(ok)) {
@@ -171,42 +190,32 @@ __global__ void __launch_bounds__(kTcThreads) k_pair_gemm_tc(c3l_pair_program pp
             break;
         }
         const uint32_t st = sbase + s * kStageBytes;
-        // anchor tile: this thread's row, the chunk's 8 anchors
-        float ar[kTcK], ai[kTcK];
+        // anchor tile: this thread's row, the chunk's 16 anchors, 4 per 16-byte store
 #pragma unroll
-        for (int k = 0; k < kTcK; ++k) {
-            float2 v = make_float2(0.0f, 0.0f);
-            if (a_ok && k0 + k < g.kend) v = ws[pp.aoff[k0 + k] + t.m0 + tid];
-            ar[k] = v.x;
-            ai[k] = v.y;
-        }
-#pragma unroll
-        for (int half = 0; half < 2; ++half) {
+        for (int q4 = 0; q4 < kTcChunk / 4; ++q4) {
             float h[4], l[4], hi2[4], li[4];
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
-                tf32_split(ar[4 * half + q], h[q], l[q]);
-                tf32_split(ai[4 * half + q], hi2[q], li[q]);
+                tf32_split(av[4 * q4 + q].x, h[q], l[q]);
+                tf32_split(av[4 * q4 + q].y, hi2[q], li[q]);
             }
-            const uint32_t off = kmajor_off(tid, 4 * half);
+            const uint32_t off = kmajor_off(tid, 4 * q4);
             st_shared_v4(st + 0 * kATile + off, h[0], h[1], h[2], h[3]);
             st_shared_v4(st + 1 * kATile + off, l[0], l[1], l[2], l[3]);
             st_shared_v4(st + 2 * kATile + off, hi2[0], hi2[1], hi2[2], hi2[3]);
             st_shared_v4(st + 3 * kATile + off, li[0], li[1], li[2], li[3]);
         }
-        // rest tile: this thread's column, 4 of the chunk's anchors
-        {
+        // rest tile: this thread's column, 8 of the chunk's anchors
+        const uint32_t bt = st + 4 * kATile;
+#pragma unroll
+        for (int q4 = 0; q4 < kBPerThread / 4; ++q4) {
             float h[4], l[4], hi2[4], li[4];
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
-                float2 v = make_float2(0.0f, 0.0f);
-                const int64_t k = k0 + bk0 + q;
-                if (b_ok && k < g.kend) v = ws[pp.roff[k] + t.n0 + bcol];
-                tf32_split(v.x, h[q], l[q]);
-                tf32_split(v.y, hi2[q], li[q]);
+                tf32_split(bv[4 * q4 + q].x, h[q], l[q]);
+                tf32_split(bv[4 * q4 + q].y, hi2[q], li[q]);
             }
-            const uint32_t off = kmajor_off(bcol, bk0);
-            const uint32_t bt = st + 4 * kATile;
+            const uint32_t off = kmajor_off(bcol, bk0 + 4 * q4);
             st_shared_v4(bt + 0 * kBTile + off, h[0], h[1], h[2], h[3]);
             st_shared_v4(bt + 1 * kBTile + off, l[0], l[1], l[2], l[3]);
             st_shared_v4(bt + 2 * kBTile + off, hi2[0], hi2[1], hi2[2], hi2[3]);
@@ -217,28 +226,32 @@ __global__ void __launch_bounds__(kTcThreads) k_pair_gemm_tc(c3l_pair_program pp
         __syncthreads();
         if (tid == 0) {
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const uint64_t arh = smem_desc(st), arl = smem_desc(st + kATile), aih = smem_desc(st + 2 * kATile),
-                           ail = smem_desc(st + 3 * kATile);
-            const uint32_t bb = st + 4 * kATile;
-            const uint64_t brh = smem_desc(bb), brl = smem_desc(bb + kBTile), bih = smem_desc(bb + 2 * kBTile),
-                           bil = smem_desc(bb + 3 * kBTile);
             const uint32_t dre = tmem, dim = tmem + kTcN;
             const uint32_t pos = idesc_tf32(false), neg = idesc_tf32(true);
-            const uint32_t first = c > 0 ? 1u : 0u;
-            mma_tf32(dre, arh, brh, pos, first);
-            mma_tf32(dre, arh, brl, pos, 1u);
-            mma_tf32(dre, arl, brh, pos, 1u);
-            mma_tf32(dre, aih, bih, neg, 1u);
-            mma_tf32(dre, aih, bil, neg, 1u);
-            mma_tf32(dre, ail, bih, neg, 1u);
-            mma_tf32(dim, arh, bih, pos, first);
-            mma_tf32(dim, arh, bil, pos, 1u);
-            mma_tf32(dim, arl, bih, pos, 1u);
-            mma_tf32(dim, aih, brh, pos, 1u);
-            mma_tf32(dim, aih, brl, pos, 1u);
-            mma_tf32(dim, ail, brh, pos, 1u);
+#pragma unroll
+            for (int j = 0; j < kTcChunk / kTcK; ++j) {
+                const uint32_t kb = 256u * j;  // MMA K-step j: 8 anchors = two core-matrix columns
+                const uint64_t arh = smem_desc(st + kb), arl = smem_desc(st + kATile + kb),
+                               aih = smem_desc(st + 2 * kATile + kb), ail = smem_desc(st + 3 * kATile + kb);
+                const uint64_t brh = smem_desc(bt + kb), brl = smem_desc(bt + kBTile + kb),
+                               bih = smem_desc(bt + 2 * kBTile + kb), bil = smem_desc(bt + 3 * kBTile + kb);
+                const uint32_t first = (c > 0 || j > 0) ? 1u : 0u;
+                mma_tf32(dre, arh, brh, pos, first);
+                mma_tf32(dre, arh, brl, pos, 1u);
+                mma_tf32(dre, arl, brh, pos, 1u);
+                mma_tf32(dre, aih, bih, neg, 1u);
+                mma_tf32(dre, aih, bil, neg, 1u);
+                mma_tf32(dre, ail, bih, neg, 1u);
+                mma_tf32(dim, arh, bih, pos, first);
+                mma_tf32(dim, arh, bil, pos, 1u);
+                mma_tf32(dim, arl, bih, pos, 1u);
+                mma_tf32(dim, aih, brh, pos, 1u);
+                mma_tf32(dim, aih, brl, pos, 1u);
+                mma_tf32(dim, ail, brh, pos, 1u);
+            }
             mma_commit(mbar0 + 8 * s);
         }
+        if (c + 1 < nchunks) load(c + 1);  // in flight while the MMAs run
     }
     // the last chunk's commit covers every MMA issued before it
     if (ok && nchunks > 0) ok = mbar_wait(mbar0 + 8 * ((nchunks - 1) & 1), (uint32_t)(((nchunks - 1) >> 1) & 1));
