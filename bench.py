@@ -32,6 +32,7 @@ extrapolated to the workload's call counts (labelled as such).
 from __future__ import annotations
 
 import argparse
+import dataclasses
 import json
 import os
 import statistics
@@ -66,7 +67,7 @@ WORKLOADS = {
                           "(5 orbitals x 2 spins, charge +1) x 4096 omega in [-12,12], eta=0.02"),
     "config3": dict(spec="kanamori3x8", omega=(-10.0, 10.0, 2001), eta=0.02, sites=(0, 1, 2), spins=(0, 1),
                     charges=(1, -1), scales=(0.5, 0.75, 1.0), policy=CONTINUATION_POLICY, golden=None,
-                    similar="kanamori3x2",
+                    similar="kanamori3x2", batched_sources=True,
                     label="3-orbital Kanamori U=2 J=0.3, 8 pseudomodes per orbital (n=27, 779,301 amplitudes, S13 dim "
                           "29,187); 6 sources (3 orbitals x 2 spins) x charge +1/-1 x 2001 omega in [-10,10], eta=0.02"),
     "siam10": dict(spec="siam10", omega=(-8.0, 8.0, 1001), eta=0.0, sites=None, spins=(0,), charges=(1,),
@@ -228,17 +229,41 @@ class Pipeline:
         sol, stages = self.static(problem, precision)
         amps = sol.device_amplitudes if sol.device_amplitudes is not None else sol.amplitudes
         greens = {}
+        grid = self.omega if grid is None else grid
         for b in self.blocks:
             ctx = c3.ComponentEOMContext(eoms[b], amps, interaction_scale=sol.interaction_scale)
             op = c3.ComponentSigmaOperator(ctx)
+            if self.wl.get("batched_sources") and method == "arnoldi" and sources is None:
+                # every source of the block at once: the matrix Arnoldi response steps all
+                # 2 x S channels together (one launch per kernel); a source's G^R is its diagonal
+                srcs = [c3.component_eom_sources(ctx, site=site) for site in self.sites]
+                res = c3.component_retarded_matrix_green_arnoldi(op, srcs, grid, self.eta,
+                                                                 maximum_krylov_dimension=4096)
+                for i, site in enumerate(self.sites):
+                    greens[(b[0], b[1], site)] = SourceGreen(
+                        res.addition[:, i, i], res.removal[:, i, i], res.retarded[:, i, i],
+                        res.addition_relative_residuals[:, i], res.removal_relative_residuals[:, i],
+                        (res.addition_projections[i].dimension, res.removal_projections[i].dimension))
+                continue
             for site in self.sites:
                 key = (b[0], b[1], site)
                 if sources is not None and key not in sources:
                     continue
                 src = c3.component_eom_sources(ctx, site=site)
-                greens[key] = c3.component_retarded_green(op, src, self.omega if grid is None else grid, self.eta,
-                                                          method=method)
+                greens[key] = c3.component_retarded_green(op, src, grid, self.eta, method=method)
         return sol, stages, greens
+
+
+@dataclasses.dataclass
+class SourceGreen:
+    """One source's G^R out of a block's matrix response (its diagonal)."""
+
+    addition: np.ndarray
+    removal: np.ndarray
+    retarded: np.ndarray
+    addition_relative_residuals: np.ndarray
+    removal_relative_residuals: np.ndarray
+    krylov_dimensions: tuple
 
 
 def _rel(a, b) -> float:
@@ -407,7 +432,11 @@ def run_gpu(args) -> dict:
                    "speedup_vs_plain_fp64_extrapolated": (plain_estimate / t_step) if plain_estimate else None,
                    "green_fp64_form_seconds": t_green_fp64,
                    "batched_omega": "one CGS2 Arnoldi basis per channel for all omega (graph-replayed steps, "
-                                    "incremental FP64 shifted solves); addition and removal channels stepped together",
+                                    "incremental FP64 shifted solves); "
+                                    + ("all sources of a (spin, charge) block stepped together (matrix Arnoldi "
+                                       "response, one launch per kernel for its 2 x S channels)"
+                                       if wl.get("batched_sources") else
+                                       "addition and removal channels of a source stepped together"),
                    "warm_start": "off: the learned guess (BF16 MLP) is trained on the SIAM family only; the "
                                  "continuation starts from zero amplitudes",
                    "l2": "flushed between steps (256 MB write)",
@@ -492,6 +521,7 @@ def kernel_roofline(pipe: Pipeline, sol, dev) -> dict:
 # GMRES G^R (siam10: 33,319 calls for 1001 omega, i.e. 16.6 per frequency and
 # source for both channels)
 SIGMA_CALLS_PER_OMEGA_SOURCE = 16.6
+_ORACLE: dict = {}
 
 
 def cpu_baseline(workload: str, sol=None, greens=None, budget_s: float = 20.0) -> dict:
@@ -511,19 +541,23 @@ def cpu_baseline(workload: str, sol=None, greens=None, budget_s: float = 20.0) -
     wl = WORKLOADS[workload]
     spec = ProblemSpec.load(GOLDEN / f"{wl['similar']}.spec.npz")
     target = ProblemSpec.load(GOLDEN / f"{wl['spec']}.spec.npz")
-    p = oc.OracleProblem(spec.as_dict())
-    rng = np.random.default_rng(0)
-    nv = p.tilde.real_size
-    x = p.tilde.unpack(1e-3 * rng.normal(size=nv))
-    d = p.tilde.unpack(rng.normal(size=nv))
+    cached = _ORACLE.get(wl["similar"])
+    if cached is None:  # the oracle's setup (its EOM plan) is built once, not timed
+        p = oc.OracleProblem(spec.as_dict())
+        rng = np.random.default_rng(0)
+        nv = p.tilde.real_size
+        x = p.tilde.unpack(1e-3 * rng.normal(size=nv))
+        d = p.tilde.unpack(rng.normal(size=nv))
+        eom = oc.OracleEOM(p, x, 0, 1)
+        v = rng.normal(size=eom.dimension) + 1j * rng.normal(size=eom.dimension)
+        cached = _ORACLE[wl["similar"]] = (p, x, d, eom, v)
+    p, x, d, eom, v = cached
     t0 = time.perf_counter()
     p.residual(x)
     t_res = time.perf_counter() - t0
     t0 = time.perf_counter()
     p.jvp(x, d)
     t_jvp = time.perf_counter() - t0
-    eom = oc.OracleEOM(p, x, 0, 1)
-    v = rng.normal(size=eom.dimension) + 1j * rng.normal(size=eom.dimension)
     k = 0
     t0 = time.perf_counter()
     while k < 50 and time.perf_counter() - t0 < budget_s / 4:
