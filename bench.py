@@ -67,7 +67,7 @@ WORKLOADS = {
                           "(5 orbitals x 2 spins, charge +1) x 4096 omega in [-12,12], eta=0.02"),
     "config3": dict(spec="kanamori3x8", omega=(-10.0, 10.0, 2001), eta=0.02, sites=(0, 1, 2), spins=(0, 1),
                     charges=(1, -1), scales=(0.5, 0.75, 1.0), policy=CONTINUATION_POLICY, golden=None,
-                    similar="kanamori3x2", batched_sources=True,
+                    similar="kanamori3x2",
                     label="3-orbital Kanamori U=2 J=0.3, 8 pseudomodes per orbital (n=27, 779,301 amplitudes, S13 dim "
                           "29,187); 6 sources (3 orbitals x 2 spins) x charge +1/-1 x 2001 omega in [-10,10], eta=0.02"),
     "siam10": dict(spec="siam10", omega=(-8.0, 8.0, 1001), eta=0.0, sites=None, spins=(0,), charges=(1,),
@@ -233,30 +233,24 @@ class Pipeline:
         for b in self.blocks:
             ctx = c3.ComponentEOMContext(eoms[b], amps, interaction_scale=sol.interaction_scale)
             op = c3.ComponentSigmaOperator(ctx)
-            if self.wl.get("batched_sources") and method == "arnoldi" and sources is None:
-                # every source of the block at once: the matrix Arnoldi response steps all
-                # 2 x S channels together (one launch per kernel); a source's G^R is its diagonal
-                srcs = [c3.component_eom_sources(ctx, site=site) for site in self.sites]
-                res = c3.component_retarded_matrix_green_arnoldi(op, srcs, grid, self.eta,
-                                                                 maximum_krylov_dimension=4096)
-                for i, site in enumerate(self.sites):
-                    greens[(b[0], b[1], site)] = SourceGreen(
-                        res.addition[:, i, i], res.removal[:, i, i], res.retarded[:, i, i],
-                        res.addition_relative_residuals[:, i], res.removal_relative_residuals[:, i],
-                        (res.addition_projections[i].dimension, res.removal_projections[i].dimension))
-                continue
             for site in self.sites:
                 key = (b[0], b[1], site)
                 if sources is not None and key not in sources:
                     continue
                 src = c3.component_eom_sources(ctx, site=site)
-                greens[key] = c3.component_retarded_green(op, src, grid, self.eta, method=method)
+                res = c3.component_retarded_green(op, src, grid, self.eta, method=method)
+                # keep the values only: the result also holds its channels' Krylov bases
+                # (for solution vectors), 107 GB per source at n = 65
+                greens[key] = SourceGreen(res.addition, res.removal, res.retarded, res.addition_relative_residuals,
+                                          res.removal_relative_residuals, tuple(res.krylov_dimensions))
+                del res, src
+            del op, ctx
         return sol, stages, greens
 
 
 @dataclasses.dataclass
 class SourceGreen:
-    """One source's G^R out of a block's matrix response (its diagonal)."""
+    """One source's G^R values (without the Krylov bases behind them)."""
 
     addition: np.ndarray
     removal: np.ndarray
@@ -432,11 +426,8 @@ def run_gpu(args) -> dict:
                    "speedup_vs_plain_fp64_extrapolated": (plain_estimate / t_step) if plain_estimate else None,
                    "green_fp64_form_seconds": t_green_fp64,
                    "batched_omega": "one CGS2 Arnoldi basis per channel for all omega (graph-replayed steps, "
-                                    "incremental FP64 shifted solves); "
-                                    + ("all sources of a (spin, charge) block stepped together (matrix Arnoldi "
-                                       "response, one launch per kernel for its 2 x S channels)"
-                                       if wl.get("batched_sources") else
-                                       "addition and removal channels of a source stepped together"),
+                                    "incremental FP64 shifted solves); the addition and removal channels of a "
+                                    "source stepped together (one launch per kernel for both)",
                    "warm_start": "off: the learned guess (BF16 MLP) is trained on the SIAM family only; the "
                                  "continuation starts from zero amplitudes",
                    "l2": "flushed between steps (256 MB write)",

@@ -18,8 +18,9 @@
 // and commits them to the chunk's stage barrier, while the threads stage the
 // next chunk into the other buffer.  The error per product is about 2^-21
 // relative, the accuracy of the FP32 operands themselves.  The epilogue reads
-// the accumulators with tcgen05.ld (warp w owns tensor-memory lanes 32w ..
-// 32w + 31, i.e. tile rows) and writes P.
+// the accumulators with tcgen05.ld (warp w reads tensor-memory lanes
+// 32 (w % 4) .. + 31, i.e. tile rows; the two warpgroups split the columns)
+// and writes P.
 //
 // Every wait on a barrier is bounded; a block whose wait runs out writes 1
 // to the program's status word (when given), skips the epilogue, frees its
@@ -37,7 +38,7 @@ constexpr int kTcM = 128;        // tile rows = tensor-memory lanes
 constexpr int kTcN = 64;         // tile columns per accumulator
 constexpr int kTcK = 8;          // anchors per MMA (32 bytes of TF32)
 constexpr int kTcChunk = 16;     // anchors per stage: two MMA K-steps
-constexpr int kTcThreads = 128;  // one warpgroup
+constexpr int kTcThreads = 256;  // two warpgroups: both stage, warps w and w + 4 share lanes 32 (w % 4)
 constexpr int kTcStages = 2;
 constexpr int kRowBytes = kTcChunk * 4;               // one tile row's TF32 entries of a stage
 constexpr int kATile = kTcM * kRowBytes;              // 8 KB: one TF32 part of the anchor tile
@@ -47,9 +48,9 @@ constexpr int kTmemCols = 2 * kTcN;                   // D_re in columns [0, 64)
 constexpr int kAlign = 1024;
 constexpr int kSmemBytes = kAlign + kTcStages * kStageBytes + 64;
 constexpr uint32_t kWaitLimit = 1u << 22;  // try_wait rounds before a block gives up
+constexpr int kAPerThread = kTcM * kTcChunk / kTcThreads;  // anchor entries staged per thread
 constexpr int kBPerThread = kTcN * kTcChunk / kTcThreads;  // rest entries staged per thread
-static_assert(kTcThreads == kTcM, "one thread per tile row stages the anchor tile");
-static_assert(kBPerThread == 8, "the rest tile's staging covers 8 anchors per thread");
+static_assert(kAPerThread == 8 && kBPerThread == 4, "staging: 8 anchors of a row, 4 of a column per thread");
 
 // Byte offset of (row r, k) in a K-major no-swizzle operand tile of kTcChunk
 // anchors: core matrices of 8 rows x 16 bytes (4 TF32), the next 4 k at +128
@@ -163,16 +164,19 @@ __global__ void __launch_bounds__(kTcThreads) k_pair_gemm_tc(c3l_pair_program pp
 
     const int64_t nk = g.kend - g.kbegin;
     const int nchunks = (int)((nk + kTcChunk - 1) / kTcChunk);
-    const bool a_ok = t.m0 + tid < g.M;
+    const int arow = tid & (kTcM - 1), ak0 = (tid >> 7) * kAPerThread;  // anchor tile: row, first anchor
+    const bool a_ok = t.m0 + arow < g.M;
     const int bcol = tid & (kTcN - 1), bk0 = (tid >> 6) * kBPerThread;  // rest tile: column, first anchor
     const bool b_ok = t.n0 + bcol < g.N;
     // the operand rows of one chunk, loaded one chunk ahead of their staging
-    float2 av[kTcChunk], bv[kBPerThread];
+    float2 av[kAPerThread], bv[kBPerThread];
     auto load = [&](int c) {
         const int64_t k0 = g.kbegin + (int64_t)c * kTcChunk;
 #pragma unroll
-        for (int k = 0; k < kTcChunk; ++k)
-            av[k] = (a_ok && k0 + k < g.kend) ? ws[pp.aoff[k0 + k] + t.m0 + tid] : make_float2(0.0f, 0.0f);
+        for (int q = 0; q < kAPerThread; ++q) {
+            const int64_t k = k0 + ak0 + q;
+            av[q] = (a_ok && k < g.kend) ? ws[pp.aoff[k] + t.m0 + arow] : make_float2(0.0f, 0.0f);
+        }
 #pragma unroll
         for (int q = 0; q < kBPerThread; ++q) {
             const int64_t k = k0 + bk0 + q;
@@ -190,22 +194,22 @@ __global__ void __launch_bounds__(kTcThreads) k_pair_gemm_tc(c3l_pair_program pp
             break;
         }
         const uint32_t st = sbase + s * kStageBytes;
-        // anchor tile: this thread's row, the chunk's 16 anchors, 4 per 16-byte store
+        // anchor tile: this thread's row, 8 of the chunk's anchors, 4 per 16-byte store
 #pragma unroll
-        for (int q4 = 0; q4 < kTcChunk / 4; ++q4) {
+        for (int q4 = 0; q4 < kAPerThread / 4; ++q4) {
             float h[4], l[4], hi2[4], li[4];
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
                 tf32_split(av[4 * q4 + q].x, h[q], l[q]);
                 tf32_split(av[4 * q4 + q].y, hi2[q], li[q]);
             }
-            const uint32_t off = kmajor_off(tid, 4 * q4);
+            const uint32_t off = kmajor_off(arow, ak0 + 4 * q4);
             st_shared_v4(st + 0 * kATile + off, h[0], h[1], h[2], h[3]);
             st_shared_v4(st + 1 * kATile + off, l[0], l[1], l[2], l[3]);
             st_shared_v4(st + 2 * kATile + off, hi2[0], hi2[1], hi2[2], hi2[3]);
             st_shared_v4(st + 3 * kATile + off, li[0], li[1], li[2], li[3]);
         }
-        // rest tile: this thread's column, 8 of the chunk's anchors
+        // rest tile: this thread's column, 4 of the chunk's anchors
         const uint32_t bt = st + 4 * kATile;
 #pragma unroll
         for (int q4 = 0; q4 < kBPerThread / 4; ++q4) {
@@ -258,13 +262,16 @@ __global__ void __launch_bounds__(kTcThreads) k_pair_gemm_tc(c3l_pair_program pp
     ok = __syncthreads_and(ok);
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     if (ok && nchunks > 0) {
-        const int row = warp * 32 + lane;
+        // warp w reads tensor-memory lanes 32 (w % 4) (tile rows); warps 0-3 take
+        // columns [0, 32) of both accumulators, warps 4-7 columns [32, 64)
+        const int row = (warp & 3) * 32 + lane;
         const int m = t.m0 + row;
+        const int cbase = (warp >> 2) * (kTcN / 2);
+        const uint32_t lanes = (uint32_t)((warp & 3) * 32) << 16;
         float2* __restrict__ P = ws + pp.base + g.p_off;
 #pragma unroll 1
-        for (int c0 = 0; c0 < kTcN; c0 += 16) {
+        for (int c0 = cbase; c0 < cbase + kTcN / 2; c0 += 16) {
             float re[16], im[16];
-            const uint32_t lanes = (uint32_t)(warp * 32) << 16;
             tmem_ld16(tmem + lanes + c0, re);
             tmem_ld16(tmem + lanes + kTcN + c0, im);
             if (m < g.M) {
