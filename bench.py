@@ -600,6 +600,42 @@ def run_reference(args) -> dict | None:
             "cpu_baseline": cb, "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+def profile_case(kernel: str) -> dict:
+    """A small case for ncu captures of single kernels: on the 3-orbital, n = 27
+    Kanamori fixture, three FP32 JVPs (pair GEMMs on ``kernel``: simt or
+    tcgen05) after one linearization, then three EOM sigma calls (double-float
+    pair GEMMs) at the fixture's fixed amplitudes."""
+    import torch
+
+    import c3lindblad_gb300 as c3
+
+    os.environ["C3L_PAIR_KERNEL"] = kernel
+    dev = torch.device("cuda:0")
+    spec = c3.ProblemSpec.load(GOLDEN / "kanamori3x8.spec.npz")
+    prob = c3.ComponentStaticProblem.compile(spec, device=dev)
+    ops = prob.ops
+    D = prob.num_variables
+    x = 1e-3 * np.cos(np.arange(D) + 0.13)
+    xd = torch.from_numpy(x).to(dev)
+    d = torch.from_numpy(0.2 * np.sin(np.arange(D) + 0.31)).to(dev)
+    y = torch.empty_like(xd)
+    ops.linearize(xd, y)
+    ops.to_single()
+    for _ in range(3):
+        ops.jvp32(d, y)
+    t = prob.plan.tilde
+    amp = t.coef_a * x[t.idx_a] + t.coef_b * x[t.idx_b]
+    ctx = c3.ComponentEOMContext(c3.ComponentEOMProblem.compile(c3.eom_ccsd_problem(prob), prob, 1), amp)
+    op = c3.ComponentSigmaOperator(ctx)
+    v = torch.ones(op.dimension, dtype=torch.complex128, device=dev)
+    w = torch.empty_like(v)
+    for _ in range(3):
+        op.matvec_device(v, w)
+    torch.cuda.synchronize()
+    ops.check_device_status()
+    return {"profile_case": kernel, "jvp_norm": float(y.norm()), "sigma_norm": float(w.norm())}
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -610,7 +646,12 @@ def main() -> None:
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-step", action="store_true",
                     help="run the warm-up steps and one step inside an NVTX range named 'step', then exit")
+    ap.add_argument("--profile-case", choices=["simt", "tcgen05"],
+                    help="run the small single-kernel case for ncu captures (n = 27 Kanamori), then exit")
     args = ap.parse_args()
+    if args.profile_case:
+        print(json.dumps(profile_case(args.profile_case)))
+        return
     out = run_reference(args) if args.impl == "reference" else run_gpu(args)
     if out is not None:
         print(json.dumps(out))
