@@ -62,6 +62,8 @@ WORKLOADS = {
     "config5": dict(spec="gen5x12", omega=(-12.0, 12.0, 4096), eta=0.02, sites=(0, 1, 2, 3, 4), spins=(0, 1),
                     charges=(1,), scales=(0.5, 0.75), policy=CONTINUATION_POLICY, golden=None,
                     similar="gen5x1",
+                    # an FP64 GMRES(960) basis of 26.5 M reals is 190 GB: the FP64 form restarts at 400
+                    fp64_policy=dict(CONTINUATION_POLICY, gmres_restart=400, gmres_maximum_restart_cycles=3),
                     label="5 orbitals x 12 pseudomodes, seeded general U_abcd (n=65, 26,511,875 amplitudes, S13 dim "
                           "409,890) at interaction scale 0.75 of the homotopy from its GHF reference; 10 sources "
                           "(5 orbitals x 2 spins, charge +1) x 4096 omega in [-12,12], eta=0.02"),
@@ -214,10 +216,13 @@ class Pipeline:
 
     def static(self, problem, precision: str):
         c3 = self.c3
+        policy = self.policy
+        if precision == "fp64" and self.wl.get("fp64_policy"):
+            policy = c3.NewtonKrylovPolicy(**self.wl["fp64_policy"])
         if self.wl["scales"]:
-            return c3.solve_component_ccsd_continuation(problem, self.wl["scales"], policy=self.policy,
+            return c3.solve_component_ccsd_continuation(problem, self.wl["scales"], policy=policy,
                                                         precision=precision)
-        return c3.solve_component_ccsd(problem, policy=self.policy, precision=precision), ()
+        return c3.solve_component_ccsd(problem, policy=policy, precision=precision), ()
 
     def step(self, problem=None, eoms=None, precision: str = "mixed", method: str = "arnoldi", grid=None,
              sources=None):
@@ -321,7 +326,11 @@ def run_gpu(args) -> dict:
     t_fp64 = None
     for w in range(args.warmup):
         if w == 1:
+            # the released FP32 Krylov basis stays cached by torch; hand it back
+            # before the FP64 basis is allocated, and the FP64 one after
+            torch.cuda.empty_cache()
             t_fp64, ref64 = _timed(torch, stream, lambda: pipe.step(precision="fp64"), flush)
+            torch.cuda.empty_cache()
         else:
             pipe.step()
     torch.cuda.synchronize()
@@ -416,7 +425,8 @@ def run_gpu(args) -> dict:
                    "krylov_dimensions": {"s%d q%+d site%d" % k: list(r.krylov_dimensions) for k, r in greens.items()},
                    "fp64_form_seconds": t_fp64,
                    "fp64_form": "FP64 inner JVPs and Krylov basis in the static solve, same G^R path (the second "
-                                "warm-up step)",
+                                "warm-up step)" + (", GMRES restart %d" % wl["fp64_policy"]["gmres_restart"]
+                                                    if wl.get("fp64_policy") else ""),
                    "speedup_vs_fp64_form": (t_fp64 / t_step) if t_fp64 else None,
                    "plain_fp64_seconds_extrapolated": plain_estimate,
                    "plain_fp64_form": "FP64 static solve plus the reference's per-frequency preconditioned GMRES for "
@@ -600,18 +610,21 @@ def run_reference(args) -> dict | None:
             "cpu_baseline": cb, "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
-def profile_case(kernel: str) -> dict:
-    """A small case for ncu captures of single kernels: on the 3-orbital, n = 27
-    Kanamori fixture, three FP32 JVPs (pair GEMMs on ``kernel``: simt or
-    tcgen05) after one linearization, then three EOM sigma calls (double-float
-    pair GEMMs) at the fixture's fixed amplitudes."""
+def profile_case(kernel: str, spec_name: str = "kanamori3x8") -> dict:
+    """A case for single-kernel ncu captures and event timings: on a committed
+    fixture (default the 3-orbital, n = 27 Kanamori; ``gen5x12`` is the n = 65
+    general-U model), one linearization, then four FP32 JVPs (pair GEMMs on
+    ``kernel``: simt or tcgen05), then four EOM sigma calls (double-float pair
+    GEMMs) at fixed amplitudes.  The last three of each are timed with CUDA
+    events on the launching stream."""
     import torch
 
     import c3lindblad_gb300 as c3
 
     os.environ["C3L_PAIR_KERNEL"] = kernel
     dev = torch.device("cuda:0")
-    spec = c3.ProblemSpec.load(GOLDEN / "kanamori3x8.spec.npz")
+    stream = torch.cuda.current_stream(dev)
+    spec = c3.ProblemSpec.load(GOLDEN / f"{spec_name}.spec.npz")
     prob = c3.ComponentStaticProblem.compile(spec, device=dev)
     ops = prob.ops
     D = prob.num_variables
@@ -621,19 +634,29 @@ def profile_case(kernel: str) -> dict:
     y = torch.empty_like(xd)
     ops.linearize(xd, y)
     ops.to_single()
-    for _ in range(3):
-        ops.jvp32(d, y)
+
+    def timed(fn, reps=3):
+        fn()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize(dev)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        return e0.elapsed_time(e1) / reps
+
+    jvp_ms = timed(lambda: ops.jvp32(d, y))
     t = prob.plan.tilde
     amp = t.coef_a * x[t.idx_a] + t.coef_b * x[t.idx_b]
     ctx = c3.ComponentEOMContext(c3.ComponentEOMProblem.compile(c3.eom_ccsd_problem(prob), prob, 1), amp)
     op = c3.ComponentSigmaOperator(ctx)
     v = torch.ones(op.dimension, dtype=torch.complex128, device=dev)
     w = torch.empty_like(v)
-    for _ in range(3):
-        op.matvec_device(v, w)
-    torch.cuda.synchronize()
+    sigma_ms = timed(lambda: op.matvec_device(v, w))
     ops.check_device_status()
-    return {"profile_case": kernel, "jvp_norm": float(y.norm()), "sigma_norm": float(w.norm())}
+    return {"profile_case": kernel, "spec": spec_name, "n": spec.n, "jvp32_ms": jvp_ms, "sigma_ms": sigma_ms,
+            "jvp_norm": float(y.norm()), "sigma_norm": float(w.norm())}
 
 
 def main() -> None:
@@ -647,10 +670,12 @@ def main() -> None:
     ap.add_argument("--profile-step", action="store_true",
                     help="run the warm-up steps and one step inside an NVTX range named 'step', then exit")
     ap.add_argument("--profile-case", choices=["simt", "tcgen05"],
-                    help="run the small single-kernel case for ncu captures (n = 27 Kanamori), then exit")
+                    help="run the single-kernel case for ncu captures and event timings, then exit")
+    ap.add_argument("--profile-spec", default="kanamori3x8", choices=["kanamori3x8", "gen5x12"],
+                    help="fixture of --profile-case (n = 27 Kanamori or the n = 65 general-U model)")
     args = ap.parse_args()
     if args.profile_case:
-        print(json.dumps(profile_case(args.profile_case)))
+        print(json.dumps(profile_case(args.profile_case, args.profile_spec)))
         return
     out = run_reference(args) if args.impl == "reference" else run_gpu(args)
     if out is not None:

@@ -108,8 +108,10 @@ class DeviceStatic:
             self.lin_action = static_action(self.ws_lin, "T", ["res_rest_T", "res_scalar", "jvp_rest_T"],
                                             "res_pairs" if rp else "res", plan.scatter_T, self.canon_T, plan.epilogue,
                                             pairs=rp)
-            self.jvp_action = static_action(self.ws_lin, "V", ["jvp_rest_V", "jvp_scalar"], "jvp", plan.scatter_V,
-                                            self.canon_V, plan.epilogue_jvp)
+            jp = "jvp" if "jvp" in prog.pairs else None
+            self.jvp_action = static_action(self.ws_lin, "V", ["jvp_rest_V", "jvp_scalar"],
+                                            "jvp_pairs" if jp else "jvp", plan.scatter_V, self.canon_V,
+                                            plan.epilogue_jvp, pairs=jp)
             # single-precision twin of the JVP (inner operator of the mixed-precision solve):
             # its output stage sums the anchor ^ rest products as pair GEMMs into the
             # pair buffer that follows the FP32 workspace, then gathers them
