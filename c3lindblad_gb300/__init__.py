@@ -18,7 +18,24 @@ from .static import (
     solve_component_ccsd,
     solve_component_ccsd_continuation,
 )
-from .matsubara import MatsubaraGreen, MatsubaraGrid, component_matsubara_green, matsubara_grid
+from .matsubara import (
+    MatrixSelfEnergyResult,
+    MatsubaraGreen,
+    MatsubaraGrid,
+    MatsubaraImpuritySolution,
+    MatsubaraSelfEnergy,
+    PhysicalModel,
+    component_matsubara_green,
+    impurity_sites,
+    matrix_auxiliary_self_energy,
+    matsubara_dyson_green,
+    matsubara_grid,
+    matsubara_noninteracting_green,
+    matsubara_self_energy,
+    noninteracting_retarded_green,
+    physical_model,
+    solve_matsubara,
+)
 from .response import (
     ComponentEOMContext,
     ComponentEOMProblem,
@@ -54,5 +71,8 @@ __all__ = [
     "ComponentRetardedMatrixGreen", "ComponentRetardedMatrixTime", "ComponentShiftedMatrixArnoldiGreen",
     "component_retarded_matrix_green", "component_retarded_matrix_green_shifts", "component_retarded_matrix_time",
     "component_retarded_time", "MatsubaraGreen", "MatsubaraGrid", "component_matsubara_green", "matsubara_grid",
-    "ContinuationStage", "solve_component_ccsd_continuation",
+    "ContinuationStage", "solve_component_ccsd_continuation", "MatrixSelfEnergyResult", "MatsubaraImpuritySolution",
+    "MatsubaraSelfEnergy", "PhysicalModel", "impurity_sites", "matrix_auxiliary_self_energy", "matsubara_dyson_green",
+    "matsubara_noninteracting_green", "matsubara_self_energy", "noninteracting_retarded_green", "physical_model",
+    "solve_matsubara",
 ]

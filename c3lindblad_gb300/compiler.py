@@ -80,9 +80,38 @@ TILE_DTYPE = np.dtype([("block", np.int32), ("count", np.int32), ("start", np.in
 # P_g row-major M x N at offset p_off of the pair buffer that follows the workspace.
 PAIR_GROUP_DTYPE = np.dtype([("p_off", np.int64), ("kbegin", np.int64), ("kend", np.int64),
                              ("M", np.int32), ("N", np.int32)], align=True)
-PAIR_TILE_DTYPE = np.dtype([("group", np.int32), ("m0", np.int32), ("n0", np.int32), ("pad", np.int32)], align=True)
-PAIR_TILE = 64    # P entries per tile side (CUDA-core kernels)
+PAIR_TILE_DTYPE = np.dtype([("group", np.int32), ("m0", np.int32), ("n0", np.int32), ("shape", np.int32)],
+                           align=True)
+PAIR_TILE = 64    # P entries per side of the default CUDA-core tile
 PAIR_TILE_TC = (128, 64)  # tensor-core tiles: rows (tensor-memory lanes) x columns
+# CUDA-core tile shapes (c3l_pair_tile.shape, C3L_PAIR_SHAPE_*): rows x columns,
+# in order of preference when several pad a group equally
+PAIR_SHAPES = {0: (64, 64), 1: (32, 128), 2: (128, 32), 3: (16, 256), 4: (256, 16)}
+PAIR_COLUMN, PAIR_COLUMN_SPLIT = 5, 6      # one-column groups: 256 rows / 32 rows, anchors split by warps
+PAIR_COLUMN_ROWS = {PAIR_COLUMN: 256, PAIR_COLUMN_SPLIT: 32}
+PAIR_COLUMN_SPLIT_MIN = 16                 # anchors from which the column tiles split them
+
+
+def pair_tiles(M: int, N: int, K: int) -> list:
+    """CUDA-core tiles (m0, n0, shape) of one pair group of M x N entries and K anchors.
+
+    One-column groups (N = 1) are matrix-vector products: 256-row tiles with
+    one row per thread, or, from PAIR_COLUMN_SPLIT_MIN anchors on, 32-row
+    tiles whose 8 warps split the anchors.  Every other group takes the
+    rectangular shape that pads it least (a group of 27 rows fills a
+    32 x 128 tile to 84 %, a 64 x 64 one to 42 %).
+    """
+    if N == 1:
+        shape = PAIR_COLUMN_SPLIT if K >= PAIR_COLUMN_SPLIT_MIN else PAIR_COLUMN
+        return [(m0, 0, shape) for m0 in range(0, M, PAIR_COLUMN_ROWS[shape])]
+
+    def padded(s):
+        tm, tn = PAIR_SHAPES[s]
+        return -(-M // tm) * tm * (-(-N // tn) * tn)
+
+    shape = min(PAIR_SHAPES, key=lambda s: (padded(s), s))
+    tm, tn = PAIR_SHAPES[shape]
+    return [(m0, n0, shape) for m0 in range(0, M, tm) for n0 in range(0, N, tn)]
 
 
 def _e(g: int) -> tuple:
@@ -702,9 +731,7 @@ def compile_pairs(builder: Builder, name: str, rest_info: dict, coords: Coordina
         garr[g] = (p, len(aoff), len(aoff) + len(rows), M, N)
         aoff.extend(r[0] for r in rows)
         roff.extend(r[1] for r in rows)
-        for m0 in range(0, M, PAIR_TILE):
-            for n0 in range(0, N, PAIR_TILE):
-                tiles.append((g, m0, n0, 0))
+        tiles.extend((g, m0, n0, shape) for m0, n0, shape in pair_tiles(M, N, len(rows)))
         key = coords.keys[b]
         for sign, lists in multi_shuffles(key, [ka, kr]):
             block_rows[b][2].append((complex(sign), [(p, sum(key), lists[0] + lists[1])]))

@@ -47,6 +47,8 @@ constexpr int kStageBytes = 4 * kATile + 4 * kBTile;  // 48 KB
 constexpr int kTmemCols = 2 * kTcN;                   // D_re in columns [0, 64), D_im in [64, 128)
 constexpr int kAlign = 1024;
 constexpr int kSmemBytes = kAlign + kTcStages * kStageBytes + 64;
+constexpr int kEpiStride = kTcN + 1;  // float2 per row of the epilogue's staging tile
+static_assert(kTcM * kEpiStride * 8 <= kTcStages * kStageBytes, "the epilogue tile reuses the stage buffers");
 constexpr uint32_t kWaitLimit = 1u << 22;  // try_wait rounds before a block gives up
 constexpr int kAPerThread = kTcM * kTcChunk / kTcThreads;  // anchor entries staged per thread
 constexpr int kBPerThread = kTcN * kTcChunk / kTcThreads;  // rest entries staged per thread
@@ -136,7 +138,6 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
 
 __global__ void __launch_bounds__(kTcThreads) k_pair_gemm_tc(c3l_pair_program pp, float2* __restrict__ ws, int pdl) {
     extern __shared__ uint8_t dsmem[];
-    if (pdl) c3l::pdl_launch_dependents();
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const uint32_t raw = (uint32_t)__cvta_generic_to_shared(dsmem);
     const uint32_t sbase = (raw + kAlign - 1) & ~(uint32_t)(kAlign - 1);
@@ -168,9 +169,10 @@ __global__ void __launch_bounds__(kTcThreads) k_pair_gemm_tc(c3l_pair_program pp
     const bool a_ok = t.m0 + arow < g.M;
     const int bcol = tid & (kTcN - 1), bk0 = (tid >> 6) * kBPerThread;  // rest tile: column, first anchor
     const bool b_ok = t.n0 + bcol < g.N;
-    // the operand rows of one chunk, loaded one chunk ahead of their staging
-    float2 av[kAPerThread], bv[kBPerThread];
-    auto load = [&](int c) {
+    // the operand rows of two chunks are in flight: chunk c + 2 is loaded into
+    // the registers chunk c has just been staged from
+    float2 av0[kAPerThread], bv0[kBPerThread], av1[kAPerThread], bv1[kBPerThread];
+    auto load = [&](int c, float2 (&av)[kAPerThread], float2 (&bv)[kBPerThread]) {
         const int64_t k0 = g.kbegin + (int64_t)c * kTcChunk;
 #pragma unroll
         for (int q = 0; q < kAPerThread; ++q) {
@@ -183,15 +185,15 @@ __global__ void __launch_bounds__(kTcThreads) k_pair_gemm_tc(c3l_pair_program pp
             bv[q] = (b_ok && k < g.kend) ? ws[pp.roff[k] + t.n0 + bcol] : make_float2(0.0f, 0.0f);
         }
     };
-    if (nchunks > 0) load(0);
     bool ok = true;
-    for (int c = 0; c < nchunks; ++c) {
+    // stage chunk c from (av, bv), issue its MMAs, then load chunk c + 2 into (av, bv)
+    auto step = [&](int c, float2 (&av)[kAPerThread], float2 (&bv)[kBPerThread]) {
         const int s = c & 1;
         // the stage's previous MMAs (chunk c - 2) must be done before it is rewritten
         if (c >= kTcStages) ok = mbar_wait(mbar0 + 8 * s, (uint32_t)(((c - kTcStages) >> 1) & 1));
         if (!__syncthreads_and(ok)) {
             ok = false;
-            break;
+            return;
         }
         const uint32_t st = sbase + s * kStageBytes;
         // anchor tile: this thread's row, 8 of the chunk's anchors, 4 per 16-byte store
@@ -225,6 +227,7 @@ __global__ void __launch_bounds__(kTcThreads) k_pair_gemm_tc(c3l_pair_program pp
             st_shared_v4(bt + 2 * kBTile + off, hi2[0], hi2[1], hi2[2], hi2[3]);
             st_shared_v4(bt + 3 * kBTile + off, li[0], li[1], li[2], li[3]);
         }
+        if (c + 2 < nchunks) load(c + 2, av, bv);  // in flight while this and the next chunk run
         // the generic-proxy stores become visible to the tensor cores' reads
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncthreads();
@@ -255,31 +258,50 @@ __global__ void __launch_bounds__(kTcThreads) k_pair_gemm_tc(c3l_pair_program pp
             }
             mma_commit(mbar0 + 8 * s);
         }
-        if (c + 1 < nchunks) load(c + 1);  // in flight while the MMAs run
+    };
+    if (nchunks > 0) load(0, av0, bv0);
+    if (nchunks > 1) load(1, av1, bv1);
+    for (int c = 0; c < nchunks && ok; c += 2) {
+        step(c, av0, bv0);
+        if (ok && c + 1 < nchunks) step(c + 1, av1, bv1);
     }
     // the last chunk's commit covers every MMA issued before it
     if (ok && nchunks > 0) ok = mbar_wait(mbar0 + 8 * ((nchunks - 1) & 1), (uint32_t)(((nchunks - 1) >> 1) & 1));
+    // the dependent kernel (the output gather) may start its blocks only now:
+    // blocks of it waiting on the SMs earlier would hold shared memory and
+    // warps that this kernel's second resident block needs
+    if (pdl) c3l::pdl_launch_dependents();
     ok = __syncthreads_and(ok);
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     if (ok && nchunks > 0) {
-        // warp w reads tensor-memory lanes 32 (w % 4) (tile rows); warps 0-3 take
-        // columns [0, 32) of both accumulators, warps 4-7 columns [32, 64)
+        // every MMA has completed, so the stage buffers are free: the tile goes
+        // through shared memory (rows of kEpiStride float2, two-way bank
+        // conflicts at most) so that each warp then writes whole P rows
+        // (coalesced) instead of one entry of 32 rows per store.
+        // Warp w reads tensor-memory lanes 32 (w % 4) (tile rows); warps 0-3
+        // take columns [0, 32) of both accumulators, warps 4-7 columns [32, 64).
+        float2* stile = reinterpret_cast<float2*>(dsmem + (sbase - raw));
         const int row = (warp & 3) * 32 + lane;
-        const int m = t.m0 + row;
         const int cbase = (warp >> 2) * (kTcN / 2);
         const uint32_t lanes = (uint32_t)((warp & 3) * 32) << 16;
-        float2* __restrict__ P = ws + pp.base + g.p_off;
 #pragma unroll 1
         for (int c0 = cbase; c0 < cbase + kTcN / 2; c0 += 16) {
             float re[16], im[16];
             tmem_ld16(tmem + lanes + c0, re);
             tmem_ld16(tmem + lanes + kTcN + c0, im);
-            if (m < g.M) {
 #pragma unroll
-                for (int j = 0; j < 16; ++j) {
-                    const int nn = t.n0 + c0 + j;
-                    if (nn < g.N) P[(int64_t)m * g.N + nn] = make_float2(re[j], im[j]);
-                }
+            for (int j = 0; j < 16; ++j) stile[row * kEpiStride + c0 + j] = make_float2(re[j], im[j]);
+        }
+        __syncthreads();
+        float2* __restrict__ P = ws + pp.base + g.p_off;
+#pragma unroll 1
+        for (int r = warp * (kTcM / 8); r < (warp + 1) * (kTcM / 8); ++r) {
+            const int m = t.m0 + r;
+            if (m >= g.M) break;
+#pragma unroll
+            for (int h = 0; h < kTcN / 32; ++h) {
+                const int col = lane + 32 * h;
+                if (t.n0 + col < g.N) P[(int64_t)m * g.N + t.n0 + col] = stile[r * kEpiStride + col];
             }
         }
     } else if (!ok && tid == 0 && pp.status) {

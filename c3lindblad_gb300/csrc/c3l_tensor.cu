@@ -341,191 +341,220 @@ __global__ void __launch_bounds__(kThreads) k_contract_cluster(LevelPack pack, i
     }
 }
 
-// Pair GEMMs (c3l_pair_program): one thread block computes a 64 x 64 tile of
+// Pair GEMMs (c3l_pair_program): one thread block computes one tile of
 // P_g = sum_k A_k^T R_k, whose operand rows A_k = ws[aoff[k] ...] and
 // R_k = ws[roff[k] ...] sit anywhere in the workspace (atoms and rest forms).
-// Chunks of 8 anchors are staged through shared memory (the next chunk's
-// rows are loaded into registers while the current one is multiplied); each
-// thread accumulates a 4 x 4 block of complex entries (rows tm + 16 i,
-// columns tn + 16 j), so every shared-memory read feeds four complex FMAs.
-constexpr int kPairTile = 64;
+// The tile's shape (c3l_pair_tile.shape) is chosen per group by the compiler:
+// 16 x 16 threads, each accumulating an RM x RN block of complex entries
+// (rows tm + 16 i, columns tn + 16 j), so a 64 x 64 tile (4 x 4) feeds four
+// products from every shared-memory read and the 32 x 128 / 16 x 256 tiles
+// (and their transposes) keep groups of 27 or 65 rows from running mostly
+// padding.  Chunks of 8 anchors are staged through shared memory, the next
+// chunk's rows loaded into registers while the current one is multiplied.
+// One-column groups (N = 1) are matrix-vector products with their own tiles.
+//
+// The arithmetic is a policy: PairPlain<C> (complex FMAs in C) or PairDf
+// (double-float on the FP32 pipe); both accumulate every entry over the
+// anchors in anchor order.
 constexpr int kPairChunk = 8;
 constexpr int kPairThreads = 256;
-static_assert(kPairThreads == 4 * kPairTile, "the loader covers 4 rows of a chunk per pass");
+constexpr int kPairMaxEdge = 256;  // rows plus columns of the largest tile: 16 + 256 (staged per chunk)
 
 template <typename C>
-__global__ void __launch_bounds__(kPairThreads) k_pair_gemm(c3l_pair_program pp, Batch<C> bt) {
-    if (!bt.pdl_at_exit) c3l::pdl_launch_dependents();
-    if (batch_stopped(bt)) return;
-    C* __restrict__ ws = bt.ws[blockIdx.y];
-    __shared__ C sa[kPairChunk][kPairTile];
-    __shared__ C sr[kPairChunk][kPairTile];
-    const c3l_pair_tile t = pp.tiles[blockIdx.x];
-    const c3l_pair_group g = pp.groups[t.group];
-    const int tm = threadIdx.x / 16, tn = threadIdx.x % 16;
-    const int lc = threadIdx.x % kPairTile, lr = threadIdx.x / kPairTile;  // loader: rows lr, lr + 4
-    const bool a_ok = t.m0 + lc < g.M, r_ok = t.n0 + lc < g.N;
-    const C zero = Cx<C>::make(0.0, 0.0);
-    // operand row offsets are program tables: the first chunk's before the wait
-    int64_t ao[2] = {-1, -1}, ro[2] = {-1, -1};
-#pragma unroll
-    for (int u = 0; u < 2; ++u) {
-        const int64_t k = g.kbegin + lr + 4 * u;
-        if (k < g.kend) {
-            ao[u] = pp.aoff[k];
-            ro[u] = pp.roff[k];
-        }
-    }
-    c3l::pdl_wait();
-    C av[2], rv[2];
-#pragma unroll
-    for (int u = 0; u < 2; ++u) {
-        av[u] = (ao[u] >= 0 && a_ok) ? ws[ao[u] + t.m0 + lc] : zero;
-        rv[u] = (ro[u] >= 0 && r_ok) ? ws[ro[u] + t.n0 + lc] : zero;
-    }
-    C acc[4][4];
-#pragma unroll
-    for (int i = 0; i < 4; ++i)
-#pragma unroll
-        for (int j = 0; j < 4; ++j) acc[i][j] = zero;
-    for (int64_t k0 = g.kbegin; k0 < g.kend; k0 += kPairChunk) {
-        __syncthreads();  // the previous chunk has been used
-#pragma unroll
-        for (int u = 0; u < 2; ++u) {
-            sa[lr + 4 * u][lc] = av[u];
-            sr[lr + 4 * u][lc] = rv[u];
-        }
-        __syncthreads();
-        // the next chunk's rows, in flight during this chunk's products
-#pragma unroll
-        for (int u = 0; u < 2; ++u) {
-            const int64_t k = k0 + kPairChunk + lr + 4 * u;
-            const bool ok = k < g.kend;
-            av[u] = (ok && a_ok) ? ws[pp.aoff[k] + t.m0 + lc] : zero;
-            rv[u] = (ok && r_ok) ? ws[pp.roff[k] + t.n0 + lc] : zero;
-        }
-#pragma unroll
-        for (int r = 0; r < kPairChunk; ++r) {
-            C a[4], b[4];
-#pragma unroll
-            for (int i = 0; i < 4; ++i) {
-                a[i] = sa[r][tm + 16 * i];
-                b[i] = sr[r][tn + 16 * i];
-            }
-#pragma unroll
-            for (int i = 0; i < 4; ++i)
-#pragma unroll
-                for (int j = 0; j < 4; ++j) acc[i][j] = cfma(a[i], b[j], acc[i][j]);
-        }
-    }
-    C* __restrict__ P = ws + pp.base + g.p_off;
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        const int m = t.m0 + tm + 16 * i;
-        if (m >= g.M) continue;
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const int nn = t.n0 + tn + 16 * j;
-            if (nn < g.N) P[(int64_t)m * g.N + nn] = acc[i][j];
-        }
-    }
-}
+struct PairPlain {
+    using Elem = C;  // workspace entry
+    using S = C;     // staged entry
+    using A = C;     // accumulator
+    static __device__ __forceinline__ S stage(C v) { return v; }
+    static __device__ __forceinline__ A zero() { return Cx<C>::make(0.0, 0.0); }
+    static __device__ __forceinline__ void mac(A& acc, const S& a, const S& b) { acc = cfma(a, b, acc); }
+    static __device__ __forceinline__ void add(A& acc, const A& b) { acc = cadd(acc, b); }
+    static __device__ __forceinline__ C finish(const A& acc) { return acc; }
+};
 
-// The pair GEMMs of an FP64 workspace in double-float arithmetic on the FP32
-// pipe.  Operand entries are split into FP32 (hi, lo) pairs as they are
-// staged (complex: re hi, re lo, im hi, im lo); each real product is formed
-// to about 2^-46 (Dekker's product with one FMA, df_mac) and summed by
-// TwoSum into a (sum, correction) pair per real component, finished in FP64
-// when P is written.  The result differs from an FP64 GEMM by about 1e-14 of
+// Operand entries are split into FP32 (hi, lo) pairs as they are staged
+// (complex: re hi, re lo, im hi, im lo); each real product is formed to about
+// 2^-46 (Dekker's product with one FMA, df_mac) and summed by TwoSum into a
+// (sum, correction) pair per real component, finished in FP64 when P is
+// written.  The result differs from an FP64 GEMM by about 1e-14 of
 // sum_k |A_k[i]| |R_k[j]|, at several times the FP64 pipe's rate.
-__global__ void __launch_bounds__(kPairThreads) k_pair_gemm_df(c3l_pair_program pp, Batch<double2> bt) {
-    if (!bt.pdl_at_exit) c3l::pdl_launch_dependents();
-    if (batch_stopped(bt)) return;
-    double2* __restrict__ ws = bt.ws[blockIdx.y];
-    __shared__ float4 sa[kPairChunk][kPairTile];
-    __shared__ float4 sr[kPairChunk][kPairTile];
-    const c3l_pair_tile t = pp.tiles[blockIdx.x];
-    const c3l_pair_group g = pp.groups[t.group];
-    const int tm = threadIdx.x / 16, tn = threadIdx.x % 16;
-    const int lc = threadIdx.x % kPairTile, lr = threadIdx.x / kPairTile;
-    const bool a_ok = t.m0 + lc < g.M, r_ok = t.n0 + lc < g.N;
-    const double2 zero = make_double2(0.0, 0.0);
-    int64_t ao[2] = {-1, -1}, ro[2] = {-1, -1};
-#pragma unroll
-    for (int u = 0; u < 2; ++u) {
-        const int64_t k = g.kbegin + lr + 4 * u;
-        if (k < g.kend) {
-            ao[u] = pp.aoff[k];
-            ro[u] = pp.roff[k];
-        }
-    }
-    c3l::pdl_wait();
-    double2 av[2], rv[2];
-#pragma unroll
-    for (int u = 0; u < 2; ++u) {
-        av[u] = (ao[u] >= 0 && a_ok) ? ws[ao[u] + t.m0 + lc] : zero;
-        rv[u] = (ro[u] >= 0 && r_ok) ? ws[ro[u] + t.n0 + lc] : zero;
-    }
-    // (re sum, re correction, im sum, im correction) of each of the thread's 4 x 4 entries
-    float4 acc[4][4];
-#pragma unroll
-    for (int i = 0; i < 4; ++i)
-#pragma unroll
-        for (int j = 0; j < 4; ++j) acc[i][j] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    auto split = [](double2 v) {
+struct PairDf {
+    using Elem = double2;
+    using S = float4;  // (re hi, re lo, im hi, im lo)
+    using A = float4;  // (re sum, re correction, im sum, im correction)
+    static __device__ __forceinline__ S stage(double2 v) {
         float4 q;
         split_d(v.x, q.x, q.y);
         split_d(v.y, q.z, q.w);
         return q;
+    }
+    static __device__ __forceinline__ A zero() { return make_float4(0.0f, 0.0f, 0.0f, 0.0f); }
+    static __device__ __forceinline__ void mac(A& c, const S& a, const S& b) {
+        // re += ar br - ai bi, im += ar bi + ai br
+        df_mac(c.x, c.y, a.x, a.y, b.x, b.y);
+        df_mac(c.x, c.y, -a.z, -a.w, b.z, b.w);
+        df_mac(c.z, c.w, a.x, a.y, b.z, b.w);
+        df_mac(c.z, c.w, a.z, a.w, b.x, b.y);
+    }
+    static __device__ __forceinline__ void add(A& c, const A& b) {
+        df_add(c.x, c.y, b.x, b.y);
+        df_add(c.z, c.w, b.z, b.w);
+    }
+    static __device__ __forceinline__ double2 finish(const A& c) {
+        return make_double2((double)c.x + (double)c.y, (double)c.z + (double)c.w);
+    }
+};
+
+// A (16 RM) x (16 RN) tile.  The loader stages entry e of a chunk's anchor
+// rows (e < 8 TM: row e % TM of anchor e / TM) from thread e % 256, and the
+// same for the rest rows.
+template <class Op, int RM, int RN>
+__device__ __forceinline__ void pair_tile(const c3l_pair_program& pp, const c3l_pair_tile& t,
+                                          const c3l_pair_group& g, typename Op::Elem* __restrict__ ws,
+                                          typename Op::S* smem) {
+    using E = typename Op::Elem;
+    using S = typename Op::S;
+    using A = typename Op::A;
+    constexpr int TM = 16 * RM, TN = 16 * RN;
+    constexpr int LA = (kPairChunk * TM + kPairThreads - 1) / kPairThreads;
+    constexpr int LB = (kPairChunk * TN + kPairThreads - 1) / kPairThreads;
+    static_assert(TM + TN <= kPairMaxEdge + 16, "tile larger than the staging buffer");
+    S* sa = smem;                     // [kPairChunk][TM]
+    S* sr = smem + kPairChunk * TM;   // [kPairChunk][TN]
+    const int tid = threadIdx.x, tm = tid / 16, tn = tid % 16;
+    const E zero = Cx<E>::make(0.0, 0.0);
+    E av[LA], rv[LB];
+    auto load = [&](int64_t k0) {
+#pragma unroll
+        for (int u = 0; u < LA; ++u) {
+            const int e = tid + kPairThreads * u;
+            const int64_t k = k0 + e / TM;
+            const int m = t.m0 + e % TM;
+            av[u] = (e < kPairChunk * TM && k < g.kend && m < g.M) ? ws[pp.aoff[k] + m] : zero;
+        }
+#pragma unroll
+        for (int u = 0; u < LB; ++u) {
+            const int e = tid + kPairThreads * u;
+            const int64_t k = k0 + e / TN;
+            const int nn = t.n0 + e % TN;
+            rv[u] = (e < kPairChunk * TN && k < g.kend && nn < g.N) ? ws[pp.roff[k] + nn] : zero;
+        }
     };
+    load(g.kbegin);
+    A acc[RM][RN];
+#pragma unroll
+    for (int i = 0; i < RM; ++i)
+#pragma unroll
+        for (int j = 0; j < RN; ++j) acc[i][j] = Op::zero();
     for (int64_t k0 = g.kbegin; k0 < g.kend; k0 += kPairChunk) {
-        __syncthreads();
+        __syncthreads();  // the previous chunk has been used
 #pragma unroll
-        for (int u = 0; u < 2; ++u) {
-            sa[lr + 4 * u][lc] = split(av[u]);
-            sr[lr + 4 * u][lc] = split(rv[u]);
+        for (int u = 0; u < LA; ++u) {
+            const int e = tid + kPairThreads * u;
+            if (e < kPairChunk * TM) sa[e] = Op::stage(av[u]);
+        }
+#pragma unroll
+        for (int u = 0; u < LB; ++u) {
+            const int e = tid + kPairThreads * u;
+            if (e < kPairChunk * TN) sr[e] = Op::stage(rv[u]);
         }
         __syncthreads();
-#pragma unroll
-        for (int u = 0; u < 2; ++u) {
-            const int64_t k = k0 + kPairChunk + lr + 4 * u;
-            const bool ok = k < g.kend;
-            av[u] = (ok && a_ok) ? ws[pp.aoff[k] + t.m0 + lc] : zero;
-            rv[u] = (ok && r_ok) ? ws[pp.roff[k] + t.n0 + lc] : zero;
-        }
+        if (k0 + kPairChunk < g.kend) load(k0 + kPairChunk);  // in flight during this chunk's products
 #pragma unroll 2
         for (int r = 0; r < kPairChunk; ++r) {
-            float4 a[4], b[4];
+            if constexpr (RM <= RN) {
+                S a[RM];
 #pragma unroll
-            for (int i = 0; i < 4; ++i) {
-                a[i] = sa[r][tm + 16 * i];
-                b[i] = sr[r][tn + 16 * i];
-            }
+                for (int i = 0; i < RM; ++i) a[i] = sa[r * TM + tm + 16 * i];
 #pragma unroll
-            for (int i = 0; i < 4; ++i)
+                for (int j = 0; j < RN; ++j) {
+                    const S b = sr[r * TN + tn + 16 * j];
 #pragma unroll
-                for (int j = 0; j < 4; ++j) {
-                    float4& c = acc[i][j];
-                    // re += ar br - ai bi, im += ar bi + ai br
-                    df_mac(c.x, c.y, a[i].x, a[i].y, b[j].x, b[j].y);
-                    df_mac(c.x, c.y, -a[i].z, -a[i].w, b[j].z, b[j].w);
-                    df_mac(c.z, c.w, a[i].x, a[i].y, b[j].z, b[j].w);
-                    df_mac(c.z, c.w, a[i].z, a[i].w, b[j].x, b[j].y);
+                    for (int i = 0; i < RM; ++i) Op::mac(acc[i][j], a[i], b);
                 }
+            } else {
+                S b[RN];
+#pragma unroll
+                for (int j = 0; j < RN; ++j) b[j] = sr[r * TN + tn + 16 * j];
+#pragma unroll
+                for (int i = 0; i < RM; ++i) {
+                    const S a = sa[r * TM + tm + 16 * i];
+#pragma unroll
+                    for (int j = 0; j < RN; ++j) Op::mac(acc[i][j], a, b[j]);
+                }
+            }
         }
     }
-    double2* __restrict__ P = ws + pp.base + g.p_off;
+    E* __restrict__ P = ws + pp.base + g.p_off;
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
+    for (int i = 0; i < RM; ++i) {
         const int m = t.m0 + tm + 16 * i;
         if (m >= g.M) continue;
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
+        for (int j = 0; j < RN; ++j) {
             const int nn = t.n0 + tn + 16 * j;
-            const float4 c = acc[i][j];
-            if (nn < g.N) P[(int64_t)m * g.N + nn] = make_double2((double)c.x + (double)c.y, (double)c.z + (double)c.w);
+            if (nn < g.N) P[(int64_t)m * g.N + nn] = Op::finish(acc[i][j]);
         }
     }
+}
+
+// One-column groups: P[m] = sum_k A_k[m] R_k[0].  C3L_PAIR_SHAPE_COLUMN: 256
+// rows, each thread one row over all anchors; C3L_PAIR_SHAPE_COLUMN_SPLIT: 32
+// rows (the lanes), warp w takes anchors w, w + 8, ..., and the eight partial
+// sums are added in warp order through shared memory.
+template <class Op, bool kSplit>
+__device__ __forceinline__ void pair_column(const c3l_pair_program& pp, const c3l_pair_tile& t,
+                                            const c3l_pair_group& g, typename Op::Elem* __restrict__ ws,
+                                            typename Op::S* smem) {
+    using A = typename Op::A;
+    const int tid = threadIdx.x;
+    const int row = kSplit ? (tid & 31) : tid;
+    const int m = t.m0 + row;
+    const int kstep = kSplit ? kPairThreads / 32 : 1;
+    A acc = Op::zero();
+    if (m < g.M) {
+        for (int64_t k = g.kbegin + (kSplit ? tid / 32 : 0); k < g.kend; k += kstep)
+            Op::mac(acc, Op::stage(ws[pp.aoff[k] + m]), Op::stage(ws[pp.roff[k]]));
+    }
+    if constexpr (kSplit) {
+        static_assert(sizeof(A) <= sizeof(typename Op::S), "partial sums reuse the staging buffer");
+        A* part = reinterpret_cast<A*>(smem);
+        part[tid] = acc;
+        __syncthreads();
+        if (tid >= 32) return;
+#pragma unroll
+        for (int w = 1; w < kPairThreads / 32; ++w) Op::add(acc, part[w * 32 + tid]);
+    }
+    if (m < g.M) ws[pp.base + g.p_off + m] = Op::finish(acc);
+}
+
+template <class Op>
+__device__ __forceinline__ void pair_gemm_block(const c3l_pair_program& pp, const Batch<typename Op::Elem>& bt) {
+    if (!bt.pdl_at_exit) c3l::pdl_launch_dependents();
+    if (batch_stopped(bt)) return;
+    __shared__ typename Op::S smem[kPairChunk * (kPairMaxEdge + 16)];
+    const c3l_pair_tile t = pp.tiles[blockIdx.x];
+    const c3l_pair_group g = pp.groups[t.group];
+    c3l::pdl_wait();  // the tables above are constant; the workspace is not
+    typename Op::Elem* __restrict__ ws = bt.ws[blockIdx.y];
+    switch (t.shape) {
+        case C3L_PAIR_SHAPE_32x128: pair_tile<Op, 2, 8>(pp, t, g, ws, smem); break;
+        case C3L_PAIR_SHAPE_128x32: pair_tile<Op, 8, 2>(pp, t, g, ws, smem); break;
+        case C3L_PAIR_SHAPE_16x256: pair_tile<Op, 1, 16>(pp, t, g, ws, smem); break;
+        case C3L_PAIR_SHAPE_256x16: pair_tile<Op, 16, 1>(pp, t, g, ws, smem); break;
+        case C3L_PAIR_SHAPE_COLUMN: pair_column<Op, false>(pp, t, g, ws, smem); break;
+        case C3L_PAIR_SHAPE_COLUMN_SPLIT: pair_column<Op, true>(pp, t, g, ws, smem); break;
+        default: pair_tile<Op, 4, 4>(pp, t, g, ws, smem); break;
+    }
+}
+
+template <typename C>
+__global__ void __launch_bounds__(kPairThreads) k_pair_gemm(c3l_pair_program pp, Batch<C> bt) {
+    pair_gemm_block<PairPlain<C>>(pp, bt);
+}
+
+__global__ void __launch_bounds__(kPairThreads) k_pair_gemm_df(c3l_pair_program pp, Batch<double2> bt) {
+    pair_gemm_block<PairDf>(pp, bt);
 }
 
 // FP64 workspaces run the double-float kernel unless `fp64_pipe` asks for the

@@ -8,9 +8,16 @@ half-plane points z = i|omega_n| (one Arnoldi basis per source and channel on
 the device, all points from it); negative frequencies receive
 G(-i omega) = G(i omega)^dagger.  ``component_matsubara_green`` also accepts the
 reference's own grid objects (anything with ``upper_shifts`` and
-``from_upper``), DLR grids included.  The self-energy and Dyson steps of
-``solve_matsubara`` need the physical model (setup) and are not part of this
-package.
+``from_upper``), DLR grids included.
+
+``solve_matsubara`` chains the device static solve, EOM context, sources and
+Matsubara response with the self-energy Sigma = G0^-1 - G^-1 and the Dyson
+equation on the host (``src/c3l/matsubara/solver.py:100-232``,
+``src/c3l/matsubara/dyson.py:15-175``,
+``src/c3l/spectra/reconstruction.py:174-257``): small dense solves of the
+impurity block per grid point, read from the physical one-body model that a
+``ProblemSpec`` carries (E, gamma_loss, gamma_gain, interaction sites) or from
+the reference's own ``FermionicLindbladModel``.
 """
 
 from __future__ import annotations
@@ -146,3 +153,237 @@ def component_matsubara_green(operator, sources, grid, *, maximum_krylov_dimensi
         maximum_krylov_dimension=maximum_krylov_dimension, residual_tolerance=residual_tolerance,
         minimum_krylov_dimension=minimum_krylov_dimension, check_interval=check_interval)
     return MatsubaraGreen(grid=grid, sites=upper.sites, green=grid.from_upper(upper.retarded), upper=upper)
+
+
+# ------------------------------------------------------ self-energy and Dyson
+@dataclass(frozen=True)
+class PhysicalModel:
+    """The one-body Lindblad model of one spin block (the attributes of the
+    reference's ``FermionicLindbladModel`` that the Dyson steps read)."""
+
+    E: np.ndarray
+    gamma_loss: np.ndarray
+    gamma_gain: np.ndarray
+    interaction_sites: tuple
+    has_interactions: bool
+
+    @property
+    def n_sites(self) -> int:
+        return int(self.E.shape[0])
+
+
+def physical_model(obj) -> PhysicalModel:
+    """The physical model of a ``ProblemSpec``, a compiled problem carrying one,
+    or a reference model (duck-typed: ``E``, ``gamma_loss``, ``gamma_gain``,
+    ``interaction_sites``, ``has_interactions``)."""
+    if isinstance(obj, PhysicalModel):
+        return obj
+    spec = getattr(obj, "spec", obj)
+    if hasattr(spec, "has_model"):
+        if not spec.has_model:
+            raise ValueError("the problem spec carries no physical model (E, gamma_loss, gamma_gain)")
+        return PhysicalModel(np.asarray(spec.model_E, np.complex128), np.asarray(spec.model_gamma_loss, np.complex128),
+                             np.asarray(spec.model_gamma_gain, np.complex128),
+                             tuple(int(v) for v in spec.interaction_sites), bool(spec.has_interactions))
+    if all(hasattr(obj, a) for a in ("E", "gamma_loss", "gamma_gain", "interaction_sites", "has_interactions")):
+        return PhysicalModel(np.asarray(obj.E, np.complex128), np.asarray(obj.gamma_loss, np.complex128),
+                             np.asarray(obj.gamma_gain, np.complex128), tuple(int(v) for v in obj.interaction_sites),
+                             bool(obj.has_interactions))
+    raise TypeError("model must be a ProblemSpec with a physical model or a FermionicLindbladModel")
+
+
+def impurity_sites(model, sites=None) -> tuple:
+    """The impurity block S (``dyson.py:15-40``): default the interaction sites;
+    every interacting site must be included, or G0^-1 - G^-1 is not the
+    impurity self-energy."""
+    m = physical_model(model)
+    chosen = tuple(m.interaction_sites if sites is None else sites)
+    if not chosen:
+        raise ValueError("at least one impurity site is required")
+    if any(isinstance(v, (bool, np.bool_)) or not isinstance(v, (int, np.integer)) for v in chosen):
+        raise TypeError("impurity sites must be integers")
+    chosen = tuple(int(v) for v in chosen)
+    if any(not 0 <= v < m.n_sites for v in chosen):
+        raise ValueError("an impurity site is outside the model")
+    if len(set(chosen)) != len(chosen):
+        raise ValueError("impurity sites must be unique")
+    if m.has_interactions and not set(m.interaction_sites) <= set(chosen):
+        raise ValueError("impurity sites must include every interaction site")
+    return chosen
+
+
+def noninteracting_retarded_green(model, shifts, sites=None) -> np.ndarray:
+    """[(z - E + i(gamma_loss + gamma_gain))^-1]_SS at each shift z (``dyson.py:43-64``)."""
+    m = physical_model(model)
+    block = list(impurity_sites(m, sites))
+    z = np.asarray(shifts, dtype=np.complex128)
+    if z.ndim != 1 or z.size == 0 or not np.all(np.isfinite(z)):
+        raise ValueError("shifts must be a finite nonempty vector")
+    n = m.n_sites
+    eye = np.eye(n, dtype=np.complex128)
+    effective = m.E - 1j * (m.gamma_loss + m.gamma_gain)
+    lhs = z[:, None, None] * eye[None] - effective[None]
+    cols = np.broadcast_to(eye[:, block], (z.size, n, len(block)))
+    return np.ascontiguousarray(np.linalg.solve(lhs, cols)[:, block, :])
+
+
+def matsubara_noninteracting_green(model, grid, sites=None) -> np.ndarray:
+    """The noninteracting impurity block on a Matsubara grid (``dyson.py:67-74``)."""
+    return grid.from_upper(noninteracting_retarded_green(model, grid.upper_shifts, sites))
+
+
+@dataclass(frozen=True, eq=False)
+class MatrixSelfEnergyResult:
+    """Sigma = G0^-1 - G^-1 per grid point and the conditioning of both solves."""
+
+    retarded: np.ndarray
+    G0_condition_number: np.ndarray
+    G_condition_number: np.ndarray
+    conditioning_limited: np.ndarray
+
+
+def matrix_auxiliary_self_energy(G0_R, G_R, *, conditioning_limit: float = 1.0e10) -> MatrixSelfEnergyResult:
+    """Sigma = G0^-1 - G^-1 by ordered linear solves (``reconstruction.py:174-212``)."""
+    G0 = np.asarray(G0_R, dtype=np.complex128)
+    G = np.asarray(G_R, dtype=np.complex128)
+    if G0.ndim != 3 or G0.shape[1] != G0.shape[2] or G.shape != G0.shape:
+        raise ValueError("G0_R and G_R must have the same shape (points, m, m)")
+    if not (np.all(np.isfinite(G0)) and np.all(np.isfinite(G))):
+        raise ValueError("Green functions must be finite")
+    limit = float(conditioning_limit)
+    if not np.isfinite(limit) or limit <= 1.0:
+        raise ValueError("conditioning_limit must be finite and larger than one")
+    eye = np.broadcast_to(np.eye(G.shape[1], dtype=np.complex128), G.shape)
+    c0 = np.linalg.cond(G0, p=2)
+    c = np.linalg.cond(G, p=2)
+    sigma = np.linalg.solve(G0, eye) - np.linalg.solve(G, eye)
+    return MatrixSelfEnergyResult(sigma, c0, c, (c0 > limit) | (c > limit))
+
+
+@dataclass(frozen=True, eq=False)
+class MatsubaraSelfEnergy:
+    """Auxiliary Dyson quantities on a Matsubara grid (axes n, a, b); the
+    hybridization is Delta = i omega_n - h - G0^-1 with h = E_SS."""
+
+    grid: object
+    sites: tuple
+    one_body: np.ndarray
+    noninteracting: np.ndarray
+    hybridization: np.ndarray
+    self_energy: np.ndarray
+    G0_condition_number: np.ndarray
+    G_condition_number: np.ndarray
+    conditioning_limited: np.ndarray
+
+
+def matsubara_self_energy(model, grid, green, *, sites=None, conditioning_limit: float = 1.0e10
+                          ) -> MatsubaraSelfEnergy:
+    """Sigma = G0^-1 - G^-1 for ``green`` on ``grid`` (``dyson.py:98-133``)."""
+    m = physical_model(model)
+    block = impurity_sites(m, sites)
+    G = np.asarray(green, dtype=np.complex128)
+    if G.shape != (len(grid), len(block), len(block)) or not np.all(np.isfinite(G)):
+        raise ValueError("green must be finite with shape (len(grid), len(sites), len(sites))")
+    G0 = matsubara_noninteracting_green(m, grid, block)
+    result = matrix_auxiliary_self_energy(G0, G, conditioning_limit=conditioning_limit)
+    h = m.E[np.ix_(block, block)].copy()
+    eye = np.eye(len(block), dtype=np.complex128)
+    hyb = grid.iw[:, None, None] * eye[None] - h[None] - np.linalg.inv(G0)
+    return MatsubaraSelfEnergy(grid=grid, sites=block, one_body=h, noninteracting=G0, hybridization=hyb,
+                               self_energy=result.retarded, G0_condition_number=result.G0_condition_number,
+                               G_condition_number=result.G_condition_number,
+                               conditioning_limited=result.conditioning_limited)
+
+
+def matsubara_dyson_green(grid, one_body, hybridization, self_energy) -> np.ndarray:
+    """G = [i omega_n - h - Delta(i omega_n) - Sigma(i omega_n)]^-1 (``dyson.py:136-164``)."""
+    delta = np.asarray(hybridization, dtype=np.complex128)
+    sigma = np.asarray(self_energy, dtype=np.complex128)
+    h = np.asarray(one_body, dtype=np.complex128)
+    if (delta.ndim != 3 or delta.shape[0] != len(grid) or delta.shape[1] != delta.shape[2]
+            or sigma.shape != delta.shape or h.shape != delta.shape[1:]):
+        raise ValueError("one_body, hybridization, and self_energy have incompatible shapes")
+    if not all(np.all(np.isfinite(v)) for v in (delta, sigma, h)):
+        raise ValueError("Dyson inputs must be finite")
+    eye = np.eye(h.shape[0], dtype=np.complex128)
+    lhs = grid.iw[:, None, None] * eye[None] - h[None] - delta - sigma
+    return np.linalg.solve(lhs, np.broadcast_to(eye, lhs.shape))
+
+
+@dataclass(frozen=True, eq=False)
+class MatsubaraImpuritySolution:
+    """CCSD + EOM impurity solution on a Matsubara grid: ``green`` and
+    ``self_energy`` have axes (n, a, b) over ``sites``; :meth:`dyson` inserts
+    the self-energy into another hybridization."""
+
+    grid: object
+    sites: tuple
+    rank: str
+    response_spin: int
+    green: np.ndarray
+    self_energy: np.ndarray
+    noninteracting: np.ndarray
+    hybridization: np.ndarray
+    one_body: np.ndarray
+    amplitudes: np.ndarray
+    static_residual: float | None
+    response: MatsubaraGreen
+    dyson_terms: MatsubaraSelfEnergy
+
+    def dyson(self, hybridization) -> np.ndarray:
+        """[i omega_n - h - Delta - Sigma]^-1 for a target ``hybridization``."""
+        return matsubara_dyson_green(self.grid, self.one_body, hybridization, self.self_energy)
+
+
+def solve_matsubara(model, grid, *, sites=None, rank: str = "S13", response_spin: int = 0, amplitudes=None,
+                    policy=None, precision: str = "mixed", maximum_krylov_dimension: int = 320,
+                    residual_tolerance: float = 1.0e-10, minimum_krylov_dimension: int = 16,
+                    check_interval: int = 8) -> MatsubaraImpuritySolution:
+    """Solve CCSD and the EOM response on the device, returning G(i omega_n) and
+    Sigma(i omega_n) (``src/c3l/matsubara/solver.py:100-232``).
+
+    ``model`` is a ``ComponentStaticProblem`` or ``ProblemSpec`` carrying the
+    physical model, or the reference's ``ComponentStaticProblem`` /
+    ``FactorizedCCProblem``.  Converged ``amplitudes`` skip the static solve.
+    The reference's ``platform``/``production`` switches select its NumPy or
+    JAX backends and have no counterpart here: the device path always runs
+    (``precision`` picks the static solve's form).  Only the retained S13
+    response space is built.
+    """
+    from .response import (ComponentEOMProblem, ComponentSigmaOperator, component_eom_context,
+                           component_eom_sources, eom_ccsd_problem)
+    from .static import ComponentStaticProblem, component_static_residual, solve_component_ccsd
+
+    if not (hasattr(grid, "upper_shifts") and hasattr(grid, "from_upper") and hasattr(grid, "iw")):
+        raise TypeError("grid must be a MatsubaraGrid")
+    if rank not in ("S13", "S135"):
+        raise ValueError("rank must be 'S13' or 'S135'")
+    if rank == "S135":
+        raise NotImplementedError("the S135 response space is not built; use rank='S13'")
+    static = ComponentStaticProblem.compile(model)
+    physical = physical_model(static.spec) if static.spec.has_model else physical_model(static.oracle.model)
+    block = impurity_sites(physical, sites)
+    if amplitudes is None:
+        solution = solve_component_ccsd(static, policy=policy, precision=precision)
+        if not solution.converged:
+            raise RuntimeError(f"static CCSD did not converge (residual {solution.packed_residual_norm:.3e})")
+        converged = np.asarray(solution.amplitudes, dtype=np.complex128)
+        static_residual = float(solution.packed_residual_norm)
+    else:
+        converged = np.asarray(amplitudes, dtype=np.complex128)
+        retained = component_static_residual(static, converged).retained
+        static_residual = float(np.linalg.norm(static.pack(retained)))
+    eom = eom_ccsd_problem(static, response_spin=response_spin)
+    context = component_eom_context(ComponentEOMProblem.compile(eom, static, 1), converged)
+    sources = tuple(component_eom_sources(context, site=site) for site in block)
+    response = component_matsubara_green(ComponentSigmaOperator(context), sources, grid,
+                                         maximum_krylov_dimension=maximum_krylov_dimension,
+                                         residual_tolerance=residual_tolerance,
+                                         minimum_krylov_dimension=minimum_krylov_dimension,
+                                         check_interval=check_interval)
+    terms = matsubara_self_energy(physical, grid, response.green, sites=block)
+    return MatsubaraImpuritySolution(grid=grid, sites=block, rank=rank, response_spin=int(response_spin),
+                                     green=response.green, self_energy=terms.self_energy,
+                                     noninteracting=terms.noninteracting, hybridization=terms.hybridization,
+                                     one_body=terms.one_body, amplitudes=converged, static_residual=static_residual,
+                                     response=response, dyson_terms=terms)

@@ -14,7 +14,10 @@ from the reference's setup layer (``src/c3l/cc/factorized.py:248-423``):
 * the mode-level tilde partners and phases (``src/c3l/ci/tilde.py:211-251``)
   from which the amplitude tilde map is induced (``src/c3l/cc/symmetry.py:150-187``);
 * for every site and spin, the factor indices of the physical operators
-  c, c^dagger, tilde c and tilde c^dagger used as EOM sources and sinks.
+  c, c^dagger, tilde c and tilde c^dagger used as EOM sources and sinks;
+* optionally the physical one-body model (E, gamma_loss, gamma_gain of one
+  spin block and the interaction sites, ``src/c3l/models.py:175-290``), which
+  the Matsubara self-energy and Dyson steps read.
 
 Specs are plain ``.npz`` files.  ``from_reference`` builds one from the
 reference's ``ComponentStaticProblem`` when that package is importable.
@@ -42,6 +45,11 @@ class ProblemSpec:
     source_factor: np.ndarray     # int [n, 2, 4]: c, c_dagger, tilde_c, tilde_c_dagger
     impurity_site: int = 0
     recipe: str = ""
+    model_E: np.ndarray | None = None           # complex [n, n]
+    model_gamma_loss: np.ndarray | None = None  # complex [n, n]
+    model_gamma_gain: np.ndarray | None = None  # complex [n, n]
+    interaction_sites: np.ndarray | None = None  # int [k], the impurity site first
+    has_interactions: bool = True
 
     def __post_init__(self) -> None:
         n = int(self.n)
@@ -67,6 +75,17 @@ class ProblemSpec:
         for row, ln in zip(pf, pl):
             if ln < 1 or np.any(row[:ln] < 0) or np.any(row[:ln] >= F):
                 raise ValueError("a product references a missing factor")
+        model = [self.model_E, self.model_gamma_loss, self.model_gamma_gain]
+        if any(m is not None for m in model):
+            if any(m is None or np.asarray(m).shape != (n, n) or not np.all(np.isfinite(m)) for m in model):
+                raise ValueError("the physical model needs finite [n, n] E, gamma_loss and gamma_gain")
+            sites = np.asarray(self.interaction_sites if self.interaction_sites is not None else [], np.int64)
+            if sites.ndim != 1 or sites.size == 0 or np.any(sites < 0) or np.any(sites >= n):
+                raise ValueError("interaction_sites must be a nonempty vector of sites")
+
+    @property
+    def has_model(self) -> bool:
+        return self.model_E is not None
 
     @property
     def num_factors(self) -> int:
@@ -93,7 +112,18 @@ class ProblemSpec:
             source_factor=np.asarray(data["source_factor"], np.int64),
             impurity_site=int(data["impurity_site"]) if "impurity_site" in data else 0,
             recipe=str(data["recipe"]) if "recipe" in data else "",
+            **cls._model_fields(data),
         )
+
+    @staticmethod
+    def _model_fields(data) -> dict:
+        if "model_E" not in data:
+            return {}
+        return dict(model_E=np.asarray(data["model_E"], np.complex128),
+                    model_gamma_loss=np.asarray(data["model_gamma_loss"], np.complex128),
+                    model_gamma_gain=np.asarray(data["model_gamma_gain"], np.complex128),
+                    interaction_sites=np.asarray(data["interaction_sites"], np.int64),
+                    has_interactions=bool(data["has_interactions"]))
 
     def as_dict(self) -> dict:
         return {
@@ -103,7 +133,11 @@ class ProblemSpec:
             "mode_partner": self.mode_partner, "mode_phase": self.mode_phase,
             "source_factor": self.source_factor, "impurity_site": np.int64(self.impurity_site),
             "recipe": np.array(self.recipe),
-        }
+        } | ({} if not self.has_model else {
+            "model_E": self.model_E, "model_gamma_loss": self.model_gamma_loss,
+            "model_gamma_gain": self.model_gamma_gain, "interaction_sites": self.interaction_sites,
+            "has_interactions": np.bool_(self.has_interactions),
+        })
 
     def save(self, path: str | Path) -> None:
         np.savez_compressed(path, **self.as_dict())
@@ -173,4 +207,15 @@ class ProblemSpec:
             rapidities=np.asarray(cc.rapidities, complex),
             mode_partner=np.asarray(det.partners, np.int64), mode_phase=np.asarray(det.factors, complex),
             source_factor=src, impurity_site=int(cc.model.impurity_site), recipe=recipe,
+            **model_fields(cc.model),
         )
+
+
+def model_fields(model) -> dict:
+    """The one-body model of a reference ``FermionicLindbladModel`` (spin
+    layout: one spin block; ``src/c3l/models.py:175-290``)."""
+    return dict(model_E=np.asarray(model.E, np.complex128),
+                model_gamma_loss=np.asarray(model.gamma_loss, np.complex128),
+                model_gamma_gain=np.asarray(model.gamma_gain, np.complex128),
+                interaction_sites=np.asarray(model.interaction_sites, np.int64),
+                has_interactions=bool(model.has_interactions))

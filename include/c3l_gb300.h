@@ -110,15 +110,28 @@ typedef struct {
     int32_t N;
 } c3l_pair_group;
 
-/* One thread block: the 64 x 64 entries of group `group` starting at (m0, n0). */
+/* One thread block: the entries of group `group` starting at (m0, n0).  In
+ * `tiles` (CUDA-core kernels) `shape` selects the tile: C3L_PAIR_SHAPE_64x64 ..
+ * C3L_PAIR_SHAPE_256x16 are rows x columns (16 x 16 threads, each a
+ * (rows / 16) x (columns / 16) block of entries); the two column shapes are
+ * for groups of one column (N = 1): 256 rows, one per thread, or 32 rows
+ * whose anchors the block's 8 warps split.  In `tiles_tc` shape is 0
+ * (128 x 64). */
+#define C3L_PAIR_SHAPE_64x64 0
+#define C3L_PAIR_SHAPE_32x128 1
+#define C3L_PAIR_SHAPE_128x32 2
+#define C3L_PAIR_SHAPE_16x256 3
+#define C3L_PAIR_SHAPE_256x16 4
+#define C3L_PAIR_SHAPE_COLUMN 5
+#define C3L_PAIR_SHAPE_COLUMN_SPLIT 6
 typedef struct {
     int32_t group;
     int32_t m0;
     int32_t n0;
-    int32_t pad;
+    int32_t shape;
 } c3l_pair_tile;
 
-/* kernel: C3L_PAIR_SIMT runs the CUDA-core kernels over `tiles` (64 x 64);
+/* kernel: C3L_PAIR_SIMT runs the CUDA-core kernels over `tiles`;
  * C3L_PAIR_TCGEN05 runs FP32 workspaces on the tensor cores over `tiles_tc`
  * (128 x 64, split-TF32, c3l_pair_gemm_tc); status (optional) receives 1 if
  * a tensor-core block gave up waiting for its MMAs. */

@@ -21,7 +21,10 @@ Usage: ``python tests/golden/make_fixtures.py [--reference SRC] [names...]``;
 ``... matrix [fixtures...]``, ``... warmstart``, ``... drivers [names...]`` and
 ``... ed`` write the matrix-response, warm-start, response-driver and
 exact-diagonalisation fixtures; ``... spec [names...]`` writes the specs of
-``SPEC_ONLY`` (no reference outputs).
+``SPEC_ONLY`` (no reference outputs); ``... model [names...]`` adds the
+physical one-body model (E, gamma_loss, gamma_gain, interaction sites) to
+committed specs; ``... matsubara`` writes the reference's ``solve_matsubara``
+outputs.
 """
 
 from __future__ import annotations
@@ -554,6 +557,50 @@ DRIVERS = {
 }
 
 
+# the reference's solve_matsubara on fixed amplitudes (the converged siam10
+# root; the fixed Kanamori amplitudes of the EOM goldens), both spin blocks
+MATSUBARA = {
+    "siam10": dict(beta=10.0, n_iw=8),
+    "kanamori3x2": dict(beta=8.0, n_iw=6),
+}
+
+
+def export_matsubara(name: str, path: Path) -> None:
+    """``solve_matsubara`` (``src/c3l/matsubara/solver.py:100``) with the
+    fixture's amplitudes (the static solve skipped), the default impurity block
+    (the interaction sites) and response spins 0 and 1; plus the Dyson
+    re-insertion into a semicircular target bath (half-bandwidth 2, hopping
+    0.3)."""
+    from c3l.cc.component_tensor import ComponentStaticProblem
+    from c3l.matsubara.grid import matsubara_grid
+    from c3l.matsubara.solver import solve_matsubara
+
+    spec = MATSUBARA[name]
+    cc = build_problem(FIXTURES[name])
+    static = ComponentStaticProblem.compile(cc)
+    golden = np.load(HERE / f"{name}.golden.npz")
+    amplitudes = golden["eom_amplitudes" if "eom_amplitudes" in golden.files else "solution_amplitudes"]
+    grid = matsubara_grid(spec["beta"], n_iw=spec["n_iw"])
+    # the amplitudes are the fixture golden's (not stored again)
+    out: dict = {"beta": np.float64(spec["beta"]), "indices": np.asarray(grid.indices, np.int64)}
+    z = grid.iw
+    target = (0.09 * (z - np.sign(z.imag) * np.sqrt(z ** 2 - 4.0 + 0j)) / 2.0)
+    for spin in (0, 1):
+        t0 = time.perf_counter()
+        sol = solve_matsubara(static, grid, amplitudes=amplitudes, response_spin=spin)
+        m = len(sol.sites)
+        hyb = np.broadcast_to(target[:, None, None] * np.eye(m), (len(grid), m, m))
+        out.update({f"s{spin}_green": sol.green, f"s{spin}_self_energy": sol.self_energy,
+                    f"s{spin}_noninteracting": sol.noninteracting, f"s{spin}_hybridization": sol.hybridization,
+                    f"s{spin}_dyson_target": sol.dyson(hyb), f"s{spin}_seconds": np.float64(time.perf_counter() - t0)})
+        out["sites"] = np.asarray(sol.sites, np.int64)
+        out["one_body"] = sol.one_body
+        out["static_residual"] = np.float64(sol.static_residual)
+        print(f"[{name}] matsubara spin {spin}: sites {sol.sites} {time.perf_counter() - t0:.1f}s", flush=True)
+    out["dyson_target_hybridization"] = target
+    np.savez_compressed(path, **out)
+
+
 def export_drivers(name: str, path: Path) -> None:
     """The reference's other response drivers on a fixture's converged
     amplitudes, charge +1: component_retarded_matrix_green (one GMRES solve per
@@ -696,6 +743,23 @@ def main() -> None:
             export_spec(cc, HERE / f"{name}.spec.npz", SPEC_ONLY[name]["recipe"])
             print(f"[{name}] n={model.n_sites} products={len(cc.products)} spec {time.perf_counter() - t0:.1f}s",
                   flush=True)
+        return
+    if args.names and args.names[0] == "model":
+        # add the physical one-body model to committed specs without rebuilding them
+        sys.path.insert(0, str(HERE.parents[1]))
+        from c3lindblad_gb300.spec import model_fields
+
+        for name in args.names[1:] or [*FIXTURES, *SPEC_ONLY]:
+            fx = FIXTURES.get(name) or SPEC_ONLY[name]
+            path = HERE / f"{name}.spec.npz"
+            data = dict(np.load(path))
+            data.update(model_fields(fx["model"]()))
+            np.savez_compressed(path, **data)
+            print(f"[{name}] model added", flush=True)
+        return
+    if args.names and args.names[0] == "matsubara":
+        for name in args.names[1:] or list(MATSUBARA):
+            export_matsubara(name, HERE / f"{name}.matsubara.npz")
         return
     if args.names and args.names[0] == "drivers":
         for name in args.names[1:] or list(DRIVERS):

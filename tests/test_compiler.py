@@ -155,7 +155,7 @@ def test_program_table_layouts_match_c_structs():
                     ("M", ctypes.c_int32), ("N", ctypes.c_int32)]
 
     class PairTile(ctypes.Structure):
-        _fields_ = [("group", ctypes.c_int32), ("m0", ctypes.c_int32), ("n0", ctypes.c_int32), ("pad", ctypes.c_int32)]
+        _fields_ = [("group", ctypes.c_int32), ("m0", ctypes.c_int32), ("n0", ctypes.c_int32), ("shape", ctypes.c_int32)]
 
     for dt, cs in ((compiler.CONTRACT_DTYPE, Task), (compiler.INSTANCE_DTYPE, Inst),
                    (compiler.BLOCK_DTYPE, Block), (compiler.TILE_DTYPE, Tile),
@@ -184,3 +184,26 @@ def test_multi_shuffle_signs_match_pairwise_wedge():
             acc += v
         got[idx] = acc
     assert np.allclose(got, ref, atol=1e-13)
+
+
+@pytest.mark.parametrize("M,N,K", [(1, 1, 1), (65, 65, 9), (27, 729, 40), (729, 27, 3), (4225, 65, 20),
+                                   (65, 274625, 10), (19683, 1, 6), (4225, 1, 200), (11, 121, 5)])
+def test_pair_tiles_cover_each_entry_once(M, N, K):
+    """The CUDA-core tiles of a pair group cover its M x N entries exactly once
+    and pick the least padded shape (one-column groups: the column tiles)."""
+    tiles = compiler.pair_tiles(M, N, K)
+    hit = np.zeros((M, N), np.int32)
+    for m0, n0, shape in tiles:
+        if shape in compiler.PAIR_COLUMN_ROWS:
+            assert N == 1
+            tm, tn = compiler.PAIR_COLUMN_ROWS[shape], 1
+            assert (shape == compiler.PAIR_COLUMN_SPLIT) == (K >= compiler.PAIR_COLUMN_SPLIT_MIN)
+        else:
+            tm, tn = compiler.PAIR_SHAPES[shape]
+        hit[m0:m0 + tm, n0:n0 + tn] += 1
+    assert np.all(hit == 1)
+    if N > 1:
+        shape = tiles[0][2]
+        tm, tn = compiler.PAIR_SHAPES[shape]
+        area = len(tiles) * tm * tn
+        assert area == min(-(-M // a) * a * (-(-N // b) * b) for a, b in compiler.PAIR_SHAPES.values())

@@ -19,8 +19,13 @@ pytestmark = pytest.mark.gpu
 
 torch = pytest.importorskip("torch")
 
+# (M, N, K); the CUDA-core tiles come from compiler.pair_tiles, so these cover
+# every shape: 64 x 64 (65 x 65), 32 x 128 (27 x 729), 128 x 32 (729 x 27),
+# 16 x 256 (1 x 300, 11 x 200), 256 x 16 (4225 x 65), and the one-column
+# tiles without (300 x 1, 2000 x 1) and with anchor splitting (700 x 1 x 37)
 SHAPES = [(1, 1, 1), (3, 7, 2), (64, 64, 8), (65, 65, 9), (130, 17, 23), (1, 300, 5), (300, 1, 5),
-          (197, 201, 37), (4225, 65, 3)]
+          (197, 201, 37), (4225, 65, 3), (27, 729, 9), (729, 27, 12), (11, 200, 17), (2000, 1, 6),
+          (700, 1, 37), (33, 1, 16)]
 
 
 def _program(rng, ws_size: int):
@@ -31,9 +36,7 @@ def _program(rng, ws_size: int):
         groups[g] = (p, len(aoff), len(aoff) + K, M, N)
         aoff.extend(int(v) for v in rng.integers(0, ws_size - M + 1, K))
         roff.extend(int(v) for v in rng.integers(0, ws_size - N + 1, K))
-        for m0 in range(0, M, compiler.PAIR_TILE):
-            for n0 in range(0, N, compiler.PAIR_TILE):
-                tiles.append((g, m0, n0, 0))
+        tiles.extend((g, m0, n0, shape) for m0, n0, shape in compiler.pair_tiles(M, N, K))
         for m0 in range(0, M, compiler.PAIR_TILE_TC[0]):
             for n0 in range(0, N, compiler.PAIR_TILE_TC[1]):
                 tiles_tc.append((g, m0, n0, 0))
