@@ -20,7 +20,7 @@ from .plans import EOMPlan, SourcePlan, StaticPlan
 
 PAIR_KERNELS = {"simt": rt.PAIR_SIMT, "tcgen05": rt.PAIR_TCGEN05}
 # the kernel used before (or without) tuning
-PAIR_KERNEL_DEFAULT = "simt"
+PAIR_KERNEL_DEFAULT = "auto"
 
 
 def pair_kernel_setting() -> str:
@@ -32,8 +32,10 @@ def pair_kernel_setting() -> str:
 
 
 def pair_kernel() -> int:
+    """The kernel a new action starts with (the CUDA cores under 'auto', until
+    the autotuner has timed both)."""
     v = pair_kernel_setting()
-    return PAIR_KERNELS[PAIR_KERNEL_DEFAULT if v == "auto" else v]
+    return PAIR_KERNELS["simt" if v == "auto" else v]
 
 
 def _cz(n: int, device) -> torch.Tensor:
@@ -204,8 +206,9 @@ class DeviceStatic:
 
     def tune_pair_kernel(self, reps: int = 3) -> dict:
         """Project autotuner of the FP32 JVP's contraction tiles: times the JVP
-        (after ``to_single``) with each pair-GEMM kernel -- CUDA cores on 64 x 64
-        tiles, tcgen05 tensor cores on 128 x 64 tiles -- and keeps the faster.
+        (after ``to_single``) with each pair-GEMM kernel -- CUDA cores on the
+        compiler's per-group tile shapes, tcgen05 tensor cores on 128 x 64
+        tiles -- and keeps the faster.
         Returns {kernel: milliseconds}.  Both kernels sum in FP32 (the
         tensor-core one in split TF32), so the choice does not move the JVP
         beyond FP32 rounding."""

@@ -13,7 +13,7 @@ import ctypes as C
 import numpy as np
 import pytest
 
-from conftest import eom_amplitudes, golden_names, load, relerr
+from conftest import GOLDEN, eom_amplitudes, golden_names, load, relerr
 
 pytestmark = pytest.mark.gpu
 
@@ -464,6 +464,34 @@ def test_single_precision_jvp_tracks_fp64(name, kernel, cuda_device, monkeypatch
     assert 0 < err < 1e-5
 
 
+def test_pair_kernel_autotuner_keeps_the_faster_kernel(cuda_device, monkeypatch):
+    """C3L_PAIR_KERNEL=auto (the default): the tuner times the FP32 JVP with
+    both pair-GEMM kernels, keeps the faster, and the JVP it leaves behind is
+    still the FP32 JVP (within FP32 rounding of the FP64 one)."""
+    import c3lindblad_gb300 as c3
+    from c3lindblad_gb300 import device_ops
+
+    monkeypatch.setenv("C3L_PAIR_KERNEL", "auto")
+    spec = c3.ProblemSpec.load(GOLDEN / "kanamori3x8.spec.npz")
+    p = c3.ComponentStaticProblem.compile(spec, device=cuda_device)
+    ops = p.ops
+    idx = torch.arange(p.num_variables, dtype=torch.float64, device=cuda_device)
+    x = 1e-3 * torch.cos(idx + 0.13)
+    d = 0.2 * torch.sin(idx + 0.31)
+    r = torch.empty_like(x)
+    ops.linearize(x, r)
+    ops.to_single()
+    times = ops.tune_pair_kernel()
+    assert set(times) == set(device_ops.PAIR_KERNELS) and all(t > 0 for t in times.values())
+    assert ops.pair_kernel_name == min(times, key=times.get)
+    j64 = torch.empty_like(x)
+    j32 = torch.empty_like(x)
+    ops.jvp(d, j64)
+    ops.jvp32(d, j32)
+    ops.check_device_status()
+    assert 0 < relerr(j32.cpu().numpy(), j64.cpu().numpy()) < 1e-5
+
+
 @pytest.mark.parametrize("basis_f32,restart", [(False, 30), (True, 30), (True, 70)])
 def test_newton_correction_gmres_fp32_operator(basis_f32, restart, problems, cuda_device):
     """c3l_gmres with the FP32 JVP, with an FP64 or an FP32 Krylov basis: the
@@ -559,8 +587,12 @@ def test_response_drivers_match_reference(name, problems):
     and real-axis points), the time-domain propagation of one source and the
     time-domain matrix with its separate channels.  Frequency-domain values
     1e-8 relative (the G^R contract); Krylov dimensions within one check
-    interval; time-domain values 1e-7 relative (the Krylov spaces agree to
-    FP64 rounding, which the propagator carries to t = 20)."""
+    interval; time-domain values 1e-8 relative where the Krylov basis
+    converged.  A basis that stops at the 160-vector cap without meeting the
+    time-residual test (the siam10 matrix propagation) is an unconverged
+    approximation in both codes: there the two agree to 1e-7 (measured
+    1.5e-8), the FP64 rounding of two different orthogonalizations carried
+    through an unconverged propagator to t = 20."""
     import c3lindblad_gb300 as c3
     from conftest import GOLDEN
 
@@ -607,8 +639,10 @@ def test_response_drivers_match_reference(name, problems):
     print(name, {k: f"{v:.2e}" for k, v in errors.items()})
     for k in ("gmres", "gmres_addition", "shifts", "shifts_removal"):
         assert errors[k] < 1e-8, (k, errors[k])
-    for k in ("time", "matrix_time", "matrix_time_addition"):
-        assert errors[k] < 1e-7, (k, errors[k])
+    assert errors["time"] < 1e-8, errors["time"]
+    capped = max(pr.dimension for pr in mt.combined_projections) >= 160
+    for k in ("matrix_time", "matrix_time_addition"):
+        assert errors[k] < (1e-7 if capped else 1e-8), (k, errors[k], capped)
     # the Matsubara grid form (the complex-shift driver at i|omega_n|)
     op = c3.ComponentSigmaOperator(ctx)
     grid = c3.matsubara_grid(float(ref["matsubara_beta"]), indices=ref["matsubara_indices"])
