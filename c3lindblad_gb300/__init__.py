@@ -36,6 +36,7 @@ from .matsubara import (
     physical_model,
     solve_matsubara,
 )
+from .s135 import CompiledFullS135Action, FullS135ResponseOperator
 from .response import (
     ComponentEOMContext,
     ComponentEOMProblem,
@@ -74,5 +75,5 @@ __all__ = [
     "ContinuationStage", "solve_component_ccsd_continuation", "MatrixSelfEnergyResult", "MatsubaraImpuritySolution",
     "MatsubaraSelfEnergy", "PhysicalModel", "impurity_sites", "matrix_auxiliary_self_energy", "matsubara_dyson_green",
     "matsubara_noninteracting_green", "matsubara_self_energy", "noninteracting_retarded_green", "physical_model",
-    "solve_matsubara",
+    "solve_matsubara", "CompiledFullS135Action", "FullS135ResponseOperator",
 ]

@@ -49,6 +49,7 @@ import numpy as np
 from .layout import Coordinates
 
 MAX_FACTORS = 6
+MAX_DEGREE = 6   # index digits per output (C3L_MAX_DEGREE): static and S13 need 4, S135 5
 MAX_SOURCES = 4
 TILE = 256        # outputs per contraction tile (one thread each)
 WEDGE_WIDTHS = (64, 32, 16, 8)  # outputs per wedge tile; a block of 256 threads splits
@@ -65,7 +66,7 @@ CONTRACT_DTYPE = np.dtype([
 INSTANCE_DTYPE = np.dtype([
     ("coef", np.float64, (2,)), ("nfac", np.int32), ("pad", np.int32),
     ("fac_off", np.int64, (MAX_FACTORS,)), ("fac_deg", np.int32, (MAX_FACTORS,)),
-    ("axes", np.int8, (MAX_FACTORS, 4)),
+    ("axes", np.int8, (MAX_FACTORS, MAX_DEGREE)),
 ], align=True)
 
 BLOCK_DTYPE = np.dtype([
@@ -203,7 +204,7 @@ class Symbolic:
         self.source_keys = {
             "T": {2: frozenset(k for k in skeys if sum(k) == 2), 4: frozenset(k for k in skeys if sum(k) == 4)},
             "V": {2: frozenset(k for k in skeys if sum(k) == 2), 4: frozenset(k for k in skeys if sum(k) == 4)},
-            "X": {d: frozenset(k for k in eom_keys if sum(k) == d) for d in (1, 3)},
+            "X": {d: frozenset(k for k in eom_keys if sum(k) == d) for d in (1, 3, 5)},
         }
         self._blocks: dict = {}
 
@@ -759,18 +760,20 @@ def static_terms(sym: Symbolic, spec):
 
 
 def eom_terms(sym: Symbolic, spec, eom_keys, vacuum: dict):
-    """Sigma monomials: products acting on X, minus vacuum ^ X (component_tensor.py:2116-2223)."""
+    """Sigma monomials: products acting on X, minus vacuum ^ X (component_tensor.py:2116-2223);
+    with rank-five keys, the full S135 action (``src/c3l/cc/s135_full.py:51-98``)."""
     acc: dict = defaultdict(complex)
     degs = sorted({sum(k) for k in eom_keys})
+    keep = set(degs)  # {1, 3} for S13, {1, 3, 5} with the rank-five shell
     for d in degs:
         x = Atom("X", -1, d)
         if not sym.nonzero(x):
             continue
-        part = sym.expand(list(spec.products()), (x,), 3, {1, 3})
+        part = sym.expand(list(spec.products()), (x,), max(degs), keep)
         for k, v in part.items():
             acc[k] += v
         for atoms, coef in vacuum.items():
-            if sum(a.degree for a in atoms) + d not in (1, 3):
+            if sum(a.degree for a in atoms) + d not in keep:
                 continue
             cc, ca = sym.canonical(-coef, atoms + (x,))
             acc[ca] += cc

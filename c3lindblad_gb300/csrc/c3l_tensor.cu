@@ -241,7 +241,8 @@ __device__ __forceinline__ void contract_entry(const c3l_contract_task& task, in
     if (task.const_off >= 0) acc = vectors[task.const_off + e];
     for (int j = 0; j < task.nsrc; ++j) {
         const int axis = task.axis[j];
-        // entries of a padded block are below n^4 < 2^32 (n <= 255): 32-bit division
+        // entries of a padded block are below n^deg < 2^32 (n <= 255 for the
+        // degree-4 blocks, n <= 73 for the rank-five response shell): 32-bit division
         const uint32_t low = (uint32_t)pw[task.deg - axis];
         const uint32_t hi = (uint32_t)e / low;
         const uint32_t lo = (uint32_t)e - hi * low;
@@ -616,10 +617,10 @@ __global__ void __launch_bounds__(kThreads) k_wedge(c3l_wedge_stage st, int n, B
     const int64_t e = tile.start + ex;
     int64_t pw[6];
     powers(n, pw);
-    int dig[4] = {0, 0, 0, 0};
+    int dig[C3L_MAX_DEGREE] = {0, 0, 0, 0, 0, 0};
     if (active) {
         if (MODE == kPadded) {
-            uint32_t r = (uint32_t)e;  // below n^4 < 2^32
+            uint32_t r = (uint32_t)e;  // below n^deg < 2^31 (checked when the plan is compiled)
             for (int c = blk.deg - 1; c >= 0; --c) {
                 const uint32_t q = r / (uint32_t)n;
                 dig[c] = (int)(r - q * (uint32_t)n);
@@ -628,7 +629,7 @@ __global__ void __launch_bounds__(kThreads) k_wedge(c3l_wedge_stage st, int n, B
         } else {
             const int64_t packed = st.digits[e];
 #pragma unroll
-            for (int c = 0; c < 4; ++c) dig[c] = (int)((packed >> (8 * c)) & 0xFF);
+            for (int c = 0; c < C3L_MAX_DEGREE; ++c) dig[c] = (int)((packed >> (8 * c)) & 0xFF);
         }
     }
     // the epilogue's table entries of group 0's output, fetched before the
@@ -656,6 +657,7 @@ __global__ void __launch_bounds__(kThreads) k_wedge(c3l_wedge_stage st, int n, B
     auto stage = [&](int64_t base, int cnt) {
         const int64_t* src = reinterpret_cast<const int64_t*>(st.instances + base);
         int64_t* dst = reinterpret_cast<int64_t*>(sinst);
+        static_assert(sizeof(c3l_instance) % 8 == 0, "instances are copied as 8-byte words");
         const int words = cnt * (int)(sizeof(c3l_instance) / 8);
         for (int w = threadIdx.x; w < words; w += blockDim.x) dst[w] = src[w];
     };

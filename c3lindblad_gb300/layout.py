@@ -119,8 +119,19 @@ def static_coordinates(n: int) -> Coordinates:
     return _ordered(n, rk)
 
 
-def eom_coordinates(n: int, spin: int, charge: int) -> Coordinates:
-    """S13 coordinates of one response spin and charge."""
+def eom_coordinates(n: int, spin: int, charge: int, space: str = "S13") -> Coordinates:
+    """S13 coordinates of one response spin and charge; ``space="S135"``
+    appends the rank-five shell.
+
+    S13 is ordered like the reference's mask basis (``_ordered``).  The
+    rank-five shell follows it block by block, in the reference's
+    ``_charge_shell_keys`` order (keys of five creators with the response
+    spin's charge, lexicographic over the four group counts) and, inside a
+    block, row-major over each group's lexicographic index combinations
+    (``ComponentCoordinateShell``, ``src/c3l/cc/component_tensor.py:384-559``).
+    """
+    if space not in ("S13", "S135"):
+        raise ValueError("space must be 'S13' or 'S135'")
     rk = []
     for rank in (0, 1):
         for a in range(rank + 1):
@@ -130,7 +141,29 @@ def eom_coordinates(n: int, spin: int, charge: int) -> Coordinates:
             npl, nmi = (a + 1, a) if charge == 1 else (a, a + 1)
             key = (npl, nmi, b, b) if spin == 0 else (b, b, npl, nmi)
             rk.append((rank, key))
-    return _ordered(n, rk)
+    base = _ordered(n, rk)
+    if space == "S13":
+        return base
+    counts = range(min(n, 5) + 1)
+    shell = [k for k in product(counts, counts, counts, counts)
+             if sum(k) == 5 and (k[0] - k[1], k[2] - k[3]) == ((charge, 0) if spin == 0 else (0, charge))]
+    keys = sorted(set(base.keys) | set(shell))
+    remap = np.asarray([keys.index(k) for k in base.keys], np.int64)
+    blocks, tuples, modes = [remap[base.block_of]], [], []
+    dmax = 5
+    pad = -np.ones((base.dimension, dmax - base.tuples.shape[1]), np.int64)
+    tuples.append(np.concatenate([base.tuples, pad], axis=1))
+    modes.append(np.concatenate([base.modes, pad], axis=1))
+    for key in shell:
+        t = block_tuples(n, key)
+        if t.shape[0] == 0:
+            continue
+        blocks.append(np.full(t.shape[0], keys.index(key), np.int64))
+        tuples.append(t)
+        modes.append(np.sort(_modes(n, key, t), axis=1))
+    block_of = np.concatenate(blocks)
+    deg = np.asarray([sum(keys[b]) for b in block_of], np.int64)
+    return Coordinates(n, keys, block_of, np.concatenate(tuples), deg, np.concatenate(modes))
 
 
 # ------------------------------------------------------------------- tilde

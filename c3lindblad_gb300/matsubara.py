@@ -347,8 +347,8 @@ def solve_matsubara(model, grid, *, sites=None, rank: str = "S13", response_spin
     ``FactorizedCCProblem``.  Converged ``amplitudes`` skip the static solve.
     The reference's ``platform``/``production`` switches select its NumPy or
     JAX backends and have no counterpart here: the device path always runs
-    (``precision`` picks the static solve's form).  Only the retained S13
-    response space is built.
+    (``precision`` picks the static solve's form).  ``rank="S135"`` responds
+    through ``FullS135ResponseOperator`` (the rank-five shell).
     """
     from .response import (ComponentEOMProblem, ComponentSigmaOperator, component_eom_context,
                            component_eom_sources, eom_ccsd_problem)
@@ -358,8 +358,6 @@ def solve_matsubara(model, grid, *, sites=None, rank: str = "S13", response_spin
         raise TypeError("grid must be a MatsubaraGrid")
     if rank not in ("S13", "S135"):
         raise ValueError("rank must be 'S13' or 'S135'")
-    if rank == "S135":
-        raise NotImplementedError("the S135 response space is not built; use rank='S13'")
     static = ComponentStaticProblem.compile(model)
     physical = physical_model(static.spec) if static.spec.has_model else physical_model(static.oracle.model)
     block = impurity_sites(physical, sites)
@@ -376,7 +374,13 @@ def solve_matsubara(model, grid, *, sites=None, rank: str = "S13", response_spin
     eom = eom_ccsd_problem(static, response_spin=response_spin)
     context = component_eom_context(ComponentEOMProblem.compile(eom, static, 1), converged)
     sources = tuple(component_eom_sources(context, site=site) for site in block)
-    response = component_matsubara_green(ComponentSigmaOperator(context), sources, grid,
+    if rank == "S13":
+        operator = ComponentSigmaOperator(context)
+    else:
+        from .s135 import CompiledFullS135Action, FullS135ResponseOperator
+
+        operator = FullS135ResponseOperator(CompiledFullS135Action(context))
+    response = component_matsubara_green(operator, sources, grid,
                                          maximum_krylov_dimension=maximum_krylov_dimension,
                                          residual_tolerance=residual_tolerance,
                                          minimum_krylov_dimension=minimum_krylov_dimension,

@@ -121,20 +121,24 @@ class StaticPlan:
 
 
 class EOMPlan:
-    """S13 sigma action of one (spin, charge) block.
+    """S13 sigma action of one (spin, charge) block, or with ``space="S135"``
+    the full action among S1, S3 and the rank-five shell S5.
 
     Mirrors ``component_eom_context`` / ``component_eom_sigma``
-    (``src/c3l/cc/component_tensor.py:2234-2302``).
+    (``src/c3l/cc/component_tensor.py:2234-2302``) and ``FullS135ResponseOperator``
+    (``src/c3l/cc/s135_full.py:296-361``).
     """
 
-    def __init__(self, static: StaticPlan, spin: int = 0, charge: int = 1):
+    def __init__(self, static: StaticPlan, spin: int = 0, charge: int = 1, space: str = "S13"):
         if spin not in (0, 1) or charge not in (1, -1):
             raise ValueError("response spin must be 0/1 and charge +1/-1")
         spec = static.spec
         self.static = static
-        self.spin, self.charge = spin, charge
+        self.spin, self.charge, self.space = spin, charge, space
         n = spec.n
-        self.coords = coords = eom_coordinates(n, spin, charge)
+        if space == "S135" and n ** 5 >= 2 ** 31:
+            raise ValueError("the rank-five padded blocks need n**5 < 2**31 (n <= 73)")
+        self.coords = coords = eom_coordinates(n, spin, charge, space)
         sym = Symbolic(spec, static.coords, coords.keys)
         self.sym = sym
         # the vacuum interaction uses the static monomials (all degree 0/2/4 blocks)

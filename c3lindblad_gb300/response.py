@@ -52,14 +52,18 @@ def eom_ccsd_problem(cc, *, response_spin: int = 0, build_next_rank_masks: bool 
 
 
 class ComponentEOMProblem:
-    """One charge block of the S13 EOM action."""
+    """One charge block of the S13 EOM action (``space="S135"``: the full
+    action on S1 + S3 + the rank-five shell, used by ``FullS135ResponseOperator``)."""
 
-    def __init__(self, static: ComponentStaticProblem, response_spin: int, charge: int):
+    def __init__(self, static: ComponentStaticProblem, response_spin: int, charge: int, *, space: str = "S13"):
         if charge not in (-1, 1):
             raise ValueError("response charge must be +1 or -1")
+        if space not in ("S13", "S135"):
+            raise ValueError("space must be 'S13' or 'S135'")
         self.static = static
         self.response_spin = int(response_spin)
         self.charge = int(charge)
+        self.space = space
         self._plan = None
         self._tables = {}  # device -> Uploader holding this problem's program tables (shared by contexts)
 
@@ -73,7 +77,7 @@ class ComponentEOMProblem:
     def plan(self):
         if self._plan is None:
             from .plans import EOMPlan
-            self._plan = EOMPlan(self.static.plan, self.response_spin, self.charge)
+            self._plan = EOMPlan(self.static.plan, self.response_spin, self.charge, self.space)
         return self._plan
 
     @property
@@ -100,6 +104,7 @@ class ComponentEOMContext:
             t = torch.from_numpy(arr.copy())
         self.ops = DeviceEOM(problem.plan, t, st._device, tables=problem._tables, interaction_scale=interaction_scale)
         self.amplitudes = self.ops.amplitudes
+        self.interaction_scale = float(interaction_scale)
 
 
 def component_eom_context(problem, amplitudes, *, interaction_scale: float = 1.0) -> ComponentEOMContext:

@@ -38,6 +38,9 @@ typedef struct { float re, im; } c3l_complex32;
  */
 #define C3L_MAX_SOURCES 4
 #define C3L_MAX_FACTORS 6
+/* largest block degree: 4 for the static amplitudes and S13, 5 with the
+ * rank-five response shell (S135); index digits are one byte each */
+#define C3L_MAX_DEGREE 6
 
 /* One padded destination block of an atom: dst = const + sum_j sign_j *
  * sum_m vec_j[m] * src_j[... m at axis_j ...] (interior product,
@@ -60,7 +63,7 @@ typedef struct {
     int32_t pad;
     int64_t fac_off[C3L_MAX_FACTORS];
     int32_t fac_deg[C3L_MAX_FACTORS];
-    int8_t axes[C3L_MAX_FACTORS][4];
+    int8_t axes[C3L_MAX_FACTORS][C3L_MAX_DEGREE];
 } c3l_instance;
 
 typedef struct {

@@ -24,7 +24,8 @@ exact-diagonalisation fixtures; ``... spec [names...]`` writes the specs of
 ``SPEC_ONLY`` (no reference outputs); ``... model [names...]`` adds the
 physical one-body model (E, gamma_loss, gamma_gain, interaction sites) to
 committed specs; ``... matsubara`` writes the reference's ``solve_matsubara``
-outputs.
+outputs; ``... s135 [names...]`` writes the reference's full S135 response
+actions.
 """
 
 from __future__ import annotations
@@ -557,20 +558,121 @@ DRIVERS = {
 }
 
 
+# the reference's full S1 + S3 + S5 response action (its rank-five shell) at the
+# fixture's fixed amplitudes: one action per (response spin, charge), G^R on a
+# short grid for the two smallest models
+S135 = {
+    "readme": dict(green=True, omega=np.linspace(-4.0, 4.0, 9), eta=0.1),
+    "s135fix": dict(green=True, omega=np.linspace(-3.0, 3.0, 7), eta=0.05),
+    "twosrc": dict(green=False),
+    "kanamori3x2": dict(green=False),
+}
+
+
+S135_FULL_MAX = 5000  # larger S135 actions keep sampled outputs only
+
+
+def s135_seed(spin: int, charge: int) -> int:
+    return 20260722 + 2 * spin + (charge > 0)
+
+
+def s135_sample(tag: str, y, p_dimension: int, diagonal, s5_keys, s5_tuples) -> dict:
+    """Every S13 coordinate and 4,000 seeded rank-five coordinates of an action:
+    the outputs, the diagonal and the shell's keys and index tuples there."""
+    rng = np.random.default_rng(7)
+    idx = np.concatenate([np.arange(p_dimension),
+                          np.sort(rng.choice(np.arange(p_dimension, y.size), 4000, replace=False))])
+    s5 = idx[idx >= p_dimension] - p_dimension
+    return {f"{tag}_y_index": idx.astype(np.int64), f"{tag}_y_sample": y[idx], f"{tag}_dimension": np.int64(y.size),
+            f"{tag}_diagonal_sample": diagonal[idx], f"{tag}_s5_index": s5.astype(np.int64),
+            f"{tag}_s5_keys_sample": s5_keys[s5].astype(np.int8), f"{tag}_s5_tuples_sample": s5_tuples[s5].astype(np.int8),
+            f"{tag}_s5_dimension": np.int64(s5_keys.shape[0])}
+
+
+def export_s135(name: str, path: Path) -> None:
+    """``CompiledFullS135Action`` / ``FullS135ResponseOperator``
+    (``src/c3l/cc/s135_full.py:101``, ``:296``): the action on a seeded vector,
+    the rapidity diagonal and the S5 coordinate order (block keys and index
+    tuples) for response spins 0 and 1 and charges +1 and -1; G^R of site 0
+    through the S135 operator (``component_retarded_green`` pads the S13
+    sources with zeros) where cheap."""
+    from c3l.cc.component_response import component_retarded_matrix_green_arnoldi
+    from c3l.cc.component_tensor import (
+        ComponentEOMProblem, ComponentStaticProblem, component_eom_context, component_eom_sources,
+    )
+    from c3l.cc.eom import eom_ccsd_problem
+    from c3l.cc.s135_full import CompiledFullS135Action, FullS135ResponseOperator, rapidity_diagonal
+
+    spec = S135[name]
+    cc = build_problem(FIXTURES[name])
+    static = ComponentStaticProblem.compile(cc)
+    golden = np.load(HERE / f"{name}.golden.npz")
+    amplitudes = golden["eom_amplitudes" if "eom_amplitudes" in golden.files else "solution_amplitudes"]
+    out: dict = {}
+    for spin in (0, 1):
+        eom = eom_ccsd_problem(cc, response_spin=spin, build_next_rank_masks=False)
+        for charge in (1, -1):
+            t0 = time.perf_counter()
+            problem = ComponentEOMProblem.compile(eom, static, charge)
+            context = component_eom_context(problem, amplitudes)
+            op = FullS135ResponseOperator(CompiledFullS135Action(context))
+            tag = f"s{spin}q{'p' if charge == 1 else 'm'}"
+            rng = np.random.default_rng(s135_seed(spin, charge))
+            x = rng.normal(size=op.dimension) + 1j * rng.normal(size=op.dimension)
+            y = op.matvec(x)
+            diagonal = rapidity_diagonal(cc.rapidities, op.coordinates)
+            keys, tuples = [], []
+            for blk in op.S5.blocks:
+                keys.append(np.broadcast_to(np.asarray(blk.key, np.int64), (blk.vector_positions.size, 4)))
+                tuples.append(np.pad(blk.indices, ((0, 0), (0, 5 - blk.indices.shape[1])), constant_values=-1))
+                assert np.array_equal(blk.vector_positions, np.arange(blk.vector_positions[0],
+                                                                      blk.vector_positions[0] + blk.vector_positions.size))
+            keys, tuples = np.concatenate(keys), np.concatenate(tuples)
+            out[f"{tag}_p_dimension"] = np.int64(op.p_dimension)
+            if op.dimension <= S135_FULL_MAX:
+                out.update({f"{tag}_x": x, f"{tag}_y": y, f"{tag}_diagonal": diagonal, f"{tag}_s5_keys": keys,
+                            f"{tag}_s5_tuples": tuples})
+            else:  # the input is regenerated from its seed; the rest kept at sampled coordinates
+                out.update(s135_sample(tag, y, op.p_dimension, diagonal, keys, tuples))
+            if spec["green"] and spin == 0:
+                # the reference's S135 G^R goes through its Arnoldi drivers (the S135
+                # operator has no Jacobi diagonal for the per-frequency GMRES)
+                src = component_eom_sources(context, site=0)
+
+                class Counted:  # the call counters the reference's matrix driver reads
+                    dimension = op.dimension
+                    action_calls = 0
+                    action_wall_seconds = 0.0
+
+                    def matvec(self, v):
+                        self.action_calls += 1
+                        return op.matvec(v)
+
+                res = component_retarded_matrix_green_arnoldi(Counted(), [src], spec["omega"], spec["eta"])
+                out[f"{tag}_green_omega"] = np.asarray(spec["omega"])
+                out[f"{tag}_green_eta"] = np.float64(spec["eta"])
+                out[f"{tag}_green_retarded"] = np.asarray(res.retarded)[:, 0, 0]
+                out[f"{tag}_green_addition"] = np.asarray(res.addition)[:, 0, 0]
+            print(f"[{name}] S135 spin {spin} charge {charge:+d}: dim {op.dimension} "
+                  f"(S13 {op.p_dimension}) {time.perf_counter() - t0:.1f}s", flush=True)
+    np.savez_compressed(path, **out)
+
+
 # the reference's solve_matsubara on fixed amplitudes (the converged siam10
 # root; the fixed Kanamori amplitudes of the EOM goldens), both spin blocks
 MATSUBARA = {
     "siam10": dict(beta=10.0, n_iw=8),
     "kanamori3x2": dict(beta=8.0, n_iw=6),
+    "readme": dict(beta=10.0, n_iw=6, ranks=("S13", "S135")),
 }
 
 
 def export_matsubara(name: str, path: Path) -> None:
     """``solve_matsubara`` (``src/c3l/matsubara/solver.py:100``) with the
     fixture's amplitudes (the static solve skipped), the default impurity block
-    (the interaction sites) and response spins 0 and 1; plus the Dyson
-    re-insertion into a semicircular target bath (half-bandwidth 2, hopping
-    0.3)."""
+    (the interaction sites) and response spins 0 and 1 (and, where the table
+    asks, the S135 response space); plus the Dyson re-insertion into a
+    semicircular target bath (half-bandwidth 2, hopping 0.3)."""
     from c3l.cc.component_tensor import ComponentStaticProblem
     from c3l.matsubara.grid import matsubara_grid
     from c3l.matsubara.solver import solve_matsubara
@@ -585,18 +687,21 @@ def export_matsubara(name: str, path: Path) -> None:
     out: dict = {"beta": np.float64(spec["beta"]), "indices": np.asarray(grid.indices, np.int64)}
     z = grid.iw
     target = (0.09 * (z - np.sign(z.imag) * np.sqrt(z ** 2 - 4.0 + 0j)) / 2.0)
-    for spin in (0, 1):
-        t0 = time.perf_counter()
-        sol = solve_matsubara(static, grid, amplitudes=amplitudes, response_spin=spin)
-        m = len(sol.sites)
-        hyb = np.broadcast_to(target[:, None, None] * np.eye(m), (len(grid), m, m))
-        out.update({f"s{spin}_green": sol.green, f"s{spin}_self_energy": sol.self_energy,
-                    f"s{spin}_noninteracting": sol.noninteracting, f"s{spin}_hybridization": sol.hybridization,
-                    f"s{spin}_dyson_target": sol.dyson(hyb), f"s{spin}_seconds": np.float64(time.perf_counter() - t0)})
-        out["sites"] = np.asarray(sol.sites, np.int64)
-        out["one_body"] = sol.one_body
-        out["static_residual"] = np.float64(sol.static_residual)
-        print(f"[{name}] matsubara spin {spin}: sites {sol.sites} {time.perf_counter() - t0:.1f}s", flush=True)
+    for rank in spec.get("ranks", ("S13",)):
+        for spin in (0, 1):
+            t0 = time.perf_counter()
+            sol = solve_matsubara(static, grid, amplitudes=amplitudes, response_spin=spin, rank=rank)
+            m = len(sol.sites)
+            hyb = np.broadcast_to(target[:, None, None] * np.eye(m), (len(grid), m, m))
+            tag = f"s{spin}" if rank == "S13" else f"s{spin}_{rank}"
+            out.update({f"{tag}_green": sol.green, f"{tag}_self_energy": sol.self_energy,
+                        f"{tag}_noninteracting": sol.noninteracting, f"{tag}_hybridization": sol.hybridization,
+                        f"{tag}_dyson_target": sol.dyson(hyb), f"{tag}_seconds": np.float64(time.perf_counter() - t0)})
+            out["sites"] = np.asarray(sol.sites, np.int64)
+            out["one_body"] = sol.one_body
+            out["static_residual"] = np.float64(sol.static_residual)
+            print(f"[{name}] matsubara {rank} spin {spin}: sites {sol.sites} {time.perf_counter() - t0:.1f}s",
+                  flush=True)
     out["dyson_target_hybridization"] = target
     np.savez_compressed(path, **out)
 
@@ -756,6 +861,10 @@ def main() -> None:
             data.update(model_fields(fx["model"]()))
             np.savez_compressed(path, **data)
             print(f"[{name}] model added", flush=True)
+        return
+    if args.names and args.names[0] == "s135":
+        for name in args.names[1:] or list(S135):
+            export_s135(name, HERE / f"{name}.s135.npz")
         return
     if args.names and args.names[0] == "matsubara":
         for name in args.names[1:] or list(MATSUBARA):

@@ -11,16 +11,20 @@ import numpy as np
 
 
 def _digits_padded(size: int, deg: int, n: int) -> np.ndarray:
+    from c3lindblad_gb300.compiler import MAX_DEGREE
+
     e = np.arange(size)
-    out = np.zeros((size, 4), np.int64)
+    out = np.zeros((size, MAX_DEGREE), np.int64)
     for c in range(deg):
         out[:, c] = (e // n ** (deg - 1 - c)) % n
     return out
 
 
 def _digits_packed(packed: np.ndarray) -> np.ndarray:
-    out = np.zeros((packed.size, 4), np.int64)
-    for c in range(4):
+    from c3lindblad_gb300.compiler import MAX_DEGREE
+
+    out = np.zeros((packed.size, MAX_DEGREE), np.int64)
+    for c in range(MAX_DEGREE):
         out[:, c] = (packed >> (8 * c)) & 0xFF
     return out
 

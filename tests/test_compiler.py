@@ -141,7 +141,7 @@ def test_program_table_layouts_match_c_structs():
 
     class Inst(ctypes.Structure):
         _fields_ = [("coef", ctypes.c_double * 2), ("nfac", ctypes.c_int32), ("pad", ctypes.c_int32),
-                    ("fac_off", ctypes.c_int64 * 6), ("fac_deg", ctypes.c_int32 * 6), ("axes", (ctypes.c_int8 * 4) * 6)]
+                    ("fac_off", ctypes.c_int64 * 6), ("fac_deg", ctypes.c_int32 * 6), ("axes", (ctypes.c_int8 * 6) * 6)]
 
     class Block(ctypes.Structure):
         _fields_ = [("inst_begin", ctypes.c_int64), ("inst_end", ctypes.c_int64), ("out_off", ctypes.c_int64),
