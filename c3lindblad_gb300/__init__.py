@@ -19,7 +19,6 @@ from .static import (
     solve_component_ccsd_continuation,
 )
 from .matsubara import (
-    MatrixSelfEnergyResult,
     MatsubaraGreen,
     MatsubaraGrid,
     MatsubaraImpuritySolution,
@@ -27,7 +26,6 @@ from .matsubara import (
     PhysicalModel,
     component_matsubara_green,
     impurity_sites,
-    matrix_auxiliary_self_energy,
     matsubara_dyson_green,
     matsubara_grid,
     matsubara_noninteracting_green,
@@ -37,6 +35,25 @@ from .matsubara import (
     solve_matsubara,
 )
 from .s135 import CompiledFullS135Action, FullS135ResponseOperator
+from .spectra import (
+    MatrixDysonResult,
+    MatrixOrderedReconstruction,
+    MatrixResolventDiagnostics,
+    MatrixSelfEnergyResult,
+    MatrixSpectralDiagnostics,
+    PhysicalDysonResult,
+    auxiliary_self_energy,
+    equilibrium_fdt_defect,
+    matrix_auxiliary_self_energy,
+    matrix_dyson_green,
+    matrix_ordered_dyson_reconstruction,
+    matrix_resolvent_diagnostics,
+    matrix_spectral_diagnostics,
+    noninteracting_auxiliary_green,
+    particle_hole_spectral_defect,
+    physical_dyson_reconstruction,
+    spectral_grid_diagnostics,
+)
 from .response import (
     ComponentEOMContext,
     ComponentEOMProblem,
@@ -75,5 +92,9 @@ __all__ = [
     "ContinuationStage", "solve_component_ccsd_continuation", "MatrixSelfEnergyResult", "MatsubaraImpuritySolution",
     "MatsubaraSelfEnergy", "PhysicalModel", "impurity_sites", "matrix_auxiliary_self_energy", "matsubara_dyson_green",
     "matsubara_noninteracting_green", "matsubara_self_energy", "noninteracting_retarded_green", "physical_model",
-    "solve_matsubara", "CompiledFullS135Action", "FullS135ResponseOperator",
+    "solve_matsubara", "CompiledFullS135Action", "FullS135ResponseOperator", "MatrixDysonResult",
+    "MatrixOrderedReconstruction", "MatrixResolventDiagnostics", "MatrixSpectralDiagnostics", "PhysicalDysonResult",
+    "auxiliary_self_energy", "equilibrium_fdt_defect", "matrix_dyson_green", "matrix_ordered_dyson_reconstruction",
+    "matrix_resolvent_diagnostics", "matrix_spectral_diagnostics", "noninteracting_auxiliary_green",
+    "particle_hole_spectral_defect", "physical_dyson_reconstruction", "spectral_grid_diagnostics",
 ]

@@ -27,6 +27,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from .response import component_retarded_matrix_green_shifts
+from .spectra import matrix_auxiliary_self_energy
 
 _MATSUBARA_TOLERANCE = 1.0e-8
 
@@ -166,6 +167,7 @@ class PhysicalModel:
     gamma_gain: np.ndarray
     interaction_sites: tuple
     has_interactions: bool
+    impurity_site: int = 0
 
     @property
     def n_sites(self) -> int:
@@ -184,11 +186,12 @@ def physical_model(obj) -> PhysicalModel:
             raise ValueError("the problem spec carries no physical model (E, gamma_loss, gamma_gain)")
         return PhysicalModel(np.asarray(spec.model_E, np.complex128), np.asarray(spec.model_gamma_loss, np.complex128),
                              np.asarray(spec.model_gamma_gain, np.complex128),
-                             tuple(int(v) for v in spec.interaction_sites), bool(spec.has_interactions))
+                             tuple(int(v) for v in spec.interaction_sites), bool(spec.has_interactions),
+                             int(spec.impurity_site))
     if all(hasattr(obj, a) for a in ("E", "gamma_loss", "gamma_gain", "interaction_sites", "has_interactions")):
         return PhysicalModel(np.asarray(obj.E, np.complex128), np.asarray(obj.gamma_loss, np.complex128),
                              np.asarray(obj.gamma_gain, np.complex128), tuple(int(v) for v in obj.interaction_sites),
-                             bool(obj.has_interactions))
+                             bool(obj.has_interactions), int(getattr(obj, "impurity_site", 0)))
     raise TypeError("model must be a ProblemSpec with a physical model or a FermionicLindbladModel")
 
 
@@ -230,34 +233,6 @@ def noninteracting_retarded_green(model, shifts, sites=None) -> np.ndarray:
 def matsubara_noninteracting_green(model, grid, sites=None) -> np.ndarray:
     """The noninteracting impurity block on a Matsubara grid (``dyson.py:67-74``)."""
     return grid.from_upper(noninteracting_retarded_green(model, grid.upper_shifts, sites))
-
-
-@dataclass(frozen=True, eq=False)
-class MatrixSelfEnergyResult:
-    """Sigma = G0^-1 - G^-1 per grid point and the conditioning of both solves."""
-
-    retarded: np.ndarray
-    G0_condition_number: np.ndarray
-    G_condition_number: np.ndarray
-    conditioning_limited: np.ndarray
-
-
-def matrix_auxiliary_self_energy(G0_R, G_R, *, conditioning_limit: float = 1.0e10) -> MatrixSelfEnergyResult:
-    """Sigma = G0^-1 - G^-1 by ordered linear solves (``reconstruction.py:174-212``)."""
-    G0 = np.asarray(G0_R, dtype=np.complex128)
-    G = np.asarray(G_R, dtype=np.complex128)
-    if G0.ndim != 3 or G0.shape[1] != G0.shape[2] or G.shape != G0.shape:
-        raise ValueError("G0_R and G_R must have the same shape (points, m, m)")
-    if not (np.all(np.isfinite(G0)) and np.all(np.isfinite(G))):
-        raise ValueError("Green functions must be finite")
-    limit = float(conditioning_limit)
-    if not np.isfinite(limit) or limit <= 1.0:
-        raise ValueError("conditioning_limit must be finite and larger than one")
-    eye = np.broadcast_to(np.eye(G.shape[1], dtype=np.complex128), G.shape)
-    c0 = np.linalg.cond(G0, p=2)
-    c = np.linalg.cond(G, p=2)
-    sigma = np.linalg.solve(G0, eye) - np.linalg.solve(G, eye)
-    return MatrixSelfEnergyResult(sigma, c0, c, (c0 > limit) | (c > limit))
 
 
 @dataclass(frozen=True, eq=False)

@@ -25,7 +25,7 @@ exact-diagonalisation fixtures; ``... spec [names...]`` writes the specs of
 physical one-body model (E, gamma_loss, gamma_gain, interaction sites) to
 committed specs; ``... matsubara`` writes the reference's ``solve_matsubara``
 outputs; ``... s135 [names...]`` writes the reference's full S135 response
-actions.
+actions; ``... spectra`` the reference's spectra reconstruction outputs.
 """
 
 from __future__ import annotations
@@ -658,6 +658,65 @@ def export_s135(name: str, path: Path) -> None:
     np.savez_compressed(path, **out)
 
 
+def export_spectra(path: Path) -> None:
+    """The reference's spectra reconstruction (``src/c3l/spectra/reconstruction.py``)
+    on the siam10 CCSD G^R (its full 1,001-omega golden) and on the n = 9
+    Kanamori model's 3 x 3 impurity block: the auxiliary G0, the scalar
+    auxiliary self-energy and physical Dyson reconstruction (G^K from the
+    equilibrium relation at T = 0.1; a semicircular target bath), the matrix
+    self-energy, Dyson and ordered reconstruction, and the diagnostics."""
+    from c3l.matsubara.dyson import noninteracting_retarded_green
+    from c3l.spectra import reconstruction as rc
+
+    out: dict = {}
+    g = np.load(HERE / "siam10.golden.npz")
+    model = FIXTURES["siam10"]["model"]()
+    w = np.asarray(g["green_omega"], np.float64)
+    gr = np.asarray(g["green_retarded"])
+    g0r, g0k = rc.noninteracting_auxiliary_green(model, w, eta=0.05)
+    gk = (gr - gr.conj()) * np.tanh(w / 0.2)
+    sr, sk = rc.auxiliary_self_energy(g0r, g0k, gr, gk)
+    z = w + 0.05j
+    dr = 0.09 * (z - np.sqrt(z - 2.0 + 0j) * np.sqrt(z + 2.0 + 0j)) / 2.0
+    dk = (dr - dr.conj()) * np.tanh(w / 0.2)
+    phys = rc.physical_dyson_reconstruction(w, -2.0, dr, dk, sr, sk)
+    out.update(scalar_omega=w, scalar_G_R=gr, scalar_G_K=gk, scalar_G0_R=g0r, scalar_G0_K=g0k, scalar_Sigma_R=sr,
+               scalar_Sigma_K=sk, scalar_Delta_R=dr, scalar_Delta_K=dk, phys_retarded=phys.retarded,
+               phys_keldysh=phys.keldysh, phys_spectral=phys.spectral,
+               fdt_defect=np.float64(rc.equilibrium_fdt_defect(w, gr, gk, 0.1)),
+               ph_defect=np.float64(rc.particle_hole_spectral_defect(w, -gr.imag / np.pi)),
+               grid_diagnostics=np.asarray(list(rc.spectral_grid_diagnostics(w, gr).values())))
+    # matrix forms on the Kanamori impurity block (3 orbitals), real axis with broadening
+    kmodel = FIXTURES["kanamori3x2"]["model"]()
+    wm = np.linspace(-3.0, 3.0, 61)
+    zm = wm + 0.1j
+    G0 = noninteracting_retarded_green(kmodel, zm, (0, 1, 2))
+    rng = np.random.default_rng(11)
+    S = rng.normal(size=(3, 3)) + 1j * rng.normal(size=(3, 3))
+    sigma = 0.1 * (S + S.conj().T) / 2 - 0.05j * np.eye(3)
+    G = np.linalg.inv(np.linalg.inv(G0) - sigma[None])
+    mse = rc.matrix_auxiliary_self_energy(G0, G)
+    h = np.asarray(kmodel.E)[np.ix_((0, 1, 2), (0, 1, 2))]
+    delta_pm = zm[:, None, None] * np.eye(3)[None] - h[None] - np.linalg.inv(G0)
+    delta_ph = 0.09 * ((zm - np.sqrt(zm - 2.0 + 0j) * np.sqrt(zm + 2.0 + 0j)) / 2.0)[:, None, None] * np.eye(3)[None]
+    md = rc.matrix_dyson_green(zm, h, delta_ph, mse.retarded)
+    mo = rc.matrix_ordered_dyson_reconstruction(G, delta_pm, delta_ph)
+    out.update(matrix_z=zm, matrix_G0=G0, matrix_G=G, matrix_h=h, matrix_Delta_PM=delta_pm, matrix_Delta_phys=delta_ph,
+               mse_retarded=mse.retarded, mse_G0_cond=mse.G0_condition_number, mse_G_cond=mse.G_condition_number,
+               mse_dyson_right=mse.dyson.right_backward_residual, mse_dyson_left=mse.dyson.left_backward_residual,
+               md_retarded=md.retarded, md_inverse=md.inverse_retarded, md_cond=md.resolvent.condition_number,
+               md_right=md.resolvent.right_backward_residual, md_left=md.resolvent.left_backward_residual,
+               md_spectral=md.spectral.spectral, md_min_eig=md.spectral.minimum_eigenvalue,
+               md_max_eig=md.spectral.maximum_eigenvalue, md_neg=md.spectral.negative_ratio,
+               md_herm=md.spectral.hermiticity_defect,
+               mo_retarded=mo.retarded, mo_right_order=mo.retarded_from_right_order,
+               mo_left_res=mo.left_ordered_residual, mo_right_res=mo.right_ordered_residual,
+               mo_left_id=mo.left_resolvent_identity_residual, mo_right_id=mo.right_resolvent_identity_residual,
+               mo_diff=mo.ordering_difference, mo_left_cond=mo.left_operator_condition_number,
+               mo_right_cond=mo.right_operator_condition_number)
+    np.savez_compressed(path, **out)
+
+
 # the reference's solve_matsubara on fixed amplitudes (the converged siam10
 # root; the fixed Kanamori amplitudes of the EOM goldens), both spin blocks
 MATSUBARA = {
@@ -861,6 +920,9 @@ def main() -> None:
             data.update(model_fields(fx["model"]()))
             np.savez_compressed(path, **data)
             print(f"[{name}] model added", flush=True)
+        return
+    if args.names == ["spectra"]:
+        export_spectra(HERE / "spectra.reconstruction.npz")
         return
     if args.names and args.names[0] == "s135":
         for name in args.names[1:] or list(S135):
