@@ -48,4 +48,26 @@ static __device__ __forceinline__ void split_d(double x, float& hi, float& lo) {
     hi = (float)x;
     lo = (float)(x - (double)hi);
 }
+// The same pair from the bits of x, with no FP64 instruction (the conversions
+// above run on the narrow FP64 pipe): hi keeps the sign, the exponent and the
+// top 23 fraction bits (x truncated to 24 significant bits), lo = x - hi is
+// the low 29 fraction bits times 2^(e - 52), rounded once to FP32, so
+// |hi + lo - x| <= 2^-48 |x|.  Exponents outside [-100, 100] (and zeros,
+// subnormals, infinities, NaN) take the FP64 route.
+static __device__ __forceinline__ void split_d_bits(double x, float& hi, float& lo) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned int top = (unsigned int)(b >> 32);
+    const int e = (int)((top >> 20) & 0x7FFu) - 1023;
+    if (e < -100 || e > 100) {
+        split_d(x, hi, lo);
+        return;
+    }
+    const unsigned int sign = top & 0x80000000u;
+    const unsigned long long m = b & 0x000FFFFFFFFFFFFFull;
+    hi = __uint_as_float(sign | ((unsigned int)(e + 127) << 23) | (unsigned int)(m >> 29));
+    const float r = __uint2float_rn((unsigned int)(m & 0x1FFFFFFFull));
+    // r 2^(e - 52) = (r 2^-64) 2^(e + 12): both factors normal floats for |e| <= 100
+    const float l = __fmul_rn(__fmul_rn(r, 0x1p-64f), __uint_as_float((unsigned int)(e + 139) << 23));
+    lo = sign ? -l : l;
+}
 

@@ -374,7 +374,8 @@ struct PairPlain {
 };
 
 // Operand entries are split into FP32 (hi, lo) pairs as they are staged
-// (complex: re hi, re lo, im hi, im lo); each real product is formed to about
+// (complex: re hi, re lo, im hi, im lo; from the bits of the double, so the
+// staging issues no FP64 instruction); each real product is formed to about
 // 2^-46 (Dekker's product with one FMA, df_mac) and summed by TwoSum into a
 // (sum, correction) pair per real component, finished in FP64 when P is
 // written.  The result differs from an FP64 GEMM by about 1e-14 of
@@ -385,8 +386,8 @@ struct PairDf {
     using A = float4;  // (re sum, re correction, im sum, im correction)
     static __device__ __forceinline__ S stage(double2 v) {
         float4 q;
-        split_d(v.x, q.x, q.y);
-        split_d(v.y, q.z, q.w);
+        split_d_bits(v.x, q.x, q.y);
+        split_d_bits(v.y, q.z, q.w);
         return q;
     }
     static __device__ __forceinline__ A zero() { return make_float4(0.0f, 0.0f, 0.0f, 0.0f); }
