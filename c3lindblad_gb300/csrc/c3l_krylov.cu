@@ -966,6 +966,14 @@ __global__ void __launch_bounds__(X * Y) k_arn_axpy(c3l::ArnoldiBatch bt, int pa
 // the pass-2 projections (k) followed by |w'|^2, so h = sqrt(|w'|^2 - |c2|^2);
 // H[:k+1, j] = c1 + c2 | h goes to column j of Hc, h to hval, and the step
 // counter of the other parity to k.
+//
+// An exhausted Krylov space is a breakdown also when h is above the absolute
+// breakdown tolerance but below kExhausted |w'|: the FP32 first pass leaves
+// w' ~ 1e-7 |w| inside the span, and its FP32-product second update a floor of
+// ~1e-14 |w| in h, so h / |w'| < 1e-6 means the true remainder is below
+// ~1e-13 |w| -- the new vector would be rounding noise.  h is then stored as 0,
+// which the shifted solves and the normalization read as a breakdown.
+constexpr double kExhausted = 1.0e-6;
 __device__ void arnoldi_column_tail(const double2* __restrict__ c1, const double2* __restrict__ c2, int k,
                                     double2* __restrict__ Hc, int64_t ldc, double* __restrict__ hval, int* next) {
     __shared__ double red[32];
@@ -975,7 +983,8 @@ __device__ void arnoldi_column_tail(const double2* __restrict__ c1, const double
     double2* col = Hc + (int64_t)(k - 1) * ldc;
     for (int i = threadIdx.x; i < k; i += blockDim.x) col[i] = make_double2(c1[i].x + c2[i].x, c1[i].y + c2[i].y);
     if (threadIdx.x == 0) {
-        const double h = sqrt(fmax(c2[k].x - sq, 0.0));
+        double h = sqrt(fmax(c2[k].x - sq, 0.0));
+        if (h <= kExhausted * sqrt(fmax(c2[k].x, 0.0))) h = 0.0;
         col[k] = make_double2(h, 0.0);
         *hval = h;
         *next = k;
