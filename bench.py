@@ -671,6 +671,45 @@ def profile_case(kernel: str, spec_name: str = "kanamori3x8") -> dict:
             "jvp_norm": float(y.norm()), "sigma_norm": float(w.norm())}
 
 
+def profile_arnoldi(spec_name: str = "kanamori3x8", m: int = 1024) -> dict:
+    """A case for per-launch DRAM captures of the Arnoldi CGS2 kernels: at the
+    fixture's fixed amplitudes (charge +1, spin 0, site 0 source), one channel's
+    basis is built once to dimension ``m`` (no early convergence), so the
+    j-th launch of each CGS2 kernel is step j.  Reports the build time and the
+    algorithmic bytes of the CGS2 kernels per step (48 per basis entry)."""
+    import torch
+
+    import c3lindblad_gb300 as c3
+    from c3lindblad_gb300.krylov import arnoldi_channels
+
+    dev = torch.device("cuda:0")
+    stream = torch.cuda.current_stream(dev)
+    spec = c3.ProblemSpec.load(GOLDEN / f"{spec_name}.spec.npz")
+    prob = c3.ComponentStaticProblem.compile(spec, device=dev)
+    x = 1e-3 * np.cos(np.arange(prob.num_variables) + 0.13)
+    t = prob.plan.tilde
+    amp = t.coef_a * x[t.idx_a] + t.coef_b * x[t.idx_b]
+    ctx = c3.ComponentEOMContext(c3.ComponentEOMProblem.compile(c3.eom_ccsd_problem(prob), prob, 1), amp)
+    op = c3.ComponentSigmaOperator(ctx)
+    b = c3.component_eom_sources(ctx, site=0).device[0].contiguous()
+    N = op.dimension
+    m = int(min(m, N - 1))
+    shifts = torch.tensor([complex(0.0, 1.0e3)], dtype=torch.complex128, device=dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    basis = arnoldi_channels(ctx.ops, [b], shifts, maximum_dimension=m, residual_tolerance=1e-300,
+                             minimum_dimension=m, check_interval=m)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return {"profile_arnoldi": spec_name, "vector_dimension": N, "basis_dimension": basis[0].m,
+            "build_seconds": e0.elapsed_time(e1) / 1000.0,
+            "cgs2_bytes_at_step_j": "48 * N * (j + 1) (FP32 first projections 8, double-float first update 16, "
+                                    "second projections 16, FP32-product second update 8)",
+            "k_arn_axpy_bytes_at_step_j": "16 * N * (j + 1) read (rows, hi/lo) + 16 * N read (w) + 32 * N written "
+                                          "(w' and its hi/lo)"}
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -685,7 +724,12 @@ def main() -> None:
                     help="run the single-kernel case for ncu captures and event timings, then exit")
     ap.add_argument("--profile-spec", default="kanamori3x8", choices=["kanamori3x8", "gen5x12"],
                     help="fixture of --profile-case (n = 27 Kanamori or the n = 65 general-U model)")
+    ap.add_argument("--profile-arnoldi", action="store_true",
+                    help="build one 1,024-vector Arnoldi basis at the n = 27 fixture's fixed amplitudes, then exit")
     args = ap.parse_args()
+    if args.profile_arnoldi:
+        print(json.dumps(profile_arnoldi()))
+        return
     if args.profile_case:
         print(json.dumps(profile_case(args.profile_case, args.profile_spec)))
         return
