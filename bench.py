@@ -511,11 +511,24 @@ def kernel_roofline(pipe: Pipeline, sol, dev) -> dict:
     alg = 48.0 * N * rows + 96.0 * N * m_built  # basis rows + per-step vectors
     del basis, ctx, op, src
     torch.cuda.empty_cache()
+    # DRAM bytes of one k_arn_axpy launch at step 500 (ncu, N = 29,187), as a
+    # ratio to that launch's algorithmic bytes, scaled to this workload's N
+    k = ARN_AXPY_TRAFFIC["rows"]
+    alg_axpy = 16.0 * N * (k + 1) + 32.0 * N
     return {"bound": "hbm", "kernel": "Arnoldi CGS2 step (k_arn_dot1, k_arn_axpy, k_arn_dot2, k_arn_scale)",
-            "achieved": alg / t_cgs2 / 1e9, "unit": "GB/s", "traffic": None, "algorithmic_bytes": alg,
-            "basis_dimension": m_built, "vector_dimension": N, "cgs2_seconds": t_cgs2, "sigma_ms": t_sigma * 1e3,
-            "traffic_note": "DRAM bytes per CGS2 kernel launch are in profiles/ (ncu); the JSON traffic is null "
-                            "because the four kernels' per-launch bytes depend on the step index"}
+            "achieved": alg / t_cgs2 / 1e9, "unit": "GB/s", "traffic": ARN_AXPY_TRAFFIC["ratio"] * alg_axpy,
+            "algorithmic_bytes": alg, "basis_dimension": m_built, "vector_dimension": N, "cgs2_seconds": t_cgs2,
+            "sigma_ms": t_sigma * 1e3,
+            "traffic_kernel": f"k_arn_axpy at step {k - 1} ({k} basis rows), bytes per launch",
+            "traffic_algorithmic_bytes": alg_axpy, "traffic_over_algorithmic": ARN_AXPY_TRAFFIC["ratio"],
+            "traffic_note": ("ncu dram__bytes_read + dram__bytes_write of that launch on the n = 27 fixture "
+                             "(N = 29,187; profiles/k_arn_axpy_kanamori3x8.md), scaled by N to this workload: "
+                             "the rows are read once, no re-reads")}
+
+
+# ncu: k_arn_axpy at step 500 of a 1,024-row build (bench.py --profile-arnoldi),
+# three launches: DRAM read + write over algorithmic bytes 16 N (k + 1) + 32 N
+ARN_AXPY_TRAFFIC = {"rows": 501, "ratio": 1.001}
 
 
 # per-call counts of the reference's CPU path on each workload: the Newton
