@@ -111,9 +111,17 @@ __device__ __forceinline__ double2 tilde_value(const double* __restrict__ x, con
 __global__ void k_tilde_unpack(int64_t dim, const double* __restrict__ x, const int64_t* __restrict__ ia,
                                const int64_t* __restrict__ ib, const double2* __restrict__ ca,
                                const double2* __restrict__ cb, double2* __restrict__ t) {
+    c3l::pdl_launch_dependents();
+    c3l::pdl_wait();  // x is the previous kernel's output (a no-op without programmatic launch)
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < dim; i += (int64_t)gridDim.x * blockDim.x)
         t[i] = tilde_value(x, ia, ib, ca, cb, i);
 }
+
+// Scatter entries from which a static action unpacks into the canonical
+// vector first and scatters from it (two launches: the fused kernel below
+// re-reads 48 bytes of tilde tables and two x entries per padded entry, which
+// costs more than the second launch once the padded blocks are large).
+constexpr int64_t kSplitScatter = 1 << 20;  // runtime.SPLIT_SCATTER counts the launches the same way
 
 // The tilde unpack and the scatter into padded blocks in one launch: t[i]
 // for the canonical vector (read again by the output stage) and, per scatter
@@ -858,14 +866,25 @@ c3l_status static_apply(const c3l_static_action* sa, const double* x, double* xo
     const c3l_action* a = &sa->action;
     Batch<C> bt = single<C>(reinterpret_cast<C*>(a->ws), reinterpret_cast<const double2*>(sa->canon));
     bt.pdl = true;
-    const int64_t n = sa->num_amplitudes > a->scatter_count ? sa->num_amplitudes : a->scatter_count;
-    c3l_status st = c3l::launch_pdl(
-        k_unpack_scatter<C>, dim3(grid_for(n)), dim3(kThreads), 0, s, 0, true, sa->num_amplitudes, x,
-        (const int64_t*)sa->tilde_ia, (const int64_t*)sa->tilde_ib, reinterpret_cast<const double2*>(sa->tilde_ca),
-        reinterpret_cast<const double2*>(sa->tilde_cb), reinterpret_cast<double2*>(sa->canon), a->scatter_count,
-        (const int64_t*)a->scatter_dst, (const int64_t*)a->scatter_pos, (const double*)a->scatter_sign,
-        reinterpret_cast<C*>(a->ws));
-    if (st) return st;
+    c3l_status st;
+    if (a->scatter_count >= kSplitScatter) {
+        // canonical vector, then the padded scatter from it (k_scatter waits for the unpack)
+        st = c3l::launch_pdl(k_tilde_unpack, dim3(grid_for(sa->num_amplitudes)), dim3(kThreads), 0, s, 0, true,
+                             sa->num_amplitudes, x, (const int64_t*)sa->tilde_ia, (const int64_t*)sa->tilde_ib,
+                             reinterpret_cast<const double2*>(sa->tilde_ca),
+                             reinterpret_cast<const double2*>(sa->tilde_cb), reinterpret_cast<double2*>(sa->canon));
+        if (st) return st;
+        if ((st = scatter<C>(a, bt, s))) return st;
+    } else {
+        const int64_t n = sa->num_amplitudes > a->scatter_count ? sa->num_amplitudes : a->scatter_count;
+        st = c3l::launch_pdl(
+            k_unpack_scatter<C>, dim3(grid_for(n)), dim3(kThreads), 0, s, 0, true, sa->num_amplitudes, x,
+            (const int64_t*)sa->tilde_ia, (const int64_t*)sa->tilde_ib, reinterpret_cast<const double2*>(sa->tilde_ca),
+            reinterpret_cast<const double2*>(sa->tilde_cb), reinterpret_cast<double2*>(sa->canon), a->scatter_count,
+            (const int64_t*)a->scatter_dst, (const int64_t*)a->scatter_pos, (const double*)a->scatter_sign,
+            reinterpret_cast<C*>(a->ws));
+        if (st) return st;
+    }
     if ((st = run_levels<C>(a, bt, s))) return st;
     if ((st = run_padded<C>(a, bt, s))) return st;
     if ((st = run_pairs<C>(a->pairs, bt, s))) return st;

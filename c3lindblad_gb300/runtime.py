@@ -438,8 +438,14 @@ CLUSTER_LEVEL_MAX_TILES = 16  # levels this small at the end of the list run as 
                               # (16-CTA clusters on GB300; the count is an estimate where only 8 are allowed)
 
 
+SPLIT_SCATTER = 1 << 20  # scatter entries from which c3l_static_apply unpacks and scatters in two launches
+
+
 def static_launches(a: Action) -> int:
-    """Kernels of one c3l_static_apply: the fused unpack/scatter replaces the scatter."""
+    """Kernels of one c3l_static_apply: the unpack and the scatter (fused
+    below SPLIT_SCATTER entries) replace the action's scatter."""
+    if a.scatter_count >= SPLIT_SCATTER:
+        return action_launches(a) + 1
     return action_launches(a) + (0 if a.scatter_count > 0 else 1)
 
 
