@@ -370,15 +370,20 @@ def run_gpu(args) -> dict:
         problem, eoms = pipe.fresh()
         return problem, eoms, pipe.step(problem, eoms)
 
-    t_e2e, (problem, eoms, out2) = _timed(torch, stream, e2e_step, flush)
-    h2d = sum(t.numel() * t.element_size() for t in problem.ops._up.keep)
-    h2d += sum(t.numel() * t.element_size() for e in eoms.values() for up in e._tables.values() for t in up.keep)
-    h2d += 16 * pipe.omega.size * len(out2[2])
-    d2h = out2[0].amplitudes.nbytes + out2[0].variables.nbytes
-    d2h += sum(r.retarded.nbytes * 3 + r.addition_relative_residuals.nbytes * 2 for r in out2[2].values())
-    d2h += sum(16 * pipe.eoms[b].dimension * 3 * len(pipe.sites) for b in pipe.blocks)  # sources and sink
-    del problem, eoms, out2
-    torch.cuda.empty_cache()
+    # repeated up to three times (fresh tables each time), each repeat timed alone
+    e2e_times = []
+    for _ in range(max(1, min(args.steps, 3))):
+        t_i, (problem, eoms, out2) = _timed(torch, stream, e2e_step, flush)
+        e2e_times.append(t_i)
+        h2d = sum(t.numel() * t.element_size() for t in problem.ops._up.keep)
+        h2d += sum(t.numel() * t.element_size() for e in eoms.values() for up in e._tables.values() for t in up.keep)
+        h2d += 16 * pipe.omega.size * len(out2[2])
+        d2h = out2[0].amplitudes.nbytes + out2[0].variables.nbytes
+        d2h += sum(r.retarded.nbytes * 3 + r.addition_relative_residuals.nbytes * 2 for r in out2[2].values())
+        d2h += sum(16 * pipe.eoms[b].dimension * 3 * len(pipe.sites) for b in pipe.blocks)  # sources and sink
+        del problem, eoms, out2
+        torch.cuda.empty_cache()
+    t_e2e = float(np.mean(e2e_times))
 
     # the reference's own G^R method on the same kernels: one preconditioned GMRES
     # per frequency and channel (batching over omega off), timed on 8 consecutive
@@ -447,7 +452,10 @@ def run_gpu(args) -> dict:
                    **accuracy},
         "gpu_launches": int(launches),
         "e2e": {"value": t_e2e, "unit": "s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-                "setup_seconds_excluded": pipe.setup_seconds},
+                "setup_seconds_excluded": pipe.setup_seconds, "repeats": len(e2e_times),
+                "min": float(np.min(e2e_times)), "max": float(np.max(e2e_times))},
+        "step_seconds_spread": {"min": float(np.min(times)), "median": float(np.median(times)),
+                                "max": float(np.max(times))},
         "roofline": dict(roof, peak=hbm, frac=roof["achieved"] / hbm, peak_source=peak_kind),
         "clocks": clocks.summary(),
     }
