@@ -600,12 +600,13 @@ def _group_by_anchor(terms: dict):
 
 
 def _digits(coords: Coordinates, positions: np.ndarray) -> np.ndarray:
+    """Index digits of each output packed one byte each, digit c in byte c
+    (little-endian int64; padding digits are 0)."""
     tup = coords.tuples[positions]
-    out = np.zeros(len(positions), np.int64)
-    for c in range(tup.shape[1]):
-        col = np.where(tup[:, c] >= 0, tup[:, c], 0)
-        out |= (col & 0xFF) << (8 * c)
-    return out.astype(np.int64)
+    np.maximum(tup, 0, out=tup)
+    packed = np.zeros((tup.shape[0], 8), np.uint8)
+    packed[:, :tup.shape[1]] = tup  # every digit is below 256 (n <= 255)
+    return packed.view("<i8").reshape(-1).astype(np.int64, copy=False)
 
 
 def compile_output(builder: Builder, name: str, terms: dict, coords: Coordinates,

@@ -101,9 +101,16 @@ def _ordered(n: int, rank_keys: list) -> Coordinates:
     tup = np.concatenate(recs_tuple)
     mod = np.concatenate(recs_modes)
     # colexicographic order of the ascending mode tuple within each rank:
-    # primary key rank, then the highest mode, then the next highest, ...
-    sort_keys = [mod[:, c] for c in range(dmax)] + [rank]
-    order = np.lexsort(sort_keys)
+    # primary key rank, then the highest mode, then the next highest, ...;
+    # one integer key (modes + 1 < 2^bits, padding -1 -> 0) sorted stably
+    bits = int(4 * n + 1).bit_length()
+    if bits * dmax + int(rank.max()).bit_length() < 63:
+        key = rank.astype(np.int64) << (bits * dmax)
+        for c in range(dmax):
+            key |= (mod[:, c] + 1) << (bits * c)
+        order = np.argsort(key, kind="stable")
+    else:
+        order = np.lexsort([mod[:, c] for c in range(dmax)] + [rank])
     deg = np.asarray([sum(keys[b]) for b in block[order]], np.int64)
     return Coordinates(n, keys, block[order], tup[order], deg, mod[order])
 
@@ -235,7 +242,9 @@ def tilde_layout(coords: Coordinates, mode_partner: np.ndarray, mode_phase: np.n
     widths = np.where(rep_pair == 1, 2, 1)
     rep_col = np.concatenate([[0], np.cumsum(widths)[:-1]]).astype(np.int64)
     real_size = int(widths.sum())
-    scales = _self_scales(phase)
+    scales = np.ones(D, np.complex128)  # read at self-partner positions only
+    self_pos = rep_pos[rep_pair == 0]
+    scales[self_pos] = _self_scales(phase[self_pos])
     idx_a = np.zeros(D, np.int64)
     idx_b = np.zeros(D, np.int64)
     coef_a = np.zeros(D, np.complex128)
