@@ -278,7 +278,19 @@ def padded_gather(coords: Coordinates, key: Key) -> tuple[np.ndarray, np.ndarray
     """For each padded entry of a block: canonical vector position and sign.
 
     Entries with a repeated index inside a group get position -1 and sign 0.
+    The tables are kept on the coordinate object: the static plan, every EOM
+    plan and every source plan scatter the same amplitude blocks.
     """
+    cache = coords.__dict__.setdefault("_padded_gather", {})
+    got = cache.get(tuple(key))
+    if got is None:
+        got = cache[tuple(key)] = _padded_gather(coords, key)
+        for a in got:
+            a.setflags(write=False)
+    return got
+
+
+def _padded_gather(coords: Coordinates, key: Key) -> tuple[np.ndarray, np.ndarray]:
     n = coords.n
     d = sum(key)
     size = n ** d
