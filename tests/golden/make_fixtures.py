@@ -25,7 +25,9 @@ exact-diagonalisation fixtures; ``... spec [names...]`` writes the specs of
 physical one-body model (E, gamma_loss, gamma_gain, interaction sites) to
 committed specs; ``... matsubara`` writes the reference's ``solve_matsubara``
 outputs; ``... s135 [names...]`` writes the reference's full S135 response
-actions; ``... spectra`` the reference's spectra reconstruction outputs.
+actions; ``... spectra`` the reference's spectra reconstruction outputs;
+``... static names...`` the static goldens alone (residual and JVP at the fixed
+amplitudes).
 """
 
 from __future__ import annotations
@@ -920,6 +922,14 @@ def main() -> None:
             data.update(model_fields(fx["model"]()))
             np.savez_compressed(path, **data)
             print(f"[{name}] model added", flush=True)
+        return
+    if args.names and args.names[0] == "static":
+        # the static goldens only (fixed-amplitude residual and JVP, tilde map),
+        # for fixtures whose EOM goldens take the reference hours
+        for name in args.names[1:]:
+            fx = dict(FIXTURES[name], solve=False, eom=False)
+            cc = build_problem(fx)
+            export_golden(name, fx, cc, HERE / f"{name}.golden.npz")
         return
     if args.names == ["spectra"]:
         export_spectra(HERE / "spectra.reconstruction.npz")
